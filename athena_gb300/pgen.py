@@ -1,0 +1,368 @@
+"""Problem generators (initial conditions) for the stage-update workloads.
+
+Each generator returns per-block arrays in the layout of :mod:`athena_gb300.mesh`:
+``u[nb, 5, nc3, nc2, nc1]`` (conserved: density, momenta, total energy) and face fields
+``b1, b2, b3`` (``w`` primitive instead of ``u`` for the relativistic problems).
+Ghost zones are left at zero; the stage update fills them by the ghost exchange.
+
+The linear wave restates the reference's ``pgen/linear_wave.cpp`` (InitUserMeshData
+:78-188, Eigensystem :626-855, ProblemGenerator :436-585, vector potential A1-A3
+:588-624) with the same libm calls, so its arrays are bit-identical to the reference's
+when ``exact=True``.  The other generators are seeded synthetic inputs with the shapes,
+sizes and value distributions of the benchmark configurations.
+"""
+import math
+
+import numpy as np
+
+from .mesh import MeshSpec
+
+IDN, IM1, IM2, IM3, IEN = 0, 1, 2, 3, 4
+TINY_NUMBER = 1.0e-20
+
+
+def _sign(x):
+    return -1.0 if x < 0.0 else 1.0
+
+
+def mhd_right_eigenvectors(gm1, d, v1, v2, v3, h, b1, b2, b3, x, y):
+    """Adiabatic-MHD eigenvalues and right eigenvectors (columns), the branch of
+    Eigensystem in linear_wave.cpp:633-763 used for the MHD linear wave."""
+    vsq = v1 * v1 + v2 * v2 + v3 * v3
+    btsq = b2 * b2 + b3 * b3
+    bt_starsq = (gm1 - (gm1 - 1.0) * y) * btsq
+    vaxsq = b1 * b1 / d
+    hp = h - (vaxsq + btsq / d)
+    twid_asq = max((gm1 * (hp - 0.5 * vsq) - (gm1 - 1.0) * x), TINY_NUMBER)
+    ct2 = bt_starsq / d
+    tsum = vaxsq + ct2 + twid_asq
+    tdif = vaxsq + ct2 - twid_asq
+    cf2_cs2 = math.sqrt(tdif * tdif + 4.0 * twid_asq * ct2)
+    cfsq = 0.5 * (tsum + cf2_cs2)
+    cf = math.sqrt(cfsq)
+    cssq = twid_asq * vaxsq / cfsq
+    cs = math.sqrt(cssq)
+    bt = math.sqrt(btsq)
+    bt_star = math.sqrt(bt_starsq)
+    if bt == 0.0:
+        bet2, bet3 = 1.0, 0.0
+    else:
+        bet2, bet3 = b2 / bt, b3 / bt
+    bet2_star = bet2 / math.sqrt(gm1 - (gm1 - 1.0) * y)
+    bet3_star = bet3 / math.sqrt(gm1 - (gm1 - 1.0) * y)
+    bet_starsq = bet2_star * bet2_star + bet3_star * bet3_star
+    vbet = v2 * bet2_star + v3 * bet3_star
+    if (cfsq - cssq) == 0.0:
+        alpha_f, alpha_s = 1.0, 0.0
+    elif (twid_asq - cssq) <= 0.0:
+        alpha_f, alpha_s = 0.0, 1.0
+    elif (cfsq - twid_asq) <= 0.0:
+        alpha_f, alpha_s = 1.0, 0.0
+    else:
+        alpha_f = math.sqrt((twid_asq - cssq) / (cfsq - cssq))
+        alpha_s = math.sqrt((cfsq - twid_asq) / (cfsq - cssq))
+    sqrtd = math.sqrt(d)
+    isqrtd = 1.0 / sqrtd
+    s = _sign(b1)
+    twid_a = math.sqrt(twid_asq)
+    qf = cf * alpha_f * s
+    qs = cs * alpha_s * s
+    af_prime = twid_a * alpha_f * isqrtd
+    as_prime = twid_a * alpha_s * isqrtd
+    afpbb = af_prime * bt_star * bet_starsq
+    aspbb = as_prime * bt_star * bet_starsq
+    vax = math.sqrt(vaxsq)
+    ev = [v1 - cf, v1 - vax, v1 - cs, v1, v1 + cs, v1 + vax, v1 + cf]
+    r = [[0.0] * 7 for _ in range(7)]
+    r[0] = [alpha_f, 0.0, alpha_s, 1.0, alpha_s, 0.0, alpha_f]
+    r[1] = [alpha_f * ev[0], 0.0, alpha_s * ev[2], v1, alpha_s * ev[4], 0.0,
+            alpha_f * ev[6]]
+    qa, qb, qc, qd = alpha_f * v2, alpha_s * v2, qs * bet2_star, qf * bet2_star
+    r[2] = [qa + qc, -bet3, qb - qd, v2, qb + qd, bet3, qa - qc]
+    qa, qb, qc, qd = alpha_f * v3, alpha_s * v3, qs * bet3_star, qf * bet3_star
+    r[3] = [qa + qc, bet2, qb - qd, v3, qb + qd, -bet2, qa - qc]
+    r41 = -(v2 * bet3 - v3 * bet2)
+    r[4] = [alpha_f * (hp - v1 * cf) + qs * vbet + aspbb, r41,
+            alpha_s * (hp - v1 * cs) - qf * vbet - afpbb, 0.5 * vsq + (gm1 - 1.0) * x / gm1,
+            alpha_s * (hp + v1 * cs) + qf * vbet - afpbb, -r41,
+            alpha_f * (hp + v1 * cf) - qs * vbet + aspbb]
+    r50, r51, r52 = as_prime * bet2_star, -bet3 * s * isqrtd, -af_prime * bet2_star
+    r[5] = [r50, r51, r52, 0.0, r52, r51, r50]
+    r60, r61, r62 = as_prime * bet3_star, bet2 * s * isqrtd, -af_prime * bet3_star
+    r[6] = [r60, r61, r62, 0.0, r62, r61, r60]
+    return ev, r
+
+
+class LinearWave:
+    """Adiabatic-MHD linear wave on a periodic box, wavevector along the grid diagonal
+    (linear_wave.cpp:78-188)."""
+
+    def __init__(self, mesh: MeshSpec, gamma=1.666666666666667, wave_flag=0, amp=1.0e-6,
+                 vflow=0.0):
+        self.mesh, self.gam, self.wave_flag, self.amp = mesh, gamma, wave_flag, amp
+        self.gm1 = gamma - 1.0
+        x1size = mesh.xmax[0] - mesh.xmin[0]
+        x2size = mesh.xmax[1] - mesh.xmin[1]
+        x3size = mesh.xmax[2] - mesh.xmin[2]
+        ang_3 = math.atan(x1size / x2size)
+        self.sin_a3, self.cos_a3 = math.sin(ang_3), math.cos(ang_3)
+        ang_2 = math.atan(0.5 * (x1size * self.cos_a3 + x2size * self.sin_a3) / x3size)
+        self.sin_a2, self.cos_a2 = math.sin(ang_2), math.cos(ang_2)
+        x1 = x1size * self.cos_a2 * self.cos_a3
+        x2 = x2size * self.cos_a2 * self.sin_a3
+        x3 = x3size * self.sin_a2
+        lam = x1
+        if ang_3 != 0.0:
+            lam = min(lam, x2)
+        if ang_2 != 0.0:
+            lam = min(lam, x3)
+        self.lam = lam
+        self.k_par = 2.0 * 3.1415926535897932 / lam
+        self.d0, self.u0 = 1.0, vflow
+        self.bx0, self.by0, self.bz0 = 1.0, math.sqrt(2.0), 0.5
+        self.p0 = 1.0 / gamma
+        h0 = ((self.p0 / self.gm1 + 0.5 * self.d0 * (self.u0 * self.u0)) + self.p0) / self.d0
+        h0 += (self.bx0 * self.bx0 + self.by0 * self.by0 + self.bz0 * self.bz0) / self.d0
+        self.ev, self.rem = mhd_right_eigenvectors(self.gm1, self.d0, self.u0, 0.0, 0.0, h0,
+                                                   self.bx0, self.by0, self.bz0, 0.0, 1.0)
+        self.dby = amp * self.rem[5][wave_flag]
+        self.dbz = amp * self.rem[6][wave_flag]
+
+    def period(self):
+        """tlim for problem/test = true with tlim = 1 (linear_wave.cpp:174-179)."""
+        return self.lam / abs(self.ev[self.wave_flag]) * 1.0
+
+    def _xy(self, x1, x2, x3):
+        x = x1 * self.cos_a2 * self.cos_a3 + x2 * self.cos_a2 * self.sin_a3 + x3 * self.sin_a2
+        y = -x1 * self.sin_a3 + x2 * self.cos_a3
+        return x, y
+
+    def A1(self, x1, x2, x3):
+        x, y = self._xy(x1, x2, x3)
+        Ay = self.bz0 * x - (self.dbz / self.k_par) * math.cos(self.k_par * (x))
+        Az = -self.by0 * x + (self.dby / self.k_par) * math.cos(self.k_par * (x)) + \
+            self.bx0 * y
+        return -Ay * self.sin_a3 - Az * self.sin_a2 * self.cos_a3
+
+    def A2(self, x1, x2, x3):
+        x, y = self._xy(x1, x2, x3)
+        Ay = self.bz0 * x - (self.dbz / self.k_par) * math.cos(self.k_par * (x))
+        Az = -self.by0 * x + (self.dby / self.k_par) * math.cos(self.k_par * (x)) + \
+            self.bx0 * y
+        return Ay * self.cos_a3 - Az * self.sin_a2 * self.sin_a3
+
+    def A3(self, x1, x2, x3):
+        x, y = self._xy(x1, x2, x3)
+        Az = -self.by0 * x + (self.dby / self.k_par) * math.cos(self.k_par * (x)) + \
+            self.bx0 * y
+        return Az * self.cos_a2
+
+    def generate(self):
+        """Per-block u, b1, b2, b3 (ProblemGenerator, linear_wave.cpp:436-585)."""
+        m = self.mesh
+        ng = m.ng
+        n1, n2, n3 = m.bx
+        u = np.zeros((m.nblocks, 5) + m.cell_shape)
+        b1 = np.zeros((m.nblocks,) + m.face_shapes[0])
+        b2 = np.zeros((m.nblocks,) + m.face_shapes[1])
+        b3 = np.zeros((m.nblocks,) + m.face_shapes[2])
+        wf, amp, rem = self.wave_flag, self.amp, self.rem
+        for b in range(m.nblocks):
+            l1, l2, l3 = m.block_loc(b)
+            x1f, dx1f = m.face_coords(0, l1)
+            x2f, dx2f = m.face_coords(1, l2)
+            x3f, dx3f = m.face_coords(2, l3)
+            x1v, x2v, x3v = m.cell_centers(0, l1), m.cell_centers(1, l2), m.cell_centers(2, l3)
+            sh = (n3 + 1, n2 + 1, n1 + 1)
+            a1, a2, a3 = np.zeros(sh), np.zeros(sh), np.zeros(sh)
+            for kk in range(n3 + 1):
+                k = ng + kk
+                for jj in range(n2 + 1):
+                    j = ng + jj
+                    for ii in range(n1 + 1):
+                        i = ng + ii
+                        a1[kk, jj, ii] = self.A1(x1v[i], x2f[j], x3f[k])
+                        a2[kk, jj, ii] = self.A2(x1f[i], x2v[j], x3f[k])
+                        a3[kk, jj, ii] = self.A3(x1f[i], x2f[j], x3v[k])
+            for kk in range(n3):
+                for jj in range(n2):
+                    for ii in range(n1 + 1):
+                        b1[b, ng + kk, ng + jj, ng + ii] = \
+                            (a3[kk, jj + 1, ii] - a3[kk, jj, ii]) / dx2f[ng + jj] - \
+                            (a2[kk + 1, jj, ii] - a2[kk, jj, ii]) / dx3f[ng + kk]
+            for kk in range(n3):
+                for jj in range(n2 + 1):
+                    for ii in range(n1):
+                        b2[b, ng + kk, ng + jj, ng + ii] = \
+                            (a1[kk + 1, jj, ii] - a1[kk, jj, ii]) / dx3f[ng + kk] - \
+                            (a3[kk, jj, ii + 1] - a3[kk, jj, ii]) / dx1f[ng + ii]
+            for kk in range(n3 + 1):
+                for jj in range(n2):
+                    for ii in range(n1):
+                        b3[b, ng + kk, ng + jj, ng + ii] = \
+                            (a2[kk, jj, ii + 1] - a2[kk, jj, ii]) / dx1f[ng + ii] - \
+                            (a1[kk, jj + 1, ii] - a1[kk, jj, ii]) / dx2f[ng + jj]
+            ca2, sa2, ca3, sa3 = self.cos_a2, self.sin_a2, self.cos_a3, self.sin_a3
+            for kk in range(n3):
+                k = ng + kk
+                for jj in range(n2):
+                    j = ng + jj
+                    for ii in range(n1):
+                        i = ng + ii
+                        x = ca2 * (x1v[i] * ca3 + x2v[j] * sa3) + x3v[k] * sa2
+                        sn = math.sin(self.k_par * x)
+                        u[b, IDN, k, j, i] = self.d0 + amp * sn * rem[0][wf]
+                        mx = self.d0 * self.u0 + amp * sn * rem[1][wf]
+                        my = amp * sn * rem[2][wf]
+                        mz = amp * sn * rem[3][wf]
+                        u[b, IM1, k, j, i] = mx * ca2 * ca3 - my * sa3 - mz * sa2 * ca3
+                        u[b, IM2, k, j, i] = mx * ca2 * sa3 + my * ca3 - mz * sa2 * sa3
+                        u[b, IM3, k, j, i] = mx * sa2 + mz * ca2
+                        e = self.p0 / self.gm1 + 0.5 * self.d0 * self.u0 * self.u0 + \
+                            amp * sn * rem[4][wf]
+                        e += 0.5 * (self.bx0 * self.bx0 + self.by0 * self.by0 +
+                                    self.bz0 * self.bz0)
+                        u[b, IEN, k, j, i] = e
+        return u, b1, b2, b3
+
+    def l1_errors(self, u, bcc):
+        """L1 errors of cell-centred conserved variables and fields against the initial
+        wave (Mesh::UserWorkAfterLoop, linear_wave.cpp:190-424).  Returns
+        (rms_l1, l1[8], max[8])."""
+        m = self.mesh
+        ng = m.ng
+        n1, n2, n3 = m.bx
+        l1 = np.zeros(8)
+        mx_err = np.zeros(8)
+        wf, amp, rem = self.wave_flag, self.amp, self.rem
+        ca2, sa2, ca3, sa3 = self.cos_a2, self.sin_a2, self.cos_a3, self.sin_a3
+        for b in range(m.nblocks):
+            l1b, l2b, l3b = m.block_loc(b)
+            x1v, x2v, x3v = m.cell_centers(0, l1b), m.cell_centers(1, l2b), \
+                m.cell_centers(2, l3b)
+            _, dx1f = m.face_coords(0, l1b)
+            _, dx2f = m.face_coords(1, l2b)
+            _, dx3f = m.face_coords(2, l3b)
+            for k in range(ng, ng + n3):
+                for j in range(ng, ng + n2):
+                    for i in range(ng, ng + n1):
+                        x = ca2 * (x1v[i] * ca3 + x2v[j] * sa3) + x3v[k] * sa2
+                        sn = math.sin(self.k_par * x)
+                        d1 = self.d0 + amp * sn * rem[0][wf]
+                        mx = self.d0 * self.u0 + amp * sn * rem[1][wf]
+                        my = amp * sn * rem[2][wf]
+                        mz = amp * sn * rem[3][wf]
+                        m1 = mx * ca2 * ca3 - my * sa3 - mz * sa2 * ca3
+                        m2 = mx * ca2 * sa3 + my * ca3 - mz * sa2 * sa3
+                        m3 = mx * sa2 + mz * ca2
+                        e0 = self.p0 / self.gm1 + 0.5 * self.d0 * self.u0 * self.u0 + \
+                            amp * sn * rem[4][wf]
+                        e0 += 0.5 * (self.bx0 * self.bx0 + self.by0 * self.by0 +
+                                     self.bz0 * self.bz0)
+                        bx = self.bx0
+                        by = self.by0 + amp * sn * rem[5][wf]
+                        bz = self.bz0 + amp * sn * rem[6][wf]
+                        bb1 = bx * ca2 * ca3 - by * sa3 - bz * sa2 * ca3
+                        bb2 = bx * ca2 * sa3 + by * ca3 - bz * sa2 * sa3
+                        bb3 = bx * sa2 + bz * ca2
+                        vol = dx1f[i] * dx2f[j] * dx3f[k]
+                        ref = (d1, m1, m2, m3, e0)
+                        for n in range(5):
+                            err = abs(ref[n] - u[b, n, k, j, i])
+                            l1[n] += err * vol
+                            mx_err[n] = max(err, mx_err[n])
+                        for n, bref in enumerate((bb1, bb2, bb3)):
+                            err = abs(bref - bcc[b, n, k, j, i])
+                            l1[5 + n] += err * vol
+                            mx_err[5 + n] = max(err, mx_err[5 + n])
+        vol = (m.xmax[0] - m.xmin[0]) * (m.xmax[1] - m.xmin[1]) * (m.xmax[2] - m.xmin[2])
+        l1 = l1 / vol
+        rms = math.sqrt(sum(v * v for v in l1))
+        return rms, l1, mx_err
+
+
+def prim_to_cons(w, bcc, gamma):
+    """Newtonian adiabatic MHD W -> U (EquationOfState::PrimitiveToConserved,
+    adiabatic_mhd.cpp:99-136)."""
+    igm1 = 1.0 / (gamma - 1.0)
+    u = np.empty_like(w)
+    d, vx, vy, vz, p = w
+    u[0] = d
+    u[1] = vx * d
+    u[2] = vy * d
+    u[3] = vz * d
+    u[4] = p * igm1 + 0.5 * (d * (vx * vx + vy * vy + vz * vz) +
+                             (bcc[0] * bcc[0] + bcc[1] * bcc[1] + bcc[2] * bcc[2]))
+    return u
+
+
+def faces_from_uniform(nx, b):
+    """Global face arrays of a uniform field b = (b1, b2, b3)."""
+    n1, n2, n3 = nx
+    return (np.full((n3, n2, n1 + 1), b[0]), np.full((n3, n2 + 1, n1), b[1]),
+            np.full((n3 + 1, n2, n1), b[2]))
+
+
+def cell_centered(f1, f2, f3):
+    """Uniform-mesh cell-centred field from global face arrays (field.cpp:112-180)."""
+    return np.stack([0.5 * f1[:, :, :-1] + 0.5 * f1[:, :, 1:],
+                     0.5 * f2[:, :-1, :] + 0.5 * f2[:, 1:, :],
+                     0.5 * f3[:-1, :, :] + 0.5 * f3[1:, :, :]])
+
+
+def solenoidal_velocity(nx, kmin, kmax, seed):
+    """Seeded random-phase solenoidal field with power in kmin <= |k| <= kmax (integer
+    wavenumbers of the periodic box), unit rms.  Returns v[3, NX3, NX2, NX1]."""
+    n1, n2, n3 = nx
+    rng = np.random.default_rng(seed)
+    k3 = np.fft.fftfreq(n3, 1.0 / n3)[:, None, None]
+    k2 = np.fft.fftfreq(n2, 1.0 / n2)[None, :, None]
+    k1 = np.fft.rfftfreq(n1, 1.0 / n1)[None, None, :]
+    kk = np.sqrt(k1 * k1 + k2 * k2 + k3 * k3)
+    shell = (kk >= kmin) & (kk <= kmax)
+    shape = kk.shape
+    vk = []
+    for _ in range(3):
+        amp = rng.standard_normal(shape)
+        ph = rng.uniform(0.0, 2.0 * np.pi, shape)
+        vk.append(np.where(shell, amp * np.exp(1j * ph), 0.0))
+    kvec = (k1 + 0 * k2 + 0 * k3, k2 + 0 * k1 + 0 * k3, k3 + 0 * k1 + 0 * k2)
+    ksq = np.where(kk > 0, kk * kk, 1.0)
+    div = (kvec[0] * vk[0] + kvec[1] * vk[1] + kvec[2] * vk[2]) / ksq
+    vk = [vk[d] - kvec[d] * div for d in range(3)]
+    v = np.stack([np.fft.irfftn(vk[d], s=(n3, n2, n1)) for d in range(3)])
+    rms = np.sqrt(np.mean(np.sum(v * v, axis=0)))
+    return v / rms
+
+
+def turbulence(nx, seed=20261204, gamma=5.0 / 3.0, mach=1.0, beta=1.0, p0=1.0,
+               kmin=1.0, kmax=4.0):
+    """Decaying-MHD-turbulence initial state on a periodic unit box: rho = 1, uniform
+    B along x with plasma beta = 2 p / B^2, seeded solenoidal velocity with power in
+    kmin <= |k| <= kmax scaled to rms Mach `mach`.  Global arrays (u, f1, f2, f3)."""
+    bx = np.sqrt(2.0 * p0 / beta)
+    cs = np.sqrt(gamma * p0 / 1.0)
+    v = solenoidal_velocity(nx, kmin, kmax, seed) * (mach * cs)
+    n1, n2, n3 = nx
+    w = np.empty((5, n3, n2, n1))
+    w[0] = 1.0
+    w[1:4] = v
+    w[4] = p0
+    f1, f2, f3 = faces_from_uniform(nx, (bx, 0.0, 0.0))
+    u = prim_to_cons(w, cell_centered(f1, f2, f3), gamma)
+    return u, f1, f2, f3
+
+
+def blast(nx, xmin=(-0.5, -0.5, -0.5), xmax=(0.5, 0.5, 0.5), gamma=5.0 / 3.0, p_in=10.0,
+          p_out=0.1, radius=0.1, b=(1.0 / np.sqrt(2.0),) * 3):
+    """MHD blast wave: rho = 1, p = p_in inside r < radius, p_out outside, uniform B
+    (components b).  Global arrays (u, f1, f2, f3)."""
+    n1, n2, n3 = nx
+    xs = [xmin[d] + (np.arange(nx[d]) + 0.5) * (xmax[d] - xmin[d]) / nx[d] for d in range(3)]
+    r = np.sqrt(xs[0][None, None, :] ** 2 + xs[1][None, :, None] ** 2 +
+                xs[2][:, None, None] ** 2)
+    w = np.zeros((5, n3, n2, n1))
+    w[0] = 1.0
+    w[4] = np.where(r < radius, p_in, p_out)
+    f1, f2, f3 = faces_from_uniform(nx, b)
+    return prim_to_cons(w, cell_centered(f1, f2, f3), gamma), f1, f2, f3

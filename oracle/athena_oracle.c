@@ -1,0 +1,1269 @@
+/* CPU oracle for the Athena++ MHD stage update — TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain C99, FP64 throughout.  Every routine restates one reference routine and keeps
+ * its floating-point association (operand order and grouping) so that results can be
+ * compared bit for bit; comments give the reference file:line followed.  Compile with
+ * -ffp-contract=off (no FMA contraction), without -ffast-math.
+ *
+ * Used only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.
+ */
+#include "athena_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* std::min / std::max semantics (return the first argument unless the second is
+ * strictly smaller / larger) */
+static inline double smin(double a, double b) { return (b < a) ? b : a; }
+static inline double smax(double a, double b) { return (a < b) ? b : a; }
+#define SQR(x) ((x) * (x))
+#define SIGN(x) (((x) < 0.0) ? -1.0 : 1.0)
+
+enum { IDN = 0, IVX = 1, IVY = 2, IVZ = 3, IPR = 4, IBY = 5, IBZ = 6, NWAVE = 7 };
+enum { NHYDRO = 5 };
+
+struct orc_mesh {
+  orc_params p;
+  int nb, nc1, nc2, nc3, is, ie, js, je, ks, ke;
+  long ncell, nf1, nf2, nf3; /* per-block array sizes (one variable) */
+  /* per block state, AthenaArray layout */
+  double *u, *u1, *w, *w1, *bcc, *b1, *b2, *b3, *bb1, *bb2, *bb3;
+  double *x1f, *dx1f, *x2f, *dx2f, *x3f, *dx3f; /* per block */
+  double *x1v, *x2v, *x3v;
+  double *e1, *e2, *e3;  /* per block edge EMFs before the shared-edge averaging */
+  long ne1, ne2, ne3;
+  double dt, time;
+  long c2p_fail;
+};
+
+/* ------------------------------------------------------------------------------------
+ * indexing helpers (athena_arrays.hpp:140-143)
+ */
+#define CIDX(m, n, k, j, i) ((((long)(n) * (m)->nc3 + (k)) * (m)->nc2 + (j)) * (m)->nc1 + (i))
+#define F1IDX(m, k, j, i) ((((long)(k)) * (m)->nc2 + (j)) * ((m)->nc1 + 1) + (i))
+#define F2IDX(m, k, j, i) ((((long)(k)) * ((m)->nc2 + 1) + (j)) * (m)->nc1 + (i))
+#define F3IDX(m, k, j, i) ((((long)(k)) * (m)->nc2 + (j)) * (m)->nc1 + (i))
+
+/* per-block scratch used within one stage (the reference keeps these per object,
+ * hydro.cpp:31-148, field.cpp:27-105) */
+typedef struct {
+  double *flx1, *flx2, *flx3;          /* NHYDRO x face arrays */
+  double *e3x1, *e2x1, *w1f;           /* x1 faces */
+  double *e1x2, *e3x2, *w2f;           /* x2 faces */
+  double *e1x3, *e2x3, *w3f;           /* x3 faces */
+  double *e1, *e2, *e3;                /* edges */
+  double *cce;                         /* 3 x cells */
+} scratch;
+
+static void scratch_alloc(const orc_mesh *m, scratch *s) {
+  long n1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1);
+  long n2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1;
+  long n3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  s->flx1 = calloc(NHYDRO * n1, sizeof(double));
+  s->flx2 = calloc(NHYDRO * n2, sizeof(double));
+  s->flx3 = calloc(NHYDRO * n3, sizeof(double));
+  s->e3x1 = calloc(n1, sizeof(double)); s->e2x1 = calloc(n1, sizeof(double));
+  s->w1f = calloc(n1, sizeof(double));
+  s->e1x2 = calloc(n2, sizeof(double)); s->e3x2 = calloc(n2, sizeof(double));
+  s->w2f = calloc(n2, sizeof(double));
+  s->e1x3 = calloc(n3, sizeof(double)); s->e2x3 = calloc(n3, sizeof(double));
+  s->w3f = calloc(n3, sizeof(double));
+  /* edges: x1e (nc3+1, nc2+1, nc1), x2e (nc3+1, nc2, nc1+1), x3e (nc3, nc2+1, nc1+1)
+   * (athena.hpp:141-148) */
+  s->e1 = calloc((long)(m->nc3 + 1) * (m->nc2 + 1) * m->nc1, sizeof(double));
+  s->e2 = calloc((long)(m->nc3 + 1) * m->nc2 * (m->nc1 + 1), sizeof(double));
+  s->e3 = calloc((long)m->nc3 * (m->nc2 + 1) * (m->nc1 + 1), sizeof(double));
+  s->cce = calloc(3 * m->ncell, sizeof(double));
+}
+
+static void scratch_free(scratch *s) {
+  free(s->flx1); free(s->flx2); free(s->flx3); free(s->e3x1); free(s->e2x1);
+  free(s->w1f); free(s->e1x2); free(s->e3x2); free(s->w2f); free(s->e1x3);
+  free(s->e2x3); free(s->w3f); free(s->e1); free(s->e2); free(s->e3); free(s->cce);
+}
+
+#define E1IDX(m, k, j, i) ((((long)(k)) * ((m)->nc2 + 1) + (j)) * (m)->nc1 + (i))
+#define E2IDX(m, k, j, i) ((((long)(k)) * (m)->nc2 + (j)) * ((m)->nc1 + 1) + (i))
+#define E3IDX(m, k, j, i) ((((long)(k)) * ((m)->nc2 + 1) + (j)) * ((m)->nc1 + 1) + (i))
+
+/* ------------------------------------------------------------------------------------
+ * EOS pieces (eos/adiabatic_mhd.cpp)
+ */
+
+/* FastMagnetosonicSpeed, adiabatic_mhd.cpp:149-156 */
+static double fast_ms(double gamma, const double prim[NWAVE], double bx) {
+  double asq = gamma * prim[IPR];
+  double vaxsq = bx * bx;
+  double ct2 = (prim[IBY] * prim[IBY] + prim[IBZ] * prim[IBZ]);
+  double qsq = vaxsq + ct2 + asq;
+  double tmp = vaxsq + ct2 - asq;
+  return sqrt(0.5 * (qsq + sqrt(tmp * tmp + 4.0 * asq * ct2)) / prim[IDN]);
+}
+
+/* Hydro::GetWeightForCT, hydro.cpp:154-158 */
+static double weight_for_ct(double dflx, double rhol, double rhor, double dx, double dt) {
+  double v_over_c = (1024.0) * dt * dflx / (dx * (rhol + rhor));
+  double tmp_min = smin(0.5, v_over_c);
+  return 0.5 + smax(-0.5, tmp_min);
+}
+
+/* ------------------------------------------------------------------------------------
+ * Riemann solvers.  wl/wr are in the solver's local order (IDN, normal v, two
+ * transverse v, p, IBY, IBZ) as loaded in hlld.cpp:59-75.  out: f[0..4] = mass,
+ * normal/transverse momentum, energy fluxes in that local order, f[5] = F(By),
+ * f[6] = F(Bz).
+ */
+
+/* HLLD, hydro/rsolvers/mhd/hlld.cpp:36-376 (Miyoshi & Kusano 2005) */
+typedef struct { double d, mx, my, mz, e, by, bz; } cons1d;
+
+static void hlld(double gamma, const double *wli, const double *wri, double bxi,
+                 double *flxi) {
+  const double SMALL_NUMBER = 1.0e-4;
+  double igm1 = 1.0 / (gamma - 1.0);
+  cons1d ul, ur, ulst, uldst, urdst, urst, fl, fr;
+  double spd[5];
+
+  double bxsq = bxi * bxi;
+  double pbl = 0.5 * (bxsq + (SQR(wli[IBY]) + SQR(wli[IBZ])));
+  double pbr = 0.5 * (bxsq + (SQR(wri[IBY]) + SQR(wri[IBZ])));
+  double kel = 0.5 * wli[IDN] * (SQR(wli[IVX]) + (SQR(wli[IVY]) + SQR(wli[IVZ])));
+  double ker = 0.5 * wri[IDN] * (SQR(wri[IVX]) + (SQR(wri[IVY]) + SQR(wri[IVZ])));
+
+  ul.d = wli[IDN];
+  ul.mx = wli[IVX] * ul.d;
+  ul.my = wli[IVY] * ul.d;
+  ul.mz = wli[IVZ] * ul.d;
+  ul.e = wli[IPR] * igm1 + kel + pbl;
+  ul.by = wli[IBY];
+  ul.bz = wli[IBZ];
+
+  ur.d = wri[IDN];
+  ur.mx = wri[IVX] * ur.d;
+  ur.my = wri[IVY] * ur.d;
+  ur.mz = wri[IVZ] * ur.d;
+  ur.e = wri[IPR] * igm1 + ker + pbr;
+  ur.by = wri[IBY];
+  ur.bz = wri[IBZ];
+
+  /* eqn (67) wave speeds, hlld.cpp:104-108 */
+  double cfl = fast_ms(gamma, wli, bxi);
+  double cfr = fast_ms(gamma, wri, bxi);
+  spd[0] = smin(wli[IVX] - cfl, wri[IVX] - cfr);
+  spd[4] = smax(wli[IVX] + cfl, wri[IVX] + cfr);
+
+  /* L/R fluxes, hlld.cpp:121-142 */
+  double ptl = wli[IPR] + pbl;
+  double ptr = wri[IPR] + pbr;
+  fl.d = ul.mx;
+  fl.mx = ul.mx * wli[IVX] + ptl - bxsq;
+  fl.my = ul.my * wli[IVX] - bxi * ul.by;
+  fl.mz = ul.mz * wli[IVX] - bxi * ul.bz;
+  fl.e = wli[IVX] * (ul.e + ptl - bxsq) - bxi * (wli[IVY] * ul.by + wli[IVZ] * ul.bz);
+  fl.by = ul.by * wli[IVX] - bxi * wli[IVY];
+  fl.bz = ul.bz * wli[IVX] - bxi * wli[IVZ];
+
+  fr.d = ur.mx;
+  fr.mx = ur.mx * wri[IVX] + ptr - bxsq;
+  fr.my = ur.my * wri[IVX] - bxi * ur.by;
+  fr.mz = ur.mz * wri[IVX] - bxi * ur.bz;
+  fr.e = wri[IVX] * (ur.e + ptr - bxsq) - bxi * (wri[IVY] * ur.by + wri[IVZ] * ur.bz);
+  fr.by = ur.by * wri[IVX] - bxi * wri[IVY];
+  fr.bz = ur.bz * wri[IVX] - bxi * wri[IVZ];
+
+  /* middle and Alfven speeds, hlld.cpp:144-171 */
+  double sdl = spd[0] - wli[IVX];
+  double sdr = spd[4] - wri[IVX];
+  spd[2] = (sdr * ur.mx - sdl * ul.mx + (ptl - ptr)) / (sdr * ur.d - sdl * ul.d);
+  double sdml = spd[0] - spd[2];
+  double sdmr = spd[4] - spd[2];
+  double sdml_inv = 1.0 / sdml;
+  double sdmr_inv = 1.0 / sdmr;
+  ulst.d = ul.d * sdl * sdml_inv;
+  urst.d = ur.d * sdr * sdmr_inv;
+  double ulst_d_inv = 1.0 / ulst.d;
+  double urst_d_inv = 1.0 / urst.d;
+  double sqrtdl = sqrt(ulst.d);
+  double sqrtdr = sqrt(urst.d);
+  spd[1] = spd[2] - fabs(bxi) / sqrtdl;
+  spd[3] = spd[2] + fabs(bxi) / sqrtdr;
+
+  /* intermediate states, hlld.cpp:173-300 */
+  double ptstl = ptl + ul.d * sdl * (spd[2] - wli[IVX]);
+  double ptstr = ptr + ur.d * sdr * (spd[2] - wri[IVX]);
+  double ptst = 0.5 * (ptstr + ptstl);
+
+  ulst.mx = ulst.d * spd[2];
+  if (fabs(ul.d * sdl * sdml - bxsq) < (SMALL_NUMBER)*ptst) {
+    ulst.my = ulst.d * wli[IVY];
+    ulst.mz = ulst.d * wli[IVZ];
+    ulst.by = ul.by;
+    ulst.bz = ul.bz;
+  } else {
+    double tmp = bxi * (sdl - sdml) / (ul.d * sdl * sdml - bxsq);
+    ulst.my = ulst.d * (wli[IVY] - ul.by * tmp);
+    ulst.mz = ulst.d * (wli[IVZ] - ul.bz * tmp);
+    tmp = (ul.d * SQR(sdl) - bxsq) / (ul.d * sdl * sdml - bxsq);
+    ulst.by = ul.by * tmp;
+    ulst.bz = ul.bz * tmp;
+  }
+  double vbstl = (ulst.mx * bxi + (ulst.my * ulst.by + ulst.mz * ulst.bz)) * ulst_d_inv;
+  ulst.e = (sdl * ul.e - ptl * wli[IVX] + ptst * spd[2] +
+            bxi * (wli[IVX] * bxi + (wli[IVY] * ul.by + wli[IVZ] * ul.bz) - vbstl)) *
+           sdml_inv;
+
+  urst.mx = urst.d * spd[2];
+  if (fabs(ur.d * sdr * sdmr - bxsq) < (SMALL_NUMBER)*ptst) {
+    urst.my = urst.d * wri[IVY];
+    urst.mz = urst.d * wri[IVZ];
+    urst.by = ur.by;
+    urst.bz = ur.bz;
+  } else {
+    double tmp = bxi * (sdr - sdmr) / (ur.d * sdr * sdmr - bxsq);
+    urst.my = urst.d * (wri[IVY] - ur.by * tmp);
+    urst.mz = urst.d * (wri[IVZ] - ur.bz * tmp);
+    tmp = (ur.d * SQR(sdr) - bxsq) / (ur.d * sdr * sdmr - bxsq);
+    urst.by = ur.by * tmp;
+    urst.bz = ur.bz * tmp;
+  }
+  double vbstr = (urst.mx * bxi + (urst.my * urst.by + urst.mz * urst.bz)) * urst_d_inv;
+  urst.e = (sdr * ur.e - ptr * wri[IVX] + ptst * spd[2] +
+            bxi * (wri[IVX] * bxi + (wri[IVY] * ur.by + wri[IVZ] * ur.bz) - vbstr)) *
+           sdmr_inv;
+
+  double invsumd = 1.0 / (sqrtdl + sqrtdr);
+  double bxsig = (bxi > 0.0 ? 1.0 : -1.0);
+  uldst.d = ulst.d;
+  urdst.d = urst.d;
+  uldst.mx = ulst.mx;
+  urdst.mx = urst.mx;
+  double tmp = invsumd * (sqrtdl * (ulst.my * ulst_d_inv) + sqrtdr * (urst.my * urst_d_inv) +
+                          bxsig * (urst.by - ulst.by));
+  uldst.my = uldst.d * tmp;
+  urdst.my = urdst.d * tmp;
+  tmp = invsumd * (sqrtdl * (ulst.mz * ulst_d_inv) + sqrtdr * (urst.mz * urst_d_inv) +
+                   bxsig * (urst.bz - ulst.bz));
+  uldst.mz = uldst.d * tmp;
+  urdst.mz = urdst.d * tmp;
+  tmp = invsumd * (sqrtdl * urst.by + sqrtdr * ulst.by +
+                   bxsig * sqrtdl * sqrtdr * ((urst.my * urst_d_inv) - (ulst.my * ulst_d_inv)));
+  uldst.by = urdst.by = tmp;
+  tmp = invsumd * (sqrtdl * urst.bz + sqrtdr * ulst.bz +
+                   bxsig * sqrtdl * sqrtdr * ((urst.mz * urst_d_inv) - (ulst.mz * ulst_d_inv)));
+  uldst.bz = urdst.bz = tmp;
+  tmp = spd[2] * bxi + (uldst.my * uldst.by + uldst.mz * uldst.bz) / uldst.d;
+  uldst.e = ulst.e - sqrtdl * bxsig * (vbstl - tmp);
+  urdst.e = urst.e + sqrtdr * bxsig * (vbstr - tmp);
+
+  /* jumps across the waves, hlld.cpp:302-332 */
+#define JUMP(dst, a, b, s)                     \
+  do {                                         \
+    dst.d = (s) * (a.d - b.d);                 \
+    dst.mx = (s) * (a.mx - b.mx);              \
+    dst.my = (s) * (a.my - b.my);              \
+    dst.mz = (s) * (a.mz - b.mz);              \
+    dst.e = (s) * (a.e - b.e);                 \
+    dst.by = (s) * (a.by - b.by);              \
+    dst.bz = (s) * (a.bz - b.bz);              \
+  } while (0)
+  JUMP(uldst, uldst, ulst, spd[1]);
+  JUMP(ulst, ulst, ul, spd[0]);
+  JUMP(urdst, urdst, urst, spd[3]);
+  JUMP(urst, urst, ur, spd[4]);
+#undef JUMP
+
+  /* upwind selection, hlld.cpp:334-370 */
+  cons1d f;
+  if (spd[0] >= 0.0) {
+    f = fl;
+  } else if (spd[4] <= 0.0) {
+    f = fr;
+  } else if (spd[1] >= 0.0) {
+    f.d = fl.d + ulst.d; f.mx = fl.mx + ulst.mx; f.my = fl.my + ulst.my;
+    f.mz = fl.mz + ulst.mz; f.e = fl.e + ulst.e; f.by = fl.by + ulst.by;
+    f.bz = fl.bz + ulst.bz;
+  } else if (spd[3] <= 0.0) {
+    f.d = fr.d + urst.d; f.mx = fr.mx + urst.mx; f.my = fr.my + urst.my;
+    f.mz = fr.mz + urst.mz; f.e = fr.e + urst.e; f.by = fr.by + urst.by;
+    f.bz = fr.bz + urst.bz;
+  } else if (spd[2] >= 0.0) {
+    f.d = fl.d + ulst.d + uldst.d; f.mx = fl.mx + ulst.mx + uldst.mx;
+    f.my = fl.my + ulst.my + uldst.my; f.mz = fl.mz + ulst.mz + uldst.mz;
+    f.e = fl.e + ulst.e + uldst.e; f.by = fl.by + ulst.by + uldst.by;
+    f.bz = fl.bz + ulst.bz + uldst.bz;
+  } else {
+    f.d = fr.d + urst.d + urdst.d; f.mx = fr.mx + urst.mx + urdst.mx;
+    f.my = fr.my + urst.my + urdst.my; f.mz = fr.mz + urst.mz + urdst.mz;
+    f.e = fr.e + urst.e + urdst.e; f.by = fr.by + urst.by + urdst.by;
+    f.bz = fr.bz + urst.bz + urdst.bz;
+  }
+  flxi[0] = f.d; flxi[1] = f.mx; flxi[2] = f.my; flxi[3] = f.mz; flxi[4] = f.e;
+  flxi[5] = f.by; flxi[6] = f.bz;
+}
+
+/* HLLE, hydro/rsolvers/mhd/hlle_mhd.cpp:25-182 */
+static void hlle(double gamma, const double *wli, const double *wri, double bxi,
+                 double *flxi) {
+  double gm1 = gamma - 1.0;
+  double fl[NWAVE], fr[NWAVE];
+  double sqrtdl = sqrt(wli[IDN]);
+  double sqrtdr = sqrt(wri[IDN]);
+  double isdlpdr = 1.0 / (sqrtdl + sqrtdr);
+  double wroe_d = sqrtdl * sqrtdr;
+  double wroe_vx = (sqrtdl * wli[IVX] + sqrtdr * wri[IVX]) * isdlpdr;
+  double wroe_vy = (sqrtdl * wli[IVY] + sqrtdr * wri[IVY]) * isdlpdr;
+  double wroe_vz = (sqrtdl * wli[IVZ] + sqrtdr * wri[IVZ]) * isdlpdr;
+  double wroe_by = (sqrtdr * wli[IBY] + sqrtdl * wri[IBY]) * isdlpdr;
+  double wroe_bz = (sqrtdr * wli[IBZ] + sqrtdl * wri[IBZ]) * isdlpdr;
+  double x = 0.5 * (SQR(wli[IBY] - wri[IBY]) + SQR(wli[IBZ] - wri[IBZ])) /
+             (SQR(sqrtdl + sqrtdr));
+  double y = 0.5 * (wli[IDN] + wri[IDN]) / wroe_d;
+
+  double pbl = 0.5 * (bxi * bxi + SQR(wli[IBY]) + SQR(wli[IBZ]));
+  double pbr = 0.5 * (bxi * bxi + SQR(wri[IBY]) + SQR(wri[IBZ]));
+  double el = wli[IPR] / gm1 +
+              0.5 * wli[IDN] * (SQR(wli[IVX]) + SQR(wli[IVY]) + SQR(wli[IVZ])) + pbl;
+  double er = wri[IPR] / gm1 +
+              0.5 * wri[IDN] * (SQR(wri[IVX]) + SQR(wri[IVY]) + SQR(wri[IVZ])) + pbr;
+  double hroe = ((el + wli[IPR] + pbl) / sqrtdl + (er + wri[IPR] + pbr) / sqrtdr) * isdlpdr;
+
+  double cl = fast_ms(gamma, wli, bxi);
+  double cr = fast_ms(gamma, wri, bxi);
+
+  double btsq = SQR(wroe_by) + SQR(wroe_bz);
+  double vaxsq = bxi * bxi / wroe_d;
+  double bt_starsq = (gm1 - (gm1 - 1.0) * y) * btsq;
+  double hp = hroe - (vaxsq + btsq / wroe_d);
+  double vsq = SQR(wroe_vx) + SQR(wroe_vy) + SQR(wroe_vz);
+  double twid_asq = smax((gm1 * (hp - 0.5 * vsq) - (gm1 - 1.0) * x), 0.0);
+  double ct2 = bt_starsq / wroe_d;
+  double tsum = vaxsq + ct2 + twid_asq;
+  double tdif = vaxsq + ct2 - twid_asq;
+  double cf2_cs2 = sqrt(tdif * tdif + 4.0 * twid_asq * ct2);
+  double cfsq = 0.5 * (tsum + cf2_cs2);
+  double a = sqrt(cfsq);
+
+  double al = smin((wroe_vx - a), (wli[IVX] - cl));
+  double ar = smax((wroe_vx + a), (wri[IVX] + cr));
+  double bp = ar > 0.0 ? ar : 0.0;
+  double bm = al < 0.0 ? al : 0.0;
+
+  double vxl = wli[IVX] - bm;
+  double vxr = wri[IVX] - bp;
+  fl[IDN] = wli[IDN] * vxl;
+  fr[IDN] = wri[IDN] * vxr;
+  fl[IVX] = wli[IDN] * wli[IVX] * vxl + pbl - SQR(bxi);
+  fr[IVX] = wri[IDN] * wri[IVX] * vxr + pbr - SQR(bxi);
+  fl[IVY] = wli[IDN] * wli[IVY] * vxl - bxi * wli[IBY];
+  fr[IVY] = wri[IDN] * wri[IVY] * vxr - bxi * wri[IBY];
+  fl[IVZ] = wli[IDN] * wli[IVZ] * vxl - bxi * wli[IBZ];
+  fr[IVZ] = wri[IDN] * wri[IVZ] * vxr - bxi * wri[IBZ];
+  fl[IVX] += wli[IPR];
+  fr[IVX] += wri[IPR];
+  fl[IPR] = el * vxl + wli[IVX] * (wli[IPR] + pbl - bxi * bxi);
+  fr[IPR] = er * vxr + wri[IVX] * (wri[IPR] + pbr - bxi * bxi);
+  fl[IPR] -= bxi * (wli[IBY] * wli[IVY] + wli[IBZ] * wli[IVZ]);
+  fr[IPR] -= bxi * (wri[IBY] * wri[IVY] + wri[IBZ] * wri[IVZ]);
+  fl[IBY] = wli[IBY] * vxl - bxi * wli[IVY];
+  fr[IBY] = wri[IBY] * vxr - bxi * wri[IVY];
+  fl[IBZ] = wli[IBZ] * vxl - bxi * wli[IVZ];
+  fr[IBZ] = wri[IBZ] * vxr - bxi * wri[IVZ];
+
+  double tmp = 0.0;
+  if (bp != bm) tmp = 0.5 * (bp + bm) / (bp - bm);
+  for (int n = 0; n < NWAVE; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Reconstruction of one cell along a direction: given the 7-component wave vector of the
+ * cell and its neighbours, return the value at its upper face (qlp, becomes wl of the
+ * next face) and at its lower face (qrm, becomes wr of this face).
+ */
+
+/* PiecewiseLinearX1/2/3 uniform van Leer branch, plm.cpp:103-112 and :148-152 */
+static void plm_cell(const double *qm, const double *q0, const double *qp, double cp,
+                     double cm, double *qlp, double *qrm) {
+  for (int n = 0; n < NWAVE; ++n) {
+    double dwl = (q0[n] - qm[n]);
+    double dwr = (qp[n] - q0[n]);
+    double dw2 = dwl * dwr;
+    double dwm = 2.0 * dw2 / (dwl + dwr);
+    if (dw2 <= 0.0) dwm = 0.0;
+    qlp[n] = q0[n] + cp * dwm;
+    qrm[n] = q0[n] - cm * dwm;
+  }
+}
+
+/* PiecewiseParabolicX1/2/3 uniform-Cartesian CS08 branch, ppm.cpp:113-315,
+ * coefficients c1..c6 = 1/2,1/2,1/2,1/2,1/6,-1/6 (reconstruction.cpp:499-504);
+ * floors ppm.cpp:326-331.  q[0..4] = cells i-2..i+2. */
+static void ppm_cell(const double *const q[5], double dfloor, double pfloor, double *qlp,
+                     double *qrm) {
+  const double C2 = 1.25;
+  const double c1 = 0.5, c2 = 0.5, c3 = 0.5, c4 = 0.5, c5 = 1.0 / 6.0, c6 = -1.0 / 6.0;
+  for (int n = 0; n < NWAVE; ++n) {
+    double q_im2 = q[0][n], q_im1 = q[1][n], qc = q[2][n], q_ip1 = q[3][n], q_ip2 = q[4][n];
+    double qa = (qc - q_im1);
+    double qb = (q_ip1 - qc);
+    double dd_im1 = c1 * qa + c2 * (q_im1 - q_im2);
+    double dd = c1 * qb + c2 * qa;
+    double dd_ip1 = c1 * (q_ip2 - q_ip1) + c2 * qb;
+    double dph = (c3 * q_im1 + c4 * qc) + (c5 * dd_im1 + c6 * dd);
+    double dph_ip1 = (c3 * qc + c4 * q_ip1) + (c5 * dd + c6 * dd_ip1);
+
+    double d2qc_im1 = q_im2 + qc - 2.0 * q_im1;
+    double d2qc = q_im1 + q_ip1 - 2.0 * qc;
+    double d2qc_ip1 = qc + q_ip2 - 2.0 * q_ip1;
+
+    { /* i-1/2 */
+      double qa_tmp = dph - q_im1;
+      double qb_tmp = qc - dph;
+      double a = 3.0 * (q_im1 + qc - 2.0 * dph);
+      double b = d2qc_im1, c = d2qc, d = 0.0;
+      if (SIGN(a) == SIGN(b) && SIGN(a) == SIGN(c))
+        d = SIGN(a) * smin(C2 * fabs(b), smin(C2 * fabs(c), fabs(a)));
+      double dph_tmp = 0.5 * (q_im1 + qc) - d / 6.0;
+      if (qa_tmp * qb_tmp < 0.0) dph = dph_tmp;
+    }
+    { /* i+1/2 */
+      double qa_tmp = dph_ip1 - qc;
+      double qb_tmp = q_ip1 - dph_ip1;
+      double a = 3.0 * (qc + q_ip1 - 2.0 * dph_ip1);
+      double b = d2qc, c = d2qc_ip1, d = 0.0;
+      if (SIGN(a) == SIGN(b) && SIGN(a) == SIGN(c))
+        d = SIGN(a) * smin(C2 * fabs(b), smin(C2 * fabs(c), fabs(a)));
+      double dphip1_tmp = 0.5 * (qc + q_ip1) - d / 6.0;
+      if (qa_tmp * qb_tmp < 0.0) dph_ip1 = dphip1_tmp;
+    }
+    double d2qf = 6.0 * (dph + dph_ip1 - 2.0 * qc);
+    double qminus = dph, qplus = dph_ip1;
+    double dqf_minus = qc - qminus;
+    double dqf_plus = qplus - qc;
+    { /* CS limiter, ppm.cpp:234-288 */
+      double qa_tmp = dqf_minus * dqf_plus;
+      double qb_tmp = (q_ip1 - qc) * (qc - q_im1);
+      double a = d2qc_im1, b = d2qc, c = d2qc_ip1, d = d2qf, e = 0.0;
+      if (SIGN(a) == SIGN(b) && SIGN(a) == SIGN(c) && SIGN(a) == SIGN(d))
+        e = SIGN(d) * smin(smin(C2 * fabs(a), C2 * fabs(b)), smin(C2 * fabs(c), fabs(d)));
+      a = smax(fabs(q_im1), fabs(q_im2));
+      b = smax(smax(fabs(qc), fabs(q_ip1)), fabs(q_ip2));
+      double rho = 0.0;
+      if (fabs(d) > (1.0e-12) * smax(a, b)) rho = e / d;
+      double tmp_m = qc - rho * dqf_minus;
+      double tmp_p = qc + rho * dqf_plus;
+      double tmp2_m = qc - 2.0 * dqf_plus;
+      double tmp2_p = qc + 2.0 * dqf_minus;
+      if ((qa_tmp <= 0.0 || qb_tmp <= 0.0)) {
+        if (rho <= (1.0 - (1.0e-12))) {
+          qminus = tmp_m;
+          qplus = tmp_p;
+        }
+      } else {
+        if (fabs(dqf_minus) >= 2.0 * fabs(dqf_plus)) qminus = tmp2_m;
+        if (fabs(dqf_plus) >= 2.0 * fabs(dqf_minus)) qplus = tmp2_p;
+      }
+    }
+    qlp[n] = qplus;
+    qrm[n] = qminus;
+  }
+  /* ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 */
+  qlp[IDN] = (qlp[IDN] > dfloor) ? qlp[IDN] : dfloor;
+  qlp[IPR] = (qlp[IPR] > pfloor) ? qlp[IPR] : pfloor;
+  qrm[IDN] = (qrm[IDN] > dfloor) ? qrm[IDN] : dfloor;
+  qrm[IPR] = (qrm[IPR] > pfloor) ? qrm[IPR] : pfloor;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Hydro::CalculateFluxes, calculate_fluxes.cpp:38-415 (MHD, 3-D, order 1/2/3)
+ */
+
+/* wave vector of cell (k,j,i) for sweep direction dir: w in natural order, then the
+ * two transverse cell-centred field components (plm.cpp:45-57 for x1, :196-208 for x2,
+ * x3 analogous). */
+static void load_wave(const orc_mesh *m, const double *w, const double *bcc, int dir, int k,
+                      int j, int i, double *q) {
+  for (int n = 0; n < NHYDRO; ++n) q[n] = w[CIDX(m, n, k, j, i)];
+  q[IBY] = bcc[CIDX(m, (dir + 1) % 3, k, j, i)];
+  q[IBZ] = bcc[CIDX(m, (dir + 2) % 3, k, j, i)];
+}
+
+/* recon of cell c along dir; returns upper-face (qlp) and lower-face (qrm) states */
+static void recon_cell(const orc_mesh *m, int b, const double *w, const double *bcc,
+                       int order, int dir, int k, int j, int i, double *qlp, double *qrm) {
+  int dk = (dir == 2), dj = (dir == 1), di = (dir == 0);
+  if (order == 1) { /* DonorCellX1/2/3, dc.cpp:24-104 */
+    load_wave(m, w, bcc, dir, k, j, i, qlp);
+    memcpy(qrm, qlp, sizeof(double) * NWAVE);
+  } else if (order == 2) {
+    double qm[NWAVE], q0[NWAVE], qp[NWAVE];
+    load_wave(m, w, bcc, dir, k - dk, j - dj, i - di, qm);
+    load_wave(m, w, bcc, dir, k, j, i, q0);
+    load_wave(m, w, bcc, dir, k + dk, j + dj, i + di, qp);
+    /* (x?f(c+1) - x?v(c))/dx?f(c) and (x?v(c) - x?f(c))/dx?f(c), plm.cpp:148-152 */
+    const double *xf, *xv, *dxf;
+    int c;
+    if (dir == 0) {
+      xf = m->x1f + (long)b * (m->nc1 + 1); xv = m->x1v + (long)b * m->nc1;
+      dxf = m->dx1f + (long)b * m->nc1; c = i;
+    } else if (dir == 1) {
+      xf = m->x2f + (long)b * (m->nc2 + 1); xv = m->x2v + (long)b * m->nc2;
+      dxf = m->dx2f + (long)b * m->nc2; c = j;
+    } else {
+      xf = m->x3f + (long)b * (m->nc3 + 1); xv = m->x3v + (long)b * m->nc3;
+      dxf = m->dx3f + (long)b * m->nc3; c = k;
+    }
+    double cp = (xf[c + 1] - xv[c]) / dxf[c];
+    double cm = (xv[c] - xf[c]) / dxf[c];
+    plm_cell(qm, q0, qp, cp, cm, qlp, qrm);
+  } else {
+    double qs[5][NWAVE];
+    const double *qp[5];
+    for (int s = 0; s < 5; ++s) {
+      load_wave(m, w, bcc, dir, k + (s - 2) * dk, j + (s - 2) * dj, i + (s - 2) * di, qs[s]);
+      qp[s] = qs[s];
+    }
+    ppm_cell(qp, m->p.dfloor, m->p.pfloor, qlp, qrm);
+  }
+}
+
+static void riemann(const orc_mesh *m, int dir, const double *wl, const double *wr,
+                    double bx, double *flx7) {
+  /* local order: IDN, v_normal, v_t1, v_t2, p, IBY, IBZ; ivx = IVX+dir,
+   * ivy = IVX+(dir+1)%3, ivz = IVX+(dir+2)%3 (hlld.cpp:42-43, 59-75) */
+  int ivx = IVX + dir, ivy = IVX + (dir + 1) % 3, ivz = IVX + (dir + 2) % 3;
+  double wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
+  double wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
+  if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
+  else hlle(m->p.gamma, wli, wri, bx, flx7);
+}
+
+static void calculate_fluxes(orc_mesh *m, int b, int order, scratch *s) {
+  const double *w = m->w + (long)b * NHYDRO * m->ncell;
+  const double *bcc = m->bcc + (long)b * 3 * m->ncell;
+  const double *b1 = m->b1 + (long)b * m->nf1, *b2 = m->b2 + (long)b * m->nf2,
+               *b3 = m->b3 + (long)b * m->nf3;
+  const double *dx1f = m->dx1f + (long)b * m->nc1, *dx2f = m->dx2f + (long)b * m->nc2,
+               *dx3f = m->dx3f + (long)b * m->nc3;
+  double dt = m->dt;
+  int is = m->is, ie = m->ie, js = m->js, je = m->je, ks = m->ks, ke = m->ke;
+  long n1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1), n2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1,
+       n3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  double wl[NWAVE], wr[NWAVE], tmp[NWAVE], f[NWAVE];
+
+  /* x1: k in [ks-1,ke+1], j in [js-1,je+1], faces i in [is,ie+1] (:64-76, :78-102) */
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j)
+      for (int i = is; i <= ie + 1; ++i) {
+        recon_cell(m, b, w, bcc, order, 0, k, j, i - 1, wl, tmp);
+        recon_cell(m, b, w, bcc, order, 0, k, j, i, tmp, wr);
+        long fi = F1IDX(m, k, j, i);
+        riemann(m, 0, wl, wr, b1[fi], f);
+        s->flx1[0 * n1 + fi] = f[0];
+        s->flx1[1 * n1 + fi] = f[1];
+        s->flx1[2 * n1 + fi] = f[2];
+        s->flx1[3 * n1 + fi] = f[3];
+        s->flx1[4 * n1 + fi] = f[4];
+        s->e3x1[fi] = -f[5];
+        s->e2x1[fi] = f[6];
+        s->w1f[fi] = weight_for_ct(f[0], wl[IDN], wr[IDN], dx1f[i], dt);
+      }
+  /* x2: k in [ks-1,ke+1], i in [is-1,ie+1], faces j in [js,je+1] (:169-237) */
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is - 1; i <= ie + 1; ++i) {
+        recon_cell(m, b, w, bcc, order, 1, k, j - 1, i, wl, tmp);
+        recon_cell(m, b, w, bcc, order, 1, k, j, i, tmp, wr);
+        long fi = F2IDX(m, k, j, i);
+        riemann(m, 1, wl, wr, b2[fi], f);
+        /* flux slots: IDN, ivx=IVY, ivy=IVZ, ivz=IVX, IEN */
+        s->flx2[0 * n2 + fi] = f[0];
+        s->flx2[2 * n2 + fi] = f[1];
+        s->flx2[3 * n2 + fi] = f[2];
+        s->flx2[1 * n2 + fi] = f[3];
+        s->flx2[4 * n2 + fi] = f[4];
+        s->e1x2[fi] = -f[5];
+        s->e3x2[fi] = f[6];
+        s->w2f[fi] = weight_for_ct(f[0], wl[IDN], wr[IDN], dx2f[j], dt);
+      }
+  /* x3: j in [js-1,je+1], i in [is-1,ie+1], faces k in [ks,ke+1] (:292-356) */
+  for (int k = ks; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j)
+      for (int i = is - 1; i <= ie + 1; ++i) {
+        recon_cell(m, b, w, bcc, order, 2, k - 1, j, i, wl, tmp);
+        recon_cell(m, b, w, bcc, order, 2, k, j, i, tmp, wr);
+        long fi = F3IDX(m, k, j, i);
+        riemann(m, 2, wl, wr, b3[fi], f);
+        /* flux slots: IDN, ivx=IVZ, ivy=IVX, ivz=IVY, IEN */
+        s->flx3[0 * n3 + fi] = f[0];
+        s->flx3[3 * n3 + fi] = f[1];
+        s->flx3[1 * n3 + fi] = f[2];
+        s->flx3[2 * n3 + fi] = f[3];
+        s->flx3[4 * n3 + fi] = f[4];
+        s->e2x3[fi] = -f[5];
+        s->e1x3[fi] = f[6];
+        s->w3f[fi] = weight_for_ct(f[0], wl[IDN], wr[IDN], dx3f[k], dt);
+      }
+}
+
+/* ------------------------------------------------------------------------------------
+ * Field::ComputeCornerE, calculate_corner_e.cpp:124-236 (3-D, Newtonian and SR branches)
+ */
+static void corner_e(orc_mesh *m, int b, scratch *s) {
+  const double *w = m->w + (long)b * NHYDRO * m->ncell;
+  const double *bcc = m->bcc + (long)b * 3 * m->ncell;
+  int is = m->is, ie = m->ie, js = m->js, je = m->je, ks = m->ks, ke = m->ke;
+  double *cce = s->cce;
+  long nc = m->ncell;
+  for (int k = ks - 1; k <= ke + 1; ++k)
+    for (int j = js - 1; j <= je + 1; ++j)
+      for (int i = is - 1; i <= ie + 1; ++i) {
+        long c = CIDX(m, 0, k, j, i);
+        if (m->p.relativistic) {
+          /* SR branch, calculate_corner_e.cpp:161-172 */
+          double u1 = w[c + 1 * nc], u2 = w[c + 2 * nc], u3 = w[c + 3 * nc];
+          double u0 = sqrt(1.0 + SQR(u1) + SQR(u2) + SQR(u3));
+          cce[c] = (u3 * bcc[c + 1 * nc] - u2 * bcc[c + 2 * nc]) / u0;
+          cce[c + nc] = (u1 * bcc[c + 2 * nc] - u3 * bcc[c]) / u0;
+          cce[c + 2 * nc] = (u2 * bcc[c] - u1 * bcc[c + 1 * nc]) / u0;
+        } else {
+          cce[c] = w[c + 3 * nc] * bcc[c + 1 * nc] - w[c + 2 * nc] * bcc[c + 2 * nc];
+          cce[c + nc] = w[c + 1 * nc] * bcc[c + 2 * nc] - w[c + 3 * nc] * bcc[c];
+          cce[c + 2 * nc] = w[c + 2 * nc] * bcc[c] - w[c + 1 * nc] * bcc[c + 1 * nc];
+        }
+      }
+#define CC(n, k, j, i) cce[CIDX(m, n, k, j, i)]
+#define W1F(k, j, i) s->w1f[F1IDX(m, k, j, i)]
+#define W2F(k, j, i) s->w2f[F2IDX(m, k, j, i)]
+#define W3F(k, j, i) s->w3f[F3IDX(m, k, j, i)]
+#define E3X1(k, j, i) s->e3x1[F1IDX(m, k, j, i)]
+#define E2X1(k, j, i) s->e2x1[F1IDX(m, k, j, i)]
+#define E1X2(k, j, i) s->e1x2[F2IDX(m, k, j, i)]
+#define E3X2(k, j, i) s->e3x2[F2IDX(m, k, j, i)]
+#define E1X3(k, j, i) s->e1x3[F3IDX(m, k, j, i)]
+#define E2X3(k, j, i) s->e2x3[F3IDX(m, k, j, i)]
+  for (int k = ks; k <= ke + 1; ++k)
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie + 1; ++i) {
+        double de1_l3 = (1.0 - W2F(k - 1, j, i)) * (E1X3(k, j, i) - CC(0, k - 1, j, i)) +
+                        (W2F(k - 1, j, i)) * (E1X3(k, j - 1, i) - CC(0, k - 1, j - 1, i));
+        double de1_r3 = (1.0 - W2F(k, j, i)) * (E1X3(k, j, i) - CC(0, k, j, i)) +
+                        (W2F(k, j, i)) * (E1X3(k, j - 1, i) - CC(0, k, j - 1, i));
+        double de1_l2 = (1.0 - W3F(k, j - 1, i)) * (E1X2(k, j, i) - CC(0, k, j - 1, i)) +
+                        (W3F(k, j - 1, i)) * (E1X2(k - 1, j, i) - CC(0, k - 1, j - 1, i));
+        double de1_r2 = (1.0 - W3F(k, j, i)) * (E1X2(k, j, i) - CC(0, k, j, i)) +
+                        (W3F(k, j, i)) * (E1X2(k - 1, j, i) - CC(0, k - 1, j, i));
+        if (i <= ie)
+          m->e1[(long)b * m->ne1 + E1IDX(m, k, j, i)] =
+              0.25 * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + E1X2(k - 1, j, i) + E1X2(k, j, i) +
+                      E1X3(k, j - 1, i) + E1X3(k, j, i));
+
+        double de2_l3 = (1.0 - W1F(k - 1, j, i)) * (E2X3(k, j, i) - CC(1, k - 1, j, i)) +
+                        (W1F(k - 1, j, i)) * (E2X3(k, j, i - 1) - CC(1, k - 1, j, i - 1));
+        double de2_r3 = (1.0 - W1F(k, j, i)) * (E2X3(k, j, i) - CC(1, k, j, i)) +
+                        (W1F(k, j, i)) * (E2X3(k, j, i - 1) - CC(1, k, j, i - 1));
+        double de2_l1 = (1.0 - W3F(k, j, i - 1)) * (E2X1(k, j, i) - CC(1, k, j, i - 1)) +
+                        (W3F(k, j, i - 1)) * (E2X1(k - 1, j, i) - CC(1, k - 1, j, i - 1));
+        double de2_r1 = (1.0 - W3F(k, j, i)) * (E2X1(k, j, i) - CC(1, k, j, i)) +
+                        (W3F(k, j, i)) * (E2X1(k - 1, j, i) - CC(1, k - 1, j, i));
+        if (j <= je)
+          m->e2[(long)b * m->ne2 + E2IDX(m, k, j, i)] =
+              0.25 * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + E2X3(k, j, i - 1) + E2X3(k, j, i) +
+                      E2X1(k - 1, j, i) + E2X1(k, j, i));
+
+        double de3_l2 = (1.0 - W1F(k, j - 1, i)) * (E3X2(k, j, i) - CC(2, k, j - 1, i)) +
+                        (W1F(k, j - 1, i)) * (E3X2(k, j, i - 1) - CC(2, k, j - 1, i - 1));
+        double de3_r2 = (1.0 - W1F(k, j, i)) * (E3X2(k, j, i) - CC(2, k, j, i)) +
+                        (W1F(k, j, i)) * (E3X2(k, j, i - 1) - CC(2, k, j, i - 1));
+        double de3_l1 = (1.0 - W2F(k, j, i - 1)) * (E3X1(k, j, i) - CC(2, k, j, i - 1)) +
+                        (W2F(k, j, i - 1)) * (E3X1(k, j - 1, i) - CC(2, k, j - 1, i - 1));
+        double de3_r1 = (1.0 - W2F(k, j, i)) * (E3X1(k, j, i) - CC(2, k, j, i)) +
+                        (W2F(k, j, i)) * (E3X1(k, j - 1, i) - CC(2, k, j - 1, i));
+        if (k <= ke)
+          m->e3[(long)b * m->ne3 + E3IDX(m, k, j, i)] =
+              0.25 * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + E3X2(k, j, i - 1) + E3X2(k, j, i) +
+                      E3X1(k, j - 1, i) + E3X1(k, j, i));
+      }
+#undef CC
+#undef W1F
+#undef W2F
+#undef W3F
+#undef E3X1
+#undef E2X1
+#undef E1X2
+#undef E3X2
+#undef E1X3
+#undef E2X3
+}
+
+/* ------------------------------------------------------------------------------------
+ * Same-level EMF correction on block faces, FaceCenteredBoundaryVariable
+ * (flux_correction_fc.cpp:51-260 pack, :689-940 add, :1355-1530 average).  Every edge on
+ * a block face receives the pre-averaging values that the blocks sharing it computed,
+ * added to its own in the order of the neighbour list (bvals_base.cpp:326-720: faces
+ * x1-, x1+, x2-, x2+, x3-, x3+, then x1x2, x1x3, x2x3 edges), and is then scaled by 1/2
+ * (edges inside a face) or 1/4 (edges shared by four blocks).  Periodic uniform mesh:
+ * the neighbour in direction o holds the same edge at index - o*nx.
+ */
+static int nbr_block(const orc_mesh *m, int b, int o1, int o2, int o3) {
+  int n1 = m->p.nbx1, n2 = m->p.nbx2, n3 = m->p.nbx3;
+  int l1 = b % n1, l2 = (b / n1) % n2, l3 = b / (n1 * n2);
+  l1 = (l1 + o1 + n1) % n1; l2 = (l2 + o2 + n2) % n2; l3 = (l3 + o3 + n3) % n3;
+  return (l3 * n2 + l2) * n1 + l1;
+}
+
+/* corrected value of edge component c (0,1,2 = e1,e2,e3) at (k,j,i) of block b */
+static double emf_corrected(const orc_mesh *m, int b, int c, int k, int j, int i) {
+  const double *E = (c == 0) ? m->e1 : (c == 1) ? m->e2 : m->e3;
+  long ne = (c == 0) ? m->ne1 : (c == 1) ? m->ne2 : m->ne3;
+#define EV(bb, kk, jj, ii) \
+  E[(long)(bb) * ne + ((c == 0) ? E1IDX(m, kk, jj, ii) : (c == 1) ? E2IDX(m, kk, jj, ii) \
+                                                                    : E3IDX(m, kk, jj, ii))]
+  int o[3] = {0, 0, 0};  /* position of the edge on the block faces, per axis */
+  if (c != 0) o[0] = (i == m->is) ? -1 : (i == m->ie + 1) ? 1 : 0;
+  if (c != 1) o[1] = (j == m->js) ? -1 : (j == m->je + 1) ? 1 : 0;
+  if (c != 2) o[2] = (k == m->ks) ? -1 : (k == m->ke + 1) ? 1 : 0;
+  int nx[3] = {m->p.nx1, m->p.nx2, m->p.nx3};
+  int on = (o[0] != 0) + (o[1] != 0) + (o[2] != 0);
+  double own = EV(b, k, j, i);
+  if (on == 0) return own;
+  /* the two transverse axes of this component, in neighbour-list order */
+  int a0 = (c == 0) ? 1 : 0, a1 = (c == 2) ? 1 : 2;
+  double sum = own;
+  int axes[2] = {a0, a1};
+  for (int t = 0; t < 2; ++t) { /* face neighbours */
+    int ax = axes[t];
+    if (o[ax] == 0) continue;
+    int d[3] = {0, 0, 0};
+    d[ax] = o[ax];
+    int nb = nbr_block(m, b, d[0], d[1], d[2]);
+    sum += EV(nb, k - d[2] * nx[2], j - d[1] * nx[1], i - d[0] * nx[0]);
+  }
+  if (on == 2) { /* edge neighbour */
+    int nb = nbr_block(m, b, o[0], o[1], o[2]);
+    sum += EV(nb, k - o[2] * nx[2], j - o[1] * nx[1], i - o[0] * nx[0]);
+    return sum * (1.0 / 4.0);
+  }
+  return sum * 0.5;
+#undef EV
+}
+
+/* own edge EMFs with the block-face edges replaced by their corrected values */
+static void corrected_edges(const orc_mesh *m, int b, scratch *s) {
+  memcpy(s->e1, m->e1 + (long)b * m->ne1, sizeof(double) * m->ne1);
+  memcpy(s->e2, m->e2 + (long)b * m->ne2, sizeof(double) * m->ne2);
+  memcpy(s->e3, m->e3 + (long)b * m->ne3, sizeof(double) * m->ne3);
+  int is = m->is, ie = m->ie, js = m->js, je = m->je, ks = m->ks, ke = m->ke;
+  for (int k = ks; k <= ke + 1; ++k)
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie; ++i)
+        if (j == js || j == je + 1 || k == ks || k == ke + 1)
+          s->e1[E1IDX(m, k, j, i)] = emf_corrected(m, b, 0, k, j, i);
+  for (int k = ks; k <= ke + 1; ++k)
+    for (int j = js; j <= je; ++j)
+      for (int i = is; i <= ie + 1; ++i)
+        if (i == is || i == ie + 1 || k == ks || k == ke + 1)
+          s->e2[E2IDX(m, k, j, i)] = emf_corrected(m, b, 1, k, j, i);
+  for (int k = ks; k <= ke; ++k)
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie + 1; ++i)
+        if (i == is || i == ie + 1 || j == js || j == je + 1)
+          s->e3[E3IDX(m, k, j, i)] = emf_corrected(m, b, 2, k, j, i);
+}
+
+/* ------------------------------------------------------------------------------------
+ * Hydro::AddFluxDivergence, add_flux_divergence.cpp:39-96 (Cartesian areas and volumes,
+ * coordinates.cpp:448-548)
+ */
+static void add_flux_divergence(orc_mesh *m, int b, double wght, double *u, scratch *s) {
+  const double *dx1f = m->dx1f + (long)b * m->nc1, *dx2f = m->dx2f + (long)b * m->nc2,
+               *dx3f = m->dx3f + (long)b * m->nc3;
+  long n1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1), n2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1,
+       n3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  for (int k = m->ks; k <= m->ke; ++k)
+    for (int j = m->js; j <= m->je; ++j)
+      for (int i = m->is; i <= m->ie; ++i) {
+        double x1area = dx2f[j] * dx3f[k];
+        double x2area = dx1f[i] * dx3f[k];
+        double x3area = dx1f[i] * dx2f[j];
+        double vol = dx1f[i] * dx2f[j] * dx3f[k];
+        for (int n = 0; n < NHYDRO; ++n) {
+          double dflx = (x1area * s->flx1[n * n1 + F1IDX(m, k, j, i + 1)] -
+                         x1area * s->flx1[n * n1 + F1IDX(m, k, j, i)]);
+          dflx += (x2area * s->flx2[n * n2 + F2IDX(m, k, j + 1, i)] -
+                   x2area * s->flx2[n * n2 + F2IDX(m, k, j, i)]);
+          dflx += (x3area * s->flx3[n * n3 + F3IDX(m, k + 1, j, i)] -
+                   x3area * s->flx3[n * n3 + F3IDX(m, k, j, i)]);
+          u[CIDX(m, n, k, j, i)] -= wght * dflx / vol;
+        }
+      }
+}
+
+/* Field::CT, ct.cpp:31-116 (Cartesian edge lengths and areas) */
+static void ct_update(orc_mesh *m, int b, double wght, double *b1, double *b2, double *b3,
+                      scratch *s) {
+  const double *dx1f = m->dx1f + (long)b * m->nc1, *dx2f = m->dx2f + (long)b * m->nc2,
+               *dx3f = m->dx3f + (long)b * m->nc3;
+  int is = m->is, ie = m->ie, js = m->js, je = m->je, ks = m->ks, ke = m->ke;
+  for (int k = ks; k <= ke; ++k)
+    for (int j = js; j <= je; ++j)
+      for (int i = is; i <= ie + 1; ++i) {
+        double area = dx2f[j] * dx3f[k];
+        double len = dx3f[k], len_p1 = dx3f[k];
+        double *bf = &b1[F1IDX(m, k, j, i)];
+        *bf -= (wght / area) * (len_p1 * s->e3[E3IDX(m, k, j + 1, i)] -
+                                len * s->e3[E3IDX(m, k, j, i)]);
+        len = dx2f[j]; len_p1 = dx2f[j];
+        *bf += (wght / area) * (len_p1 * s->e2[E2IDX(m, k + 1, j, i)] -
+                                len * s->e2[E2IDX(m, k, j, i)]);
+      }
+  for (int k = ks; k <= ke; ++k)
+    for (int j = js; j <= je + 1; ++j)
+      for (int i = is; i <= ie; ++i) {
+        double area = dx1f[i] * dx3f[k];
+        double len = dx3f[k], len_ip1 = dx3f[k];
+        double *bf = &b2[F2IDX(m, k, j, i)];
+        *bf += (wght / area) * (len_ip1 * s->e3[E3IDX(m, k, j, i + 1)] -
+                                len * s->e3[E3IDX(m, k, j, i)]);
+        len = dx1f[i];
+        double len_p1 = dx1f[i];
+        *bf -= (wght / area) * (len_p1 * s->e1[E1IDX(m, k + 1, j, i)] -
+                                len * s->e1[E1IDX(m, k, j, i)]);
+      }
+  for (int k = ks; k <= ke + 1; ++k)
+    for (int j = js; j <= je; ++j)
+      for (int i = is; i <= ie; ++i) {
+        double area = dx1f[i] * dx2f[j];
+        double len = dx2f[j], len_ip1 = dx2f[j];
+        double *bf = &b3[F3IDX(m, k, j, i)];
+        *bf -= (wght / area) * (len_ip1 * s->e2[E2IDX(m, k, j, i + 1)] -
+                                len * s->e2[E2IDX(m, k, j, i)]);
+        len = dx1f[i];
+        double len_p1 = dx1f[i];
+        *bf += (wght / area) * (len_p1 * s->e1[E1IDX(m, k, j + 1, i)] -
+                                len * s->e1[E1IDX(m, k, j, i)]);
+      }
+}
+
+/* ------------------------------------------------------------------------------------
+ * Field::CalculateCellCenteredField (field.cpp:112-180, uniform branch) and
+ * EquationOfState::ConservedToPrimitive (adiabatic_mhd.cpp:41-90) over [kl,ku]x...
+ */
+static void cell_centered_field(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl,
+                                int ku) {
+  const double *b1 = m->b1 + (long)b * m->nf1, *b2 = m->b2 + (long)b * m->nf2,
+               *b3 = m->b3 + (long)b * m->nf3;
+  double *bcc = m->bcc + (long)b * 3 * m->ncell;
+  for (int k = kl; k <= ku; ++k)
+    for (int j = jl; j <= ju; ++j)
+      for (int i = il; i <= iu; ++i) {
+        double lw = 0.5, rw = 0.5;
+        bcc[CIDX(m, 0, k, j, i)] = lw * b1[F1IDX(m, k, j, i)] + rw * b1[F1IDX(m, k, j, i + 1)];
+        bcc[CIDX(m, 1, k, j, i)] = lw * b2[F2IDX(m, k, j, i)] + rw * b2[F2IDX(m, k, j + 1, i)];
+        bcc[CIDX(m, 2, k, j, i)] = lw * b3[F3IDX(m, k, j, i)] + rw * b3[F3IDX(m, k + 1, j, i)];
+      }
+}
+
+static long sr_c2p_block(orc_mesh *m, int b, double *u, double *prim, int il, int iu,
+                         int jl, int ju, int kl, int ku);
+
+static long con2prim(orc_mesh *m, int b, double *u, double *prim) {
+  int il = 0, iu = m->nc1 - 1, jl = 0, ju = m->nc2 - 1, kl = 0, ku = m->nc3 - 1;
+  cell_centered_field(m, b, il, iu, jl, ju, kl, ku);
+  if (m->p.relativistic) return sr_c2p_block(m, b, u, prim, il, iu, jl, ju, kl, ku);
+  const double *bcc = m->bcc + (long)b * 3 * m->ncell;
+  double gm1 = m->p.gamma - 1.0;
+  double dfl = m->p.dfloor, pfl = m->p.pfloor;
+  long nc = m->ncell;
+  for (int k = kl; k <= ku; ++k)
+    for (int j = jl; j <= ju; ++j)
+      for (int i = il; i <= iu; ++i) {
+        long c = CIDX(m, 0, k, j, i);
+        double *u_d = &u[c], *u_e = &u[c + 4 * nc];
+        double u_m1 = u[c + nc], u_m2 = u[c + 2 * nc], u_m3 = u[c + 3 * nc];
+        *u_d = (*u_d > dfl) ? *u_d : dfl;
+        prim[c] = *u_d;
+        double di = 1.0 / *u_d;
+        prim[c + nc] = u_m1 * di;
+        prim[c + 2 * nc] = u_m2 * di;
+        prim[c + 3 * nc] = u_m3 * di;
+        double bcc1 = bcc[c], bcc2 = bcc[c + nc], bcc3 = bcc[c + 2 * nc];
+        double pb = 0.5 * (SQR(bcc1) + SQR(bcc2) + SQR(bcc3));
+        double e_k = 0.5 * di * (SQR(u_m1) + SQR(u_m2) + SQR(u_m3));
+        double w_p = gm1 * (*u_e - e_k - pb);
+        *u_e = (w_p > pfl) ? *u_e : ((pfl / gm1) + e_k + pb);
+        prim[c + 4 * nc] = (w_p > pfl) ? w_p : pfl;
+      }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------------------
+ * SR-MHD conserved->primitive (eos/adiabatic_mhd_sr.cpp) — filled in with the SR path.
+ */
+static long sr_c2p_block(orc_mesh *m, int b, double *u, double *prim, int il, int iu,
+                         int jl, int ju, int kl, int ku) {
+  (void)m; (void)b; (void)u; (void)prim; (void)il; (void)iu; (void)jl; (void)ju; (void)kl;
+  (void)ku;
+  return -1;
+}
+
+void orc_sr_c2p_cells(long n, double gamma, double pgas_floor, const double *cons,
+                      const double *bcc, const double *pgas_guess, double *prim,
+                      int *iterations) {
+  (void)gamma; (void)pgas_floor; (void)cons; (void)bcc; (void)pgas_guess; (void)prim;
+  for (long c = 0; c < n; ++c) iterations[c] = -1;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Hydro::NewBlockTimeStep, new_blockdt.cpp:45-230 (MHD branch :80-103)
+ */
+static double new_block_dt(orc_mesh *m, int b) {
+  const double *w = m->w + (long)b * NHYDRO * m->ncell;
+  const double *bcc = m->bcc + (long)b * 3 * m->ncell;
+  const double *b1 = m->b1 + (long)b * m->nf1, *b2 = m->b2 + (long)b * m->nf2,
+               *b3 = m->b3 + (long)b * m->nf3;
+  const double *dx1f = m->dx1f + (long)b * m->nc1, *dx2f = m->dx2f + (long)b * m->nc2,
+               *dx3f = m->dx3f + (long)b * m->nc3;
+  long nc = m->ncell;
+  double min_dt = DBL_MAX;
+  const double cspeed = 0.0;
+  for (int k = m->ks; k <= m->ke; ++k)
+    for (int j = m->js; j <= m->je; ++j)
+      for (int i = m->is; i <= m->ie; ++i) {
+        double dt1 = dx1f[i], dt2 = dx2f[j], dt3 = dx3f[k];
+        if (!m->p.relativistic) {
+          long c = CIDX(m, 0, k, j, i);
+          double wi[NWAVE];
+          wi[IDN] = w[c]; wi[IVX] = w[c + nc]; wi[IVY] = w[c + 2 * nc];
+          wi[IVZ] = w[c + 3 * nc]; wi[IPR] = w[c + 4 * nc];
+          double bc1 = bcc[c], bc2 = bcc[c + nc], bc3 = bcc[c + 2 * nc];
+          double bx = bc1 + fabs(b1[F1IDX(m, k, j, i)] - bc1);
+          wi[IBY] = bc2; wi[IBZ] = bc3;
+          double cf = fast_ms(m->p.gamma, wi, bx);
+          double speed = smax(cspeed, (fabs(wi[IVX]) + cf));
+          dt1 /= (speed);
+          wi[IBY] = bc3; wi[IBZ] = bc1;
+          bx = bc2 + fabs(b2[F2IDX(m, k, j, i)] - bc2);
+          cf = fast_ms(m->p.gamma, wi, bx);
+          speed = smax(cspeed, (fabs(wi[IVY]) + cf));
+          dt2 /= (speed);
+          wi[IBY] = bc1; wi[IBZ] = bc2;
+          bx = bc3 + fabs(b3[F3IDX(m, k, j, i)] - bc3);
+          cf = fast_ms(m->p.gamma, wi, bx);
+          speed = smax(cspeed, (fabs(wi[IVZ]) + cf));
+          dt3 /= (speed);
+        }
+        min_dt = smin(min_dt, dt1);
+        min_dt = smin(min_dt, dt2);
+        min_dt = smin(min_dt, dt3);
+      }
+  return min_dt * m->p.cfl_number;
+}
+
+/* Mesh::NewTimeStep, mesh.cpp:1236-1281 */
+static void new_time_step(orc_mesh *m, const double *block_dt) {
+  double dt = 2.0 * m->dt;
+  for (int b = 0; b < m->nb; ++b) dt = smin(dt, block_dt[b]);
+  if (m->time < m->p.tlim && (m->p.tlim - m->time) < dt) dt = m->p.tlim - m->time;
+  m->dt = dt;
+}
+
+/* ------------------------------------------------------------------------------------
+ * Same-level periodic ghost exchange: the value every ghost receives from its neighbour
+ * (bvals_cc.cpp:287-430; face fields bvals_fc.cpp:344-397 and the matching set routine).
+ * For face fields the block's own faces in the normal direction are [is, ie+1]; faces
+ * outside that range come from the neighbour, as in LoadBoundaryBufferSameLevel.
+ */
+/* returns 1 when idx lies outside the block's own range and was mapped to the
+ * neighbour (which is the block itself when the mesh has one block along the axis) */
+static int locate(int own_lo, int own_hi, int n, int nb, int lx, int idx, int *nlx,
+                  int *nidx) {
+  if (idx < own_lo) { *nlx = (lx - 1 + nb) % nb; *nidx = idx + n; return 1; }
+  if (idx > own_hi) { *nlx = (lx + 1) % nb; *nidx = idx - n; return 1; }
+  *nlx = lx; *nidx = idx;
+  return 0;
+}
+
+static void exchange(orc_mesh *m, double *cc, int nvar, double *f1, double *f2, double *f3) {
+  int nbx1 = m->p.nbx1, nbx2 = m->p.nbx2, nbx3 = m->p.nbx3;
+  int nx1 = m->p.nx1, nx2 = m->p.nx2, nx3 = m->p.nx3;
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < m->nb; ++b) {
+    int lx1 = b % nbx1, lx2 = (b / nbx1) % nbx2, lx3 = b / (nbx1 * nbx2);
+    for (int k = 0; k < m->nc3; ++k)
+      for (int j = 0; j < m->nc2; ++j)
+        for (int i = 0; i < m->nc1 + 1; ++i) {
+          int a1, a2, a3, si, sj, sk;
+          int mv = locate(m->ks, m->ke, nx3, nbx3, lx3, k, &a3, &sk);
+          mv |= locate(m->js, m->je, nx2, nbx2, lx2, j, &a2, &sj);
+          int sb;
+          if (cc && i < m->nc1) {
+            if (locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si) | mv) {
+              sb = (a3 * nbx2 + a2) * nbx1 + a1;
+              for (int n = 0; n < nvar; ++n)
+                cc[(long)b * nvar * m->ncell + CIDX(m, n, k, j, i)] =
+                    cc[(long)sb * nvar * m->ncell + CIDX(m, n, sk, sj, si)];
+            }
+          }
+          if (f1) {
+            if (locate(m->is, m->ie + 1, nx1, nbx1, lx1, i, &a1, &si) | mv) {
+              sb = (a3 * nbx2 + a2) * nbx1 + a1;
+              f1[(long)b * m->nf1 + F1IDX(m, k, j, i)] =
+                  f1[(long)sb * m->nf1 + F1IDX(m, sk, sj, si)];
+            }
+          }
+        }
+    if (f2)
+      for (int k = 0; k < m->nc3; ++k)
+        for (int j = 0; j < m->nc2 + 1; ++j)
+          for (int i = 0; i < m->nc1; ++i) {
+            int a1, a2, a3, si, sj, sk;
+            int mv = locate(m->ks, m->ke, nx3, nbx3, lx3, k, &a3, &sk);
+            mv |= locate(m->js, m->je + 1, nx2, nbx2, lx2, j, &a2, &sj);
+            mv |= locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si);
+            if (mv) {
+              int sb = (a3 * nbx2 + a2) * nbx1 + a1;
+              f2[(long)b * m->nf2 + F2IDX(m, k, j, i)] =
+                  f2[(long)sb * m->nf2 + F2IDX(m, sk, sj, si)];
+            }
+          }
+    if (f3)
+      for (int k = 0; k < m->nc3 + 1; ++k)
+        for (int j = 0; j < m->nc2; ++j)
+          for (int i = 0; i < m->nc1; ++i) {
+            int a1, a2, a3, si, sj, sk;
+            int mv = locate(m->ks, m->ke + 1, nx3, nbx3, lx3, k, &a3, &sk);
+            mv |= locate(m->js, m->je, nx2, nbx2, lx2, j, &a2, &sj);
+            mv |= locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si);
+            if (mv) {
+              int sb = (a3 * nbx2 + a2) * nbx1 + a1;
+              f3[(long)b * m->nf3 + F3IDX(m, k, j, i)] =
+                  f3[(long)sb * m->nf3 + F3IDX(m, sk, sj, si)];
+            }
+          }
+  }
+}
+
+/* ------------------------------------------------------------------------------------
+ * mesh life cycle
+ */
+orc_mesh *orc_create(const orc_params *p, const double *x1f, const double *dx1f,
+                     const double *x2f, const double *dx2f, const double *x3f,
+                     const double *dx3f) {
+  orc_mesh *m = calloc(1, sizeof(orc_mesh));
+  m->p = *p;
+  m->nb = p->nbx1 * p->nbx2 * p->nbx3;
+  m->nc1 = p->nx1 + 2 * p->ng; m->nc2 = p->nx2 + 2 * p->ng; m->nc3 = p->nx3 + 2 * p->ng;
+  m->is = p->ng; m->ie = p->ng + p->nx1 - 1;
+  m->js = p->ng; m->je = p->ng + p->nx2 - 1;
+  m->ks = p->ng; m->ke = p->ng + p->nx3 - 1;
+  m->ncell = (long)m->nc1 * m->nc2 * m->nc3;
+  m->nf1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1);
+  m->nf2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1;
+  m->nf3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  m->ne1 = (long)(m->nc3 + 1) * (m->nc2 + 1) * m->nc1;
+  m->ne2 = (long)(m->nc3 + 1) * m->nc2 * (m->nc1 + 1);
+  m->ne3 = (long)m->nc3 * (m->nc2 + 1) * (m->nc1 + 1);
+  long nb = m->nb;
+  m->e1 = calloc(nb * m->ne1, sizeof(double));
+  m->e2 = calloc(nb * m->ne2, sizeof(double));
+  m->e3 = calloc(nb * m->ne3, sizeof(double));
+  m->u = calloc(nb * NHYDRO * m->ncell, sizeof(double));
+  m->u1 = calloc(nb * NHYDRO * m->ncell, sizeof(double));
+  m->w = calloc(nb * NHYDRO * m->ncell, sizeof(double));
+  m->w1 = calloc(nb * NHYDRO * m->ncell, sizeof(double));
+  m->bcc = calloc(nb * 3 * m->ncell, sizeof(double));
+  m->b1 = calloc(nb * m->nf1, sizeof(double));
+  m->b2 = calloc(nb * m->nf2, sizeof(double));
+  m->b3 = calloc(nb * m->nf3, sizeof(double));
+  m->bb1 = calloc(nb * m->nf1, sizeof(double));
+  m->bb2 = calloc(nb * m->nf2, sizeof(double));
+  m->bb3 = calloc(nb * m->nf3, sizeof(double));
+  m->x1f = malloc(sizeof(double) * nb * (m->nc1 + 1));
+  m->x2f = malloc(sizeof(double) * nb * (m->nc2 + 1));
+  m->x3f = malloc(sizeof(double) * nb * (m->nc3 + 1));
+  m->dx1f = malloc(sizeof(double) * nb * m->nc1);
+  m->dx2f = malloc(sizeof(double) * nb * m->nc2);
+  m->dx3f = malloc(sizeof(double) * nb * m->nc3);
+  m->x1v = malloc(sizeof(double) * nb * m->nc1);
+  m->x2v = malloc(sizeof(double) * nb * m->nc2);
+  m->x3v = malloc(sizeof(double) * nb * m->nc3);
+  memcpy(m->x1f, x1f, sizeof(double) * nb * (m->nc1 + 1));
+  memcpy(m->x2f, x2f, sizeof(double) * nb * (m->nc2 + 1));
+  memcpy(m->x3f, x3f, sizeof(double) * nb * (m->nc3 + 1));
+  memcpy(m->dx1f, dx1f, sizeof(double) * nb * m->nc1);
+  memcpy(m->dx2f, dx2f, sizeof(double) * nb * m->nc2);
+  memcpy(m->dx3f, dx3f, sizeof(double) * nb * m->nc3);
+  /* x?v = 0.5*(x?f(i+1) + x?f(i)), cartesian.cpp:28-32 */
+  for (long b = 0; b < nb; ++b) {
+    for (int i = 0; i < m->nc1; ++i)
+      m->x1v[b * m->nc1 + i] = 0.5 * (m->x1f[b * (m->nc1 + 1) + i + 1] +
+                                      m->x1f[b * (m->nc1 + 1) + i]);
+    for (int j = 0; j < m->nc2; ++j)
+      m->x2v[b * m->nc2 + j] = 0.5 * (m->x2f[b * (m->nc2 + 1) + j + 1] +
+                                      m->x2f[b * (m->nc2 + 1) + j]);
+    for (int k = 0; k < m->nc3; ++k)
+      m->x3v[b * m->nc3 + k] = 0.5 * (m->x3f[b * (m->nc3 + 1) + k + 1] +
+                                      m->x3f[b * (m->nc3 + 1) + k]);
+  }
+  m->dt = DBL_MAX;  /* mesh.cpp:100 */
+  m->time = 0.0;
+  return m;
+}
+
+void orc_destroy(orc_mesh *m) {
+  if (!m) return;
+  free(m->u); free(m->u1); free(m->w); free(m->w1); free(m->bcc); free(m->b1);
+  free(m->b2); free(m->b3); free(m->bb1); free(m->bb2); free(m->bb3); free(m->x1f);
+  free(m->x2f); free(m->x3f); free(m->dx1f); free(m->dx2f); free(m->dx3f);
+  free(m->x1v); free(m->x2v); free(m->x3v); free(m->e1); free(m->e2); free(m->e3);
+  free(m);
+}
+
+int orc_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+void orc_set_state(orc_mesh *m, const double *u, const double *b1, const double *b2,
+                   const double *b3) {
+  memcpy(m->u, u, sizeof(double) * m->nb * NHYDRO * m->ncell);
+  memcpy(m->b1, b1, sizeof(double) * m->nb * m->nf1);
+  memcpy(m->b2, b2, sizeof(double) * m->nb * m->nf2);
+  memcpy(m->b3, b3, sizeof(double) * m->nb * m->nf3);
+}
+
+void orc_set_prim(orc_mesh *m, const double *w) {
+  memcpy(m->w, w, sizeof(double) * m->nb * NHYDRO * m->ncell);
+  memcpy(m->w1, w, sizeof(double) * m->nb * NHYDRO * m->ncell);
+}
+
+void orc_get_state(const orc_mesh *m, double *u, double *b1, double *b2, double *b3) {
+  if (u) memcpy(u, m->u, sizeof(double) * m->nb * NHYDRO * m->ncell);
+  if (b1) memcpy(b1, m->b1, sizeof(double) * m->nb * m->nf1);
+  if (b2) memcpy(b2, m->b2, sizeof(double) * m->nb * m->nf2);
+  if (b3) memcpy(b3, m->b3, sizeof(double) * m->nb * m->nf3);
+}
+
+void orc_get_prim(const orc_mesh *m, double *w, double *bcc) {
+  if (w) memcpy(w, m->w, sizeof(double) * m->nb * NHYDRO * m->ncell);
+  if (bcc) memcpy(bcc, m->bcc, sizeof(double) * m->nb * 3 * m->ncell);
+}
+
+double orc_get_dt(const orc_mesh *m) { return m->dt; }
+double orc_get_time(const orc_mesh *m) { return m->time; }
+void orc_set_dt(orc_mesh *m, double dt) { m->dt = dt; }
+long orc_c2p_failures(const orc_mesh *m) { return m->c2p_fail; }
+
+static void all_con2prim(orc_mesh *m, double *wout) {
+  long fails = 0;
+#pragma omp parallel for schedule(static) reduction(+ : fails)
+  for (int b = 0; b < m->nb; ++b)
+    fails += con2prim(m, b, m->u + (long)b * NHYDRO * m->ncell,
+                      wout + (long)b * NHYDRO * m->ncell);
+  m->c2p_fail = fails;
+}
+
+static void all_new_dt(orc_mesh *m) {
+  double *bdt = malloc(sizeof(double) * m->nb);
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < m->nb; ++b) bdt[b] = new_block_dt(m, b);
+  new_time_step(m, bdt);
+  free(bdt);
+}
+
+void orc_initialize(orc_mesh *m) {
+  /* Mesh::Initialize: boundaries (mesh.cpp:1698-1725), W(U) into w over the whole block
+   * (mesh.cpp:1833), NewBlockTimeStep + NewTimeStep (mesh.cpp:1959-1964) */
+  exchange(m, m->u, NHYDRO, m->b1, m->b2, m->b3);
+  all_con2prim(m, m->w);
+  all_new_dt(m);
+}
+
+#define SWAP(a, b) do { double *t_ = (a); (a) = (b); (b) = t_; } while (0)
+
+/* one VL2 stage of TimeIntegratorTaskList for MHD (time_integrator.cpp:1606-2318):
+ * StartupTaskList zeroing, CalculateHydroFlux (DC on stage 1), CalculateEMF, EMF
+ * averaging, IntegrateHydro/IntegrateField with the register swaps, ghost exchange,
+ * Primitives (W(U) into w1 then swap), NewBlockTimeStep on the last stage. */
+void orc_stage(orc_mesh *m, int stage) {
+  const double beta = (stage == 1) ? 0.5 : 1.0;      /* time_integrator.cpp:216-217 */
+  const double delta = (stage == 1) ? 1.0 : 0.0;     /* :228-236 */
+  const int order = (stage == 1) ? 1 : m->p.xorder;  /* :1700-1703 */
+  long nb = m->nb;
+  if (stage == 1) { /* StartupTaskList, :1606-1625 */
+    memset(m->u1, 0, sizeof(double) * nb * NHYDRO * m->ncell);
+    memset(m->bb1, 0, sizeof(double) * nb * m->nf1);
+    memset(m->bb2, 0, sizeof(double) * nb * m->nf2);
+    memset(m->bb3, 0, sizeof(double) * nb * m->nf3);
+  }
+#pragma omp parallel
+  {
+    scratch s;
+    scratch_alloc(m, &s);
+    /* phase A: fluxes, corner EMFs, hydro register average + flux divergence */
+#pragma omp for schedule(dynamic, 1)
+    for (int b = 0; b < m->nb; ++b) {
+      calculate_fluxes(m, b, order, &s);
+      corner_e(m, b, &s);
+      double *u = m->u + (long)b * NHYDRO * m->ncell;
+      double *u1 = m->u1 + (long)b * NHYDRO * m->ncell;
+      /* WeightedAve(u1, u, ..., {1, delta, 0, 0, 0}), weighted_ave.cpp:35-95 */
+      if (delta != 0.0)
+        for (int n = 0; n < NHYDRO; ++n)
+          for (int k = m->ks; k <= m->ke; ++k)
+            for (int j = m->js; j <= m->je; ++j)
+              for (int i = m->is; i <= m->ie; ++i)
+                u1[CIDX(m, n, k, j, i)] += delta * u[CIDX(m, n, k, j, i)];
+      /* gamma = (0, 1, 0): the registers swap (time_integrator.cpp:1815-1817); the
+       * pointer swap happens after the loops, so the register updated here is u1 */
+      add_flux_divergence(m, b, beta * m->dt, u1, &s);
+    }
+    /* phase B: EMF correction (needs every block's edges), field registers + CT */
+#pragma omp for schedule(dynamic, 1)
+    for (int b = 0; b < m->nb; ++b) {
+      double *f[3] = {m->bb1 + b * m->nf1, m->bb2 + b * m->nf2, m->bb3 + b * m->nf3};
+      const double *g[3] = {m->b1 + b * m->nf1, m->b2 + b * m->nf2, m->b3 + b * m->nf3};
+      if (delta != 0.0) { /* WeightedAve for FaceField, weighted_ave.cpp:360-420 */
+        for (int k = m->ks; k <= m->ke; ++k)
+          for (int j = m->js; j <= m->je; ++j)
+            for (int i = m->is; i <= m->ie + 1; ++i)
+              f[0][F1IDX(m, k, j, i)] += delta * g[0][F1IDX(m, k, j, i)];
+        for (int k = m->ks; k <= m->ke; ++k)
+          for (int j = m->js; j <= m->je + 1; ++j)
+            for (int i = m->is; i <= m->ie; ++i)
+              f[1][F2IDX(m, k, j, i)] += delta * g[1][F2IDX(m, k, j, i)];
+        for (int k = m->ks; k <= m->ke + 1; ++k)
+          for (int j = m->js; j <= m->je; ++j)
+            for (int i = m->is; i <= m->ie; ++i)
+              f[2][F3IDX(m, k, j, i)] += delta * g[2][F3IDX(m, k, j, i)];
+      }
+      corrected_edges(m, b, &s);
+      ct_update(m, b, beta * m->dt, f[0], f[1], f[2], &s);
+    }
+    scratch_free(&s);
+  }
+  SWAP(m->u, m->u1);
+  SWAP(m->b1, m->bb1);
+  SWAP(m->b2, m->bb2);
+  SWAP(m->b3, m->bb3);
+  exchange(m, m->u, NHYDRO, m->b1, m->b2, m->b3);
+  all_con2prim(m, m->w1);  /* ConservedToPrimitive(u, w, b, w1, ...) (:2221-2223) */
+  SWAP(m->w, m->w1);       /* :2269 */
+}
+
+void orc_cycle(orc_mesh *m) {
+  orc_stage(m, 1);
+  orc_stage(m, 2);
+  m->time += m->dt;  /* main.cpp:535 */
+  all_new_dt(m);     /* NewBlockTimeStep (last stage) + Mesh::NewTimeStep */
+}

@@ -1,0 +1,76 @@
+/* CPU oracle for the Athena++ MHD stage update — TEST INFRASTRUCTURE, not the product.
+ *
+ * A plain-C, FP64 restatement of the reference's algorithm for the hot path
+ * (reconstruction, Riemann solvers, flux divergence, corner EMF + constrained transport,
+ * conserved->primitive, CFL time step, same-level ghost exchange, the VL2 stage
+ * sequence).  Each routine in athena_oracle.c cites the reference file:line it follows.
+ * It keeps the reference's floating-point association term for term so that its
+ * results can be compared bit for bit with the reference binary built by
+ * oracle/build_ref.py, and it is the checker for the CUDA path in tests/, in
+ * __graft_entry__.smoke() and in bench.py's CPU-baseline leg.  Nothing in the
+ * athena_gb300 package links or calls it.
+ *
+ * Data layout: every MeshBlock keeps the reference's AthenaArray layout
+ * (athena_arrays.hpp:140-143, last index fastest, ghosts included); blocks are stored
+ * in lexicographic order b = (lx3*nbx2 + lx2)*nbx1 + lx1.  Only a uniform, periodic,
+ * single-level 3-D mesh is supported.
+ */
+#ifndef ATHENA_ORACLE_H_
+#define ATHENA_ORACLE_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int nbx1, nbx2, nbx3;   /* MeshBlocks per direction */
+  int nx1, nx2, nx3;      /* interior cells per MeshBlock */
+  int ng;                 /* ghost layers (NGHOST) */
+  int xorder;             /* 2 = PLM, 3 = PPM in the second VL2 stage */
+  int rsolver;            /* 0 = HLLD, 1 = HLLE */
+  int relativistic;       /* 0 = Newtonian adiabatic MHD, 1 = special relativistic */
+  double gamma, dfloor, pfloor, cfl_number, tlim;
+  double sigma_max, beta_min, gamma_max; /* SR floors (adiabatic_mhd_sr.cpp:46-48) */
+} orc_params;
+
+typedef struct orc_mesh orc_mesh;
+
+/* x?f: per block, nc?+1 face coordinates; dx?f: per block, nc? face spacings, exactly
+ * as the reference's Coordinates holds them (coordinates.cpp:92-146). */
+orc_mesh *orc_create(const orc_params *p, const double *x1f, const double *dx1f,
+                     const double *x2f, const double *dx2f, const double *x3f,
+                     const double *dx3f);
+void orc_destroy(orc_mesh *m);
+int orc_num_threads(int n);
+
+/* state I/O, whole-mesh arrays in block order (ghosts included) */
+void orc_set_state(orc_mesh *m, const double *u, const double *b1, const double *b2,
+                   const double *b3);
+void orc_set_prim(orc_mesh *m, const double *w);  /* SR: initial W and NH guess */
+void orc_get_state(const orc_mesh *m, double *u, double *b1, double *b2, double *b3);
+void orc_get_prim(const orc_mesh *m, double *w, double *bcc);
+double orc_get_dt(const orc_mesh *m);
+double orc_get_time(const orc_mesh *m);
+void orc_set_dt(orc_mesh *m, double dt);
+
+/* Mesh::Initialize tail (mesh.cpp:1698-1833,1962): ghost exchange, W(U) on the whole
+ * block, first time step. */
+void orc_initialize(orc_mesh *m);
+/* one VL2 cycle (main.cpp:512-541): both stages, time += dt, NewTimeStep */
+void orc_cycle(orc_mesh *m);
+/* one stage only (for intermediate comparisons); stage = 1 or 2 */
+void orc_stage(orc_mesh *m, int stage);
+/* counts of cells that hit the SR fallback in the last W(U) call */
+long orc_c2p_failures(const orc_mesh *m);
+
+/* per-cell SR conserved->primitive (adiabatic_mhd_sr.cpp:404-522) on independent
+ * cells: cons[n][5] (D, E, M1..M3 in the reference's IDN,IEN,IM1..IM3 slots), bcc[n][3],
+ * guess pgas[n]; out prim[n][5] and iterations[n] (-1 = not converged). */
+void orc_sr_c2p_cells(long n, double gamma, double pgas_floor, const double *cons,
+                      const double *bcc, const double *pgas_guess, double *prim,
+                      int *iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

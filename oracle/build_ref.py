@@ -1,0 +1,161 @@
+"""Build recipe for the reference (Athena++) binaries used to pin the oracle.
+
+Test infrastructure only: nothing in the product imports or runs this.
+
+The reference's own build (``configure.py`` -> ``Makefile``/``src/defs.hpp``) writes
+into its source tree, which is read-only here, so this recipe does the same two steps
+itself without touching the tree:
+
+* it fills the reference's ``src/defs.hpp.in`` template with the macro values that
+  ``configure.py -b --flux=<f> [--nghost=3] [-s]`` would choose (configure.py:451-560)
+  and writes the result to ``oracle/_ref/<variant>/gen/defs.hpp``;
+* it compiles the same source list as ``Makefile.in:29-75`` with ``g++ -O3 -std=c++11``
+  (the flags configure.py uses for g++, configure.py:560-566) straight from the
+  reference's ``src/`` into ``oracle/_ref/<variant>/obj`` and links two executables:
+  ``athena_lw`` (the reference's own ``pgen/linear_wave.cpp``) and ``athena_ic``
+  (``oracle/ref_pgen/load_ic.cpp``), both with ``oracle/ref_pgen/dump_hook.cpp``.
+
+Nothing is copied out of the reference tree; all outputs go under ``oracle/_ref/``.
+Usage: ``python oracle/build_ref.py [variant ...]`` (default: all variants).
+"""
+import glob
+import os
+import re
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+REF = os.environ.get("ATHENA_REF_SRC", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+
+# variant -> (riemann solver, nghost, relativistic)
+VARIANTS = {
+    "mhd_hlld_g2": ("hlld", 2, False),
+    "mhd_hlld_g3": ("hlld", 3, False),
+    "mhd_hlle_g2": ("hlle", 2, False),
+    "mhd_hlle_g3": ("hlle", 3, False),
+    "srmhd_hlle_g2": ("hlle", 2, True),
+}
+
+
+def defs_values(flux, ng, sr):
+    return {
+        "PROBLEM": "linear_wave", "COORDINATE_SYSTEM": "cartesian", "RSOLVER": flux,
+        "EQUATION_OF_STATE": "adiabatic",
+        "CHEMNETWORK_HEADER": "../chemistry/network/chem_network.hpp",
+        "CHEMRADIATION_INTEGRATOR": "none", "GENERAL_EOS": "0", "EOS_TABLE_ENABLED": "0",
+        "NON_BAROTROPIC_EOS": "1", "MAGNETIC_FIELDS_ENABLED": "1", "STS_ENABLED": "0",
+        "SELF_GRAVITY_ENABLED": "0", "CHEMISTRY_ENABLED": "0",
+        "CHEMRADIATION_ENABLED": "0", "NR_RADIATION_ENABLED": "0",
+        "IM_RADIATION_ENABLED": "0", "CR_ENABLED": "0", "CRDIFFUSION_ENABLED": "0",
+        "RELATIVISTIC_DYNAMICS": "1" if sr else "0", "GENERAL_RELATIVITY": "0",
+        "SINGLE_PRECISION_ENABLED": "0", "H5_DOUBLE_PRECISION_ENABLED": "0",
+        "DEBUG_OPTION": "0", "FFT_OPTION": "NO_FFT", "MPI_OPTION": "NOT_MPI_PARALLEL",
+        "OPENMP_OPTION": "NOT_OPENMP_PARALLEL", "HDF5_OPTION": "NO_HDF5OUTPUT",
+        "CVODE_OPTION": "NO_CVODE", "EXCEPTION_HANDLING_OPTION": "ENABLE_EXCEPTIONS",
+        "COMPILER_CHOICE": "g++", "COMPILER_COMMAND": "g++",
+        "COMPILER_FLAGS": "-O3 -std=c++11", "NHYDRO_VARIABLES": "5",
+        "NFIELD_VARIABLES": "3", "NWAVE_VALUE": "7", "NUMBER_PASSIVE_SCALARS": "0",
+        "NUMBER_CHEMICAL_SPECIES": "0", "NUMBER_GHOST_CELLS": str(ng),
+        "NCR_VARIABLES": "0", "NRAD_VARIABLES": "0",
+    }
+
+
+def source_list(flux, sr):
+    s = os.path.join(REF, "src")
+    files = []
+    for d in ["", "bvals", "bvals/cc", "bvals/cc/fft_grav", "bvals/cc/hydro", "bvals/cc/mg",
+              "bvals/cc/nr_radiation", "bvals/fc", "bvals/orbital", "bvals/sixray",
+              "bvals/utils", "chem_rad", "fft", "field", "field/field_diffusion",
+              "gravity", "hydro", "hydro/srcterms", "hydro/hydro_diffusion",
+              "nr_radiation", "nr_radiation/integrators",
+              "nr_radiation/integrators/srcterms", "nr_radiation/implicit", "cr",
+              "cr/integrators", "crdiffusion", "inputs", "mesh", "multigrid",
+              "orbital_advection", "outputs", "reconstruct", "scalars", "task_list",
+              "utils", "units", "chemistry/utils"]:
+        files += sorted(glob.glob(os.path.join(s, d, "*.cpp")))
+    eos = "adiabatic_mhd_sr.cpp" if sr else "adiabatic_mhd.cpp"
+    # configure.py:476-531: hlle/llf/roe get "_mhd", then "_rel" for -s
+    rs = flux + ("_mhd" if flux in ("hlle", "llf", "roe") else "") + \
+        ("_rel" if sr else "") + ".cpp"
+    files += [
+        os.path.join(s, "coordinates/coordinates.cpp"),
+        os.path.join(s, "coordinates/cartesian.cpp"),
+        os.path.join(s, "eos", eos),
+        os.path.join(s, "eos/general/noop.cpp"),  # GENERAL_EOS_FILE (configure.py:462)
+        os.path.join(s, "eos/eos_high_order.cpp"),
+        os.path.join(s, "eos/eos_scalars.cpp"),
+        os.path.join(s, "chemistry/network_wrapper.cpp"),
+        os.path.join(s, "chemistry/network/none.cpp"),
+        os.path.join(s, "chemistry/forward_euler.cpp"),
+        os.path.join(s, "chem_rad/integrators/const.cpp"),
+        os.path.join(s, "hydro/rsolvers/mhd", rs),
+        os.path.join(s, "pgen/default_pgen.cpp"),
+    ]
+    return files
+
+
+def run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+
+
+def build_variant(name, jobs=None):
+    flux, ng, sr = VARIANTS[name]
+    vdir = os.path.join(OUT, name)
+    gen, obj = os.path.join(vdir, "gen"), os.path.join(vdir, "obj")
+    os.makedirs(gen, exist_ok=True)
+    os.makedirs(obj, exist_ok=True)
+    tmpl = open(os.path.join(REF, "src/defs.hpp.in")).read()
+    for k, v in defs_values(flux, ng, sr).items():
+        tmpl = re.sub(r"@%s@" % k, v, tmpl)
+    defs = os.path.join(gen, "defs.hpp")
+    if not os.path.exists(defs) or open(defs).read() != tmpl:
+        with open(defs, "w") as f:
+            f.write(tmpl)
+    # the sources include the configured header as "defs.hpp", "../defs.hpp",
+    # "../../defs.hpp" and "../../../../defs.hpp"; give each form a search directory
+    # that resolves to gen/defs.hpp
+    deep = os.path.join(gen, "a", "b", "c", "d")
+    os.makedirs(deep, exist_ok=True)
+    cxx = ["g++", "-O3", "-std=c++11", "-ffp-contract=off", "-I", gen,
+           "-I", os.path.join(gen, "a"), "-I", os.path.join(gen, "a", "b"), "-I", deep,
+           "-I", os.path.join(REF, "src")]
+    srcs = source_list(flux, sr)
+    extra = {"dump_hook": os.path.join(HERE, "ref_pgen/dump_hook.cpp"),
+             "load_ic": os.path.join(HERE, "ref_pgen/load_ic.cpp"),
+             "linear_wave": os.path.join(REF, "src/pgen/linear_wave.cpp")}
+
+    def objname(src):
+        rel = os.path.relpath(src, REF).replace("/", "_") if src.startswith(REF) else \
+            os.path.basename(src)
+        return os.path.join(obj, rel[:-4] + ".o")
+
+    def compile_one(src):
+        o = objname(src)
+        if os.path.exists(o) and os.path.getmtime(o) >= max(os.path.getmtime(src),
+                                                            os.path.getmtime(defs)):
+            return o
+        run(cxx + ["-c", src, "-o", o])
+        return o
+
+    with ThreadPoolExecutor(jobs or os.cpu_count()) as ex:
+        objs = list(ex.map(compile_one, srcs))
+        eobj = dict(zip(extra, ex.map(compile_one, extra.values())))
+    for exe, pg in (("athena_lw", "linear_wave"), ("athena_ic", "load_ic")):
+        if sr and pg == "linear_wave":
+            continue
+        run(cxx + ["-o", os.path.join(vdir, exe)] + objs + [eobj[pg], eobj["dump_hook"]])
+    return vdir
+
+
+def main(argv):
+    names = argv or list(VARIANTS)
+    for n in names:
+        print("building", n, "->", build_variant(n), flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,136 @@
+"""ctypes wrapper of the C oracle (athena_oracle.c) — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = os.path.join(HERE, "athena_oracle.c")
+
+
+def build(force=False):
+    """Compile liboracle.so (plain C, no FMA contraction, OpenMP over MeshBlocks)."""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "athena_oracle.h"))):
+        return LIB
+    cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
+           "-o", LIB + ".tmp", SRC, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("nbx1", ctypes.c_int), ("nbx2", ctypes.c_int), ("nbx3", ctypes.c_int),
+                ("nx1", ctypes.c_int), ("nx2", ctypes.c_int), ("nx3", ctypes.c_int),
+                ("ng", ctypes.c_int), ("xorder", ctypes.c_int), ("rsolver", ctypes.c_int),
+                ("relativistic", ctypes.c_int), ("gamma", ctypes.c_double),
+                ("dfloor", ctypes.c_double), ("pfloor", ctypes.c_double),
+                ("cfl_number", ctypes.c_double), ("tlim", ctypes.c_double),
+                ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
+                ("gamma_max", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.POINTER(Params)] + [dp] * 6
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_set_state.argtypes = [ctypes.c_void_p, dp, dp, dp, dp]
+        L.orc_set_prim.argtypes = [ctypes.c_void_p, dp]
+        L.orc_get_state.argtypes = [ctypes.c_void_p, dp, dp, dp, dp]
+        L.orc_get_prim.argtypes = [ctypes.c_void_p, dp, dp]
+        L.orc_get_dt.argtypes = [ctypes.c_void_p]
+        L.orc_get_dt.restype = ctypes.c_double
+        L.orc_get_time.argtypes = [ctypes.c_void_p]
+        L.orc_get_time.restype = ctypes.c_double
+        L.orc_set_dt.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_initialize.argtypes = [ctypes.c_void_p]
+        L.orc_cycle.argtypes = [ctypes.c_void_p]
+        L.orc_stage.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_num_threads.argtypes = [ctypes.c_int]
+        L.orc_num_threads.restype = ctypes.c_int
+        L.orc_c2p_failures.argtypes = [ctypes.c_void_p]
+        L.orc_c2p_failures.restype = ctypes.c_long
+        L.orc_sr_c2p_cells.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double,
+                                       dp, dp, dp, dp, ctypes.POINTER(ctypes.c_int)]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class OracleMesh:
+    """The oracle's mesh: the same MeshSpec, parameters and arrays as the CUDA path."""
+
+    def __init__(self, mesh, gamma, xorder=2, rsolver="hlld", cfl=0.3, tlim=1e30,
+                 dfloor=None, pfloor=None, relativistic=False, threads=0):
+        L = lib()
+        import math
+        fmin = float(np.finfo(np.float32).tiny)
+        floor = math.sqrt(1024 * fmin)   # adiabatic_mhd.cpp:29-30
+        self.mesh = mesh
+        self.p = Params(mesh.nb[0], mesh.nb[1], mesh.nb[2], mesh.bx[0], mesh.bx[1],
+                        mesh.bx[2], mesh.ng, xorder, 0 if rsolver == "hlld" else 1,
+                        1 if relativistic else 0, gamma,
+                        floor if dfloor is None else dfloor,
+                        floor if pfloor is None else pfloor, cfl, tlim, 0.0, 0.0, 0.0)
+        self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
+        self.h = L.orc_create(ctypes.byref(self.p), *[_p(c) for c in self.coords])
+        if threads:
+            L.orc_num_threads(threads)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def set_state(self, u, b1, b2, b3):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, b1, b2, b3)]
+        lib().orc_set_state(self.h, *[_p(a) for a in arrs])
+
+    def state(self):
+        m = self.mesh
+        u = np.zeros((m.nblocks, 5) + m.cell_shape)
+        b = [np.zeros((m.nblocks,) + s) for s in m.face_shapes]
+        lib().orc_get_state(self.h, _p(u), *[_p(x) for x in b])
+        return u, b[0], b[1], b[2]
+
+    def prim(self):
+        m = self.mesh
+        w = np.zeros((m.nblocks, 5) + m.cell_shape)
+        bcc = np.zeros((m.nblocks, 3) + m.cell_shape)
+        lib().orc_get_prim(self.h, _p(w), _p(bcc))
+        return w, bcc
+
+    @property
+    def dt(self):
+        return lib().orc_get_dt(self.h)
+
+    @property
+    def time(self):
+        return lib().orc_get_time(self.h)
+
+    def initialize(self):
+        lib().orc_initialize(self.h)
+
+    def cycle(self, n=1):
+        for _ in range(n):
+            lib().orc_cycle(self.h)
+
+    def stage(self, s):
+        lib().orc_stage(self.h, s)

@@ -1,0 +1,90 @@
+"""Run the reference binaries built by oracle/build_ref.py and read their state dumps.
+
+TEST INFRASTRUCTURE ONLY (used to make and check golden fixtures in this container;
+the reference source tree is not present where the GPU tests run).
+"""
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_OUT = os.path.join(HERE, "_ref")
+
+
+def athinput(mesh, gamma, xorder, cfl, nlim, tlim, problem, extra_problem=None,
+             integrator="vl2", num_threads=1):
+    """Text of an athinput file for a uniform periodic mesh described by MeshSpec."""
+    lines = ["<job>", "problem_id = Ref", "<time>", "cfl_number = %r" % cfl,
+             "nlim = %d" % nlim, "tlim = %r" % tlim, "integrator = %s" % integrator,
+             "xorder = %s" % xorder, "ncycle_out = 100000", "<mesh>"]
+    for d, n in enumerate(("1", "2", "3")):
+        lines += ["nx%s = %d" % (n, mesh.nx[d]), "x%smin = %r" % (n, mesh.xmin[d]),
+                  "x%smax = %r" % (n, mesh.xmax[d]), "ix%s_bc = periodic" % n,
+                  "ox%s_bc = periodic" % n]
+    lines += ["num_threads = %d" % num_threads, "refinement = none", "<meshblock>"]
+    for d, n in enumerate(("1", "2", "3")):
+        lines.append("nx%s = %d" % (n, mesh.bx[d]))
+    lines += ["<hydro>", "gamma = %r" % gamma, "iso_sound_speed = 1.0", "<problem>"]
+    for k, v in (problem or {}).items():
+        lines.append("%s = %s" % (k, v))
+    for k, v in (extra_problem or {}).items():
+        lines.append("%s = %s" % (k, v))
+    return "\n".join(lines) + "\n"
+
+
+def read_dump(path, mesh):
+    """Parse one dump written by ref_pgen/dump_hook.cpp into per-block arrays in the
+    lexicographic block order of MeshSpec."""
+    with open(path, "rb") as f:
+        data = f.read()
+    magic, ver, nbl, ncyc = struct.unpack_from("<4i", data, 0)
+    assert magic == 0x41544844 and ver == 1
+    t_after, dt_used = struct.unpack_from("<2d", data, 16)
+    nc1, nc2, nc3, ng, nh = struct.unpack_from("<5i", data, 32)
+    off = 52
+    ncell = nc1 * nc2 * nc3
+    sizes = [nh * ncell, nh * ncell, nc3 * nc2 * (nc1 + 1), nc3 * (nc2 + 1) * nc1,
+             (nc3 + 1) * nc2 * nc1, 3 * ncell]
+    out = {k: np.zeros((mesh.nblocks,) + s) for k, s in (
+        ("u", (5,) + mesh.cell_shape), ("w", (5,) + mesh.cell_shape),
+        ("b1", mesh.face_shapes[0]), ("b2", mesh.face_shapes[1]),
+        ("b3", mesh.face_shapes[2]), ("bcc", (3,) + mesh.cell_shape))}
+    for _ in range(nbl):
+        lx1, lx2, lx3 = struct.unpack_from("<3q", data, off)
+        off += 28
+        b = (lx3 * mesh.nb[1] + lx2) * mesh.nb[0] + lx1
+        for key, sz in zip(("u", "w", "b1", "b2", "b3", "bcc"), sizes):
+            arr = np.frombuffer(data, dtype="<f8", count=sz, offset=off)
+            out[key][b] = arr.reshape(out[key].shape[1:])
+            off += 8 * sz
+    out.update(ncycle=ncyc, time=t_after, dt=dt_used)
+    return out
+
+
+def write_ic(path, kind, q, f1, f2, f3):
+    """Binary initial state read by ref_pgen/load_ic.cpp (global interior arrays)."""
+    nx3, nx2, nx1 = q.shape[1:]
+    with open(path, "wb") as f:
+        f.write(struct.pack("<4i", kind, nx1, nx2, nx3))
+        for a in (q, f1, f2, f3):
+            f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+
+
+def run_reference(variant, exe, text, workdir=None, ic=None):
+    """Run oracle/_ref/<variant>/<exe> on an athinput text; returns (dir, stdout)."""
+    binpath = os.path.join(REF_OUT, variant, exe)
+    if not os.path.exists(binpath):
+        from build_ref import build_variant
+        build_variant(variant)
+    d = workdir or tempfile.mkdtemp(prefix="athref_")
+    if ic is not None:
+        write_ic(os.path.join(d, "ic.bin"), *ic)
+    with open(os.path.join(d, "athinput"), "w") as f:
+        f.write(text)
+    r = subprocess.run([binpath, "-i", "athinput"], cwd=d, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
+    return d, r.stdout

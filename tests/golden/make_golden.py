@@ -1,0 +1,144 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that has the reference source tree (default /root/reference):
+
+    python tests/golden/make_golden.py
+
+It builds the reference (oracle/build_ref.py), runs each case below through the
+unmodified reference code path (the reference's own linear_wave problem generator, or
+the IC-loading generator oracle/ref_pgen/load_ic.cpp for seeded states), and stores the
+inputs and the reference's per-cell outputs:
+
+* ``<case>.npz``: ``ic_*`` (initial state as loaded), ``u``, ``b1``, ``b2``, ``b3``
+  (per-block interiors after ``ncycle`` cycles), ``dt`` (the dt of every cycle), ``time``;
+* ``golden.json``: case parameters, and for the full config-1 linear wave the
+  reference's linearwave-errors.dat line plus a SHA-256 of its final state.
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from athena_gb300.mesh import MeshSpec  # noqa: E402
+from athena_gb300 import pgen  # noqa: E402
+import build_ref  # noqa: E402
+import ref_run  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+GAMMA_LW = 1.666666666666667
+
+CASES = {
+    # name: (variant, mesh args, problem, xorder, cfl, ncycle)
+    "lw_hlld_plm_1blk": ("mhd_hlld_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
+                                         (3.0, 1.5, 1.5)), "linear_wave", 2, 0.3, 3),
+    "lw_hlld_plm_8blk": ("mhd_hlld_g2", ((32, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                         (3.0, 1.5, 1.5)), "linear_wave", 2, 0.3, 2),
+    "turb_hlld_ppm_8blk": ("mhd_hlld_g3", ((16, 16, 16), (2, 2, 2), 3, (0., 0., 0.),
+                                           (1., 1., 1.)), "turbulence", 3, 0.3, 3),
+    "turb_hlle_plm_8blk": ("mhd_hlle_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                           (1., 1., 1.)), "turbulence", 2, 0.3, 3),
+    "turb_hlle_ppm_1blk": ("mhd_hlle_g3", ((16, 16, 16), (1, 1, 1), 3, (0., 0., 0.),
+                                           (1., 1., 1.)), "turbulence", 3, 0.3, 2),
+    "blast_hlld_plm_8blk": ("mhd_hlld_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                            (.5, .5, .5)), "blast", 2, 0.3, 3),
+    "blast_hlle_ppm_8blk": ("mhd_hlle_g3", ((16, 16, 16), (2, 2, 2), 3, (-.5, -.5, -.5),
+                                            (.5, .5, .5)), "blast", 3, 0.3, 3),
+}
+
+
+def global_ic(problem, mesh):
+    if problem == "turbulence":
+        return pgen.turbulence(mesh.nx, seed=7, mach=1.0)
+    if problem == "blast":
+        return pgen.blast(mesh.nx, xmin=mesh.xmin, xmax=mesh.xmax, radius=0.25)
+    raise ValueError(problem)
+
+
+def gamma_of(problem):
+    return GAMMA_LW if problem == "linear_wave" else 5.0 / 3.0
+
+
+def state_hash(u, b1, b2, b3, mesh):
+    ng = mesh.ng
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(mesh.interior(u)).tobytes())
+    for b in (b1, b2, b3):
+        h.update(np.ascontiguousarray(b[:, ng:-ng, ng:-ng, ng:-ng]).tobytes())
+    return h.hexdigest()
+
+
+def run_case(name, spec):
+    variant, margs, problem, xorder, cfl, ncycle = spec
+    mesh = MeshSpec(*margs)
+    gamma = gamma_of(problem)
+    if problem == "linear_wave":
+        lw = pgen.LinearWave(mesh, gamma=GAMMA_LW)
+        u0, b10, b20, b30 = lw.generate()
+        text = ref_run.athinput(mesh, gamma, xorder, cfl, ncycle, 1.0e3, {
+            "compute_error": "false", "wave_flag": 0, "amp": 1.0e-6, "vflow": 0.0})
+        d, _ = ref_run.run_reference(variant, "athena_lw", text)
+        tlim = 1.0e3
+    else:
+        gu, g1, g2, g3 = global_ic(problem, mesh)
+        u0 = mesh.scatter_cells(gu)
+        b10, b20, b30 = mesh.scatter_faces(g1, g2, g3)
+        text = ref_run.athinput(mesh, gamma, xorder, cfl, ncycle, 1.0e3,
+                                {"ic_file": "ic.bin"})
+        d, _ = ref_run.run_reference(variant, "athena_ic", text, ic=(0, gu, g1, g2, g3))
+        tlim = 1.0e3
+    dts = []
+    for c in range(1, ncycle + 1):
+        dump = ref_run.read_dump(os.path.join(d, "dump.%05d.bin" % c), mesh)
+        dts.append(dump["dt"])
+    ng = mesh.ng
+    fi = lambda b: b[:, ng:-ng, ng:-ng, ng:-ng]  # noqa: E731
+    np.savez_compressed(
+        os.path.join(OUT, name + ".npz"),
+        ic_u=mesh.interior(u0), ic_b1=fi(b10), ic_b2=fi(b20), ic_b3=fi(b30),
+        u=mesh.interior(dump["u"]), b1=fi(dump["b1"]), b2=fi(dump["b2"]), b3=fi(dump["b3"]),
+        dt=np.array(dts), time=dump["time"])
+    return {"variant": variant, "nx": mesh.nx, "nb": mesh.nb, "ng": mesh.ng,
+            "xmin": mesh.xmin, "xmax": mesh.xmax, "problem": problem, "xorder": xorder,
+            "rsolver": "hlld" if "hlld" in variant else "hlle", "cfl": cfl,
+            "ncycle": ncycle, "gamma": gamma, "tlim": tlim}
+
+
+def run_config1():
+    """Config 1: 64x32x32 fast wave, one period, compute_error (the reference's own
+    problem generator and error routine)."""
+    mesh = MeshSpec((64, 32, 32), (1, 1, 1), 2, (0., 0., 0.), (3.0, 1.5, 1.5))
+    text = ref_run.athinput(mesh, GAMMA_LW, 2, 0.3, -1, 1.0, {
+        "compute_error": "true", "wave_flag": 0, "amp": 1.0e-6, "vflow": 0.0,
+        "test": "true"})
+    d, out = ref_run.run_reference("mhd_hlld_g2", "athena_lw", text)
+    lines = open(os.path.join(d, "linearwave-errors.dat")).read().strip().splitlines()
+    files = sorted(f for f in os.listdir(d) if f.startswith("dump."))
+    last = ref_run.read_dump(os.path.join(d, files[-1]), mesh)
+    zc = [ln for ln in out.splitlines() if "zone-cycles/cpu_second" in ln]
+    return {"errors_header": lines[0], "errors": lines[-1],
+            "ncycle": last["ncycle"], "time": last["time"],
+            "sha256_final": state_hash(last["u"], last["b1"], last["b2"], last["b3"], mesh),
+            "reference_zone_cycles_per_cpu_second_here": zc[-1] if zc else None}
+
+
+def main():
+    for v in sorted({c[0] for c in CASES.values()}):
+        build_ref.build_variant(v)
+    meta = {"cases": {}}
+    for name, spec in CASES.items():
+        print("case", name, flush=True)
+        meta["cases"][name] = run_case(name, spec)
+    print("config1", flush=True)
+    meta["config1_linear_wave"] = run_config1()
+    with open(os.path.join(OUT, "golden.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

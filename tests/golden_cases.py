@@ -1,0 +1,47 @@
+"""Shared loaders for the golden fixtures made by tests/golden/make_golden.py."""
+import json
+import os
+
+import numpy as np
+
+from athena_gb300.mesh import MeshSpec
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def meta():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        return json.load(f)
+
+
+def case_names():
+    return sorted(meta()["cases"])
+
+
+def load_case(name):
+    c = meta()["cases"][name]
+    mesh = MeshSpec(tuple(c["nx"]), tuple(c["nb"]), c["ng"], tuple(c["xmin"]),
+                    tuple(c["xmax"]))
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ng = mesh.ng
+
+    def pad_cells(a):
+        out = np.zeros((mesh.nblocks, a.shape[1]) + mesh.cell_shape)
+        out[:, :, ng:-ng, ng:-ng, ng:-ng] = a
+        return out
+
+    def pad_faces(a, d):
+        out = np.zeros((mesh.nblocks,) + mesh.face_shapes[d])
+        out[:, ng:-ng, ng:-ng, ng:-ng] = a
+        return out
+
+    ic = (pad_cells(z["ic_u"]), pad_faces(z["ic_b1"], 0), pad_faces(z["ic_b2"], 1),
+          pad_faces(z["ic_b3"], 2))
+    ref = {k: z[k] for k in ("u", "b1", "b2", "b3", "dt")}
+    ref["time"] = float(z["time"])
+    return c, mesh, ic, ref
+
+
+def interior_faces(mesh, b):
+    ng = mesh.ng
+    return b[:, ng:-ng, ng:-ng, ng:-ng]
