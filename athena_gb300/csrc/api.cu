@@ -1,0 +1,480 @@
+// C ABI of the stage update (include/athena_gb300.h).
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "ctx.h"
+
+using namespace athgpu;
+
+namespace {
+thread_local std::string g_err;
+
+athgpu_status fail(athgpu_status code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+athgpu_status cuda_fail(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return ATHGPU_ERR_CUDA;
+}
+#define CK(call)                                          \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+  } while (0)
+
+// double <-> (float hi, float lo) conversions for the FP32 path
+__global__ void split_kernel(const double* __restrict__ src, float* __restrict__ hi,
+                             float* __restrict__ lo, long long n) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double v = src[t];
+  float h = (float)v;
+  hi[t] = h;
+  if (lo) lo[t] = (float)(v - (double)h);
+}
+__global__ void join_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
+                            double* __restrict__ dst, long long n) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  dst[t] = (double)hi[t] + (lo ? (double)lo[t] : 0.0);
+}
+
+long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
+
+void free_all(athgpu_ctx* c) {
+  Registers& r = c->r;
+  void* ptrs[] = {r.u, r.ustar, r.ulo, r.w, r.bcc, r.flx1, r.flx2, r.flx3, r.e3x1, r.e2x1,
+                  r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
+                  r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->nbr,
+                  c->staging};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
+  if (c->cycle_exec) cudaGraphExecDestroy(c->cycle_exec);
+  if (c->cycle_graph) cudaGraphDestroy(c->cycle_graph);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+cudaError_t run_stage_dispatch(athgpu_ctx* c, int stage) {
+  return c->desc.precision == ATHGPU_FP64 ? stage_fp64(c, stage) : stage_fp32(c, stage);
+}
+
+// host copy of a double array into a bulk-precision device register
+athgpu_status upload_bulk(athgpu_ctx* c, const double* h, void* dev, void* lo, long long n) {
+  if (c->real_bytes == 8) {
+    CK(cudaMemcpyAsync(dev, h, n * 8, cudaMemcpyHostToDevice, c->stream));
+  } else {
+    CK(cudaMemcpyAsync(c->staging, h, n * 8, cudaMemcpyHostToDevice, c->stream));
+    split_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(c->staging, (float*)dev,
+                                                                     (float*)lo, n);
+    CK(cudaGetLastError());
+  }
+  return ATHGPU_OK;
+}
+
+athgpu_status download_bulk(athgpu_ctx* c, double* h, const void* dev, const void* lo,
+                            long long n) {
+  if (c->real_bytes == 8) {
+    CK(cudaMemcpyAsync(h, dev, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    join_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(
+        (const float*)dev, (const float*)lo, c->staging, n);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h, c->staging, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  }
+  return ATHGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char* athgpu_last_error(void) { return g_err.c_str(); }
+const char* athgpu_version(void) { return "athena_gb300 0.1 (sm_103a)"; }
+
+athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
+  if (!out || !d) return fail(ATHGPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (d->nbx1 < 1 || d->nbx2 < 1 || d->nbx3 < 1 || d->nx1 < 1 || d->nx2 < 1 || d->nx3 < 1)
+    return fail(ATHGPU_ERR_ARG, "mesh sizes must be positive");
+  if (d->nx2 < 2 || d->nx3 < 2)
+    return fail(ATHGPU_ERR_UNSUPPORTED, "only 3-D meshes (nx2, nx3 > 1) are supported");
+  if (d->xorder < 1 || d->xorder > 3)
+    return fail(ATHGPU_ERR_UNSUPPORTED, "xorder must be 1, 2 or 3");
+  const int need_ng = d->xorder == 3 ? 3 : 2;
+  if (d->nghost < need_ng)
+    return fail(ATHGPU_ERR_ARG, "nghost too small for the reconstruction "
+                                "(reconstruction.cpp:117-127)");
+  if (d->nx1 < d->nghost || d->nx2 < d->nghost || d->nx3 < d->nghost)
+    return fail(ATHGPU_ERR_ARG, "MeshBlock smaller than the ghost width");
+  if (d->rsolver != ATHGPU_HLLD && d->rsolver != ATHGPU_HLLE)
+    return fail(ATHGPU_ERR_ARG, "unknown Riemann solver");
+  if (d->precision != ATHGPU_FP64 && d->precision != ATHGPU_FP32)
+    return fail(ATHGPU_ERR_ARG, "unknown precision");
+  if (d->relativistic)
+    return fail(ATHGPU_ERR_UNSUPPORTED, "relativistic MHD is not in this entry point");
+  if (!d->x1f || !d->dx1f || !d->x2f || !d->dx2f || !d->x3f || !d->dx3f)
+    return fail(ATHGPU_ERR_ARG, "coordinate arrays are required");
+  if (!(d->gamma > 1.0) || !(d->cfl_number > 0.0))
+    return fail(ATHGPU_ERR_ARG, "gamma must exceed 1 and cfl_number be positive");
+
+  athgpu_ctx* c = new athgpu_ctx();
+  c->desc = *d;
+  c->real_bytes = d->precision == ATHGPU_FP64 ? 8 : 4;
+  DevMesh& m = c->m;
+  m.nbx1 = d->nbx1; m.nbx2 = d->nbx2; m.nbx3 = d->nbx3;
+  m.nb = d->nbx1 * d->nbx2 * d->nbx3;
+  m.nx1 = d->nx1; m.nx2 = d->nx2; m.nx3 = d->nx3; m.ng = d->nghost;
+  m.nc1 = d->nx1 + 2 * m.ng; m.nc2 = d->nx2 + 2 * m.ng; m.nc3 = d->nx3 + 2 * m.ng;
+  m.is = m.ng; m.ie = m.ng + m.nx1 - 1;
+  m.js = m.ng; m.je = m.ng + m.nx2 - 1;
+  m.ks = m.ng; m.ke = m.ng + m.nx3 - 1;
+  m.ncell = (i64)m.nc1 * m.nc2 * m.nc3;
+  m.nf1 = (i64)m.nc3 * m.nc2 * (m.nc1 + 1);
+  m.nf2 = (i64)m.nc3 * (m.nc2 + 1) * m.nc1;
+  m.nf3 = (i64)(m.nc3 + 1) * m.nc2 * m.nc1;
+  m.ne1 = (i64)(m.nc3 + 1) * (m.nc2 + 1) * m.nc1;
+  m.ne2 = (i64)(m.nc3 + 1) * m.nc2 * (m.nc1 + 1);
+  m.ne3 = (i64)m.nc3 * (m.nc2 + 1) * (m.nc1 + 1);
+  m.gamma = d->gamma; m.dfloor = d->dfloor; m.pfloor = d->pfloor;
+  m.cfl = d->cfl_number; m.tlim = d->tlim;
+  m.ncmax = m.nc1 > m.nc2 ? (m.nc1 > m.nc3 ? m.nc1 : m.nc3) : (m.nc2 > m.nc3 ? m.nc2 : m.nc3);
+
+  auto bail = [&](athgpu_status s) {
+    free_all(c);
+    delete c;
+    return s;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+  c->stream = c->own_stream;
+
+  const i64 nb = m.nb, rb = c->real_bytes;
+  Registers& r = c->r;
+  struct A { void** p; i64 bytes; };
+  std::vector<A> allocs = {
+      {&r.u, nb * 5 * m.ncell * rb}, {&r.ustar, nb * 5 * m.ncell * rb},
+      {&r.w, nb * 5 * m.ncell * rb}, {&r.bcc, nb * 3 * m.ncell * rb},
+      {&r.flx1, 5 * nb * m.nf1 * rb}, {&r.flx2, 5 * nb * m.nf2 * rb},
+      {&r.flx3, 5 * nb * m.nf3 * rb},
+      {&r.e3x1, nb * m.nf1 * rb}, {&r.e2x1, nb * m.nf1 * rb}, {&r.w1f, nb * m.nf1 * rb},
+      {&r.e1x2, nb * m.nf2 * rb}, {&r.e3x2, nb * m.nf2 * rb}, {&r.w2f, nb * m.nf2 * rb},
+      {&r.e1x3, nb * m.nf3 * rb}, {&r.e2x3, nb * m.nf3 * rb}, {&r.w3f, nb * m.nf3 * rb},
+      {&r.e1, nb * m.ne1 * rb}, {&r.e2, nb * m.ne2 * rb}, {&r.e3, nb * m.ne3 * rb},
+      {(void**)&r.b1, nb * m.nf1 * 8}, {(void**)&r.b2, nb * m.nf2 * 8},
+      {(void**)&r.b3, nb * m.nf3 * 8}, {(void**)&r.bs1, nb * m.nf1 * 8},
+      {(void**)&r.bs2, nb * m.nf2 * 8}, {(void**)&r.bs3, nb * m.nf3 * 8},
+      {(void**)&c->clk, (i64)sizeof(DevClock)}};
+  if (rb == 4) {
+    allocs.push_back({&r.ulo, nb * 5 * m.ncell * rb});
+    allocs.push_back({(void**)&c->staging, nb * 5 * m.ncell * 8});
+  }
+  for (auto& a : allocs) {
+    e = cudaMalloc(a.p, a.bytes);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
+    e = cudaMemsetAsync(*a.p, 0, a.bytes, c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemset"));
+  }
+
+  // coordinates: dx?f [nb][nc?] and the PLM interface coefficients
+  // (x?f(c+1)-x?v(c))/dx?f(c), (x?v(c)-x?f(c))/dx?f(c) with x?v = (x?f(c+1)+x?f(c))/2
+  // (plm.cpp:148-152, cartesian.cpp:28-32), laid out [nb][3][2][ncmax]
+  const int nc[3] = {m.nc1, m.nc2, m.nc3};
+  const double* xf[3] = {d->x1f, d->x2f, d->x3f};
+  const double* dxf[3] = {d->dx1f, d->dx2f, d->dx3f};
+  const i64 ncoord = nb * (m.nc1 + m.nc2 + m.nc3) + nb * 6 * m.ncmax;
+  std::vector<double> hc(ncoord, 0.0);
+  i64 off = 0;
+  i64 dxoff[3];
+  for (int dd = 0; dd < 3; ++dd) {
+    dxoff[dd] = off;
+    memcpy(&hc[off], dxf[dd], sizeof(double) * nb * nc[dd]);
+    off += nb * nc[dd];
+  }
+  const i64 plmoff = off;
+  for (i64 b = 0; b < nb; ++b)
+    for (int dd = 0; dd < 3; ++dd)
+      for (int cc = 0; cc < nc[dd]; ++cc) {
+        const double* f = xf[dd] + b * (nc[dd] + 1);
+        const double* df = dxf[dd] + b * nc[dd];
+        double xv = 0.5 * (f[cc + 1] + f[cc]);
+        hc[plmoff + ((b * 3 + dd) * 2 + 0) * m.ncmax + cc] = (f[cc + 1] - xv) / df[cc];
+        hc[plmoff + ((b * 3 + dd) * 2 + 1) * m.ncmax + cc] = (xv - f[cc]) / df[cc];
+      }
+  e = cudaMalloc((void**)&c->coords, sizeof(double) * ncoord);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc coords"));
+  e = cudaMemcpy(c->coords, hc.data(), sizeof(double) * ncoord, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy coords"));
+  m.dx1f = c->coords + dxoff[0];
+  m.dx2f = c->coords + dxoff[1];
+  m.dx3f = c->coords + dxoff[2];
+  m.plm = c->coords + plmoff;
+
+  // neighbour table of the periodic block grid
+  std::vector<int> hn(nb * 27);
+  for (i64 b = 0; b < nb; ++b) {
+    int l1 = (int)(b % m.nbx1), l2 = (int)((b / m.nbx1) % m.nbx2),
+        l3 = (int)(b / ((i64)m.nbx1 * m.nbx2));
+    for (int o3 = -1; o3 <= 1; ++o3)
+      for (int o2 = -1; o2 <= 1; ++o2)
+        for (int o1 = -1; o1 <= 1; ++o1) {
+          int a1 = (l1 + o1 + m.nbx1) % m.nbx1, a2 = (l2 + o2 + m.nbx2) % m.nbx2,
+              a3 = (l3 + o3 + m.nbx3) % m.nbx3;
+          hn[b * 27 + ((o3 + 1) * 3 + (o2 + 1)) * 3 + (o1 + 1)] =
+              (a3 * m.nbx2 + a2) * m.nbx1 + a1;
+        }
+  }
+  e = cudaMalloc((void**)&c->nbr, sizeof(int) * hn.size());
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc nbr"));
+  e = cudaMemcpy(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy nbr"));
+  m.nbr = c->nbr;
+
+  DevClock hclk;
+  hclk.dt = DBL_MAX;  // mesh.cpp:100
+  hclk.time = 0.0;
+  double dmax = DBL_MAX;
+  memcpy(&hclk.dtmin_bits, &dmax, 8);
+  hclk.c2p_floor_count = 0;
+  hclk.pad = 0;
+  e = cudaMemcpy(c->clk, &hclk, sizeof(hclk), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy clock"));
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "create sync"));
+  *out = c;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_destroy(athgpu_ctx* c) {
+  if (!c) return ATHGPU_OK;
+  cudaStreamSynchronize(c->stream);
+  free_all(c);
+  delete c;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_stream(athgpu_ctx* c, void* stream) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_upload_state(athgpu_ctx* c, const double* u, const double* b1,
+                                  const double* b2, const double* b3) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  const DevMesh& m = c->m;
+  athgpu_status s;
+  if (u && (s = upload_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
+    return s;
+  if (b1) CK(cudaMemcpyAsync(c->r.b1, b1, m.nb * m.nf1 * 8, cudaMemcpyHostToDevice, c->stream));
+  if (b2) CK(cudaMemcpyAsync(c->r.b2, b2, m.nb * m.nf2 * 8, cudaMemcpyHostToDevice, c->stream));
+  if (b3) CK(cudaMemcpyAsync(c->r.b3, b3, m.nb * m.nf3 * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_download_state(athgpu_ctx* c, double* u, double* b1, double* b2,
+                                    double* b3) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  const DevMesh& m = c->m;
+  athgpu_status s;
+  if (u && (s = download_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
+    return s;
+  if (b1) CK(cudaMemcpyAsync(b1, c->r.b1, m.nb * m.nf1 * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (b2) CK(cudaMemcpyAsync(b2, c->r.b2, m.nb * m.nf2 * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (b3) CK(cudaMemcpyAsync(b3, c->r.b3, m.nb * m.nf3 * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_download_prim(athgpu_ctx* c, double* w, double* bcc) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  const DevMesh& m = c->m;
+  athgpu_status s;
+  if (w && (s = download_bulk(c, w, c->r.w, nullptr, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
+    return s;
+  if (bcc && (s = download_bulk(c, bcc, c->r.bcc, nullptr, (i64)m.nb * 3 * m.ncell)) !=
+                 ATHGPU_OK)
+    return s;
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_initialize(athgpu_ctx* c) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  cudaError_t e = c->desc.precision == ATHGPU_FP64 ? init_fp64(c) : init_fp32(c);
+  if (e != cudaSuccess) return cuda_fail(e, "initialize");
+  CK(cudaStreamSynchronize(c->stream));
+  c->initialized = true;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_stage(athgpu_ctx* c, int stage) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (!c->initialized) return fail(ATHGPU_ERR_STATE, "athgpu_initialize not called");
+  if (stage != 1 && stage != 2) return fail(ATHGPU_ERR_ARG, "stage must be 1 or 2");
+  cudaError_t e = run_stage_dispatch(c, stage);
+  if (e != cudaSuccess) return cuda_fail(e, "stage");
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_cycle(athgpu_ctx* c, int ncycles) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (!c->initialized) return fail(ATHGPU_ERR_STATE, "athgpu_initialize not called");
+  if (ncycles < 0) return fail(ATHGPU_ERR_ARG, "ncycles < 0");
+  if (!c->cycle_exec || c->graph_stream != c->stream) {
+    if (c->cycle_exec) { cudaGraphExecDestroy(c->cycle_exec); c->cycle_exec = nullptr; }
+    if (c->cycle_graph) { cudaGraphDestroy(c->cycle_graph); c->cycle_graph = nullptr; }
+    long long l0 = c->launches;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e1 = run_stage_dispatch(c, 1);
+    cudaError_t e2 = run_stage_dispatch(c, 2);
+    cudaError_t e3 = run_stage_dispatch(c, 0);
+    cudaGraph_t g = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+    if (e1 != cudaSuccess) return cuda_fail(e1, "capture stage 1");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "capture stage 2");
+    if (e3 != cudaSuccess) return cuda_fail(e3, "capture end of cycle");
+    if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
+    c->cycle_graph = g;
+    CK(cudaGraphInstantiate(&c->cycle_exec, g, 0));
+    c->graph_stream = c->stream;
+    c->per_cycle = c->launches - l0;  // kernels in one replay of the graph
+    c->launches = l0;                 // capturing launched nothing
+
+  }
+  for (int n = 0; n < ncycles; ++n) {
+    CK(cudaGraphLaunch(c->cycle_exec, c->stream));
+  }
+  c->launches += (long long)ncycles * c->per_cycle;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_run_until(athgpu_ctx* c, double tlim, int max_cycles, int* nrun) {
+  if (!c || !nrun) return fail(ATHGPU_ERR_ARG, "null argument");
+  *nrun = 0;
+  for (int n = 0; n < max_cycles; ++n) {
+    double t, dt;
+    athgpu_status s = athgpu_get_clock(c, &t, &dt);
+    if (s != ATHGPU_OK) return s;
+    if (!(t < tlim)) break;
+    s = athgpu_cycle(c, 1);
+    if (s != ATHGPU_OK) return s;
+    ++*nrun;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_get_clock(athgpu_ctx* c, double* time, double* dt) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  DevClock h;
+  CK(cudaMemcpyAsync(&h, c->clk, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (time) *time = h.time;
+  if (dt) *dt = h.dt;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_clock(athgpu_ctx* c, double time, double dt) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  DevClock h;
+  CK(cudaMemcpyAsync(&h, c->clk, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  h.time = time;
+  h.dt = dt;
+  CK(cudaMemcpyAsync(c->clk, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_synchronize(athgpu_ctx* c) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_floor_count(athgpu_ctx* c, long long* count, int reset) {
+  if (!c || !count) return fail(ATHGPU_ERR_ARG, "null argument");
+  DevClock h;
+  CK(cudaMemcpyAsync(&h, c->clk, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *count = h.c2p_floor_count;
+  if (reset) {
+    int z = 0;
+    CK(cudaMemcpyAsync((char*)c->clk + offsetof(DevClock, c2p_floor_count), &z, sizeof(int),
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_device_state_ptrs(athgpu_ctx* c, athgpu_device_state* out) {
+  if (!c || !out) return fail(ATHGPU_ERR_ARG, "null argument");
+  out->u = c->r.u;
+  out->ulo = c->r.ulo;
+  out->w = c->r.w;
+  out->bcc = c->r.bcc;
+  out->b1 = c->r.b1;
+  out->b2 = c->r.b2;
+  out->b3 = c->r.b3;
+  out->real_bytes = c->real_bytes;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_sweep_segment(athgpu_ctx* c, int seg_x2, int seg_x3) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (seg_x2 < 0 || seg_x3 < 0) return fail(ATHGPU_ERR_ARG, "negative segment");
+  c->lc.seg_x2 = seg_x2;
+  c->lc.seg_x3 = seg_x3;
+  if (c->cycle_exec) {  // re-capture with the new launch shapes
+    CK(cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(c->cycle_exec);
+    c->cycle_exec = nullptr;
+    cudaGraphDestroy(c->cycle_graph);
+    c->cycle_graph = nullptr;
+  }
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_profile_cycle(athgpu_ctx* c, int cap, float* ms, int* count) {
+  if (!c || !ms || !count) return fail(ATHGPU_ERR_ARG, "null argument");
+  if (!c->initialized) return fail(ATHGPU_ERR_STATE, "athgpu_initialize not called");
+  CK(cudaStreamSynchronize(c->stream));
+  for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
+  c->prof_events.clear();
+  c->prof_names.clear();
+  c->profiling = true;
+  cudaError_t e1 = run_stage_dispatch(c, 1);
+  cudaError_t e2 = run_stage_dispatch(c, 2);
+  cudaError_t e3 = run_stage_dispatch(c, 0);
+  c->profiling = false;
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+    return cuda_fail(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3, "profile cycle");
+  CK(cudaStreamSynchronize(c->stream));
+  const int n = (int)c->prof_names.size();
+  *count = n;
+  for (int i = 0; i < n && i < cap; ++i)
+    CK(cudaEventElapsedTime(&ms[i], c->prof_events[2 * i], c->prof_events[2 * i + 1]));
+  return ATHGPU_OK;
+}
+
+const char* athgpu_profile_label(athgpu_ctx* c, int idx) {
+  if (!c || idx < 0 || idx >= (int)c->prof_names.size()) return "";
+  return c->prof_names[idx].c_str();
+}
+
+athgpu_status athgpu_launch_count(athgpu_ctx* c, long long* count, int reset) {
+  if (!c || !count) return fail(ATHGPU_ERR_ARG, "null argument");
+  *count = c->launches;
+  if (reset) c->launches = 0;
+  return ATHGPU_OK;
+}
+
+}  // extern "C"

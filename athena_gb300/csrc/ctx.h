@@ -1,0 +1,81 @@
+// Internal state of an athgpu context (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/athena_gb300.h"
+#include "kernels.cuh"
+
+namespace athgpu {
+
+struct Registers {
+  // bulk precision (double or float) arrays; `void*` so one struct serves both paths
+  void *u = nullptr, *ustar = nullptr, *ulo = nullptr, *w = nullptr, *bcc = nullptr;
+  void *flx1 = nullptr, *flx2 = nullptr, *flx3 = nullptr;
+  void *e3x1 = nullptr, *e2x1 = nullptr, *w1f = nullptr;
+  void *e1x2 = nullptr, *e3x2 = nullptr, *w2f = nullptr;
+  void *e1x3 = nullptr, *e2x3 = nullptr, *w3f = nullptr;
+  void *e1 = nullptr, *e2 = nullptr, *e3 = nullptr;
+  // always FP64: face field B and its stage-1 register
+  double *b1 = nullptr, *b2 = nullptr, *b3 = nullptr;
+  double *bs1 = nullptr, *bs2 = nullptr, *bs3 = nullptr;
+};
+
+struct LaunchConfig {
+  int seg_x2 = 0, seg_x3 = 0;  // faces per thread along the x2/x3 sweeps (0: default)
+};
+
+}  // namespace athgpu
+
+struct athgpu_ctx {
+  athgpu_mesh_desc desc;
+  athgpu::DevMesh m;
+  athgpu::Registers r;
+  athgpu::LaunchConfig lc;
+  athgpu::DevClock* clk = nullptr;
+  double* coords = nullptr;  // dx1f | dx2f | dx3f | plm coefficients (device)
+  int* nbr = nullptr;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  cudaGraphExec_t cycle_exec = nullptr;
+  cudaGraph_t cycle_graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  bool initialized = false;
+  int real_bytes = 8;
+  long long launches = 0;
+  long long per_cycle = 0;
+  double* staging = nullptr;  // device staging of FP64 host data in FP32 mode
+  // per-kernel timing of one non-graph cycle (athgpu_profile_cycle)
+  bool profiling = false;
+  std::vector<std::string> prof_names;
+  std::vector<cudaEvent_t> prof_events;  // two per launch
+};
+
+// record an event pair around one launch when the context is profiling
+struct ProfScope {
+  athgpu_ctx* c;
+  ProfScope(athgpu_ctx* ctx, const char* name) : c(ctx) {
+    if (!c->profiling) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->prof_events.push_back(e);
+    c->prof_names.push_back(name);
+  }
+  ~ProfScope() {
+    if (!c->profiling) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->prof_events.push_back(e);
+  }
+};
+
+namespace athgpu {
+// stage drivers, one per precision translation unit
+cudaError_t stage_fp64(athgpu_ctx* c, int stage);
+cudaError_t stage_fp32(athgpu_ctx* c, int stage);
+cudaError_t init_fp64(athgpu_ctx* c);
+cudaError_t init_fp32(athgpu_ctx* c);
+}  // namespace athgpu

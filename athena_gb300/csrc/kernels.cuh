@@ -1,0 +1,656 @@
+// Stage-update kernels over all MeshBlocks of a uniform single-level mesh.
+//
+// Device layout: every field is one allocation holding all MeshBlocks back to back, each
+// block in the reference's AthenaArray layout (athena_arrays.hpp:140-143, ghosts
+// included): cells [nb][nvar][nc3][nc2][nc1], x1 faces [nb][nc3][nc2][nc1+1], x2 faces
+// [nb][nc3][nc2+1][nc1], x3 faces [nb][nc3+1][nc2][nc1], edges x1e [nb][nc3+1][nc2+1][nc1],
+// x2e [nb][nc3+1][nc2][nc1+1], x3e [nb][nc3][nc2+1][nc1+1] (athena.hpp:128-148).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "physics.cuh"
+
+namespace athgpu {
+
+typedef long long i64;
+
+struct DevMesh {
+  int nb, nbx1, nbx2, nbx3;
+  int nx1, nx2, nx3, ng;
+  int nc1, nc2, nc3;
+  int is, ie, js, je, ks, ke;
+  i64 ncell, nf1, nf2, nf3, ne1, ne2, ne3;  // per-block element counts
+  double gamma, dfloor, pfloor, cfl, tlim;
+  const double* dx1f;  // [nb][nc1]
+  const double* dx2f;  // [nb][nc2]
+  const double* dx3f;  // [nb][nc3]
+  const double* plm;   // [nb][3][2][ncmax]: (x?f(c+1)-x?v(c))/dx?f(c), (x?v(c)-x?f(c))/dx?f(c)
+  int ncmax;
+  const int* nbr;      // [nb][27] neighbour block for offset ((o3+1)*3+(o2+1))*3+(o1+1)
+};
+
+// device-resident scalars of the time integrator
+struct DevClock {
+  double dt, time;
+  unsigned long long dtmin_bits;  // min over cells of dx/speed, as ordered bits
+  int c2p_floor_count;
+  int pad;
+};
+
+__device__ __forceinline__ i64 cidx(const DevMesh& m, int b, int n, int nvar, int k, int j,
+                                    int i) {
+  return (((i64)b * nvar + n) * m.nc3 + k) * m.nc2 * m.nc1 + (i64)j * m.nc1 + i;
+}
+__device__ __forceinline__ i64 f1idx(const DevMesh& m, int b, int k, int j, int i) {
+  return (i64)b * m.nf1 + ((i64)k * m.nc2 + j) * (m.nc1 + 1) + i;
+}
+__device__ __forceinline__ i64 f2idx(const DevMesh& m, int b, int k, int j, int i) {
+  return (i64)b * m.nf2 + ((i64)k * (m.nc2 + 1) + j) * m.nc1 + i;
+}
+__device__ __forceinline__ i64 f3idx(const DevMesh& m, int b, int k, int j, int i) {
+  return (i64)b * m.nf3 + ((i64)k * m.nc2 + j) * m.nc1 + i;
+}
+__device__ __forceinline__ i64 e1idx(const DevMesh& m, int b, int k, int j, int i) {
+  return (i64)b * m.ne1 + ((i64)k * (m.nc2 + 1) + j) * m.nc1 + i;
+}
+__device__ __forceinline__ i64 e2idx(const DevMesh& m, int b, int k, int j, int i) {
+  return (i64)b * m.ne2 + ((i64)k * m.nc2 + j) * (m.nc1 + 1) + i;
+}
+__device__ __forceinline__ i64 e3idx(const DevMesh& m, int b, int k, int j, int i) {
+  return (i64)b * m.ne3 + ((i64)k * (m.nc2 + 1) + j) * (m.nc1 + 1) + i;
+}
+// per-block face-array offset of (k,j,i) for the face arrays of direction DIR
+template <int DIR>
+__device__ __forceinline__ i64 fidx(const DevMesh& m, int b, int k, int j, int i) {
+  return DIR == 0 ? f1idx(m, b, k, j, i) : DIR == 1 ? f2idx(m, b, k, j, i)
+                                                    : f3idx(m, b, k, j, i);
+}
+// flux scratch arrays are variable-major over the whole mesh, [5][nb][face]: stride of
+// one variable
+template <int DIR>
+__device__ __forceinline__ i64 fsize(const DevMesh& m) {
+  return (i64)m.nb * (DIR == 0 ? m.nf1 : DIR == 1 ? m.nf2 : m.nf3);
+}
+
+// ---------------------------------------------------------------------------------------
+// Reconstruction of one cell along DIR: wave vector (natural order d, v1, v2, v3, p, then
+// the two transverse cell-centred field components, plm.cpp:45-57 / :196-208) of the
+// cell and its neighbours; returns the upper-face value qlp and lower-face value qrm.
+template <typename Real, int DIR, int ORDER>
+__device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restrict__ w,
+                                           const Real* __restrict__ bcc, int b, int k,
+                                           int j, int i, Real* qlp, Real* qrm) {
+  const i64 sw = DIR == 0 ? 1 : DIR == 1 ? (i64)m.nc1 : (i64)m.nc1 * m.nc2;
+  const i64 base_w = cidx(m, b, 0, NHYDRO, k, j, i);
+  const i64 base_b = cidx(m, b, 0, 3, k, j, i);
+  const i64 vs = m.ncell;  // variable stride within a block
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    const Real* src;
+    i64 o;
+    if (n < NHYDRO) {
+      src = w;
+      o = base_w + n * vs;
+    } else {
+      src = bcc;
+      o = base_b + (i64)((DIR + n - NHYDRO + 1) % 3) * vs;
+    }
+    if (ORDER == 1) {  // DonorCellX1/2/3, reconstruct/dc.cpp:24-104
+      Real q = __ldg(src + o);
+      qlp[n] = q;
+      qrm[n] = q;
+    } else if (ORDER == 2) {
+      int c = DIR == 0 ? i : DIR == 1 ? j : k;
+      const double* pc = m.plm + ((i64)b * 3 + DIR) * 2 * m.ncmax;
+      plm_one<Real>(__ldg(src + o - sw), __ldg(src + o), __ldg(src + o + sw),
+                    (Real)__ldg(pc + c), (Real)__ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
+    } else {
+      ppm_one<Real>(__ldg(src + o - 2 * sw), __ldg(src + o - sw), __ldg(src + o),
+                    __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n]);
+    }
+  }
+  if (ORDER == 3) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
+    const Real dfl = (Real)m.dfloor, pfl = (Real)m.pfloor;
+    qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
+    qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
+    qrm[IDN] = (qrm[IDN] > dfl) ? qrm[IDN] : dfl;
+    qrm[IPR] = (qrm[IPR] > pfl) ? qrm[IPR] : pfl;
+  }
+}
+
+// Riemann solve on one face of direction DIR and store flux, face EMFs and CT weight
+// (Hydro::CalculateFluxes calculate_fluxes.cpp:102/:221/:340; hlld.cpp:372-376)
+template <typename Real, int DIR, int RS>
+__device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, const Real* wr,
+                                           Real bx, Real dx, Real dt, i64 fo,
+                                           Real* __restrict__ flx, Real* __restrict__ ey,
+                                           Real* __restrict__ ez, Real* __restrict__ wct) {
+  // local order: d, v_normal, v_t1, v_t2, p, By, Bz (hlld.cpp:42-43)
+  const int ivx = IVX + DIR, ivy = IVX + (DIR + 1) % 3, ivz = IVX + (DIR + 2) % 3;
+  Real wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
+  Real wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
+  Real f[NWAVE];
+  if (RS == 0) hlld<Real>((Real)m.gamma, wli, wri, bx, f);
+  else hlle<Real>((Real)m.gamma, wli, wri, bx, f);
+  const i64 fs = fsize<DIR>(m);
+  flx[fo] = f[0];
+  flx[(i64)ivx * fs + fo] = f[1];
+  flx[(i64)ivy * fs + fo] = f[2];
+  flx[(i64)ivz * fs + fo] = f[3];
+  flx[(i64)IPR * fs + fo] = f[4];
+  ey[fo] = -f[5];
+  ez[fo] = f[6];
+  wct[fo] = weight_for_ct<Real>(f[0], wl[IDN], wr[IDN], dx, dt);
+}
+
+// x1 sweep: rows (b, k in [ks-1,ke+1], j in [js-1,je+1]); cells i in [is-1, ie+1] are
+// flattened over rows; a warp reconstructs 32 consecutive cells (the first one overlaps
+// the previous warp) and passes each cell's upper-face state to the next lane with a
+// shuffle, so that every cell is reconstructed once and every face solved once.
+// flx layout: [5][nb][nc3][nc2][nc1+1]; e3/e2/wct: [nb][nc3][nc2][nc1+1].
+template <typename Real, int ORDER, int RS>
+__global__ void __launch_bounds__(128)
+flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ bcc,
+               const double* __restrict__ b1, const DevClock* __restrict__ clk,
+               Real* __restrict__ flx, Real* __restrict__ e3, Real* __restrict__ e2,
+               Real* __restrict__ wct) {
+  const int lane = threadIdx.x & 31;
+  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int ncr = m.nx1 + 2, nrj = m.nx2 + 2, nrk = m.nx3 + 2;
+  const i64 total = (i64)m.nb * nrk * nrj * ncr;
+  const i64 g = warp * 31 + lane - 1;
+  const bool valid = (g >= 0) && (g < total);
+  Real qlp[NWAVE], qrm[NWAVE];
+  int b = 0, k = 0, j = 0, c = 0;
+  if (valid) {
+    i64 row = g / ncr;
+    c = (int)(g - row * ncr);
+    j = (int)(row % nrj) + m.js - 1;
+    i64 r2 = row / nrj;
+    k = (int)(r2 % nrk) + m.ks - 1;
+    b = (int)(r2 / nrk);
+    recon_cell<Real, 0, ORDER>(m, w, bcc, b, k, j, m.is - 1 + c, qlp, qrm);
+  } else {
+#pragma unroll
+    for (int n = 0; n < NWAVE; ++n) qlp[n] = qrm[n] = Real(0);
+  }
+  Real wl[NWAVE];
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) wl[n] = __shfl_up_sync(0xffffffffu, qlp[n], 1);
+  if (!valid || lane == 0 || c == 0) return;
+  const int i = m.is - 1 + c;
+  const double dt = clk->dt;
+  const i64 fo = f1idx(m, b, k, j, i);
+  solve_face<Real, 0, RS>(m, wl, qrm, (Real)__ldg(b1 + fo),
+                          (Real)__ldg(m.dx1f + (i64)b * m.nc1 + i), (Real)dt,
+                          fo, flx, e3, e2, wct);
+}
+
+// x2 / x3 sweeps: a thread owns one column (b, transverse index, i) and walks SEG faces
+// along the sweep, carrying the previous cell's upper-face state in registers (the
+// reference's wl/wlb swap, calculate_fluxes.cpp:184-237 and :304-356).  Columns:
+// x2: k in [ks-1,ke+1], i in [is-1,ie+1]; x3: j in [js-1,je+1], i in [is-1,ie+1].
+template <typename Real, int DIR, int ORDER, int RS>
+__global__ void __launch_bounds__(128)
+flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
+                  const Real* __restrict__ bcc, const double* __restrict__ bn,
+                  const DevClock* __restrict__ clk, Real* __restrict__ flx,
+                  Real* __restrict__ ey, Real* __restrict__ ez, Real* __restrict__ wct) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ni = m.nx1 + 2;
+  const int nt = (DIR == 1) ? m.nx3 + 2 : m.nx2 + 2;
+  const int nface = (DIR == 1) ? m.nx2 + 1 : m.nx3 + 1;
+  const int nseg = (nface + seg - 1) / seg;
+  const i64 total = (i64)nseg * m.nb * nt * ni;
+  if (t >= total) return;
+  const int ii = (int)(t % ni);
+  i64 r = t / ni;
+  const int tt = (int)(r % nt);
+  r /= nt;
+  const int b = (int)(r % m.nb);
+  const int s = (int)(r / m.nb);
+  const int i = m.is - 1 + ii;
+  const int s0 = (DIR == 1 ? m.js : m.ks) + s * seg;
+  const int s1 = min(s0 + seg - 1, (DIR == 1 ? m.je : m.ke) + 1);
+  const double dt = clk->dt;
+  Real wl[NWAVE], qlp[NWAVE], qrm[NWAVE];
+  if (DIR == 1) {
+    const int k = m.ks - 1 + tt;
+    recon_cell<Real, 1, ORDER>(m, w, bcc, b, k, s0 - 1, i, wl, qrm);
+    for (int jf = s0; jf <= s1; ++jf) {
+      recon_cell<Real, 1, ORDER>(m, w, bcc, b, k, jf, i, qlp, qrm);
+      const i64 fo = f2idx(m, b, k, jf, i);
+      solve_face<Real, 1, RS>(m, wl, qrm, (Real)__ldg(bn + fo),
+                              (Real)__ldg(m.dx2f + (i64)b * m.nc2 + jf), (Real)dt, fo,
+                              flx, ey, ez, wct);
+#pragma unroll
+      for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
+    }
+  } else {
+    const int j = m.js - 1 + tt;
+    recon_cell<Real, 2, ORDER>(m, w, bcc, b, s0 - 1, j, i, wl, qrm);
+    for (int kf = s0; kf <= s1; ++kf) {
+      recon_cell<Real, 2, ORDER>(m, w, bcc, b, kf, j, i, qlp, qrm);
+      const i64 fo = f3idx(m, b, kf, j, i);
+      solve_face<Real, 2, RS>(m, wl, qrm, (Real)__ldg(bn + fo),
+                              (Real)__ldg(m.dx3f + (i64)b * m.nc3 + kf), (Real)dt, fo,
+                              flx, ey, ez, wct);
+#pragma unroll
+      for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Field::ComputeCornerE, calculate_corner_e.cpp:124-236 (3-D Newtonian branch).  The cell
+// centred E = -v x B (cc_e_, :174-181) is formed on the fly from w and bcc.  One thread
+// per corner point (b, k, j, i) in [ks,ke+1]x[js,je+1]x[is,ie+1].
+template <typename Real>
+__device__ __forceinline__ Real cce(const DevMesh& m, const Real* __restrict__ w,
+                                    const Real* __restrict__ bcc, int b, int n, int k,
+                                    int j, int i) {
+  const i64 cw = cidx(m, b, 0, NHYDRO, k, j, i), cb = cidx(m, b, 0, 3, k, j, i);
+  const i64 vs = m.ncell;
+  if (n == 0)
+    return __ldg(w + cw + 3 * vs) * __ldg(bcc + cb + vs) -
+           __ldg(w + cw + 2 * vs) * __ldg(bcc + cb + 2 * vs);
+  if (n == 1)
+    return __ldg(w + cw + vs) * __ldg(bcc + cb + 2 * vs) -
+           __ldg(w + cw + 3 * vs) * __ldg(bcc + cb);
+  return __ldg(w + cw + 2 * vs) * __ldg(bcc + cb) - __ldg(w + cw + vs) * __ldg(bcc + cb + vs);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(128)
+corner_e_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ bcc,
+                const Real* __restrict__ e3x1, const Real* __restrict__ e2x1,
+                const Real* __restrict__ w1f, const Real* __restrict__ e1x2,
+                const Real* __restrict__ e3x2, const Real* __restrict__ w2f,
+                const Real* __restrict__ e1x3, const Real* __restrict__ e2x3,
+                const Real* __restrict__ w3f, Real* __restrict__ e1, Real* __restrict__ e2,
+                Real* __restrict__ e3) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = m.nx1 + 1, n2 = m.nx2 + 1, n3 = m.nx3 + 1;
+  if (t >= (i64)m.nb * n3 * n2 * n1) return;
+  const int i = m.is + (int)(t % n1);
+  i64 r = t / n1;
+  const int j = m.js + (int)(r % n2);
+  r /= n2;
+  const int k = m.ks + (int)(r % n3);
+  const int b = (int)(r / n3);
+  const Real one = Real(1.0), quarter = Real(0.25);
+#define W1F(kk, jj, ii) __ldg(w1f + f1idx(m, b, kk, jj, ii))
+#define W2F(kk, jj, ii) __ldg(w2f + f2idx(m, b, kk, jj, ii))
+#define W3F(kk, jj, ii) __ldg(w3f + f3idx(m, b, kk, jj, ii))
+#define E3X1(kk, jj, ii) __ldg(e3x1 + f1idx(m, b, kk, jj, ii))
+#define E2X1(kk, jj, ii) __ldg(e2x1 + f1idx(m, b, kk, jj, ii))
+#define E1X2(kk, jj, ii) __ldg(e1x2 + f2idx(m, b, kk, jj, ii))
+#define E3X2(kk, jj, ii) __ldg(e3x2 + f2idx(m, b, kk, jj, ii))
+#define E1X3(kk, jj, ii) __ldg(e1x3 + f3idx(m, b, kk, jj, ii))
+#define E2X3(kk, jj, ii) __ldg(e2x3 + f3idx(m, b, kk, jj, ii))
+#define CC(n, kk, jj, ii) cce<Real>(m, w, bcc, b, n, kk, jj, ii)
+  if (i <= m.ie) {
+    Real de1_l3 = (one - W2F(k - 1, j, i)) * (E1X3(k, j, i) - CC(0, k - 1, j, i)) +
+                  (W2F(k - 1, j, i)) * (E1X3(k, j - 1, i) - CC(0, k - 1, j - 1, i));
+    Real de1_r3 = (one - W2F(k, j, i)) * (E1X3(k, j, i) - CC(0, k, j, i)) +
+                  (W2F(k, j, i)) * (E1X3(k, j - 1, i) - CC(0, k, j - 1, i));
+    Real de1_l2 = (one - W3F(k, j - 1, i)) * (E1X2(k, j, i) - CC(0, k, j - 1, i)) +
+                  (W3F(k, j - 1, i)) * (E1X2(k - 1, j, i) - CC(0, k - 1, j - 1, i));
+    Real de1_r2 = (one - W3F(k, j, i)) * (E1X2(k, j, i) - CC(0, k, j, i)) +
+                  (W3F(k, j, i)) * (E1X2(k - 1, j, i) - CC(0, k - 1, j, i));
+    e1[e1idx(m, b, k, j, i)] =
+        quarter * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + E1X2(k - 1, j, i) + E1X2(k, j, i) +
+                   E1X3(k, j - 1, i) + E1X3(k, j, i));
+  }
+  if (j <= m.je) {
+    Real de2_l3 = (one - W1F(k - 1, j, i)) * (E2X3(k, j, i) - CC(1, k - 1, j, i)) +
+                  (W1F(k - 1, j, i)) * (E2X3(k, j, i - 1) - CC(1, k - 1, j, i - 1));
+    Real de2_r3 = (one - W1F(k, j, i)) * (E2X3(k, j, i) - CC(1, k, j, i)) +
+                  (W1F(k, j, i)) * (E2X3(k, j, i - 1) - CC(1, k, j, i - 1));
+    Real de2_l1 = (one - W3F(k, j, i - 1)) * (E2X1(k, j, i) - CC(1, k, j, i - 1)) +
+                  (W3F(k, j, i - 1)) * (E2X1(k - 1, j, i) - CC(1, k - 1, j, i - 1));
+    Real de2_r1 = (one - W3F(k, j, i)) * (E2X1(k, j, i) - CC(1, k, j, i)) +
+                  (W3F(k, j, i)) * (E2X1(k - 1, j, i) - CC(1, k - 1, j, i));
+    e2[e2idx(m, b, k, j, i)] =
+        quarter * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + E2X3(k, j, i - 1) + E2X3(k, j, i) +
+                   E2X1(k - 1, j, i) + E2X1(k, j, i));
+  }
+  if (k <= m.ke) {
+    Real de3_l2 = (one - W1F(k, j - 1, i)) * (E3X2(k, j, i) - CC(2, k, j - 1, i)) +
+                  (W1F(k, j - 1, i)) * (E3X2(k, j, i - 1) - CC(2, k, j - 1, i - 1));
+    Real de3_r2 = (one - W1F(k, j, i)) * (E3X2(k, j, i) - CC(2, k, j, i)) +
+                  (W1F(k, j, i)) * (E3X2(k, j, i - 1) - CC(2, k, j, i - 1));
+    Real de3_l1 = (one - W2F(k, j, i - 1)) * (E3X1(k, j, i) - CC(2, k, j, i - 1)) +
+                  (W2F(k, j, i - 1)) * (E3X1(k, j - 1, i) - CC(2, k, j - 1, i - 1));
+    Real de3_r1 = (one - W2F(k, j, i)) * (E3X1(k, j, i) - CC(2, k, j, i)) +
+                  (W2F(k, j, i)) * (E3X1(k, j - 1, i) - CC(2, k, j - 1, i));
+    e3[e3idx(m, b, k, j, i)] =
+        quarter * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + E3X2(k, j, i - 1) + E3X2(k, j, i) +
+                   E3X1(k, j - 1, i) + E3X1(k, j, i));
+  }
+#undef W1F
+#undef W2F
+#undef W3F
+#undef E3X1
+#undef E2X1
+#undef E1X2
+#undef E3X2
+#undef E1X3
+#undef E2X3
+#undef CC
+}
+
+// ---------------------------------------------------------------------------------------
+// Same-level EMF correction (flux_correction_fc.cpp:51-260, :689-940, :1355-1530): an
+// edge on a block face is the sum of the pre-averaging values of the blocks sharing it,
+// own value first and the others in neighbour-list order (faces x1, x2, x3, then the
+// edge neighbour; bvals_base.cpp:326-720), times 1/2 (two blocks) or 1/4 (four blocks).
+// C = 0, 1, 2 for e1, e2, e3.
+__device__ __forceinline__ int nbr_of(const DevMesh& m, int b, int o1, int o2, int o3) {
+  return __ldg(m.nbr + (i64)b * 27 + ((o3 + 1) * 3 + (o2 + 1)) * 3 + (o1 + 1));
+}
+
+template <typename Real, int C>
+__device__ __forceinline__ Real edge_value(const DevMesh& m, const Real* __restrict__ e,
+                                           int b, int k, int j, int i) {
+  auto at = [&](int bb, int kk, int jj, int ii) -> Real {
+    return __ldg(e + (C == 0 ? e1idx(m, bb, kk, jj, ii)
+                     : C == 1 ? e2idx(m, bb, kk, jj, ii) : e3idx(m, bb, kk, jj, ii)));
+  };
+  int o1 = 0, o2 = 0, o3 = 0;
+  if (C != 0) o1 = (i == m.is) ? -1 : (i == m.ie + 1) ? 1 : 0;
+  if (C != 1) o2 = (j == m.js) ? -1 : (j == m.je + 1) ? 1 : 0;
+  if (C != 2) o3 = (k == m.ks) ? -1 : (k == m.ke + 1) ? 1 : 0;
+  Real own = at(b, k, j, i);
+  const int on = (o1 != 0) + (o2 != 0) + (o3 != 0);
+  if (on == 0) return own;
+  Real sum = own;
+  // face neighbours in list order: x1 before x2 before x3
+  if (o1 != 0) sum += at(nbr_of(m, b, o1, 0, 0), k, j, i - o1 * m.nx1);
+  if (o2 != 0) sum += at(nbr_of(m, b, 0, o2, 0), k, j - o2 * m.nx2, i);
+  if (o3 != 0) sum += at(nbr_of(m, b, 0, 0, o3), k - o3 * m.nx3, j, i);
+  if (on == 2) {
+    sum += at(nbr_of(m, b, o1, o2, o3), k - o3 * m.nx3, j - o2 * m.nx2, i - o1 * m.nx1);
+    return sum * Real(0.25);
+  }
+  return sum * Real(0.5);
+}
+
+// Field::CT, field/ct.cpp:31-116, plus the VL2 register average (weighted_ave.cpp) which
+// for VL2 reduces to out = in on the first stage and an in-place update on the second.
+// One thread per face of all three face arrays.  Edge EMFs are read with the correction
+// above.  bin/bout may alias (second stage).
+template <typename Real>
+__global__ void __launch_bounds__(128)
+ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
+          const Real* __restrict__ e1, const Real* __restrict__ e2,
+          const Real* __restrict__ e3, const double* b1in, const double* b2in,
+          const double* b3in, double* b1out, double* b2out, double* b3out) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const i64 nf1 = (i64)m.nx3 * m.nx2 * (m.nx1 + 1);
+  const i64 nf2 = (i64)m.nx3 * (m.nx2 + 1) * m.nx1;
+  const i64 nf3 = (i64)(m.nx3 + 1) * m.nx2 * m.nx1;
+  const i64 per = nf1 + nf2 + nf3;
+  if (t >= per * m.nb) return;
+  const int b = (int)(t / per);
+  i64 r = t - (i64)b * per;
+  const double wght = beta * clk->dt;
+  const double* dx1f = m.dx1f + (i64)b * m.nc1;
+  const double* dx2f = m.dx2f + (i64)b * m.nc2;
+  const double* dx3f = m.dx3f + (i64)b * m.nc3;
+  if (r < nf1) {
+    const int i = m.is + (int)(r % (m.nx1 + 1));
+    r /= (m.nx1 + 1);
+    const int j = m.js + (int)(r % m.nx2);
+    const int k = m.ks + (int)(r / m.nx2);
+    const i64 o = f1idx(m, b, k, j, i);
+    double area = dx2f[j] * dx3f[k];
+    double len = dx3f[k], len_p1 = dx3f[k];
+    double v = b1in[o];
+    v -= (wght / area) * (len_p1 * (double)edge_value<Real, 2>(m, e3, b, k, j + 1, i) -
+                          len * (double)edge_value<Real, 2>(m, e3, b, k, j, i));
+    len = dx2f[j];
+    len_p1 = dx2f[j];
+    v += (wght / area) * (len_p1 * (double)edge_value<Real, 1>(m, e2, b, k + 1, j, i) -
+                          len * (double)edge_value<Real, 1>(m, e2, b, k, j, i));
+    b1out[o] = v;
+  } else if (r < nf1 + nf2) {
+    r -= nf1;
+    const int i = m.is + (int)(r % m.nx1);
+    r /= m.nx1;
+    const int j = m.js + (int)(r % (m.nx2 + 1));
+    const int k = m.ks + (int)(r / (m.nx2 + 1));
+    const i64 o = f2idx(m, b, k, j, i);
+    double area = dx1f[i] * dx3f[k];
+    double len = dx3f[k], len_ip1 = dx3f[k];
+    double v = b2in[o];
+    v += (wght / area) * (len_ip1 * (double)edge_value<Real, 2>(m, e3, b, k, j, i + 1) -
+                          len * (double)edge_value<Real, 2>(m, e3, b, k, j, i));
+    len = dx1f[i];
+    double len_p1 = dx1f[i];
+    v -= (wght / area) * (len_p1 * (double)edge_value<Real, 0>(m, e1, b, k + 1, j, i) -
+                          len * (double)edge_value<Real, 0>(m, e1, b, k, j, i));
+    b2out[o] = v;
+  } else {
+    r -= nf1 + nf2;
+    const int i = m.is + (int)(r % m.nx1);
+    r /= m.nx1;
+    const int j = m.js + (int)(r % m.nx2);
+    const int k = m.ks + (int)(r / m.nx2);
+    const i64 o = f3idx(m, b, k, j, i);
+    double area = dx1f[i] * dx2f[j];
+    double len = dx2f[j], len_ip1 = dx2f[j];
+    double v = b3in[o];
+    v -= (wght / area) * (len_ip1 * (double)edge_value<Real, 1>(m, e2, b, k, j, i + 1) -
+                          len * (double)edge_value<Real, 1>(m, e2, b, k, j, i));
+    len = dx1f[i];
+    double len_p1 = dx1f[i];
+    v += (wght / area) * (len_p1 * (double)edge_value<Real, 0>(m, e1, b, k, j + 1, i) -
+                          len * (double)edge_value<Real, 0>(m, e1, b, k, j, i));
+    b3out[o] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Hydro::AddFluxDivergence (add_flux_divergence.cpp:39-96, Cartesian areas/volumes
+// coordinates.cpp:448-548) fused with the VL2 register average.  KAHAN = 0: out = in -
+// wght*dflx/vol (FP64 path; in/out may alias).  KAHAN = 1 (FP32 path): the conserved
+// state is the compensated pair (hi, lo); stage 1 writes the predictor
+// out = hi + (lo + du), stage 2 adds du to (hi, lo) with a compensated sum.
+template <typename Real, int KAHAN>
+__global__ void __launch_bounds__(128)
+update_kernel(DevMesh m, double beta, int stage, const DevClock* __restrict__ clk,
+              const Real* __restrict__ f1, const Real* __restrict__ f2,
+              const Real* __restrict__ f3, const Real* uin, Real* uout, Real* ulo) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (i64)m.nb * m.nx3 * m.nx2 * m.nx1) return;
+  const int i = m.is + (int)(t % m.nx1);
+  i64 r = t / m.nx1;
+  const int j = m.js + (int)(r % m.nx2);
+  r /= m.nx2;
+  const int k = m.ks + (int)(r % m.nx3);
+  const int b = (int)(r / m.nx3);
+  const Real dx1 = (Real)m.dx1f[(i64)b * m.nc1 + i], dx2 = (Real)m.dx2f[(i64)b * m.nc2 + j],
+             dx3 = (Real)m.dx3f[(i64)b * m.nc3 + k];
+  const Real wght = (Real)(beta * clk->dt);
+  const Real x1area = dx2 * dx3, x2area = dx1 * dx3, x3area = dx1 * dx2;
+  const Real vol = dx1 * dx2 * dx3;
+  const i64 o1 = f1idx(m, b, k, j, i), o2 = f2idx(m, b, k, j, i), o3 = f3idx(m, b, k, j, i);
+  const i64 s2 = m.nc1, s3 = (i64)m.nc2 * m.nc1;
+  const i64 v1 = fsize<0>(m), v2 = fsize<1>(m), v3 = fsize<2>(m);
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) {
+    Real dflx = (x1area * __ldg(f1 + n * v1 + o1 + 1) - x1area * __ldg(f1 + n * v1 + o1));
+    dflx += (x2area * __ldg(f2 + n * v2 + o2 + s2) - x2area * __ldg(f2 + n * v2 + o2));
+    dflx += (x3area * __ldg(f3 + n * v3 + o3 + s3) - x3area * __ldg(f3 + n * v3 + o3));
+    const i64 c = cidx(m, b, n, NHYDRO, k, j, i);
+    if (KAHAN == 0) {
+      uout[c] = uin[c] - wght * dflx / vol;
+    } else {
+      const Real du = -(wght * dflx / vol);
+      const Real hi = uin[c], lo = ulo[c];
+      if (stage == 1) {
+        uout[c] = hi + (lo + du);
+      } else {
+        const Real y = du + lo;
+        const Real tt = hi + y;
+        ulo[c] = y - (tt - hi);
+        uout[c] = tt;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Same-level periodic ghost exchange: every ghost cell / face receives the value of the
+// neighbour block that owns it (bvals_cc.cpp:287-430; face fields bvals_fc.cpp:344-397,
+// where a block's own faces along the normal are [is, ie+1]).  WHAT = 0: cells
+// (nvar variables), 1/2/3: x1/x2/x3 face field.
+__device__ __forceinline__ int own_map(int idx, int lo, int hi, int n, int* o) {
+  if (idx < lo) { *o = -1; return idx + n; }
+  if (idx > hi) { *o = 1; return idx - n; }
+  *o = 0;
+  return idx;
+}
+
+template <typename T, int WHAT>
+__global__ void __launch_bounds__(256)
+exchange_kernel(DevMesh m, int nvar, T* __restrict__ a) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = m.nc1 + (WHAT == 1), n2 = m.nc2 + (WHAT == 2), n3 = m.nc3 + (WHAT == 3);
+  const i64 per = (i64)n3 * n2 * n1;
+  if (t >= per * m.nb) return;
+  const int b = (int)(t / per);
+  i64 r = t - (i64)b * per;
+  const int i = (int)(r % n1);
+  r /= n1;
+  const int j = (int)(r % n2);
+  const int k = (int)(r / n2);
+  int o1, o2, o3;
+  const int si = own_map(i, m.is, m.ie + (WHAT == 1), m.nx1, &o1);
+  const int sj = own_map(j, m.js, m.je + (WHAT == 2), m.nx2, &o2);
+  const int sk = own_map(k, m.ks, m.ke + (WHAT == 3), m.nx3, &o3);
+  if ((o1 | o2 | o3) == 0) return;
+  const int sb = nbr_of(m, b, o1, o2, o3);
+  if (sb < 0) return;
+  if (WHAT == 0) {
+    for (int n = 0; n < nvar; ++n)
+      a[cidx(m, b, n, nvar, k, j, i)] = a[cidx(m, sb, n, nvar, sk, sj, si)];
+  } else {
+    i64 d, s;
+    if (WHAT == 1) { d = f1idx(m, b, k, j, i); s = f1idx(m, sb, sk, sj, si); }
+    else if (WHAT == 2) { d = f2idx(m, b, k, j, i); s = f2idx(m, sb, sk, sj, si); }
+    else { d = f3idx(m, b, k, j, i); s = f3idx(m, sb, sk, sj, si); }
+    a[d] = a[s];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Field::CalculateCellCenteredField (field.cpp:112-180, uniform weights) and
+// EquationOfState::ConservedToPrimitive (adiabatic_mhd.cpp:41-90) over whole blocks,
+// fused with Hydro::NewBlockTimeStep (new_blockdt.cpp:80-103) on the interior when
+// do_dt is set: the per-cell dx/(|v|+c_f) minimum is reduced with warp shuffles and one
+// atomicMin per warp on the order-preserving bit pattern of the positive double.
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <typename Real, int KAHAN>
+__global__ void __launch_bounds__(128)
+c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
+           const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
+           Real* ulo, Real* __restrict__ w, Real* __restrict__ bcc, DevClock* clk) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double cell_dt = 1.0e300;
+  if (t < (i64)m.nb * m.ncell) {
+    const int b = (int)(t / m.ncell);
+    i64 r = t - (i64)b * m.ncell;
+    const int i = (int)(r % m.nc1);
+    r /= m.nc1;
+    const int j = (int)(r % m.nc2);
+    const int k = (int)(r / m.nc2);
+    const double lw = 0.5, rw = 0.5;
+    const double bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
+    const double bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
+    const double bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
+    const i64 vs = m.ncell;
+    const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
+    const i64 cb = cidx(m, b, 0, 3, k, j, i);
+    const Real gm1 = (Real)m.gamma - Real(1.0);
+    const Real dfl = (Real)m.dfloor, pfl = (Real)m.pfloor;
+    Real u_d = u[c], u_m1 = u[c + vs], u_m2 = u[c + 2 * vs], u_m3 = u[c + 3 * vs],
+         u_e = u[c + 4 * vs];
+    const Real bcc1 = (Real)bc1, bcc2 = (Real)bc2, bcc3 = (Real)bc3;
+    const bool dfloored = !(u_d > dfl);
+    u_d = (u_d > dfl) ? u_d : dfl;
+    Real di = Real(1.0) / u_d;
+    Real vx = u_m1 * di, vy = u_m2 * di, vz = u_m3 * di;
+    Real pb = Real(0.5) * (bcc1 * bcc1 + bcc2 * bcc2 + bcc3 * bcc3);
+    Real e_k = Real(0.5) * di * (u_m1 * u_m1 + u_m2 * u_m2 + u_m3 * u_m3);
+    Real w_p = gm1 * (u_e - e_k - pb);
+    const bool pfloored = !(w_p > pfl);
+    u_e = (w_p > pfl) ? u_e : ((pfl / gm1) + e_k + pb);
+    w_p = (w_p > pfl) ? w_p : pfl;
+    if (dfloored) {
+      u[c] = u_d;
+      if (KAHAN && ulo) ulo[c] = Real(0);
+    }
+    if (pfloored) {
+      u[c + 4 * vs] = u_e;
+      if (KAHAN && ulo) ulo[c + 4 * vs] = Real(0);
+    }
+    if ((dfloored || pfloored) && do_dt) atomicAdd(&clk->c2p_floor_count, 1);
+    w[c] = u_d;
+    w[c + vs] = vx;
+    w[c + 2 * vs] = vy;
+    w[c + 3 * vs] = vz;
+    w[c + 4 * vs] = w_p;
+    bcc[cb] = bcc1;
+    bcc[cb + vs] = bcc2;
+    bcc[cb + 2 * vs] = bcc3;
+    if (do_dt && i >= m.is && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
+        k <= m.ke) {
+      // new_blockdt.cpp:80-103, evaluated in FP64 on the stored primitives
+      const double gam = m.gamma, wd = (double)u_d, wp = (double)w_p;
+      const double wb1 = (double)bcc1, wb2 = (double)bcc2, wb3 = (double)bcc3;
+      double dt1 = m.dx1f[(i64)b * m.nc1 + i], dt2 = m.dx2f[(i64)b * m.nc2 + j],
+             dt3 = m.dx3f[(i64)b * m.nc3 + k];
+      double bx = wb1 + fabs(b1[f1idx(m, b, k, j, i)] - wb1);
+      double cf = fast_ms<double>(gam, wd, wp, wb2, wb3, bx);
+      double speed = smax<double>(0.0, (fabs((double)vx) + cf));
+      dt1 /= (speed);
+      bx = wb2 + fabs(b2[f2idx(m, b, k, j, i)] - wb2);
+      cf = fast_ms<double>(gam, wd, wp, wb3, wb1, bx);
+      speed = smax<double>(0.0, (fabs((double)vy) + cf));
+      dt2 /= (speed);
+      bx = wb3 + fabs(b3[f3idx(m, b, k, j, i)] - wb3);
+      cf = fast_ms<double>(gam, wd, wp, wb1, wb2, bx);
+      speed = smax<double>(0.0, (fabs((double)vz) + cf));
+      dt3 /= (speed);
+      cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
+    }
+  }
+  if (do_dt) {
+    double v = warp_min(cell_dt);
+    if ((threadIdx.x & 31) == 0 && v < 1.0e300)
+      atomicMin(&clk->dtmin_bits, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// Mesh::NewTimeStep (mesh.cpp:1236-1281) after the main loop's time += dt
+// (main.cpp:535): dt = min(2 dt_old, cfl * min cell dt), clipped to tlim.
+static __global__ void advance_clock_kernel(DevClock* clk, double cfl, double tlim, int advance) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (advance) clk->time = clk->time + clk->dt;
+  double block_dt = __longlong_as_double((long long)clk->dtmin_bits) * cfl;
+  double dt = 2.0 * clk->dt;
+  dt = smin<double>(dt, block_dt);
+  if (clk->time < tlim && (tlim - clk->time) < dt) dt = tlim - clk->time;
+  clk->dt = dt;
+  clk->dtmin_bits = 0x7fefffffffffffffULL;  // DBL_MAX for the next reduction
+}
+
+}  // namespace athgpu

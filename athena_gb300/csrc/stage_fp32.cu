@@ -1,0 +1,12 @@
+// FP32 stage update: reconstruction, Riemann solvers, corner EMFs and the flux
+// divergence in FP32 with a compensated (Kahan) conserved update; the face field, the CT
+// update and the time step stay FP64.
+#include "stage_impl.cuh"
+
+namespace athgpu {
+cudaError_t stage_fp32(athgpu_ctx* c, int stage) {
+  if (stage == 0) return run_end_cycle(c);
+  return run_stage<float, 1>(c, stage);
+}
+cudaError_t init_fp32(athgpu_ctx* c) { return run_init<float, 1>(c); }
+}  // namespace athgpu

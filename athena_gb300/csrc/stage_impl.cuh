@@ -1,0 +1,139 @@
+// Host-side stage driver, templated on the bulk precision.  Included by stage_fp64.cu
+// (compiled without FMA contraction, -fmad=false, for bit parity with the reference) and
+// stage_fp32.cu (FMA contraction on).
+#pragma once
+#include "ctx.h"
+
+namespace athgpu {
+
+static inline unsigned nblk(long long n, int tpb) {
+  return (unsigned)((n + tpb - 1) / tpb);
+}
+
+template <typename Real, int ORDER, int RS>
+static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const double* b1,
+                          const double* b2, const double* b3) {
+  const DevMesh& m = c->m;
+  Registers& r = c->r;
+  cudaStream_t s = c->stream;
+  {
+    const long long cells = (long long)m.nb * (m.nx3 + 2) * (m.nx2 + 2) * (m.nx1 + 2);
+    const long long warps = (cells + 30) / 31;
+    ProfScope ps(c, "flux_x1");
+    flux_x1_kernel<Real, ORDER, RS><<<nblk(warps * 32, 128), 128, 0, s>>>(
+        m, w, bcc, b1, c->clk, (Real*)r.flx1, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f);
+  }
+  {
+    int seg = c->lc.seg_x2 > 0 ? c->lc.seg_x2 : m.nx2 + 1;
+    const long long nseg = (m.nx2 + 1 + seg - 1) / seg;
+    const long long n = nseg * m.nb * (m.nx3 + 2) * (long long)(m.nx1 + 2);
+    ProfScope ps(c, "flux_x2");
+    flux_sweep_kernel<Real, 1, ORDER, RS><<<nblk(n, 128), 128, 0, s>>>(
+        m, seg, w, bcc, b2, c->clk, (Real*)r.flx2, (Real*)r.e1x2, (Real*)r.e3x2,
+        (Real*)r.w2f);
+  }
+  {
+    int seg = c->lc.seg_x3 > 0 ? c->lc.seg_x3 : m.nx3 + 1;
+    const long long nseg = (m.nx3 + 1 + seg - 1) / seg;
+    const long long n = nseg * m.nb * (m.nx2 + 2) * (long long)(m.nx1 + 2);
+    ProfScope ps(c, "flux_x3");
+    flux_sweep_kernel<Real, 2, ORDER, RS><<<nblk(n, 128), 128, 0, s>>>(
+        m, seg, w, bcc, b3, c->clk, (Real*)r.flx3, (Real*)r.e2x3, (Real*)r.e1x3,
+        (Real*)r.w3f);
+  }
+  c->launches += 3;
+}
+
+template <typename Real, int KAHAN>
+static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* b2,
+                                    double* b3, int do_dt) {
+  const DevMesh& m = c->m;
+  cudaStream_t s = c->stream;
+  const long long nc = (long long)m.nb * m.ncell;
+  {
+    ProfScope ps(c, "exchange_u");
+    exchange_kernel<Real, 0><<<nblk(nc, 256), 256, 0, s>>>(m, NHYDRO, u);
+  }
+  {
+    ProfScope ps(c, "exchange_b");
+    exchange_kernel<double, 1><<<nblk((long long)m.nb * m.nf1, 256), 256, 0, s>>>(m, 1, b1);
+    exchange_kernel<double, 2><<<nblk((long long)m.nb * m.nf2, 256), 256, 0, s>>>(m, 1, b2);
+    exchange_kernel<double, 3><<<nblk((long long)m.nb * m.nf3, 256), 256, 0, s>>>(m, 1, b3);
+  }
+  // the compensation register belongs to U only; the stage-1 register U* has none
+  Real* lo = (u == (Real*)c->r.u) ? (Real*)c->r.ulo : nullptr;
+  ProfScope ps(c, "c2p");
+  c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
+      m, do_dt, b1, b2, b3, u, lo, (Real*)c->r.w, (Real*)c->r.bcc, c->clk);
+  c->launches += 5;
+}
+
+template <typename Real, int KAHAN>
+static cudaError_t run_stage(athgpu_ctx* c, int stage) {
+  const DevMesh& m = c->m;
+  Registers& r = c->r;
+  cudaStream_t s = c->stream;
+  const int order = (stage == 1) ? 1 : c->desc.xorder;
+  const double beta = (stage == 1) ? 0.5 : 1.0;
+  // stage 1 reads U^n, B^n and writes U*, B*; stage 2 reads W*, B* and updates U, B
+  const double* bb1 = (stage == 1) ? r.b1 : r.bs1;
+  const double* bb2 = (stage == 1) ? r.b2 : r.bs2;
+  const double* bb3 = (stage == 1) ? r.b3 : r.bs3;
+  const Real* w = (const Real*)r.w;
+  const Real* bcc = (const Real*)r.bcc;
+  const int rs = c->desc.rsolver;
+#define FLUX(O, R) launch_fluxes<Real, O, R>(c, w, bcc, bb1, bb2, bb3)
+  if (order == 1) { if (rs == 0) FLUX(1, 0); else FLUX(1, 1); }
+  else if (order == 2) { if (rs == 0) FLUX(2, 0); else FLUX(2, 1); }
+  else { if (rs == 0) FLUX(3, 0); else FLUX(3, 1); }
+#undef FLUX
+  {
+    const long long n = (long long)m.nb * (m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
+    ProfScope ps(c, "corner_e");
+    corner_e_kernel<Real><<<nblk(n, 128), 128, 0, s>>>(
+        m, w, bcc, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f, (Real*)r.e1x2,
+        (Real*)r.e3x2, (Real*)r.w2f, (Real*)r.e1x3, (Real*)r.e2x3, (Real*)r.w3f,
+        (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
+  }
+  Real* uout = (stage == 1) ? (Real*)r.ustar : (Real*)r.u;
+  {
+    const long long n = (long long)m.nb * m.nx3 * m.nx2 * m.nx1;
+    ProfScope ps(c, "update");
+    update_kernel<Real, KAHAN><<<nblk(n, 128), 128, 0, s>>>(
+        m, beta, stage, c->clk, (Real*)r.flx1, (Real*)r.flx2, (Real*)r.flx3, (Real*)r.u,
+        uout, (Real*)r.ulo);
+  }
+  double* o1 = (stage == 1) ? r.bs1 : r.b1;
+  double* o2 = (stage == 1) ? r.bs2 : r.b2;
+  double* o3 = (stage == 1) ? r.bs3 : r.b3;
+  {
+    const long long per = (long long)m.nx3 * m.nx2 * (m.nx1 + 1) +
+                          (long long)m.nx3 * (m.nx2 + 1) * m.nx1 +
+                          (long long)(m.nx3 + 1) * m.nx2 * m.nx1;
+    ProfScope ps(c, "ct");
+    ct_kernel<Real><<<nblk(per * m.nb, 128), 128, 0, s>>>(
+        m, beta, c->clk, (Real*)r.e1, (Real*)r.e2, (Real*)r.e3, r.b1, r.b2, r.b3, o1, o2,
+        o3);
+  }
+  c->launches += 3;
+  launch_exchange_and_c2p<Real, KAHAN>(c, uout, o1, o2, o3, stage == 2);
+  return cudaGetLastError();
+}
+
+// end of a main-loop cycle: time += dt, Mesh::NewTimeStep (main.cpp:535-541)
+static inline cudaError_t run_end_cycle(athgpu_ctx* c) {
+  ProfScope ps(c, "advance_clock");
+  advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->clk, c->m.cfl, c->m.tlim, 1);
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+template <typename Real, int KAHAN>
+static cudaError_t run_init(athgpu_ctx* c) {
+  launch_exchange_and_c2p<Real, KAHAN>(c, (Real*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1);
+  advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->clk, c->m.cfl, c->m.tlim, 0);
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace athgpu

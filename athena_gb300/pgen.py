@@ -330,7 +330,7 @@ def solenoidal_velocity(nx, kmin, kmax, seed):
     ksq = np.where(kk > 0, kk * kk, 1.0)
     div = (kvec[0] * vk[0] + kvec[1] * vk[1] + kvec[2] * vk[2]) / ksq
     vk = [vk[d] - kvec[d] * div for d in range(3)]
-    v = np.stack([np.fft.irfftn(vk[d], s=(n3, n2, n1)) for d in range(3)])
+    v = np.stack([np.fft.irfftn(vk[d], s=(n3, n2, n1), axes=(0, 1, 2)) for d in range(3)])
     rms = np.sqrt(np.mean(np.sum(v * v, axis=0)))
     return v / rms
 

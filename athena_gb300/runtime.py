@@ -1,0 +1,247 @@
+"""Python binding of the C ABI (include/athena_gb300.h) over ctypes.
+
+``StageUpdate`` mirrors how the reference drives the hot path: construct it for a
+uniform mesh (the MeshBlock/Coordinates set-up), load the conserved state and face field
+(what MeshBlock::ProblemGenerator produces), ``initialize()`` (the tail of
+Mesh::Initialize), then ``cycle()`` / ``run_until()`` (the main loop over
+TimeIntegratorTaskList stages).  There is no CPU fallback: if the CUDA library is
+missing or no GPU is present, construction raises.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from .mesh import MeshSpec
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libathgpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300.h")
+
+HLLD, HLLE = 0, 1
+FP64, FP32 = 0, 1
+
+
+class AthGPUError(RuntimeError):
+    pass
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("nbx1", ctypes.c_int), ("nbx2", ctypes.c_int), ("nbx3", ctypes.c_int),
+                ("nx1", ctypes.c_int), ("nx2", ctypes.c_int), ("nx3", ctypes.c_int),
+                ("nghost", ctypes.c_int), ("xorder", ctypes.c_int),
+                ("rsolver", ctypes.c_int), ("precision", ctypes.c_int),
+                ("relativistic", ctypes.c_int), ("gamma", ctypes.c_double),
+                ("dfloor", ctypes.c_double), ("pfloor", ctypes.c_double),
+                ("cfl_number", ctypes.c_double), ("tlim", ctypes.c_double),
+                ("x1f", ctypes.POINTER(ctypes.c_double)),
+                ("dx1f", ctypes.POINTER(ctypes.c_double)),
+                ("x2f", ctypes.POINTER(ctypes.c_double)),
+                ("dx2f", ctypes.POINTER(ctypes.c_double)),
+                ("x3f", ctypes.POINTER(ctypes.c_double)),
+                ("dx3f", ctypes.POINTER(ctypes.c_double))]
+
+
+class DeviceState(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p), ("ulo", ctypes.c_void_p), ("w", ctypes.c_void_p),
+                ("bcc", ctypes.c_void_p), ("b1", ctypes.c_void_p), ("b2", ctypes.c_void_p),
+                ("b3", ctypes.c_void_p), ("real_bytes", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load libathgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise AthGPUError("libathgpu.so is missing: run athena_gb300.build.build() first")
+    L = ctypes.CDLL(path)
+    vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
+    sig = {
+        "athgpu_create": ([ctypes.POINTER(vp), ctypes.POINTER(MeshDesc)], ip),
+        "athgpu_destroy": ([vp], ip),
+        "athgpu_set_stream": ([vp, vp], ip),
+        "athgpu_upload_state": ([vp, dp, dp, dp, dp], ip),
+        "athgpu_download_state": ([vp, dp, dp, dp, dp], ip),
+        "athgpu_download_prim": ([vp, dp, dp], ip),
+        "athgpu_initialize": ([vp], ip),
+        "athgpu_stage": ([vp, ip], ip),
+        "athgpu_cycle": ([vp, ip], ip),
+        "athgpu_run_until": ([vp, ctypes.c_double, ip, ctypes.POINTER(ip)], ip),
+        "athgpu_get_clock": ([vp, dp, dp], ip),
+        "athgpu_set_clock": ([vp, ctypes.c_double, ctypes.c_double], ip),
+        "athgpu_synchronize": ([vp], ip),
+        "athgpu_floor_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
+        "athgpu_device_state_ptrs": ([vp, ctypes.POINTER(DeviceState)], ip),
+        "athgpu_set_sweep_segment": ([vp, ip, ip], ip),
+        "athgpu_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
+        "athgpu_profile_cycle": ([vp, ip, ctypes.POINTER(ctypes.c_float),
+                                  ctypes.POINTER(ip)], ip),
+        "athgpu_profile_label": ([vp, ip], ctypes.c_char_p),
+        "athgpu_last_error": ([], ctypes.c_char_p),
+        "athgpu_version": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes, f.restype = args, res
+    _lib = L
+    return L
+
+
+def header_functions(path=HEADER):
+    """Names of the functions declared in include/athena_gb300.h."""
+    import re
+    text = open(path).read()
+    return sorted(set(re.findall(r"\b(athgpu_[a-z_0-9]+)\s*\(", text)))
+
+
+def _check(status, what):
+    if status != 0:
+        msg = load_library().athgpu_last_error().decode()
+        raise AthGPUError("%s failed (%d): %s" % (what, status, msg))
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def default_floor():
+    """sqrt(1024 * FLT_MIN), the reference's dfloor/pfloor default
+    (adiabatic_mhd.cpp:29-30)."""
+    return math.sqrt(1024 * float(np.finfo(np.float32).tiny))
+
+
+class StageUpdate:
+    """All MeshBlocks of one uniform mesh advanced by the GPU stage update."""
+
+    def __init__(self, mesh: MeshSpec, gamma, xorder=2, rsolver="hlld", precision="fp64",
+                 cfl=0.3, tlim=1.0e30, dfloor=None, pfloor=None):
+        L = load_library()
+        self.mesh = mesh
+        self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
+        fl = default_floor()
+        d = MeshDesc()
+        d.nbx1, d.nbx2, d.nbx3 = mesh.nb
+        d.nx1, d.nx2, d.nx3 = mesh.bx
+        d.nghost, d.xorder = mesh.ng, xorder
+        d.rsolver = HLLD if rsolver == "hlld" else HLLE
+        d.precision = FP64 if precision == "fp64" else FP32
+        d.relativistic = 0
+        d.gamma = gamma
+        d.dfloor = fl if dfloor is None else dfloor
+        d.pfloor = fl if pfloor is None else pfloor
+        d.cfl_number, d.tlim = cfl, tlim
+        d.x1f, d.dx1f, d.x2f, d.dx2f, d.x3f, d.dx3f = [_dp(c) for c in self.coords]
+        self.desc = d
+        h = ctypes.c_void_p()
+        _check(L.athgpu_create(ctypes.byref(h), ctypes.byref(d)), "athgpu_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().athgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- state ------------------------------------------------------------------------
+    def set_state(self, u, b1, b2, b3):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, b1, b2, b3)]
+        _check(load_library().athgpu_upload_state(self.h, *[_dp(a) for a in arrs]),
+               "athgpu_upload_state")
+
+    def state(self):
+        m = self.mesh
+        u = np.zeros((m.nblocks, 5) + m.cell_shape)
+        b = [np.zeros((m.nblocks,) + s) for s in m.face_shapes]
+        _check(load_library().athgpu_download_state(self.h, _dp(u), *[_dp(x) for x in b]),
+               "athgpu_download_state")
+        return u, b[0], b[1], b[2]
+
+    def prim(self):
+        m = self.mesh
+        w = np.zeros((m.nblocks, 5) + m.cell_shape)
+        bcc = np.zeros((m.nblocks, 3) + m.cell_shape)
+        _check(load_library().athgpu_download_prim(self.h, _dp(w), _dp(bcc)),
+               "athgpu_download_prim")
+        return w, bcc
+
+    # --- time integration -------------------------------------------------------------
+    def initialize(self):
+        _check(load_library().athgpu_initialize(self.h), "athgpu_initialize")
+
+    def stage(self, s):
+        _check(load_library().athgpu_stage(self.h, s), "athgpu_stage")
+
+    def cycle(self, n=1):
+        _check(load_library().athgpu_cycle(self.h, n), "athgpu_cycle")
+
+    def run_until(self, tlim, max_cycles=1 << 30):
+        n = ctypes.c_int(0)
+        _check(load_library().athgpu_run_until(self.h, tlim, max_cycles, ctypes.byref(n)),
+               "athgpu_run_until")
+        return n.value
+
+    def synchronize(self):
+        _check(load_library().athgpu_synchronize(self.h), "athgpu_synchronize")
+
+    def clock(self):
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        _check(load_library().athgpu_get_clock(self.h, ctypes.byref(t), ctypes.byref(dt)),
+               "athgpu_get_clock")
+        return t.value, dt.value
+
+    @property
+    def time(self):
+        return self.clock()[0]
+
+    @property
+    def dt(self):
+        return self.clock()[1]
+
+    def set_clock(self, time, dt):
+        _check(load_library().athgpu_set_clock(self.h, time, dt), "athgpu_set_clock")
+
+    def floor_count(self, reset=False):
+        n = ctypes.c_longlong()
+        _check(load_library().athgpu_floor_count(self.h, ctypes.byref(n), int(reset)),
+               "athgpu_floor_count")
+        return n.value
+
+    def launch_count(self, reset=False):
+        n = ctypes.c_longlong()
+        _check(load_library().athgpu_launch_count(self.h, ctypes.byref(n), int(reset)),
+               "athgpu_launch_count")
+        return n.value
+
+    def profile_cycle(self):
+        """One non-graph cycle with per-kernel CUDA-event timings: [(name, ms), ...]."""
+        L = load_library()
+        buf = (ctypes.c_float * 256)()
+        n = ctypes.c_int()
+        _check(L.athgpu_profile_cycle(self.h, 256, buf, ctypes.byref(n)),
+               "athgpu_profile_cycle")
+        return [(L.athgpu_profile_label(self.h, i).decode(), buf[i])
+                for i in range(min(n.value, 256))]
+
+    def set_sweep_segment(self, seg_x2, seg_x3):
+        _check(load_library().athgpu_set_sweep_segment(self.h, seg_x2, seg_x3),
+               "athgpu_set_sweep_segment")
+
+    def set_stream(self, stream_ptr):
+        _check(load_library().athgpu_set_stream(self.h, ctypes.c_void_p(stream_ptr)),
+               "athgpu_set_stream")
+
+    def device_state(self):
+        s = DeviceState()
+        _check(load_library().athgpu_device_state_ptrs(self.h, ctypes.byref(s)),
+               "athgpu_device_state_ptrs")
+        return s

@@ -1,0 +1,150 @@
+/* athena_gb300 — GB300-native MHD stage update behind a C ABI.
+ *
+ * The library advances every MeshBlock of a uniform, single-level, periodic 3-D mesh
+ * through the reference's (Athena++) VL2 stage update on one GPU.  Arrays cross the
+ * boundary as plain pointers in the reference's AthenaArray layout (last index fastest,
+ * ghosts included, athena_arrays.hpp:140-143), with all MeshBlocks back to back in
+ * lexicographic block order b = (lx3*nbx2 + lx2)*nbx1 + lx1:
+ *   cells  u, w        [nb][5][nc3][nc2][nc1]      (ncN = nxN + 2*nghost)
+ *          bcc         [nb][3][nc3][nc2][nc1]
+ *   faces  b.x1f       [nb][nc3][nc2][nc1+1]
+ *          b.x2f       [nb][nc3][nc2+1][nc1]
+ *          b.x3f       [nb][nc3+1][nc2][nc1]
+ * Host pointers are FP64 (Real = double, the reference's default build); the FP32
+ * precision mode converts on upload/download.
+ *
+ * Every call returns an athgpu_status: 0 on success, a negative code on failure; the
+ * message of the last failure on the calling thread is athgpu_last_error().
+ * Calls on one context are not thread-safe (the reference runs one OpenMP thread per
+ * MeshBlock at a time, task_list.cpp:71-82).
+ */
+#ifndef ATHENA_GB300_H_
+#define ATHENA_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int athgpu_status;
+#define ATHGPU_OK 0
+#define ATHGPU_ERR_ARG (-1)      /* invalid argument */
+#define ATHGPU_ERR_CUDA (-2)     /* CUDA runtime error (message has the CUDA string) */
+#define ATHGPU_ERR_UNSUPPORTED (-3)
+#define ATHGPU_ERR_STATE (-4)    /* call out of order (e.g. stage before initialize) */
+
+#define ATHGPU_HLLD 0            /* --flux=hlld  (hydro/rsolvers/mhd/hlld.cpp) */
+#define ATHGPU_HLLE 1            /* --flux=hlle  (hydro/rsolvers/mhd/hlle_mhd.cpp) */
+#define ATHGPU_FP64 0            /* every operation in FP64: bit-identical to the reference */
+#define ATHGPU_FP32 1            /* FP32 reconstruction/Riemann/divergence, compensated
+                                    (Kahan) conserved update, FP64 CT and time step */
+
+typedef struct athgpu_ctx athgpu_ctx;
+
+/* Mesh and physics description.  Replaces the configuration the reference reads in
+ * the Mesh/MeshBlock constructors (mesh.cpp:100-400, <mesh>/<meshblock>/<time>/<hydro>
+ * input blocks, parameter_input.cpp) and fixes at create time what configure.py fixes at
+ * compile time (NGHOST, the Riemann solver, configure.py:451-531). */
+typedef struct {
+  int nbx1, nbx2, nbx3;   /* MeshBlocks per direction (mesh/nx / meshblock/nx) */
+  int nx1, nx2, nx3;      /* interior cells per MeshBlock (meshblock/nx1..3) */
+  int nghost;             /* NGHOST: 2 for PLM, >= 3 for PPM (reconstruction.cpp:117-127) */
+  int xorder;             /* time/xorder: 2 = PLM, 3 = PPM (stage 1 is donor cell) */
+  int rsolver;            /* ATHGPU_HLLD or ATHGPU_HLLE */
+  int precision;          /* ATHGPU_FP64 or ATHGPU_FP32 */
+  int relativistic;       /* must be 0 in this version */
+  double gamma;           /* hydro/gamma */
+  double dfloor, pfloor;  /* hydro/dfloor, hydro/pfloor (adiabatic_mhd.cpp:29-30) */
+  double cfl_number;      /* time/cfl_number */
+  double tlim;            /* time/tlim: the time step is clipped to it (mesh.cpp:1271) */
+  /* per-block coordinate arrays exactly as Coordinates holds them (coordinates.cpp:92-146):
+   * x?f [nb][nc?+1] face positions, dx?f [nb][nc?] face spacings (host memory) */
+  const double *x1f, *dx1f, *x2f, *dx2f, *x3f, *dx3f;
+} athgpu_mesh_desc;
+
+/* Allocate all device registers of the stage update for the mesh (replaces the
+ * Hydro/Field/EquationOfState/Reconstruction constructors, hydro.cpp:31-148,
+ * field.cpp:27-105). */
+athgpu_status athgpu_create(athgpu_ctx **ctx, const athgpu_mesh_desc *desc);
+athgpu_status athgpu_destroy(athgpu_ctx *ctx);
+
+/* Use a caller-provided CUDA stream (cudaStream_t passed as void*) for all work;
+ * NULL restores the context's own stream. */
+athgpu_status athgpu_set_stream(athgpu_ctx *ctx, void *stream);
+
+/* Host <-> device copies of the conserved state U = phydro->u and the face field
+ * B = pfield->b (the arrays MeshBlock::ProblemGenerator fills and restart.cpp:193-201
+ * writes); any pointer may be NULL to skip that array.  Synchronous. */
+athgpu_status athgpu_upload_state(athgpu_ctx *ctx, const double *u, const double *b1,
+                                  const double *b2, const double *b3);
+athgpu_status athgpu_download_state(athgpu_ctx *ctx, double *u, double *b1, double *b2,
+                                    double *b3);
+/* primitives W = phydro->w and bcc = pfield->bcc of the last conserved->primitive call */
+athgpu_status athgpu_download_prim(athgpu_ctx *ctx, double *w, double *bcc);
+
+/* Tail of Mesh::Initialize (mesh.cpp:1698-1833 and :1959-1964): ghost exchange of U and
+ * B, EquationOfState::ConservedToPrimitive over whole blocks, NewBlockTimeStep and
+ * Mesh::NewTimeStep. */
+athgpu_status athgpu_initialize(athgpu_ctx *ctx);
+
+/* One VL2 stage for all MeshBlocks, i.e. the MHD task list of
+ * TimeIntegratorTaskList::DoTaskListOneStage for stage 1 or 2
+ * (time_integrator.cpp:904-1208): CalculateHydroFlux (donor cell on stage 1,
+ * :1700-1703) -> Hydro::CalculateFluxes + RiemannSolver; CalculateEMF ->
+ * Field::ComputeCornerE; Send/ReceiveFluxCorrection (same-level EMF averaging);
+ * IntegrateHydro -> WeightedAve + Hydro::AddFluxDivergence; IntegrateField ->
+ * WeightedAve + Field::CT; ghost exchange of U and B; Primitives ->
+ * EquationOfState::ConservedToPrimitive; on stage 2 NewBlockTimeStep.  Asynchronous on
+ * the context's stream. */
+athgpu_status athgpu_stage(athgpu_ctx *ctx, int stage);
+
+/* ncycles full cycles of the main loop (main.cpp:457-541): both stages, time += dt,
+ * Mesh::NewTimeStep.  The cycle is captured once into a CUDA graph and replayed; dt and
+ * time stay on the device.  Asynchronous on the context's stream. */
+athgpu_status athgpu_cycle(athgpu_ctx *ctx, int ncycles);
+
+/* Run whole cycles while time < tlim (main.cpp:457-458), at most max_cycles; returns the
+ * number of cycles run in *ncycles_run. Synchronous. */
+athgpu_status athgpu_run_until(athgpu_ctx *ctx, double tlim, int max_cycles,
+                               int *ncycles_run);
+
+/* Mesh::time and Mesh::dt (synchronous read). */
+athgpu_status athgpu_get_clock(athgpu_ctx *ctx, double *time, double *dt);
+athgpu_status athgpu_set_clock(athgpu_ctx *ctx, double time, double dt);
+
+/* Wait for the context's stream. */
+athgpu_status athgpu_synchronize(athgpu_ctx *ctx);
+
+/* Cells whose density or pressure floor was applied by the conserved->primitive calls
+ * that computed a time step since the last reset (adiabatic_mhd.cpp:65-84). */
+athgpu_status athgpu_floor_count(athgpu_ctx *ctx, long long *count, int reset);
+
+/* Device pointers of the registers, for callers that keep their data on the GPU
+ * (u and ustar: Real = double in FP64 mode, float in FP32 mode). */
+typedef struct {
+  void *u, *ulo, *w, *bcc;
+  double *b1, *b2, *b3;
+  int real_bytes;
+} athgpu_device_state;
+athgpu_status athgpu_device_state_ptrs(athgpu_ctx *ctx, athgpu_device_state *out);
+
+/* Launch tiling of the x2/x3 flux sweeps: faces per thread along the sweep (the
+ * autotuner's knob); 0 = heuristic default. */
+athgpu_status athgpu_set_sweep_segment(athgpu_ctx *ctx, int seg_x2, int seg_x3);
+
+/* Run one cycle without the CUDA graph, timing every kernel launch with CUDA events on
+ * the context's stream; ms[i] (i < cap) receives the duration of launch i, *count the
+ * number of launches, athgpu_profile_label(ctx, i) its kernel name.  The state advances
+ * by one cycle.  Synchronous. */
+athgpu_status athgpu_profile_cycle(athgpu_ctx *ctx, int cap, float *ms, int *count);
+const char *athgpu_profile_label(athgpu_ctx *ctx, int idx);
+
+/* Number of kernels the library launched since the last reset. */
+athgpu_status athgpu_launch_count(athgpu_ctx *ctx, long long *count, int reset);
+
+const char *athgpu_last_error(void);
+const char *athgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATHENA_GB300_H_ */

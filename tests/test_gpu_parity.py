@@ -1,0 +1,190 @@
+"""Parity of the CUDA stage update (through the C ABI) with the reference and the oracle.
+
+FP64 mode must be bit-identical: per-cell conserved variables, face fields and the time
+step sequence.  FP32 mode is compared with FP64 within stated tolerances.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+from athena_gb300 import build, pgen
+from athena_gb300.mesh import MeshSpec
+from athena_gb300.runtime import StageUpdate
+from golden_cases import case_names, interior_faces, load_case, meta
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    build.build()
+
+
+def _faces(mesh, bs):
+    return [interior_faces(mesh, b) for b in bs]
+
+
+def _run_gpu(mesh, c, ic, ncycle, precision="fp64"):
+    g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
+                    precision=precision, cfl=c["cfl"], tlim=c["tlim"])
+    g.set_state(*ic)
+    g.initialize()
+    dts = []
+    for _ in range(ncycle):
+        dts.append(g.dt)
+        g.cycle(1)
+    out = g.state()
+    w, bcc = g.prim()
+    g.close()
+    return out, np.array(dts), w, bcc
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_fp64_matches_reference_bitwise(name):
+    c, mesh, ic, ref = load_case(name)
+    (u, b1, b2, b3), dts, _, _ = _run_gpu(mesh, c, ic, c["ncycle"])
+    assert np.array_equal(dts, ref["dt"])
+    assert np.array_equal(mesh.interior(u), ref["u"])
+    for got, want in zip(_faces(mesh, (b1, b2, b3)), (ref["b1"], ref["b2"], ref["b3"])):
+        assert np.array_equal(got, want)
+
+
+def test_config1_full_period_bitwise_and_l1():
+    """Config 1: 64x32x32 fast wave, VL2 + PLM + HLLD, one period (72 cycles): final
+    state hash and L1 error line equal to the reference's."""
+    g0 = meta()["config1_linear_wave"]
+    mesh = MeshSpec((64, 32, 32), (1, 1, 1), 2, (0., 0., 0.), (3.0, 1.5, 1.5))
+    lw = pgen.LinearWave(mesh, gamma=1.666666666666667)
+    g = StageUpdate(mesh, lw.gam, xorder=2, rsolver="hlld", tlim=lw.period())
+    g.set_state(*lw.generate())
+    g.initialize()
+    n = g.run_until(lw.period())
+    assert n == g0["ncycle"]
+    u, b1, b2, b3 = g.state()
+    w, bcc = g.prim()
+    ng = mesh.ng
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(mesh.interior(u)).tobytes())
+    for b in (b1, b2, b3):
+        h.update(np.ascontiguousarray(b[:, ng:-ng, ng:-ng, ng:-ng]).tobytes())
+    rms, l1, _ = lw.l1_errors(u, bcc)
+    fields = g0["errors"].split()
+    assert "%e" % rms == fields[4]
+    assert h.hexdigest() == g0["sha256_final"]
+
+
+def _turb_case(nx=(32, 32, 32), nb=(2, 2, 2), ng=3, xorder=3, rsolver="hlld", seed=11,
+               mach=2.0):
+    mesh = MeshSpec(nx, nb, ng)
+    gu, f1, f2, f3 = pgen.turbulence(nx, seed=seed, mach=mach)
+    ic = (mesh.scatter_cells(gu),) + mesh.scatter_faces(f1, f2, f3)
+    c = {"gamma": 5.0 / 3.0, "xorder": xorder, "rsolver": rsolver, "cfl": 0.3,
+         "tlim": 1.0e3}
+    return mesh, ic, c
+
+
+@pytest.mark.parametrize("xorder,rsolver,nb", [(3, "hlld", (2, 2, 2)),
+                                               (2, "hlle", (4, 2, 1)),
+                                               (2, "hlld", (1, 1, 1))])
+def test_fp64_matches_oracle_bitwise(xorder, rsolver, nb):
+    mesh, ic, c = _turb_case(nb=nb, xorder=xorder, rsolver=rsolver,
+                             ng=3 if xorder == 3 else 2)
+    (u, b1, b2, b3), dts, w, bcc = _run_gpu(mesh, c, ic, 4)
+    om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"])
+    om.set_state(*ic)
+    om.initialize()
+    odts = []
+    for _ in range(4):
+        odts.append(om.dt)
+        om.cycle()
+    uo, o1, o2, o3 = om.state()
+    wo, bcco = om.prim()
+    assert np.array_equal(dts, np.array(odts))
+    assert np.array_equal(mesh.interior(u), mesh.interior(uo))
+    assert np.array_equal(mesh.interior(w), mesh.interior(wo))
+    for a, b in zip(_faces(mesh, (b1, b2, b3)), _faces(mesh, (o1, o2, o3))):
+        assert np.array_equal(a, b)
+
+
+def _div_b(mesh, b1, b2, b3):
+    ng = mesh.ng
+    n1, n2, n3 = mesh.bx
+    d1 = b1[:, ng:ng + n3, ng:ng + n2, ng + 1:ng + n1 + 1] - b1[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
+    d2 = b2[:, ng:ng + n3, ng + 1:ng + n2 + 1, ng:ng + n1] - b2[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
+    d3 = b3[:, ng + 1:ng + n3 + 1, ng:ng + n2, ng:ng + n1] - b3[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
+    return d1 + d2 + d3   # times 1/dx for a cubic cell
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_div_b_stays_at_roundoff(precision):
+    mesh, ic, c = _turb_case()
+    (u, b1, b2, b3), _, _, _ = _run_gpu(mesh, c, ic, 5, precision=precision)
+    div = np.abs(_div_b(mesh, b1, b2, b3)).max()
+    bmax = max(np.abs(b1).max(), np.abs(b2).max(), np.abs(b3).max())
+    assert div / bmax < 1e-13
+
+
+def test_fp32_tracks_fp64():
+    """FP32 bulk + compensated update + FP64 CT stays within a small relative L1
+    distance of the FP64 path on a Mach-2 turbulent state after 5 cycles."""
+    mesh, ic, c = _turb_case()
+    (u64, *_), dt64, _, _ = _run_gpu(mesh, c, ic, 5, "fp64")
+    (u32, *_), dt32, _, _ = _run_gpu(mesh, c, ic, 5, "fp32")
+    a, b = mesh.interior(u64), mesh.interior(u32)
+    for n in range(5):
+        rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(a[:, n]).mean()
+        assert rel < 2e-5, (n, rel)
+    assert np.allclose(dt32, dt64, rtol=1e-5)
+
+
+def test_sweep_segments_do_not_change_results():
+    mesh, ic, c = _turb_case(nx=(16, 16, 16), nb=(1, 1, 1), xorder=2, ng=2)
+    outs = []
+    for seg in ((0, 0), (1, 1), (4, 5), (17, 3)):
+        g = StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlld", tlim=1e3)
+        g.set_sweep_segment(*seg)
+        g.set_state(*ic)
+        g.initialize()
+        g.cycle(2)
+        outs.append(g.state()[0])
+        g.close()
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_floors_match_oracle():
+    """A near-vacuum pocket drives the density and pressure floors of W(U)
+    (adiabatic_mhd.cpp:65-84); the floored cells match the oracle bit for bit."""
+    nx = (16, 16, 16)
+    mesh = MeshSpec(nx, (2, 1, 1), 2)
+    gu, f1, f2, f3 = pgen.turbulence(nx, seed=3, mach=3.0)
+    gu[0, 4:8, 4:8, 4:8] = 1e-12
+    gu[4, 4:8, 4:8, 4:8] = 1e-12
+    ic = (mesh.scatter_cells(gu),) + mesh.scatter_faces(f1, f2, f3)
+    c = {"gamma": 5.0 / 3.0, "xorder": 2, "rsolver": "hlle", "cfl": 0.3, "tlim": 1e3}
+    g = StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlle", tlim=1e3)
+    g.set_state(*ic)
+    g.initialize()
+    g.cycle(2)
+    g.synchronize()
+    assert g.floor_count() > 0
+    u = g.state()[0]
+    om = O.OracleMesh(mesh, c["gamma"], xorder=2, rsolver="hlle", tlim=1e3)
+    om.set_state(*ic)
+    om.initialize()
+    om.cycle(2)
+    assert np.array_equal(mesh.interior(u), mesh.interior(om.state()[0]))
+
+
+def test_graph_replay_counts_launches():
+    mesh, ic, c = _turb_case(nx=(16, 16, 16), nb=(2, 1, 1), xorder=2, ng=2)
+    g = StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlld", tlim=1e3)
+    g.set_state(*ic)
+    g.initialize()
+    g.launch_count(reset=True)
+    g.cycle(3)
+    g.synchronize()
+    per = g.launch_count() / 3
+    assert per == 2 * 11 + 1   # two stages of 11 kernels, one clock update
