@@ -1,0 +1,329 @@
+"""Benchmark: zone-cycles/s of the GPU MHD stage update on one GB300.
+
+Workload (one "step" = one full VL2 cycle, both stages, over the whole mesh): decaying
+MHD turbulence, 256^3 periodic unit box as 512 MeshBlocks of 32^3, rho = 1, plasma
+beta = 1 with uniform B along x, seeded solenoidal velocity with power in |k| in [1,4]
+at rms Mach 1, gamma = 5/3, VL2 + PPM + HLLD.  Synthetic inputs with those shapes.
+
+The headline ``value`` is the FP32 pipeline (FP32 reconstruction / Riemann / divergence
+with a compensated conserved update, FP64 CT and time step); the plain FP64 GPU path
+is timed on the same inputs beside it.  ``e2e`` runs the same cycles through the C ABI
+with the state uploaded from and downloaded to pinned host memory every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With torchrun (N > 1) every rank advances its own replica of the mesh on its own GPU
+(the path has no cross-GPU exchange on one-GPU hosts: replicas only).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("zone-cycles/s on 1 GB300: FP32+learned c2p vs plain FP64 GPU at equal L1 "
+          "error")
+NX, NB, NG = (256, 256, 256), (8, 8, 8), 3
+BYTES_PER_ZONE_CYCLE = {"fp32": 260.0, "fp64": 320.0}  # algorithmic HBM bytes
+ACC_CYCLES = 10   # cycles run by both paths for the FP32-vs-FP64 L1 comparison
+
+
+def workload_config(nx=NX, nb=NB):
+    return {"workload": "decaying MHD turbulence %dx%dx%d periodic as %d MeshBlocks of "
+                        "%dx%dx%d, VL2 + PPM + HLLD, gamma 5/3, beta 1, rms Mach 1" % (
+                            nx + (nb[0] * nb[1] * nb[2],) + tuple(nx[d] // nb[d]
+                                                               for d in range(3))),
+            "zones": nx[0] * nx[1] * nx[2], "meshblocks": nb[0] * nb[1] * nb[2],
+            "reconstruction": "PPM (stage 1 donor cell)", "riemann": "HLLD",
+            "integrator": "vl2", "cfl": 0.3,
+            "precision": "FP32 bulk + Kahan conserved update, FP64 CT and dt",
+            "l2": "inputs larger than L2 (0.56 GB per FP32 state register)"}
+
+
+def make_ic(nx=NX, nb=NB, ng=NG, seed=20261204):
+    from athena_gb300.mesh import MeshSpec
+    from athena_gb300 import pgen
+    mesh = MeshSpec(nx, nb, ng)
+    gu, f1, f2, f3 = pgen.turbulence(nx, seed=seed, mach=1.0, beta=1.0)
+    u = mesh.scatter_cells(gu)
+    b1, b2, b3 = mesh.scatter_faces(f1, f2, f3)
+    return mesh, (u, b1, b2, b3)
+
+
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                    timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------------------------
+def time_device_cycles(g, stream, steps, warmup):
+    """Cycles timed with CUDA events on the library's stream (inputs resident)."""
+    import torch
+    g.cycle(warmup)
+    g.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        s.record(stream)
+        g.cycle(steps)
+        e.record(stream)
+    e.synchronize()
+    return s.elapsed_time(e) / 1e3
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from athena_gb300 import build
+    from athena_gb300.runtime import StageUpdate
+    build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    mesh, ic = make_ic()
+    zones = mesh.nx[0] * mesh.nx[1] * mesh.nx[2]
+    stream = torch.cuda.Stream(device=dev)
+    res = {}
+    for prec in ("fp32", "fp64"):
+        g = StageUpdate(mesh, 5.0 / 3.0, xorder=3, rsolver="hlld", precision=prec, cfl=0.3)
+        g.set_stream(stream.cuda_stream)
+        g.set_state(*ic)
+        g.initialize()
+        steps = args.steps if prec == "fp32" else max(3, min(args.steps, 10))
+        sampler = ClockSampler(local_rank) if prec == "fp32" else None
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            with sampler:
+                dt = time_device_cycles(g, stream, steps, args.warmup)
+        else:
+            dt = time_device_cycles(g, stream, steps, args.warmup)
+        torch.cuda.synchronize()
+        if world > 1:
+            t = torch.tensor([dt], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        res[prec] = {"seconds": dt, "steps": steps, "value": world * zones * steps / dt,
+                     "ms_per_step": dt / steps * 1e3}
+        # accuracy: the same number of cycles from the same initial state in each path
+        g.set_state(*ic)
+        g.set_clock(0.0, 1.7976931348623157e308)
+        g.initialize()
+        g.cycle(ACC_CYCLES)
+        res["u_" + prec] = mesh.interior(g.state()[0])
+        if prec == "fp64":
+            res["profile64"] = g.profile_cycle()
+        else:
+            res["clocks"] = sampler.summary()
+            g.launch_count(reset=True)
+            g.cycle(1)
+            g.synchronize()
+            res["launches_per_step"] = g.launch_count()
+            res["profile32"] = g.profile_cycle()
+            # e2e through the C ABI with pinned host buffers
+            pinned = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+                      for a in ic]
+            for p, a in zip(pinned, ic):
+                p[...] = a
+            ebytes = sum(p.nbytes for p in pinned)
+            e_steps = max(2, min(args.steps, 10))
+            for _ in range(2):
+                g.set_state(*pinned)
+                g.cycle(1)
+                out = g.state()
+            torch.cuda.synchronize()
+            if world > 1:
+                dist.barrier()
+            t0 = time.perf_counter()
+            for _ in range(e_steps):
+                g.set_state(*pinned)    # host -> device (pinned) every step
+                g.cycle(1)
+                out = g.state()         # device -> host every step
+            torch.cuda.synchronize()
+            te = time.perf_counter() - t0
+            if world > 1:
+                t = torch.tensor([te], device=dev)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                te = float(t.item())
+            res["e2e"] = {"value": world * zones * e_steps / te, "unit": "zone-cycles/s",
+                          "h2d_bytes_per_step": ebytes, "d2h_bytes_per_step": ebytes,
+                          "steps": e_steps}
+        g.close()
+    return mesh, res
+
+
+def l1_rel(a, b):
+    return [float(np.abs(a[:, n] - b[:, n]).mean() / np.abs(b[:, n]).mean())
+            for n in range(a.shape[1])]
+
+
+def cpu_baseline(mesh_ic, cycles=2, threads=None):
+    """The oracle (C port of the reference algorithm, FP64, OpenMP over MeshBlocks) on the
+    host cores: `cycles` full cycles of the same 256^3 workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    mesh, ic = mesh_ic
+    threads = threads or os.cpu_count()
+    om = oracle.OracleMesh(mesh, 5.0 / 3.0, xorder=3, rsolver="hlld", cfl=0.3,
+                           threads=threads)
+    om.set_state(*ic)
+    om.initialize()
+    t0 = time.perf_counter()
+    om.cycle(cycles)
+    dt = time.perf_counter() - t0
+    zones = mesh.nx[0] * mesh.nx[1] * mesh.nx[2]
+    return {"value": zones * cycles / dt, "unit": "zone-cycles/s", "cores": threads,
+            "kind": "port", "sample": "%d full VL2 cycles of the 256^3 workload, FP64, "
+                                      "%d OpenMP threads" % (cycles, threads)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        mesh_ic = make_ic()
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        mesh, ic = mesh_ic
+        threads = os.cpu_count()
+        om = oracle.OracleMesh(mesh, 5.0 / 3.0, xorder=3, rsolver="hlld", cfl=0.3,
+                               threads=threads)
+        om.set_state(*ic)
+        om.initialize()
+        om.cycle(args.warmup)
+        t0 = time.perf_counter()
+        om.cycle(args.steps)
+        dt = time.perf_counter() - t0
+        zones = NX[0] * NX[1] * NX[2]
+        v = zones * args.steps / dt
+        line = {"metric": METRIC, "value": v, "unit": "zone-cycles/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "impl": "reference",
+                "config": workload_config(),
+                "cpu_baseline": {"value": v, "unit": "zone-cycles/s", "cores": threads,
+                                 "kind": "port",
+                                 "sample": "each step one full VL2 cycle of the 256^3 "
+                                           "workload, FP64, %d OpenMP threads" % threads},
+                "e2e": {"value": v, "unit": "zone-cycles/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    mesh, res = run_gpu(args, rank, world, local_rank)
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    zones = mesh.nx[0] * mesh.nx[1] * mesh.nx[2]
+    r32, r64 = res["fp32"], res["fp64"]
+    peak, peak_kind = measured_peaks()
+    # dominant unit: the whole VL2 cycle (CUDA graph of all stage kernels)
+    achieved = BYTES_PER_ZONE_CYCLE["fp32"] * zones / (r32["seconds"] / r32["steps"]) / 1e9
+    l1 = l1_rel(res["u_fp32"], res["u_fp64"])
+    line = {"metric": METRIC, "value": r32["value"], "unit": "zone-cycles/s",
+            "n_gpus": world, "steps": r32["steps"], "warmup": args.warmup,
+            "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(),
+            "fp64_gpu": {"value": r64["value"], "ms_per_step": r64["ms_per_step"],
+                         "steps": r64["steps"]},
+            "speedup_fp32_vs_fp64_gpu": r32["value"] / r64["value"],
+            "l1_rel_fp32_vs_fp64": {"cycles": ACC_CYCLES, "d": l1[0], "m1": l1[1],
+                                    "m2": l1[2], "m3": l1[3], "e": l1[4]},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "kernel": "vl2_cycle (CUDA graph, %d kernels)" %
+                                   res["launches_per_step"],
+                         "bytes_per_zone_cycle": BYTES_PER_ZONE_CYCLE["fp32"],
+                         "peak_kind": peak_kind},
+            "e2e": res["e2e"], "gpu_launches": res["launches_per_step"] * r32["steps"],
+            "clocks": res["clocks"],
+            "kernel_ms_fp32": res["profile32"], "kernel_ms_fp64": res["profile64"]}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline((mesh, make_ic()[1]))
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -379,6 +379,77 @@ static void hlle(double gamma, const double *wli, const double *wri, double bxi,
   for (int n = 0; n < NWAVE; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
 }
 
+/* FastMagnetosonicSpeedsGR with the SR metric (g00, g01, g11) = (-1, 0, 1),
+ * adiabatic_mhd_sr.cpp:350-370 */
+static void sr_fast_speeds(double gamma_adi, double wgas, double pgas, double u0, double u1,
+                           double b_sq, double *lp, double *lm) {
+  const double g00 = -1.0, g01 = 0.0, g11 = 1.0;
+  double cs_sq = gamma_adi * pgas / wgas;
+  double va_sq = b_sq / (b_sq + wgas);
+  double cms_sq = cs_sq + va_sq - cs_sq * va_sq;
+  double a = SQR(u0) - (g00 + SQR(u0)) * cms_sq;
+  double b = -2.0 * (u0 * u1 - (g01 + u0 * u1) * cms_sq);
+  double c = SQR(u1) - (g11 + SQR(u1)) * cms_sq;
+  double a1 = b / a;
+  double a0 = c / a;
+  double s = sqrt(smax(SQR(a1) - 4.0 * a0, 0.0));
+  *lp = (a1 >= 0.0) ? -2.0 * a0 / (a1 + s) : (-a1 + s) / 2.0;
+  *lm = (a1 >= 0.0) ? (-a1 - s) / 2.0 : -2.0 * a0 / (a1 - s);
+}
+
+/* SR frame-transforming HLLE, hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330 (SR branch).
+ * Local order as for hlld(); velocities are the spatial 4-velocity u^i. */
+static void hlle_sr(double gamma_adi, const double *wli, const double *wri, double bb1,
+                    double *f) {
+  double cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  double lml, lpl, lmr, lpr;
+  const double *wv[2] = {wli, wri};
+  double *cv[2] = {cl, cr}, *fv[2] = {fl, fr}, *lm[2] = {&lml, &lmr}, *lp[2] = {&lpl, &lpr};
+  for (int s = 0; s < 2; ++s) {
+    const double *w = wv[s];
+    double rho = w[IDN], pgas = w[IPR];
+    double u[4];
+    u[0] = sqrt(1.0 + SQR(w[IVX]) + SQR(w[IVY]) + SQR(w[IVZ]));
+    u[1] = w[IVX]; u[2] = w[IVY]; u[3] = w[IVZ];
+    double bb2 = w[IBY], bb3 = w[IBZ];
+    double b[4];
+    b[0] = bb1 * u[1] + bb2 * u[2] + bb3 * u[3];
+    b[1] = (bb1 + b[0] * u[1]) / u[0];
+    b[2] = (bb2 + b[0] * u[2]) / u[0];
+    b[3] = (bb3 + b[0] * u[3]) / u[0];
+    double b_sq = -SQR(b[0]) + SQR(b[1]) + SQR(b[2]) + SQR(b[3]);
+    double wgas = rho + gamma_adi / (gamma_adi - 1.0) * pgas;
+    sr_fast_speeds(gamma_adi, wgas, pgas, u[0], u[1], b_sq, lp[s], lm[s]);
+    double wtot = wgas + b_sq, ptot = pgas + 0.5 * b_sq;
+    double *c = cv[s], *f = fv[s];
+    /* local slots: 0 mass, 1..3 momenta (normal, t1, t2), 4 energy, 5/6 fields */
+    c[0] = rho * u[0];
+    c[4] = wtot * u[0] * u[0] - b[0] * b[0] - ptot;
+    c[1] = wtot * u[1] * u[0] - b[1] * b[0];
+    c[2] = wtot * u[2] * u[0] - b[2] * b[0];
+    c[3] = wtot * u[3] * u[0] - b[3] * b[0];
+    c[5] = b[2] * u[0] - b[0] * u[2];
+    c[6] = b[3] * u[0] - b[0] * u[3];
+    f[0] = rho * u[1];
+    f[4] = wtot * u[0] * u[1] - b[0] * b[1];
+    f[1] = wtot * u[1] * u[1] - b[1] * b[1] + ptot;
+    f[2] = wtot * u[2] * u[1] - b[2] * b[1];
+    f[3] = wtot * u[3] * u[1] - b[3] * b[1];
+    f[5] = b[2] * u[1] - b[1] * u[2];
+    f[6] = b[3] * u[1] - b[1] * u[3];
+  }
+  double lambda_l = smin(lml, lmr);
+  double lambda_r = smax(lpl, lpr);
+  double lambda_diff_inv = 1.0 / (lambda_r - lambda_l);
+  const double v_interface = 0.0;
+  for (int n = 0; n < NWAVE; ++n) {
+    if (lambda_l >= v_interface) f[n] = fl[n];
+    else if (lambda_r <= v_interface) f[n] = fr[n];
+    else f[n] = (lambda_r * fl[n] - lambda_l * fr[n] + lambda_l * lambda_r * (cr[n] - cl[n])) *
+                lambda_diff_inv;
+  }
+}
+
 /* ------------------------------------------------------------------------------------
  * Reconstruction of one cell along a direction: given the 7-component wave vector of the
  * cell and its neighbours, return the value at its upper face (qlp, becomes wl of the
@@ -538,7 +609,8 @@ static void riemann(const orc_mesh *m, int dir, const double *wl, const double *
   int ivx = IVX + dir, ivy = IVX + (dir + 1) % 3, ivz = IVX + (dir + 2) % 3;
   double wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
   double wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
-  if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
+  if (m->p.relativistic) hlle_sr(m->p.gamma, wli, wri, bx, flx7);
+  else if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
   else hlle(m->p.gamma, wli, wri, bx, flx7);
 }
 
@@ -902,20 +974,247 @@ static long con2prim(orc_mesh *m, int b, double *u, double *prim) {
 }
 
 /* ------------------------------------------------------------------------------------
- * SR-MHD conserved->primitive (eos/adiabatic_mhd_sr.cpp) — filled in with the SR path.
+ * SR-MHD conserved->primitive, eos/adiabatic_mhd_sr.cpp:72-272, with the Newman & Hamlin
+ * (2014) fixed-point solve ConservedToPrimitiveNormal (:404-522).
  */
+#define ORC_PI 3.1415926535897932 /* defs.hpp.in:140 */
+
+/* ConservedToPrimitiveNormal, adiabatic_mhd_sr.cpp:404-522.  prim[5] receives
+ * (rho, u1, u2, u3, pgas) in IDN, IVX..IVZ, IPR slots.  *iters = loop index at exit. */
+static int sr_normal(double gamma_adi, double dd, double ee, double mm_sq, double mm1,
+                     double mm2, double mm3, double bb_sq, double bb1, double bb2,
+                     double bb3, double tt, double pgas_old, double *prim,
+                     double *p_gamma_lor, double *p_pmag, int *iters) {
+  const int max_iterations = 15;
+  const double tol = 1.0e-12;
+  const double pgas_uniform_min = 1.0e-12;
+  const double a_min = 1.0e-12;
+  const double v_sq_max = 1.0 - 1.0e-12;
+  const double rr_max = 1.0 - 1.0e-12;
+  double d = 0.5 * (mm_sq * bb_sq - SQR(tt));
+  d = smax(d, 0.0);
+  double pgas_min = cbrt(27.0 / 4.0 * d) - ee - 0.5 * bb_sq;
+  pgas_min = smax(pgas_min, pgas_uniform_min);
+  double pgas[3];
+  pgas[0] = smax(pgas_old, pgas_min);
+  int n;
+  for (n = 0; n < max_iterations; ++n) {
+    double a = 0.0;
+    if (n % 3 != 2) {
+      a = ee + pgas[n % 3] + 0.5 * bb_sq;
+      a = smax(a, a_min);
+    }
+    if (n % 3 != 2) {
+      double phi = acos(1.0 / a * sqrt(27.0 * d / (4.0 * a)));
+      double eee = a / 3.0 - 2.0 / 3.0 * a * cos(2.0 / 3.0 * (phi + ORC_PI));
+      double ll = eee - bb_sq;
+      double v_sq = (mm_sq * SQR(ll) + SQR(tt) * (bb_sq + 2.0 * ll)) / SQR(ll * (bb_sq + ll));
+      v_sq = smin(smax(v_sq, 0.0), v_sq_max);
+      double gamma_sq = 1.0 / (1.0 - v_sq);
+      double gamma = sqrt(gamma_sq);
+      double wgas = ll / gamma_sq;
+      double rho = dd / gamma;
+      pgas[(n + 1) % 3] = (gamma_adi - 1.0) / gamma_adi * (wgas - rho);
+      pgas[(n + 1) % 3] = smax(pgas[(n + 1) % 3], pgas_min);
+    }
+    if (n % 3 != 2) {
+      if (pgas[(n + 1) % 3] > pgas_min && fabs(pgas[(n + 1) % 3] - pgas[n % 3]) < tol) break;
+    }
+    if (n % 3 == 2) {
+      double rr = (pgas[2] - pgas[1]) / (pgas[1] - pgas[0]);
+      if (!isfinite(rr) || fabs(rr) > rr_max) continue;
+      pgas[0] = pgas[1] + (pgas[2] - pgas[1]) / (1.0 - rr);
+      pgas[0] = smax(pgas[0], pgas_min);
+      if (pgas[0] > pgas_min && fabs(pgas[0] - pgas[2]) < tol) break;
+    }
+  }
+  *iters = n;
+  if (n == max_iterations) return 0;
+  prim[IPR] = pgas[(n + 1) % 3];
+  if (!isfinite(prim[IPR])) return 0;
+  double a = ee + prim[IPR] + 0.5 * bb_sq;
+  a = smax(a, a_min);
+  double phi = acos(1.0 / a * sqrt(27.0 * d / (4.0 * a)));
+  double eee = a / 3.0 - 2.0 / 3.0 * a * cos(2.0 / 3.0 * (phi + ORC_PI));
+  double ll = eee - bb_sq;
+  double v_sq = (mm_sq * SQR(ll) + SQR(tt) * (bb_sq + 2.0 * ll)) / SQR(ll * (bb_sq + ll));
+  v_sq = smin(smax(v_sq, 0.0), v_sq_max);
+  double gamma_sq = 1.0 / (1.0 - v_sq);
+  double gamma = sqrt(gamma_sq);
+  prim[IDN] = dd / gamma;
+  if (!isfinite(prim[IDN])) return 0;
+  double ss = tt / ll;
+  double v1 = (mm1 + ss * bb1) / (ll + bb_sq);
+  double v2 = (mm2 + ss * bb2) / (ll + bb_sq);
+  double v3 = (mm3 + ss * bb3) / (ll + bb_sq);
+  prim[IVX] = gamma * v1;
+  prim[IVY] = gamma * v2;
+  prim[IVZ] = gamma * v3;
+  if (!isfinite(prim[IVX]) || !isfinite(prim[IVY]) || !isfinite(prim[IVZ])) return 0;
+  *p_gamma_lor = gamma;
+  *p_pmag = 0.5 * (bb_sq / gamma_sq + SQR(ss));
+  return 1;
+}
+
+/* one cell of EquationOfState::ConservedToPrimitive (SR), adiabatic_mhd_sr.cpp:87-268.
+ * cons[5] (natural slots) may be rewritten; prim[5] holds the fallback/guess on entry and
+ * the result on exit.  Returns 1 if the cell used the fallback. */
+static int sr_c2p_cell(double gamma_adi, double dfloor, double pfloor, double sigma_max,
+                       double beta_min, double gamma_max, double *cons, double bc1,
+                       double bc2, double bc3, double *prim, int *iters) {
+  const double mm_sq_ee_sq_max = 1.0 - 1.0e-12;
+  double dd = cons[IDN], ee = cons[IPR];
+  double mm_sq = SQR(cons[IVX]) + SQR(cons[IVY]) + SQR(cons[IVZ]);
+  double mm1 = cons[IVX], mm2 = cons[IVY], mm3 = cons[IVZ];
+  double bb_sq = SQR(bc1) + SQR(bc2) + SQR(bc3);
+  double tt = cons[IVX] * bc1 + cons[IVY] * bc2 + cons[IVZ] * bc3;
+  int fixed = 0;
+  double density_floor_local = dfloor, pressure_floor_local = pfloor;
+  double dd_min = density_floor_local;
+  if (dd < dd_min) { dd = dd_min; fixed = 1; }
+  double ee_min = density_floor_local + pressure_floor_local / (gamma_adi - 1.0) + 0.5 * bb_sq;
+  if (ee < ee_min) { ee = ee_min; fixed = 1; }
+  double mm_sq_max = mm_sq_ee_sq_max * SQR(ee);
+  if (mm_sq > mm_sq_max) {
+    double factor = sqrt(mm_sq_max / mm_sq);
+    mm_sq = mm_sq_max;
+    mm1 *= factor; mm2 *= factor; mm3 *= factor;
+    tt *= factor;
+    fixed = 1;
+  }
+  double rho_old = smax(prim[IDN], density_floor_local);
+  double pgas_old = smax(prim[IPR], pressure_floor_local);
+  double u1_old = prim[IVX], u2_old = prim[IVY], u3_old = prim[IVZ];
+  double gamma = 0.0, pmag = 0.0;
+  int success = sr_normal(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2, bc3, tt,
+                          pgas_old, prim, &gamma, &pmag, iters);
+  if (!success) {
+    prim[IDN] = rho_old; prim[IPR] = pgas_old;
+    prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;
+    fixed = 1;
+  }
+  if (sigma_max > 0.0) density_floor_local = smax(density_floor_local, 2.0 * pmag / sigma_max);
+  if (beta_min > 0.0) pressure_floor_local = smax(pressure_floor_local, beta_min * pmag);
+  double rho_add = smax(density_floor_local - prim[IDN], 0.0);
+  double pgas_add = smax(pressure_floor_local - prim[IPR], 0.0);
+  if (success && (rho_add > 0.0 || pgas_add > 0.0)) {
+    double wgas_add = rho_add + gamma_adi / (gamma_adi - 1.0) * pgas_add;
+    dd += rho_add * gamma;
+    ee += wgas_add * SQR(gamma) + pgas_add;
+    int it2;
+    success = sr_normal(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2, bc3, tt,
+                        pgas_old, prim, &gamma, &pmag, &it2);
+    if (!success) {
+      prim[IDN] = rho_old; prim[IPR] = pgas_old;
+      prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;
+    }
+    fixed = 1;
+  }
+  double *u1 = &prim[IVX], *u2 = &prim[IVY], *u3 = &prim[IVZ];
+  if (!success) gamma = sqrt(1.0 + SQR(*u1) + SQR(*u2) + SQR(*u3));
+  int velocity_ceiling = 0;
+  if (gamma > gamma_max) {
+    double factor = sqrt((SQR(gamma_max) - 1.0) / (SQR(gamma) - 1.0));
+    *u1 *= factor; *u2 *= factor; *u3 *= factor;
+    fixed = 1;
+    velocity_ceiling = 1;
+  }
+  if (velocity_ceiling) {
+    double b0 = *u1 * bc1 + *u2 * bc2 + *u3 * bc3;
+    pmag = 0.5 * (bb_sq / SQR(gamma) + SQR(b0 / gamma));
+  }
+  density_floor_local = dfloor;
+  if (sigma_max > 0.0) density_floor_local = smax(density_floor_local, 2.0 * pmag / sigma_max);
+  pressure_floor_local = pfloor;
+  if (beta_min > 0.0) pressure_floor_local = smax(pressure_floor_local, beta_min * pmag);
+  double *rho = &prim[IDN], *pgas = &prim[IPR];
+  if (*rho < density_floor_local) { *rho = density_floor_local; fixed = 1; }
+  if (*pgas < pressure_floor_local) { *pgas = pressure_floor_local; fixed = 1; }
+  if (!success) {
+    *rho = density_floor_local;
+    *pgas = pressure_floor_local;
+    *u1 = *u2 = *u3 = 0.0;
+  }
+  if (fixed) {
+    gamma = sqrt(1.0 + SQR(*u1) + SQR(*u2) + SQR(*u3));
+    double b0 = bc1 * *u1 + bc2 * *u2 + bc3 * *u3;
+    double b1 = (bc1 + b0 * *u1) / gamma;
+    double b2 = (bc2 + b0 * *u2) / gamma;
+    double b3 = (bc3 + b0 * *u3) / gamma;
+    double b_sq = -SQR(b0) + SQR(b1) + SQR(b2) + SQR(b3);
+    double wgas = *rho + gamma_adi / (gamma_adi - 1.0) * *pgas;
+    double wtot = wgas + b_sq;
+    pmag = 0.5 * b_sq;
+    cons[IDN] = *rho * gamma;
+    cons[IPR] = wtot * SQR(gamma) - SQR(b0) - (*pgas + pmag);
+    cons[IVX] = wtot * gamma * *u1 - b0 * b1;
+    cons[IVY] = wtot * gamma * *u2 - b0 * b2;
+    cons[IVZ] = wtot * gamma * *u3 - b0 * b3;
+  }
+  return !success;
+}
+
 static long sr_c2p_block(orc_mesh *m, int b, double *u, double *prim, int il, int iu,
                          int jl, int ju, int kl, int ku) {
-  (void)m; (void)b; (void)u; (void)prim; (void)il; (void)iu; (void)jl; (void)ju; (void)kl;
-  (void)ku;
-  return -1;
+  const double *bcc = m->bcc + (long)b * 3 * m->ncell;
+  long nc = m->ncell, fails = 0;
+  for (int k = kl; k <= ku; ++k)
+    for (int j = jl; j <= ju; ++j)
+      for (int i = il; i <= iu; ++i) {
+        long c = CIDX(m, 0, k, j, i);
+        double cons[5], pr[5];
+        for (int n = 0; n < 5; ++n) { cons[n] = u[c + n * nc]; pr[n] = prim[c + n * nc]; }
+        int it;
+        fails += sr_c2p_cell(m->p.gamma, m->p.dfloor, m->p.pfloor, m->p.sigma_max,
+                             m->p.beta_min, m->p.gamma_max, cons, bcc[c], bcc[c + nc],
+                             bcc[c + 2 * nc], pr, &it);
+        for (int n = 0; n < 5; ++n) { u[c + n * nc] = cons[n]; prim[c + n * nc] = pr[n]; }
+      }
+  return fails;
 }
 
 void orc_sr_c2p_cells(long n, double gamma, double pgas_floor, const double *cons,
                       const double *bcc, const double *pgas_guess, double *prim,
                       int *iterations) {
-  (void)gamma; (void)pgas_floor; (void)cons; (void)bcc; (void)pgas_guess; (void)prim;
-  for (long c = 0; c < n; ++c) iterations[c] = -1;
+  (void)pgas_floor;
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < n; ++c) {
+    const double *q = cons + 5 * c, *bb = bcc + 3 * c;
+    double mm_sq = SQR(q[IVX]) + SQR(q[IVY]) + SQR(q[IVZ]);
+    double bb_sq = SQR(bb[0]) + SQR(bb[1]) + SQR(bb[2]);
+    double tt = q[IVX] * bb[0] + q[IVY] * bb[1] + q[IVZ] * bb[2];
+    double pr[5] = {0, 0, 0, 0, 0}, g, pm;
+    int it;
+    int ok = sr_normal(gamma, q[IDN], q[IPR], mm_sq, q[IVX], q[IVY], q[IVZ], bb_sq, bb[0],
+                       bb[1], bb[2], tt, pgas_guess[c], pr, &g, &pm, &it);
+    for (int v = 0; v < 5; ++v) prim[5 * c + v] = pr[v];
+    iterations[c] = ok ? it : -1;
+  }
+}
+
+/* SR prim -> cons, adiabatic_mhd_sr.cpp:284-332 (used by tests to build states) */
+static void sr_p2c(double gamma_adi, const double *w, double bb1, double bb2, double bb3,
+                   double *u) {
+  double gamma_adi_red = gamma_adi / (gamma_adi - 1.0);
+  double rho = w[IDN], pgas = w[IPR], u1 = w[IVX], u2 = w[IVY], u3 = w[IVZ];
+  double u0 = sqrt(1.0 + SQR(u1) + SQR(u2) + SQR(u3));
+  double b0 = bb1 * u1 + bb2 * u2 + bb3 * u3;
+  double b1 = (bb1 + b0 * u1) / u0;
+  double b2 = (bb2 + b0 * u2) / u0;
+  double b3 = (bb3 + b0 * u3) / u0;
+  double b_sq = -SQR(b0) + SQR(b1) + SQR(b2) + SQR(b3);
+  double wtot_u02 = (rho + gamma_adi_red * pgas + b_sq) * u0 * u0;
+  u[IDN] = rho * u0;
+  u[IPR] = wtot_u02 - b0 * b0 - (pgas + 0.5 * b_sq);
+  u[IVX] = wtot_u02 * u1 / u0 - b0 * b1;
+  u[IVY] = wtot_u02 * u2 / u0 - b0 * b2;
+  u[IVZ] = wtot_u02 * u3 / u0 - b0 * b3;
+}
+
+void orc_sr_prim_to_cons(long n, double gamma, const double *w, const double *bcc,
+                         double *u) {
+  for (long c = 0; c < n; ++c) sr_p2c(gamma, w + 5 * c, bcc[3 * c], bcc[3 * c + 1],
+                                      bcc[3 * c + 2], u + 5 * c);
 }
 
 /* ------------------------------------------------------------------------------------

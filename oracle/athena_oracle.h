@@ -70,6 +70,11 @@ void orc_sr_c2p_cells(long n, double gamma, double pgas_floor, const double *con
                       const double *bcc, const double *pgas_guess, double *prim,
                       int *iterations);
 
+/* SR prim -> cons (adiabatic_mhd_sr.cpp:284-332) on independent cells: w[n][5] natural
+ * slots (rho, u1, u2, u3, p), bcc[n][3] -> u[n][5] (D, M1..M3, E in IDN, IM1.., IEN). */
+void orc_sr_prim_to_cons(long n, double gamma, const double *w, const double *bcc,
+                         double *u);
+
 #ifdef __cplusplus
 }
 #endif
