@@ -132,6 +132,9 @@ def time_device_cycles(g, stream, steps, warmup):
 
 
 def run_gpu(args, rank, world, local_rank):
+    global NX, NB
+    NX = (args.nx,) * 3
+    NB = (args.nx // 32,) * 3
     import torch
     import torch.distributed as dist
     from athena_gb300 import build
@@ -139,7 +142,7 @@ def run_gpu(args, rank, world, local_rank):
     build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    mesh, ic = make_ic()
+    mesh, ic = make_ic(NX, NB)
     zones = mesh.nx[0] * mesh.nx[1] * mesh.nx[2]
     stream = torch.cuda.Stream(device=dev)
     res = {}
@@ -244,6 +247,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=256,
+                    help="cells per direction (MeshBlocks of 32^3); 256 is the workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))
@@ -287,6 +292,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     mesh, res = run_gpu(args, rank, world, local_rank)
+    line_config = workload_config(NX, NB)
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
@@ -302,7 +308,7 @@ def main():
             "n_gpus": world, "steps": r32["steps"], "warmup": args.warmup,
             "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(),
+            "config": line_config,
             "fp64_gpu": {"value": r64["value"], "ms_per_step": r64["ms_per_step"],
                          "steps": r64["steps"]},
             "speedup_fp32_vs_fp64_gpu": r32["value"] / r64["value"],
@@ -318,7 +324,7 @@ def main():
             "clocks": res["clocks"],
             "kernel_ms_fp32": res["profile32"], "kernel_ms_fp64": res["profile64"]}
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline((mesh, make_ic()[1]))
+        line["cpu_baseline"] = cpu_baseline((mesh, make_ic(NX, NB)[1]))
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
