@@ -21,6 +21,7 @@ UNITS = {
     "api.cu": ["-fmad=false"],
     "stage_fp64.cu": ["-fmad=false"],
     "stage_fp32.cu": ["-fmad=true"],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -92,6 +92,11 @@ athgpu_status download_bulk(athgpu_ctx* c, double* h, const void* dev, const voi
 }
 }  // namespace
 
+namespace athgpu {
+// lets other translation units report through athgpu_last_error()
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace athgpu
+
 extern "C" {
 
 const char* athgpu_last_error(void) { return g_err.c_str(); }

@@ -144,6 +144,37 @@ athgpu_status athgpu_launch_count(athgpu_ctx *ctx, long long *count, int reset);
 const char *athgpu_last_error(void);
 const char *athgpu_version(void);
 
+/* Conserved->primitive over whole MeshBlocks plus the first CFL time step, for callers
+ * that cannot let a library allocate device memory: hosts whose device memory belongs
+ * to their own pool allocator, real-time loops that forbid allocation latency, plugins
+ * that must leave the device heap untouched.  No counterpart in the reference: it has no
+ * device memory; this computes what EquationOfState::ConservedToPrimitive
+ * (adiabatic_mhd.cpp:41-90) followed by Hydro::NewBlockTimeStep (new_blockdt.cpp:45-230)
+ * and the block minimum of Mesh::NewTimeStep compute, bit for bit like
+ * athgpu_initialize, on arrays the caller owns.
+ *
+ * All array arguments are DEVICE pointers in the layout at the top of this file: u (may be
+ * rewritten where the density/pressure floors apply), face field b1/b2/b3, outputs w and
+ * bcc, per-block spacings dx?f [nblocks][nc?], and dt_out (one double: cfl_number times the
+ * minimum over interior cells of dx/(|v|+c_f)).  Asynchronous on `stream` (a
+ * cudaStream_t, NULL = legacy default stream).
+ *
+ * Allocates nothing: no cudaMalloc/cudaFree and no allocating library routine.  The
+ * reduction's scratch is a fixed array of 65,536 doubles inside the library, held by every
+ * GPU that loads it until the process exits, so a call covers at most
+ * ATHGPU_NOALLOC_MAX_CELLS cells (ghosts included, all blocks) and larger meshes are
+ * rejected with ATHGPU_ERR_ARG.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call before
+ * any stream capture.  Every call on a device shares the one array, which keeps the last
+ * call's contents: calls that overlap on the GPU (different streams, no ordering) race;
+ * order them on one stream or with events. */
+#define ATHGPU_NOALLOC_MAX_CELLS 16777216LL
+athgpu_status athgpu_con2prim_timestep_noalloc(
+    int nblocks, int nx1, int nx2, int nx3, int nghost, double gamma, double dfloor,
+    double pfloor, double cfl_number, const double *dx1f, const double *dx2f,
+    const double *dx3f, const double *b1, const double *b2, const double *b3, double *u,
+    double *w, double *bcc, double *dt_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
