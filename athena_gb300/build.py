@@ -20,7 +20,8 @@ BASE = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "
 UNITS = {
     "api.cu": ["-fmad=false"],
     "stage_fp64.cu": ["-fmad=false"],
-    "stage_fp32.cu": ["-fmad=true"],
+    # FP32 path: FMA contraction and the fast (approximate) FP32 divide and square root
+    "stage_fp32.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"],
     "noalloc.cu": ["-fmad=false"],
 }
 

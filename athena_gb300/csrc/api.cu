@@ -49,7 +49,7 @@ long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
 void free_all(athgpu_ctx* c) {
   Registers& r = c->r;
-  void* ptrs[] = {r.u, r.ustar, r.ulo, r.w, r.bcc, r.flx1, r.flx2, r.flx3, r.e3x1, r.e2x1,
+  void* ptrs[] = {r.u, r.ustar, r.ulo, r.w, r.bcc, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->nbr,
                   c->staging};
@@ -127,6 +127,19 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "coordinate arrays are required");
   if (!(d->gamma > 1.0) || !(d->cfl_number > 0.0))
     return fail(ATHGPU_ERR_ARG, "gamma must exceed 1 and cfl_number be positive");
+  {
+    // uniform Cartesian spacing within every block (x?rat = 1, coordinates.cpp:126-146):
+    // the kernels use the reference's uniform-mesh branches (plm.cpp:103, ppm.cpp:156)
+    const long long nbk = (long long)d->nbx1 * d->nbx2 * d->nbx3;
+    const int ncs[3] = {d->nx1 + 2 * d->nghost, d->nx2 + 2 * d->nghost, d->nx3 + 2 * d->nghost};
+    const double* dxs[3] = {d->dx1f, d->dx2f, d->dx3f};
+    for (int dd = 0; dd < 3; ++dd)
+      for (long long b = 0; b < nbk; ++b)
+        for (int cc = 1; cc < ncs[dd]; ++cc)
+          if (dxs[dd][b * ncs[dd] + cc] != dxs[dd][b * ncs[dd]] || !(dxs[dd][b * ncs[dd]] > 0.0))
+            return fail(ATHGPU_ERR_UNSUPPORTED,
+                        "face spacings must be positive and uniform within each MeshBlock");
+  }
 
   athgpu_ctx* c = new athgpu_ctx();
   c->desc = *d;
@@ -165,8 +178,7 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   std::vector<A> allocs = {
       {&r.u, nb * 5 * m.ncell * rb}, {&r.ustar, nb * 5 * m.ncell * rb},
       {&r.w, nb * 5 * m.ncell * rb}, {&r.bcc, nb * 3 * m.ncell * rb},
-      {&r.flx1, 5 * nb * m.nf1 * rb}, {&r.flx2, 5 * nb * m.nf2 * rb},
-      {&r.flx3, 5 * nb * m.nf3 * rb},
+      {&r.dflx, nb * 5 * m.ncell * rb},
       {&r.e3x1, nb * m.nf1 * rb}, {&r.e2x1, nb * m.nf1 * rb}, {&r.w1f, nb * m.nf1 * rb},
       {&r.e1x2, nb * m.nf2 * rb}, {&r.e3x2, nb * m.nf2 * rb}, {&r.w2f, nb * m.nf2 * rb},
       {&r.e1x3, nb * m.nf3 * rb}, {&r.e2x3, nb * m.nf3 * rb}, {&r.w3f, nb * m.nf3 * rb},

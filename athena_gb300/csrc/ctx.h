@@ -13,7 +13,7 @@ namespace athgpu {
 struct Registers {
   // bulk precision (double or float) arrays; `void*` so one struct serves both paths
   void *u = nullptr, *ustar = nullptr, *ulo = nullptr, *w = nullptr, *bcc = nullptr;
-  void *flx1 = nullptr, *flx2 = nullptr, *flx3 = nullptr;
+  void *dflx = nullptr;  // per-cell flux divergence accumulated by the sweeps
   void *e3x1 = nullptr, *e2x1 = nullptr, *w1f = nullptr;
   void *e1x2 = nullptr, *e3x2 = nullptr, *w2f = nullptr;
   void *e1x3 = nullptr, *e2x3 = nullptr, *w3f = nullptr;

@@ -119,13 +119,14 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
   }
 }
 
-// Riemann solve on one face of direction DIR and store flux, face EMFs and CT weight
-// (Hydro::CalculateFluxes calculate_fluxes.cpp:102/:221/:340; hlld.cpp:372-376)
+// Riemann solve on one face of direction DIR: stores the two face EMFs and the CT weight
+// (calculate_fluxes.cpp:102/:221/:340; hlld.cpp:372-376) and returns the five hydro
+// fluxes in natural slots (IDN, IM1, IM2, IM3, IEN).
 template <typename Real, int DIR, int RS>
 __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, const Real* wr,
-                                           Real bx, Real dx, Real dt, i64 fo,
-                                           Real* __restrict__ flx, Real* __restrict__ ey,
-                                           Real* __restrict__ ez, Real* __restrict__ wct) {
+                                           Real bx, Real dx, Real dt, i64 fo, Real* fn,
+                                           Real* __restrict__ ey, Real* __restrict__ ez,
+                                           Real* __restrict__ wct) {
   // local order: d, v_normal, v_t1, v_t2, p, By, Bz (hlld.cpp:42-43)
   const int ivx = IVX + DIR, ivy = IVX + (DIR + 1) % 3, ivz = IVX + (DIR + 2) % 3;
   Real wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
@@ -133,33 +134,46 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   Real f[NWAVE];
   if (RS == 0) hlld<Real>((Real)m.gamma, wli, wri, bx, f);
   else hlle<Real>((Real)m.gamma, wli, wri, bx, f);
-  const i64 fs = fsize<DIR>(m);
-  flx[fo] = f[0];
-  flx[(i64)ivx * fs + fo] = f[1];
-  flx[(i64)ivy * fs + fo] = f[2];
-  flx[(i64)ivz * fs + fo] = f[3];
-  flx[(i64)IPR * fs + fo] = f[4];
+  fn[IDN] = f[0];
+  fn[ivx] = f[1];
+  fn[ivy] = f[2];
+  fn[ivz] = f[3];
+  fn[IPR] = f[4];
   ey[fo] = -f[5];
   ez[fo] = f[6];
   wct[fo] = weight_for_ct<Real>(f[0], wl[IDN], wr[IDN], dx, dt);
 }
 
-// x1 sweep: rows (b, k in [ks-1,ke+1], j in [js-1,je+1]); cells i in [is-1, ie+1] are
-// flattened over rows; a warp reconstructs 32 consecutive cells (the first one overlaps
-// the previous warp) and passes each cell's upper-face state to the next lane with a
-// shuffle, so that every cell is reconstructed once and every face solved once.
-// flx layout: [5][nb][nc3][nc2][nc1+1]; e3/e2/wct: [nb][nc3][nc2][nc1+1].
+// The flux divergence of Hydro::AddFluxDivergence (add_flux_divergence.cpp:50-94) is
+// accumulated by the three sweeps in the reference's order: the x1 sweep stores
+// dflx = A1*F1(i+1) - A1*F1(i), the x2 sweep adds (A2*F2(j+1) - A2*F2(j)), the x3 sweep
+// adds (A3*F3(k+1) - A3*F3(k)) and applies u_out = u_in - wght*dflx/vol.  So no flux
+// array is stored.  Cartesian areas and volumes, coordinates.cpp:448-548.
+struct UpdateArgs {
+  double beta;            // stage weight (time_integrator.cpp:216-217)
+  int stage;
+  const void* uin;        // U^n
+  void* uout;             // U* (stage 1) or U^n+1 (stage 2; may alias uin)
+  void* ulo;              // compensation of U (FP32 path)
+};
+
+// x1 sweep: rows (b, k in [ks-1,ke+1], j in [js-1,je+1]) of cells i in [is-1, ie+1],
+// flattened over rows.  A warp reconstructs 32 consecutive cells: lane L > 0 solves the
+// left face of its cell with the upper-face state of lane L-1 (shuffle up), and lanes
+// 1..30 form their cell's x1 flux difference with the face flux of lane L+1 (shuffle
+// down).  Warps advance by 30 cells, so every cell is reconstructed at most twice, every
+// face solved at most twice (identical duplicate stores) and every difference formed once.
 template <typename Real, int ORDER, int RS>
 __global__ void __launch_bounds__(128)
 flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ bcc,
                const double* __restrict__ b1, const DevClock* __restrict__ clk,
-               Real* __restrict__ flx, Real* __restrict__ e3, Real* __restrict__ e2,
+               Real* __restrict__ dflx, Real* __restrict__ e3, Real* __restrict__ e2,
                Real* __restrict__ wct) {
   const int lane = threadIdx.x & 31;
   const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int ncr = m.nx1 + 2, nrj = m.nx2 + 2, nrk = m.nx3 + 2;
   const i64 total = (i64)m.nb * nrk * nrj * ncr;
-  const i64 g = warp * 31 + lane - 1;
+  const i64 g = warp * 30 + lane - 1;
   const bool valid = (g >= 0) && (g < total);
   Real qlp[NWAVE], qrm[NWAVE];
   int b = 0, k = 0, j = 0, c = 0;
@@ -178,30 +192,45 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
   Real wl[NWAVE];
 #pragma unroll
   for (int n = 0; n < NWAVE; ++n) wl[n] = __shfl_up_sync(0xffffffffu, qlp[n], 1);
-  if (!valid || lane == 0 || c == 0) return;
   const int i = m.is - 1 + c;
-  const double dt = clk->dt;
-  const i64 fo = f1idx(m, b, k, j, i);
-  solve_face<Real, 0, RS>(m, wl, qrm, (Real)__ldg(b1 + fo),
-                          (Real)__ldg(m.dx1f + (i64)b * m.nc1 + i), (Real)dt,
-                          fo, flx, e3, e2, wct);
+  Real fn[NHYDRO] = {Real(0), Real(0), Real(0), Real(0), Real(0)};
+  const bool has_face = valid && lane > 0 && c > 0;
+  if (has_face) {
+    const i64 fo = f1idx(m, b, k, j, i);
+    solve_face<Real, 0, RS>(m, wl, qrm, (Real)__ldg(b1 + fo),
+                            (Real)__ldg(m.dx1f + (i64)b * m.nc1 + i), (Real)clk->dt, fo, fn,
+                            e3, e2, wct);
+  }
+  Real fp[NHYDRO];
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) fp[n] = __shfl_down_sync(0xffffffffu, fn[n], 1);
+  if (has_face && lane <= 30 && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
+      k <= m.ke) {
+    const Real x1area = (Real)m.dx2f[(i64)b * m.nc2 + j] * (Real)m.dx3f[(i64)b * m.nc3 + k];
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n)
+      dflx[cidx(m, b, n, NHYDRO, k, j, i)] = (x1area * fp[n] - x1area * fn[n]);
+  }
 }
 
-// x2 / x3 sweeps: a thread owns one column (b, transverse index, i) and walks SEG faces
-// along the sweep, carrying the previous cell's upper-face state in registers (the
-// reference's wl/wlb swap, calculate_fluxes.cpp:184-237 and :304-356).  Columns:
-// x2: k in [ks-1,ke+1], i in [is-1,ie+1]; x3: j in [js-1,je+1], i in [is-1,ie+1].
-template <typename Real, int DIR, int ORDER, int RS>
+// x2 / x3 sweeps: a thread owns one column (b, transverse index, i) and walks a segment
+// of cells along the sweep, carrying the previous cell's upper-face state and the
+// previous face's flux in registers (the reference's wl/wlb swap,
+// calculate_fluxes.cpp:184-237 and :304-356).  Columns: x2: k in [ks-1,ke+1],
+// i in [is-1,ie+1]; x3: j in [js-1,je+1], i in [is-1,ie+1].  A segment of cells
+// [c0,c1] solves faces c0..c1+1, so neighbouring segments share one face.
+template <typename Real, int DIR, int ORDER, int RS, int KAHAN>
 __global__ void __launch_bounds__(128)
 flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                   const Real* __restrict__ bcc, const double* __restrict__ bn,
-                  const DevClock* __restrict__ clk, Real* __restrict__ flx,
-                  Real* __restrict__ ey, Real* __restrict__ ez, Real* __restrict__ wct) {
+                  const DevClock* __restrict__ clk, Real* __restrict__ dflx,
+                  Real* __restrict__ ey, Real* __restrict__ ez, Real* __restrict__ wct,
+                  UpdateArgs ua) {
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   const int ni = m.nx1 + 2;
   const int nt = (DIR == 1) ? m.nx3 + 2 : m.nx2 + 2;
-  const int nface = (DIR == 1) ? m.nx2 + 1 : m.nx3 + 1;
-  const int nseg = (nface + seg - 1) / seg;
+  const int ncellsw = (DIR == 1) ? m.nx2 : m.nx3;
+  const int nseg = (ncellsw + seg - 1) / seg;
   const i64 total = (i64)nseg * m.nb * nt * ni;
   if (t >= total) return;
   const int ii = (int)(t % ni);
@@ -209,36 +238,80 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   const int tt = (int)(r % nt);
   r /= nt;
   const int b = (int)(r % m.nb);
-  const int s = (int)(r / m.nb);
+  const int sg = (int)(r / m.nb);
   const int i = m.is - 1 + ii;
-  const int s0 = (DIR == 1 ? m.js : m.ks) + s * seg;
-  const int s1 = min(s0 + seg - 1, (DIR == 1 ? m.je : m.ke) + 1);
-  const double dt = clk->dt;
+  const int lo = (DIR == 1) ? m.js : m.ks;
+  const int c0 = lo + sg * seg;
+  const int c1 = min(c0 + seg - 1, lo + ncellsw - 1);
+  const int trans = (DIR == 1 ? m.ks : m.js) - 1 + tt;  // k for x2, j for x3
+  const bool interior = ii >= 1 && ii <= m.nx1 && trans >= (DIR == 1 ? m.ks : m.js) &&
+                        trans <= (DIR == 1 ? m.ke : m.je);
+  const Real dt = (Real)clk->dt;
+  const double* dxs = (DIR == 1) ? m.dx2f + (i64)b * m.nc2 : m.dx3f + (i64)b * m.nc3;
+  // area of this direction's faces (the same for every face of a uniform block)
+  const Real dx1 = (Real)m.dx1f[(i64)b * m.nc1 + i];
+  const Real dxt = (DIR == 1) ? (Real)m.dx3f[(i64)b * m.nc3 + trans]
+                              : (Real)m.dx2f[(i64)b * m.nc2 + trans];
+  const Real area = dx1 * dxt;
   Real wl[NWAVE], qlp[NWAVE], qrm[NWAVE];
-  if (DIR == 1) {
-    const int k = m.ks - 1 + tt;
-    recon_cell<Real, 1, ORDER>(m, w, bcc, b, k, s0 - 1, i, wl, qrm);
-    for (int jf = s0; jf <= s1; ++jf) {
-      recon_cell<Real, 1, ORDER>(m, w, bcc, b, k, jf, i, qlp, qrm);
-      const i64 fo = f2idx(m, b, k, jf, i);
-      solve_face<Real, 1, RS>(m, wl, qrm, (Real)__ldg(bn + fo),
-                              (Real)__ldg(m.dx2f + (i64)b * m.nc2 + jf), (Real)dt, fo,
-                              flx, ey, ez, wct);
+  Real fprev[NHYDRO];
+  const int k0 = (DIR == 1) ? trans : 0, j0 = (DIR == 2) ? trans : 0;
+  auto cell = [&](int s, Real* ql, Real* qr) {
+    if (DIR == 1) recon_cell<Real, 1, ORDER>(m, w, bcc, b, k0, s, i, ql, qr);
+    else recon_cell<Real, 2, ORDER>(m, w, bcc, b, s, j0, i, ql, qr);
+  };
+  cell(c0 - 1, wl, qrm);
+  for (int s = c0; s <= c1 + 1; ++s) {
+    cell(s, qlp, qrm);
+    const i64 fo = (DIR == 1) ? f2idx(m, b, k0, s, i) : f3idx(m, b, s, j0, i);
+    Real fn[NHYDRO];
+    solve_face<Real, DIR, RS>(m, wl, qrm, (Real)__ldg(bn + fo), (Real)__ldg(dxs + s), dt, fo,
+                              fn, ey, ez, wct);
+    if (s > c0 && interior) {
+      // cell s-1: this direction's flux difference
+      const int kc = (DIR == 1) ? k0 : s - 1, jc = (DIR == 1) ? s - 1 : j0;
+      if (DIR == 1) {
 #pragma unroll
-      for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
-    }
-  } else {
-    const int j = m.js - 1 + tt;
-    recon_cell<Real, 2, ORDER>(m, w, bcc, b, s0 - 1, j, i, wl, qrm);
-    for (int kf = s0; kf <= s1; ++kf) {
-      recon_cell<Real, 2, ORDER>(m, w, bcc, b, kf, j, i, qlp, qrm);
-      const i64 fo = f3idx(m, b, kf, j, i);
-      solve_face<Real, 2, RS>(m, wl, qrm, (Real)__ldg(bn + fo),
-                              (Real)__ldg(m.dx3f + (i64)b * m.nc3 + kf), (Real)dt, fo,
-                              flx, ey, ez, wct);
+        for (int n = 0; n < NHYDRO; ++n) {
+          const i64 cc = cidx(m, b, n, NHYDRO, kc, jc, i);
+          Real d = dflx[cc];
+          d += (area * fn[n] - area * fprev[n]);
+          dflx[cc] = d;
+        }
+      } else {
+        const Real dx2 = (Real)m.dx2f[(i64)b * m.nc2 + jc];
+        const Real dx3 = (Real)m.dx3f[(i64)b * m.nc3 + kc];
+        const Real vol = dx1 * dx2 * dx3;
+        const Real wght = (Real)(ua.beta * clk->dt);
 #pragma unroll
-      for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
+        for (int n = 0; n < NHYDRO; ++n) {
+          const i64 cc = cidx(m, b, n, NHYDRO, kc, jc, i);
+          Real d = dflx[cc];
+          d += (area * fn[n] - area * fprev[n]);
+          const Real* uin = (const Real*)ua.uin;
+          Real* uout = (Real*)ua.uout;
+          if (KAHAN == 0) {
+            uout[cc] = uin[cc] - wght * d / vol;
+          } else {
+            Real* ulo = (Real*)ua.ulo;
+            const Real du = -(wght * d / vol);
+            const Real hi = uin[cc], lw = ulo[cc];
+            if (ua.stage == 1) {
+              uout[cc] = hi + (lw + du);
+            } else {
+              const Real y = du + lw;
+              const Real tt2 = hi + y;
+              ulo[cc] = y - (tt2 - hi);
+              uout[cc] = tt2;
+            }
+          }
+        }
+      }
     }
+#pragma unroll
+    for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n) fprev[n] = fn[n];
   }
 }
 
@@ -377,127 +450,83 @@ __device__ __forceinline__ Real edge_value(const DevMesh& m, const Real* __restr
   return sum * Real(0.5);
 }
 
-// Field::CT, field/ct.cpp:31-116, plus the VL2 register average (weighted_ave.cpp) which
-// for VL2 reduces to out = in on the first stage and an in-place update on the second.
-// One thread per face of all three face arrays.  Edge EMFs are read with the correction
-// above.  bin/bout may alias (second stage).
+// Field::CT, field/ct.cpp:31-116, plus the VL2 register average (weighted_ave.cpp),
+// which for VL2 reduces to out = in on the first stage and an in-place update on the
+// second.  blockIdx.y is the MeshBlock; the CTA computes the block's (wght/area) factors
+// once (areas and edge lengths are constant on a uniform block) and strides over the
+// block's faces of all three arrays.  Edge EMFs are read with the correction above.
+// FP64 path (Real = double): (wght/area)*(len*e(+) - len*e(-)) exactly as the reference.
+// FP32 path: the EMFs are FP32 and the update FP64 as ((wght/area)*len)*(e(+) - e(-)),
+// whose difference of two floats is exact in FP64.  bin/bout may alias.
 template <typename Real>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
           const Real* __restrict__ e1, const Real* __restrict__ e2,
           const Real* __restrict__ e3, const double* b1in, const double* b2in,
           const double* b3in, double* b1out, double* b2out, double* b3out) {
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  const double* dx1f = m.dx1f + (i64)b * m.nc1;
+  const double* dx2f = m.dx2f + (i64)b * m.nc2;
+  const double* dx3f = m.dx3f + (i64)b * m.nc3;
+  __shared__ double q[3];
+  if (threadIdx.x < 3) {
+    const double wght = beta * clk->dt;
+    const double area = threadIdx.x == 0 ? dx2f[m.js] * dx3f[m.ks]
+                      : threadIdx.x == 1 ? dx1f[m.is] * dx3f[m.ks] : dx1f[m.is] * dx2f[m.js];
+    q[threadIdx.x] = wght / area;
+  }
+  __syncthreads();
+  const double l1 = dx1f[m.is], l2 = dx2f[m.js], l3 = dx3f[m.ks];
+  const bool exact = sizeof(Real) == 8;
+  auto term = [&](double qd, double len, Real ep, Real em) -> double {
+    return exact ? qd * (len * (double)ep - len * (double)em)
+                 : (qd * len) * ((double)ep - (double)em);
+  };
   const i64 nf1 = (i64)m.nx3 * m.nx2 * (m.nx1 + 1);
   const i64 nf2 = (i64)m.nx3 * (m.nx2 + 1) * m.nx1;
   const i64 nf3 = (i64)(m.nx3 + 1) * m.nx2 * m.nx1;
   const i64 per = nf1 + nf2 + nf3;
-  if (t >= per * m.nb) return;
-  const int b = (int)(t / per);
-  i64 r = t - (i64)b * per;
-  const double wght = beta * clk->dt;
-  const double* dx1f = m.dx1f + (i64)b * m.nc1;
-  const double* dx2f = m.dx2f + (i64)b * m.nc2;
-  const double* dx3f = m.dx3f + (i64)b * m.nc3;
-  if (r < nf1) {
-    const int i = m.is + (int)(r % (m.nx1 + 1));
-    r /= (m.nx1 + 1);
-    const int j = m.js + (int)(r % m.nx2);
-    const int k = m.ks + (int)(r / m.nx2);
-    const i64 o = f1idx(m, b, k, j, i);
-    double area = dx2f[j] * dx3f[k];
-    double len = dx3f[k], len_p1 = dx3f[k];
-    double v = b1in[o];
-    v -= (wght / area) * (len_p1 * (double)edge_value<Real, 2>(m, e3, b, k, j + 1, i) -
-                          len * (double)edge_value<Real, 2>(m, e3, b, k, j, i));
-    len = dx2f[j];
-    len_p1 = dx2f[j];
-    v += (wght / area) * (len_p1 * (double)edge_value<Real, 1>(m, e2, b, k + 1, j, i) -
-                          len * (double)edge_value<Real, 1>(m, e2, b, k, j, i));
-    b1out[o] = v;
-  } else if (r < nf1 + nf2) {
-    r -= nf1;
-    const int i = m.is + (int)(r % m.nx1);
-    r /= m.nx1;
-    const int j = m.js + (int)(r % (m.nx2 + 1));
-    const int k = m.ks + (int)(r / (m.nx2 + 1));
-    const i64 o = f2idx(m, b, k, j, i);
-    double area = dx1f[i] * dx3f[k];
-    double len = dx3f[k], len_ip1 = dx3f[k];
-    double v = b2in[o];
-    v += (wght / area) * (len_ip1 * (double)edge_value<Real, 2>(m, e3, b, k, j, i + 1) -
-                          len * (double)edge_value<Real, 2>(m, e3, b, k, j, i));
-    len = dx1f[i];
-    double len_p1 = dx1f[i];
-    v -= (wght / area) * (len_p1 * (double)edge_value<Real, 0>(m, e1, b, k + 1, j, i) -
-                          len * (double)edge_value<Real, 0>(m, e1, b, k, j, i));
-    b2out[o] = v;
-  } else {
-    r -= nf1 + nf2;
-    const int i = m.is + (int)(r % m.nx1);
-    r /= m.nx1;
-    const int j = m.js + (int)(r % m.nx2);
-    const int k = m.ks + (int)(r / m.nx2);
-    const i64 o = f3idx(m, b, k, j, i);
-    double area = dx1f[i] * dx2f[j];
-    double len = dx2f[j], len_ip1 = dx2f[j];
-    double v = b3in[o];
-    v -= (wght / area) * (len_ip1 * (double)edge_value<Real, 1>(m, e2, b, k, j, i + 1) -
-                          len * (double)edge_value<Real, 1>(m, e2, b, k, j, i));
-    len = dx1f[i];
-    double len_p1 = dx1f[i];
-    v += (wght / area) * (len_p1 * (double)edge_value<Real, 0>(m, e1, b, k, j + 1, i) -
-                          len * (double)edge_value<Real, 0>(m, e1, b, k, j, i));
-    b3out[o] = v;
-  }
-}
-
-// ---------------------------------------------------------------------------------------
-// Hydro::AddFluxDivergence (add_flux_divergence.cpp:39-96, Cartesian areas/volumes
-// coordinates.cpp:448-548) fused with the VL2 register average.  KAHAN = 0: out = in -
-// wght*dflx/vol (FP64 path; in/out may alias).  KAHAN = 1 (FP32 path): the conserved
-// state is the compensated pair (hi, lo); stage 1 writes the predictor
-// out = hi + (lo + du), stage 2 adds du to (hi, lo) with a compensated sum.
-template <typename Real, int KAHAN>
-__global__ void __launch_bounds__(128)
-update_kernel(DevMesh m, double beta, int stage, const DevClock* __restrict__ clk,
-              const Real* __restrict__ f1, const Real* __restrict__ f2,
-              const Real* __restrict__ f3, const Real* uin, Real* uout, Real* ulo) {
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (i64)m.nb * m.nx3 * m.nx2 * m.nx1) return;
-  const int i = m.is + (int)(t % m.nx1);
-  i64 r = t / m.nx1;
-  const int j = m.js + (int)(r % m.nx2);
-  r /= m.nx2;
-  const int k = m.ks + (int)(r % m.nx3);
-  const int b = (int)(r / m.nx3);
-  const Real dx1 = (Real)m.dx1f[(i64)b * m.nc1 + i], dx2 = (Real)m.dx2f[(i64)b * m.nc2 + j],
-             dx3 = (Real)m.dx3f[(i64)b * m.nc3 + k];
-  const Real wght = (Real)(beta * clk->dt);
-  const Real x1area = dx2 * dx3, x2area = dx1 * dx3, x3area = dx1 * dx2;
-  const Real vol = dx1 * dx2 * dx3;
-  const i64 o1 = f1idx(m, b, k, j, i), o2 = f2idx(m, b, k, j, i), o3 = f3idx(m, b, k, j, i);
-  const i64 s2 = m.nc1, s3 = (i64)m.nc2 * m.nc1;
-  const i64 v1 = fsize<0>(m), v2 = fsize<1>(m), v3 = fsize<2>(m);
-#pragma unroll
-  for (int n = 0; n < NHYDRO; ++n) {
-    Real dflx = (x1area * __ldg(f1 + n * v1 + o1 + 1) - x1area * __ldg(f1 + n * v1 + o1));
-    dflx += (x2area * __ldg(f2 + n * v2 + o2 + s2) - x2area * __ldg(f2 + n * v2 + o2));
-    dflx += (x3area * __ldg(f3 + n * v3 + o3 + s3) - x3area * __ldg(f3 + n * v3 + o3));
-    const i64 c = cidx(m, b, n, NHYDRO, k, j, i);
-    if (KAHAN == 0) {
-      uout[c] = uin[c] - wght * dflx / vol;
+  for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < per;
+       r += (i64)gridDim.x * blockDim.x) {
+    if (r < nf1) {
+      i64 rr = r;
+      const int i = m.is + (int)(rr % (m.nx1 + 1));
+      rr /= (m.nx1 + 1);
+      const int j = m.js + (int)(rr % m.nx2);
+      const int k = m.ks + (int)(rr / m.nx2);
+      const i64 o = f1idx(m, b, k, j, i);
+      double v = b1in[o];
+      v -= term(q[0], l3, edge_value<Real, 2>(m, e3, b, k, j + 1, i),
+                edge_value<Real, 2>(m, e3, b, k, j, i));
+      v += term(q[0], l2, edge_value<Real, 1>(m, e2, b, k + 1, j, i),
+                edge_value<Real, 1>(m, e2, b, k, j, i));
+      b1out[o] = v;
+    } else if (r < nf1 + nf2) {
+      i64 rr = r - nf1;
+      const int i = m.is + (int)(rr % m.nx1);
+      rr /= m.nx1;
+      const int j = m.js + (int)(rr % (m.nx2 + 1));
+      const int k = m.ks + (int)(rr / (m.nx2 + 1));
+      const i64 o = f2idx(m, b, k, j, i);
+      double v = b2in[o];
+      v += term(q[1], l3, edge_value<Real, 2>(m, e3, b, k, j, i + 1),
+                edge_value<Real, 2>(m, e3, b, k, j, i));
+      v -= term(q[1], l1, edge_value<Real, 0>(m, e1, b, k + 1, j, i),
+                edge_value<Real, 0>(m, e1, b, k, j, i));
+      b2out[o] = v;
     } else {
-      const Real du = -(wght * dflx / vol);
-      const Real hi = uin[c], lo = ulo[c];
-      if (stage == 1) {
-        uout[c] = hi + (lo + du);
-      } else {
-        const Real y = du + lo;
-        const Real tt = hi + y;
-        ulo[c] = y - (tt - hi);
-        uout[c] = tt;
-      }
+      i64 rr = r - nf1 - nf2;
+      const int i = m.is + (int)(rr % m.nx1);
+      rr /= m.nx1;
+      const int j = m.js + (int)(rr % m.nx2);
+      const int k = m.ks + (int)(rr / m.nx2);
+      const i64 o = f3idx(m, b, k, j, i);
+      double v = b3in[o];
+      v -= term(q[2], l2, edge_value<Real, 1>(m, e2, b, k, j, i + 1),
+                edge_value<Real, 1>(m, e2, b, k, j, i));
+      v += term(q[2], l1, edge_value<Real, 0>(m, e1, b, k, j + 1, i),
+                edge_value<Real, 0>(m, e1, b, k, j, i));
+      b3out[o] = v;
     }
   }
 }
@@ -505,8 +534,9 @@ update_kernel(DevMesh m, double beta, int stage, const DevClock* __restrict__ cl
 // ---------------------------------------------------------------------------------------
 // Same-level periodic ghost exchange: every ghost cell / face receives the value of the
 // neighbour block that owns it (bvals_cc.cpp:287-430; face fields bvals_fc.cpp:344-397,
-// where a block's own faces along the normal are [is, ie+1]).  WHAT = 0: cells
-// (nvar variables), 1/2/3: x1/x2/x3 face field.
+// where a block's own faces along the normal are [is, ie+1]).  Threads enumerate ghost
+// elements only: per block and array, the k slabs, then the j slabs of the interior k
+// range, then the i slabs of the interior (k, j) range.
 __device__ __forceinline__ int own_map(int idx, int lo, int hi, int n, int* o) {
   if (idx < lo) { *o = -1; return idx + n; }
   if (idx > hi) { *o = 1; return idx - n; }
@@ -514,35 +544,78 @@ __device__ __forceinline__ int own_map(int idx, int lo, int hi, int n, int* o) {
   return idx;
 }
 
-template <typename T, int WHAT>
+// r-th ghost element of an array of extent (N1,N2,N3) whose own part has extent
+// (I1,I2,I3) starting at ng in every direction
+__device__ __forceinline__ void ghost_coord(i64 r, int N1, int N2, int N3, int I1, int I2,
+                                            int I3, int ng, int& k, int& j, int& i) {
+  const i64 A = (i64)2 * ng * N2 * N1;
+  if (r < A) {
+    int kk = (int)(r / ((i64)N2 * N1));
+    i64 rem = r - (i64)kk * N2 * N1;
+    k = kk < ng ? kk : kk - ng + ng + I3;
+    j = (int)(rem / N1);
+    i = (int)(rem % N1);
+    return;
+  }
+  r -= A;
+  const i64 B = (i64)2 * ng * N1 * I3;
+  if (r < B) {
+    int kk = (int)(r / ((i64)2 * ng * N1));
+    i64 rem = r - (i64)kk * 2 * ng * N1;
+    k = ng + kk;
+    int jj = (int)(rem / N1);
+    j = jj < ng ? jj : jj - ng + ng + I2;
+    i = (int)(rem % N1);
+    return;
+  }
+  r -= B;
+  int kk = (int)(r / ((i64)2 * ng * I2));
+  i64 rem = r - (i64)kk * 2 * ng * I2;
+  k = ng + kk;
+  j = ng + (int)(rem / (2 * ng));
+  int ii = (int)(rem % (2 * ng));
+  i = ii < ng ? ii : ii - ng + ng + I1;
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256)
-exchange_kernel(DevMesh m, int nvar, T* __restrict__ a) {
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  const int n1 = m.nc1 + (WHAT == 1), n2 = m.nc2 + (WHAT == 2), n3 = m.nc3 + (WHAT == 3);
-  const i64 per = (i64)n3 * n2 * n1;
-  if (t >= per * m.nb) return;
+exchange_kernel(DevMesh m, T* __restrict__ u, double* __restrict__ b1,
+                double* __restrict__ b2, double* __restrict__ b3) {
+  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = m.nx1, n2 = m.nx2, n3 = m.nx3, ng = m.ng;
+  // ghost counts per block: cells, x1/x2/x3 faces
+  const i64 gc = m.ncell - (i64)n1 * n2 * n3;
+  const i64 g1 = m.nf1 - (i64)(n1 + 1) * n2 * n3;
+  const i64 g2 = m.nf2 - (i64)n1 * (n2 + 1) * n3;
+  const i64 g3 = m.nf3 - (i64)n1 * n2 * (n3 + 1);
+  int what;
+  i64 per;
+  if (t < gc * m.nb) { what = 0; per = gc; }
+  else if ((t -= gc * m.nb) < g1 * m.nb) { what = 1; per = g1; }
+  else if ((t -= g1 * m.nb) < g2 * m.nb) { what = 2; per = g2; }
+  else if ((t -= g2 * m.nb) < g3 * m.nb) { what = 3; per = g3; }
+  else return;
   const int b = (int)(t / per);
-  i64 r = t - (i64)b * per;
-  const int i = (int)(r % n1);
-  r /= n1;
-  const int j = (int)(r % n2);
-  const int k = (int)(r / n2);
+  const i64 r = t - (i64)b * per;
+  int k, j, i;
+  ghost_coord(r, m.nc1 + (what == 1), m.nc2 + (what == 2), m.nc3 + (what == 3),
+              n1 + (what == 1), n2 + (what == 2), n3 + (what == 3), ng, k, j, i);
   int o1, o2, o3;
-  const int si = own_map(i, m.is, m.ie + (WHAT == 1), m.nx1, &o1);
-  const int sj = own_map(j, m.js, m.je + (WHAT == 2), m.nx2, &o2);
-  const int sk = own_map(k, m.ks, m.ke + (WHAT == 3), m.nx3, &o3);
-  if ((o1 | o2 | o3) == 0) return;
+  const int si = own_map(i, m.is, m.ie + (what == 1), n1, &o1);
+  const int sj = own_map(j, m.js, m.je + (what == 2), n2, &o2);
+  const int sk = own_map(k, m.ks, m.ke + (what == 3), n3, &o3);
   const int sb = nbr_of(m, b, o1, o2, o3);
   if (sb < 0) return;
-  if (WHAT == 0) {
-    for (int n = 0; n < nvar; ++n)
-      a[cidx(m, b, n, nvar, k, j, i)] = a[cidx(m, sb, n, nvar, sk, sj, si)];
+  if (what == 0) {
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n)
+      u[cidx(m, b, n, NHYDRO, k, j, i)] = u[cidx(m, sb, n, NHYDRO, sk, sj, si)];
+  } else if (what == 1) {
+    b1[f1idx(m, b, k, j, i)] = b1[f1idx(m, sb, sk, sj, si)];
+  } else if (what == 2) {
+    b2[f2idx(m, b, k, j, i)] = b2[f2idx(m, sb, sk, sj, si)];
   } else {
-    i64 d, s;
-    if (WHAT == 1) { d = f1idx(m, b, k, j, i); s = f1idx(m, sb, sk, sj, si); }
-    else if (WHAT == 2) { d = f2idx(m, b, k, j, i); s = f2idx(m, sb, sk, sj, si); }
-    else { d = f3idx(m, b, k, j, i); s = f3idx(m, sb, sk, sj, si); }
-    a[d] = a[s];
+    b3[f3idx(m, b, k, j, i)] = b3[f3idx(m, sb, sk, sj, si)];
   }
 }
 
@@ -613,24 +686,24 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     bcc[cb + 2 * vs] = bcc3;
     if (do_dt && i >= m.is && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
         k <= m.ke) {
-      // new_blockdt.cpp:80-103, evaluated in FP64 on the stored primitives
-      const double gam = m.gamma, wd = (double)u_d, wp = (double)w_p;
-      const double wb1 = (double)bcc1, wb2 = (double)bcc2, wb3 = (double)bcc3;
-      double dt1 = m.dx1f[(i64)b * m.nc1 + i], dt2 = m.dx2f[(i64)b * m.nc2 + j],
-             dt3 = m.dx3f[(i64)b * m.nc3 + k];
-      double bx = wb1 + fabs(b1[f1idx(m, b, k, j, i)] - wb1);
-      double cf = fast_ms<double>(gam, wd, wp, wb2, wb3, bx);
-      double speed = smax<double>(0.0, (fabs((double)vx) + cf));
+      // new_blockdt.cpp:80-103, in the bulk precision on the stored primitives (FP64
+      // path: the reference's arithmetic; FP32 path: FP32, reduced in FP64)
+      const Real gam = (Real)m.gamma;
+      Real dt1 = (Real)m.dx1f[(i64)b * m.nc1 + i], dt2 = (Real)m.dx2f[(i64)b * m.nc2 + j],
+           dt3 = (Real)m.dx3f[(i64)b * m.nc3 + k];
+      Real bx = bcc1 + dabs((Real)b1[f1idx(m, b, k, j, i)] - bcc1);
+      Real cf = fast_ms<Real>(gam, u_d, w_p, bcc2, bcc3, bx);
+      Real speed = smax<Real>(Real(0.0), (dabs(vx) + cf));
       dt1 /= (speed);
-      bx = wb2 + fabs(b2[f2idx(m, b, k, j, i)] - wb2);
-      cf = fast_ms<double>(gam, wd, wp, wb3, wb1, bx);
-      speed = smax<double>(0.0, (fabs((double)vy) + cf));
+      bx = bcc2 + dabs((Real)b2[f2idx(m, b, k, j, i)] - bcc2);
+      cf = fast_ms<Real>(gam, u_d, w_p, bcc3, bcc1, bx);
+      speed = smax<Real>(Real(0.0), (dabs(vy) + cf));
       dt2 /= (speed);
-      bx = wb3 + fabs(b3[f3idx(m, b, k, j, i)] - wb3);
-      cf = fast_ms<double>(gam, wd, wp, wb1, wb2, bx);
-      speed = smax<double>(0.0, (fabs((double)vz) + cf));
+      bx = bcc3 + dabs((Real)b3[f3idx(m, b, k, j, i)] - bcc3);
+      cf = fast_ms<Real>(gam, u_d, w_p, bcc1, bcc2, bx);
+      speed = smax<Real>(Real(0.0), (dabs(vz) + cf));
       dt3 /= (speed);
-      cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
+      cell_dt = (double)smin<Real>(smin<Real>(dt1, dt2), dt3);
     }
   }
   if (do_dt) {

@@ -10,36 +10,36 @@ static inline unsigned nblk(long long n, int tpb) {
   return (unsigned)((n + tpb - 1) / tpb);
 }
 
-template <typename Real, int ORDER, int RS>
+template <typename Real, int ORDER, int RS, int KAHAN>
 static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const double* b1,
-                          const double* b2, const double* b3) {
+                          const double* b2, const double* b3, const UpdateArgs& ua) {
   const DevMesh& m = c->m;
   Registers& r = c->r;
   cudaStream_t s = c->stream;
   {
     const long long cells = (long long)m.nb * (m.nx3 + 2) * (m.nx2 + 2) * (m.nx1 + 2);
-    const long long warps = (cells + 30) / 31;
+    const long long warps = (cells + 29) / 30;
     ProfScope ps(c, "flux_x1");
     flux_x1_kernel<Real, ORDER, RS><<<nblk(warps * 32, 128), 128, 0, s>>>(
-        m, w, bcc, b1, c->clk, (Real*)r.flx1, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f);
+        m, w, bcc, b1, c->clk, (Real*)r.dflx, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f);
   }
   {
-    int seg = c->lc.seg_x2 > 0 ? c->lc.seg_x2 : m.nx2 + 1;
-    const long long nseg = (m.nx2 + 1 + seg - 1) / seg;
+    int seg = c->lc.seg_x2 > 0 ? c->lc.seg_x2 : m.nx2;
+    const long long nseg = (m.nx2 + seg - 1) / seg;
     const long long n = nseg * m.nb * (m.nx3 + 2) * (long long)(m.nx1 + 2);
     ProfScope ps(c, "flux_x2");
-    flux_sweep_kernel<Real, 1, ORDER, RS><<<nblk(n, 128), 128, 0, s>>>(
-        m, seg, w, bcc, b2, c->clk, (Real*)r.flx2, (Real*)r.e1x2, (Real*)r.e3x2,
-        (Real*)r.w2f);
+    flux_sweep_kernel<Real, 1, ORDER, RS, KAHAN><<<nblk(n, 128), 128, 0, s>>>(
+        m, seg, w, bcc, b2, c->clk, (Real*)r.dflx, (Real*)r.e1x2, (Real*)r.e3x2,
+        (Real*)r.w2f, ua);
   }
   {
-    int seg = c->lc.seg_x3 > 0 ? c->lc.seg_x3 : m.nx3 + 1;
-    const long long nseg = (m.nx3 + 1 + seg - 1) / seg;
+    int seg = c->lc.seg_x3 > 0 ? c->lc.seg_x3 : m.nx3;
+    const long long nseg = (m.nx3 + seg - 1) / seg;
     const long long n = nseg * m.nb * (m.nx2 + 2) * (long long)(m.nx1 + 2);
-    ProfScope ps(c, "flux_x3");
-    flux_sweep_kernel<Real, 2, ORDER, RS><<<nblk(n, 128), 128, 0, s>>>(
-        m, seg, w, bcc, b3, c->clk, (Real*)r.flx3, (Real*)r.e2x3, (Real*)r.e1x3,
-        (Real*)r.w3f);
+    ProfScope ps(c, "flux_x3_update");
+    flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN><<<nblk(n, 128), 128, 0, s>>>(
+        m, seg, w, bcc, b3, c->clk, (Real*)r.dflx, (Real*)r.e2x3, (Real*)r.e1x3,
+        (Real*)r.w3f, ua);
   }
   c->launches += 3;
 }
@@ -51,21 +51,20 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
   cudaStream_t s = c->stream;
   const long long nc = (long long)m.nb * m.ncell;
   {
-    ProfScope ps(c, "exchange_u");
-    exchange_kernel<Real, 0><<<nblk(nc, 256), 256, 0, s>>>(m, NHYDRO, u);
-  }
-  {
-    ProfScope ps(c, "exchange_b");
-    exchange_kernel<double, 1><<<nblk((long long)m.nb * m.nf1, 256), 256, 0, s>>>(m, 1, b1);
-    exchange_kernel<double, 2><<<nblk((long long)m.nb * m.nf2, 256), 256, 0, s>>>(m, 1, b2);
-    exchange_kernel<double, 3><<<nblk((long long)m.nb * m.nf3, 256), 256, 0, s>>>(m, 1, b3);
+    const long long gc = m.ncell - (long long)m.nx1 * m.nx2 * m.nx3;
+    const long long g1 = m.nf1 - (long long)(m.nx1 + 1) * m.nx2 * m.nx3;
+    const long long g2 = m.nf2 - (long long)m.nx1 * (m.nx2 + 1) * m.nx3;
+    const long long g3 = m.nf3 - (long long)m.nx1 * m.nx2 * (m.nx3 + 1);
+    const long long n = (gc + g1 + g2 + g3) * m.nb;
+    ProfScope ps(c, "exchange");
+    exchange_kernel<Real><<<nblk(n, 256), 256, 0, s>>>(m, u, b1, b2, b3);
   }
   // the compensation register belongs to U only; the stage-1 register U* has none
   Real* lo = (u == (Real*)c->r.u) ? (Real*)c->r.ulo : nullptr;
   ProfScope ps(c, "c2p");
   c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
       m, do_dt, b1, b2, b3, u, lo, (Real*)c->r.w, (Real*)c->r.bcc, c->clk);
-  c->launches += 5;
+  c->launches += 2;
 }
 
 template <typename Real, int KAHAN>
@@ -82,7 +81,14 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   const Real* w = (const Real*)r.w;
   const Real* bcc = (const Real*)r.bcc;
   const int rs = c->desc.rsolver;
-#define FLUX(O, R) launch_fluxes<Real, O, R>(c, w, bcc, bb1, bb2, bb3)
+  Real* uout = (stage == 1) ? (Real*)r.ustar : (Real*)r.u;
+  UpdateArgs ua;
+  ua.beta = beta;
+  ua.stage = stage;
+  ua.uin = r.u;
+  ua.uout = uout;
+  ua.ulo = r.ulo;
+#define FLUX(O, R) launch_fluxes<Real, O, R, KAHAN>(c, w, bcc, bb1, bb2, bb3, ua)
   if (order == 1) { if (rs == 0) FLUX(1, 0); else FLUX(1, 1); }
   else if (order == 2) { if (rs == 0) FLUX(2, 0); else FLUX(2, 1); }
   else { if (rs == 0) FLUX(3, 0); else FLUX(3, 1); }
@@ -95,14 +101,6 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
         (Real*)r.e3x2, (Real*)r.w2f, (Real*)r.e1x3, (Real*)r.e2x3, (Real*)r.w3f,
         (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
   }
-  Real* uout = (stage == 1) ? (Real*)r.ustar : (Real*)r.u;
-  {
-    const long long n = (long long)m.nb * m.nx3 * m.nx2 * m.nx1;
-    ProfScope ps(c, "update");
-    update_kernel<Real, KAHAN><<<nblk(n, 128), 128, 0, s>>>(
-        m, beta, stage, c->clk, (Real*)r.flx1, (Real*)r.flx2, (Real*)r.flx3, (Real*)r.u,
-        uout, (Real*)r.ulo);
-  }
   double* o1 = (stage == 1) ? r.bs1 : r.b1;
   double* o2 = (stage == 1) ? r.bs2 : r.b2;
   double* o3 = (stage == 1) ? r.bs3 : r.b3;
@@ -110,12 +108,12 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
     const long long per = (long long)m.nx3 * m.nx2 * (m.nx1 + 1) +
                           (long long)m.nx3 * (m.nx2 + 1) * m.nx1 +
                           (long long)(m.nx3 + 1) * m.nx2 * m.nx1;
+    dim3 grid(nblk(per, 256) < 64 ? nblk(per, 256) : 64, m.nb);
     ProfScope ps(c, "ct");
-    ct_kernel<Real><<<nblk(per * m.nb, 128), 128, 0, s>>>(
-        m, beta, c->clk, (Real*)r.e1, (Real*)r.e2, (Real*)r.e3, r.b1, r.b2, r.b3, o1, o2,
-        o3);
+    ct_kernel<Real><<<grid, 256, 0, s>>>(m, beta, c->clk, (Real*)r.e1, (Real*)r.e2,
+                                         (Real*)r.e3, r.b1, r.b2, r.b3, o1, o2, o3);
   }
-  c->launches += 3;
+  c->launches += 2;
   launch_exchange_and_c2p<Real, KAHAN>(c, uout, o1, o2, o3, stage == 2);
   return cudaGetLastError();
 }

@@ -66,3 +66,15 @@ def test_null_context_calls_fail(lib):
     assert lib.athgpu_cycle(None, 1) == -1
     assert lib.athgpu_initialize(None) == -1
     assert lib.athgpu_destroy(None) == 0
+
+
+def test_non_uniform_spacing_is_rejected(lib):
+    """The kernels implement the reference's uniform-Cartesian branches only."""
+    mesh = MeshSpec((16, 8, 8), (2, 1, 1), 2)
+    coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
+    coords[1][1, 5] *= 1.01   # one x1 spacing of block 1
+    d, _ = _desc(mesh)
+    d.x1f, d.dx1f, d.x2f, d.dx2f, d.x3f, d.dx3f = [rt._dp(c) for c in coords]
+    h = ctypes.c_void_p()
+    assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -3
+    assert b"uniform" in lib.athgpu_last_error()

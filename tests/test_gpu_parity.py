@@ -187,4 +187,4 @@ def test_graph_replay_counts_launches():
     g.cycle(3)
     g.synchronize()
     per = g.launch_count() / 3
-    assert per == 2 * 11 + 1   # two stages of 11 kernels, one clock update
+    assert per == 2 * 7 + 1   # two stages of 7 kernels, one clock update
