@@ -23,6 +23,8 @@ UNITS = {
     # FP32 path: FMA contraction and the fast (approximate) FP32 divide and square root
     "stage_fp32.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"],
     "noalloc.cu": ["-fmad=false"],
+    # learned con2prim: the FP64 polish keeps the reference's rounding (no contraction)
+    "sr_learned.cu": ["-fmad=false"],
 }
 
 

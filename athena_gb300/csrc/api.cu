@@ -49,7 +49,7 @@ long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
 void free_all(athgpu_ctx* c) {
   Registers& r = c->r;
-  void* ptrs[] = {r.u, r.ustar, r.ulo, r.w, r.bcc, r.dflx, r.e3x1, r.e2x1,
+  void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->nbr,
                   c->staging};
@@ -121,8 +121,11 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "unknown Riemann solver");
   if (d->precision != ATHGPU_FP64 && d->precision != ATHGPU_FP32)
     return fail(ATHGPU_ERR_ARG, "unknown precision");
-  if (d->relativistic)
-    return fail(ATHGPU_ERR_UNSUPPORTED, "relativistic MHD is not in this entry point");
+  if (d->relativistic && d->rsolver != ATHGPU_HLLE)
+    return fail(ATHGPU_ERR_UNSUPPORTED,
+                "relativistic MHD supports the HLLE solver (hlle_mhd_rel.cpp) only");
+  if (d->relativistic && !(d->gamma_max > 1.0))
+    return fail(ATHGPU_ERR_ARG, "gamma_max must exceed 1 (adiabatic_mhd_sr.cpp:48)");
   if (!d->x1f || !d->dx1f || !d->x2f || !d->dx2f || !d->x3f || !d->dx3f)
     return fail(ATHGPU_ERR_ARG, "coordinate arrays are required");
   if (!(d->gamma > 1.0) || !(d->cfl_number > 0.0))
@@ -177,7 +180,8 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   struct A { void** p; i64 bytes; };
   std::vector<A> allocs = {
       {&r.u, nb * 5 * m.ncell * rb}, {&r.ustar, nb * 5 * m.ncell * rb},
-      {&r.w, nb * 5 * m.ncell * rb}, {&r.bcc, nb * 3 * m.ncell * rb},
+      {&r.wbuf[0], nb * 5 * m.ncell * rb}, {&r.wbuf[1], nb * 5 * m.ncell * rb},
+      {&r.bcc, nb * 3 * m.ncell * rb},
       {&r.dflx, nb * 5 * m.ncell * rb},
       {&r.e3x1, nb * m.nf1 * rb}, {&r.e2x1, nb * m.nf1 * rb}, {&r.w1f, nb * m.nf1 * rb},
       {&r.e1x2, nb * m.nf2 * rb}, {&r.e3x2, nb * m.nf2 * rb}, {&r.w2f, nb * m.nf2 * rb},
@@ -296,6 +300,16 @@ athgpu_status athgpu_upload_state(athgpu_ctx* c, const double* u, const double* 
   return ATHGPU_OK;
 }
 
+athgpu_status athgpu_upload_prim(athgpu_ctx* c, const double* w) {
+  if (!c || !w) return fail(ATHGPU_ERR_ARG, "null argument");
+  const i64 n = (i64)c->m.nb * 5 * c->m.ncell;
+  athgpu_status s;
+  for (int q = 0; q < 2; ++q)
+    if ((s = upload_bulk(c, w, c->r.wbuf[q], nullptr, n)) != ATHGPU_OK) return s;
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
 athgpu_status athgpu_download_state(athgpu_ctx* c, double* u, double* b1, double* b2,
                                     double* b3) {
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
@@ -314,7 +328,8 @@ athgpu_status athgpu_download_prim(athgpu_ctx* c, double* w, double* bcc) {
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   const DevMesh& m = c->m;
   athgpu_status s;
-  if (w && (s = download_bulk(c, w, c->r.w, nullptr, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
+  if (w && (s = download_bulk(c, w, c->r.wbuf[c->r.wsel], nullptr, (i64)m.nb * 5 * m.ncell)) !=
+               ATHGPU_OK)
     return s;
   if (bcc && (s = download_bulk(c, bcc, c->r.bcc, nullptr, (i64)m.nb * 3 * m.ncell)) !=
                  ATHGPU_OK)
@@ -345,7 +360,7 @@ athgpu_status athgpu_cycle(athgpu_ctx* c, int ncycles) {
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   if (!c->initialized) return fail(ATHGPU_ERR_STATE, "athgpu_initialize not called");
   if (ncycles < 0) return fail(ATHGPU_ERR_ARG, "ncycles < 0");
-  if (!c->cycle_exec || c->graph_stream != c->stream) {
+  if (!c->cycle_exec || c->graph_stream != c->stream || c->graph_wsel != c->r.wsel) {
     if (c->cycle_exec) { cudaGraphExecDestroy(c->cycle_exec); c->cycle_exec = nullptr; }
     if (c->cycle_graph) { cudaGraphDestroy(c->cycle_graph); c->cycle_graph = nullptr; }
     long long l0 = c->launches;
@@ -362,6 +377,7 @@ athgpu_status athgpu_cycle(athgpu_ctx* c, int ncycles) {
     c->cycle_graph = g;
     CK(cudaGraphInstantiate(&c->cycle_exec, g, 0));
     c->graph_stream = c->stream;
+    c->graph_wsel = c->r.wsel;  // the graph bakes in which primitive buffer is current
     c->per_cycle = c->launches - l0;  // kernels in one replay of the graph
     c->launches = l0;                 // capturing launched nothing
 
@@ -436,7 +452,7 @@ athgpu_status athgpu_device_state_ptrs(athgpu_ctx* c, athgpu_device_state* out) 
   if (!c || !out) return fail(ATHGPU_ERR_ARG, "null argument");
   out->u = c->r.u;
   out->ulo = c->r.ulo;
-  out->w = c->r.w;
+  out->w = c->r.wbuf[c->r.wsel];
   out->bcc = c->r.bcc;
   out->b1 = c->r.b1;
   out->b2 = c->r.b2;

@@ -12,7 +12,11 @@ namespace athgpu {
 
 struct Registers {
   // bulk precision (double or float) arrays; `void*` so one struct serves both paths
-  void *u = nullptr, *ustar = nullptr, *ulo = nullptr, *w = nullptr, *bcc = nullptr;
+  void *u = nullptr, *ustar = nullptr, *ulo = nullptr, *bcc = nullptr;
+  // primitives, double-buffered: each W(U) writes the buffer that is not current, seeded
+  // with its previous contents (the reference's w / w1 pair, time_integrator.cpp:2221-2269)
+  void* wbuf[2] = {nullptr, nullptr};
+  int wsel = 0;  // index of the current primitives
   void *dflx = nullptr;  // per-cell flux divergence accumulated by the sweeps
   void *e3x1 = nullptr, *e2x1 = nullptr, *w1f = nullptr;
   void *e1x2 = nullptr, *e3x2 = nullptr, *w2f = nullptr;
@@ -41,6 +45,7 @@ struct athgpu_ctx {
   cudaGraphExec_t cycle_exec = nullptr;
   cudaGraph_t cycle_graph = nullptr;
   cudaStream_t graph_stream = nullptr;
+  int graph_wsel = 0;
   bool initialized = false;
   int real_bytes = 8;
   long long launches = 0;

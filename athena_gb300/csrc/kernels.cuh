@@ -133,7 +133,8 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   Real wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
   Real f[NWAVE];
   if (RS == 0) hlld<Real>((Real)m.gamma, wli, wri, bx, f);
-  else hlle<Real>((Real)m.gamma, wli, wri, bx, f);
+  else if (RS == 1) hlle<Real>((Real)m.gamma, wli, wri, bx, f);
+  else hlle_sr<Real>((Real)m.gamma, wli, wri, bx, f);  // special relativity
   fn[IDN] = f[0];
   fn[ivx] = f[1];
   fn[ivy] = f[2];
@@ -319,22 +320,26 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
 // Field::ComputeCornerE, calculate_corner_e.cpp:124-236 (3-D Newtonian branch).  The cell
 // centred E = -v x B (cc_e_, :174-181) is formed on the fly from w and bcc.  One thread
 // per corner point (b, k, j, i) in [ks,ke+1]x[js,je+1]x[is,ie+1].
-template <typename Real>
+template <typename Real, bool SR>
 __device__ __forceinline__ Real cce(const DevMesh& m, const Real* __restrict__ w,
                                     const Real* __restrict__ bcc, int b, int n, int k,
                                     int j, int i) {
   const i64 cw = cidx(m, b, 0, NHYDRO, k, j, i), cb = cidx(m, b, 0, 3, k, j, i);
   const i64 vs = m.ncell;
-  if (n == 0)
-    return __ldg(w + cw + 3 * vs) * __ldg(bcc + cb + vs) -
-           __ldg(w + cw + 2 * vs) * __ldg(bcc + cb + 2 * vs);
-  if (n == 1)
-    return __ldg(w + cw + vs) * __ldg(bcc + cb + 2 * vs) -
-           __ldg(w + cw + 3 * vs) * __ldg(bcc + cb);
-  return __ldg(w + cw + 2 * vs) * __ldg(bcc + cb) - __ldg(w + cw + vs) * __ldg(bcc + cb + vs);
+  const Real v1 = __ldg(w + cw + vs), v2 = __ldg(w + cw + 2 * vs), v3 = __ldg(w + cw + 3 * vs);
+  const Real b1 = __ldg(bcc + cb), b2 = __ldg(bcc + cb + vs), b3 = __ldg(bcc + cb + 2 * vs);
+  if (SR) {  // calculate_corner_e.cpp:161-172: E = -(u x B)/u0 with u^i the 4-velocity
+    const Real u0 = dsqrt(Real(1.0) + v1 * v1 + v2 * v2 + v3 * v3);
+    if (n == 0) return (v3 * b2 - v2 * b3) / u0;
+    if (n == 1) return (v1 * b3 - v3 * b1) / u0;
+    return (v2 * b1 - v1 * b2) / u0;
+  }
+  if (n == 0) return v3 * b2 - v2 * b3;
+  if (n == 1) return v1 * b3 - v3 * b1;
+  return v2 * b1 - v1 * b2;
 }
 
-template <typename Real>
+template <typename Real, bool SR>
 __global__ void __launch_bounds__(128)
 corner_e_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ bcc,
                 const Real* __restrict__ e3x1, const Real* __restrict__ e2x1,
@@ -362,7 +367,7 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ 
 #define E3X2(kk, jj, ii) __ldg(e3x2 + f2idx(m, b, kk, jj, ii))
 #define E1X3(kk, jj, ii) __ldg(e1x3 + f3idx(m, b, kk, jj, ii))
 #define E2X3(kk, jj, ii) __ldg(e2x3 + f3idx(m, b, kk, jj, ii))
-#define CC(n, kk, jj, ii) cce<Real>(m, w, bcc, b, n, kk, jj, ii)
+#define CC(n, kk, jj, ii) cce<Real, SR>(m, w, bcc, b, n, kk, jj, ii)
   if (i <= m.ie) {
     Real de1_l3 = (one - W2F(k - 1, j, i)) * (E1X3(k, j, i) - CC(0, k - 1, j, i)) +
                   (W2F(k - 1, j, i)) * (E1X3(k, j - 1, i) - CC(0, k - 1, j - 1, i));
@@ -704,6 +709,71 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
       speed = smax<Real>(Real(0.0), (dabs(vz) + cf));
       dt3 /= (speed);
       cell_dt = (double)smin<Real>(smin<Real>(dt1, dt2), dt3);
+    }
+  }
+  if (do_dt) {
+    double v = warp_min(cell_dt);
+    if ((threadIdx.x & 31) == 0 && v < 1.0e300)
+      atomicMin(&clk->dtmin_bits, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// EquationOfState::ConservedToPrimitive for SR MHD (adiabatic_mhd_sr.cpp:72-272) over
+// whole blocks, in FP64: the Newman-Hamlin solve of every cell is seeded from the output
+// array's previous contents (wout holds the primitives of two con2prim calls ago, the
+// reference's w1 register, :143-154 and time_integrator.cpp:2221-2269).  In FP32 mode the
+// conserved input is hi + lo and a re-synced conserved state is split back.  When do_dt
+// is set the interior cells contribute min(dx1, dx2, dx3) to the CFL reduction (the SR
+// branch of new_blockdt.cpp:74 keeps the widths: signal speed 1).
+template <typename Real, int KAHAN>
+__global__ void __launch_bounds__(128)
+c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
+              const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
+              Real* ulo, Real* __restrict__ wout, Real* __restrict__ bcc, DevClock* clk) {
+  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  double cell_dt = 1.0e300;
+  if (t < (i64)m.nb * m.ncell) {
+    const int b = (int)(t / m.ncell);
+    i64 r = t - (i64)b * m.ncell;
+    const int i = (int)(r % m.nc1);
+    r /= m.nc1;
+    const int j = (int)(r % m.nc2);
+    const int k = (int)(r / m.nc2);
+    const double lw = 0.5, rw = 0.5;
+    const double bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
+    const double bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
+    const double bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
+    const i64 vs = m.ncell;
+    const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
+    const i64 cb = cidx(m, b, 0, 3, k, j, i);
+    double cons[NHYDRO], prim[NHYDRO];
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n) {
+      cons[n] = (double)u[c + n * vs] + ((KAHAN && ulo) ? (double)ulo[c + n * vs] : 0.0);
+      prim[n] = (double)wout[c + n * vs];
+    }
+    bool fixed = false;
+    int it = 0;
+    const bool ok = sr_c2p_cell(fp, cons, bc1, bc2, bc3, prim, &fixed, &it);
+#pragma unroll
+    for (int n = 0; n < NHYDRO; ++n) wout[c + n * vs] = (Real)prim[n];
+    bcc[cb] = (Real)bc1;
+    bcc[cb + vs] = (Real)bc2;
+    bcc[cb + 2 * vs] = (Real)bc3;
+    if (fixed) {
+#pragma unroll
+      for (int n = 0; n < NHYDRO; ++n) {
+        const Real hi = (Real)cons[n];
+        u[c + n * vs] = hi;
+        if (KAHAN && ulo) ulo[c + n * vs] = (Real)(cons[n] - (double)hi);
+      }
+    }
+    if (do_dt && (fixed || !ok)) atomicAdd(&clk->c2p_floor_count, 1);
+    if (do_dt && i >= m.is && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
+        k <= m.ke) {
+      const double dt1 = m.dx1f[(i64)b * m.nc1 + i], dt2 = m.dx2f[(i64)b * m.nc2 + j],
+                   dt3 = m.dx3f[(i64)b * m.nc3 + k];
+      cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
     }
   }
   if (do_dt) {

@@ -388,5 +388,323 @@ __device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_
   qrm = qminus;
 }
 
+
+// ---------------------------------------------------------------------------------------
+// Special-relativistic MHD.  Primitive velocities are the spatial 4-velocity u^i.
+
+// FastMagnetosonicSpeedsGR with the SR metric (g00, g01, g11) = (-1, 0, 1),
+// eos/adiabatic_mhd_sr.cpp:350-370
+template <typename Real>
+__device__ __forceinline__ void sr_fast_speeds(Real gamma_adi, Real wgas, Real pgas, Real u0,
+                                               Real u1, Real b_sq, Real* lp, Real* lm) {
+  const Real g00 = RC(-1.0), g01 = RC(0.0), g11 = RC(1.0);
+  Real cs_sq = gamma_adi * pgas / wgas;
+  Real va_sq = b_sq / (b_sq + wgas);
+  Real cms_sq = cs_sq + va_sq - cs_sq * va_sq;
+  Real a = u0 * u0 - (g00 + u0 * u0) * cms_sq;
+  Real b = RC(-2.0) * (u0 * u1 - (g01 + u0 * u1) * cms_sq);
+  Real c = u1 * u1 - (g11 + u1 * u1) * cms_sq;
+  Real a1 = b / a;
+  Real a0 = c / a;
+  Real s = dsqrt(smax(a1 * a1 - RC(4.0) * a0, RC(0.0)));
+  *lp = (a1 >= RC(0.0)) ? RC(-2.0) * a0 / (a1 + s) : (-a1 + s) / RC(2.0);
+  *lm = (a1 >= RC(0.0)) ? (-a1 - s) / RC(2.0) : RC(-2.0) * a0 / (a1 - s);
+}
+
+// Frame-transforming HLLE (Mignone & Bodo 2005), SR branch of
+// hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330.  Local order as for hlld().
+template <typename Real>
+__device__ __forceinline__ void hlle_sr(Real gamma_adi, const Real* wli, const Real* wri,
+                                        Real bb1, Real* f) {
+  Real cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  Real lml, lpl, lmr, lpr;
+#pragma unroll
+  for (int sd = 0; sd < 2; ++sd) {
+    const Real* w = sd == 0 ? wli : wri;
+    Real* c = sd == 0 ? cl : cr;
+    Real* ff = sd == 0 ? fl : fr;
+    Real rho = w[IDN], pgas = w[IPR];
+    Real u0 = dsqrt(RC(1.0) + w[IVX] * w[IVX] + w[IVY] * w[IVY] + w[IVZ] * w[IVZ]);
+    Real u1 = w[IVX], u2 = w[IVY], u3 = w[IVZ];
+    Real bb2 = w[IBY], bb3 = w[IBZ];
+    Real b0 = bb1 * u1 + bb2 * u2 + bb3 * u3;
+    Real b1 = (bb1 + b0 * u1) / u0;
+    Real b2 = (bb2 + b0 * u2) / u0;
+    Real b3 = (bb3 + b0 * u3) / u0;
+    Real b_sq = -(b0 * b0) + b1 * b1 + b2 * b2 + b3 * b3;
+    Real wgas = rho + gamma_adi / (gamma_adi - RC(1.0)) * pgas;
+    if (sd == 0) sr_fast_speeds(gamma_adi, wgas, pgas, u0, u1, b_sq, &lpl, &lml);
+    else sr_fast_speeds(gamma_adi, wgas, pgas, u0, u1, b_sq, &lpr, &lmr);
+    Real wtot = wgas + b_sq, ptot = pgas + RC(0.5) * b_sq;
+    c[0] = rho * u0;
+    c[4] = wtot * u0 * u0 - b0 * b0 - ptot;
+    c[1] = wtot * u1 * u0 - b1 * b0;
+    c[2] = wtot * u2 * u0 - b2 * b0;
+    c[3] = wtot * u3 * u0 - b3 * b0;
+    c[5] = b2 * u0 - b0 * u2;
+    c[6] = b3 * u0 - b0 * u3;
+    ff[0] = rho * u1;
+    ff[4] = wtot * u0 * u1 - b0 * b1;
+    ff[1] = wtot * u1 * u1 - b1 * b1 + ptot;
+    ff[2] = wtot * u2 * u1 - b2 * b1;
+    ff[3] = wtot * u3 * u1 - b3 * b1;
+    ff[5] = b2 * u1 - b1 * u2;
+    ff[6] = b3 * u1 - b1 * u3;
+  }
+  Real lambda_l = smin(lml, lmr);
+  Real lambda_r = smax(lpl, lpr);
+  Real lambda_diff_inv = RC(1.0) / (lambda_r - lambda_l);
+  const Real v_interface = RC(0.0);
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    if (lambda_l >= v_interface) f[n] = fl[n];
+    else if (lambda_r <= v_interface) f[n] = fr[n];
+    else f[n] = (lambda_r * fl[n] - lambda_l * fr[n] + lambda_l * lambda_r * (cr[n] - cl[n])) *
+                lambda_diff_inv;
+  }
+}
+
+// Newman & Hamlin (2014) fixed-point con2prim with Aitken acceleration,
+// ConservedToPrimitiveNormal, eos/adiabatic_mhd_sr.cpp:404-522.  prim[5] in natural
+// slots (rho, u1, u2, u3, p).  *iters = loop index at exit.  The FP64 instantiation is the
+// reference's solve; the FP32 one (tolerance relative to p) only refines a starting guess.
+__device__ __forceinline__ double m_acos(double x) { return acos(x); }
+__device__ __forceinline__ float m_acos(float x) { return acosf(x); }
+__device__ __forceinline__ double m_cos(double x) { return cos(x); }
+__device__ __forceinline__ float m_cos(float x) { return __cosf(x); }
+__device__ __forceinline__ double m_cbrt(double x) { return cbrt(x); }
+__device__ __forceinline__ float m_cbrt(float x) { return cbrtf(x); }
+
+// Loop indices [n0, n1) of the iteration on pgas[3] (the whole solver state at a loop
+// index: a solve stopped at any index resumes exactly).  Returns the index at which the
+// convergence test passed, or n1.  *last receives the most recently written pressure.
+template <typename Real>
+__device__ __forceinline__ int sr_nh_loop(Real gamma_adi, Real dd, Real ee, Real mm_sq,
+                                          Real bb_sq, Real tt, Real d, Real pgas_min,
+                                          Real* pgas, int n0, int n1, Real tol, bool rel_tol,
+                                          Real* last) {
+  const Real a_min = RC(1.0e-12);
+  const Real v_sq_max = RC(1.0) - RC(1.0e-12);
+  const Real rr_max = RC(1.0) - RC(1.0e-12);
+  const Real PI_ = RC(3.1415926535897932);
+  int n;
+  for (n = n0; n < n1; ++n) {
+    if (n % 3 != 2) {
+      Real a = ee + pgas[n % 3] + RC(0.5) * bb_sq;
+      a = smax(a, a_min);
+      Real phi = m_acos(RC(1.0) / a * dsqrt(RC(27.0) * d / (RC(4.0) * a)));
+      Real eee = a / RC(3.0) - RC(2.0) / RC(3.0) * a * m_cos(RC(2.0) / RC(3.0) * (phi + PI_));
+      Real ll = eee - bb_sq;
+      Real v_sq = (mm_sq * (ll * ll) + (tt * tt) * (bb_sq + RC(2.0) * ll)) /
+                  ((ll * (bb_sq + ll)) * (ll * (bb_sq + ll)));
+      v_sq = smin(smax(v_sq, RC(0.0)), v_sq_max);
+      Real gamma_sq = RC(1.0) / (RC(1.0) - v_sq);
+      Real gamma = dsqrt(gamma_sq);
+      Real wgas = ll / gamma_sq;
+      Real rho = dd / gamma;
+      Real pn = (gamma_adi - RC(1.0)) / gamma_adi * (wgas - rho);
+      pn = smax(pn, pgas_min);
+      pgas[(n + 1) % 3] = pn;
+      *last = pn;
+      const Real lim = rel_tol ? tol * pn : tol;
+      if (pn > pgas_min && dabs(pn - pgas[n % 3]) < lim) break;
+    } else {
+      Real rr = (pgas[2] - pgas[1]) / (pgas[1] - pgas[0]);
+      if (!isfinite(rr) || dabs(rr) > rr_max) continue;
+      pgas[0] = pgas[1] + (pgas[2] - pgas[1]) / (RC(1.0) - rr);
+      pgas[0] = smax(pgas[0], pgas_min);
+      *last = pgas[0];
+      const Real lim = rel_tol ? tol * pgas[0] : tol;
+      if (pgas[0] > pgas_min && dabs(pgas[0] - pgas[2]) < lim) break;
+    }
+  }
+  return n;
+}
+
+// the quantities of the solve that do not change between iterations (NH 5.7-5.9)
+template <typename Real>
+__device__ __forceinline__ void sr_nh_setup(Real ee, Real mm_sq, Real bb_sq, Real tt,
+                                            Real* d_out, Real* pgas_min_out) {
+  const Real pgas_uniform_min = RC(1.0e-12);
+  Real d = RC(0.5) * (mm_sq * bb_sq - tt * tt);
+  d = smax(d, RC(0.0));
+  Real pgas_min = m_cbrt(RC(27.0) / RC(4.0) * d) - ee - RC(0.5) * bb_sq;
+  *d_out = d;
+  *pgas_min_out = smax(pgas_min, pgas_uniform_min);
+}
+
+// primitives from the converged pressure (adiabatic_mhd_sr.cpp:486-521)
+template <typename Real>
+__device__ __forceinline__ bool sr_nh_finish(Real dd, Real ee, Real mm_sq, Real mm1,
+                                             Real mm2, Real mm3, Real bb_sq, Real bb1,
+                                             Real bb2, Real bb3, Real tt, Real d, Real pgas,
+                                             Real* prim, Real* p_gamma_lor, Real* p_pmag) {
+  const Real a_min = RC(1.0e-12);
+  const Real v_sq_max = RC(1.0) - RC(1.0e-12);
+  const Real PI_ = RC(3.1415926535897932);
+  prim[IPR] = pgas;
+  if (!isfinite(prim[IPR])) return false;
+  Real a = ee + prim[IPR] + RC(0.5) * bb_sq;
+  a = smax(a, a_min);
+  Real phi = m_acos(RC(1.0) / a * dsqrt(RC(27.0) * d / (RC(4.0) * a)));
+  Real eee = a / RC(3.0) - RC(2.0) / RC(3.0) * a * m_cos(RC(2.0) / RC(3.0) * (phi + PI_));
+  Real ll = eee - bb_sq;
+  Real v_sq = (mm_sq * (ll * ll) + (tt * tt) * (bb_sq + RC(2.0) * ll)) /
+              ((ll * (bb_sq + ll)) * (ll * (bb_sq + ll)));
+  v_sq = smin(smax(v_sq, RC(0.0)), v_sq_max);
+  Real gamma_sq = RC(1.0) / (RC(1.0) - v_sq);
+  Real gamma = dsqrt(gamma_sq);
+  prim[IDN] = dd / gamma;
+  if (!isfinite(prim[IDN])) return false;
+  Real ss = tt / ll;
+  Real v1 = (mm1 + ss * bb1) / (ll + bb_sq);
+  Real v2 = (mm2 + ss * bb2) / (ll + bb_sq);
+  Real v3 = (mm3 + ss * bb3) / (ll + bb_sq);
+  prim[IVX] = gamma * v1;
+  prim[IVY] = gamma * v2;
+  prim[IVZ] = gamma * v3;
+  if (!isfinite(prim[IVX]) || !isfinite(prim[IVY]) || !isfinite(prim[IVZ])) return false;
+  *p_gamma_lor = gamma;
+  *p_pmag = RC(0.5) * (bb_sq / gamma_sq + ss * ss);
+  return true;
+}
+
+template <typename Real>
+__device__ __forceinline__ bool sr_normal_t(Real gamma_adi, Real dd, Real ee, Real mm_sq,
+                                            Real mm1, Real mm2, Real mm3, Real bb_sq,
+                                            Real bb1, Real bb2, Real bb3, Real tt,
+                                            Real pgas_old, Real* prim, Real* p_gamma_lor,
+                                            Real* p_pmag, int* iters, int max_iterations,
+                                            Real tol, bool rel_tol) {
+  Real d, pgas_min, last;
+  sr_nh_setup<Real>(ee, mm_sq, bb_sq, tt, &d, &pgas_min);
+  Real pgas[3];
+  pgas[0] = smax(pgas_old, pgas_min);
+  const int n = sr_nh_loop<Real>(gamma_adi, dd, ee, mm_sq, bb_sq, tt, d, pgas_min, pgas, 0,
+                                 max_iterations, tol, rel_tol, &last);
+  *iters = n;
+  if (n == max_iterations) return false;
+  return sr_nh_finish<Real>(dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bb1, bb2, bb3, tt, d,
+                            pgas[(n + 1) % 3], prim, p_gamma_lor, p_pmag);
+}
+
+// the reference's solve: at most 15 iterations, absolute tolerance 1e-12 on p
+// (adiabatic_mhd_sr.cpp:409-411)
+__device__ __forceinline__ bool sr_normal(double gamma_adi, double dd, double ee,
+                                          double mm_sq, double mm1, double mm2, double mm3,
+                                          double bb_sq, double bb1, double bb2, double bb3,
+                                          double tt, double pgas_old, double* prim,
+                                          double* p_gamma_lor, double* p_pmag, int* iters) {
+  return sr_normal_t<double>(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bb1, bb2, bb3,
+                             tt, pgas_old, prim, p_gamma_lor, p_pmag, iters, 15, 1.0e-12,
+                             false);
+}
+
+struct SRFloors { double gamma_adi, dfloor, pfloor, sigma_max, beta_min, gamma_max; };
+
+// One cell of EquationOfState::ConservedToPrimitive (SR), adiabatic_mhd_sr.cpp:87-268:
+// conserved floors, solve from the guess in prim (the output array's stale value,
+// :143-154), fallback, floors, gamma ceiling, conserved re-sync.  cons[5] (natural slots)
+// may be rewritten (*fixed set).  Returns false if the solve failed.
+__device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, double bc1,
+                                            double bc2, double bc3, double* prim,
+                                            bool* fixed_out, int* iters) {
+  const double gamma_adi = fp.gamma_adi;
+  const double mm_sq_ee_sq_max = 1.0 - 1.0e-12;
+  double dd = cons[IDN], ee = cons[IPR];
+  double mm_sq = cons[IVX] * cons[IVX] + cons[IVY] * cons[IVY] + cons[IVZ] * cons[IVZ];
+  double mm1 = cons[IVX], mm2 = cons[IVY], mm3 = cons[IVZ];
+  double bb_sq = bc1 * bc1 + bc2 * bc2 + bc3 * bc3;
+  double tt = cons[IVX] * bc1 + cons[IVY] * bc2 + cons[IVZ] * bc3;
+  bool fixed = false;
+  double density_floor_local = fp.dfloor, pressure_floor_local = fp.pfloor;
+  if (dd < density_floor_local) { dd = density_floor_local; fixed = true; }
+  double ee_min = density_floor_local + pressure_floor_local / (gamma_adi - 1.0) + 0.5 * bb_sq;
+  if (ee < ee_min) { ee = ee_min; fixed = true; }
+  double mm_sq_max = mm_sq_ee_sq_max * (ee * ee);
+  if (mm_sq > mm_sq_max) {
+    double factor = sqrt(mm_sq_max / mm_sq);
+    mm_sq = mm_sq_max;
+    mm1 *= factor; mm2 *= factor; mm3 *= factor;
+    tt *= factor;
+    fixed = true;
+  }
+  double rho_old = smax(prim[IDN], density_floor_local);
+  double pgas_old = smax(prim[IPR], pressure_floor_local);
+  double u1_old = prim[IVX], u2_old = prim[IVY], u3_old = prim[IVZ];
+  double gamma = 0.0, pmag = 0.0;
+  bool success = sr_normal(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2, bc3, tt,
+                           pgas_old, prim, &gamma, &pmag, iters);
+  if (!success) {
+    prim[IDN] = rho_old; prim[IPR] = pgas_old;
+    prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;
+    fixed = true;
+  }
+  if (fp.sigma_max > 0.0)
+    density_floor_local = smax(density_floor_local, 2.0 * pmag / fp.sigma_max);
+  if (fp.beta_min > 0.0)
+    pressure_floor_local = smax(pressure_floor_local, fp.beta_min * pmag);
+  double rho_add = smax(density_floor_local - prim[IDN], 0.0);
+  double pgas_add = smax(pressure_floor_local - prim[IPR], 0.0);
+  if (success && (rho_add > 0.0 || pgas_add > 0.0)) {
+    double wgas_add = rho_add + gamma_adi / (gamma_adi - 1.0) * pgas_add;
+    dd += rho_add * gamma;
+    ee += wgas_add * (gamma * gamma) + pgas_add;
+    int it2;
+    success = sr_normal(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2, bc3, tt,
+                        pgas_old, prim, &gamma, &pmag, &it2);
+    if (!success) {
+      prim[IDN] = rho_old; prim[IPR] = pgas_old;
+      prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;
+    }
+    fixed = true;
+  }
+  if (!success)
+    gamma = sqrt(1.0 + prim[IVX] * prim[IVX] + prim[IVY] * prim[IVY] + prim[IVZ] * prim[IVZ]);
+  bool velocity_ceiling = false;
+  if (gamma > fp.gamma_max) {
+    double factor = sqrt((fp.gamma_max * fp.gamma_max - 1.0) / (gamma * gamma - 1.0));
+    prim[IVX] *= factor; prim[IVY] *= factor; prim[IVZ] *= factor;
+    fixed = true;
+    velocity_ceiling = true;
+  }
+  if (velocity_ceiling) {
+    double b0 = prim[IVX] * bc1 + prim[IVY] * bc2 + prim[IVZ] * bc3;
+    pmag = 0.5 * (bb_sq / (gamma * gamma) + (b0 / gamma) * (b0 / gamma));
+  }
+  density_floor_local = fp.dfloor;
+  if (fp.sigma_max > 0.0)
+    density_floor_local = smax(density_floor_local, 2.0 * pmag / fp.sigma_max);
+  pressure_floor_local = fp.pfloor;
+  if (fp.beta_min > 0.0)
+    pressure_floor_local = smax(pressure_floor_local, fp.beta_min * pmag);
+  if (prim[IDN] < density_floor_local) { prim[IDN] = density_floor_local; fixed = true; }
+  if (prim[IPR] < pressure_floor_local) { prim[IPR] = pressure_floor_local; fixed = true; }
+  if (!success) {
+    prim[IDN] = density_floor_local;
+    prim[IPR] = pressure_floor_local;
+    prim[IVX] = prim[IVY] = prim[IVZ] = 0.0;
+  }
+  if (fixed) {
+    double u1 = prim[IVX], u2 = prim[IVY], u3 = prim[IVZ], rho = prim[IDN], pg = prim[IPR];
+    gamma = sqrt(1.0 + u1 * u1 + u2 * u2 + u3 * u3);
+    double b0 = bc1 * u1 + bc2 * u2 + bc3 * u3;
+    double b1 = (bc1 + b0 * u1) / gamma;
+    double b2 = (bc2 + b0 * u2) / gamma;
+    double b3 = (bc3 + b0 * u3) / gamma;
+    double b_sq = -(b0 * b0) + b1 * b1 + b2 * b2 + b3 * b3;
+    double wgas = rho + gamma_adi / (gamma_adi - 1.0) * pg;
+    double wtot = wgas + b_sq;
+    pmag = 0.5 * b_sq;
+    cons[IDN] = rho * gamma;
+    cons[IPR] = wtot * (gamma * gamma) - (b0 * b0) - (pg + pmag);
+    cons[IVX] = wtot * gamma * u1 - b0 * b1;
+    cons[IVY] = wtot * gamma * u2 - b0 * b2;
+    cons[IVZ] = wtot * gamma * u3 - b0 * b3;
+  }
+  *fixed_out = fixed;
+  return success;
+}
+
 #undef RC
 }  // namespace athgpu

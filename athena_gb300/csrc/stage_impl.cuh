@@ -46,7 +46,7 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
 
 template <typename Real, int KAHAN>
 static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* b2,
-                                    double* b3, int do_dt) {
+                                    double* b3, int do_dt, bool rotate = true) {
   const DevMesh& m = c->m;
   cudaStream_t s = c->stream;
   const long long nc = (long long)m.nb * m.ncell;
@@ -61,9 +61,22 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
   }
   // the compensation register belongs to U only; the stage-1 register U* has none
   Real* lo = (u == (Real*)c->r.u) ? (Real*)c->r.ulo : nullptr;
-  ProfScope ps(c, "c2p");
-  c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
-      m, do_dt, b1, b2, b3, u, lo, (Real*)c->r.w, (Real*)c->r.bcc, c->clk);
+  // W(U) writes the non-current primitive buffer (seeded with its old contents), which
+  // then becomes current; initialize writes the current one in place
+  Real* wout = (Real*)c->r.wbuf[rotate ? 1 - c->r.wsel : c->r.wsel];
+  {
+    ProfScope ps(c, "c2p");
+    if (c->desc.relativistic) {
+      SRFloors fp{c->desc.gamma, c->desc.dfloor, c->desc.pfloor, c->desc.sigma_max,
+                  c->desc.beta_min, c->desc.gamma_max};
+      c2p_sr_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
+          m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, c->clk);
+    } else {
+      c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
+          m, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, c->clk);
+    }
+  }
+  if (rotate) c->r.wsel = 1 - c->r.wsel;
   c->launches += 2;
 }
 
@@ -78,9 +91,9 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   const double* bb1 = (stage == 1) ? r.b1 : r.bs1;
   const double* bb2 = (stage == 1) ? r.b2 : r.bs2;
   const double* bb3 = (stage == 1) ? r.b3 : r.bs3;
-  const Real* w = (const Real*)r.w;
+  const Real* w = (const Real*)r.wbuf[r.wsel];
   const Real* bcc = (const Real*)r.bcc;
-  const int rs = c->desc.rsolver;
+  const int rs = c->desc.relativistic ? 2 : c->desc.rsolver;
   Real* uout = (stage == 1) ? (Real*)r.ustar : (Real*)r.u;
   UpdateArgs ua;
   ua.beta = beta;
@@ -89,14 +102,15 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   ua.uout = uout;
   ua.ulo = r.ulo;
 #define FLUX(O, R) launch_fluxes<Real, O, R, KAHAN>(c, w, bcc, bb1, bb2, bb3, ua)
-  if (order == 1) { if (rs == 0) FLUX(1, 0); else FLUX(1, 1); }
-  else if (order == 2) { if (rs == 0) FLUX(2, 0); else FLUX(2, 1); }
-  else { if (rs == 0) FLUX(3, 0); else FLUX(3, 1); }
+  if (order == 1) { if (rs == 0) FLUX(1, 0); else if (rs == 1) FLUX(1, 1); else FLUX(1, 2); }
+  else if (order == 2) { if (rs == 0) FLUX(2, 0); else if (rs == 1) FLUX(2, 1); else FLUX(2, 2); }
+  else { if (rs == 0) FLUX(3, 0); else if (rs == 1) FLUX(3, 1); else FLUX(3, 2); }
 #undef FLUX
   {
     const long long n = (long long)m.nb * (m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
     ProfScope ps(c, "corner_e");
-    corner_e_kernel<Real><<<nblk(n, 128), 128, 0, s>>>(
+    auto kern = c->desc.relativistic ? corner_e_kernel<Real, true> : corner_e_kernel<Real, false>;
+    kern<<<nblk(n, 128), 128, 0, s>>>(
         m, w, bcc, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f, (Real*)r.e1x2,
         (Real*)r.e3x2, (Real*)r.w2f, (Real*)r.e1x3, (Real*)r.e2x3, (Real*)r.w3f,
         (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
@@ -128,7 +142,8 @@ static inline cudaError_t run_end_cycle(athgpu_ctx* c) {
 
 template <typename Real, int KAHAN>
 static cudaError_t run_init(athgpu_ctx* c) {
-  launch_exchange_and_c2p<Real, KAHAN>(c, (Real*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1);
+  launch_exchange_and_c2p<Real, KAHAN>(c, (Real*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1,
+                                       false);
   advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->clk, c->m.cfl, c->m.tlim, 0);
   c->launches += 1;
   return cudaGetLastError();

@@ -366,3 +366,88 @@ def blast(nx, xmin=(-0.5, -0.5, -0.5), xmax=(0.5, 0.5, 0.5), gamma=5.0 / 3.0, p_
     w[4] = np.where(r < radius, p_in, p_out)
     f1, f2, f3 = faces_from_uniform(nx, b)
     return prim_to_cons(w, cell_centered(f1, f2, f3), gamma), f1, f2, f3
+
+
+# ---------------------------------------------------------------------------------------
+# Special-relativistic MHD states.  Primitives are (rho, u1, u2, u3, p) with u^i = gamma
+# v^i, the reference's SR convention (adiabatic_mhd_sr.cpp:489-520).
+
+def sr_prim_to_cons(w, bcc, gamma):
+    """SR-MHD W -> U (EquationOfState::PrimitiveToConserved, adiabatic_mhd_sr.cpp:284-332),
+    elementwise in the reference's operand order.  w[5, ...], bcc[3, ...]."""
+    gamma_adi_red = gamma / (gamma - 1.0)
+    rho, u1, u2, u3, pgas = w[0], w[1], w[2], w[3], w[4]
+    bb1, bb2, bb3 = bcc[0], bcc[1], bcc[2]
+    u0 = np.sqrt(1.0 + u1 * u1 + u2 * u2 + u3 * u3)
+    b0 = bb1 * u1 + bb2 * u2 + bb3 * u3
+    b1 = (bb1 + b0 * u1) / u0
+    b2 = (bb2 + b0 * u2) / u0
+    b3 = (bb3 + b0 * u3) / u0
+    b_sq = -(b0 * b0) + b1 * b1 + b2 * b2 + b3 * b3
+    wtot_u02 = (rho + gamma_adi_red * pgas + b_sq) * u0 * u0
+    u = np.empty_like(w)
+    u[0] = rho * u0
+    u[4] = wtot_u02 - b0 * b0 - (pgas + 0.5 * b_sq)
+    u[1] = wtot_u02 * u1 / u0 - b0 * b1
+    u[2] = wtot_u02 * u2 / u0 - b0 * b2
+    u[3] = wtot_u02 * u3 / u0 - b0 * b3
+    return u
+
+
+def sr_kelvin_helmholtz(nx, seed=20261204, gamma=4.0 / 3.0, vshear=0.5, width=0.01,
+                        rho_in=1.0, rho_out=0.1, p0=1.0, sigma=0.1, noise=1.0e-3):
+    """Relativistic Kelvin-Helmholtz shear layer on a periodic unit box: v_x = +vshear
+    for |y - 1/2| < 1/4 and -vshear outside, with tanh transitions of the given width,
+    density rho_in inside / rho_out outside, uniform pressure p0, uniform B_x with
+    magnetization sigma = B^2 / (rho_in h) of the inner layer, and seeded velocity noise.
+    Returns global primitives w[5, NX3, NX2, NX1] and face fields (f1, f2, f3)."""
+    n1, n2, n3 = nx
+    rng = np.random.default_rng(seed)
+    y = (np.arange(n2) + 0.5) / n2
+    prof = 0.5 * (np.tanh((y - 0.25) / width) - np.tanh((y - 0.75) / width))  # 1 inside
+    vx = (-vshear + 2.0 * vshear * prof)[None, :, None] * np.ones((n3, n2, n1))
+    rho = (rho_out + (rho_in - rho_out) * prof)[None, :, None] * np.ones((n3, n2, n1))
+    vx = vx + noise * rng.uniform(-1.0, 1.0, (n3, n2, n1))
+    vy = noise * rng.uniform(-1.0, 1.0, (n3, n2, n1))
+    vz = noise * rng.uniform(-1.0, 1.0, (n3, n2, n1))
+    lor = 1.0 / np.sqrt(1.0 - (vx * vx + vy * vy + vz * vz))
+    h = 1.0 + gamma / (gamma - 1.0) * p0 / rho_in
+    bx = np.sqrt(sigma * rho_in * h)
+    w = np.empty((5, n3, n2, n1))
+    w[0] = rho
+    w[1], w[2], w[3] = lor * vx, lor * vy, lor * vz
+    w[4] = p0
+    f1, f2, f3 = faces_from_uniform(nx, (bx, 0.0, 0.0))
+    return w, f1, f2, f3
+
+
+def sr_isolated_cells(n, seed=20261204, gamma=4.0 / 3.0, lorentz=(1.0, 10.0),
+                      sigma=(1.0e-2, 1.0e2), rho=(1.0e-4, 1.0), p_over_rho=(1.0e-3, 10.0)):
+    """Independent SR-MHD cells for the con2prim benchmark: Lorentz factor, magnetization
+    sigma = b^2/(rho h), rho and p/rho log-uniform in the given ranges, isotropic
+    directions of v and B.  Returns primitives w[n, 5] (rho, u1, u2, u3, p), lab-frame
+    field bcc[n, 3] and conserved u[n, 5] (D, M1, M2, M3, E)."""
+    rng = np.random.default_rng(seed)
+
+    def logu(lo_hi):
+        lo, hi = lo_hi
+        return np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+
+    def unit():
+        v = rng.standard_normal((n, 3))
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+    lor = logu(lorentz)
+    sig = logu(sigma)
+    d = logu(rho)
+    p = d * logu(p_over_rho)
+    uvec = np.sqrt(lor * lor - 1.0)[:, None] * unit()
+    bdir = unit()
+    h = 1.0 + gamma / (gamma - 1.0) * p / d
+    # comoving b^2 = sigma rho h; for lab field B along bdir with b^2 = (B^2 + (B.u)^2)/lor^2
+    bu = np.einsum("ij,ij->i", bdir, uvec)
+    bmag = np.sqrt(sig * d * h * lor * lor / (1.0 + bu * bu))
+    bcc = bmag[:, None] * bdir
+    w = np.stack([d, uvec[:, 0], uvec[:, 1], uvec[:, 2], p], axis=1)
+    u = sr_prim_to_cons(w.T, bcc.T, gamma).T
+    return w, bcc, u

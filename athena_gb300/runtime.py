@@ -40,7 +40,9 @@ class MeshDesc(ctypes.Structure):
                 ("x2f", ctypes.POINTER(ctypes.c_double)),
                 ("dx2f", ctypes.POINTER(ctypes.c_double)),
                 ("x3f", ctypes.POINTER(ctypes.c_double)),
-                ("dx3f", ctypes.POINTER(ctypes.c_double))]
+                ("dx3f", ctypes.POINTER(ctypes.c_double)),
+                ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
+                ("gamma_max", ctypes.c_double)]
 
 
 class DeviceState(ctypes.Structure):
@@ -66,6 +68,7 @@ def load_library(path=LIB_PATH):
         "athgpu_destroy": ([vp], ip),
         "athgpu_set_stream": ([vp, vp], ip),
         "athgpu_upload_state": ([vp, dp, dp, dp, dp], ip),
+        "athgpu_upload_prim": ([vp, dp], ip),
         "athgpu_download_state": ([vp, dp, dp, dp, dp], ip),
         "athgpu_download_prim": ([vp, dp, dp], ip),
         "athgpu_initialize": ([vp], ip),
@@ -119,7 +122,8 @@ class StageUpdate:
     """All MeshBlocks of one uniform mesh advanced by the GPU stage update."""
 
     def __init__(self, mesh: MeshSpec, gamma, xorder=2, rsolver="hlld", precision="fp64",
-                 cfl=0.3, tlim=1.0e30, dfloor=None, pfloor=None):
+                 cfl=0.3, tlim=1.0e30, dfloor=None, pfloor=None, relativistic=False,
+                 sigma_max=0.0, beta_min=0.0, gamma_max=1000.0):
         L = load_library()
         self.mesh = mesh
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
@@ -130,7 +134,8 @@ class StageUpdate:
         d.nghost, d.xorder = mesh.ng, xorder
         d.rsolver = HLLD if rsolver == "hlld" else HLLE
         d.precision = FP64 if precision == "fp64" else FP32
-        d.relativistic = 0
+        d.relativistic = 1 if relativistic else 0
+        d.sigma_max, d.beta_min, d.gamma_max = sigma_max, beta_min, gamma_max
         d.gamma = gamma
         d.dfloor = fl if dfloor is None else dfloor
         d.pfloor = fl if pfloor is None else pfloor
@@ -157,6 +162,11 @@ class StageUpdate:
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, b1, b2, b3)]
         _check(load_library().athgpu_upload_state(self.h, *[_dp(a) for a in arrs]),
                "athgpu_upload_state")
+
+    def set_prim(self, w):
+        """Initial primitives (relativistic runs: also the con2prim seed)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        _check(load_library().athgpu_upload_prim(self.h, _dp(w)), "athgpu_upload_prim")
 
     def state(self):
         m = self.mesh

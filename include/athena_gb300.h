@@ -51,7 +51,8 @@ typedef struct {
   int xorder;             /* time/xorder: 2 = PLM, 3 = PPM (stage 1 is donor cell) */
   int rsolver;            /* ATHGPU_HLLD or ATHGPU_HLLE */
   int precision;          /* ATHGPU_FP64 or ATHGPU_FP32 */
-  int relativistic;       /* must be 0 in this version */
+  int relativistic;       /* 1: special-relativistic MHD (-s): HLLE solver only, FP64
+                             Newman-Hamlin con2prim (adiabatic_mhd_sr.cpp) */
   double gamma;           /* hydro/gamma */
   double dfloor, pfloor;  /* hydro/dfloor, hydro/pfloor (adiabatic_mhd.cpp:29-30) */
   double cfl_number;      /* time/cfl_number */
@@ -59,6 +60,9 @@ typedef struct {
   /* per-block coordinate arrays exactly as Coordinates holds them (coordinates.cpp:92-146):
    * x?f [nb][nc?+1] face positions, dx?f [nb][nc?] face spacings (host memory) */
   const double *x1f, *dx1f, *x2f, *dx2f, *x3f, *dx3f;
+  /* SR floors and ceiling: hydro/sigma_max, beta_min (0 = off), gamma_max (reference
+   * default 1000), adiabatic_mhd_sr.cpp:46-48 */
+  double sigma_max, beta_min, gamma_max;
 } athgpu_mesh_desc;
 
 /* Allocate all device registers of the stage update for the mesh (replaces the
@@ -78,6 +82,10 @@ athgpu_status athgpu_upload_state(athgpu_ctx *ctx, const double *u, const double
                                   const double *b2, const double *b3);
 athgpu_status athgpu_download_state(athgpu_ctx *ctx, double *u, double *b1, double *b2,
                                     double *b3);
+/* Initial primitives W = phydro->w (relativistic runs: also the initial guess of the
+ * con2prim solve, which the reference seeds from its w / w1 registers,
+ * adiabatic_mhd_sr.cpp:143-154).  Synchronous. */
+athgpu_status athgpu_upload_prim(athgpu_ctx *ctx, const double *w);
 /* primitives W = phydro->w and bcc = pfield->bcc of the last conserved->primitive call */
 athgpu_status athgpu_download_prim(athgpu_ctx *ctx, double *w, double *bcc);
 
@@ -143,6 +151,65 @@ athgpu_status athgpu_launch_count(athgpu_ctx *ctx, long long *count, int reset);
 
 const char *athgpu_last_error(void);
 const char *athgpu_version(void);
+
+/* ---- Learned initial guess for the special-relativistic con2prim ----
+ * A 5 -> 64 -> 64 -> 2 SiLU network predicts (log(p_gas/E), log(Lorentz factor)) from the
+ * features of athgpu_sr_features; its start replaces the previous-pressure start of the
+ * Newman-Hamlin iteration in EquationOfState::ConservedToPrimitive
+ * (adiabatic_mhd_sr.cpp:143-154, solve :404-522).  No counterpart in the reference.
+ * Parameters are ATHGPU_MLP_NPARAM floats (device): W1[64][5], b1[64], W2[64][64], b2[64],
+ * W3[2][64], b3[2], then input means[5], input scales[5], output means[2], output
+ * scales[2] (inputs and targets are standardized as (v - mean)/scale).
+ * Per-cell arrays are cell-major: cons[n][5] = (D, M1, M2, M3, E) with E the total energy
+ * density including rest mass, bcc[n][3], prim[n][5] = (rho, u1, u2, u3, p_gas) (the
+ * reference's slots IDN, IVX, IVY, IVZ, IPR; u^i the spatial 4-velocity), features[n][5].
+ * All pointers are DEVICE pointers; calls are asynchronous on `stream` unless stated. */
+#define ATHGPU_MLP_NPARAM 4688
+
+/* features[n][5] = (log(D/E), log(M^2/E^2), log(B^2/E), (M.B)^2/(M^2 B^2),
+ * log((E - sqrt(M^2 + D^2))/E)), the last difference formed in FP64. */
+athgpu_status athgpu_sr_features(long long n, const double *cons, const double *bcc,
+                                 float *features, void *stream);
+
+/* Network outputs out[n][2] (de-standardized) for raw features[n][5], evaluated by the
+ * same BF16 tensor-core code (FP32 accumulation) as the fused con2prim. */
+athgpu_status athgpu_mlp_infer(long long n, const float *params, const float *features,
+                               float *out, void *stream);
+
+/* Newman-Hamlin root find per independent cell.  mode 0: start from pgas_guess[c] (the
+ * reference's start) or from pfloor when pgas_guess is NULL; mode 1: start from the
+ * network; mode 2: network start refined by at most 12 FP32 iterations of the same scheme.
+ * Two launches: loop indices [0, phase1_iterations) for every cell (0 = default: 7 in
+ * mode 0, 4 in modes 1-2), then the cells still iterating, resumed exactly.  Mode 0 is the
+ * reference's solve.  Modes 1-2 solve a cell again from the mode-0 start when the learned
+ * start does not converge within the reference's 15 FP64 iterations, and then from the
+ * learned attempt's last iterate (*fallbacks, may be NULL, counts cells that needed it).
+ * prim[n][5] as ConservedToPrimitiveNormal leaves it (zeros before the solve),
+ * iters64[n] = FP64 loop passes over all attempts (-1 = not converged), iters32[n] (may
+ * be NULL) = FP32 refinement passes.  Allocates a queue of 40 bytes per cell with
+ * cudaMallocAsync on the stream. */
+athgpu_status athgpu_sr_c2p_cells(long long n, double gamma, double pfloor, const double *cons,
+                                  const double *bcc, const double *pgas_guess,
+                                  const float *params, int mode, int phase1_iterations,
+                                  double *prim, int *iters64, int *iters32, int *fallbacks,
+                                  void *stream);
+
+/* Gradient of the mean squared error over batch rows and both outputs of standardized
+ * inputs x[batch][5] against standardized targets t[batch][2] with respect to the 4674
+ * trainable parameters: grad[4674], loss[1].  FP32 forward/backward kernels (the
+ * batch-chunk partial sums of the weight gradient are added atomically, so the last bits
+ * may vary between calls); allocates scratch with cudaMallocAsync on the stream. */
+athgpu_status athgpu_mlp_loss_grad(const float *params, const float *x, const float *t,
+                                   int batch, float *grad, float *loss, void *stream);
+
+/* Adam training (beta 0.9/0.999, eps 1e-8, step size decaying from lr to lr/50 on a
+ * cosine) on n (features, raw targets) rows for `steps`
+ * mini-batches of `batch` rows drawn with replacement (seeded); params updated in place
+ * (standardization entries must be filled in).  loss_history (HOST, may be NULL) receives
+ * the per-step loss.  Synchronous. */
+athgpu_status athgpu_mlp_train(const float *features, const float *targets, long long n,
+                               float *params, int steps, int batch, float lr,
+                               unsigned long long seed, float *loss_history, void *stream);
 
 /* Conserved->primitive over whole MeshBlocks plus the first CFL time step, for callers
  * that cannot let a library allocate device memory: hosts whose device memory belongs

@@ -66,6 +66,7 @@ def lib():
         L.orc_c2p_failures.restype = ctypes.c_long
         L.orc_sr_c2p_cells.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double,
                                        dp, dp, dp, dp, ctypes.POINTER(ctypes.c_int)]
+        L.orc_sr_prim_to_cons.argtypes = [ctypes.c_long, ctypes.c_double, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -78,7 +79,8 @@ class OracleMesh:
     """The oracle's mesh: the same MeshSpec, parameters and arrays as the CUDA path."""
 
     def __init__(self, mesh, gamma, xorder=2, rsolver="hlld", cfl=0.3, tlim=1e30,
-                 dfloor=None, pfloor=None, relativistic=False, threads=0):
+                 dfloor=None, pfloor=None, relativistic=False, threads=0, sigma_max=0.0,
+                 beta_min=0.0, gamma_max=1000.0):
         L = lib()
         import math
         fmin = float(np.finfo(np.float32).tiny)
@@ -88,7 +90,8 @@ class OracleMesh:
                         mesh.bx[2], mesh.ng, xorder, 0 if rsolver == "hlld" else 1,
                         1 if relativistic else 0, gamma,
                         floor if dfloor is None else dfloor,
-                        floor if pfloor is None else pfloor, cfl, tlim, 0.0, 0.0, 0.0)
+                        floor if pfloor is None else pfloor, cfl, tlim, sigma_max,
+                        beta_min, gamma_max)
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         self.h = L.orc_create(ctypes.byref(self.p), *[_p(c) for c in self.coords])
         if threads:
@@ -102,6 +105,11 @@ class OracleMesh:
     def set_state(self, u, b1, b2, b3):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, b1, b2, b3)]
         lib().orc_set_state(self.h, *[_p(a) for a in arrs])
+
+    def set_prim(self, w):
+        """Initial primitives (SR: also the first con2prim guess)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        lib().orc_set_prim(self.h, _p(w))
 
     def state(self):
         m = self.mesh
@@ -134,3 +142,26 @@ class OracleMesh:
 
     def stage(self, s):
         lib().orc_stage(self.h, s)
+
+
+def sr_c2p_cells(cons, bcc, guess, gamma):
+    """Per-cell SR con2prim (Newman-Hamlin) on independent cells: cons[n,5] (D, M1..M3,
+    E), bcc[n,3], pgas guesses[n] -> prim[n,5], iterations[n] (-1: not converged)."""
+    n = cons.shape[0]
+    cons = np.ascontiguousarray(cons, dtype=np.float64)
+    bcc = np.ascontiguousarray(bcc, dtype=np.float64)
+    guess = np.ascontiguousarray(guess, dtype=np.float64)
+    prim = np.zeros((n, 5))
+    it = np.zeros(n, dtype=np.int32)
+    lib().orc_sr_c2p_cells(n, gamma, 0.0, _p(cons), _p(bcc), _p(guess), _p(prim),
+                           it.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return prim, it
+
+
+def sr_prim_to_cons(w, bcc, gamma):
+    n = w.shape[0]
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    bcc = np.ascontiguousarray(bcc, dtype=np.float64)
+    u = np.zeros((n, 5))
+    lib().orc_sr_prim_to_cons(n, gamma, _p(w), _p(bcc), _p(u))
+    return u

@@ -49,6 +49,11 @@ CASES = {
                                             (.5, .5, .5)), "blast", 2, 0.3, 3),
     "blast_hlle_ppm_8blk": ("mhd_hlle_g3", ((16, 16, 16), (2, 2, 2), 3, (-.5, -.5, -.5),
                                             (.5, .5, .5)), "blast", 3, 0.3, 3),
+    # special-relativistic MHD (-s -b --flux=hlle): relativistic Kelvin-Helmholtz layer
+    "srkh_hlle_plm_8blk": ("srmhd_hlle_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                            (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
+    "srkh_hlle_plm_1blk": ("srmhd_hlle_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
+                                            (1., 1., 1.)), "sr_kh", 2, 0.4, 4),
 }
 
 
@@ -61,6 +66,8 @@ def global_ic(problem, mesh):
 
 
 def gamma_of(problem):
+    if problem == "sr_kh":
+        return 4.0 / 3.0
     return GAMMA_LW if problem == "linear_wave" else 5.0 / 3.0
 
 
@@ -84,6 +91,16 @@ def run_case(name, spec):
             "compute_error": "false", "wave_flag": 0, "amp": 1.0e-6, "vflow": 0.0})
         d, _ = ref_run.run_reference(variant, "athena_lw", text)
         tlim = 1.0e3
+    elif problem == "sr_kh":
+        gw, g1, g2, g3 = pgen.sr_kelvin_helmholtz(mesh.nx, seed=9, noise=0.05)
+        gu = pgen.sr_prim_to_cons(gw, pgen.cell_centered(g1, g2, g3), gamma)
+        u0 = mesh.scatter_cells(gu)
+        w0 = mesh.scatter_cells(gw)
+        b10, b20, b30 = mesh.scatter_faces(g1, g2, g3)
+        text = ref_run.athinput(mesh, gamma, xorder, cfl, ncycle, 1.0e3,
+                                {"ic_file": "ic.bin"})
+        d, _ = ref_run.run_reference(variant, "athena_ic", text, ic=(1, gw, g1, g2, g3))
+        tlim = 1.0e3
     else:
         gu, g1, g2, g3 = global_ic(problem, mesh)
         u0 = mesh.scatter_cells(gu)
@@ -98,12 +115,14 @@ def run_case(name, spec):
         dts.append(dump["dt"])
     ng = mesh.ng
     fi = lambda b: b[:, ng:-ng, ng:-ng, ng:-ng]  # noqa: E731
+    extra = {"ic_w": mesh.interior(w0)} if problem == "sr_kh" else {}
     np.savez_compressed(
         os.path.join(OUT, name + ".npz"),
         ic_u=mesh.interior(u0), ic_b1=fi(b10), ic_b2=fi(b20), ic_b3=fi(b30),
         u=mesh.interior(dump["u"]), b1=fi(dump["b1"]), b2=fi(dump["b2"]), b3=fi(dump["b3"]),
-        dt=np.array(dts), time=dump["time"])
+        w=mesh.interior(dump["w"]), dt=np.array(dts), time=dump["time"], **extra)
     return {"variant": variant, "nx": mesh.nx, "nb": mesh.nb, "ng": mesh.ng,
+            "relativistic": problem == "sr_kh",
             "xmin": mesh.xmin, "xmax": mesh.xmax, "problem": problem, "xorder": xorder,
             "rsolver": "hlld" if "hlld" in variant else "hlle", "cfl": cfl,
             "ncycle": ncycle, "gamma": gamma, "tlim": tlim}
@@ -127,18 +146,25 @@ def run_config1():
             "reference_zone_cycles_per_cpu_second_here": zc[-1] if zc else None}
 
 
-def main():
+def main(only=None):
     for v in sorted({c[0] for c in CASES.values()}):
         build_ref.build_variant(v)
     meta = {"cases": {}}
+    path = os.path.join(OUT, "golden.json")
+    if only and os.path.exists(path):
+        with open(path) as f:
+            meta = json.load(f)
     for name, spec in CASES.items():
+        if only and name not in only:
+            continue
         print("case", name, flush=True)
         meta["cases"][name] = run_case(name, spec)
-    print("config1", flush=True)
-    meta["config1_linear_wave"] = run_config1()
+    if not only:
+        print("config1", flush=True)
+        meta["config1_linear_wave"] = run_config1()
     with open(os.path.join(OUT, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

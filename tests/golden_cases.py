@@ -14,8 +14,11 @@ def meta():
         return json.load(f)
 
 
-def case_names():
-    return sorted(meta()["cases"])
+def case_names(relativistic=None):
+    """Case names; ``relativistic`` True/False selects SR or Newtonian cases only."""
+    cases = meta()["cases"]
+    return sorted(n for n, c in cases.items()
+                  if relativistic is None or bool(c.get("relativistic")) == relativistic)
 
 
 def load_case(name):
@@ -37,7 +40,11 @@ def load_case(name):
 
     ic = (pad_cells(z["ic_u"]), pad_faces(z["ic_b1"], 0), pad_faces(z["ic_b2"], 1),
           pad_faces(z["ic_b3"], 2))
+    if "ic_w" in z.files:   # relativistic: initial primitives (also the first guess)
+        c["ic_w"] = pad_cells(z["ic_w"])
     ref = {k: z[k] for k in ("u", "b1", "b2", "b3", "dt")}
+    if "w" in z.files:
+        ref["w"] = z["w"]
     ref["time"] = float(z["time"])
     return c, mesh, ic, ref
 

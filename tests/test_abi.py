@@ -34,6 +34,7 @@ def _desc(mesh, **kw):
     d.nx1, d.nx2, d.nx3 = mesh.bx
     d.nghost, d.xorder, d.rsolver, d.precision = mesh.ng, 2, 0, 0
     d.gamma, d.dfloor, d.pfloor, d.cfl_number, d.tlim = 5 / 3, 1e-10, 1e-10, 0.3, 1.0
+    d.sigma_max, d.beta_min, d.gamma_max = 0.0, 0.0, 1000.0
     d.x1f, d.dx1f, d.x2f, d.dx2f, d.x3f, d.dx3f = [rt._dp(c) for c in coords]
     for k, v in kw.items():
         setattr(d, k, v)
@@ -78,3 +79,13 @@ def test_non_uniform_spacing_is_rejected(lib):
     h = ctypes.c_void_p()
     assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -3
     assert b"uniform" in lib.athgpu_last_error()
+
+
+def test_relativistic_options_are_checked(lib):
+    mesh = MeshSpec((16, 8, 8), (1, 1, 1), 2)
+    h = ctypes.c_void_p()
+    d, keep = _desc(mesh, relativistic=1, rsolver=0)      # SR + HLLD: not provided
+    assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -3
+    d, keep = _desc(mesh, relativistic=1, rsolver=1, gamma_max=0.5)
+    assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -1
+    assert b"gamma_max" in lib.athgpu_last_error()

@@ -41,7 +41,7 @@ def _run_gpu(mesh, c, ic, ncycle, precision="fp64"):
     return out, np.array(dts), w, bcc
 
 
-@pytest.mark.parametrize("name", case_names())
+@pytest.mark.parametrize("name", case_names(relativistic=False))
 def test_fp64_matches_reference_bitwise(name):
     c, mesh, ic, ref = load_case(name)
     (u, b1, b2, b3), dts, _, _ = _run_gpu(mesh, c, ic, c["ncycle"])

@@ -1,0 +1,106 @@
+"""Special-relativistic MHD stage update on the GPU against the reference and the oracle.
+
+The SR con2prim calls acos, cos and cbrt, whose CUDA implementations may differ from the
+host libm in the last bit, so the FP64 SR path is compared per cell within 1e-12 relative
+(the acceptance bar for the FP64 path), not bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from athena_gb300 import build, pgen
+from athena_gb300.mesh import MeshSpec
+from athena_gb300.runtime import StageUpdate
+from golden_cases import case_names, interior_faces, load_case
+
+pytestmark = pytest.mark.gpu
+
+SR_CASES = case_names(relativistic=True)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    build.build()
+
+
+def close(a, b, rtol=1e-12):
+    """|a-b| <= rtol*|b| + rtol*max|b| (per variable): relative per cell, with an
+    absolute floor at the variable's scale for components that pass through zero."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    scale = np.abs(b).max()
+    return bool(np.all(np.abs(a - b) <= rtol * np.abs(b) + rtol * scale))
+
+
+def _run(mesh, c, ic, w0, ncycle, precision="fp64"):
+    g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver="hlle",
+                    precision=precision, cfl=c["cfl"], tlim=c["tlim"], relativistic=True)
+    g.set_state(*ic)
+    g.set_prim(w0)
+    g.initialize()
+    dts = []
+    for _ in range(ncycle):
+        dts.append(g.dt)
+        g.cycle(1)
+    out = g.state()
+    w, bcc = g.prim()
+    g.close()
+    return out, w, np.array(dts)
+
+
+@pytest.mark.parametrize("name", SR_CASES)
+def test_sr_fp64_matches_reference(name):
+    c, mesh, ic, ref = load_case(name)
+    (u, b1, b2, b3), w, dts = _run(mesh, c, ic, c["ic_w"], c["ncycle"])
+    assert np.array_equal(dts, ref["dt"])   # SR time step depends on the widths only
+    ui = mesh.interior(u)
+    for n in range(5):
+        assert close(ui[:, n], ref["u"][:, n]), n
+    wi = mesh.interior(w)
+    for n in range(5):
+        assert close(wi[:, n], ref["w"][:, n], rtol=1e-11), n
+    for got, want in zip((b1, b2, b3), (ref["b1"], ref["b2"], ref["b3"])):
+        assert close(interior_faces(mesh, got), want)
+
+
+def _sr_kh(nx=(32, 32, 32), nb=(2, 2, 2), seed=4):
+    mesh = MeshSpec(nx, nb, 2)
+    gw, f1, f2, f3 = pgen.sr_kelvin_helmholtz(nx, seed=seed, noise=0.02)
+    gu = pgen.sr_prim_to_cons(gw, pgen.cell_centered(f1, f2, f3), 4.0 / 3.0)
+    ic = (mesh.scatter_cells(gu),) + mesh.scatter_faces(f1, f2, f3)
+    c = {"gamma": 4.0 / 3.0, "xorder": 2, "cfl": 0.3, "tlim": 1e3}
+    return mesh, ic, mesh.scatter_cells(gw), c
+
+
+def test_sr_fp64_matches_oracle():
+    mesh, ic, w0, c = _sr_kh()
+    (u, *_), w, dts = _run(mesh, c, ic, w0, 4)
+    om = O.OracleMesh(mesh, c["gamma"], xorder=2, rsolver="hlle", tlim=c["tlim"],
+                      relativistic=True)
+    om.set_state(*ic)
+    om.set_prim(w0)
+    om.initialize()
+    om.cycle(4)
+    uo = om.state()[0]
+    wo = om.prim()[0]
+    a, b = mesh.interior(u), mesh.interior(uo)
+    for n in range(5):
+        assert close(a[:, n], b[:, n]), n
+    aw, bw = mesh.interior(w), mesh.interior(wo)
+    for n in range(5):
+        assert close(aw[:, n], bw[:, n], rtol=1e-11), n
+
+
+def test_sr_fp32_tracks_fp64_and_keeps_div_b():
+    mesh, ic, w0, c = _sr_kh(nx=(32, 32, 32), nb=(1, 1, 1))
+    (u64, *_), _, _ = _run(mesh, c, ic, w0, 4, "fp64")
+    (u32, b1, b2, b3), _, _ = _run(mesh, c, ic, w0, 4, "fp32")
+    a, b = mesh.interior(u32), mesh.interior(u64)
+    for n in range(5):
+        rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(b[:, n]).mean()
+        assert rel < 1e-4, (n, rel)
+    ng, (n1, n2, n3) = mesh.ng, mesh.bx
+    div = (b1[:, ng:ng + n3, ng:ng + n2, ng + 1:ng + n1 + 1] - b1[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
+           + b2[:, ng:ng + n3, ng + 1:ng + n2 + 1, ng:ng + n1] - b2[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
+           + b3[:, ng + 1:ng + n3 + 1, ng:ng + n2, ng:ng + n1] - b3[:, ng:ng + n3, ng:ng + n2, ng:ng + n1])
+    assert np.abs(div).max() / np.abs(b1).max() < 1e-13

@@ -15,8 +15,10 @@ from golden_cases import case_names, load_case, interior_faces, meta
 def test_oracle_matches_reference_bitwise(name):
     c, mesh, ic, ref = load_case(name)
     om = O.OracleMesh(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
-                      cfl=c["cfl"], tlim=c["tlim"])
+                      cfl=c["cfl"], tlim=c["tlim"], relativistic=c.get("relativistic", False))
     om.set_state(*ic)
+    if "ic_w" in c:
+        om.set_prim(c["ic_w"])
     om.initialize()
     dts = []
     for _ in range(c["ncycle"]):
@@ -27,6 +29,9 @@ def test_oracle_matches_reference_bitwise(name):
     assert np.array_equal(mesh.interior(u), ref["u"])
     for got, want in ((b1, ref["b1"]), (b2, ref["b2"]), (b3, ref["b3"])):
         assert np.array_equal(interior_faces(mesh, got), want)
+    if "w" in ref:
+        w, _ = om.prim()
+        assert np.array_equal(mesh.interior(w), ref["w"])
 
 
 def test_linear_wave_ic_matches_reference():
