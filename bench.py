@@ -212,7 +212,62 @@ def run_gpu(args, rank, world, local_rank):
                           "h2d_bytes_per_step": ebytes, "d2h_bytes_per_step": ebytes,
                           "steps": e_steps}
         g.close()
+    if not args.no_learned:
+        res["learned_c2p"] = run_learned_c2p()
     return mesh, res
+
+
+LEARNED_CELLS = 1 << 24
+
+
+def run_learned_c2p(reps=5):
+    """Learned con2prim in isolation: 2^24 independent SR-MHD cells (gamma 4/3, Lorentz
+    factor in [1,10], sigma in [1e-2,1e2], rho in [1e-4,1], p/rho in [1e-3,10], all
+    log-uniform, isotropic v and B).  The network is trained here on 2^20 solver-made
+    pairs; the plain solve starts from the pressure floor (an isolated cell has no
+    previous pressure), the learned one from the BF16 network refined in FP32, both
+    finished by the reference's FP64 iteration (two warp-coherent launches each)."""
+    import torch
+    from athena_gb300 import pgen
+    from athena_gb300.learned_c2p import LearnedC2P, MODE_LEARNED_FP32, MODE_PLAIN
+    net = LearnedC2P(4.0 / 3.0, seed=0)
+    t0 = time.perf_counter()
+    feats, targ = net.solver_pairs(1 << 20, 101)
+    net.set_standardization(feats, targ)
+    hist = net.train(feats, targ, steps=8000, batch=4096, lr=2.0e-3, seed=101)
+    t_train = time.perf_counter() - t0
+    w, bcc, u = pgen.sr_isolated_cells(LEARNED_CELLS, seed=777)
+    cons, b = net.to_dev(u), net.to_dev(bcc)
+    del w, bcc, u
+    out = {"workload": "2^24 independent SR-MHD cells, gamma 4/3, Lorentz factor "
+                       "log-uniform [1,10], sigma [1e-2,1e2], rho [1e-4,1], p/rho "
+                       "[1e-3,10], isotropic v and B (synthetic, seeded)",
+           "cells": LEARNED_CELLS,
+           "training": {"pairs": feats.shape[0], "steps": 8000, "batch": 4096,
+                        "seconds": t_train, "loss_first": float(hist[:10].mean()),
+                        "loss_last": float(hist[-100:].mean())}}
+    stream = torch.cuda.current_stream()
+    for name, mode in (("plain", MODE_PLAIN), ("learned", MODE_LEARNED_FP32)):
+        ts = []
+        for rep in range(reps + 2):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            prim, it, it32, fb = net.solve(cons, b, mode, want_iters32=True)
+            s1.record(stream)
+            s1.synchronize()
+            if rep >= 2:
+                ts.append(s0.elapsed_time(s1))
+        it = it.cpu().numpy()
+        ms = float(np.median(ts))
+        out[name] = {"ms": ms, "cells_per_s": LEARNED_CELLS / (ms * 1e-3),
+                     "mean_fp64_passes": float(it[it >= 0].mean()),
+                     "unconverged": int((it < 0).sum())}
+        if mode == MODE_LEARNED_FP32:
+            out[name]["mean_fp32_passes"] = float(it32.float().mean().item())
+            out[name]["fallbacks"] = fb
+    out["speedup"] = out["plain"]["ms"] / out["learned"]["ms"]
+    out["passes_ratio"] = out["learned"]["mean_fp64_passes"] / out["plain"]["mean_fp64_passes"]
+    return out
 
 
 def l1_rel(a, b):
@@ -247,6 +302,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the isolated learned-con2prim measurement")
     ap.add_argument("--nx", type=int, default=256,
                     help="cells per direction (MeshBlocks of 32^3); 256 is the workload")
     args = ap.parse_args()
@@ -323,6 +380,8 @@ def main():
             "e2e": res["e2e"], "gpu_launches": res["launches_per_step"] * r32["steps"],
             "clocks": res["clocks"],
             "kernel_ms_fp32": res["profile32"], "kernel_ms_fp64": res["profile64"]}
+    if "learned_c2p" in res:
+        line["learned_c2p"] = res["learned_c2p"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline((mesh, make_ic(NX, NB)[1]))
     print(json.dumps(line))
