@@ -51,8 +51,8 @@ void free_all(athgpu_ctx* c) {
   Registers& r = c->r;
   void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
-                  r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->nbr,
-                  c->staging};
+                  r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
+                  c->nbr, c->staging};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
@@ -163,6 +163,7 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.ne2 = (i64)(m.nc3 + 1) * m.nc2 * (m.nc1 + 1);
   m.ne3 = (i64)m.nc3 * (m.nc2 + 1) * (m.nc1 + 1);
   m.gamma = d->gamma; m.dfloor = d->dfloor; m.pfloor = d->pfloor;
+  m.gammaf = (float)d->gamma; m.dfloorf = (float)d->dfloor; m.pfloorf = (float)d->pfloor;
   m.cfl = d->cfl_number; m.tlim = d->tlim;
   m.ncmax = m.nc1 > m.nc2 ? (m.nc1 > m.nc3 ? m.nc1 : m.nc3) : (m.nc2 > m.nc3 ? m.nc2 : m.nc3);
 
@@ -235,6 +236,18 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.dx2f = c->coords + dxoff[1];
   m.dx3f = c->coords + dxoff[2];
   m.plm = c->coords + plmoff;
+  {  // FP32 copies: the FP32 kernels read these instead of converting on the FP64 pipe
+    std::vector<float> hf(ncoord);
+    for (i64 q = 0; q < ncoord; ++q) hf[q] = (float)hc[q];
+    e = cudaMalloc((void**)&c->coords32, sizeof(float) * ncoord);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc coords32"));
+    e = cudaMemcpy(c->coords32, hf.data(), sizeof(float) * ncoord, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy coords32"));
+    m.dx1f32 = c->coords32 + dxoff[0];
+    m.dx2f32 = c->coords32 + dxoff[1];
+    m.dx3f32 = c->coords32 + dxoff[2];
+    m.plm32 = c->coords32 + plmoff;
+  }
 
   // neighbour table of the periodic block grid
   std::vector<int> hn(nb * 27);
@@ -262,7 +275,7 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   double dmax = DBL_MAX;
   memcpy(&hclk.dtmin_bits, &dmax, 8);
   hclk.c2p_floor_count = 0;
-  hclk.pad = 0;
+  hclk.dtf = (float)hclk.dt;
   e = cudaMemcpy(c->clk, &hclk, sizeof(hclk), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy clock"));
   e = cudaStreamSynchronize(c->stream);
@@ -422,6 +435,7 @@ athgpu_status athgpu_set_clock(athgpu_ctx* c, double time, double dt) {
   CK(cudaStreamSynchronize(c->stream));
   h.time = time;
   h.dt = dt;
+  h.dtf = (float)dt;
   CK(cudaMemcpyAsync(c->clk, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return ATHGPU_OK;

@@ -40,6 +40,7 @@ struct athgpu_ctx {
   athgpu::LaunchConfig lc;
   athgpu::DevClock* clk = nullptr;
   double* coords = nullptr;  // dx1f | dx2f | dx3f | plm coefficients (device)
+  float* coords32 = nullptr; // the same, rounded to FP32, for the FP32 kernels
   int* nbr = nullptr;
   cudaStream_t own_stream = nullptr, stream = nullptr;
   cudaGraphExec_t cycle_exec = nullptr;

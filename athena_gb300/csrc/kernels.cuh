@@ -28,6 +28,13 @@ struct DevMesh {
   const double* plm;   // [nb][3][2][ncmax]: (x?f(c+1)-x?v(c))/dx?f(c), (x?v(c)-x?f(c))/dx?f(c)
   int ncmax;
   const int* nbr;      // [nb][27] neighbour block for offset ((o3+1)*3+(o2+1))*3+(o1+1)
+  // FP32 copies of the scalars and coordinate arrays above (rounded once on the host,
+  // the values the FP32 kernels would otherwise convert per use)
+  float gammaf, dfloorf, pfloorf;
+  const float* dx1f32;
+  const float* dx2f32;
+  const float* dx3f32;
+  const float* plm32;
 };
 
 // device-resident scalars of the time integrator
@@ -35,8 +42,28 @@ struct DevClock {
   double dt, time;
   unsigned long long dtmin_bits;  // min over cells of dx/speed, as ordered bits
   int c2p_floor_count;
-  int pad;
+  float dtf;                      // dt rounded to FP32 (written with dt)
 };
+
+// The mesh scalars, coordinates and dt in the kernel's arithmetic type: the FP64 kernels
+// read the FP64 values, the FP32 kernels their FP32 roundings (the same values a
+// conversion at each use would give, without the FP64-pipe conversion).
+__device__ __forceinline__ double rgamma(const DevMesh& m, double) { return m.gamma; }
+__device__ __forceinline__ float rgamma(const DevMesh& m, float) { return m.gammaf; }
+__device__ __forceinline__ double rdfloor(const DevMesh& m, double) { return m.dfloor; }
+__device__ __forceinline__ float rdfloor(const DevMesh& m, float) { return m.dfloorf; }
+__device__ __forceinline__ double rpfloor(const DevMesh& m, double) { return m.pfloor; }
+__device__ __forceinline__ float rpfloor(const DevMesh& m, float) { return m.pfloorf; }
+__device__ __forceinline__ const double* rdx(const DevMesh& m, int d, double) {
+  return d == 0 ? m.dx1f : d == 1 ? m.dx2f : m.dx3f;
+}
+__device__ __forceinline__ const float* rdx(const DevMesh& m, int d, float) {
+  return d == 0 ? m.dx1f32 : d == 1 ? m.dx2f32 : m.dx3f32;
+}
+__device__ __forceinline__ const double* rplm(const DevMesh& m, double) { return m.plm; }
+__device__ __forceinline__ const float* rplm(const DevMesh& m, float) { return m.plm32; }
+__device__ __forceinline__ double rdt(const DevClock* c, double) { return c->dt; }
+__device__ __forceinline__ float rdt(const DevClock* c, float) { return c->dtf; }
 
 __device__ __forceinline__ i64 cidx(const DevMesh& m, int b, int n, int nvar, int k, int j,
                                     int i) {
@@ -73,6 +100,23 @@ __device__ __forceinline__ i64 fsize(const DevMesh& m) {
   return (i64)m.nb * (DIR == 0 ? m.nf1 : DIR == 1 ? m.nf2 : m.nf3);
 }
 
+// Asynchronous global -> shared copies of single elements (cp.async, completion tracked
+// per thread with commit/wait groups).
+template <typename Real>
+__device__ __forceinline__ void cp_async_elem(Real* smem_dst, const Real* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  if (sizeof(Real) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------------------
 // Reconstruction of one cell along DIR: wave vector (natural order d, v1, v2, v3, p, then
 // the two transverse cell-centred field components, plm.cpp:45-57 / :196-208) of the
@@ -102,16 +146,53 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
       qrm[n] = q;
     } else if (ORDER == 2) {
       int c = DIR == 0 ? i : DIR == 1 ? j : k;
-      const double* pc = m.plm + ((i64)b * 3 + DIR) * 2 * m.ncmax;
-      plm_one<Real>(__ldg(src + o - sw), __ldg(src + o), __ldg(src + o + sw),
-                    (Real)__ldg(pc + c), (Real)__ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
+      const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
+      plm_one<Real>(__ldg(src + o - sw), __ldg(src + o), __ldg(src + o + sw), __ldg(pc + c),
+                    __ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
     } else {
       ppm_one<Real>(__ldg(src + o - 2 * sw), __ldg(src + o - sw), __ldg(src + o),
                     __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n]);
     }
   }
   if (ORDER == 3) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
-    const Real dfl = (Real)m.dfloor, pfl = (Real)m.pfloor;
+    const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
+    qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
+    qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
+    qrm[IDN] = (qrm[IDN] > dfl) ? qrm[IDN] : dfl;
+    qrm[IPR] = (qrm[IPR] > pfl) ? qrm[IPR] : pfl;
+  }
+}
+
+// The seven wave variables of one cell for a sweep along DIR: w[0..4] at wp + n*vs, the
+// two transverse cell-centred field components (DIR+1)%3, (DIR+2)%3 at bp.
+template <typename Real, int DIR>
+__device__ __forceinline__ void load_wave(const Real* __restrict__ wp,
+                                          const Real* __restrict__ bp, i64 vs, Real* v) {
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) v[n] = __ldg(wp + n * vs);
+  v[IBY] = __ldg(bp + ((DIR + 1) % 3) * vs);
+  v[IBZ] = __ldg(bp + ((DIR + 2) % 3) * vs);
+}
+
+// recon_cell on a stencil window held in registers: win[q] is cell c - R + q along the
+// sweep (R = 0, 1, 2 for DC, PLM, PPM); cp/cm are the PLM coefficients of cell c.  Same
+// arithmetic as recon_cell.
+template <typename Real, int ORDER>
+__device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)[NWAVE],
+                                             Real cp, Real cm, Real* qlp, Real* qrm) {
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    if (ORDER == 1) {
+      qlp[n] = win[0][n];
+      qrm[n] = win[0][n];
+    } else if (ORDER == 2) {
+      plm_one<Real>(win[0][n], win[1][n], win[2][n], cp, cm, qlp[n], qrm[n]);
+    } else {
+      ppm_one<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qlp[n], qrm[n]);
+    }
+  }
+  if (ORDER == 3) {
+    const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
     qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
     qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
     qrm[IDN] = (qrm[IDN] > dfl) ? qrm[IDN] : dfl;
@@ -132,9 +213,10 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   Real wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
   Real wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
   Real f[NWAVE];
-  if (RS == 0) hlld<Real>((Real)m.gamma, wli, wri, bx, f);
-  else if (RS == 1) hlle<Real>((Real)m.gamma, wli, wri, bx, f);
-  else hlle_sr<Real>((Real)m.gamma, wli, wri, bx, f);  // special relativity
+  const Real gam = rgamma(m, Real());
+  if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
+  else if (RS == 1) hlle<Real>(gam, wli, wri, bx, f);
+  else hlle_sr<Real>(gam, wli, wri, bx, f);  // special relativity
   fn[IDN] = f[0];
   fn[ivx] = f[1];
   fn[ivy] = f[2];
@@ -199,15 +281,15 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
   if (has_face) {
     const i64 fo = f1idx(m, b, k, j, i);
     solve_face<Real, 0, RS>(m, wl, qrm, (Real)__ldg(b1 + fo),
-                            (Real)__ldg(m.dx1f + (i64)b * m.nc1 + i), (Real)clk->dt, fo, fn,
-                            e3, e2, wct);
+                            __ldg(rdx(m, 0, Real()) + (i64)b * m.nc1 + i), rdt(clk, Real()),
+                            fo, fn, e3, e2, wct);
   }
   Real fp[NHYDRO];
 #pragma unroll
   for (int n = 0; n < NHYDRO; ++n) fp[n] = __shfl_down_sync(0xffffffffu, fn[n], 1);
   if (has_face && lane <= 30 && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
       k <= m.ke) {
-    const Real x1area = (Real)m.dx2f[(i64)b * m.nc2 + j] * (Real)m.dx3f[(i64)b * m.nc3 + k];
+    const Real x1area = rdx(m, 1, Real())[(i64)b * m.nc2 + j] * rdx(m, 2, Real())[(i64)b * m.nc3 + k];
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n)
       dflx[cidx(m, b, n, NHYDRO, k, j, i)] = (x1area * fp[n] - x1area * fn[n]);
@@ -221,7 +303,7 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
 // i in [is-1,ie+1]; x3: j in [js-1,je+1], i in [is-1,ie+1].  A segment of cells
 // [c0,c1] solves faces c0..c1+1, so neighbouring segments share one face.
 template <typename Real, int DIR, int ORDER, int RS, int KAHAN>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(Real) == 4 ? 4 : 1)
 flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                   const Real* __restrict__ bcc, const double* __restrict__ bn,
                   const DevClock* __restrict__ clk, Real* __restrict__ dflx,
@@ -247,27 +329,80 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   const int trans = (DIR == 1 ? m.ks : m.js) - 1 + tt;  // k for x2, j for x3
   const bool interior = ii >= 1 && ii <= m.nx1 && trans >= (DIR == 1 ? m.ks : m.js) &&
                         trans <= (DIR == 1 ? m.ke : m.je);
-  const Real dt = (Real)clk->dt;
-  const double* dxs = (DIR == 1) ? m.dx2f + (i64)b * m.nc2 : m.dx3f + (i64)b * m.nc3;
+  const Real dt = rdt(clk, Real());
+  const Real* dxs = rdx(m, DIR, Real()) + (i64)b * (DIR == 1 ? m.nc2 : m.nc3);
   // area of this direction's faces (the same for every face of a uniform block)
-  const Real dx1 = (Real)m.dx1f[(i64)b * m.nc1 + i];
-  const Real dxt = (DIR == 1) ? (Real)m.dx3f[(i64)b * m.nc3 + trans]
-                              : (Real)m.dx2f[(i64)b * m.nc2 + trans];
+  const Real dx1 = rdx(m, 0, Real())[(i64)b * m.nc1 + i];
+  const Real dxt = (DIR == 1) ? rdx(m, 2, Real())[(i64)b * m.nc3 + trans]
+                              : rdx(m, 1, Real())[(i64)b * m.nc2 + trans];
   const Real area = dx1 * dxt;
+  const int k0 = (DIR == 1) ? trans : 0, j0 = (DIR == 2) ? trans : 0;
+  // Stencil ring in shared memory: each thread owns one column of a ring of WN+1 cell
+  // slots x 7 wave variables (layout [slot][variable][thread], conflict-free).  The cell
+  // s+R+1 needed by the next step is copied in with cp.async while this step's face is
+  // solved, so each cell's seven values are read from memory once and the load latency
+  // hides behind a whole Riemann solve.  No thread reads another thread's column, so no
+  // barrier is needed.
+  constexpr int R = ORDER == 3 ? 2 : ORDER == 2 ? 1 : 0;
+  constexpr int WN = 2 * R + 1;
+  constexpr int NS = WN + 1;
+  extern __shared__ __align__(16) unsigned char sweep_smem[];
+  Real* ring = reinterpret_cast<Real*>(sweep_smem) + threadIdx.x;
+  const int bd = blockDim.x;
+  const i64 sw = (DIR == 1) ? (i64)m.nc1 : (i64)m.nc1 * m.nc2;
+  const i64 vs = m.ncell;
+  const int cfirst = c0 - 1 - R;
+  const Real* wp = w + ((DIR == 1) ? cidx(m, b, 0, NHYDRO, k0, cfirst, i)
+                                   : cidx(m, b, 0, NHYDRO, cfirst, j0, i));
+  const Real* bp = bcc + ((DIR == 1) ? cidx(m, b, 0, 3, k0, cfirst, i)
+                                     : cidx(m, b, 0, 3, cfirst, j0, i));
+  auto issue = [&](int rel) {  // cell cfirst + rel -> slot rel % NS
+    const int slot = rel % NS;
+    const Real* wc = wp + rel * sw;
+    const Real* bc = bp + rel * sw;
+#pragma unroll
+    for (int n = 0; n < NWAVE; ++n) {
+      const Real* src = n < NHYDRO ? wc + n * vs
+                                   : bc + ((DIR + 1 + (n - NHYDRO)) % 3) * vs;
+      cp_async_elem<Real>(ring + (slot * NWAVE + n) * bd, src);
+    }
+  };
+  auto window = [&](int rel0, Real (*win)[NWAVE]) {  // cells cfirst+rel0 .. +WN-1
+#pragma unroll
+    for (int q = 0; q < WN; ++q) {
+      const int slot = (rel0 + q) % NS;
+#pragma unroll
+      for (int n = 0; n < NWAVE; ++n) win[q][n] = ring[(slot * NWAVE + n) * bd];
+    }
+  };
+  for (int q = 0; q <= WN; ++q) issue(q);  // cells c0-1-R .. c0+R
+  cp_async_commit();
+  cp_async_wait_all();
+  const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
   Real wl[NWAVE], qlp[NWAVE], qrm[NWAVE];
   Real fprev[NHYDRO];
-  const int k0 = (DIR == 1) ? trans : 0, j0 = (DIR == 2) ? trans : 0;
-  auto cell = [&](int s, Real* ql, Real* qr) {
-    if (DIR == 1) recon_cell<Real, 1, ORDER>(m, w, bcc, b, k0, s, i, ql, qr);
-    else recon_cell<Real, 2, ORDER>(m, w, bcc, b, s, j0, i, ql, qr);
-  };
-  cell(c0 - 1, wl, qrm);
+  {
+    Real win[WN][NWAVE];
+    window(0, win);
+    recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + c0 - 1) : Real(0),
+                              ORDER == 2 ? __ldg(pc + m.ncmax + c0 - 1) : Real(0), wl, qrm);
+  }
   for (int s = c0; s <= c1 + 1; ++s) {
-    cell(s, qlp, qrm);
+    const int rel0 = s - R - cfirst;  // window = cells s-R..s+R
+    if (s <= c1) {  // prefetch cell s+R+1 into the slot of cell s-R-1
+      issue(rel0 + WN);
+      cp_async_commit();
+    }
+    {
+      Real win[WN][NWAVE];
+      window(rel0, win);
+      recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + s) : Real(0),
+                                ORDER == 2 ? __ldg(pc + m.ncmax + s) : Real(0), qlp, qrm);
+    }
     const i64 fo = (DIR == 1) ? f2idx(m, b, k0, s, i) : f3idx(m, b, s, j0, i);
     Real fn[NHYDRO];
-    solve_face<Real, DIR, RS>(m, wl, qrm, (Real)__ldg(bn + fo), (Real)__ldg(dxs + s), dt, fo,
-                              fn, ey, ez, wct);
+    solve_face<Real, DIR, RS>(m, wl, qrm, (Real)__ldg(bn + fo), __ldg(dxs + s), dt, fo, fn,
+                              ey, ez, wct);
     if (s > c0 && interior) {
       // cell s-1: this direction's flux difference
       const int kc = (DIR == 1) ? k0 : s - 1, jc = (DIR == 1) ? s - 1 : j0;
@@ -280,10 +415,12 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
           dflx[cc] = d;
         }
       } else {
-        const Real dx2 = (Real)m.dx2f[(i64)b * m.nc2 + jc];
-        const Real dx3 = (Real)m.dx3f[(i64)b * m.nc3 + kc];
+        const Real dx2 = rdx(m, 1, Real())[(i64)b * m.nc2 + jc];
+        const Real dx3 = rdx(m, 2, Real())[(i64)b * m.nc3 + kc];
         const Real vol = dx1 * dx2 * dx3;
-        const Real wght = (Real)(ua.beta * clk->dt);
+        // beta is 1/2 or 1, so beta * (FP32 dt) equals the FP32 rounding of beta * dt
+        const Real wght = (sizeof(Real) == 8) ? (Real)(ua.beta * clk->dt)
+                                              : (Real)ua.beta * dt;
 #pragma unroll
         for (int n = 0; n < NHYDRO; ++n) {
           const i64 cc = cidx(m, b, n, NHYDRO, kc, jc, i);
@@ -313,7 +450,14 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) fprev[n] = fn[n];
+    cp_async_wait_all();  // the next step's cell has landed in its slot
   }
+}
+
+// shared-memory bytes of the x2/x3 sweep's stencil ring for a CTA of `threads` threads
+__host__ __device__ inline int sweep_smem_bytes(int order, int real_bytes, int threads) {
+  const int r = order == 3 ? 2 : order == 2 ? 1 : 0;
+  return (2 * r + 2) * NWAVE * threads * real_bytes;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -483,53 +627,56 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   __syncthreads();
   const double l1 = dx1f[m.is], l2 = dx2f[m.js], l3 = dx3f[m.ks];
   const bool exact = sizeof(Real) == 8;
-  auto term = [&](double qd, double len, Real ep, Real em) -> double {
+  // FP32 path: the (wght/area)*len products are the same for every face of the block
+  const double q0l3 = q[0] * l3, q0l2 = q[0] * l2, q1l3 = q[1] * l3, q1l1 = q[1] * l1,
+               q2l2 = q[2] * l2, q2l1 = q[2] * l1;
+  auto term = [&](double qd, double len, double qlen, Real ep, Real em) -> double {
     return exact ? qd * (len * (double)ep - len * (double)em)
-                 : (qd * len) * ((double)ep - (double)em);
+                 : qlen * ((double)ep - (double)em);
   };
-  const i64 nf1 = (i64)m.nx3 * m.nx2 * (m.nx1 + 1);
-  const i64 nf2 = (i64)m.nx3 * (m.nx2 + 1) * m.nx1;
-  const i64 nf3 = (i64)(m.nx3 + 1) * m.nx2 * m.nx1;
-  const i64 per = nf1 + nf2 + nf3;
-  for (i64 r = (i64)blockIdx.x * blockDim.x + threadIdx.x; r < per;
-       r += (i64)gridDim.x * blockDim.x) {
+  // per-block face counts fit in 32 bits
+  const int nf1 = m.nx3 * m.nx2 * (m.nx1 + 1);
+  const int nf2 = m.nx3 * (m.nx2 + 1) * m.nx1;
+  const int nf3 = (m.nx3 + 1) * m.nx2 * m.nx1;
+  const int per = nf1 + nf2 + nf3;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < per; r += gridDim.x * blockDim.x) {
     if (r < nf1) {
-      i64 rr = r;
-      const int i = m.is + (int)(rr % (m.nx1 + 1));
+      int rr = r;
+      const int i = m.is + rr % (m.nx1 + 1);
       rr /= (m.nx1 + 1);
-      const int j = m.js + (int)(rr % m.nx2);
-      const int k = m.ks + (int)(rr / m.nx2);
+      const int j = m.js + rr % m.nx2;
+      const int k = m.ks + rr / m.nx2;
       const i64 o = f1idx(m, b, k, j, i);
       double v = b1in[o];
-      v -= term(q[0], l3, edge_value<Real, 2>(m, e3, b, k, j + 1, i),
+      v -= term(q[0], l3, q0l3, edge_value<Real, 2>(m, e3, b, k, j + 1, i),
                 edge_value<Real, 2>(m, e3, b, k, j, i));
-      v += term(q[0], l2, edge_value<Real, 1>(m, e2, b, k + 1, j, i),
+      v += term(q[0], l2, q0l2, edge_value<Real, 1>(m, e2, b, k + 1, j, i),
                 edge_value<Real, 1>(m, e2, b, k, j, i));
       b1out[o] = v;
     } else if (r < nf1 + nf2) {
-      i64 rr = r - nf1;
-      const int i = m.is + (int)(rr % m.nx1);
+      int rr = r - nf1;
+      const int i = m.is + rr % m.nx1;
       rr /= m.nx1;
-      const int j = m.js + (int)(rr % (m.nx2 + 1));
-      const int k = m.ks + (int)(rr / (m.nx2 + 1));
+      const int j = m.js + rr % (m.nx2 + 1);
+      const int k = m.ks + rr / (m.nx2 + 1);
       const i64 o = f2idx(m, b, k, j, i);
       double v = b2in[o];
-      v += term(q[1], l3, edge_value<Real, 2>(m, e3, b, k, j, i + 1),
+      v += term(q[1], l3, q1l3, edge_value<Real, 2>(m, e3, b, k, j, i + 1),
                 edge_value<Real, 2>(m, e3, b, k, j, i));
-      v -= term(q[1], l1, edge_value<Real, 0>(m, e1, b, k + 1, j, i),
+      v -= term(q[1], l1, q1l1, edge_value<Real, 0>(m, e1, b, k + 1, j, i),
                 edge_value<Real, 0>(m, e1, b, k, j, i));
       b2out[o] = v;
     } else {
-      i64 rr = r - nf1 - nf2;
-      const int i = m.is + (int)(rr % m.nx1);
+      int rr = r - nf1 - nf2;
+      const int i = m.is + rr % m.nx1;
       rr /= m.nx1;
-      const int j = m.js + (int)(rr % m.nx2);
-      const int k = m.ks + (int)(rr / m.nx2);
+      const int j = m.js + rr % m.nx2;
+      const int k = m.ks + rr / m.nx2;
       const i64 o = f3idx(m, b, k, j, i);
       double v = b3in[o];
-      v -= term(q[2], l2, edge_value<Real, 1>(m, e2, b, k, j, i + 1),
+      v -= term(q[2], l2, q2l2, edge_value<Real, 1>(m, e2, b, k, j, i + 1),
                 edge_value<Real, 1>(m, e2, b, k, j, i));
-      v += term(q[2], l1, edge_value<Real, 0>(m, e1, b, k, j + 1, i),
+      v += term(q[2], l1, q2l1, edge_value<Real, 0>(m, e1, b, k, j + 1, i),
                 edge_value<Real, 0>(m, e1, b, k, j, i));
       b3out[o] = v;
     }
@@ -793,6 +940,7 @@ static __global__ void advance_clock_kernel(DevClock* clk, double cfl, double tl
   dt = smin<double>(dt, block_dt);
   if (clk->time < tlim && (tlim - clk->time) < dt) dt = tlim - clk->time;
   clk->dt = dt;
+  clk->dtf = (float)dt;
   clk->dtmin_bits = 0x7fefffffffffffffULL;  // DBL_MAX for the next reduction
 }
 
