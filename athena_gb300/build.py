@@ -25,6 +25,7 @@ UNITS = {
     "noalloc.cu": ["-fmad=false"],
     # learned con2prim: the FP64 polish keeps the reference's rounding (no contraction)
     "sr_learned.cu": ["-fmad=false"],
+    "selftest.cu": ["-fmad=false"],
 }
 
 

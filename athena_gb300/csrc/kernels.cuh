@@ -174,7 +174,17 @@ __device__ __forceinline__ void load_wave(const Real* __restrict__ wp,
   v[IBZ] = __ldg(bp + ((DIR + 2) % 3) * vs);
 }
 
-// recon_cell on a stencil window held in registers: win[q] is cell c - R + q along the
+// ApplyPrimitiveFloors on the PPM face states (adiabatic_mhd.cpp:162-172, ppm.cpp:326-331)
+template <typename Real>
+__device__ __forceinline__ void ppm_floors(const DevMesh& m, Real* qlp, Real* qrm) {
+  const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
+  qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
+  qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
+  qrm[IDN] = (qrm[IDN] > dfl) ? qrm[IDN] : dfl;
+  qrm[IPR] = (qrm[IPR] > pfl) ? qrm[IPR] : pfl;
+}
+
+// recon_cell on a stencil window: win[q] is cell c - R + q along the
 // sweep (R = 0, 1, 2 for DC, PLM, PPM); cp/cm are the PLM coefficients of cell c.  Same
 // arithmetic as recon_cell.
 template <typename Real, int ORDER>
@@ -191,13 +201,7 @@ __device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)
       ppm_one<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qlp[n], qrm[n]);
     }
   }
-  if (ORDER == 3) {
-    const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
-    qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
-    qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
-    qrm[IDN] = (qrm[IDN] > dfl) ? qrm[IDN] : dfl;
-    qrm[IPR] = (qrm[IPR] > pfl) ? qrm[IPR] : pfl;
-  }
+  if (ORDER == 3) ppm_floors(m, qlp, qrm);
 }
 
 // Riemann solve on one face of direction DIR: stores the two face EMFs and the CT weight
@@ -280,7 +284,7 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
   const bool has_face = valid && lane > 0 && c > 0;
   if (has_face) {
     const i64 fo = f1idx(m, b, k, j, i);
-    solve_face<Real, 0, RS>(m, wl, qrm, (Real)__ldg(b1 + fo),
+    solve_face<Real, 0, RS>(m, wl, qrm, to_real(__ldg(b1 + fo), Real()),
                             __ldg(rdx(m, 0, Real()) + (i64)b * m.nc1 + i), rdt(clk, Real()),
                             fo, fn, e3, e2, wct);
   }
@@ -381,11 +385,24 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
   Real wl[NWAVE], qlp[NWAVE], qrm[NWAVE];
   Real fprev[NHYDRO];
+  Real dphc[ORDER == 3 ? NWAVE : 1];  // PPM: limited lower interface of the current cell
   {
     Real win[WN][NWAVE];
     window(0, win);
-    recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + c0 - 1) : Real(0),
-                              ORDER == 2 ? __ldg(pc + m.ncmax + c0 - 1) : Real(0), wl, qrm);
+    if constexpr (ORDER == 3) {
+#pragma unroll
+      for (int n = 0; n < NWAVE; ++n) {
+        const Real lo = ppm_face<Real>(win[0][n], win[1][n], win[2][n], win[3][n]);
+        dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
+        ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo, dphc[n],
+                         wl[n], qrm[n]);
+      }
+      ppm_floors(m, wl, qrm);
+    } else {
+      recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + c0 - 1) : Real(0),
+                                ORDER == 2 ? __ldg(pc + m.ncmax + c0 - 1) : Real(0), wl,
+                                qrm);
+    }
   }
   for (int s = c0; s <= c1 + 1; ++s) {
     const int rel0 = s - R - cfirst;  // window = cells s-R..s+R
@@ -396,13 +413,24 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     {
       Real win[WN][NWAVE];
       window(rel0, win);
-      recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + s) : Real(0),
-                                ORDER == 2 ? __ldg(pc + m.ncmax + s) : Real(0), qlp, qrm);
+      if constexpr (ORDER == 3) {  // the lower interface is the previous cell's upper one
+#pragma unroll
+        for (int n = 0; n < NWAVE; ++n) {
+          const Real lo = dphc[n];
+          dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
+          ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo,
+                           dphc[n], qlp[n], qrm[n]);
+        }
+        ppm_floors(m, qlp, qrm);
+      } else {
+        recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + s) : Real(0),
+                                  ORDER == 2 ? __ldg(pc + m.ncmax + s) : Real(0), qlp, qrm);
+      }
     }
     const i64 fo = (DIR == 1) ? f2idx(m, b, k0, s, i) : f3idx(m, b, s, j0, i);
     Real fn[NHYDRO];
-    solve_face<Real, DIR, RS>(m, wl, qrm, (Real)__ldg(bn + fo), __ldg(dxs + s), dt, fo, fn,
-                              ey, ez, wct);
+    solve_face<Real, DIR, RS>(m, wl, qrm, to_real(__ldg(bn + fo), Real()), __ldg(dxs + s),
+                              dt, fo, fn, ey, ez, wct);
     if (s > c0 && interior) {
       // cell s-1: this direction's flux difference
       const int kc = (DIR == 1) ? k0 : s - 1, jc = (DIR == 1) ? s - 1 : j0;
@@ -573,9 +601,14 @@ __device__ __forceinline__ int nbr_of(const DevMesh& m, int b, int o1, int o2, i
   return __ldg(m.nbr + (i64)b * 27 + ((o3 + 1) * 3 + (o2 + 1)) * 3 + (o1 + 1));
 }
 
+// The corner EMF of edge (b,k,j,i) as CT uses it: the value itself, or on a block face /
+// edge the average over the blocks that share it (flux_correction_fc.cpp), formed in the
+// bulk precision; returned widened to FP64 (exactly; on the integer pipe for FP32).
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) { return f2d_exact(x); }
 template <typename Real, int C>
-__device__ __forceinline__ Real edge_value(const DevMesh& m, const Real* __restrict__ e,
-                                           int b, int k, int j, int i) {
+__device__ __forceinline__ Real edge_avg(const DevMesh& m, const Real* __restrict__ e,
+                                         int b, int k, int j, int i) {
   auto at = [&](int bb, int kk, int jj, int ii) -> Real {
     return __ldg(e + (C == 0 ? e1idx(m, bb, kk, jj, ii)
                      : C == 1 ? e2idx(m, bb, kk, jj, ii) : e3idx(m, bb, kk, jj, ii)));
@@ -599,14 +632,21 @@ __device__ __forceinline__ Real edge_value(const DevMesh& m, const Real* __restr
   return sum * Real(0.5);
 }
 
+template <typename Real, int C>
+__device__ __forceinline__ double edge_value(const DevMesh& m, const Real* __restrict__ e,
+                                             int b, int k, int j, int i) {
+  return widen(edge_avg<Real, C>(m, e, b, k, j, i));
+}
+
 // Field::CT, field/ct.cpp:31-116, plus the VL2 register average (weighted_ave.cpp),
 // which for VL2 reduces to out = in on the first stage and an in-place update on the
 // second.  blockIdx.y is the MeshBlock; the CTA computes the block's (wght/area) factors
 // once (areas and edge lengths are constant on a uniform block) and strides over the
 // block's faces of all three arrays.  Edge EMFs are read with the correction above.
 // FP64 path (Real = double): (wght/area)*(len*e(+) - len*e(-)) exactly as the reference.
-// FP32 path: the EMFs are FP32 and the update FP64 as ((wght/area)*len)*(e(+) - e(-)),
-// whose difference of two floats is exact in FP64.  bin/bout may alias.
+// FP32 path: the corner EMFs are FP32, widened exactly, and the update is
+// ((wght/area)*len)*(e(+) - e(-)) in FP64 (the difference of two floats is exact in FP64).
+// bin/bout may alias.
 template <typename Real>
 __global__ void __launch_bounds__(256)
 ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
@@ -630,9 +670,8 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   // FP32 path: the (wght/area)*len products are the same for every face of the block
   const double q0l3 = q[0] * l3, q0l2 = q[0] * l2, q1l3 = q[1] * l3, q1l1 = q[1] * l1,
                q2l2 = q[2] * l2, q2l1 = q[2] * l1;
-  auto term = [&](double qd, double len, double qlen, Real ep, Real em) -> double {
-    return exact ? qd * (len * (double)ep - len * (double)em)
-                 : qlen * ((double)ep - (double)em);
+  auto term = [&](double qd, double len, double qlen, double ep, double em) -> double {
+    return exact ? qd * (len * ep - len * em) : qlen * (ep - em);
   };
   // per-block face counts fit in 32 bits
   const int nf1 = m.nx3 * m.nx2 * (m.nx1 + 1);
@@ -698,57 +737,60 @@ __device__ __forceinline__ int own_map(int idx, int lo, int hi, int n, int* o) {
 
 // r-th ghost element of an array of extent (N1,N2,N3) whose own part has extent
 // (I1,I2,I3) starting at ng in every direction
-__device__ __forceinline__ void ghost_coord(i64 r, int N1, int N2, int N3, int I1, int I2,
+__device__ __forceinline__ void ghost_coord(int r, int N1, int N2, int N3, int I1, int I2,
                                             int I3, int ng, int& k, int& j, int& i) {
-  const i64 A = (i64)2 * ng * N2 * N1;
+  // per-block ghost counts fit in 32 bits
+  const int A = 2 * ng * N2 * N1;
   if (r < A) {
-    int kk = (int)(r / ((i64)N2 * N1));
-    i64 rem = r - (i64)kk * N2 * N1;
+    const int kk = r / (N2 * N1);
+    const int rem = r - kk * N2 * N1;
     k = kk < ng ? kk : kk - ng + ng + I3;
-    j = (int)(rem / N1);
-    i = (int)(rem % N1);
+    j = rem / N1;
+    i = rem % N1;
     return;
   }
   r -= A;
-  const i64 B = (i64)2 * ng * N1 * I3;
+  const int B = 2 * ng * N1 * I3;
   if (r < B) {
-    int kk = (int)(r / ((i64)2 * ng * N1));
-    i64 rem = r - (i64)kk * 2 * ng * N1;
+    const int kk = r / (2 * ng * N1);
+    const int rem = r - kk * 2 * ng * N1;
     k = ng + kk;
-    int jj = (int)(rem / N1);
+    const int jj = rem / N1;
     j = jj < ng ? jj : jj - ng + ng + I2;
-    i = (int)(rem % N1);
+    i = rem % N1;
     return;
   }
   r -= B;
-  int kk = (int)(r / ((i64)2 * ng * I2));
-  i64 rem = r - (i64)kk * 2 * ng * I2;
+  const int kk = r / (2 * ng * I2);
+  const int rem = r - kk * 2 * ng * I2;
   k = ng + kk;
-  j = ng + (int)(rem / (2 * ng));
-  int ii = (int)(rem % (2 * ng));
+  j = ng + rem / (2 * ng);
+  const int ii = rem % (2 * ng);
   i = ii < ng ? ii : ii - ng + ng + I1;
 }
 
-template <typename T>
+// I: index type of the element enumeration (32-bit when the whole mesh's ghost count
+// fits, which the launch checks).
+template <typename T, typename I>
 __global__ void __launch_bounds__(256)
 exchange_kernel(DevMesh m, T* __restrict__ u, double* __restrict__ b1,
                 double* __restrict__ b2, double* __restrict__ b3) {
-  i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  I t = (I)blockIdx.x * blockDim.x + threadIdx.x;
   const int n1 = m.nx1, n2 = m.nx2, n3 = m.nx3, ng = m.ng;
   // ghost counts per block: cells, x1/x2/x3 faces
-  const i64 gc = m.ncell - (i64)n1 * n2 * n3;
-  const i64 g1 = m.nf1 - (i64)(n1 + 1) * n2 * n3;
-  const i64 g2 = m.nf2 - (i64)n1 * (n2 + 1) * n3;
-  const i64 g3 = m.nf3 - (i64)n1 * n2 * (n3 + 1);
+  const int gc = (int)(m.ncell - (i64)n1 * n2 * n3);
+  const int g1 = (int)(m.nf1 - (i64)(n1 + 1) * n2 * n3);
+  const int g2 = (int)(m.nf2 - (i64)n1 * (n2 + 1) * n3);
+  const int g3 = (int)(m.nf3 - (i64)n1 * n2 * (n3 + 1));
   int what;
-  i64 per;
-  if (t < gc * m.nb) { what = 0; per = gc; }
-  else if ((t -= gc * m.nb) < g1 * m.nb) { what = 1; per = g1; }
-  else if ((t -= g1 * m.nb) < g2 * m.nb) { what = 2; per = g2; }
-  else if ((t -= g2 * m.nb) < g3 * m.nb) { what = 3; per = g3; }
+  int per;
+  if (t < (I)gc * m.nb) { what = 0; per = gc; }
+  else if ((t -= (I)gc * m.nb) < (I)g1 * m.nb) { what = 1; per = g1; }
+  else if ((t -= (I)g1 * m.nb) < (I)g2 * m.nb) { what = 2; per = g2; }
+  else if ((t -= (I)g2 * m.nb) < (I)g3 * m.nb) { what = 3; per = g3; }
   else return;
   const int b = (int)(t / per);
-  const i64 r = t - (i64)b * per;
+  const int r = (int)(t - (I)b * per);
   int k, j, i;
   ghost_coord(r, m.nc1 + (what == 1), m.nc2 + (what == 2), m.nc3 + (what == 3),
               n1 + (what == 1), n2 + (what == 2), n3 + (what == 3), ng, k, j, i);
@@ -782,6 +824,38 @@ __device__ __forceinline__ double warp_min(double v) {
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+// "no time step limit" marker of a cell outside the interior
+__device__ __forceinline__ double big_dt(double) { return 1.0e300; }
+__device__ __forceinline__ float big_dt(float) { return 3.0e38f; }
+
+// Minimum of v over the CTA, then one atomicMin on the ordered bits of the double (positive
+// doubles order like their bit patterns), skipped when it would not lower the stored
+// value: most CTAs' minima do not, so the single address sees few atomics.  Every thread
+// of the CTA must call it.
+template <typename Real>
+__device__ __forceinline__ void cta_min_to_clock(Real v, DevClock* clk) {
+  __shared__ Real red[32];
+  v = warp_min(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    Real x = lane < nw ? red[lane] : big_dt(Real());
+    x = warp_min(x);
+    if (lane == 0 && x < big_dt(Real())) {
+      const unsigned long long bits =
+          (unsigned long long)__double_as_longlong((double)x);
+      if (bits < *(volatile unsigned long long*)&clk->dtmin_bits)
+        atomicMin(&clk->dtmin_bits, bits);
+    }
+  }
+}
 
 template <typename Real, int KAHAN>
 __global__ void __launch_bounds__(128)
@@ -789,7 +863,7 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
            const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
            Real* ulo, Real* __restrict__ w, Real* __restrict__ bcc, DevClock* clk) {
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double cell_dt = 1.0e300;
+  Real cell_dt = big_dt(Real());
   if (t < (i64)m.nb * m.ncell) {
     const int b = (int)(t / m.ncell);
     i64 r = t - (i64)b * m.ncell;
@@ -797,18 +871,30 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     r /= m.nc1;
     const int j = (int)(r % m.nc2);
     const int k = (int)(r / m.nc2);
-    const double lw = 0.5, rw = 0.5;
-    const double bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
-    const double bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
-    const double bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
+    const double b1l = b1[f1idx(m, b, k, j, i)], b1r = b1[f1idx(m, b, k, j, i + 1)];
+    const double b2l = b2[f2idx(m, b, k, j, i)], b2r = b2[f2idx(m, b, k, j + 1, i)];
+    const double b3l = b3[f3idx(m, b, k, j, i)], b3r = b3[f3idx(m, b, k + 1, j, i)];
+    // the lower faces in the bulk precision (also the dt's |b_face - bcc| term)
+    const Real b1lr = to_real(b1l, Real()), b2lr = to_real(b2l, Real()),
+               b3lr = to_real(b3l, Real());
+    Real bcc1, bcc2, bcc3;
+    if constexpr (sizeof(Real) == 8) {  // field.cpp:112-180, the reference's arithmetic
+      const double lw = 0.5, rw = 0.5;
+      bcc1 = lw * b1l + rw * b1r;
+      bcc2 = lw * b2l + rw * b2r;
+      bcc3 = lw * b3l + rw * b3r;
+    } else {  // FP32 path: average of the FP32-rounded faces (no FP64-pipe work)
+      bcc1 = Real(0.5) * b1lr + Real(0.5) * to_real(b1r, Real());
+      bcc2 = Real(0.5) * b2lr + Real(0.5) * to_real(b2r, Real());
+      bcc3 = Real(0.5) * b3lr + Real(0.5) * to_real(b3r, Real());
+    }
     const i64 vs = m.ncell;
     const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
     const i64 cb = cidx(m, b, 0, 3, k, j, i);
-    const Real gm1 = (Real)m.gamma - Real(1.0);
-    const Real dfl = (Real)m.dfloor, pfl = (Real)m.pfloor;
+    const Real gm1 = rgamma(m, Real()) - Real(1.0);
+    const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
     Real u_d = u[c], u_m1 = u[c + vs], u_m2 = u[c + 2 * vs], u_m3 = u[c + 3 * vs],
          u_e = u[c + 4 * vs];
-    const Real bcc1 = (Real)bc1, bcc2 = (Real)bc2, bcc3 = (Real)bc3;
     const bool dfloored = !(u_d > dfl);
     u_d = (u_d > dfl) ? u_d : dfl;
     Real di = Real(1.0) / u_d;
@@ -840,29 +926,26 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
         k <= m.ke) {
       // new_blockdt.cpp:80-103, in the bulk precision on the stored primitives (FP64
       // path: the reference's arithmetic; FP32 path: FP32, reduced in FP64)
-      const Real gam = (Real)m.gamma;
-      Real dt1 = (Real)m.dx1f[(i64)b * m.nc1 + i], dt2 = (Real)m.dx2f[(i64)b * m.nc2 + j],
-           dt3 = (Real)m.dx3f[(i64)b * m.nc3 + k];
-      Real bx = bcc1 + dabs((Real)b1[f1idx(m, b, k, j, i)] - bcc1);
+      const Real gam = rgamma(m, Real());
+      Real dt1 = rdx(m, 0, Real())[(i64)b * m.nc1 + i],
+           dt2 = rdx(m, 1, Real())[(i64)b * m.nc2 + j],
+           dt3 = rdx(m, 2, Real())[(i64)b * m.nc3 + k];
+      Real bx = bcc1 + dabs(b1lr - bcc1);
       Real cf = fast_ms<Real>(gam, u_d, w_p, bcc2, bcc3, bx);
       Real speed = smax<Real>(Real(0.0), (dabs(vx) + cf));
       dt1 /= (speed);
-      bx = bcc2 + dabs((Real)b2[f2idx(m, b, k, j, i)] - bcc2);
+      bx = bcc2 + dabs(b2lr - bcc2);
       cf = fast_ms<Real>(gam, u_d, w_p, bcc3, bcc1, bx);
       speed = smax<Real>(Real(0.0), (dabs(vy) + cf));
       dt2 /= (speed);
-      bx = bcc3 + dabs((Real)b3[f3idx(m, b, k, j, i)] - bcc3);
+      bx = bcc3 + dabs(b3lr - bcc3);
       cf = fast_ms<Real>(gam, u_d, w_p, bcc1, bcc2, bx);
       speed = smax<Real>(Real(0.0), (dabs(vz) + cf));
       dt3 /= (speed);
-      cell_dt = (double)smin<Real>(smin<Real>(dt1, dt2), dt3);
+      cell_dt = smin<Real>(smin<Real>(dt1, dt2), dt3);
     }
   }
-  if (do_dt) {
-    double v = warp_min(cell_dt);
-    if ((threadIdx.x & 31) == 0 && v < 1.0e300)
-      atomicMin(&clk->dtmin_bits, (unsigned long long)__double_as_longlong(v));
-  }
+  if (do_dt) cta_min_to_clock<Real>(cell_dt, clk);  // reduced in the bulk precision
 }
 
 // EquationOfState::ConservedToPrimitive for SR MHD (adiabatic_mhd_sr.cpp:72-272) over
@@ -923,11 +1006,7 @@ c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
       cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
     }
   }
-  if (do_dt) {
-    double v = warp_min(cell_dt);
-    if ((threadIdx.x & 31) == 0 && v < 1.0e300)
-      atomicMin(&clk->dtmin_bits, (unsigned long long)__double_as_longlong(v));
-  }
+  if (do_dt) cta_min_to_clock<double>(cell_dt, clk);
 }
 
 // Mesh::NewTimeStep (mesh.cpp:1236-1281) after the main loop's time += dt

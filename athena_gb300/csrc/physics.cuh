@@ -27,6 +27,43 @@ __device__ __forceinline__ float dsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }
 __device__ __forceinline__ float dabs(float x) { return fabsf(x); }
 
+// FP64 <-> FP32 conversions on the integer pipe.  GB300's FP64 pipe also executes the
+// F2F conversion instructions, at about two lane-operations per clock per SM; a kernel
+// already bound by that pipe (the CT update) converts with integer bit arithmetic
+// instead: IEEE-754 round to nearest, ties to even, for every value whose result is a
+// normal float (or zero); denormal results, infinities and NaNs take the hardware
+// conversion.  Both give the same bits as the hardware conversion.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const unsigned sign = hi & 0x80000000u;
+  const int fe = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;  // biased FP32 exponent
+  if (fe >= 1 && fe <= 254) {
+    // keep the top 23 of the 52 fraction bits, round on the 29 dropped bits
+    unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu, half = 0x10000000u;
+    m += (rem > half) | ((rem == half) & (m & 1u));
+    // a carry out of the fraction increments the exponent (to infinity from 254)
+    return __uint_as_float(sign | (((unsigned)fe << 23) + m));
+  }
+  if ((u << 1) == 0ull) return __uint_as_float(sign);  // +-0
+  return (float)x;
+}
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u) {  // normal
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+  }
+  if ((b << 1) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // +-0
+  return (double)f;
+}
+// a face-field (always FP64) value in the bulk precision (hardware conversion: where the
+// kernel is not bound by the FP64 pipe, F2F costs fewer issue slots than d2f_rn)
+__device__ __forceinline__ double to_real(double x, double) { return x; }
+__device__ __forceinline__ float to_real(double x, float) { return (float)x; }
+
 // EquationOfState::FastMagnetosonicSpeed, eos/adiabatic_mhd.cpp:149-156
 template <typename Real>
 __device__ __forceinline__ Real fast_ms(Real gamma, Real d, Real p, Real by, Real bz,
@@ -320,9 +357,13 @@ __device__ __forceinline__ void plm_one(Real qm, Real q0, Real qp, Real cp, Real
 // PiecewiseParabolicX1/2/3, uniform-Cartesian Colella-Sekora branch
 // (reconstruct/ppm.cpp:113-315), coefficients c1..c6 = 1/2,1/2,1/2,1/2,1/6,-1/6
 // (reconstruct/reconstruction.cpp:499-504).  One wave component; q_im2..q_ip2 stencil.
+// Limited PPM interface value between cells i-1 and i from cells i-2..i+1: the
+// interface estimate of Step 1 (ppm.cpp:115-127) and the Step 2a limiter of that
+// interface (ppm.cpp:139-166).  The upper interface of cell i is ppm_face(q_im1, qc, q_ip1, q_ip2),
+// the same operations as the lower interface of cell i+1, so a sweep computes each
+// interface once and carries it to the next cell.
 template <typename Real>
-__device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_ip1,
-                                        Real q_ip2, Real& qlp, Real& qrm) {
+__device__ __forceinline__ Real ppm_face(Real q_im2, Real q_im1, Real qc, Real q_ip1) {
   const Real C2 = RC(1.25);
   const Real c1 = RC(0.5), c2 = RC(0.5), c3 = RC(0.5), c4 = RC(0.5);
   const Real c5 = RC(1.0 / 6.0), c6 = RC(-1.0 / 6.0);
@@ -330,32 +371,31 @@ __device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_
   Real qb = (q_ip1 - qc);
   Real dd_im1 = c1 * qa + c2 * (q_im1 - q_im2);
   Real dd = c1 * qb + c2 * qa;
-  Real dd_ip1 = c1 * (q_ip2 - q_ip1) + c2 * qb;
   Real dph = (c3 * q_im1 + c4 * qc) + (c5 * dd_im1 + c6 * dd);
-  Real dph_ip1 = (c3 * qc + c4 * q_ip1) + (c5 * dd + c6 * dd_ip1);
+  Real d2qc_im1 = q_im2 + qc - RC(2.0) * q_im1;
+  Real d2qc = q_im1 + q_ip1 - RC(2.0) * qc;
+  Real qa_tmp = dph - q_im1;
+  Real qb_tmp = qc - dph;
+  Real a = RC(3.0) * (q_im1 + qc - RC(2.0) * dph);
+  Real b = d2qc_im1, c = d2qc, d = RC(0.0);
+  if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
+    d = sgn(a) * smin(C2 * dabs(b), smin(C2 * dabs(c), dabs(a)));
+  Real dph_tmp = RC(0.5) * (q_im1 + qc) - d / RC(6.0);
+  if (qa_tmp * qb_tmp < RC(0.0)) dph = dph_tmp;
+  return dph;
+}
+
+// PPM cell values from the limited interfaces dph (i-1/2) and dph_ip1 (i+1/2): d2qf of
+// Step 2a (ppm.cpp:192) and the Step 3 limiter of the parabola (ppm.cpp:216-315, uniform
+// branch).
+template <typename Real>
+__device__ __forceinline__ void ppm_finish(Real q_im2, Real q_im1, Real qc, Real q_ip1,
+                                           Real q_ip2, Real dph, Real dph_ip1, Real& qlp,
+                                           Real& qrm) {
+  const Real C2 = RC(1.25);
   Real d2qc_im1 = q_im2 + qc - RC(2.0) * q_im1;
   Real d2qc = q_im1 + q_ip1 - RC(2.0) * qc;
   Real d2qc_ip1 = qc + q_ip2 - RC(2.0) * q_ip1;
-  {
-    Real qa_tmp = dph - q_im1;
-    Real qb_tmp = qc - dph;
-    Real a = RC(3.0) * (q_im1 + qc - RC(2.0) * dph);
-    Real b = d2qc_im1, c = d2qc, d = RC(0.0);
-    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
-      d = sgn(a) * smin(C2 * dabs(b), smin(C2 * dabs(c), dabs(a)));
-    Real dph_tmp = RC(0.5) * (q_im1 + qc) - d / RC(6.0);
-    if (qa_tmp * qb_tmp < RC(0.0)) dph = dph_tmp;
-  }
-  {
-    Real qa_tmp = dph_ip1 - qc;
-    Real qb_tmp = q_ip1 - dph_ip1;
-    Real a = RC(3.0) * (qc + q_ip1 - RC(2.0) * dph_ip1);
-    Real b = d2qc, c = d2qc_ip1, d = RC(0.0);
-    if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
-      d = sgn(a) * smin(C2 * dabs(b), smin(C2 * dabs(c), dabs(a)));
-    Real dphip1_tmp = RC(0.5) * (qc + q_ip1) - d / RC(6.0);
-    if (qa_tmp * qb_tmp < RC(0.0)) dph_ip1 = dphip1_tmp;
-  }
   Real d2qf = RC(6.0) * (dph + dph_ip1 - RC(2.0) * qc);
   Real qminus = dph, qplus = dph_ip1;
   Real dqf_minus = qc - qminus;
@@ -386,6 +426,13 @@ __device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_
   }
   qlp = qplus;
   qrm = qminus;
+}
+
+template <typename Real>
+__device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_ip1,
+                                        Real q_ip2, Real& qlp, Real& qrm) {
+  ppm_finish<Real>(q_im2, q_im1, qc, q_ip1, q_ip2, ppm_face<Real>(q_im2, q_im1, qc, q_ip1),
+                   ppm_face<Real>(q_im1, qc, q_ip1, q_ip2), qlp, qrm);
 }
 
 

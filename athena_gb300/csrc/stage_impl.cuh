@@ -59,7 +59,10 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
     const long long g3 = m.nf3 - (long long)m.nx1 * m.nx2 * (m.nx3 + 1);
     const long long n = (gc + g1 + g2 + g3) * m.nb;
     ProfScope ps(c, "exchange");
-    exchange_kernel<Real><<<nblk(n, 256), 256, 0, s>>>(m, u, b1, b2, b3);
+    if (n < (1LL << 31) - 256)
+      exchange_kernel<Real, int><<<nblk(n, 256), 256, 0, s>>>(m, u, b1, b2, b3);
+    else
+      exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, s>>>(m, u, b1, b2, b3);
   }
   // the compensation register belongs to U only; the stage-1 register U* has none
   Real* lo = (u == (Real*)c->r.u) ? (Real*)c->r.ulo : nullptr;
@@ -126,8 +129,9 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
                           (long long)(m.nx3 + 1) * m.nx2 * m.nx1;
     dim3 grid(nblk(per, 256) < 64 ? nblk(per, 256) : 64, m.nb);
     ProfScope ps(c, "ct");
-    ct_kernel<Real><<<grid, 256, 0, s>>>(m, beta, c->clk, (Real*)r.e1, (Real*)r.e2,
-                                         (Real*)r.e3, r.b1, r.b2, r.b3, o1, o2, o3);
+    ct_kernel<Real><<<grid, 256, 0, s>>>(m, beta, c->clk, (const Real*)r.e1,
+                                         (const Real*)r.e2, (const Real*)r.e3, r.b1, r.b2,
+                                         r.b3, o1, o2, o3);
   }
   c->launches += 2;
   launch_exchange_and_c2p<Real, KAHAN>(c, uout, o1, o2, o3, stage == 2);

@@ -211,6 +211,14 @@ athgpu_status athgpu_mlp_train(const float *features, const float *targets, long
                                float *params, int steps, int batch, float lr,
                                unsigned long long seed, float *loss_history, void *stream);
 
+/* Self-check of the FP64 <-> FP32 conversions the FP32 kernels do on the integer pipe
+ * (GB300's FP64 pipe, which also runs the conversion instructions, is narrow): for device
+ * arrays d[n], f[n], mismatches[0] (device) receives the number of d[q] whose integer-pipe
+ * rounding to float differs bitwise from the hardware's, mismatches[1] the same for the
+ * widening of f[q].  No counterpart in the reference. */
+athgpu_status athgpu_selftest_conversions(long long n, const double *d, const float *f,
+                                          unsigned long long *mismatches, void *stream);
+
 /* Conserved->primitive over whole MeshBlocks plus the first CFL time step, for callers
  * that cannot let a library allocate device memory: hosts whose device memory belongs
  * to their own pool allocator, real-time loops that forbid allocation latency, plugins
