@@ -341,18 +341,23 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                               : rdx(m, 1, Real())[(i64)b * m.nc2 + trans];
   const Real area = dx1 * dxt;
   const int k0 = (DIR == 1) ? trans : 0, j0 = (DIR == 2) ? trans : 0;
-  // Stencil ring in shared memory: each thread owns one column of a ring of WN+1 cell
-  // slots x 7 wave variables (layout [slot][variable][thread], conflict-free).  The cell
-  // s+R+1 needed by the next step is copied in with cp.async while this step's face is
-  // solved, so each cell's seven values are read from memory once and the load latency
-  // hides behind a whole Riemann solve.  No thread reads another thread's column, so no
-  // barrier is needed.
+  // Shared-memory staging, per thread (layout [slot][variable][thread]: conflict-free; no
+  // thread reads another thread's column, so no barrier is needed):
+  //  * ring: WN+1 cell slots x 7 wave variables.  The cell s+R+1 needed by the next step
+  //    is copied in with cp.async while this step's face is solved, so each cell's seven
+  //    values are read from memory once and the load latency hides behind a Riemann solve;
+  //  * fbuf: the normal face field of faces s and s+1 (FP64, double-buffered);
+  //  * aux: the divergence register (x2) or divergence, U^n and compensation (x3) of the
+  //    cell updated in this step, copied in before the face solve.
   constexpr int R = ORDER == 3 ? 2 : ORDER == 2 ? 1 : 0;
   constexpr int WN = 2 * R + 1;
   constexpr int NS = WN + 1;
+  constexpr int NAUX = DIR == 1 ? NHYDRO : 3 * NHYDRO;
   extern __shared__ __align__(16) unsigned char sweep_smem[];
-  Real* ring = reinterpret_cast<Real*>(sweep_smem) + threadIdx.x;
   const int bd = blockDim.x;
+  double* fbuf = reinterpret_cast<double*>(sweep_smem) + threadIdx.x;          // [2][bd]
+  Real* ring = reinterpret_cast<Real*>(sweep_smem + 2 * sizeof(double) * bd) + threadIdx.x;
+  Real* aux = ring + NS * NWAVE * bd;                                            // [NAUX][bd]
   const i64 sw = (DIR == 1) ? (i64)m.nc1 : (i64)m.nc1 * m.nc2;
   const i64 vs = m.ncell;
   const int cfirst = c0 - 1 - R;
@@ -371,6 +376,10 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
       cp_async_elem<Real>(ring + (slot * NWAVE + n) * bd, src);
     }
   };
+  auto issue_face = [&](int f) {  // normal field of face f
+    const i64 fo = (DIR == 1) ? f2idx(m, b, k0, f, i) : f3idx(m, b, f, j0, i);
+    cp_async_elem<double>(fbuf + (f & 1) * bd, bn + fo);
+  };
   auto window = [&](int rel0, Real (*win)[NWAVE]) {  // cells cfirst+rel0 .. +WN-1
 #pragma unroll
     for (int q = 0; q < WN; ++q) {
@@ -380,6 +389,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     }
   };
   for (int q = 0; q <= WN; ++q) issue(q);  // cells c0-1-R .. c0+R
+  issue_face(c0);
   cp_async_commit();
   cp_async_wait_all();
   const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
@@ -404,12 +414,29 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                                 qrm);
     }
   }
+  const Real* uin = (const Real*)ua.uin;
+  Real* uout = (Real*)ua.uout;
+  Real* ulo = (Real*)ua.ulo;
   for (int s = c0; s <= c1 + 1; ++s) {
     const int rel0 = s - R - cfirst;  // window = cells s-R..s+R
-    if (s <= c1) {  // prefetch cell s+R+1 into the slot of cell s-R-1
+    const bool upd = s > c0 && interior;  // this step finishes cell s-1
+    const int kc = (DIR == 1) ? k0 : s - 1, jc = (DIR == 1) ? s - 1 : j0;
+    const i64 cc0 = cidx(m, b, 0, NHYDRO, kc, jc, i);
+    if (s <= c1) {  // prefetch cell s+R+1 into the slot of cell s-R-1, and face s+1
       issue(rel0 + WN);
-      cp_async_commit();
+      issue_face(s + 1);
     }
+    if (upd) {
+#pragma unroll
+      for (int n = 0; n < NHYDRO; ++n) {
+        cp_async_elem<Real>(aux + n * bd, dflx + cc0 + n * vs);
+        if (DIR == 2) {
+          cp_async_elem<Real>(aux + (NHYDRO + n) * bd, uin + cc0 + n * vs);
+          if (KAHAN) cp_async_elem<Real>(aux + (2 * NHYDRO + n) * bd, ulo + cc0 + n * vs);
+        }
+      }
+    }
+    cp_async_commit();
     {
       Real win[WN][NWAVE];
       window(rel0, win);
@@ -429,18 +456,17 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     }
     const i64 fo = (DIR == 1) ? f2idx(m, b, k0, s, i) : f3idx(m, b, s, j0, i);
     Real fn[NHYDRO];
-    solve_face<Real, DIR, RS>(m, wl, qrm, to_real(__ldg(bn + fo), Real()), __ldg(dxs + s),
-                              dt, fo, fn, ey, ez, wct);
-    if (s > c0 && interior) {
+    solve_face<Real, DIR, RS>(m, wl, qrm, to_real(fbuf[(s & 1) * bd], Real()),
+                              __ldg(dxs + s), dt, fo, fn, ey, ez, wct);
+    cp_async_wait_all();  // this step's aux values and the next step's cell and face
+    if (upd) {
       // cell s-1: this direction's flux difference
-      const int kc = (DIR == 1) ? k0 : s - 1, jc = (DIR == 1) ? s - 1 : j0;
       if (DIR == 1) {
 #pragma unroll
         for (int n = 0; n < NHYDRO; ++n) {
-          const i64 cc = cidx(m, b, n, NHYDRO, kc, jc, i);
-          Real d = dflx[cc];
+          Real d = aux[n * bd];
           d += (area * fn[n] - area * fprev[n]);
-          dflx[cc] = d;
+          dflx[cc0 + n * vs] = d;
         }
       } else {
         const Real dx2 = rdx(m, 1, Real())[(i64)b * m.nc2 + jc];
@@ -451,17 +477,14 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                                               : (Real)ua.beta * dt;
 #pragma unroll
         for (int n = 0; n < NHYDRO; ++n) {
-          const i64 cc = cidx(m, b, n, NHYDRO, kc, jc, i);
-          Real d = dflx[cc];
+          const i64 cc = cc0 + n * vs;
+          Real d = aux[n * bd];
           d += (area * fn[n] - area * fprev[n]);
-          const Real* uin = (const Real*)ua.uin;
-          Real* uout = (Real*)ua.uout;
           if (KAHAN == 0) {
-            uout[cc] = uin[cc] - wght * d / vol;
+            uout[cc] = aux[(NHYDRO + n) * bd] - wght * d / vol;
           } else {
-            Real* ulo = (Real*)ua.ulo;
             const Real du = -(wght * d / vol);
-            const Real hi = uin[cc], lw = ulo[cc];
+            const Real hi = aux[(NHYDRO + n) * bd], lw = aux[(2 * NHYDRO + n) * bd];
             if (ua.stage == 1) {
               uout[cc] = hi + (lw + du);
             } else {
@@ -478,14 +501,15 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     for (int n = 0; n < NWAVE; ++n) wl[n] = qlp[n];
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) fprev[n] = fn[n];
-    cp_async_wait_all();  // the next step's cell has landed in its slot
   }
 }
 
-// shared-memory bytes of the x2/x3 sweep's stencil ring for a CTA of `threads` threads
-__host__ __device__ inline int sweep_smem_bytes(int order, int real_bytes, int threads) {
+// shared-memory bytes of the x2/x3 sweep's staging for a CTA of `threads` threads
+__host__ __device__ inline int sweep_smem_bytes(int dir, int order, int real_bytes,
+                                                int threads) {
   const int r = order == 3 ? 2 : order == 2 ? 1 : 0;
-  return (2 * r + 2) * NWAVE * threads * real_bytes;
+  const int naux = dir == 1 ? NHYDRO : 3 * NHYDRO;
+  return 2 * 8 * threads + ((2 * r + 2) * NWAVE + naux) * threads * real_bytes;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -28,8 +28,14 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
     const long long nseg = (m.nx2 + seg - 1) / seg;
     const long long n = nseg * m.nb * (m.nx3 + 2) * (long long)(m.nx1 + 2);
     ProfScope ps(c, "flux_x2");
-    flux_sweep_kernel<Real, 1, ORDER, RS, KAHAN>
-        <<<nblk(n, 128), 128, sweep_smem_bytes(ORDER, sizeof(Real), 128), s>>>(
+    const int smem = sweep_smem_bytes(1, ORDER, sizeof(Real), 128);
+    static bool attr = false;  // opt in above 48 KB once per instantiation
+    if (!attr) {
+      cudaFuncSetAttribute(flux_sweep_kernel<Real, 1, ORDER, RS, KAHAN>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      attr = true;
+    }
+    flux_sweep_kernel<Real, 1, ORDER, RS, KAHAN><<<nblk(n, 128), 128, smem, s>>>(
         m, seg, w, bcc, b2, c->clk, (Real*)r.dflx, (Real*)r.e1x2, (Real*)r.e3x2,
         (Real*)r.w2f, ua);
   }
@@ -38,8 +44,14 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
     const long long nseg = (m.nx3 + seg - 1) / seg;
     const long long n = nseg * m.nb * (m.nx2 + 2) * (long long)(m.nx1 + 2);
     ProfScope ps(c, "flux_x3_update");
-    flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN>
-        <<<nblk(n, 128), 128, sweep_smem_bytes(ORDER, sizeof(Real), 128), s>>>(
+    const int smem = sweep_smem_bytes(2, ORDER, sizeof(Real), 128);
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      attr = true;
+    }
+    flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN><<<nblk(n, 128), 128, smem, s>>>(
         m, seg, w, bcc, b3, c->clk, (Real*)r.dflx, (Real*)r.e2x3, (Real*)r.e1x3,
         (Real*)r.w3f, ua);
   }
