@@ -49,7 +49,7 @@ long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
 void free_all(athgpu_ctx* c) {
   Registers& r = c->r;
-  void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.dflx, r.e3x1, r.e2x1,
+  void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.cce, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
                   c->nbr, c->staging};
@@ -182,7 +182,7 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   std::vector<A> allocs = {
       {&r.u, nb * 5 * m.ncell * rb}, {&r.ustar, nb * 5 * m.ncell * rb},
       {&r.wbuf[0], nb * 5 * m.ncell * rb}, {&r.wbuf[1], nb * 5 * m.ncell * rb},
-      {&r.bcc, nb * 3 * m.ncell * rb},
+      {&r.bcc, nb * 3 * m.ncell * rb}, {&r.cce, nb * 3 * m.ncell * rb},
       {&r.dflx, nb * 5 * m.ncell * rb},
       {&r.e3x1, nb * m.nf1 * rb}, {&r.e2x1, nb * m.nf1 * rb}, {&r.w1f, nb * m.nf1 * rb},
       {&r.e1x2, nb * m.nf2 * rb}, {&r.e3x2, nb * m.nf2 * rb}, {&r.w2f, nb * m.nf2 * rb},

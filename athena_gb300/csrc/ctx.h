@@ -13,6 +13,8 @@ namespace athgpu {
 struct Registers {
   // bulk precision (double or float) arrays; `void*` so one struct serves both paths
   void *u = nullptr, *ustar = nullptr, *ulo = nullptr, *bcc = nullptr;
+  // cell-centred E = -v x B [nb][3][cells], written by W(U) for the corner EMFs
+  void* cce = nullptr;
   // primitives, double-buffered: each W(U) writes the buffer that is not current, seeded
   // with its previous contents (the reference's w / w1 pair, time_integrator.cpp:2221-2269)
   void* wbuf[2] = {nullptr, nullptr};

@@ -513,32 +513,31 @@ __host__ __device__ inline int sweep_smem_bytes(int dir, int order, int real_byt
 }
 
 // ---------------------------------------------------------------------------------------
-// Field::ComputeCornerE, calculate_corner_e.cpp:124-236 (3-D Newtonian branch).  The cell
-// centred E = -v x B (cc_e_, :174-181) is formed on the fly from w and bcc.  One thread
-// per corner point (b, k, j, i) in [ks,ke+1]x[js,je+1]x[is,ie+1].
+// Field::ComputeCornerE, calculate_corner_e.cpp:124-236 (3-D branch).  The cell-centred
+// E = -v x B (cc_e_, :174-181; SR: -(u x B)/u0 with u^i the 4-velocity, :161-172) is
+// written by W(U) (store_cce below) and read here.  One thread per corner point
+// (b, k, j, i) in [ks,ke+1]x[js,je+1]x[is,ie+1].
+// Store the cell-centred E = -v x B of one cell (the values cce() forms), from the
+// primitives and cell-centred field just written by W(U): the corner-EMF kernel then reads
+// three values per cell instead of forming them from six.
 template <typename Real, bool SR>
-__device__ __forceinline__ Real cce(const DevMesh& m, const Real* __restrict__ w,
-                                    const Real* __restrict__ bcc, int b, int n, int k,
-                                    int j, int i) {
-  const i64 cw = cidx(m, b, 0, NHYDRO, k, j, i), cb = cidx(m, b, 0, 3, k, j, i);
-  const i64 vs = m.ncell;
-  const Real v1 = __ldg(w + cw + vs), v2 = __ldg(w + cw + 2 * vs), v3 = __ldg(w + cw + 3 * vs);
-  const Real b1 = __ldg(bcc + cb), b2 = __ldg(bcc + cb + vs), b3 = __ldg(bcc + cb + 2 * vs);
-  if (SR) {  // calculate_corner_e.cpp:161-172: E = -(u x B)/u0 with u^i the 4-velocity
+__device__ __forceinline__ void store_cce(Real* __restrict__ cc, i64 cb, i64 vs, Real v1,
+                                          Real v2, Real v3, Real b1, Real b2, Real b3) {
+  if (SR) {
     const Real u0 = dsqrt(Real(1.0) + v1 * v1 + v2 * v2 + v3 * v3);
-    if (n == 0) return (v3 * b2 - v2 * b3) / u0;
-    if (n == 1) return (v1 * b3 - v3 * b1) / u0;
-    return (v2 * b1 - v1 * b2) / u0;
+    cc[cb] = (v3 * b2 - v2 * b3) / u0;
+    cc[cb + vs] = (v1 * b3 - v3 * b1) / u0;
+    cc[cb + 2 * vs] = (v2 * b1 - v1 * b2) / u0;
+  } else {
+    cc[cb] = v3 * b2 - v2 * b3;
+    cc[cb + vs] = v1 * b3 - v3 * b1;
+    cc[cb + 2 * vs] = v2 * b1 - v1 * b2;
   }
-  if (n == 0) return v3 * b2 - v2 * b3;
-  if (n == 1) return v1 * b3 - v3 * b1;
-  return v2 * b1 - v1 * b2;
 }
 
 template <typename Real, bool SR>
 __global__ void __launch_bounds__(128)
-corner_e_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ bcc,
-                const Real* __restrict__ e3x1, const Real* __restrict__ e2x1,
+corner_e_kernel(DevMesh m, const Real* __restrict__ cc, const Real* __restrict__ e3x1, const Real* __restrict__ e2x1,
                 const Real* __restrict__ w1f, const Real* __restrict__ e1x2,
                 const Real* __restrict__ e3x2, const Real* __restrict__ w2f,
                 const Real* __restrict__ e1x3, const Real* __restrict__ e2x3,
@@ -563,7 +562,7 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ 
 #define E3X2(kk, jj, ii) __ldg(e3x2 + f2idx(m, b, kk, jj, ii))
 #define E1X3(kk, jj, ii) __ldg(e1x3 + f3idx(m, b, kk, jj, ii))
 #define E2X3(kk, jj, ii) __ldg(e2x3 + f3idx(m, b, kk, jj, ii))
-#define CC(n, kk, jj, ii) cce<Real, SR>(m, w, bcc, b, n, kk, jj, ii)
+#define CC(n, kk, jj, ii) __ldg(cc + cidx(m, b, n, 3, kk, jj, ii))
   if (i <= m.ie) {
     Real de1_l3 = (one - W2F(k - 1, j, i)) * (E1X3(k, j, i) - CC(0, k - 1, j, i)) +
                   (W2F(k - 1, j, i)) * (E1X3(k, j - 1, i) - CC(0, k - 1, j - 1, i));
@@ -665,8 +664,11 @@ __device__ __forceinline__ double edge_value(const DevMesh& m, const Real* __res
 // Field::CT, field/ct.cpp:31-116, plus the VL2 register average (weighted_ave.cpp),
 // which for VL2 reduces to out = in on the first stage and an in-place update on the
 // second.  blockIdx.y is the MeshBlock; the CTA computes the block's (wght/area) factors
-// once (areas and edge lengths are constant on a uniform block) and strides over the
-// block's faces of all three arrays.  Edge EMFs are read with the correction above.
+// once (areas and edge lengths are constant on a uniform block).  A thread owns the cell
+// point (k,j,i) of [ks,ke+1]x[js,je+1]x[is,ie+1] and updates the faces whose lower corner
+// it is: x1 face (k,j,i) for j<=je, k<=ke; x2 face for i<=ie, k<=ke; x3 face for i<=ie,
+// j<=je.  The three faces share the edges e1, e2, e3 at (k,j,i), so a thread reads nine
+// edge values for up to three faces.  Edge EMFs are read with the correction above.
 // FP64 path (Real = double): (wght/area)*(len*e(+) - len*e(-)) exactly as the reference.
 // FP32 path: the corner EMFs are FP32, widened exactly, and the update is
 // ((wght/area)*len)*(e(+) - e(-)) in FP64 (the difference of two floats is exact in FP64).
@@ -689,60 +691,44 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
     q[threadIdx.x] = wght / area;
   }
   __syncthreads();
+  const int n1 = m.nx1 + 1, n2 = m.nx2 + 1, n3 = m.nx3 + 1;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n1 * n2 * n3) return;
+  const int i = m.is + r % n1;
+  const int j = m.js + (r / n1) % n2;
+  const int k = m.ks + r / (n1 * n2);
+  const bool f1 = j <= m.je && k <= m.ke;
+  const bool f2 = i <= m.ie && k <= m.ke;
+  const bool f3 = i <= m.ie && j <= m.je;
   const double l1 = dx1f[m.is], l2 = dx2f[m.js], l3 = dx3f[m.ks];
   const bool exact = sizeof(Real) == 8;
-  // FP32 path: the (wght/area)*len products are the same for every face of the block
-  const double q0l3 = q[0] * l3, q0l2 = q[0] * l2, q1l3 = q[1] * l3, q1l1 = q[1] * l1,
-               q2l2 = q[2] * l2, q2l1 = q[2] * l1;
-  auto term = [&](double qd, double len, double qlen, double ep, double em) -> double {
-    return exact ? qd * (len * ep - len * em) : qlen * (ep - em);
+  auto term = [&](double qd, double len, double ep, double em) -> double {
+    return exact ? qd * (len * ep - len * em) : (qd * len) * (ep - em);
   };
-  // per-block face counts fit in 32 bits
-  const int nf1 = m.nx3 * m.nx2 * (m.nx1 + 1);
-  const int nf2 = m.nx3 * (m.nx2 + 1) * m.nx1;
-  const int nf3 = (m.nx3 + 1) * m.nx2 * m.nx1;
-  const int per = nf1 + nf2 + nf3;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < per; r += gridDim.x * blockDim.x) {
-    if (r < nf1) {
-      int rr = r;
-      const int i = m.is + rr % (m.nx1 + 1);
-      rr /= (m.nx1 + 1);
-      const int j = m.js + rr % m.nx2;
-      const int k = m.ks + rr / m.nx2;
-      const i64 o = f1idx(m, b, k, j, i);
-      double v = b1in[o];
-      v -= term(q[0], l3, q0l3, edge_value<Real, 2>(m, e3, b, k, j + 1, i),
-                edge_value<Real, 2>(m, e3, b, k, j, i));
-      v += term(q[0], l2, q0l2, edge_value<Real, 1>(m, e2, b, k + 1, j, i),
-                edge_value<Real, 1>(m, e2, b, k, j, i));
-      b1out[o] = v;
-    } else if (r < nf1 + nf2) {
-      int rr = r - nf1;
-      const int i = m.is + rr % m.nx1;
-      rr /= m.nx1;
-      const int j = m.js + rr % (m.nx2 + 1);
-      const int k = m.ks + rr / (m.nx2 + 1);
-      const i64 o = f2idx(m, b, k, j, i);
-      double v = b2in[o];
-      v += term(q[1], l3, q1l3, edge_value<Real, 2>(m, e3, b, k, j, i + 1),
-                edge_value<Real, 2>(m, e3, b, k, j, i));
-      v -= term(q[1], l1, q1l1, edge_value<Real, 0>(m, e1, b, k + 1, j, i),
-                edge_value<Real, 0>(m, e1, b, k, j, i));
-      b2out[o] = v;
-    } else {
-      int rr = r - nf1 - nf2;
-      const int i = m.is + rr % m.nx1;
-      rr /= m.nx1;
-      const int j = m.js + rr % m.nx2;
-      const int k = m.ks + rr / m.nx2;
-      const i64 o = f3idx(m, b, k, j, i);
-      double v = b3in[o];
-      v -= term(q[2], l2, q2l2, edge_value<Real, 1>(m, e2, b, k, j, i + 1),
-                edge_value<Real, 1>(m, e2, b, k, j, i));
-      v += term(q[2], l1, q2l1, edge_value<Real, 0>(m, e1, b, k, j + 1, i),
-                edge_value<Real, 0>(m, e1, b, k, j, i));
-      b3out[o] = v;
-    }
+  // the shared edges, each read once (and only where a face of this thread uses it)
+  const double e1c = (f2 || f3) ? edge_value<Real, 0>(m, e1, b, k, j, i) : 0.0;
+  const double e2c = (f1 || f3) ? edge_value<Real, 1>(m, e2, b, k, j, i) : 0.0;
+  const double e3c = (f1 || f2) ? edge_value<Real, 2>(m, e3, b, k, j, i) : 0.0;
+  if (f1) {
+    const i64 o = f1idx(m, b, k, j, i);
+    double v = b1in[o];
+    v -= term(q[0], l3, edge_value<Real, 2>(m, e3, b, k, j + 1, i), e3c);
+    v += term(q[0], l2, edge_value<Real, 1>(m, e2, b, k + 1, j, i), e2c);
+    b1out[o] = v;
+  }
+  if (f2) {
+    const i64 o = f2idx(m, b, k, j, i);
+    double v = b2in[o];
+    v += term(q[1], l3, edge_value<Real, 2>(m, e3, b, k, j, i + 1), e3c);
+    v -= term(q[1], l1, edge_value<Real, 0>(m, e1, b, k + 1, j, i), e1c);
+    b2out[o] = v;
+  }
+  if (f3) {
+    const i64 o = f3idx(m, b, k, j, i);
+    double v = b3in[o];
+    v -= term(q[2], l2, edge_value<Real, 1>(m, e2, b, k, j, i + 1), e2c);
+    v += term(q[2], l1, edge_value<Real, 0>(m, e1, b, k, j + 1, i), e1c);
+    b3out[o] = v;
   }
 }
 
@@ -885,7 +871,8 @@ template <typename Real, int KAHAN>
 __global__ void __launch_bounds__(128)
 c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
            const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
-           Real* ulo, Real* __restrict__ w, Real* __restrict__ bcc, DevClock* clk) {
+           Real* ulo, Real* __restrict__ w, Real* __restrict__ bcc, Real* __restrict__ cc,
+           DevClock* clk) {
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   Real cell_dt = big_dt(Real());
   if (t < (i64)m.nb * m.ncell) {
@@ -946,6 +933,7 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     bcc[cb] = bcc1;
     bcc[cb + vs] = bcc2;
     bcc[cb + 2 * vs] = bcc3;
+    store_cce<Real, false>(cc, cb, vs, vx, vy, vz, bcc1, bcc2, bcc3);
     if (do_dt && i >= m.is && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
         k <= m.ke) {
       // new_blockdt.cpp:80-103, in the bulk precision on the stored primitives (FP64
@@ -983,7 +971,8 @@ template <typename Real, int KAHAN>
 __global__ void __launch_bounds__(128)
 c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
               const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
-              Real* ulo, Real* __restrict__ wout, Real* __restrict__ bcc, DevClock* clk) {
+              Real* ulo, Real* __restrict__ wout, Real* __restrict__ bcc,
+              Real* __restrict__ cc, DevClock* clk) {
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   double cell_dt = 1.0e300;
   if (t < (i64)m.nb * m.ncell) {
@@ -1014,6 +1003,8 @@ c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
     bcc[cb] = (Real)bc1;
     bcc[cb + vs] = (Real)bc2;
     bcc[cb + 2 * vs] = (Real)bc3;
+    store_cce<Real, true>(cc, cb, vs, (Real)prim[IVX], (Real)prim[IVY], (Real)prim[IVZ],
+                          (Real)bc1, (Real)bc2, (Real)bc3);
     if (fixed) {
 #pragma unroll
       for (int n = 0; n < NHYDRO; ++n) {

@@ -87,10 +87,10 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
       SRFloors fp{c->desc.gamma, c->desc.dfloor, c->desc.pfloor, c->desc.sigma_max,
                   c->desc.beta_min, c->desc.gamma_max};
       c2p_sr_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
-          m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, c->clk);
+          m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk);
     } else {
       c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
-          m, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, c->clk);
+          m, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk);
     }
   }
   if (rotate) c->r.wsel = 1 - c->r.wsel;
@@ -128,7 +128,7 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
     ProfScope ps(c, "corner_e");
     auto kern = c->desc.relativistic ? corner_e_kernel<Real, true> : corner_e_kernel<Real, false>;
     kern<<<nblk(n, 128), 128, 0, s>>>(
-        m, w, bcc, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f, (Real*)r.e1x2,
+        m, (const Real*)r.cce, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f, (Real*)r.e1x2,
         (Real*)r.e3x2, (Real*)r.w2f, (Real*)r.e1x3, (Real*)r.e2x3, (Real*)r.w3f,
         (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
   }
@@ -136,10 +136,8 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   double* o2 = (stage == 1) ? r.bs2 : r.b2;
   double* o3 = (stage == 1) ? r.bs3 : r.b3;
   {
-    const long long per = (long long)m.nx3 * m.nx2 * (m.nx1 + 1) +
-                          (long long)m.nx3 * (m.nx2 + 1) * m.nx1 +
-                          (long long)(m.nx3 + 1) * m.nx2 * m.nx1;
-    dim3 grid(nblk(per, 256) < 64 ? nblk(per, 256) : 64, m.nb);
+    const long long per = (long long)(m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
+    dim3 grid(nblk(per, 256), m.nb);
     ProfScope ps(c, "ct");
     ct_kernel<Real><<<grid, 256, 0, s>>>(m, beta, c->clk, (const Real*)r.e1,
                                          (const Real*)r.e2, (const Real*)r.e3, r.b1, r.b2,

@@ -34,6 +34,21 @@ METRIC = ("zone-cycles/s on 1 GB300: FP32+learned c2p vs plain FP64 GPU at equal
 NX, NB, NG = (256, 256, 256), (8, 8, 8), 3
 BYTES_PER_ZONE_CYCLE = {"fp32": 260.0, "fp64": 320.0}  # algorithmic HBM bytes
 ACC_CYCLES = 10   # cycles run by both paths for the FP32-vs-FP64 L1 comparison
+PROFILE_CYCLES = 3
+
+# Dominant kernel of the FP32 cycle: the stage-2 x1 sweep (PPM + HLLD), the largest single
+# launch.  Algorithmic bytes per interior zone: W (5) and the two transverse cell-centred
+# field components read, 5 divergence words written (FP32), the x1 face field read (FP64),
+# two face EMFs and the CT weight written (FP32): 7*4 + 5*4 + 8 + 3*4 = 68 B.
+DOMINANT = "flux_x1"
+DOMINANT_STAGE = 2
+DOMINANT_BYTES_PER_ZONE = 68.0
+# DRAM bytes per interior zone of that launch from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, 128^3 case, 2,097,152 zones: 128.0 MB + 47.1 MB), scaled by zones
+DOMINANT_TRAFFIC_PER_ZONE = (128.030976e6 + 47.098368e6) / 2097152
+# warp instructions per interior zone of that launch (ncu smsp__inst_executed.sum at 128^3)
+DOMINANT_INST_PER_ZONE = 156073553.0 / 2097152
+GB300_SMSP = 152 * 4
 
 
 def workload_config(nx=NX, nb=NB):
@@ -182,7 +197,12 @@ def run_gpu(args, rank, world, local_rank):
             g.cycle(1)
             g.synchronize()
             res["launches_per_step"] = g.launch_count()
-            res["profile32"] = g.profile_cycle()
+            # per-kernel CUDA-event profile (non-graph cycles on the library's stream),
+            # averaged over PROFILE_CYCLES cycles
+            profs = [g.profile_cycle() for _ in range(PROFILE_CYCLES)]
+            res["profile32"] = [(profs[0][q][0],
+                                 sum(p[q][1] for p in profs) / len(profs))
+                                for q in range(len(profs[0]))]
             # e2e through the C ABI with pinned host buffers
             pinned = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
                       for a in ic]
@@ -358,8 +378,15 @@ def main():
     zones = mesh.nx[0] * mesh.nx[1] * mesh.nx[2]
     r32, r64 = res["fp32"], res["fp64"]
     peak, peak_kind = measured_peaks()
-    # dominant unit: the whole VL2 cycle (CUDA graph of all stage kernels)
-    achieved = BYTES_PER_ZONE_CYCLE["fp32"] * zones / (r32["seconds"] / r32["steps"]) / 1e9
+    # the whole VL2 cycle (CUDA graph of all stage kernels) as one unit
+    cycle_achieved = (BYTES_PER_ZONE_CYCLE["fp32"] * zones /
+                      (r32["seconds"] / r32["steps"]) / 1e9)
+    # the dominant kernel: its CUDA-event duration in the profiled cycles
+    dom = [ms for name, ms in res["profile32"] if name == DOMINANT]
+    dom_ms = dom[DOMINANT_STAGE - 1]
+    dom_bytes = DOMINANT_BYTES_PER_ZONE * zones
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    sm_hz = (res["clocks"].get("sm_mhz") or 2070.0) * 1e6
     l1 = l1_rel(res["u_fp32"], res["u_fp64"])
     line = {"metric": METRIC, "value": r32["value"], "unit": "zone-cycles/s",
             "n_gpus": world, "steps": r32["steps"], "warmup": args.warmup,
@@ -372,11 +399,20 @@ def main():
             "l1_rel_fp32_vs_fp64": {"cycles": ACC_CYCLES, "d": l1[0], "m1": l1[1],
                                     "m2": l1[2], "m3": l1[3], "e": l1[4]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "kernel": "vl2_cycle (CUDA graph, %d kernels)" %
-                                   res["launches_per_step"],
-                         "bytes_per_zone_cycle": BYTES_PER_ZONE_CYCLE["fp32"],
-                         "peak_kind": peak_kind},
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": DOMINANT_TRAFFIC_PER_ZONE * zones,
+                         "kernel": "flux_x1_kernel<float, PPM, HLLD> (stage 2)",
+                         "launch_ms": dom_ms, "bytes_per_launch": dom_bytes,
+                         "traffic_source": "ncu dram bytes of the 128^3 launch, scaled by "
+                                           "zones",
+                         "limiter": "instruction issue (FP32/ALU), not HBM",
+                         "issue_frac": DOMINANT_INST_PER_ZONE * zones /
+                                       (GB300_SMSP * sm_hz * dom_ms * 1e-3),
+                         "peak_kind": peak_kind,
+                         "cycle": {"achieved": cycle_achieved,
+                                   "frac": cycle_achieved / peak,
+                                   "bytes_per_zone_cycle": BYTES_PER_ZONE_CYCLE["fp32"],
+                                   "kernels": res["launches_per_step"]}},
             "e2e": res["e2e"], "gpu_launches": res["launches_per_step"] * r32["steps"],
             "clocks": res["clocks"],
             "kernel_ms_fp32": res["profile32"], "kernel_ms_fp64": res["profile64"]}
