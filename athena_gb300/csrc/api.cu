@@ -328,8 +328,11 @@ athgpu_status athgpu_download_state(athgpu_ctx* c, double* u, double* b1, double
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   const DevMesh& m = c->m;
   athgpu_status s;
-  if (u && (s = download_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
-    return s;
+  if (u) {  // the stages do not keep U's ghost cells: refresh them from their owners
+    CK(c->desc.precision == ATHGPU_FP64 ? exchange_u_fp64(c) : exchange_u_fp32(c));
+    if ((s = download_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
+      return s;
+  }
   if (b1) CK(cudaMemcpyAsync(b1, c->r.b1, m.nb * m.nf1 * 8, cudaMemcpyDeviceToHost, c->stream));
   if (b2) CK(cudaMemcpyAsync(b2, c->r.b2, m.nb * m.nf2 * 8, cudaMemcpyDeviceToHost, c->stream));
   if (b3) CK(cudaMemcpyAsync(b3, c->r.b3, m.nb * m.nf3 * 8, cudaMemcpyDeviceToHost, c->stream));

@@ -86,4 +86,7 @@ cudaError_t stage_fp64(athgpu_ctx* c, int stage);
 cudaError_t stage_fp32(athgpu_ctx* c, int stage);
 cudaError_t init_fp64(athgpu_ctx* c);
 cudaError_t init_fp32(athgpu_ctx* c);
+// ghost exchange of U and the face fields (U's ghosts are not kept during the stages)
+cudaError_t exchange_u_fp64(athgpu_ctx* c);
+cudaError_t exchange_u_fp32(athgpu_ctx* c);
 }  // namespace athgpu

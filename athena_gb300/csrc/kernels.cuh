@@ -735,7 +735,9 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
 // ---------------------------------------------------------------------------------------
 // Same-level periodic ghost exchange: every ghost cell / face receives the value of the
 // neighbour block that owns it (bvals_cc.cpp:287-430; face fields bvals_fc.cpp:344-397,
-// where a block's own faces along the normal are [is, ie+1]).  Threads enumerate ghost
+// where a block's own faces along the normal are [is, ie+1]).  In the stage only the face
+// fields are exchanged: W(U) reads a ghost cell's conserved state from the owning block
+// directly (src_cell below), which is the value the exchange would have copied.  Threads enumerate ghost
 // elements only: per block and array, the k slabs, then the j slabs of the interior k
 // range, then the i slabs of the interior (k, j) range.
 __device__ __forceinline__ int own_map(int idx, int lo, int hi, int n, int* o) {
@@ -783,12 +785,12 @@ __device__ __forceinline__ void ghost_coord(int r, int N1, int N2, int N3, int I
 // fits, which the launch checks).
 template <typename T, typename I>
 __global__ void __launch_bounds__(256)
-exchange_kernel(DevMesh m, T* __restrict__ u, double* __restrict__ b1,
+exchange_kernel(DevMesh m, int with_u, T* __restrict__ u, double* __restrict__ b1,
                 double* __restrict__ b2, double* __restrict__ b3) {
   I t = (I)blockIdx.x * blockDim.x + threadIdx.x;
   const int n1 = m.nx1, n2 = m.nx2, n3 = m.nx3, ng = m.ng;
-  // ghost counts per block: cells, x1/x2/x3 faces
-  const int gc = (int)(m.ncell - (i64)n1 * n2 * n3);
+  // ghost counts per block: cells (none when U's ghosts are not exchanged), x1/x2/x3 faces
+  const int gc = with_u ? (int)(m.ncell - (i64)n1 * n2 * n3) : 0;
   const int g1 = (int)(m.nf1 - (i64)(n1 + 1) * n2 * n3);
   const int g2 = (int)(m.nf2 - (i64)n1 * (n2 + 1) * n3);
   const int g3 = (int)(m.nf3 - (i64)n1 * n2 * (n3 + 1));
@@ -867,6 +869,19 @@ __device__ __forceinline__ void cta_min_to_clock(Real v, DevClock* clk) {
   }
 }
 
+// Where W(U) reads the conserved state of cell (b,k,j,i): the cell itself in the
+// interior, else the cell of the neighbour block that owns it (periodic same-level mesh).
+__device__ __forceinline__ i64 src_cell(const DevMesh& m, int b, int k, int j, int i,
+                                        int nvar, bool* ghost) {
+  *ghost = i < m.is || i > m.ie || j < m.js || j > m.je || k < m.ks || k > m.ke;
+  if (!*ghost) return cidx(m, b, 0, nvar, k, j, i);
+  int o1, o2, o3;
+  const int si = own_map(i, m.is, m.ie, m.nx1, &o1);
+  const int sj = own_map(j, m.js, m.je, m.nx2, &o2);
+  const int sk = own_map(k, m.ks, m.ke, m.nx3, &o3);
+  return cidx(m, nbr_of(m, b, o1, o2, o3), 0, nvar, sk, sj, si);
+}
+
 template <typename Real, int KAHAN>
 __global__ void __launch_bounds__(128)
 c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
@@ -904,8 +919,10 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     const i64 cb = cidx(m, b, 0, 3, k, j, i);
     const Real gm1 = rgamma(m, Real()) - Real(1.0);
     const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
-    Real u_d = u[c], u_m1 = u[c + vs], u_m2 = u[c + 2 * vs], u_m3 = u[c + 3 * vs],
-         u_e = u[c + 4 * vs];
+    bool ghost;
+    const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
+    Real u_d = u[cs], u_m1 = u[cs + vs], u_m2 = u[cs + 2 * vs], u_m3 = u[cs + 3 * vs],
+         u_e = u[cs + 4 * vs];
     const bool dfloored = !(u_d > dfl);
     u_d = (u_d > dfl) ? u_d : dfl;
     Real di = Real(1.0) / u_d;
@@ -916,11 +933,12 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     const bool pfloored = !(w_p > pfl);
     u_e = (w_p > pfl) ? u_e : ((pfl / gm1) + e_k + pb);
     w_p = (w_p > pfl) ? w_p : pfl;
-    if (dfloored) {
+    // floors rewrite U in the interior only (a ghost's owner floors its own copy)
+    if (dfloored && !ghost) {
       u[c] = u_d;
       if (KAHAN && ulo) ulo[c] = Real(0);
     }
-    if (pfloored) {
+    if (pfloored && !ghost) {
       u[c + 4 * vs] = u_e;
       if (KAHAN && ulo) ulo[c + 4 * vs] = Real(0);
     }
@@ -989,10 +1007,12 @@ c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
     const i64 vs = m.ncell;
     const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
     const i64 cb = cidx(m, b, 0, 3, k, j, i);
+    bool ghost;
+    const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
     double cons[NHYDRO], prim[NHYDRO];
 #pragma unroll
     for (int n = 0; n < NHYDRO; ++n) {
-      cons[n] = (double)u[c + n * vs] + ((KAHAN && ulo) ? (double)ulo[c + n * vs] : 0.0);
+      cons[n] = (double)u[cs + n * vs] + ((KAHAN && ulo) ? (double)ulo[cs + n * vs] : 0.0);
       prim[n] = (double)wout[c + n * vs];
     }
     bool fixed = false;
@@ -1005,7 +1025,7 @@ c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
     bcc[cb + 2 * vs] = (Real)bc3;
     store_cce<Real, true>(cc, cb, vs, (Real)prim[IVX], (Real)prim[IVY], (Real)prim[IVZ],
                           (Real)bc1, (Real)bc2, (Real)bc3);
-    if (fixed) {
+    if (fixed && !ghost) {
 #pragma unroll
       for (int n = 0; n < NHYDRO; ++n) {
         const Real hi = (Real)cons[n];

@@ -9,4 +9,8 @@ cudaError_t stage_fp32(athgpu_ctx* c, int stage) {
   return run_stage<float, 1>(c, stage);
 }
 cudaError_t init_fp32(athgpu_ctx* c) { return run_init<float, 1>(c); }
+cudaError_t exchange_u_fp32(athgpu_ctx* c) {
+  launch_exchange<float>(c, (float*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1);
+  return cudaGetLastError();
+}
 }  // namespace athgpu

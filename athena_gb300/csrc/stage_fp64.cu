@@ -8,4 +8,8 @@ cudaError_t stage_fp64(athgpu_ctx* c, int stage) {
   return run_stage<double, 0>(c, stage);
 }
 cudaError_t init_fp64(athgpu_ctx* c) { return run_init<double, 0>(c); }
+cudaError_t exchange_u_fp64(athgpu_ctx* c) {
+  launch_exchange<double>(c, (double*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1);
+  return cudaGetLastError();
+}
 }  // namespace athgpu

@@ -58,23 +58,34 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
   c->launches += 3;
 }
 
+// Ghost exchange of the face fields, and of U when with_u (outside the stage: U's ghosts
+// are not needed by the stage kernels, see exchange_kernel).
+template <typename Real>
+static void launch_exchange(athgpu_ctx* c, Real* u, double* b1, double* b2, double* b3,
+                            int with_u) {
+  const DevMesh& m = c->m;
+  const long long gc = with_u ? m.ncell - (long long)m.nx1 * m.nx2 * m.nx3 : 0;
+  const long long g1 = m.nf1 - (long long)(m.nx1 + 1) * m.nx2 * m.nx3;
+  const long long g2 = m.nf2 - (long long)m.nx1 * (m.nx2 + 1) * m.nx3;
+  const long long g3 = m.nf3 - (long long)m.nx1 * m.nx2 * (m.nx3 + 1);
+  const long long n = (gc + g1 + g2 + g3) * m.nb;
+  if (n < (1LL << 31) - 256)
+    exchange_kernel<Real, int><<<nblk(n, 256), 256, 0, c->stream>>>(m, with_u, u, b1, b2, b3);
+  else
+    exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, c->stream>>>(m, with_u, u, b1,
+                                                                          b2, b3);
+}
+
 template <typename Real, int KAHAN>
 static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* b2,
-                                    double* b3, int do_dt, bool rotate = true) {
+                                    double* b3, int do_dt, bool rotate = true,
+                                    int with_u = 0) {
   const DevMesh& m = c->m;
   cudaStream_t s = c->stream;
   const long long nc = (long long)m.nb * m.ncell;
   {
-    const long long gc = m.ncell - (long long)m.nx1 * m.nx2 * m.nx3;
-    const long long g1 = m.nf1 - (long long)(m.nx1 + 1) * m.nx2 * m.nx3;
-    const long long g2 = m.nf2 - (long long)m.nx1 * (m.nx2 + 1) * m.nx3;
-    const long long g3 = m.nf3 - (long long)m.nx1 * m.nx2 * (m.nx3 + 1);
-    const long long n = (gc + g1 + g2 + g3) * m.nb;
     ProfScope ps(c, "exchange");
-    if (n < (1LL << 31) - 256)
-      exchange_kernel<Real, int><<<nblk(n, 256), 256, 0, s>>>(m, u, b1, b2, b3);
-    else
-      exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, s>>>(m, u, b1, b2, b3);
+    launch_exchange<Real>(c, u, b1, b2, b3, with_u);
   }
   // the compensation register belongs to U only; the stage-1 register U* has none
   Real* lo = (u == (Real*)c->r.u) ? (Real*)c->r.ulo : nullptr;
@@ -158,8 +169,9 @@ static inline cudaError_t run_end_cycle(athgpu_ctx* c) {
 
 template <typename Real, int KAHAN>
 static cudaError_t run_init(athgpu_ctx* c) {
+  // Mesh::Initialize exchanges U as well: its ghosts are consistent after initialization
   launch_exchange_and_c2p<Real, KAHAN>(c, (Real*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1,
-                                       false);
+                                       false, 1);
   advance_clock_kernel<<<1, 32, 0, c->stream>>>(c->clk, c->m.cfl, c->m.tlim, 0);
   c->launches += 1;
   return cudaGetLastError();

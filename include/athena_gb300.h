@@ -127,7 +127,10 @@ athgpu_status athgpu_synchronize(athgpu_ctx *ctx);
 athgpu_status athgpu_floor_count(athgpu_ctx *ctx, long long *count, int reset);
 
 /* Device pointers of the registers, for callers that keep their data on the GPU
- * (u and ustar: Real = double in FP64 mode, float in FP32 mode). */
+ * (u and ustar: Real = double in FP64 mode, float in FP32 mode).  The stages keep the
+ * ghost cells of w, bcc and the face fields current but not those of u (W(U) reads a ghost
+ * cell's conserved state from the block that owns it); athgpu_initialize and
+ * athgpu_download_state refresh u's ghosts. */
 typedef struct {
   void *u, *ulo, *w, *bcc;
   double *b1, *b2, *b3;
