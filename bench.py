@@ -44,10 +44,10 @@ DOMINANT = "flux_x1"
 DOMINANT_STAGE = 2
 DOMINANT_BYTES_PER_ZONE = 68.0
 # DRAM bytes per interior zone of that launch from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, 128^3 case, 2,097,152 zones: 128.0 MB + 47.1 MB), scaled by zones
-DOMINANT_TRAFFIC_PER_ZONE = (128.030976e6 + 47.098368e6) / 2097152
+# dram__bytes_write.sum, 128^3 case, 2,097,152 zones: 128.0 MB + 46.8 MB), scaled by zones
+DOMINANT_TRAFFIC_PER_ZONE = (128.020224e6 + 46.763776e6) / 2097152
 # warp instructions per interior zone of that launch (ncu smsp__inst_executed.sum at 128^3)
-DOMINANT_INST_PER_ZONE = 156073553.0 / 2097152
+DOMINANT_INST_PER_ZONE = 153832579.0 / 2097152
 GB300_SMSP = 152 * 4
 
 
