@@ -520,6 +520,121 @@ const char* athgpu_profile_label(athgpu_ctx* c, int idx) {
   return c->prof_names[idx].c_str();
 }
 
+namespace {
+// Device-to-device snapshot of everything a cycle changes (U and its compensation, both
+// primitive buffers, the cell-centred field and E, the face fields, the clock), so that
+// tuning runs leave the simulation state untouched.
+struct StateSnapshot {
+  std::vector<std::pair<void*, size_t>> regs;
+  char* store = nullptr;
+  DevClock clk;
+  int wsel = 0;
+};
+
+athgpu_status snapshot(athgpu_ctx* c, StateSnapshot* sn) {
+  const DevMesh& m = c->m;
+  const size_t rb = c->real_bytes, nb = m.nb, nc = m.ncell;
+  Registers& r = c->r;
+  sn->regs = {{r.u, nb * 5 * nc * rb},       {r.wbuf[0], nb * 5 * nc * rb},
+              {r.wbuf[1], nb * 5 * nc * rb}, {r.bcc, nb * 3 * nc * rb},
+              {r.cce, nb * 3 * nc * rb},     {r.b1, nb * m.nf1 * 8},
+              {r.b2, nb * m.nf2 * 8},        {r.b3, nb * m.nf3 * 8}};
+  if (r.ulo) sn->regs.push_back({r.ulo, nb * 5 * nc * rb});
+  size_t total = 0;
+  for (auto& q : sn->regs) total += q.second;
+  CK(cudaMalloc((void**)&sn->store, total));
+  size_t off = 0;
+  for (auto& q : sn->regs) {
+    CK(cudaMemcpyAsync(sn->store + off, q.first, q.second, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    off += q.second;
+  }
+  CK(cudaMemcpyAsync(&sn->clk, c->clk, sizeof(DevClock), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  sn->wsel = r.wsel;
+  return ATHGPU_OK;
+}
+
+athgpu_status restore(athgpu_ctx* c, StateSnapshot* sn) {
+  size_t off = 0;
+  for (auto& q : sn->regs) {
+    CK(cudaMemcpyAsync(q.first, sn->store + off, q.second, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    off += q.second;
+  }
+  CK(cudaMemcpyAsync(c->clk, &sn->clk, sizeof(DevClock), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->r.wsel = sn->wsel;
+  CK(cudaFree(sn->store));
+  sn->store = nullptr;
+  return ATHGPU_OK;
+}
+
+// average time of `cycles` cycles (non-graph launches, CUDA events on the stream) after
+// one warm-up cycle
+athgpu_status time_cycles(athgpu_ctx* c, int cycles, float* ms) {
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  for (int q = 0; q <= cycles; ++q) {
+    if (q == 1) CK(cudaEventRecord(a, c->stream));
+    CK(run_stage_dispatch(c, 1));
+    CK(run_stage_dispatch(c, 2));
+    CK(run_stage_dispatch(c, 0));
+  }
+  CK(cudaEventRecord(b, c->stream));
+  CK(cudaEventSynchronize(b));
+  CK(cudaEventElapsedTime(ms, a, b));
+  *ms /= cycles;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ATHGPU_OK;
+}
+}  // namespace
+
+athgpu_status athgpu_autotune(athgpu_ctx* c, int cycles, int* seg_x2, int* seg_x3) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (!c->initialized) return fail(ATHGPU_ERR_STATE, "athgpu_initialize not called");
+  if (cycles < 1) cycles = 2;
+  StateSnapshot sn;
+  athgpu_status st = snapshot(c, &sn);
+  if (st != ATHGPU_OK) return st;
+  const LaunchConfig keep = c->lc;
+  // candidate segment lengths: the whole column and its halves down to 4 cells
+  auto candidates = [](int n) {
+    std::vector<int> v;
+    for (int sgl = n; sgl >= 4; sgl /= 2) v.push_back(sgl);
+    if (v.empty()) v.push_back(n);
+    return v;
+  };
+  int best2 = c->lc.seg_x2 > 0 ? c->lc.seg_x2 : c->m.nx2;
+  int best3 = c->lc.seg_x3 > 0 ? c->lc.seg_x3 : c->m.nx3;
+  for (int dir = 2; dir <= 3 && st == ATHGPU_OK; ++dir) {  // coordinate search
+    float best_ms = 3.0e38f;
+    for (int cand : candidates(dir == 2 ? c->m.nx2 : c->m.nx3)) {
+      c->lc.seg_x2 = dir == 2 ? cand : best2;
+      c->lc.seg_x3 = dir == 3 ? cand : best3;
+      float ms = 0.0f;
+      if ((st = time_cycles(c, cycles, &ms)) != ATHGPU_OK) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        if (dir == 2) best2 = cand; else best3 = cand;
+      }
+    }
+  }
+  athgpu_status st2 = restore(c, &sn);
+  if (st != ATHGPU_OK) {
+    c->lc = keep;
+    return st;
+  }
+  if (st2 != ATHGPU_OK) return st2;
+  c->lc = keep;
+  st = athgpu_set_sweep_segment(c, best2, best3);  // also drops the captured graph
+  if (seg_x2) *seg_x2 = best2;
+  if (seg_x3) *seg_x3 = best3;
+  return st;
+}
+
 athgpu_status athgpu_launch_count(athgpu_ctx* c, long long* count, int reset) {
   if (!c || !count) return fail(ATHGPU_ERR_ARG, "null argument");
   *count = c->launches;

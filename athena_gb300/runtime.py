@@ -81,6 +81,7 @@ def load_library(path=LIB_PATH):
         "athgpu_floor_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
         "athgpu_device_state_ptrs": ([vp, ctypes.POINTER(DeviceState)], ip),
         "athgpu_set_sweep_segment": ([vp, ip, ip], ip),
+        "athgpu_autotune": ([vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
         "athgpu_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
         "athgpu_profile_cycle": ([vp, ip, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ip)], ip),
@@ -241,6 +242,14 @@ class StageUpdate:
                "athgpu_profile_cycle")
         return [(L.athgpu_profile_label(self.h, i).decode(), buf[i])
                 for i in range(min(n.value, 256))]
+
+    def autotune(self, cycles=2):
+        """Pick the x2/x3 sweep segment lengths by timing (state left unchanged);
+        returns (seg_x2, seg_x3)."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        _check(load_library().athgpu_autotune(self.h, int(cycles), ctypes.byref(a),
+                                              ctypes.byref(b)), "athgpu_autotune")
+        return a.value, b.value
 
     def set_sweep_segment(self, seg_x2, seg_x3):
         _check(load_library().athgpu_set_sweep_segment(self.h, seg_x2, seg_x3),

@@ -166,6 +166,8 @@ def run_gpu(args, rank, world, local_rank):
         g.set_stream(stream.cuda_stream)
         g.set_state(*ic)
         g.initialize()
+        if prec == "fp32":  # sweep tiling picked by the autotuner (state left unchanged)
+            res["tiling"] = dict(zip(("seg_x2", "seg_x3"), g.autotune(cycles=2)))
         steps = args.steps if prec == "fp32" else max(3, min(args.steps, 10))
         sampler = ClockSampler(local_rank) if prec == "fp32" else None
         if world > 1:
@@ -233,7 +235,9 @@ def run_gpu(args, rank, world, local_rank):
                           "steps": e_steps}
         g.close()
     if not args.no_learned:
-        res["learned_c2p"] = run_learned_c2p()
+        res["learned_c2p"], net = run_learned_c2p()
+        if not args.no_sr:
+            res["sr_kh"] = run_sr_kh(args.nx, stream, net)
     return mesh, res
 
 
@@ -287,6 +291,88 @@ def run_learned_c2p(reps=5):
             out[name]["fallbacks"] = fb
     out["speedup"] = out["plain"]["ms"] / out["learned"]["ms"]
     out["passes_ratio"] = out["learned"]["mean_fp64_passes"] / out["plain"]["mean_fp64_passes"]
+    return out, net
+
+
+SR_CYCLES = {"fp32": 10, "fp64": 3}
+SR_ACC_CYCLES = 5
+
+
+def run_sr_kh(n, stream, net):
+    """Relativistic Kelvin-Helmholtz shear layer (SURVEY config 5 workload): n^3 periodic
+    box as (n/32)^3 MeshBlocks, gamma 4/3, v_x = +-0.5c with tanh width 0.01, rho 1 / 0.1,
+    p = 1, uniform B_x with sigma 0.1, seeded 1e-3 velocity noise, VL2 + PLM + HLLE.
+    Zone-cycles/s of the FP32 and FP64 SR stage paths (CUDA events, state resident), their
+    relative L1 difference after SR_ACC_CYCLES cycles, and the con2prim start study: the
+    conserved state of one cycle solved per cell from the previous cycle's pressure (the
+    stage's start) and from the network refined in FP32."""
+    import torch
+    from athena_gb300 import pgen
+    from athena_gb300.learned_c2p import MODE_LEARNED_FP32, MODE_PLAIN
+    from athena_gb300.mesh import MeshSpec
+    from athena_gb300.runtime import StageUpdate
+    nx, nb = (n,) * 3, (n // 32,) * 3
+    mesh = MeshSpec(nx, nb, 2)
+    gam = 4.0 / 3.0
+    gw, f1, f2, f3 = pgen.sr_kelvin_helmholtz(nx, seed=20261204)
+    gu = pgen.sr_prim_to_cons(gw, pgen.cell_centered(f1, f2, f3), gam)
+    ic = (mesh.scatter_cells(gu),) + mesh.scatter_faces(f1, f2, f3)
+    w0 = mesh.scatter_cells(gw)
+    del gu, gw
+    zones = n ** 3
+    out = {"workload": "relativistic Kelvin-Helmholtz %d^3 periodic as %d MeshBlocks of "
+                       "32^3, gamma 4/3, shear +-0.5c, sigma 0.1, VL2 + PLM + HLLE" %
+                       (n, nb[0] * nb[1] * nb[2])}
+    finals = {}
+    for prec in ("fp32", "fp64"):
+        g = StageUpdate(mesh, gam, xorder=2, rsolver="hlle", precision=prec, cfl=0.3,
+                        relativistic=True)
+        g.set_stream(stream.cuda_stream)
+        g.set_state(*ic)
+        g.set_prim(w0)
+        g.initialize()
+        t = time_device_cycles(g, stream, SR_CYCLES[prec], 3)
+        out[prec] = {"value": zones * SR_CYCLES[prec] / t, "unit": "zone-cycles/s",
+                     "ms_per_step": t / SR_CYCLES[prec] * 1e3, "steps": SR_CYCLES[prec]}
+        g.set_state(*ic)
+        g.set_prim(w0)
+        g.set_clock(0.0, 1.7976931348623157e308)
+        g.initialize()
+        g.cycle(SR_ACC_CYCLES - 1)
+        if prec == "fp64":
+            w_prev, _ = g.prim()
+        g.cycle(1)
+        finals[prec] = mesh.interior(g.state()[0])
+        if prec == "fp64":
+            u_new = g.state()[0]
+            _, bcc_new = g.prim()
+        g.close()
+    out["speedup_fp32_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    l1 = l1_rel(finals["fp32"], finals["fp64"])
+    out["l1_rel_fp32_vs_fp64"] = {"cycles": SR_ACC_CYCLES, "d": l1[0], "m1": l1[1],
+                                  "m2": l1[2], "m3": l1[3], "e": l1[4]}
+    # con2prim start study on the interior cells of cycle SR_ACC_CYCLES
+    cons = np.ascontiguousarray(np.moveaxis(mesh.interior(u_new), 1, -1).reshape(-1, 5))
+    bcc = np.ascontiguousarray(np.moveaxis(mesh.interior(bcc_new), 1, -1).reshape(-1, 3))
+    pprev = np.ascontiguousarray(np.moveaxis(mesh.interior(w_prev), 1, -1)
+                                 .reshape(-1, 5)[:, 4])
+    dc, db, dp = net.to_dev(cons), net.to_dev(bcc), net.to_dev(pprev)
+    study = {"cells": int(cons.shape[0])}
+    for name, mode, guess in (("previous_pressure", MODE_PLAIN, dp),
+                              ("learned", MODE_LEARNED_FP32, dp)):
+        ts = []
+        for rep in range(4):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record()
+            prim, it, _, fb = net.solve(dc, db, mode, pgas_guess=guess)
+            s1.record()
+            s1.synchronize()
+            ts.append(s0.elapsed_time(s1))
+        it = it.cpu().numpy()
+        study[name] = {"mean_fp64_passes": float(it[it >= 0].mean()),
+                       "unconverged": int((it < 0).sum()), "ms": float(np.median(ts[1:])),
+                       "fallbacks": fb}
+    out["c2p_start_study"] = study
     return out
 
 
@@ -323,7 +409,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
-                    help="skip the isolated learned-con2prim measurement")
+                    help="skip the isolated learned-con2prim and the SR measurements")
+    ap.add_argument("--no-sr", action="store_true",
+                    help="skip the relativistic Kelvin-Helmholtz measurement")
     ap.add_argument("--nx", type=int, default=256,
                     help="cells per direction (MeshBlocks of 32^3); 256 is the workload")
     args = ap.parse_args()
@@ -370,6 +458,8 @@ def main():
         dist.init_process_group("nccl")
     mesh, res = run_gpu(args, rank, world, local_rank)
     line_config = workload_config(NX, NB)
+    if "tiling" in res:
+        line_config["sweep_tiling_autotuned"] = res["tiling"]
     if rank != 0:
         if world > 1:
             import torch.distributed as dist
@@ -418,6 +508,8 @@ def main():
             "kernel_ms_fp32": res["profile32"], "kernel_ms_fp64": res["profile64"]}
     if "learned_c2p" in res:
         line["learned_c2p"] = res["learned_c2p"]
+    if "sr_kh" in res:
+        line["sr_kh"] = res["sr_kh"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline((mesh, make_ic(NX, NB)[1]))
     print(json.dumps(line))

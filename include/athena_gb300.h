@@ -142,6 +142,15 @@ athgpu_status athgpu_device_state_ptrs(athgpu_ctx *ctx, athgpu_device_state *out
  * autotuner's knob); 0 = heuristic default. */
 athgpu_status athgpu_set_sweep_segment(athgpu_ctx *ctx, int seg_x2, int seg_x3);
 
+/* Autotuner of the sweep tiling: times `cycles` cycles (after one warm-up) for each
+ * candidate segment length of the x2 sweep (the whole column, then halves down to 4
+ * cells), keeps the fastest, then does the same for the x3 sweep, and applies the pair
+ * (*seg_x2, *seg_x3 receive it; either may be NULL).  The simulation state, the clock and
+ * the primitive-buffer rotation are snapshotted on the device before and restored after,
+ * so the call does not advance the run.  Allocates the snapshot (one copy of the state)
+ * for the duration of the call.  Synchronous. */
+athgpu_status athgpu_autotune(athgpu_ctx *ctx, int cycles, int *seg_x2, int *seg_x3);
+
 /* Run one cycle without the CUDA graph, timing every kernel launch with CUDA events on
  * the context's stream; ms[i] (i < cap) receives the duration of launch i, *count the
  * number of launches, athgpu_profile_label(ctx, i) its kernel name.  The state advances

@@ -188,3 +188,28 @@ def test_graph_replay_counts_launches():
     g.synchronize()
     per = g.launch_count() / 3
     assert per == 2 * 7 + 1   # two stages of 7 kernels, one clock update
+
+
+def test_autotune_keeps_the_state_and_the_results():
+    """The autotuner times the sweep tilings on the live state and restores it: the run
+    continues bit for bit as if it had not been called."""
+    mesh, ic, _ = _turb_case(nx=(32, 32, 32), nb=(2, 2, 2))
+    runs = []
+    for tune in (False, True):
+        g = StageUpdate(mesh, 5.0 / 3.0, xorder=3, rsolver="hlld", cfl=0.3)
+        g.set_state(*ic)
+        g.initialize()
+        g.cycle(1)
+        if tune:
+            before = g.state()
+            t_before = (g.time, g.dt)
+            s2, s3 = g.autotune(cycles=1)
+            assert s2 in (16, 8, 4) and s3 in (16, 8, 4)
+            after = g.state()
+            assert all(np.array_equal(a, b) for a, b in zip(before, after))
+            assert (g.time, g.dt) == t_before
+        g.cycle(2)
+        runs.append(g.state())
+        g.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
