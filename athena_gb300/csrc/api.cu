@@ -52,7 +52,7 @@ void free_all(athgpu_ctx* c) {
   void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.cce, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
-                  c->nbr, c->staging};
+                  c->nbr, c->staging, c->c2p_queue, c->c2p_qcount};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
@@ -195,6 +195,10 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   if (rb == 4) {
     allocs.push_back({&r.ulo, nb * 5 * m.ncell * rb});
     allocs.push_back({(void**)&c->staging, nb * 5 * m.ncell * 8});
+  }
+  if (d->relativistic) {
+    allocs.push_back({(void**)&c->c2p_queue, nb * m.nx1 * m.nx2 * m.nx3 * (i64)sizeof(int)});
+    allocs.push_back({(void**)&c->c2p_qcount, (i64)sizeof(unsigned)});
   }
   for (auto& a : allocs) {
     e = cudaMalloc(a.p, a.bytes);

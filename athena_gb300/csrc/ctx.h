@@ -31,6 +31,7 @@ struct Registers {
 
 struct LaunchConfig {
   int seg_x2 = 0, seg_x3 = 0;  // faces per thread along the x2/x3 sweeps (0: default)
+  int sr_phase1 = 0;           // SR con2prim: first-solve passes in phase 1 (0: default)
 };
 
 }  // namespace athgpu
@@ -54,6 +55,8 @@ struct athgpu_ctx {
   long long launches = 0;
   long long per_cycle = 0;
   double* staging = nullptr;  // device staging of FP64 host data in FP32 mode
+  int* c2p_queue = nullptr;      // SR con2prim: interior cells deferred to phase 2
+  unsigned* c2p_qcount = nullptr;
   // per-kernel timing of one non-graph cycle (athgpu_profile_cycle)
   bool profiling = false;
   std::vector<std::string> prof_names;

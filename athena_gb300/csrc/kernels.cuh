@@ -978,70 +978,143 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
   if (do_dt) cta_min_to_clock<Real>(cell_dt, clk);  // reduced in the bulk precision
 }
 
-// EquationOfState::ConservedToPrimitive for SR MHD (adiabatic_mhd_sr.cpp:72-272) over
-// whole blocks, in FP64: the Newman-Hamlin solve of every cell is seeded from the output
+// EquationOfState::ConservedToPrimitive for SR MHD (adiabatic_mhd_sr.cpp:72-272) on the
+// interior cells, in FP64: the Newman-Hamlin solve of every cell is seeded from the output
 // array's previous contents (wout holds the primitives of two con2prim calls ago, the
 // reference's w1 register, :143-154 and time_integrator.cpp:2221-2269).  In FP32 mode the
-// conserved input is hi + lo and a re-synced conserved state is split back.  When do_dt
-// is set the interior cells contribute min(dx1, dx2, dx3) to the CFL reduction (the SR
-// branch of new_blockdt.cpp:74 keeps the widths: signal speed 1).
-template <typename Real, int KAHAN>
+// conserved input is hi + lo, a re-synced conserved state is split back, and (REFINE) the
+// stale pressure is first refined by FP32 iterations of the same scheme, which the FP64
+// solve then finishes.  When do_dt is set the interior cells contribute
+// min(dx1, dx2, dx3) to the CFL reduction (the SR branch of new_blockdt.cpp:74 keeps the
+// widths: signal speed 1).
+//
+// Warp-coherent two-phase schedule: the iteration count varies from cell to cell and a
+// warp runs as long as its slowest lane, so phase 1 (queue != null on input, phase == 1)
+// caps the first solve at max_first passes and appends each cell still iterating to the
+// queue; phase 2 runs the whole con2prim of the queued cells (grid-stride over the
+// count).  The solve is deterministic, so the result equals one uncapped pass.  Ghost
+// cells are not solved: a ghost's primitives equal its owner's (same conserved state, same
+// stale guess, both kept equal since initialization), so copy_ghost_prims_kernel copies
+// them afterwards.
+template <typename Real, int KAHAN, int REFINE>
 __global__ void __launch_bounds__(128)
 c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
               const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
               Real* ulo, Real* __restrict__ wout, Real* __restrict__ bcc,
-              Real* __restrict__ cc, DevClock* clk) {
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  double cell_dt = 1.0e300;
-  if (t < (i64)m.nb * m.ncell) {
-    const int b = (int)(t / m.ncell);
-    i64 r = t - (i64)b * m.ncell;
-    const int i = (int)(r % m.nc1);
-    r /= m.nc1;
-    const int j = (int)(r % m.nc2);
-    const int k = (int)(r / m.nc2);
-    const double lw = 0.5, rw = 0.5;
-    const double bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
-    const double bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
-    const double bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
-    const i64 vs = m.ncell;
-    const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
-    const i64 cb = cidx(m, b, 0, 3, k, j, i);
-    bool ghost;
-    const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
-    double cons[NHYDRO], prim[NHYDRO];
-#pragma unroll
-    for (int n = 0; n < NHYDRO; ++n) {
-      cons[n] = (double)u[cs + n * vs] + ((KAHAN && ulo) ? (double)ulo[cs + n * vs] : 0.0);
-      prim[n] = (double)wout[c + n * vs];
-    }
-    bool fixed = false;
-    int it = 0;
-    const bool ok = sr_c2p_cell(fp, cons, bc1, bc2, bc3, prim, &fixed, &it);
-#pragma unroll
-    for (int n = 0; n < NHYDRO; ++n) wout[c + n * vs] = (Real)prim[n];
-    bcc[cb] = (Real)bc1;
-    bcc[cb + vs] = (Real)bc2;
-    bcc[cb + 2 * vs] = (Real)bc3;
-    store_cce<Real, true>(cc, cb, vs, (Real)prim[IVX], (Real)prim[IVY], (Real)prim[IVZ],
-                          (Real)bc1, (Real)bc2, (Real)bc3);
-    if (fixed && !ghost) {
+              Real* __restrict__ cc, DevClock* clk, int phase, int max_first,
+              int* __restrict__ queue, unsigned* __restrict__ qcount) {
+  const int n1 = m.nx1, n2 = m.nx2, n3 = m.nx3;
+  const long long ninterior = (long long)m.nb * n1 * n2 * n3;
+  long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long count = phase == 1 ? ninterior : (long long)*qcount;
+  // phase 1 runs one pass over the cells (with the CTA-wide dt reduction at the end);
+  // phase 2 strides over the queue
+  for (; phase == 2 ? e < count : true; e += stride) {
+    double cell_dt = 1.0e300;
+    bool enqueue = false;
+    long long t = -1;
+    if (e < count) t = phase == 1 ? e : (long long)queue[e];
+    if (t >= 0) {
+      const int b = (int)(t / ((long long)n1 * n2 * n3));
+      int r = (int)(t - (long long)b * n1 * n2 * n3);
+      const int i = m.is + r % n1;
+      r /= n1;
+      const int j = m.js + r % n2;
+      const int k = m.ks + r / n2;
+      const double lw = 0.5, rw = 0.5;
+      const double bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
+      const double bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
+      const double bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
+      const i64 vs = m.ncell;
+      const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
+      const i64 cb = cidx(m, b, 0, 3, k, j, i);
+      double cons[NHYDRO], prim[NHYDRO];
 #pragma unroll
       for (int n = 0; n < NHYDRO; ++n) {
-        const Real hi = (Real)cons[n];
-        u[c + n * vs] = hi;
-        if (KAHAN && ulo) ulo[c + n * vs] = (Real)(cons[n] - (double)hi);
+        cons[n] = (double)u[c + n * vs] + ((KAHAN && ulo) ? (double)ulo[c + n * vs] : 0.0);
+        prim[n] = (double)wout[c + n * vs];
+      }
+      double pstart = 0.0;
+      if (REFINE) {  // the stale pressure refined in FP32 (raw conserved state)
+        const double mm_sq = cons[IVX] * cons[IVX] + cons[IVY] * cons[IVY] +
+                             cons[IVZ] * cons[IVZ];
+        const double bb_sq = bc1 * bc1 + bc2 * bc2 + bc3 * bc3;
+        const double tt = cons[IVX] * bc1 + cons[IVY] * bc2 + cons[IVZ] * bc3;
+        int it32;
+        pstart = sr_refine_f32(fp.gamma_adi, cons[IDN], cons[IPR], mm_sq, bb_sq, tt,
+                               smax(prim[IPR], fp.pfloor), 12, 1.0e-6f, &it32);
+      }
+      bool fixed = false, deferred = false;
+      int it = 0;
+      const bool ok = sr_c2p_cell(fp, cons, bc1, bc2, bc3, prim, &fixed, &it, pstart,
+                                  phase == 1 ? max_first : 15, &deferred);
+      if (deferred) {
+        enqueue = true;
+      } else {
+#pragma unroll
+        for (int n = 0; n < NHYDRO; ++n) wout[c + n * vs] = (Real)prim[n];
+        bcc[cb] = (Real)bc1;
+        bcc[cb + vs] = (Real)bc2;
+        bcc[cb + 2 * vs] = (Real)bc3;
+        store_cce<Real, true>(cc, cb, vs, (Real)prim[IVX], (Real)prim[IVY], (Real)prim[IVZ],
+                              (Real)bc1, (Real)bc2, (Real)bc3);
+        if (fixed) {
+#pragma unroll
+          for (int n = 0; n < NHYDRO; ++n) {
+            const Real hi = (Real)cons[n];
+            u[c + n * vs] = hi;
+            if (KAHAN && ulo) ulo[c + n * vs] = (Real)(cons[n] - (double)hi);
+          }
+        }
+        if (do_dt && (fixed || !ok)) atomicAdd(&clk->c2p_floor_count, 1);
+      }
+      if (phase == 1 && do_dt) {
+        const double dt1 = m.dx1f[(i64)b * m.nc1 + i], dt2 = m.dx2f[(i64)b * m.nc2 + j],
+                     dt3 = m.dx3f[(i64)b * m.nc3 + k];
+        cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
       }
     }
-    if (do_dt && (fixed || !ok)) atomicAdd(&clk->c2p_floor_count, 1);
-    if (do_dt && i >= m.is && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
-        k <= m.ke) {
-      const double dt1 = m.dx1f[(i64)b * m.nc1 + i], dt2 = m.dx2f[(i64)b * m.nc2 + j],
-                   dt3 = m.dx3f[(i64)b * m.nc3 + k];
-      cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
+    if (phase == 2) continue;
+    // phase 1: warp-aggregated append of the deferred cells, then the dt reduction
+    const unsigned mask = __ballot_sync(0xffffffffu, enqueue);
+    if (mask) {
+      const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(qcount, (unsigned)__popc(mask));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (enqueue) queue[base + __popc(mask & ((1u << lane) - 1u))] = (int)t;
     }
+    if (do_dt) cta_min_to_clock<double>(cell_dt, clk);
+    break;
   }
-  if (do_dt) cta_min_to_clock<double>(cell_dt, clk);
+}
+
+// Ghost cells of the primitives, the cell-centred field and the cell-centred E, copied
+// from the blocks that own them (the relativistic W(U) solves interior cells only).
+template <typename Real>
+__global__ void __launch_bounds__(256)
+copy_ghost_prims_kernel(DevMesh m, Real* __restrict__ w, Real* __restrict__ bcc,
+                        Real* __restrict__ cc) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int gc = (int)(m.ncell - (i64)m.nx1 * m.nx2 * m.nx3);
+  if (t >= (long long)gc * m.nb) return;
+  const int b = (int)(t / gc);
+  int k, j, i;
+  ghost_coord((int)(t - (long long)b * gc), m.nc1, m.nc2, m.nc3, m.nx1, m.nx2, m.nx3, m.ng,
+              k, j, i);
+  bool ghost;
+  const i64 s5 = src_cell(m, b, k, j, i, NHYDRO, &ghost);
+  const i64 s3 = src_cell(m, b, k, j, i, 3, &ghost);
+  const i64 d5 = cidx(m, b, 0, NHYDRO, k, j, i), d3 = cidx(m, b, 0, 3, k, j, i);
+  const i64 vs = m.ncell;
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) w[d5 + n * vs] = w[s5 + n * vs];
+#pragma unroll
+  for (int n = 0; n < 3; ++n) {
+    bcc[d3 + n * vs] = bcc[s3 + n * vs];
+    cc[d3 + n * vs] = cc[s3 + n * vs];
+  }
 }
 
 // Mesh::NewTimeStep (mesh.cpp:1236-1281) after the main loop's time += dt

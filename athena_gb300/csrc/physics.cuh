@@ -647,15 +647,40 @@ __device__ __forceinline__ bool sr_normal(double gamma_adi, double dd, double ee
                              false);
 }
 
+// A start for the FP64 solve: up to max_it FP32 iterations of the same fixed-point scheme
+// from p0 (test relative to p, tol), returning the converged or the last FP32 iterate (p0
+// itself if the FP32 iteration produced nothing usable).  *iters = FP32 passes.
+__device__ __forceinline__ double sr_refine_f32(double gamma_adi, double dd, double ee,
+                                                double mm_sq, double bb_sq, double tt,
+                                                double p0, int max_it, float tol,
+                                                int* iters) {
+  float d, pmin, last = (float)p0, pg[3];
+  sr_nh_setup<float>((float)ee, (float)mm_sq, (float)bb_sq, (float)tt, &d, &pmin);
+  pg[0] = fmaxf((float)p0, pmin);
+  const int k = sr_nh_loop<float>((float)gamma_adi, (float)dd, (float)ee, (float)mm_sq,
+                                  (float)bb_sq, (float)tt, d, pmin, pg, 0, max_it, tol, true,
+                                  &last);
+  *iters = k < max_it ? k + 1 : max_it;
+  const float p = k < max_it ? pg[(k + 1) % 3] : last;
+  return (isfinite(p) && p > 0.0f) ? (double)p : p0;
+}
+
 struct SRFloors { double gamma_adi, dfloor, pfloor, sigma_max, beta_min, gamma_max; };
 
 // One cell of EquationOfState::ConservedToPrimitive (SR), adiabatic_mhd_sr.cpp:87-268:
 // conserved floors, solve from the guess in prim (the output array's stale value,
 // :143-154), fallback, floors, gamma ceiling, conserved re-sync.  cons[5] (natural slots)
 // may be rewritten (*fixed set).  Returns false if the solve failed.
+//
+// pstart > 0 replaces the first solve's start (the FP32 path passes the stale pressure
+// refined in FP32; the fallback state is still the stale primitives), and max_first < 15
+// caps the first solve: a cell that has not converged by then returns with *deferred set
+// and prim, cons untouched, to be solved again in full by a later pass (the solve is
+// deterministic, so the result is the same as one uncapped call).
 __device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, double bc1,
                                             double bc2, double bc3, double* prim,
-                                            bool* fixed_out, int* iters) {
+                                            bool* fixed_out, int* iters, double pstart = 0.0,
+                                            int max_first = 15, bool* deferred = nullptr) {
   const double gamma_adi = fp.gamma_adi;
   const double mm_sq_ee_sq_max = 1.0 - 1.0e-12;
   double dd = cons[IDN], ee = cons[IPR];
@@ -680,8 +705,14 @@ __device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, do
   double pgas_old = smax(prim[IPR], pressure_floor_local);
   double u1_old = prim[IVX], u2_old = prim[IVY], u3_old = prim[IVZ];
   double gamma = 0.0, pmag = 0.0;
-  bool success = sr_normal(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2, bc3, tt,
-                           pgas_old, prim, &gamma, &pmag, iters);
+  bool success = sr_normal_t<double>(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2,
+                                     bc3, tt, pstart > 0.0 ? pstart : pgas_old, prim, &gamma,
+                                     &pmag, iters, max_first, 1.0e-12, false);
+  if (!success && max_first < 15 && *iters == max_first) {  // capped: finish later
+    if (deferred) *deferred = true;
+    *fixed_out = false;
+    return false;
+  }
   if (!success) {
     prim[IDN] = rho_old; prim[IPR] = pgas_old;
     prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;

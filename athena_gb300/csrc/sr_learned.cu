@@ -490,7 +490,8 @@ sr_c2p_phase1_kernel(long long n, double gamma, double pfloor, const double* __r
                      double* __restrict__ prim, int* __restrict__ iters64,
                      int* __restrict__ iters32, int* __restrict__ fallbacks, Queue qu) {
   __shared__ SmemNet net;
-  if (mode > 0) {
+  const bool use_net = mode == 1 || mode == 2;
+  if (use_net) {
     load_net(params, net);
     __syncthreads();
   }
@@ -500,7 +501,7 @@ sr_c2p_phase1_kernel(long long n, double gamma, double pfloor, const double* __r
   const double pstd = (valid && pgas_guess) ? pgas_guess[c] : pfloor;
   double guess = pstd;
   int it32 = 0;
-  if (mode > 0) {  // the whole warp takes part in the tensor-core evaluation
+  if (use_net) {  // the whole warp takes part in the tensor-core evaluation
     float f[NIN], xin[NIN], y[NOUT];
     const double uu[5] = {q.dd, q.mm1, q.mm2, q.mm3, q.ee}, bb[3] = {q.b1, q.b2, q.b3};
     features(uu, bb, f);
@@ -508,20 +509,13 @@ sr_c2p_phase1_kernel(long long n, double gamma, double pfloor, const double* __r
     for (int k = 0; k < NIN; ++k) xin[k] = (f[k] - net.xm[k]) / net.xs[k];
     mlp_infer_warp(net, xin, y);
     guess = q.ee * (double)__expf(y[0]);
-    if (mode == 2 && valid) {
-      // FP32 iterations of the same scheme; the last iterate is kept even when the FP32
-      // test (relative 1e-6) is not met, since it is still closer than the network's value
-      float dq, pminq, lastq = (float)guess, pg[3];
-      athgpu::sr_nh_setup<float>((float)q.ee, (float)q.mm_sq, (float)q.bb_sq, (float)q.tt,
-                                 &dq, &pminq);
-      pg[0] = fmaxf((float)guess, pminq);
-      const int k = athgpu::sr_nh_loop<float>(
-          (float)gamma, (float)q.dd, (float)q.ee, (float)q.mm_sq, (float)q.bb_sq, (float)q.tt,
-          dq, pminq, pg, 0, 12, 1.0e-6f, true, &lastq);
-      it32 = k < 12 ? k + 1 : 12;
-      const float pr32 = k < 12 ? pg[(k + 1) % 3] : lastq;
-      if (isfinite(pr32) && pr32 > 0.0f) guess = (double)pr32;
-    }
+    if (mode == 2 && valid)  // FP32 iterations of the same scheme; the last iterate is kept
+      guess = athgpu::sr_refine_f32(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, guess, 12,
+                                    1.0e-6f, &it32);
+    if (!(guess > pfloor)) guess = pfloor;
+  } else if (mode == 3 && valid) {  // the mode-0 start refined in FP32
+    guess = athgpu::sr_refine_f32(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, pstd, 12,
+                                  1.0e-6f, &it32);
     if (!(guess > pfloor)) guess = pfloor;
   }
   double pg[3], last = guess, pr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -675,8 +669,9 @@ athgpu_status athgpu_sr_c2p_cells(long long n, double gamma, double pfloor, cons
   if (n < 0 || (n > 0 && (!cons || !bcc || !prim || !iters64)))
     return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: bad arguments");
   if (n >= (1LL << 31)) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: at most 2^31-1 cells");
-  if (mode < 0 || mode > 2) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: mode must be 0, 1 or 2");
-  if (mode > 0 && !params) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: mode needs parameters");
+  if (mode < 0 || mode > 3) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: mode must be 0..3");
+  if ((mode == 1 || mode == 2) && !params)
+    return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: mode needs parameters");
   if (!(gamma > 1.0)) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: gamma must exceed 1");
   if (phase1_iterations < 0 || phase1_iterations > MAXIT)
     return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: phase1_iterations must be in [0, 15]");

@@ -97,8 +97,21 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
     if (c->desc.relativistic) {
       SRFloors fp{c->desc.gamma, c->desc.dfloor, c->desc.pfloor, c->desc.sigma_max,
                   c->desc.beta_min, c->desc.gamma_max};
-      c2p_sr_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
-          m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk);
+      constexpr int REFINE = sizeof(Real) == 4;  // FP32 path: FP32-refined start
+      const int n1 = c->lc.sr_phase1 > 0 ? c->lc.sr_phase1 : (REFINE ? 5 : 7);
+      const long long ni = (long long)m.nb * m.nx1 * m.nx2 * m.nx3;
+      cudaMemsetAsync(c->c2p_qcount, 0, sizeof(unsigned), s);
+      c2p_sr_kernel<Real, KAHAN, REFINE><<<nblk(ni, 128), 128, 0, s>>>(
+          m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk,
+          1, n1, c->c2p_queue, c->c2p_qcount);
+      const long long g2 = nblk(ni, 128) < 2048 ? nblk(ni, 128) : 2048;
+      c2p_sr_kernel<Real, KAHAN, REFINE><<<g2, 128, 0, s>>>(
+          m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk,
+          2, 15, c->c2p_queue, c->c2p_qcount);
+      const long long ng = ((long long)m.ncell - (long long)m.nx1 * m.nx2 * m.nx3) * m.nb;
+      copy_ghost_prims_kernel<Real><<<nblk(ng, 256), 256, 0, s>>>(
+          m, wout, (Real*)c->r.bcc, (Real*)c->r.cce);
+      c->launches += 2;
     } else {
       c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
           m, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk);

@@ -29,7 +29,7 @@ OFF_YS = OFF_YM + NOUT
 NPARAM = OFF_YS + NOUT
 NTRAIN = OFF_XM
 
-MODE_PLAIN, MODE_LEARNED, MODE_LEARNED_FP32 = 0, 1, 2
+MODE_PLAIN, MODE_LEARNED, MODE_LEARNED_FP32, MODE_REFINED = 0, 1, 2, 3
 
 _vp, _ll, _ip = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int
 _SIG = {

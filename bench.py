@@ -305,10 +305,11 @@ def run_sr_kh(n, stream, net):
     Zone-cycles/s of the FP32 and FP64 SR stage paths (CUDA events, state resident), their
     relative L1 difference after SR_ACC_CYCLES cycles, and the con2prim start study: the
     conserved state of one cycle solved per cell from the previous cycle's pressure (the
-    stage's start) and from the network refined in FP32."""
+    reference's start, and the FP32 stage's start: that pressure refined in FP32) and from
+    the network refined in FP32."""
     import torch
     from athena_gb300 import pgen
-    from athena_gb300.learned_c2p import MODE_LEARNED_FP32, MODE_PLAIN
+    from athena_gb300.learned_c2p import MODE_LEARNED_FP32, MODE_PLAIN, MODE_REFINED
     from athena_gb300.mesh import MeshSpec
     from athena_gb300.runtime import StageUpdate
     nx, nb = (n,) * 3, (n // 32,) * 3
@@ -359,6 +360,7 @@ def run_sr_kh(n, stream, net):
     dc, db, dp = net.to_dev(cons), net.to_dev(bcc), net.to_dev(pprev)
     study = {"cells": int(cons.shape[0])}
     for name, mode, guess in (("previous_pressure", MODE_PLAIN, dp),
+                              ("previous_pressure_fp32_refined", MODE_REFINED, dp),
                               ("learned", MODE_LEARNED_FP32, dp)):
         ts = []
         for rep in range(4):

@@ -190,12 +190,13 @@ athgpu_status athgpu_mlp_infer(long long n, const float *params, const float *fe
 
 /* Newman-Hamlin root find per independent cell.  mode 0: start from pgas_guess[c] (the
  * reference's start) or from pfloor when pgas_guess is NULL; mode 1: start from the
- * network; mode 2: network start refined by at most 12 FP32 iterations of the same scheme.
+ * network; mode 2: network start refined by at most 12 FP32 iterations of the same scheme;
+ * mode 3: the mode-0 start refined the same way (no network; params may be NULL).
  * Two launches: loop indices [0, phase1_iterations) for every cell (0 = default: 7 in
  * mode 0, 4 in modes 1-2), then the cells still iterating, resumed exactly.  Mode 0 is the
- * reference's solve.  Modes 1-2 solve a cell again from the mode-0 start when the learned
- * start does not converge within the reference's 15 FP64 iterations, and then from the
- * learned attempt's last iterate (*fallbacks, may be NULL, counts cells that needed it).
+ * reference's solve.  Modes 1-3 solve a cell again from the mode-0 start when their start
+ * does not converge within the reference's 15 FP64 iterations, and then from that
+ * attempt's last iterate (*fallbacks, may be NULL, counts cells that needed it).
  * prim[n][5] as ConservedToPrimitiveNormal leaves it (zeros before the solve),
  * iters64[n] = FP64 loop passes over all attempts (-1 = not converged), iters32[n] (may
  * be NULL) = FP32 refinement passes.  Allocates a queue of 40 bytes per cell with
