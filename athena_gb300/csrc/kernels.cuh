@@ -683,12 +683,18 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const double* dx1f = m.dx1f + (i64)b * m.nc1;
   const double* dx2f = m.dx2f + (i64)b * m.nc2;
   const double* dx3f = m.dx3f + (i64)b * m.nc3;
-  __shared__ double q[3];
+  __shared__ double q[3], ql[6];
   if (threadIdx.x < 3) {
     const double wght = beta * clk->dt;
     const double area = threadIdx.x == 0 ? dx2f[m.js] * dx3f[m.ks]
                       : threadIdx.x == 1 ? dx1f[m.is] * dx3f[m.ks] : dx1f[m.is] * dx2f[m.js];
     q[threadIdx.x] = wght / area;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {  // FP32 path: the (wght/area)*len products of the block
+    const double lq[6] = {dx3f[m.ks], dx2f[m.js], dx3f[m.ks], dx1f[m.is], dx2f[m.js],
+                          dx1f[m.is]};
+    ql[threadIdx.x] = q[threadIdx.x / 2] * lq[threadIdx.x];
   }
   __syncthreads();
   const int n1 = m.nx1 + 1, n2 = m.nx2 + 1, n3 = m.nx3 + 1;
@@ -702,8 +708,8 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const bool f3 = i <= m.ie && j <= m.je;
   const double l1 = dx1f[m.is], l2 = dx2f[m.js], l3 = dx3f[m.ks];
   const bool exact = sizeof(Real) == 8;
-  auto term = [&](double qd, double len, double ep, double em) -> double {
-    return exact ? qd * (len * ep - len * em) : (qd * len) * (ep - em);
+  auto term = [&](double qd, double len, double qlen, double ep, double em) -> double {
+    return exact ? qd * (len * ep - len * em) : qlen * (ep - em);
   };
   // the shared edges, each read once (and only where a face of this thread uses it)
   const double e1c = (f2 || f3) ? edge_value<Real, 0>(m, e1, b, k, j, i) : 0.0;
@@ -712,22 +718,22 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   if (f1) {
     const i64 o = f1idx(m, b, k, j, i);
     double v = b1in[o];
-    v -= term(q[0], l3, edge_value<Real, 2>(m, e3, b, k, j + 1, i), e3c);
-    v += term(q[0], l2, edge_value<Real, 1>(m, e2, b, k + 1, j, i), e2c);
+    v -= term(q[0], l3, ql[0], edge_value<Real, 2>(m, e3, b, k, j + 1, i), e3c);
+    v += term(q[0], l2, ql[1], edge_value<Real, 1>(m, e2, b, k + 1, j, i), e2c);
     b1out[o] = v;
   }
   if (f2) {
     const i64 o = f2idx(m, b, k, j, i);
     double v = b2in[o];
-    v += term(q[1], l3, edge_value<Real, 2>(m, e3, b, k, j, i + 1), e3c);
-    v -= term(q[1], l1, edge_value<Real, 0>(m, e1, b, k + 1, j, i), e1c);
+    v += term(q[1], l3, ql[2], edge_value<Real, 2>(m, e3, b, k, j, i + 1), e3c);
+    v -= term(q[1], l1, ql[3], edge_value<Real, 0>(m, e1, b, k + 1, j, i), e1c);
     b2out[o] = v;
   }
   if (f3) {
     const i64 o = f3idx(m, b, k, j, i);
     double v = b3in[o];
-    v -= term(q[2], l2, edge_value<Real, 1>(m, e2, b, k, j, i + 1), e2c);
-    v += term(q[2], l1, edge_value<Real, 0>(m, e1, b, k, j + 1, i), e1c);
+    v -= term(q[2], l2, ql[4], edge_value<Real, 1>(m, e2, b, k, j, i + 1), e2c);
+    v += term(q[2], l1, ql[5], edge_value<Real, 0>(m, e1, b, k, j + 1, i), e1c);
     b3out[o] = v;
   }
 }

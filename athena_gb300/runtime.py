@@ -169,13 +169,21 @@ class StageUpdate:
         w = np.ascontiguousarray(w, dtype=np.float64)
         _check(load_library().athgpu_upload_prim(self.h, _dp(w)), "athgpu_upload_prim")
 
-    def state(self):
+    def state(self, out=None):
+        """Download (u, b1, b2, b3); `out` = four C-contiguous float64 arrays of those
+        shapes to fill (pinned host memory makes the copy a direct DMA)."""
         m = self.mesh
-        u = np.zeros((m.nblocks, 5) + m.cell_shape)
-        b = [np.zeros((m.nblocks,) + s) for s in m.face_shapes]
-        _check(load_library().athgpu_download_state(self.h, _dp(u), *[_dp(x) for x in b]),
-               "athgpu_download_state")
-        return u, b[0], b[1], b[2]
+        shapes = [(m.nblocks, 5) + m.cell_shape] + [(m.nblocks,) + s for s in m.face_shapes]
+        if out is None:
+            out = [np.zeros(sh) for sh in shapes]
+        else:
+            for a, sh in zip(out, shapes):
+                if a.shape != sh or a.dtype != np.float64 or not a.flags.c_contiguous:
+                    raise ValueError("state(out=...) needs C-contiguous float64 %s" % (sh,))
+        u, b1, b2, b3 = out
+        _check(load_library().athgpu_download_state(self.h, _dp(u), _dp(b1), _dp(b2),
+                                                    _dp(b3)), "athgpu_download_state")
+        return u, b1, b2, b3
 
     def prim(self):
         m = self.mesh
