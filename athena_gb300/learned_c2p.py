@@ -35,6 +35,7 @@ _vp, _ll, _ip = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int
 _SIG = {
     "athgpu_sr_features": ([_ll, _vp, _vp, _vp, _vp], _ip),
     "athgpu_mlp_infer": ([_ll, _vp, _vp, _vp, _vp], _ip),
+    "athgpu_mlp_infer_tc": ([_ll, _vp, _vp, _vp, _vp], _ip),
     "athgpu_sr_c2p_cells": ([_ll, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _ip,
                              _ip, _vp, _vp, _vp, _vp, _vp], _ip),
     "athgpu_mlp_loss_grad": ([_vp, _vp, _vp, _ip, _vp, _vp, _vp], _ip),
@@ -140,6 +141,14 @@ class LearnedC2P:
                                device=self.dev)
         _check(self.lib.athgpu_mlp_infer(feats.shape[0], _ptr(self.params), _ptr(feats),
                                          _ptr(out), _stream()), "athgpu_mlp_infer")
+        return out
+
+    def infer_tc(self, feats):
+        """infer() on the tcgen05 tensor-core path (tensor memory accumulators)."""
+        out = self.torch.empty((feats.shape[0], NOUT), dtype=self.torch.float32,
+                               device=self.dev)
+        _check(self.lib.athgpu_mlp_infer_tc(feats.shape[0], _ptr(self.params), _ptr(feats),
+                                            _ptr(out), _stream()), "athgpu_mlp_infer_tc")
         return out
 
     def solver_pairs(self, n, seed):

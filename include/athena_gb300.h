@@ -188,6 +188,13 @@ athgpu_status athgpu_sr_features(long long n, const double *cons, const double *
 athgpu_status athgpu_mlp_infer(long long n, const float *params, const float *features,
                                float *out, void *stream);
 
+/* The same network on the fifth-generation tensor cores: persistent CTAs of 128 threads
+ * evaluate 128-row tiles with tcgen05.mma (BF16 operands in shared memory, FP32
+ * accumulators in tensor memory).  Synchronous; ATHGPU_ERR_CUDA if a tensor-core wait
+ * timed out (the outputs are then NaN). */
+athgpu_status athgpu_mlp_infer_tc(long long n, const float *params, const float *features,
+                                  float *out, void *stream);
+
 /* Newman-Hamlin root find per independent cell.  mode 0: start from pgas_guess[c] (the
  * reference's start) or from pfloor when pgas_guess is NULL; mode 1: start from the
  * network; mode 2: network start refined by at most 12 FP32 iterations of the same scheme;
