@@ -401,241 +401,6 @@ __device__ void mlp_infer_warp(const SmemNet& s, const float* xin, float* yout) 
 }
 
 // ---------------------------------------------------------------------------------------
-// Per-cell SR con2prim on independent cells: the Newman-Hamlin root find of
-// ConservedToPrimitiveNormal (adiabatic_mhd_sr.cpp:404-522) from three kinds of start.
-// mode 0: pgas_guess[c] (the reference's start, max(previous pressure, floor),
-// adiabatic_mhd_sr.cpp:143-154), or the floor when pgas_guess is NULL; mode 1: the
-// learned start; mode 2: the learned start refined by FP32 iterations of the same scheme.
-//
-// Warp-coherent two-phase schedule: the iteration count varies from cell to cell and a
-// warp runs as long as its slowest lane, so phase 1 runs loop indices [0, n1) for every
-// cell and appends each cell still iterating to a queue together with its whole solver
-// state (pgas[3] and the loop index: the iteration resumes exactly where it stopped);
-// phase 2 finishes the queued cells in a grid-stride loop.  Mode 0 is then the reference's
-// solve, index for index.  Modes 1-2 add the fallback: a learned start that does not
-// converge within the reference's 15 iterations is solved again from the mode-0 start,
-// and if that fails too, from the last iterate of the learned attempt.
-constexpr int MAXIT = 15;
-constexpr double TOL = 1.0e-12;
-
-struct Queue {
-  long long* cell;
-  int* state;        // loop index | attempt << 8 | FP64 passes so far << 16
-  double* p;         // pgas[3] per entry
-  unsigned* count;
-};
-
-struct Cell {
-  double dd, ee, mm1, mm2, mm3, mm_sq, b1, b2, b3, bb_sq, tt, d, pgas_min;
-};
-
-__device__ __forceinline__ Cell load_cell(const double* __restrict__ cons,
-                                          const double* __restrict__ bcc, long long c,
-                                          bool valid) {
-  Cell q;
-  double u[5] = {1.0, 0.0, 0.0, 0.0, 2.0}, b[3] = {0.0, 0.0, 0.0};
-  if (valid) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) u[v] = cons[c * 5 + v];
-#pragma unroll
-    for (int v = 0; v < 3; ++v) b[v] = bcc[c * 3 + v];
-  }
-  q.dd = u[0]; q.mm1 = u[1]; q.mm2 = u[2]; q.mm3 = u[3]; q.ee = u[4];
-  q.b1 = b[0]; q.b2 = b[1]; q.b3 = b[2];
-  // operand order of adiabatic_mhd_sr.cpp:108-123
-  q.mm_sq = q.mm1 * q.mm1 + q.mm2 * q.mm2 + q.mm3 * q.mm3;
-  q.bb_sq = q.b1 * q.b1 + q.b2 * q.b2 + q.b3 * q.b3;
-  q.tt = q.mm1 * q.b1 + q.mm2 * q.b2 + q.mm3 * q.b3;
-  athgpu::sr_nh_setup<double>(q.ee, q.mm_sq, q.bb_sq, q.tt, &q.d, &q.pgas_min);
-  return q;
-}
-
-__device__ __forceinline__ int run64(const Cell& q, double gamma, double* pgas, int n0, int n1,
-                                     double* last) {
-  return athgpu::sr_nh_loop<double>(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, q.d, q.pgas_min,
-                                    pgas, n0, n1, TOL, false, last);
-}
-
-__device__ __forceinline__ bool finish64(const Cell& q, double p, double* prim) {
-  double gl, pm;
-  return athgpu::sr_nh_finish<double>(q.dd, q.ee, q.mm_sq, q.mm1, q.mm2, q.mm3, q.bb_sq, q.b1,
-                                      q.b2, q.b3, q.tt, q.d, p, prim, &gl, &pm);
-}
-
-__device__ __forceinline__ void store(double* __restrict__ prim, long long c, const double* pr) {
-#pragma unroll
-  for (int v = 0; v < 5; ++v) prim[c * 5 + v] = pr[v];
-}
-
-// The fallback chain of modes 1-2 after the learned attempt failed: the mode-0 start,
-// then the learned attempt's last iterate.  Returns total FP64 passes (<0: not converged).
-__device__ int fallback_chain(const Cell& q, double gamma, double pstd, double plast,
-                              double* pr, int passes) {
-  const double starts[2] = {pstd, plast};
-#pragma unroll 1
-  for (int a = 0; a < 2; ++a) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) pr[v] = 0.0;
-    double pg[3], last = 0.0;
-    pg[0] = fmax(starts[a], q.pgas_min);
-    const int n = run64(q, gamma, pg, 0, MAXIT, &last);
-    passes += n < MAXIT ? n + 1 : MAXIT;
-    if (n < MAXIT && finish64(q, pg[(n + 1) % 3], pr)) return passes;
-  }
-  return -passes;
-}
-
-__global__ void __launch_bounds__(128)
-sr_c2p_phase1_kernel(long long n, double gamma, double pfloor, const double* __restrict__ cons,
-                     const double* __restrict__ bcc, const double* __restrict__ pgas_guess,
-                     const float* __restrict__ params, int mode, int n1,
-                     double* __restrict__ prim, int* __restrict__ iters64,
-                     int* __restrict__ iters32, int* __restrict__ fallbacks, Queue qu) {
-  __shared__ SmemNet net;
-  const bool use_net = mode == 1 || mode == 2;
-  if (use_net) {
-    load_net(params, net);
-    __syncthreads();
-  }
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = c < n;
-  const Cell q = load_cell(cons, bcc, c, valid);
-  const double pstd = (valid && pgas_guess) ? pgas_guess[c] : pfloor;
-  double guess = pstd;
-  int it32 = 0;
-  if (use_net) {  // the whole warp takes part in the tensor-core evaluation
-    float f[NIN], xin[NIN], y[NOUT];
-    const double uu[5] = {q.dd, q.mm1, q.mm2, q.mm3, q.ee}, bb[3] = {q.b1, q.b2, q.b3};
-    features(uu, bb, f);
-#pragma unroll
-    for (int k = 0; k < NIN; ++k) xin[k] = (f[k] - net.xm[k]) / net.xs[k];
-    mlp_infer_warp(net, xin, y);
-    guess = q.ee * (double)__expf(y[0]);
-    if (mode == 2 && valid)  // FP32 iterations of the same scheme; the last iterate is kept
-      guess = athgpu::sr_refine_f32(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, guess, 12,
-                                    1.0e-6f, &it32);
-    if (!(guess > pfloor)) guess = pfloor;
-  } else if (mode == 3 && valid) {  // the mode-0 start refined in FP32
-    guess = athgpu::sr_refine_f32(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, pstd, 12,
-                                  1.0e-6f, &it32);
-    if (!(guess > pfloor)) guess = pfloor;
-  }
-  double pg[3], last = guess, pr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  bool enqueue = false;
-  int attempt = 0, passes = 0, nstop = 0;
-  if (valid) {
-    pg[0] = fmax(guess, q.pgas_min);
-    const int k = run64(q, gamma, pg, 0, n1, &last);
-    if (k < n1) {  // converged in phase 1
-      passes = k + 1;
-      if (finish64(q, pg[(k + 1) % 3], pr)) {
-        store(prim, c, pr);
-        iters64[c] = passes;
-      } else if (mode == 0) {
-        store(prim, c, pr);
-        iters64[c] = -1;
-      } else {
-        enqueue = true;   // go straight to the fallback chain
-        attempt = 1;
-      }
-    } else if (n1 >= MAXIT) {
-      passes = MAXIT;
-      if (mode == 0) {
-        store(prim, c, pr);
-        iters64[c] = -1;
-      } else {
-        enqueue = true;
-        attempt = 1;
-      }
-    } else {
-      passes = n1;
-      nstop = n1;
-      enqueue = true;
-    }
-    if (iters32) iters32[c] = it32;
-  }
-  // warp-aggregated append to the queue
-  const unsigned mask = __ballot_sync(0xffffffffu, enqueue);
-  if (mask) {
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(qu.count, (unsigned)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (enqueue) {
-      const unsigned slot = base + __popc(mask & ((1u << lane) - 1u));
-      qu.cell[slot] = c;
-      qu.state[slot] = nstop | (attempt << 8) | (passes << 16);
-      qu.p[3 * (long long)slot + 0] = attempt ? last : pg[0];
-      qu.p[3 * (long long)slot + 1] = pg[1];
-      qu.p[3 * (long long)slot + 2] = pg[2];
-      if (attempt && fallbacks) atomicAdd(fallbacks, 1);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(128)
-sr_c2p_phase2_kernel(double gamma, double pfloor, const double* __restrict__ cons,
-                     const double* __restrict__ bcc, const double* __restrict__ pgas_guess,
-                     int mode, double* __restrict__ prim, int* __restrict__ iters64,
-                     int* __restrict__ fallbacks, Queue qu) {
-  const unsigned total = *qu.count;
-  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += gridDim.x * blockDim.x) {
-    const long long c = qu.cell[e];
-    const int st = qu.state[e];
-    int n0 = st & 0xff, attempt = (st >> 8) & 0xff, passes = st >> 16;
-    const Cell q = load_cell(cons, bcc, c, true);
-    const double pstd = pgas_guess ? pgas_guess[c] : pfloor;
-    double pr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    double pg[3] = {qu.p[3 * (long long)e], qu.p[3 * (long long)e + 1],
-                    qu.p[3 * (long long)e + 2]};
-    double last = pg[0];
-    int result;
-    if (attempt == 0) {  // resume the first attempt at loop index n0
-      const int k = run64(q, gamma, pg, n0, MAXIT, &last);
-      passes += k < MAXIT ? k - n0 + 1 : MAXIT - n0;
-      if (k < MAXIT && finish64(q, pg[(k + 1) % 3], pr)) {
-        result = passes;
-      } else if (mode == 0) {
-        result = -1;
-      } else {
-        if (fallbacks) atomicAdd(fallbacks, 1);
-        result = fallback_chain(q, gamma, pstd, last, pr, passes);
-      }
-    } else {
-      result = fallback_chain(q, gamma, pstd, last, pr, passes);
-    }
-    store(prim, c, pr);
-    iters64[c] = result > 0 ? result : -1;
-  }
-}
-
-// network outputs for n feature rows (raw features, standardized inside)
-__global__ void __launch_bounds__(128)
-mlp_infer_kernel(long long n, const float* __restrict__ params, const float* __restrict__ fx,
-                 float* __restrict__ out) {
-  __shared__ SmemNet net;
-  load_net(params, net);
-  __syncthreads();
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  float xin[NIN], y[NOUT];
-#pragma unroll
-  for (int k = 0; k < NIN; ++k) xin[k] = c < n ? (fx[c * NIN + k] - net.xm[k]) / net.xs[k] : 0.0f;
-  mlp_infer_warp(net, xin, y);
-  if (c < n) {
-#pragma unroll
-    for (int q = 0; q < NOUT; ++q) out[c * NOUT + q] = y[q];
-  }
-}
-
-__global__ void sr_features_kernel(long long n, const double* __restrict__ cons,
-                                   const double* __restrict__ bcc, float* __restrict__ fx) {
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  features(cons + c * 5, bcc + c * 3, fx + c * NIN);
-}
-
 // ---------------------------------------------------------------------------------------
 // tcgen05 evaluation of the network (tc_mlp.cuh): operands and TMEM bookkeeping of a CTA.
 struct TcNet {
@@ -802,6 +567,259 @@ __device__ void tc_infer_tile(TcNet& s, const float* xin, float* y, uint32_t& ph
 // 228 KB, five do not
 constexpr int TC_SMEM_PAD = 21 * 1024;
 
+// Per-cell SR con2prim on independent cells: the Newman-Hamlin root find of
+// ConservedToPrimitiveNormal (adiabatic_mhd_sr.cpp:404-522) from three kinds of start.
+// mode 0: pgas_guess[c] (the reference's start, max(previous pressure, floor),
+// adiabatic_mhd_sr.cpp:143-154), or the floor when pgas_guess is NULL; mode 1: the
+// learned start; mode 2: the learned start refined by FP32 iterations of the same scheme.
+//
+// Warp-coherent two-phase schedule: the iteration count varies from cell to cell and a
+// warp runs as long as its slowest lane, so phase 1 runs loop indices [0, n1) for every
+// cell and appends each cell still iterating to a queue together with its whole solver
+// state (pgas[3] and the loop index: the iteration resumes exactly where it stopped);
+// phase 2 finishes the queued cells in a grid-stride loop.  Mode 0 is then the reference's
+// solve, index for index.  Modes 1-2 add the fallback: a learned start that does not
+// converge within the reference's 15 iterations is solved again from the mode-0 start,
+// and if that fails too, from the last iterate of the learned attempt.
+constexpr int MAXIT = 15;
+constexpr double TOL = 1.0e-12;
+
+struct Queue {
+  long long* cell;
+  int* state;        // loop index | attempt << 8 | FP64 passes so far << 16
+  double* p;         // pgas[3] per entry
+  unsigned* count;
+};
+
+struct Cell {
+  double dd, ee, mm1, mm2, mm3, mm_sq, b1, b2, b3, bb_sq, tt, d, pgas_min;
+};
+
+__device__ __forceinline__ Cell load_cell(const double* __restrict__ cons,
+                                          const double* __restrict__ bcc, long long c,
+                                          bool valid) {
+  Cell q;
+  double u[5] = {1.0, 0.0, 0.0, 0.0, 2.0}, b[3] = {0.0, 0.0, 0.0};
+  if (valid) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = cons[c * 5 + v];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) b[v] = bcc[c * 3 + v];
+  }
+  q.dd = u[0]; q.mm1 = u[1]; q.mm2 = u[2]; q.mm3 = u[3]; q.ee = u[4];
+  q.b1 = b[0]; q.b2 = b[1]; q.b3 = b[2];
+  // operand order of adiabatic_mhd_sr.cpp:108-123
+  q.mm_sq = q.mm1 * q.mm1 + q.mm2 * q.mm2 + q.mm3 * q.mm3;
+  q.bb_sq = q.b1 * q.b1 + q.b2 * q.b2 + q.b3 * q.b3;
+  q.tt = q.mm1 * q.b1 + q.mm2 * q.b2 + q.mm3 * q.b3;
+  athgpu::sr_nh_setup<double>(q.ee, q.mm_sq, q.bb_sq, q.tt, &q.d, &q.pgas_min);
+  return q;
+}
+
+__device__ __forceinline__ int run64(const Cell& q, double gamma, double* pgas, int n0, int n1,
+                                     double* last) {
+  return athgpu::sr_nh_loop<double>(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, q.d, q.pgas_min,
+                                    pgas, n0, n1, TOL, false, last);
+}
+
+__device__ __forceinline__ bool finish64(const Cell& q, double p, double* prim) {
+  double gl, pm;
+  return athgpu::sr_nh_finish<double>(q.dd, q.ee, q.mm_sq, q.mm1, q.mm2, q.mm3, q.bb_sq, q.b1,
+                                      q.b2, q.b3, q.tt, q.d, p, prim, &gl, &pm);
+}
+
+__device__ __forceinline__ void store(double* __restrict__ prim, long long c, const double* pr) {
+#pragma unroll
+  for (int v = 0; v < 5; ++v) prim[c * 5 + v] = pr[v];
+}
+
+// The fallback chain of modes 1-2 after the learned attempt failed: the mode-0 start,
+// then the learned attempt's last iterate.  Returns total FP64 passes (<0: not converged).
+__device__ int fallback_chain(const Cell& q, double gamma, double pstd, double plast,
+                              double* pr, int passes) {
+  const double starts[2] = {pstd, plast};
+#pragma unroll 1
+  for (int a = 0; a < 2; ++a) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) pr[v] = 0.0;
+    double pg[3], last = 0.0;
+    pg[0] = fmax(starts[a], q.pgas_min);
+    const int n = run64(q, gamma, pg, 0, MAXIT, &last);
+    passes += n < MAXIT ? n + 1 : MAXIT;
+    if (n < MAXIT && finish64(q, pg[(n + 1) % 3], pr)) return passes;
+  }
+  return -passes;
+}
+
+template <bool TC>
+__global__ void __launch_bounds__(128)
+sr_c2p_phase1_kernel(long long n, double gamma, double pfloor, const double* __restrict__ cons,
+                     const double* __restrict__ bcc, const double* __restrict__ pgas_guess,
+                     const float* __restrict__ params, int mode, int n1,
+                     double* __restrict__ prim, int* __restrict__ iters64,
+                     int* __restrict__ iters32, int* __restrict__ fallbacks, Queue qu,
+                     int* __restrict__ tc_err) {
+  // the network's operands: SmemNet for the warp-level mma.sync path, TcNet for tcgen05
+  extern __shared__ __align__(128) unsigned char phase1_smem[];
+  SmemNet& net = *reinterpret_cast<SmemNet*>(phase1_smem);
+  TcNet& tnet = *reinterpret_cast<TcNet*>(phase1_smem);
+  const bool use_net = mode == 1 || mode == 2;
+  if (use_net) {
+    if (TC) {
+      tc_setup(params, tnet);
+    } else {
+      load_net(params, net);
+      __syncthreads();
+    }
+  }
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = c < n;
+  const Cell q = load_cell(cons, bcc, c, valid);
+  const double pstd = (valid && pgas_guess) ? pgas_guess[c] : pfloor;
+  double guess = pstd;
+  int it32 = 0;
+  if (use_net) {  // the whole warp takes part in the tensor-core evaluation
+    float f[NIN], xin[NIN], y[NOUT];
+    const double uu[5] = {q.dd, q.mm1, q.mm2, q.mm3, q.ee}, bb[3] = {q.b1, q.b2, q.b3};
+    features(uu, bb, f);
+    if (TC) {
+#pragma unroll
+      for (int k = 0; k < NIN; ++k) xin[k] = (f[k] - tnet.xm[k]) / tnet.xs[k];
+      uint32_t ph = 0;
+      tc_infer_tile(tnet, xin, y, ph, tc_err);  // the CTA's 128 cells on tcgen05
+      tc_teardown(tnet);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NIN; ++k) xin[k] = (f[k] - net.xm[k]) / net.xs[k];
+      mlp_infer_warp(net, xin, y);
+    }
+    guess = q.ee * (double)__expf(y[0]);
+    if (mode == 2 && valid)  // FP32 iterations of the same scheme; the last iterate is kept
+      guess = athgpu::sr_refine_f32(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, guess, 12,
+                                    1.0e-6f, &it32);
+    if (!(guess > pfloor)) guess = pfloor;
+  } else if (mode == 3 && valid) {  // the mode-0 start refined in FP32
+    guess = athgpu::sr_refine_f32(gamma, q.dd, q.ee, q.mm_sq, q.bb_sq, q.tt, pstd, 12,
+                                  1.0e-6f, &it32);
+    if (!(guess > pfloor)) guess = pfloor;
+  }
+  double pg[3], last = guess, pr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  bool enqueue = false;
+  int attempt = 0, passes = 0, nstop = 0;
+  if (valid) {
+    pg[0] = fmax(guess, q.pgas_min);
+    const int k = run64(q, gamma, pg, 0, n1, &last);
+    if (k < n1) {  // converged in phase 1
+      passes = k + 1;
+      if (finish64(q, pg[(k + 1) % 3], pr)) {
+        store(prim, c, pr);
+        iters64[c] = passes;
+      } else if (mode == 0) {
+        store(prim, c, pr);
+        iters64[c] = -1;
+      } else {
+        enqueue = true;   // go straight to the fallback chain
+        attempt = 1;
+      }
+    } else if (n1 >= MAXIT) {
+      passes = MAXIT;
+      if (mode == 0) {
+        store(prim, c, pr);
+        iters64[c] = -1;
+      } else {
+        enqueue = true;
+        attempt = 1;
+      }
+    } else {
+      passes = n1;
+      nstop = n1;
+      enqueue = true;
+    }
+    if (iters32) iters32[c] = it32;
+  }
+  // warp-aggregated append to the queue
+  const unsigned mask = __ballot_sync(0xffffffffu, enqueue);
+  if (mask) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(qu.count, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (enqueue) {
+      const unsigned slot = base + __popc(mask & ((1u << lane) - 1u));
+      qu.cell[slot] = c;
+      qu.state[slot] = nstop | (attempt << 8) | (passes << 16);
+      qu.p[3 * (long long)slot + 0] = attempt ? last : pg[0];
+      qu.p[3 * (long long)slot + 1] = pg[1];
+      qu.p[3 * (long long)slot + 2] = pg[2];
+      if (attempt && fallbacks) atomicAdd(fallbacks, 1);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128)
+sr_c2p_phase2_kernel(double gamma, double pfloor, const double* __restrict__ cons,
+                     const double* __restrict__ bcc, const double* __restrict__ pgas_guess,
+                     int mode, double* __restrict__ prim, int* __restrict__ iters64,
+                     int* __restrict__ fallbacks, Queue qu) {
+  const unsigned total = *qu.count;
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += gridDim.x * blockDim.x) {
+    const long long c = qu.cell[e];
+    const int st = qu.state[e];
+    int n0 = st & 0xff, attempt = (st >> 8) & 0xff, passes = st >> 16;
+    const Cell q = load_cell(cons, bcc, c, true);
+    const double pstd = pgas_guess ? pgas_guess[c] : pfloor;
+    double pr[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    double pg[3] = {qu.p[3 * (long long)e], qu.p[3 * (long long)e + 1],
+                    qu.p[3 * (long long)e + 2]};
+    double last = pg[0];
+    int result;
+    if (attempt == 0) {  // resume the first attempt at loop index n0
+      const int k = run64(q, gamma, pg, n0, MAXIT, &last);
+      passes += k < MAXIT ? k - n0 + 1 : MAXIT - n0;
+      if (k < MAXIT && finish64(q, pg[(k + 1) % 3], pr)) {
+        result = passes;
+      } else if (mode == 0) {
+        result = -1;
+      } else {
+        if (fallbacks) atomicAdd(fallbacks, 1);
+        result = fallback_chain(q, gamma, pstd, last, pr, passes);
+      }
+    } else {
+      result = fallback_chain(q, gamma, pstd, last, pr, passes);
+    }
+    store(prim, c, pr);
+    iters64[c] = result > 0 ? result : -1;
+  }
+}
+
+// network outputs for n feature rows (raw features, standardized inside)
+__global__ void __launch_bounds__(128)
+mlp_infer_kernel(long long n, const float* __restrict__ params, const float* __restrict__ fx,
+                 float* __restrict__ out) {
+  __shared__ SmemNet net;
+  load_net(params, net);
+  __syncthreads();
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float xin[NIN], y[NOUT];
+#pragma unroll
+  for (int k = 0; k < NIN; ++k) xin[k] = c < n ? (fx[c * NIN + k] - net.xm[k]) / net.xs[k] : 0.0f;
+  mlp_infer_warp(net, xin, y);
+  if (c < n) {
+#pragma unroll
+    for (int q = 0; q < NOUT; ++q) out[c * NOUT + q] = y[q];
+  }
+}
+
+__global__ void sr_features_kernel(long long n, const double* __restrict__ cons,
+                                   const double* __restrict__ bcc, float* __restrict__ fx) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  features(cons + c * 5, bcc + c * 3, fx + c * NIN);
+}
+
+
 // network outputs for n feature rows on the tcgen05 path: persistent CTAs of 128 threads
 // over 128-row tiles
 __global__ void __launch_bounds__(128)
@@ -889,6 +907,8 @@ athgpu_status athgpu_sr_c2p_cells(long long n, double gamma, double pfloor, cons
   if (n < 0 || (n > 0 && (!cons || !bcc || !prim || !iters64)))
     return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: bad arguments");
   if (n >= (1LL << 31)) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: at most 2^31-1 cells");
+  const bool warp_mma = (mode & ATHGPU_C2P_WARP_MMA) != 0;
+  mode &= ~ATHGPU_C2P_WARP_MMA;
   if (mode < 0 || mode > 3) return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: mode must be 0..3");
   if ((mode == 1 || mode == 2) && !params)
     return fail(ATHGPU_ERR_ARG, "sr_c2p_cells: mode needs parameters");
@@ -905,9 +925,22 @@ athgpu_status athgpu_sr_c2p_cells(long long n, double gamma, double pfloor, cons
   CKE(cudaMallocAsync((void**)&qu.p, cap * 3 * sizeof(double), s));
   CKE(cudaMallocAsync((void**)&qu.count, sizeof(unsigned), s));
   CKE(cudaMemsetAsync(qu.count, 0, sizeof(unsigned), s));
-  sr_c2p_phase1_kernel<<<grid_of(n, 128), 128, 0, s>>>(n, gamma, pfloor, cons, bcc, pgas_guess,
-                                                       params, mode, n1, prim, iters64,
-                                                       iters32, fallbacks, qu);
+  int* tc_err;
+  CKE(cudaMallocAsync((void**)&tc_err, sizeof(int), s));
+  CKE(cudaMemsetAsync(tc_err, 0, sizeof(int), s));
+  const bool net = mode == 1 || mode == 2;
+  if (net && !warp_mma) {  // tcgen05 network (tensor memory), four CTAs per SM at most
+    const int smem = (int)sizeof(TcNet) + TC_SMEM_PAD;
+    CKE(cudaFuncSetAttribute(sr_c2p_phase1_kernel<true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    sr_c2p_phase1_kernel<true><<<grid_of(n, 128), 128, smem, s>>>(
+        n, gamma, pfloor, cons, bcc, pgas_guess, params, mode, n1, prim, iters64, iters32,
+        fallbacks, qu, tc_err);
+  } else {
+    sr_c2p_phase1_kernel<false><<<grid_of(n, 128), 128, net ? (int)sizeof(SmemNet) : 0, s>>>(
+        n, gamma, pfloor, cons, bcc, pgas_guess, params, mode, n1, prim, iters64, iters32,
+        fallbacks, qu, tc_err);
+  }
   int dev = 0, sms = 0;
   CKE(cudaGetDevice(&dev));
   CKE(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -920,6 +953,11 @@ athgpu_status athgpu_sr_c2p_cells(long long n, double gamma, double pfloor, cons
   CKE(cudaFreeAsync(qu.state, s));
   CKE(cudaFreeAsync(qu.p, s));
   CKE(cudaFreeAsync(qu.count, s));
+  int herr = 0;
+  CKE(cudaMemcpyAsync(&herr, tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CKE(cudaFreeAsync(tc_err, s));
+  CKE(cudaStreamSynchronize(s));
+  if (herr) return fail(ATHGPU_ERR_CUDA, "sr_c2p_cells: tensor-core wait timed out");
   return ATHGPU_OK;
 }
 

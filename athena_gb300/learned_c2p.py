@@ -30,6 +30,7 @@ NPARAM = OFF_YS + NOUT
 NTRAIN = OFF_XM
 
 MODE_PLAIN, MODE_LEARNED, MODE_LEARNED_FP32, MODE_REFINED = 0, 1, 2, 3
+WARP_MMA = 0x100   # or into a mode: the network on warp-level mma.sync instead of tcgen05
 
 _vp, _ll, _ip = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int
 _SIG = {

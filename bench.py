@@ -251,11 +251,12 @@ def run_learned_c2p(reps=5):
     factor in [1,10], sigma in [1e-2,1e2], rho in [1e-4,1], p/rho in [1e-3,10], all
     log-uniform, isotropic v and B).  The network is trained here on 2^20 solver-made
     pairs; the plain solve starts from the pressure floor (an isolated cell has no
-    previous pressure), the learned one from the BF16 network refined in FP32, both
-    finished by the reference's FP64 iteration (two warp-coherent launches each)."""
+    previous pressure), the learned one from the BF16 network (tcgen05 tensor cores, and
+    for comparison warp-level mma.sync) refined in FP32, both finished by the reference's
+    FP64 iteration (two warp-coherent launches each)."""
     import torch
     from athena_gb300 import pgen
-    from athena_gb300.learned_c2p import LearnedC2P, MODE_LEARNED_FP32, MODE_PLAIN
+    from athena_gb300.learned_c2p import LearnedC2P, MODE_LEARNED_FP32, MODE_PLAIN, WARP_MMA
     net = LearnedC2P(4.0 / 3.0, seed=0)
     t0 = time.perf_counter()
     feats, targ = net.solver_pairs(1 << 20, 101)
@@ -273,7 +274,8 @@ def run_learned_c2p(reps=5):
                         "seconds": t_train, "loss_first": float(hist[:10].mean()),
                         "loss_last": float(hist[-100:].mean())}}
     stream = torch.cuda.current_stream()
-    for name, mode in (("plain", MODE_PLAIN), ("learned", MODE_LEARNED_FP32)):
+    for name, mode in (("plain", MODE_PLAIN), ("learned", MODE_LEARNED_FP32),
+                       ("learned_warp_mma", MODE_LEARNED_FP32 | WARP_MMA)):
         ts = []
         for rep in range(reps + 2):
             s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -288,7 +290,7 @@ def run_learned_c2p(reps=5):
         out[name] = {"ms": ms, "cells_per_s": LEARNED_CELLS / (ms * 1e-3),
                      "mean_fp64_passes": float(it[it >= 0].mean()),
                      "unconverged": int((it < 0).sum())}
-        if mode == MODE_LEARNED_FP32:
+        if mode & 0xff == MODE_LEARNED_FP32:
             out[name]["mean_fp32_passes"] = float(it32.float().mean().item())
             out[name]["fallbacks"] = fb
     out["speedup"] = out["plain"]["ms"] / out["learned"]["ms"]

@@ -195,6 +195,10 @@ athgpu_status athgpu_mlp_infer(long long n, const float *params, const float *fe
 athgpu_status athgpu_mlp_infer_tc(long long n, const float *params, const float *features,
                                   float *out, void *stream);
 
+/* Flag or-ed into athgpu_sr_c2p_cells' mode: evaluate the network with warp-level
+ * mma.sync tiles instead of the default tcgen05 path. */
+#define ATHGPU_C2P_WARP_MMA 0x100
+
 /* Newman-Hamlin root find per independent cell.  mode 0: start from pgas_guess[c] (the
  * reference's start) or from pfloor when pgas_guess is NULL; mode 1: start from the
  * network; mode 2: network start refined by at most 12 FP32 iterations of the same scheme;
@@ -206,8 +210,10 @@ athgpu_status athgpu_mlp_infer_tc(long long n, const float *params, const float 
  * attempt's last iterate (*fallbacks, may be NULL, counts cells that needed it).
  * prim[n][5] as ConservedToPrimitiveNormal leaves it (zeros before the solve),
  * iters64[n] = FP64 loop passes over all attempts (-1 = not converged), iters32[n] (may
- * be NULL) = FP32 refinement passes.  Allocates a queue of 40 bytes per cell with
- * cudaMallocAsync on the stream. */
+ * be NULL) = FP32 refinement passes.  Modes 1-2 evaluate the network on the tcgen05
+ * tensor cores (one 128-cell tile per CTA) unless ATHGPU_C2P_WARP_MMA is set.  Allocates a
+ * queue of 40 bytes per cell with cudaMallocAsync on the stream and synchronizes the
+ * stream at the end (ATHGPU_ERR_CUDA if a tensor-core wait timed out). */
 athgpu_status athgpu_sr_c2p_cells(long long n, double gamma, double pfloor, const double *cons,
                                   const double *bcc, const double *pgas_guess,
                                   const float *params, int mode, int phase1_iterations,
