@@ -201,3 +201,32 @@ class LearnedC2P:
 
     def load(self, path):
         self.params = self.to_dev(np.load(path).astype(np.float32))
+
+
+def _time_inference(log2n=22, seed=9):
+    """Train a small network and time its inference on 2^log2n cells on both tensor-core
+    paths (CUDA events, median of 4).  `python -m athena_gb300.learned_c2p [log2n]`."""
+    torch = _torch()
+    net = LearnedC2P(4.0 / 3.0, seed=3)
+    feats, targ = net.solver_pairs(1 << 16, 5)
+    net.set_standardization(feats, targ)
+    net.train(feats, targ, steps=200, batch=2048, lr=2.0e-3, seed=5)
+    w, bcc, u = pgen.sr_isolated_cells(1 << log2n, seed=seed)
+    f = net.features(net.to_dev(u), net.to_dev(bcc))
+    for name, fn in (("tcgen05", net.infer_tc), ("mma.sync", net.infer)):
+        ts = []
+        for _ in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn(f)
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        print("%-9s %.3f ms for 2^%d cells" % (name, float(np.median(ts)), log2n))
+
+
+if __name__ == "__main__":
+    import sys
+    from . import build
+    build.build()
+    _time_inference(int(sys.argv[1]) if len(sys.argv) > 1 else 22)
