@@ -59,6 +59,9 @@ void free_all(athgpu_ctx* c) {
   if (c->cycle_exec) cudaGraphExecDestroy(c->cycle_exec);
   if (c->cycle_graph) cudaGraphDestroy(c->cycle_graph);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
 }
 
 cudaError_t run_stage_dispatch(athgpu_ctx* c, int stage) {
@@ -175,6 +178,12 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
   c->stream = c->own_stream;
+  e = cudaStreamCreateWithFlags(&c->aux_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate aux"));
+  e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
+  e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
 
   const i64 nb = m.nb, rb = c->real_bytes;
   Registers& r = c->r;
@@ -196,10 +205,10 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     allocs.push_back({&r.ulo, nb * 5 * m.ncell * rb});
     allocs.push_back({(void**)&c->staging, nb * 5 * m.ncell * 8});
   }
-  if (d->relativistic) {
-    allocs.push_back({(void**)&c->c2p_queue, nb * m.nx1 * m.nx2 * m.nx3 * (i64)sizeof(int)});
-    allocs.push_back({(void**)&c->c2p_qcount, (i64)sizeof(unsigned)});
-  }
+  // W(U)'s list of cells to finish later: SR solves deferred to the second pass, or the
+  // floors' rewrite of U (Newtonian)
+  allocs.push_back({(void**)&c->c2p_queue, nb * m.nx1 * m.nx2 * m.nx3 * (i64)sizeof(int)});
+  allocs.push_back({(void**)&c->c2p_qcount, (i64)sizeof(unsigned)});
   for (auto& a : allocs) {
     e = cudaMalloc(a.p, a.bytes);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));

@@ -46,6 +46,9 @@ struct athgpu_ctx {
   float* coords32 = nullptr; // the same, rounded to FP32, for the FP32 kernels
   int* nbr = nullptr;
   cudaStream_t own_stream = nullptr, stream = nullptr;
+  // second stream for the ghost exchange beside W(U), forked and joined with events
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t cycle_exec = nullptr;
   cudaGraph_t cycle_graph = nullptr;
   cudaStream_t graph_stream = nullptr;

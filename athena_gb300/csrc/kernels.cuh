@@ -832,11 +832,9 @@ exchange_kernel(DevMesh m, int with_u, T* __restrict__ u, double* __restrict__ b
 }
 
 // ---------------------------------------------------------------------------------------
-// Field::CalculateCellCenteredField (field.cpp:112-180, uniform weights) and
-// EquationOfState::ConservedToPrimitive (adiabatic_mhd.cpp:41-90) over whole blocks,
-// fused with Hydro::NewBlockTimeStep (new_blockdt.cpp:80-103) on the interior when
-// do_dt is set: the per-cell dx/(|v|+c_f) minimum is reduced with warp shuffles and one
-// atomicMin per warp on the order-preserving bit pattern of the positive double.
+// Reductions for the CFL time step of W(U) (Hydro::NewBlockTimeStep): warp shuffles, a
+// CTA reduction in shared memory and one atomicMin per CTA on the order-preserving bit
+// pattern of the positive double.
 __device__ __forceinline__ double warp_min(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -888,12 +886,75 @@ __device__ __forceinline__ i64 src_cell(const DevMesh& m, int b, int k, int j, i
   return cidx(m, nbr_of(m, b, o1, o2, o3), 0, nvar, sk, sj, si);
 }
 
+// Field::CalculateCellCenteredField (field.cpp:112-180, uniform weights) and the
+// Newtonian EquationOfState::ConservedToPrimitive (adiabatic_mhd.cpp:41-90) of one cell,
+// from the conserved state at cs (the cell itself, or its owner for a ghost cell) without
+// writing anything.
+template <typename Real>
+struct C2POne {
+  Real u_d, u_e, vx, vy, vz, w_p, bcc1, bcc2, bcc3, b1lr, b2lr, b3lr;
+  bool dfloored, pfloored;
+};
+template <typename Real>
+__device__ __forceinline__ C2POne<Real> c2p_one(const DevMesh& m, int b, int k, int j, int i,
+                                                const double* __restrict__ b1,
+                                                const double* __restrict__ b2,
+                                                const double* __restrict__ b3,
+                                                const Real* u, i64 cs, bool ghost) {
+  C2POne<Real> o;
+  // the face fields after the ghost exchange: a ghost cell's faces hold its owner's values
+  (void)ghost;
+  const double b1l = __ldg(b1 + f1idx(m, b, k, j, i)), b1r = __ldg(b1 + f1idx(m, b, k, j, i + 1));
+  const double b2l = __ldg(b2 + f2idx(m, b, k, j, i)), b2r = __ldg(b2 + f2idx(m, b, k, j + 1, i));
+  const double b3l = __ldg(b3 + f3idx(m, b, k, j, i)), b3r = __ldg(b3 + f3idx(m, b, k + 1, j, i));
+  // the lower faces in the bulk precision (also the dt's |b_face - bcc| term)
+  o.b1lr = to_real(b1l, Real());
+  o.b2lr = to_real(b2l, Real());
+  o.b3lr = to_real(b3l, Real());
+  if constexpr (sizeof(Real) == 8) {  // the reference's arithmetic
+    const double lw = 0.5, rw = 0.5;
+    o.bcc1 = lw * b1l + rw * b1r;
+    o.bcc2 = lw * b2l + rw * b2r;
+    o.bcc3 = lw * b3l + rw * b3r;
+  } else {  // FP32 path: average of the FP32-rounded faces
+    o.bcc1 = Real(0.5) * o.b1lr + Real(0.5) * to_real(b1r, Real());
+    o.bcc2 = Real(0.5) * o.b2lr + Real(0.5) * to_real(b2r, Real());
+    o.bcc3 = Real(0.5) * o.b3lr + Real(0.5) * to_real(b3r, Real());
+  }
+  const i64 vs = m.ncell;
+  const Real gm1 = rgamma(m, Real()) - Real(1.0);
+  const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
+  Real u_d = u[cs], u_m1 = u[cs + vs], u_m2 = u[cs + 2 * vs], u_m3 = u[cs + 3 * vs],
+       u_e = u[cs + 4 * vs];
+  o.dfloored = !(u_d > dfl);
+  u_d = (u_d > dfl) ? u_d : dfl;
+  Real di = Real(1.0) / u_d;
+  o.vx = u_m1 * di;
+  o.vy = u_m2 * di;
+  o.vz = u_m3 * di;
+  Real pb = Real(0.5) * (o.bcc1 * o.bcc1 + o.bcc2 * o.bcc2 + o.bcc3 * o.bcc3);
+  Real e_k = Real(0.5) * di * (u_m1 * u_m1 + u_m2 * u_m2 + u_m3 * u_m3);
+  Real w_p = gm1 * (u_e - e_k - pb);
+  o.pfloored = !(w_p > pfl);
+  o.u_e = (w_p > pfl) ? u_e : ((pfl / gm1) + e_k + pb);
+  o.w_p = (w_p > pfl) ? w_p : pfl;
+  o.u_d = u_d;
+  return o;
+}
+
+// W(U) over whole blocks (ghosts included: a ghost cell reads its conserved state from the
+// block that owns it, its faces from the exchanged face fields), fused with
+// Hydro::NewBlockTimeStep
+// (new_blockdt.cpp:80-103) on the interior when do_dt is set.  The floors' rewrite of U
+// (adiabatic_mhd.cpp:83-84) is not done here: an interior cell that needs it is appended
+// to flist, and c2p_floor_writeback_kernel rewrites U after every cell (ghost copies
+// included) has read the pre-floor state, as with the reference's exchanged ghost copies.
 template <typename Real, int KAHAN>
 __global__ void __launch_bounds__(128)
 c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
-           const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
-           Real* ulo, Real* __restrict__ w, Real* __restrict__ bcc, Real* __restrict__ cc,
-           DevClock* clk) {
+           const double* __restrict__ b2, const double* __restrict__ b3, const Real* u,
+           Real* __restrict__ w, Real* __restrict__ bcc, Real* __restrict__ cc,
+           DevClock* clk, int* __restrict__ flist, unsigned* __restrict__ fcount) {
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   Real cell_dt = big_dt(Real());
   if (t < (i64)m.nb * m.ncell) {
@@ -903,85 +964,83 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     r /= m.nc1;
     const int j = (int)(r % m.nc2);
     const int k = (int)(r / m.nc2);
-    const double b1l = b1[f1idx(m, b, k, j, i)], b1r = b1[f1idx(m, b, k, j, i + 1)];
-    const double b2l = b2[f2idx(m, b, k, j, i)], b2r = b2[f2idx(m, b, k, j + 1, i)];
-    const double b3l = b3[f3idx(m, b, k, j, i)], b3r = b3[f3idx(m, b, k + 1, j, i)];
-    // the lower faces in the bulk precision (also the dt's |b_face - bcc| term)
-    const Real b1lr = to_real(b1l, Real()), b2lr = to_real(b2l, Real()),
-               b3lr = to_real(b3l, Real());
-    Real bcc1, bcc2, bcc3;
-    if constexpr (sizeof(Real) == 8) {  // field.cpp:112-180, the reference's arithmetic
-      const double lw = 0.5, rw = 0.5;
-      bcc1 = lw * b1l + rw * b1r;
-      bcc2 = lw * b2l + rw * b2r;
-      bcc3 = lw * b3l + rw * b3r;
-    } else {  // FP32 path: average of the FP32-rounded faces (no FP64-pipe work)
-      bcc1 = Real(0.5) * b1lr + Real(0.5) * to_real(b1r, Real());
-      bcc2 = Real(0.5) * b2lr + Real(0.5) * to_real(b2r, Real());
-      bcc3 = Real(0.5) * b3lr + Real(0.5) * to_real(b3r, Real());
-    }
+    bool ghost;
+    const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
+    const C2POne<Real> o = c2p_one<Real>(m, b, k, j, i, b1, b2, b3, u, cs, ghost);
     const i64 vs = m.ncell;
     const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
     const i64 cb = cidx(m, b, 0, 3, k, j, i);
-    const Real gm1 = rgamma(m, Real()) - Real(1.0);
-    const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
-    bool ghost;
-    const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
-    Real u_d = u[cs], u_m1 = u[cs + vs], u_m2 = u[cs + 2 * vs], u_m3 = u[cs + 3 * vs],
-         u_e = u[cs + 4 * vs];
-    const bool dfloored = !(u_d > dfl);
-    u_d = (u_d > dfl) ? u_d : dfl;
-    Real di = Real(1.0) / u_d;
-    Real vx = u_m1 * di, vy = u_m2 * di, vz = u_m3 * di;
-    Real pb = Real(0.5) * (bcc1 * bcc1 + bcc2 * bcc2 + bcc3 * bcc3);
-    Real e_k = Real(0.5) * di * (u_m1 * u_m1 + u_m2 * u_m2 + u_m3 * u_m3);
-    Real w_p = gm1 * (u_e - e_k - pb);
-    const bool pfloored = !(w_p > pfl);
-    u_e = (w_p > pfl) ? u_e : ((pfl / gm1) + e_k + pb);
-    w_p = (w_p > pfl) ? w_p : pfl;
-    // floors rewrite U in the interior only (a ghost's owner floors its own copy)
-    if (dfloored && !ghost) {
-      u[c] = u_d;
-      if (KAHAN && ulo) ulo[c] = Real(0);
+    if ((o.dfloored || o.pfloored) && !ghost) {
+      const unsigned slot = atomicAdd(fcount, 1u);
+      flist[slot] = (int)(((i64)b * m.nx3 + (k - m.ks)) * m.nx2 * m.nx1 +
+                          (i64)(j - m.js) * m.nx1 + (i - m.is));
     }
-    if (pfloored && !ghost) {
-      u[c + 4 * vs] = u_e;
-      if (KAHAN && ulo) ulo[c + 4 * vs] = Real(0);
-    }
-    if ((dfloored || pfloored) && do_dt) atomicAdd(&clk->c2p_floor_count, 1);
-    w[c] = u_d;
-    w[c + vs] = vx;
-    w[c + 2 * vs] = vy;
-    w[c + 3 * vs] = vz;
-    w[c + 4 * vs] = w_p;
-    bcc[cb] = bcc1;
-    bcc[cb + vs] = bcc2;
-    bcc[cb + 2 * vs] = bcc3;
-    store_cce<Real, false>(cc, cb, vs, vx, vy, vz, bcc1, bcc2, bcc3);
-    if (do_dt && i >= m.is && i <= m.ie && j >= m.js && j <= m.je && k >= m.ks &&
-        k <= m.ke) {
+    if ((o.dfloored || o.pfloored) && do_dt) atomicAdd(&clk->c2p_floor_count, 1);
+    w[c] = o.u_d;
+    w[c + vs] = o.vx;
+    w[c + 2 * vs] = o.vy;
+    w[c + 3 * vs] = o.vz;
+    w[c + 4 * vs] = o.w_p;
+    bcc[cb] = o.bcc1;
+    bcc[cb + vs] = o.bcc2;
+    bcc[cb + 2 * vs] = o.bcc3;
+    store_cce<Real, false>(cc, cb, vs, o.vx, o.vy, o.vz, o.bcc1, o.bcc2, o.bcc3);
+    if (do_dt && !ghost) {
       // new_blockdt.cpp:80-103, in the bulk precision on the stored primitives (FP64
       // path: the reference's arithmetic; FP32 path: FP32, reduced in FP64)
       const Real gam = rgamma(m, Real());
       Real dt1 = rdx(m, 0, Real())[(i64)b * m.nc1 + i],
            dt2 = rdx(m, 1, Real())[(i64)b * m.nc2 + j],
            dt3 = rdx(m, 2, Real())[(i64)b * m.nc3 + k];
-      Real bx = bcc1 + dabs(b1lr - bcc1);
-      Real cf = fast_ms<Real>(gam, u_d, w_p, bcc2, bcc3, bx);
-      Real speed = smax<Real>(Real(0.0), (dabs(vx) + cf));
+      Real bx = o.bcc1 + dabs(o.b1lr - o.bcc1);
+      Real cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc2, o.bcc3, bx);
+      Real speed = smax<Real>(Real(0.0), (dabs(o.vx) + cf));
       dt1 /= (speed);
-      bx = bcc2 + dabs(b2lr - bcc2);
-      cf = fast_ms<Real>(gam, u_d, w_p, bcc3, bcc1, bx);
-      speed = smax<Real>(Real(0.0), (dabs(vy) + cf));
+      bx = o.bcc2 + dabs(o.b2lr - o.bcc2);
+      cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc3, o.bcc1, bx);
+      speed = smax<Real>(Real(0.0), (dabs(o.vy) + cf));
       dt2 /= (speed);
-      bx = bcc3 + dabs(b3lr - bcc3);
-      cf = fast_ms<Real>(gam, u_d, w_p, bcc1, bcc2, bx);
-      speed = smax<Real>(Real(0.0), (dabs(vz) + cf));
+      bx = o.bcc3 + dabs(o.b3lr - o.bcc3);
+      cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc1, o.bcc2, bx);
+      speed = smax<Real>(Real(0.0), (dabs(o.vz) + cf));
       dt3 /= (speed);
       cell_dt = smin<Real>(smin<Real>(dt1, dt2), dt3);
     }
   }
   if (do_dt) cta_min_to_clock<Real>(cell_dt, clk);  // reduced in the bulk precision
+}
+
+// The floors' rewrite of U for the interior cells c2p_kernel listed (grid-stride over the
+// list; usually empty): density and/or energy replaced by their floored values, the
+// compensation of a rewritten component cleared.
+template <typename Real, int KAHAN>
+__global__ void __launch_bounds__(128)
+c2p_floor_writeback_kernel(DevMesh m, const double* __restrict__ b1,
+                           const double* __restrict__ b2, const double* __restrict__ b3,
+                           Real* u, Real* ulo, const int* __restrict__ flist,
+                           const unsigned* __restrict__ fcount) {
+  const unsigned n = *fcount;
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int q = flist[e];
+    const int nint = m.nx1 * m.nx2 * m.nx3;
+    const int b = q / nint;
+    int r = q - b * nint;
+    const int i = m.is + r % m.nx1;
+    r /= m.nx1;
+    const int j = m.js + r % m.nx2;
+    const int k = m.ks + r / m.nx2;
+    const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
+    const C2POne<Real> o = c2p_one<Real>(m, b, k, j, i, b1, b2, b3, u, c, false);
+    const i64 vs = m.ncell;
+    if (o.dfloored) {
+      u[c] = o.u_d;
+      if (KAHAN && ulo) ulo[c] = Real(0);
+    }
+    if (o.pfloored) {
+      u[c + 4 * vs] = o.u_e;
+      if (KAHAN && ulo) ulo[c + 4 * vs] = Real(0);
+    }
+  }
 }
 
 // EquationOfState::ConservedToPrimitive for SR MHD (adiabatic_mhd_sr.cpp:72-272) on the

@@ -62,7 +62,8 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
 // are not needed by the stage kernels, see exchange_kernel).
 template <typename Real>
 static void launch_exchange(athgpu_ctx* c, Real* u, double* b1, double* b2, double* b3,
-                            int with_u) {
+                            int with_u, cudaStream_t st = nullptr) {
+  if (!st) st = c->stream;
   const DevMesh& m = c->m;
   const long long gc = with_u ? m.ncell - (long long)m.nx1 * m.nx2 * m.nx3 : 0;
   const long long g1 = m.nf1 - (long long)(m.nx1 + 1) * m.nx2 * m.nx3;
@@ -70,10 +71,9 @@ static void launch_exchange(athgpu_ctx* c, Real* u, double* b1, double* b2, doub
   const long long g3 = m.nf3 - (long long)m.nx1 * m.nx2 * (m.nx3 + 1);
   const long long n = (gc + g1 + g2 + g3) * m.nb;
   if (n < (1LL << 31) - 256)
-    exchange_kernel<Real, int><<<nblk(n, 256), 256, 0, c->stream>>>(m, with_u, u, b1, b2, b3);
+    exchange_kernel<Real, int><<<nblk(n, 256), 256, 0, st>>>(m, with_u, u, b1, b2, b3);
   else
-    exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, c->stream>>>(m, with_u, u, b1,
-                                                                          b2, b3);
+    exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, st>>>(m, with_u, u, b1, b2, b3);
 }
 
 template <typename Real, int KAHAN>
@@ -83,7 +83,17 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
   const DevMesh& m = c->m;
   cudaStream_t s = c->stream;
   const long long nc = (long long)m.nb * m.ncell;
-  {
+  // The relativistic W(U) reads no exchanged face (interior cells only; ghost primitives
+  // are copied from their owners), so there the ghost exchange runs on the auxiliary
+  // stream beside it (forked and joined with events, also inside the captured cycle
+  // graph); the Newtonian W(U) reads the exchanged faces of its ghost cells and follows
+  // the exchange.  The per-kernel profile runs everything one after the other.
+  const bool overlap = !c->profiling && c->aux_stream != nullptr && c->desc.relativistic;
+  if (overlap) {
+    cudaEventRecord(c->ev_fork, s);
+    cudaStreamWaitEvent(c->aux_stream, c->ev_fork, 0);
+    launch_exchange<Real>(c, u, b1, b2, b3, with_u, c->aux_stream);
+  } else {
     ProfScope ps(c, "exchange");
     launch_exchange<Real>(c, u, b1, b2, b3, with_u);
   }
@@ -113,9 +123,18 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
           m, wout, (Real*)c->r.bcc, (Real*)c->r.cce);
       c->launches += 2;
     } else {
+      cudaMemsetAsync(c->c2p_qcount, 0, sizeof(unsigned), s);
       c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
-          m, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk);
+          m, do_dt, b1, b2, b3, u, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk,
+          c->c2p_queue, c->c2p_qcount);
+      c2p_floor_writeback_kernel<Real, KAHAN><<<64, 128, 0, s>>>(
+          m, b1, b2, b3, u, lo, c->c2p_queue, c->c2p_qcount);
+      c->launches += 1;
     }
+  }
+  if (overlap) {
+    cudaEventRecord(c->ev_join, c->aux_stream);
+    cudaStreamWaitEvent(s, c->ev_join, 0);
   }
   if (rotate) c->r.wsel = 1 - c->r.wsel;
   c->launches += 2;

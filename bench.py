@@ -236,6 +236,7 @@ def run_gpu(args, rank, world, local_rank):
                           "h2d_bytes_per_step": ebytes, "d2h_bytes_per_step": ebytes,
                           "steps": e_steps}
         g.close()
+    res["linear_wave_l1"] = run_linear_wave()
     if not args.no_learned:
         res["learned_c2p"], net = run_learned_c2p()
         if not args.no_sr:
@@ -296,6 +297,38 @@ def run_learned_c2p(reps=5):
     out["speedup"] = out["plain"]["ms"] / out["learned"]["ms"]
     out["passes_ratio"] = out["learned"]["mean_fp64_passes"] / out["plain"]["mean_fp64_passes"]
     return out, net
+
+
+def run_linear_wave():
+    """Linear-wave accuracy of the FP32 and FP64 paths: the oblique fast wave (VL2 + PLM +
+    HLLD) for one period on 64x32x32 (one MeshBlock, the reference's config-1 case, and on
+    128x64x64 with 8 MeshBlocks) at the reference's amplitude 1e-6, and on 64x32x32 at
+    amplitude 1e-3; RMS L1 error against the initial state (linear_wave.cpp's error
+    routine, restated in pgen.LinearWave.l1_errors)."""
+    from athena_gb300 import pgen
+    from athena_gb300.mesh import MeshSpec
+    from athena_gb300.runtime import StageUpdate
+    out = {}
+    for nx, nb, amp in (((64, 32, 32), (1, 1, 1), 1.0e-6), ((128, 64, 64), (2, 2, 2), 1.0e-6),
+                        ((64, 32, 32), (1, 1, 1), 1.0e-3)):
+        mesh = MeshSpec(nx, nb, 2, (0.0, 0.0, 0.0), (3.0, 1.5, 1.5))
+        lw = pgen.LinearWave(mesh, gamma=1.666666666666667, amp=amp)
+        ic = lw.generate()
+        row = {}
+        for prec in ("fp64", "fp32"):
+            g = StageUpdate(mesh, lw.gam, xorder=2, rsolver="hlld", precision=prec,
+                            tlim=lw.period())
+            g.set_state(*ic)
+            g.initialize()
+            ncyc = g.run_until(lw.period())
+            u = g.state()[0]
+            _, bcc = g.prim()
+            row[prec] = lw.l1_errors(u, bcc)[0]
+            row["cycles_" + prec] = ncyc
+            g.close()
+        row["ratio_fp32_vs_fp64"] = row["fp32"] / row["fp64"]
+        out["%dx%dx%d_amp%g" % (nx + (amp,))] = row
+    return out
 
 
 SR_CYCLES = {"fp32": 10, "fp64": 3}
@@ -516,6 +549,8 @@ def main():
         line["learned_c2p"] = res["learned_c2p"]
     if "sr_kh" in res:
         line["sr_kh"] = res["sr_kh"]
+    if "linear_wave_l1" in res:
+        line["linear_wave_l1"] = res["linear_wave_l1"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline((mesh, make_ic(NX, NB)[1]))
     print(json.dumps(line))

@@ -187,7 +187,9 @@ def test_graph_replay_counts_launches():
     g.cycle(3)
     g.synchronize()
     per = g.launch_count() / 3
-    assert per == 2 * 7 + 1   # two stages of 7 kernels, one clock update
+    # two stages of 8 kernels (3 sweeps, corner EMFs, CT, ghost exchange, W(U), the
+    # floors' write-back of U), one clock update
+    assert per == 2 * 8 + 1
 
 
 def test_autotune_keeps_the_state_and_the_results():
