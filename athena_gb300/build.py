@@ -26,6 +26,7 @@ UNITS = {
     # learned con2prim: the FP64 polish keeps the reference's rounding (no contraction)
     "sr_learned.cu": ["-fmad=false"],
     "selftest.cu": ["-fmad=false"],
+    "history.cu": ["-fmad=false"],
 }
 
 

@@ -82,6 +82,7 @@ def load_library(path=LIB_PATH):
         "athgpu_device_state_ptrs": ([vp, ctypes.POINTER(DeviceState)], ip),
         "athgpu_set_sweep_segment": ([vp, ip, ip], ip),
         "athgpu_autotune": ([vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
+        "athgpu_history": ([vp, dp], ip),
         "athgpu_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
         "athgpu_profile_cycle": ([vp, ip, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ip)], ip),
@@ -250,6 +251,15 @@ class StageUpdate:
                "athgpu_profile_cycle")
         return [(L.athgpu_profile_label(self.h, i).decode(), buf[i])
                 for i in range(min(n.value, 256))]
+
+    HISTORY_NAMES = ("mass", "1-mom", "2-mom", "3-mom", "1-KE", "2-KE", "3-KE", "tot-E",
+                     "1-ME", "2-ME", "3-ME")
+
+    def history(self):
+        """The reference's history-output sums (dict name -> value)."""
+        out = np.zeros(len(self.HISTORY_NAMES))
+        _check(load_library().athgpu_history(self.h, _dp(out)), "athgpu_history")
+        return dict(zip(self.HISTORY_NAMES, out.tolist()))
 
     def autotune(self, cycles=2):
         """Pick the x2/x3 sweep segment lengths by timing (state left unchanged);

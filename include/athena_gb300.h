@@ -142,6 +142,14 @@ athgpu_status athgpu_device_state_ptrs(athgpu_ctx *ctx, athgpu_device_state *out
  * autotuner's knob); 0 = heuristic default. */
 athgpu_status athgpu_set_sweep_segment(athgpu_ctx *ctx, int seg_x2, int seg_x3);
 
+/* History output (HistoryOutput::WriteOutputFile, outputs/history.cpp:77-140): out[11]
+ * (HOST) = volume-weighted sums over the interior cells of all MeshBlocks of mass, 1-mom,
+ * 2-mom, 3-mom, 1-KE, 2-KE, 3-KE, tot-E, 1-ME, 2-ME, 3-ME, in FP64, reduced
+ * deterministically (the same bits on every call; the order differs from the
+ * reference's sequential sum).  Synchronous. */
+#define ATHGPU_NHISTORY 11
+athgpu_status athgpu_history(athgpu_ctx *ctx, double *out);
+
 /* Autotuner of the sweep tiling: times `cycles` cycles (after one warm-up) for each
  * candidate segment length of the x2 sweep (the whole column, then halves down to 4
  * cells), keeps the fastest, then does the same for the x3 sweep, and applies the pair

@@ -782,10 +782,18 @@ static void corner_e(orc_mesh *m, int b, scratch *s) {
  * the neighbour in direction o holds the same edge at index - o*nx.
  */
 static int nbr_block(const orc_mesh *m, int b, int o1, int o2, int o3) {
-  int n1 = m->p.nbx1, n2 = m->p.nbx2, n3 = m->p.nbx3;
-  int l1 = b % n1, l2 = (b / n1) % n2, l3 = b / (n1 * n2);
-  l1 = (l1 + o1 + n1) % n1; l2 = (l2 + o2 + n2) % n2; l3 = (l3 + o3 + n3) % n3;
-  return (l3 * n2 + l2) * n1 + l1;
+  int n[3] = {m->p.nbx1, m->p.nbx2, m->p.nbx3};
+  int l[3] = {b % n[0], (b / n[0]) % n[1], b / (n[0] * n[1])};
+  int o[3] = {o1, o2, o3};
+  for (int a = 0; a < 3; ++a) {
+    int t = l[a] + o[a];
+    if (t < 0 || t >= n[a]) {  /* across a mesh face: periodic wrap, else no neighbour */
+      if (m->p.bc[2 * a + (t < 0 ? 0 : 1)] != 0) return -1;
+      t = (t + n[a]) % n[a];
+    }
+    l[a] = t;
+  }
+  return (l[2] * n[1] + l[1]) * n[0] + l[0];
 }
 
 /* corrected value of edge component c (0,1,2 = e1,e2,e3) at (k,j,i) of block b */
@@ -807,20 +815,29 @@ static double emf_corrected(const orc_mesh *m, int b, int c, int k, int j, int i
   int a0 = (c == 0) ? 1 : 0, a1 = (c == 2) ? 1 : 2;
   double sum = own;
   int axes[2] = {a0, a1};
+  int count = 1; /* blocks of the same level sharing the edge (CountFineEdges) */
   for (int t = 0; t < 2; ++t) { /* face neighbours */
     int ax = axes[t];
     if (o[ax] == 0) continue;
     int d[3] = {0, 0, 0};
     d[ax] = o[ax];
     int nb = nbr_block(m, b, d[0], d[1], d[2]);
+    if (nb < 0) continue; /* a physical boundary: nothing received */
     sum += EV(nb, k - d[2] * nx[2], j - d[1] * nx[1], i - d[0] * nx[0]);
+    ++count;
   }
-  if (on == 2) { /* edge neighbour */
+  if (on == 2) { /* edge neighbour; flux_correction_fc.cpp:1477-1481 divides by the count */
     int nb = nbr_block(m, b, o[0], o[1], o[2]);
-    sum += EV(nb, k - o[2] * nx[2], j - o[1] * nx[1], i - o[0] * nx[0]);
-    return sum * (1.0 / 4.0);
+    if (nb >= 0) {
+      sum += EV(nb, k - o[2] * nx[2], j - o[1] * nx[1], i - o[0] * nx[0]);
+      ++count;
+    }
+    if (count == 1) return own;
+    return sum * (1.0 / (double)count);
   }
-  return sum * 0.5;
+  /* face interior (flux_correction_fc.cpp:1362-1380): halved only if the face has a
+   * neighbour */
+  return count == 2 ? sum * 0.5 : own;
 #undef EV
 }
 
@@ -944,7 +961,16 @@ static long sr_c2p_block(orc_mesh *m, int b, double *u, double *prim, int il, in
                          int jl, int ju, int kl, int ku);
 
 static long con2prim(orc_mesh *m, int b, double *u, double *prim) {
-  int il = 0, iu = m->nc1 - 1, jl = 0, ju = m->nc2 - 1, kl = 0, ku = m->nc3 - 1;
+  /* the interior plus the ghost layers that have a neighbour (time_integrator.cpp:
+   * 2206-2212, mesh.cpp:1820-1831); ghosts on physical boundaries come from the boundary
+   * functions instead */
+  int ng = m->p.ng;
+  int il = m->is - (nbr_block(m, b, -1, 0, 0) >= 0 ? ng : 0);
+  int iu = m->ie + (nbr_block(m, b, 1, 0, 0) >= 0 ? ng : 0);
+  int jl = m->js - (nbr_block(m, b, 0, -1, 0) >= 0 ? ng : 0);
+  int ju = m->je + (nbr_block(m, b, 0, 1, 0) >= 0 ? ng : 0);
+  int kl = m->ks - (nbr_block(m, b, 0, 0, -1) >= 0 ? ng : 0);
+  int ku = m->ke + (nbr_block(m, b, 0, 0, 1) >= 0 ? ng : 0);
   cell_centered_field(m, b, il, iu, jl, ju, kl, ku);
   if (m->p.relativistic) return sr_c2p_block(m, b, u, prim, il, iu, jl, ju, kl, ku);
   const double *bcc = m->bcc + (long)b * 3 * m->ncell;
@@ -1280,16 +1306,26 @@ static void new_time_step(orc_mesh *m, const double *block_dt) {
 /* returns 1 when idx lies outside the block's own range and was mapped to the
  * neighbour (which is the block itself when the mesh has one block along the axis) */
 static int locate(int own_lo, int own_hi, int n, int nb, int lx, int idx, int *nlx,
-                  int *nidx) {
-  if (idx < own_lo) { *nlx = (lx - 1 + nb) % nb; *nidx = idx + n; return 1; }
-  if (idx > own_hi) { *nlx = (lx + 1) % nb; *nidx = idx - n; return 1; }
+                  int *nidx, int bc_lo, int bc_hi) {
+  if (idx < own_lo) {
+    if (lx == 0 && bc_lo != 0) return -1;  /* physical boundary: no neighbour */
+    *nlx = (lx - 1 + nb) % nb; *nidx = idx + n; return 1;
+  }
+  if (idx > own_hi) {
+    if (lx == nb - 1 && bc_hi != 0) return -1;
+    *nlx = (lx + 1) % nb; *nidx = idx - n; return 1;
+  }
   *nlx = lx; *nidx = idx;
   return 0;
 }
 
+/* combine per-axis locate() results: -1 if any axis has no neighbour, else 1 if moved */
+static int loc_or(int a, int b) { return (a < 0 || b < 0) ? -1 : (a | b); }
+
 static void exchange(orc_mesh *m, double *cc, int nvar, double *f1, double *f2, double *f3) {
   int nbx1 = m->p.nbx1, nbx2 = m->p.nbx2, nbx3 = m->p.nbx3;
   int nx1 = m->p.nx1, nx2 = m->p.nx2, nx3 = m->p.nx3;
+  const int *bc = m->p.bc;
 #pragma omp parallel for schedule(static)
   for (int b = 0; b < m->nb; ++b) {
     int lx1 = b % nbx1, lx2 = (b / nbx1) % nbx2, lx3 = b / (nbx1 * nbx2);
@@ -1297,11 +1333,13 @@ static void exchange(orc_mesh *m, double *cc, int nvar, double *f1, double *f2, 
       for (int j = 0; j < m->nc2; ++j)
         for (int i = 0; i < m->nc1 + 1; ++i) {
           int a1, a2, a3, si, sj, sk;
-          int mv = locate(m->ks, m->ke, nx3, nbx3, lx3, k, &a3, &sk);
-          mv |= locate(m->js, m->je, nx2, nbx2, lx2, j, &a2, &sj);
+          int mv = locate(m->ks, m->ke, nx3, nbx3, lx3, k, &a3, &sk, bc[4], bc[5]);
+          mv = loc_or(mv, locate(m->js, m->je, nx2, nbx2, lx2, j, &a2, &sj, bc[2], bc[3]));
           int sb;
           if (cc && i < m->nc1) {
-            if (locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si) | mv) {
+            int r = loc_or(mv, locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si, bc[0],
+                                      bc[1]));
+            if (r > 0) {
               sb = (a3 * nbx2 + a2) * nbx1 + a1;
               for (int n = 0; n < nvar; ++n)
                 cc[(long)b * nvar * m->ncell + CIDX(m, n, k, j, i)] =
@@ -1309,7 +1347,9 @@ static void exchange(orc_mesh *m, double *cc, int nvar, double *f1, double *f2, 
             }
           }
           if (f1) {
-            if (locate(m->is, m->ie + 1, nx1, nbx1, lx1, i, &a1, &si) | mv) {
+            int r = loc_or(mv, locate(m->is, m->ie + 1, nx1, nbx1, lx1, i, &a1, &si, bc[0],
+                                      bc[1]));
+            if (r > 0) {
               sb = (a3 * nbx2 + a2) * nbx1 + a1;
               f1[(long)b * m->nf1 + F1IDX(m, k, j, i)] =
                   f1[(long)sb * m->nf1 + F1IDX(m, sk, sj, si)];
@@ -1321,10 +1361,11 @@ static void exchange(orc_mesh *m, double *cc, int nvar, double *f1, double *f2, 
         for (int j = 0; j < m->nc2 + 1; ++j)
           for (int i = 0; i < m->nc1; ++i) {
             int a1, a2, a3, si, sj, sk;
-            int mv = locate(m->ks, m->ke, nx3, nbx3, lx3, k, &a3, &sk);
-            mv |= locate(m->js, m->je + 1, nx2, nbx2, lx2, j, &a2, &sj);
-            mv |= locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si);
-            if (mv) {
+            int mv = locate(m->ks, m->ke, nx3, nbx3, lx3, k, &a3, &sk, bc[4], bc[5]);
+            mv = loc_or(mv, locate(m->js, m->je + 1, nx2, nbx2, lx2, j, &a2, &sj, bc[2],
+                                   bc[3]));
+            mv = loc_or(mv, locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si, bc[0], bc[1]));
+            if (mv > 0) {
               int sb = (a3 * nbx2 + a2) * nbx1 + a1;
               f2[(long)b * m->nf2 + F2IDX(m, k, j, i)] =
                   f2[(long)sb * m->nf2 + F2IDX(m, sk, sj, si)];
@@ -1335,10 +1376,10 @@ static void exchange(orc_mesh *m, double *cc, int nvar, double *f1, double *f2, 
         for (int j = 0; j < m->nc2; ++j)
           for (int i = 0; i < m->nc1; ++i) {
             int a1, a2, a3, si, sj, sk;
-            int mv = locate(m->ks, m->ke + 1, nx3, nbx3, lx3, k, &a3, &sk);
-            mv |= locate(m->js, m->je, nx2, nbx2, lx2, j, &a2, &sj);
-            mv |= locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si);
-            if (mv) {
+            int mv = locate(m->ks, m->ke + 1, nx3, nbx3, lx3, k, &a3, &sk, bc[4], bc[5]);
+            mv = loc_or(mv, locate(m->js, m->je, nx2, nbx2, lx2, j, &a2, &sj, bc[2], bc[3]));
+            mv = loc_or(mv, locate(m->is, m->ie, nx1, nbx1, lx1, i, &a1, &si, bc[0], bc[1]));
+            if (mv > 0) {
               int sb = (a3 * nbx2 + a2) * nbx1 + a1;
               f3[(long)b * m->nf3 + F3IDX(m, k, j, i)] =
                   f3[(long)sb * m->nf3 + F3IDX(m, sk, sj, si)];
@@ -1463,6 +1504,126 @@ double orc_get_time(const orc_mesh *m) { return m->time; }
 void orc_set_dt(orc_mesh *m, double dt) { m->dt = dt; }
 long orc_c2p_failures(const orc_mesh *m) { return m->c2p_fail; }
 
+/* ------------------------------------------------------------------------------------
+ * BoundaryValues::ApplyPhysicalBoundaries (bvals/bvals.cpp:453-680) on the primitives
+ * and the face field of block b: for each mesh face of the block that is a physical
+ * boundary, in the order inner/outer x1, x2, x3, the outflow or reflecting function of
+ * the hydro primitives (bvals/cc/outflow_cc.cpp, bvals/cc/hydro/reflect_hydro.cpp) and of
+ * the face field (bvals/fc/outflow_fc.cpp, bvals/fc/reflect_fc.cpp), then the
+ * cell-centred field of the ghost cells it filled (bvals.cpp:516-520).  The conserved
+ * state of those ghost cells (bvals.cpp:521-522) is not formed: nothing on the path
+ * reads it.
+ */
+static void apply_bcs(orc_mesh *m, int b, double *w) {
+  int ng = m->p.ng;
+  int lo[3] = {m->is, m->js, m->ks}, hi[3] = {m->ie, m->je, m->ke};
+  int has[6];  /* neighbour (block or periodic) across each block face */
+  for (int f = 0; f < 6; ++f) {
+    int o[3] = {0, 0, 0};
+    o[f / 2] = (f & 1) ? 1 : -1;
+    has[f] = nbr_block(m, b, o[0], o[1], o[2]) >= 0;
+  }
+  double *wb = w + (long)b * NHYDRO * m->ncell;
+  double *fb[3] = {m->b1 + (long)b * m->nf1, m->b2 + (long)b * m->nf2,
+                   m->b3 + (long)b * m->nf3};
+  long nc = m->ncell;
+  for (int a = 0; a < 3; ++a) {
+    /* transverse ranges: x1 uses the extended j/k ranges only where those faces are not
+     * physical; x2 the full i range; x3 the full i and j ranges (bvals.cpp:457-470,596) */
+    int rl[3], rh[3];
+    for (int d = 0; d < 3; ++d) { rl[d] = lo[d]; rh[d] = hi[d]; }
+    if (a == 0) {
+      if (has[2]) rl[1] -= ng;
+      if (has[3]) rh[1] += ng;
+      if (has[4]) rl[2] -= ng;
+      if (has[5]) rh[2] += ng;
+    } else if (a == 1) {
+      rl[0] -= ng; rh[0] += ng;
+      if (has[4]) rl[2] -= ng;
+      if (has[5]) rh[2] += ng;
+    } else {
+      rl[0] -= ng; rh[0] += ng;
+      rl[1] -= ng; rh[1] += ng;
+    }
+    for (int side = 0; side < 2; ++side) {
+      int f = 2 * a + side;
+      if (has[f]) continue;
+      int kind = m->p.bc[f];  /* 1 outflow, 2 reflecting */
+      /* primitives */
+      for (int g = 1; g <= ng; ++g) {
+        int dst = side ? hi[a] + g : lo[a] - g;
+        int src = (kind == 1) ? (side ? hi[a] : lo[a]) : (side ? hi[a] - g + 1 : lo[a] + g - 1);
+        int r0[3], r1[3];
+        for (int d = 0; d < 3; ++d) { r0[d] = rl[d]; r1[d] = rh[d]; }
+        r0[a] = r1[a] = dst;
+        for (int n = 0; n < NHYDRO; ++n) {
+          double sg = (kind == 2 && n == IVX + a) ? -1.0 : 1.0;
+          for (int k = r0[2]; k <= r1[2]; ++k)
+            for (int j = r0[1]; j <= r1[1]; ++j)
+              for (int i = r0[0]; i <= r1[0]; ++i) {
+                int s3[3] = {i, j, k};
+                s3[a] = src;
+                double v = wb[CIDX(m, n, s3[2], s3[1], s3[0])];
+                wb[CIDX(m, n, k, j, i)] = (sg < 0.0) ? -v : v;
+              }
+        }
+      }
+      /* face field */
+      for (int d = 0; d < 3; ++d) {
+        double *F = fb[d];
+        for (int g = 1; g <= ng; ++g) {
+          int dst, src;
+          double sg = 1.0;
+          if (d == a) { /* the normal component */
+            dst = side ? hi[a] + 1 + g : lo[a] - g;
+            src = (kind == 1) ? (side ? hi[a] + 1 : lo[a]) : (side ? hi[a] + 1 - g : lo[a] + g);
+            if (kind == 2) sg = -1.0;
+          } else {
+            dst = side ? hi[a] + g : lo[a] - g;
+            src = (kind == 1) ? (side ? hi[a] : lo[a]) : (side ? hi[a] - g + 1 : lo[a] + g - 1);
+          }
+          int r0[3], r1[3];
+          for (int e = 0; e < 3; ++e) { r0[e] = rl[e]; r1[e] = rh[e]; }
+          r1[d] += (d != a) ? 1 : 0;  /* the face count along its own direction */
+          r0[a] = r1[a] = dst;
+          for (int k = r0[2]; k <= r1[2]; ++k)
+            for (int j = r0[1]; j <= r1[1]; ++j)
+              for (int i = r0[0]; i <= r1[0]; ++i) {
+                int s3[3] = {i, j, k};
+                s3[a] = src;
+                long di = (d == 0) ? F1IDX(m, k, j, i) : (d == 1) ? F2IDX(m, k, j, i)
+                                                                   : F3IDX(m, k, j, i);
+                long si = (d == 0) ? F1IDX(m, s3[2], s3[1], s3[0])
+                        : (d == 1) ? F2IDX(m, s3[2], s3[1], s3[0])
+                                   : F3IDX(m, s3[2], s3[1], s3[0]);
+                double v = F[si];
+                F[di] = (sg < 0.0) ? -v : v;
+              }
+        }
+      }
+      /* cell-centred field of the filled ghost cells */
+      int c0[3], c1[3];
+      for (int d = 0; d < 3; ++d) { c0[d] = rl[d]; c1[d] = rh[d]; }
+      c0[a] = side ? hi[a] + 1 : lo[a] - ng;
+      c1[a] = side ? hi[a] + ng : lo[a] - 1;
+      cell_centered_field(m, b, c0[0], c1[0], c0[1], c1[1], c0[2], c1[2]);
+    }
+  }
+  (void)nc;
+}
+
+static int any_physical(const orc_mesh *m) {
+  for (int f = 0; f < 6; ++f)
+    if (m->p.bc[f] != 0) return 1;
+  return 0;
+}
+
+static void all_bcs(orc_mesh *m, double *w) {
+  if (!any_physical(m)) return;
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < m->nb; ++b) apply_bcs(m, b, w);
+}
+
 static void all_con2prim(orc_mesh *m, double *wout) {
   long fails = 0;
 #pragma omp parallel for schedule(static) reduction(+ : fails)
@@ -1485,6 +1646,7 @@ void orc_initialize(orc_mesh *m) {
    * (mesh.cpp:1833), NewBlockTimeStep + NewTimeStep (mesh.cpp:1959-1964) */
   exchange(m, m->u, NHYDRO, m->b1, m->b2, m->b3);
   all_con2prim(m, m->w);
+  all_bcs(m, m->w);  /* mesh.cpp:1886 */
   all_new_dt(m);
 }
 
@@ -1558,6 +1720,7 @@ void orc_stage(orc_mesh *m, int stage) {
   exchange(m, m->u, NHYDRO, m->b1, m->b2, m->b3);
   all_con2prim(m, m->w1);  /* ConservedToPrimitive(u, w, b, w1, ...) (:2221-2223) */
   SWAP(m->w, m->w1);       /* :2269 */
+  all_bcs(m, m->w);        /* PhysicalBoundary task, :2278-2299 */
 }
 
 void orc_cycle(orc_mesh *m) {

@@ -12,8 +12,8 @@
  *
  * Data layout: every MeshBlock keeps the reference's AthenaArray layout
  * (athena_arrays.hpp:140-143, last index fastest, ghosts included); blocks are stored
- * in lexicographic order b = (lx3*nbx2 + lx2)*nbx1 + lx1.  Only a uniform, periodic,
- * single-level 3-D mesh is supported.
+ * in lexicographic order b = (lx3*nbx2 + lx2)*nbx1 + lx1.  A uniform single-level 3-D
+ * mesh with periodic, outflow or reflecting mesh faces is supported.
  */
 #ifndef ATHENA_ORACLE_H_
 #define ATHENA_ORACLE_H_
@@ -31,6 +31,10 @@ typedef struct {
   int relativistic;       /* 0 = Newtonian adiabatic MHD, 1 = special relativistic */
   double gamma, dfloor, pfloor, cfl_number, tlim;
   double sigma_max, beta_min, gamma_max; /* SR floors (adiabatic_mhd_sr.cpp:46-48) */
+  /* boundary flags of the mesh faces inner/outer x1, x2, x3: 0 periodic, 1 outflow,
+   * 2 reflecting (bvals/cc/outflow_cc.cpp, bvals/cc/hydro/reflect_hydro.cpp,
+   * bvals/fc/outflow_fc.cpp, bvals/fc/reflect_fc.cpp) */
+  int bc[6];
 } orc_params;
 
 typedef struct orc_mesh orc_mesh;

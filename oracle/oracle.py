@@ -33,7 +33,7 @@ class Params(ctypes.Structure):
                 ("dfloor", ctypes.c_double), ("pfloor", ctypes.c_double),
                 ("cfl_number", ctypes.c_double), ("tlim", ctypes.c_double),
                 ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
-                ("gamma_max", ctypes.c_double)]
+                ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6)]
 
 
 _lib = None
@@ -80,7 +80,7 @@ class OracleMesh:
 
     def __init__(self, mesh, gamma, xorder=2, rsolver="hlld", cfl=0.3, tlim=1e30,
                  dfloor=None, pfloor=None, relativistic=False, threads=0, sigma_max=0.0,
-                 beta_min=0.0, gamma_max=1000.0):
+                 beta_min=0.0, gamma_max=1000.0, bc=(0, 0, 0, 0, 0, 0)):
         L = lib()
         import math
         fmin = float(np.finfo(np.float32).tiny)
@@ -91,7 +91,7 @@ class OracleMesh:
                         1 if relativistic else 0, gamma,
                         floor if dfloor is None else dfloor,
                         floor if pfloor is None else pfloor, cfl, tlim, sigma_max,
-                        beta_min, gamma_max)
+                        beta_min, gamma_max, (ctypes.c_int * 6)(*bc))
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         self.h = L.orc_create(ctypes.byref(self.p), *[_p(c) for c in self.coords])
         if threads:

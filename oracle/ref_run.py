@@ -14,16 +14,27 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 
 
+BC_NAMES = {0: "periodic", 1: "outflow", 2: "reflecting"}
+
+
 def athinput(mesh, gamma, xorder, cfl, nlim, tlim, problem, extra_problem=None,
-             integrator="vl2", num_threads=1):
-    """Text of an athinput file for a uniform periodic mesh described by MeshSpec."""
-    lines = ["<job>", "problem_id = Ref", "<time>", "cfl_number = %r" % cfl,
+             integrator="vl2", num_threads=1, history_every_cycle=False,
+             bc=(0, 0, 0, 0, 0, 0)):
+    """Text of an athinput file for a uniform mesh described by MeshSpec (mesh-face
+    boundary flags bc: 0 periodic, 1 outflow, 2 reflecting);
+    history_every_cycle adds a history output (Ref.hst) written after every cycle at full
+    double precision."""
+    lines = ["<job>", "problem_id = Ref"]
+    if history_every_cycle:
+        lines += ["<output1>", "file_type = hst", "dt = 1.0e-12",
+                  "data_format = %24.16e"]
+    lines += ["<time>", "cfl_number = %r" % cfl,
              "nlim = %d" % nlim, "tlim = %r" % tlim, "integrator = %s" % integrator,
              "xorder = %s" % xorder, "ncycle_out = 100000", "<mesh>"]
     for d, n in enumerate(("1", "2", "3")):
         lines += ["nx%s = %d" % (n, mesh.nx[d]), "x%smin = %r" % (n, mesh.xmin[d]),
-                  "x%smax = %r" % (n, mesh.xmax[d]), "ix%s_bc = periodic" % n,
-                  "ox%s_bc = periodic" % n]
+                  "x%smax = %r" % (n, mesh.xmax[d]), "ix%s_bc = %s" % (n, BC_NAMES[bc[2 * d]]),
+                  "ox%s_bc = %s" % (n, BC_NAMES[bc[2 * d + 1]])]
     lines += ["num_threads = %d" % num_threads, "refinement = none", "<meshblock>"]
     for d, n in enumerate(("1", "2", "3")):
         lines.append("nx%s = %d" % (n, mesh.bx[d]))
@@ -33,6 +44,17 @@ def athinput(mesh, gamma, xorder, cfl, nlim, tlim, problem, extra_problem=None,
     for k, v in (extra_problem or {}).items():
         lines.append("%s = %s" % (k, v))
     return "\n".join(lines) + "\n"
+
+
+def read_history(path):
+    """Rows of a reference history file: list of dicts column name -> value."""
+    names, rows = None, []
+    for line in open(path):
+        if line.startswith("#") and "[1]=" in line:
+            names = [tok.split("=")[1] for tok in line[1:].split()]
+        elif line.strip() and not line.startswith("#"):
+            rows.append(dict(zip(names, (float(v) for v in line.split()))))
+    return rows
 
 
 def read_dump(path, mesh):

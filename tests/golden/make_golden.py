@@ -11,8 +11,9 @@ inputs and the reference's per-cell outputs:
 
 * ``<case>.npz``: ``ic_*`` (initial state as loaded), ``u``, ``b1``, ``b2``, ``b3``
   (per-block interiors after ``ncycle`` cycles), ``dt`` (the dt of every cycle), ``time``;
-* ``golden.json``: case parameters, and for the full config-1 linear wave the
-  reference's linearwave-errors.dat line plus a SHA-256 of its final state.
+* ``golden.json``: case parameters, for the full config-1 linear wave the reference's
+  linearwave-errors.dat line plus a SHA-256 of its final state, and the reference's
+  history output after every cycle of one case (``history``).
 """
 import hashlib
 import json
@@ -54,7 +55,15 @@ CASES = {
                                             (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
     "srkh_hlle_plm_1blk": ("srmhd_hlle_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
                                             (1., 1., 1.)), "sr_kh", 2, 0.4, 4),
+    # physical boundaries (flags inner/outer x1, x2, x3: 1 outflow, 2 reflecting)
+    "blastbc_hlld_plm_8blk": ("mhd_hlld_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                              (.5, .5, .5)), "blast", 2, 0.3, 4),
+    "blastbc_hlle_ppm_1blk": ("mhd_hlle_g3", ((16, 16, 16), (1, 1, 1), 3, (-.5, -.5, -.5),
+                                              (.5, .5, .5)), "blast", 3, 0.3, 4),
 }
+# mesh-face boundary flags of the cases that are not periodic
+BCS = {"blastbc_hlld_plm_8blk": (1, 1, 2, 2, 0, 0),
+       "blastbc_hlle_ppm_1blk": (2, 1, 1, 2, 2, 1)}
 
 
 def global_ic(problem, mesh):
@@ -106,7 +115,7 @@ def run_case(name, spec):
         u0 = mesh.scatter_cells(gu)
         b10, b20, b30 = mesh.scatter_faces(g1, g2, g3)
         text = ref_run.athinput(mesh, gamma, xorder, cfl, ncycle, 1.0e3,
-                                {"ic_file": "ic.bin"})
+                                {"ic_file": "ic.bin"}, bc=BCS.get(name, (0,) * 6))
         d, _ = ref_run.run_reference(variant, "athena_ic", text, ic=(0, gu, g1, g2, g3))
         tlim = 1.0e3
     dts = []
@@ -125,7 +134,7 @@ def run_case(name, spec):
             "relativistic": problem == "sr_kh",
             "xmin": mesh.xmin, "xmax": mesh.xmax, "problem": problem, "xorder": xorder,
             "rsolver": "hlld" if "hlld" in variant else "hlle", "cfl": cfl,
-            "ncycle": ncycle, "gamma": gamma, "tlim": tlim}
+            "ncycle": ncycle, "gamma": gamma, "tlim": tlim, "bc": list(BCS.get(name, (0,) * 6))}
 
 
 def run_config1():
@@ -146,6 +155,18 @@ def run_config1():
             "reference_zone_cycles_per_cpu_second_here": zc[-1] if zc else None}
 
 
+def run_history(name="turb_hlld_ppm_8blk"):
+    """The reference's history output (outputs/history.cpp) after every cycle of one golden
+    case, written at full double precision: pins athgpu_history."""
+    variant, margs, problem, xorder, cfl, ncycle = CASES[name]
+    mesh = MeshSpec(*margs)
+    gu, g1, g2, g3 = global_ic(problem, mesh)
+    text = ref_run.athinput(mesh, gamma_of(problem), xorder, cfl, ncycle, 1.0e3,
+                            {"ic_file": "ic.bin"}, history_every_cycle=True)
+    d, _ = ref_run.run_reference(variant, "athena_ic", text, ic=(0, gu, g1, g2, g3))
+    return {"case": name, "rows": ref_run.read_history(os.path.join(d, "Ref.hst"))}
+
+
 def main(only=None):
     for v in sorted({c[0] for c in CASES.values()}):
         build_ref.build_variant(v)
@@ -159,6 +180,9 @@ def main(only=None):
             continue
         print("case", name, flush=True)
         meta["cases"][name] = run_case(name, spec)
+    if not only or "history" in only:
+        print("history", flush=True)
+        meta["history"] = run_history()
     if not only:
         print("config1", flush=True)
         meta["config1_linear_wave"] = run_config1()
