@@ -133,6 +133,17 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "coordinate arrays are required");
   if (!(d->gamma > 1.0) || !(d->cfl_number > 0.0))
     return fail(ATHGPU_ERR_ARG, "gamma must exceed 1 and cfl_number be positive");
+  for (int f = 0; f < 6; ++f) {
+    if (d->bc[f] < ATHGPU_BC_PERIODIC || d->bc[f] > ATHGPU_BC_REFLECT)
+      return fail(ATHGPU_ERR_ARG, "bc flags must be periodic (0), outflow (1) or reflecting (2)");
+    // a periodic face pairs with a periodic face (mesh.cpp:201-220)
+    if ((d->bc[f] == ATHGPU_BC_PERIODIC) != (d->bc[f ^ 1] == ATHGPU_BC_PERIODIC))
+      return fail(ATHGPU_ERR_ARG, "periodic boundaries must be set on both faces of an axis");
+    // the boundary functions read ng cells of the block's own interior
+    const int nx = f < 2 ? d->nx1 : f < 4 ? d->nx2 : d->nx3;
+    if (d->bc[f] != ATHGPU_BC_PERIODIC && nx < d->nghost)
+      return fail(ATHGPU_ERR_ARG, "a block next to a physical boundary needs nx >= nghost");
+  }
   {
     // uniform Cartesian spacing within every block (x?rat = 1, coordinates.cpp:126-146):
     // the kernels use the reference's uniform-mesh branches (plm.cpp:103, ppm.cpp:156)
@@ -167,6 +178,11 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.ne3 = (i64)m.nc3 * (m.nc2 + 1) * (m.nc1 + 1);
   m.gamma = d->gamma; m.dfloor = d->dfloor; m.pfloor = d->pfloor;
   m.gammaf = (float)d->gamma; m.dfloorf = (float)d->dfloor; m.pfloorf = (float)d->pfloor;
+  m.any_bc = 0;
+  for (int f = 0; f < 6; ++f) {
+    m.bc[f] = d->bc[f];
+    if (d->bc[f] != ATHGPU_BC_PERIODIC) m.any_bc = 1;
+  }
   m.cfl = d->cfl_number; m.tlim = d->tlim;
   m.ncmax = m.nc1 > m.nc2 ? (m.nc1 > m.nc3 ? m.nc1 : m.nc3) : (m.nc2 > m.nc3 ? m.nc2 : m.nc3);
 
@@ -262,18 +278,29 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     m.plm32 = c->coords32 + plmoff;
   }
 
-  // neighbour table of the periodic block grid
+  // neighbour table of the block grid: periodic mesh faces wrap, across a physical mesh
+  // face there is no neighbour (-1)
   std::vector<int> hn(nb * 27);
+  const int nbx[3] = {m.nbx1, m.nbx2, m.nbx3};
   for (i64 b = 0; b < nb; ++b) {
-    int l1 = (int)(b % m.nbx1), l2 = (int)((b / m.nbx1) % m.nbx2),
-        l3 = (int)(b / ((i64)m.nbx1 * m.nbx2));
+    const int l[3] = {(int)(b % m.nbx1), (int)((b / m.nbx1) % m.nbx2),
+                      (int)(b / ((i64)m.nbx1 * m.nbx2))};
     for (int o3 = -1; o3 <= 1; ++o3)
       for (int o2 = -1; o2 <= 1; ++o2)
         for (int o1 = -1; o1 <= 1; ++o1) {
-          int a1 = (l1 + o1 + m.nbx1) % m.nbx1, a2 = (l2 + o2 + m.nbx2) % m.nbx2,
-              a3 = (l3 + o3 + m.nbx3) % m.nbx3;
+          const int o[3] = {o1, o2, o3};
+          int a[3];
+          bool none = false;
+          for (int d = 0; d < 3; ++d) {
+            int t = l[d] + o[d];
+            if (t < 0 || t >= nbx[d]) {
+              if (m.bc[2 * d + (t < 0 ? 0 : 1)] != ATHGPU_BC_PERIODIC) none = true;
+              t = (t + nbx[d]) % nbx[d];
+            }
+            a[d] = t;
+          }
           hn[b * 27 + ((o3 + 1) * 3 + (o2 + 1)) * 3 + (o1 + 1)] =
-              (a3 * m.nbx2 + a2) * m.nbx1 + a1;
+              none ? -1 : (a[2] * m.nbx2 + a[1]) * m.nbx1 + a[0];
         }
   }
   e = cudaMalloc((void**)&c->nbr, sizeof(int) * hn.size());

@@ -35,6 +35,10 @@ struct DevMesh {
   const float* dx2f32;
   const float* dx3f32;
   const float* plm32;
+  // mesh-face boundary flags (inner x1, outer x1, ..., outer x3: 0 periodic, 1 outflow,
+  // 2 reflecting); any_bc is set when one of them is not periodic
+  int bc[6];
+  int any_bc;
 };
 
 // device-resident scalars of the time integrator
@@ -644,15 +648,35 @@ __device__ __forceinline__ Real edge_avg(const DevMesh& m, const Real* __restric
   const int on = (o1 != 0) + (o2 != 0) + (o3 != 0);
   if (on == 0) return own;
   Real sum = own;
+  int count = 1;  // blocks sharing the edge: a physical mesh face contributes none
   // face neighbours in list order: x1 before x2 before x3
-  if (o1 != 0) sum += at(nbr_of(m, b, o1, 0, 0), k, j, i - o1 * m.nx1);
-  if (o2 != 0) sum += at(nbr_of(m, b, 0, o2, 0), k, j - o2 * m.nx2, i);
-  if (o3 != 0) sum += at(nbr_of(m, b, 0, 0, o3), k - o3 * m.nx3, j, i);
-  if (on == 2) {
-    sum += at(nbr_of(m, b, o1, o2, o3), k - o3 * m.nx3, j - o2 * m.nx2, i - o1 * m.nx1);
-    return sum * Real(0.25);
+  if (o1 != 0) {
+    const int nb = nbr_of(m, b, o1, 0, 0);
+    if (nb >= 0) { sum += at(nb, k, j, i - o1 * m.nx1); ++count; }
   }
-  return sum * Real(0.5);
+  if (o2 != 0) {
+    const int nb = nbr_of(m, b, 0, o2, 0);
+    if (nb >= 0) { sum += at(nb, k, j - o2 * m.nx2, i); ++count; }
+  }
+  if (o3 != 0) {
+    const int nb = nbr_of(m, b, 0, 0, o3);
+    if (nb >= 0) { sum += at(nb, k - o3 * m.nx3, j, i); ++count; }
+  }
+  if (on == 2) {
+    // an edge shared by four blocks is scaled by 1/4; along a physical mesh face by 1/count
+    // (flux_correction_fc.cpp:1477-1481)
+    const int nb = nbr_of(m, b, o1, o2, o3);
+    if (nb >= 0) {
+      sum += at(nb, k - o3 * m.nx3, j - o2 * m.nx2, i - o1 * m.nx1);
+      ++count;
+    }
+    if (count == 4) return sum * Real(0.25);
+    if (count == 1) return own;
+    return sum * (Real(1.0) / Real(count));
+  }
+  // inside a block face: halved when the face has a neighbour (flux_correction_fc.cpp:
+  // 1362-1380)
+  return count == 2 ? sum * Real(0.5) : own;
 }
 
 template <typename Real, int C>
@@ -874,7 +898,9 @@ __device__ __forceinline__ void cta_min_to_clock(Real v, DevClock* clk) {
 }
 
 // Where W(U) reads the conserved state of cell (b,k,j,i): the cell itself in the
-// interior, else the cell of the neighbour block that owns it (periodic same-level mesh).
+// interior, else the cell of the neighbour block that owns it (same-level mesh); -1 for a
+// ghost cell beyond a physical mesh face, which the boundary functions fill instead
+// (time_integrator.cpp:2206-2212 leaves those out of W(U)).
 __device__ __forceinline__ i64 src_cell(const DevMesh& m, int b, int k, int j, int i,
                                         int nvar, bool* ghost) {
   *ghost = i < m.is || i > m.ie || j < m.js || j > m.je || k < m.ks || k > m.ke;
@@ -883,7 +909,8 @@ __device__ __forceinline__ i64 src_cell(const DevMesh& m, int b, int k, int j, i
   const int si = own_map(i, m.is, m.ie, m.nx1, &o1);
   const int sj = own_map(j, m.js, m.je, m.nx2, &o2);
   const int sk = own_map(k, m.ks, m.ke, m.nx3, &o3);
-  return cidx(m, nbr_of(m, b, o1, o2, o3), 0, nvar, sk, sj, si);
+  const int sb = nbr_of(m, b, o1, o2, o3);
+  return sb < 0 ? (i64)-1 : cidx(m, sb, 0, nvar, sk, sj, si);
 }
 
 // Field::CalculateCellCenteredField (field.cpp:112-180, uniform weights) and the
@@ -966,6 +993,7 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
     const int k = (int)(r / m.nc2);
     bool ghost;
     const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
+    if (cs >= 0) {  // not a physical-boundary ghost
     const C2POne<Real> o = c2p_one<Real>(m, b, k, j, i, b1, b2, b3, u, cs, ghost);
     const i64 vs = m.ncell;
     const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
@@ -1005,6 +1033,7 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
       speed = smax<Real>(Real(0.0), (dabs(o.vz) + cf));
       dt3 /= (speed);
       cell_dt = smin<Real>(smin<Real>(dt1, dt2), dt3);
+    }
     }
   }
   if (do_dt) cta_min_to_clock<Real>(cell_dt, clk);  // reduced in the bulk precision
@@ -1171,6 +1200,7 @@ copy_ghost_prims_kernel(DevMesh m, Real* __restrict__ w, Real* __restrict__ bcc,
   bool ghost;
   const i64 s5 = src_cell(m, b, k, j, i, NHYDRO, &ghost);
   const i64 s3 = src_cell(m, b, k, j, i, 3, &ghost);
+  if (s5 < 0) return;  // filled by the boundary functions
   const i64 d5 = cidx(m, b, 0, NHYDRO, k, j, i), d3 = cidx(m, b, 0, 3, k, j, i);
   const i64 vs = m.ncell;
 #pragma unroll

@@ -3,6 +3,7 @@
 // stage_fp32.cu (FMA contraction on).
 #pragma once
 #include "ctx.h"
+#include "boundary.cuh"
 
 namespace athgpu {
 
@@ -135,6 +136,20 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
   if (overlap) {
     cudaEventRecord(c->ev_join, c->aux_stream);
     cudaStreamWaitEvent(s, c->ev_join, 0);
+  }
+  if (m.any_bc) {
+    // physical mesh faces, x1 then x2 then x3, on the primitives just written and the
+    // exchanged face field
+    ProfScope ps(c, "boundary");
+    for (int a = 0; a < 3; ++a) {
+      if (m.bc[2 * a] == 0 && m.bc[2 * a + 1] == 0) continue;
+      const long long n = bc_threads(m, a);
+      bc_fill_kernel<Real><<<nblk(n, 256), 256, 0, s>>>(m, a, wout, b1, b2, b3);
+      auto cck = c->desc.relativistic ? bc_cc_kernel<Real, true> : bc_cc_kernel<Real, false>;
+      cck<<<nblk(n, 256), 256, 0, s>>>(m, a, wout, b1, b2, b3, (Real*)c->r.bcc,
+                                       (Real*)c->r.cce);
+      c->launches += 2;
+    }
   }
   if (rotate) c->r.wsel = 1 - c->r.wsel;
   c->launches += 2;

@@ -42,7 +42,22 @@ class MeshDesc(ctypes.Structure):
                 ("x3f", ctypes.POINTER(ctypes.c_double)),
                 ("dx3f", ctypes.POINTER(ctypes.c_double)),
                 ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
-                ("gamma_max", ctypes.c_double)]
+                ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6)]
+
+
+BC_PERIODIC, BC_OUTFLOW, BC_REFLECT = 0, 1, 2
+_BC_CODES = {"periodic": BC_PERIODIC, "outflow": BC_OUTFLOW, "reflecting": BC_REFLECT}
+
+
+def bc_codes(bc):
+    """Six mesh-face boundary flags (inner x1, outer x1, ..., outer x3) as integer codes;
+    entries may be codes or the reference's names ("periodic", "outflow", "reflecting")."""
+    if bc is None:
+        return (BC_PERIODIC,) * 6
+    out = tuple(_BC_CODES[b] if isinstance(b, str) else int(b) for b in bc)
+    if len(out) != 6:
+        raise ValueError("bc needs six entries (ix1, ox1, ix2, ox2, ix3, ox3)")
+    return out
 
 
 class DeviceState(ctypes.Structure):
@@ -125,7 +140,7 @@ class StageUpdate:
 
     def __init__(self, mesh: MeshSpec, gamma, xorder=2, rsolver="hlld", precision="fp64",
                  cfl=0.3, tlim=1.0e30, dfloor=None, pfloor=None, relativistic=False,
-                 sigma_max=0.0, beta_min=0.0, gamma_max=1000.0):
+                 sigma_max=0.0, beta_min=0.0, gamma_max=1000.0, bc=None):
         L = load_library()
         self.mesh = mesh
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
@@ -142,6 +157,7 @@ class StageUpdate:
         d.dfloor = fl if dfloor is None else dfloor
         d.pfloor = fl if pfloor is None else pfloor
         d.cfl_number, d.tlim = cfl, tlim
+        d.bc = (ctypes.c_int * 6)(*bc_codes(bc))
         d.x1f, d.dx1f, d.x2f, d.dx2f, d.x3f, d.dx3f = [_dp(c) for c in self.coords]
         self.desc = d
         h = ctypes.c_void_p()

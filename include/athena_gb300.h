@@ -63,7 +63,16 @@ typedef struct {
   /* SR floors and ceiling: hydro/sigma_max, beta_min (0 = off), gamma_max (reference
    * default 1000), adiabatic_mhd_sr.cpp:46-48 */
   double sigma_max, beta_min, gamma_max;
+  /* Boundary flags of the mesh faces inner x1, outer x1, inner x2, outer x2, inner x3,
+   * outer x3 (mesh/ix1_bc ... ox3_bc): ATHGPU_BC_PERIODIC (0, the zero-initialized
+   * default), ATHGPU_BC_OUTFLOW, ATHGPU_BC_REFLECT (bvals/cc/outflow_cc.cpp,
+   * bvals/cc/hydro/reflect_hydro.cpp, bvals/fc/outflow_fc.cpp, bvals/fc/reflect_fc.cpp,
+   * applied as BoundaryValues::ApplyPhysicalBoundaries does, bvals/bvals.cpp:453-680). */
+  int bc[6];
 } athgpu_mesh_desc;
+#define ATHGPU_BC_PERIODIC 0
+#define ATHGPU_BC_OUTFLOW 1
+#define ATHGPU_BC_REFLECT 2
 
 /* Allocate all device registers of the stage update for the mesh (replaces the
  * Hydro/Field/EquationOfState/Reconstruction constructors, hydro.cpp:31-148,

@@ -28,7 +28,7 @@ def _faces(mesh, bs):
 
 def _run_gpu(mesh, c, ic, ncycle, precision="fp64"):
     g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
-                    precision=precision, cfl=c["cfl"], tlim=c["tlim"])
+                    precision=precision, cfl=c["cfl"], tlim=c["tlim"], bc=c.get("bc"))
     g.set_state(*ic)
     g.initialize()
     dts = []
@@ -215,3 +215,71 @@ def test_autotune_keeps_the_state_and_the_results():
         g.close()
     for a, b in zip(*runs):
         assert np.array_equal(a, b)
+
+
+# (ix1, ox1, ix2, ox2, ix3, ox3): 1 outflow, 2 reflecting, 0 periodic
+BC_SETS = [(1, 1, 1, 1, 1, 1), (2, 2, 2, 2, 2, 2), (2, 1, 0, 0, 1, 2), (0, 0, 2, 1, 0, 0)]
+
+
+@pytest.mark.parametrize("bc", BC_SETS)
+@pytest.mark.parametrize("xorder,rsolver,nb", [(3, "hlld", (2, 2, 2)),
+                                               (2, "hlle", (1, 2, 3))])
+def test_physical_boundaries_match_oracle_bitwise(bc, xorder, rsolver, nb):
+    """Outflow and reflecting mesh faces (ApplyPhysicalBoundaries, bvals.cpp:453-680) and
+    the EMF averaging along them: every primitive, cell-centred field and face value,
+    ghost zones included, equals the oracle's after four cycles."""
+    mesh, ic, c = _turb_case(nx=(24, 24, 24), nb=nb, xorder=xorder, rsolver=rsolver,
+                             ng=3 if xorder == 3 else 2)
+    c["bc"] = bc
+    (u, b1, b2, b3), dts, w, bcc = _run_gpu(mesh, c, ic, 4)
+    om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"],
+                      bc=bc)
+    om.set_state(*ic)
+    om.initialize()
+    odts = []
+    for _ in range(4):
+        odts.append(om.dt)
+        om.cycle()
+    uo, o1, o2, o3 = om.state()
+    wo, bcco = om.prim()
+    assert np.array_equal(dts, np.array(odts))
+    assert np.array_equal(mesh.interior(u), mesh.interior(uo))
+    assert np.array_equal(w, wo)
+    assert np.array_equal(bcc, bcco)
+    for a, b in zip((b1, b2, b3), (o1, o2, o3)):
+        assert np.array_equal(a, b)
+
+
+def test_physical_boundaries_fp32_tracks_fp64():
+    mesh, ic, c = _turb_case(nb=(2, 2, 1))
+    c["bc"] = (2, 1, 1, 2, 0, 0)
+    (u64, *_), dt64, _, _ = _run_gpu(mesh, c, ic, 5, "fp64")
+    (u32, *_), dt32, _, _ = _run_gpu(mesh, c, ic, 5, "fp32")
+    a, b = mesh.interior(u64), mesh.interior(u32)
+    for n in range(5):
+        rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(a[:, n]).mean()
+        assert rel < 2e-5, (n, rel)
+    assert np.allclose(dt32, dt64, rtol=1e-5)
+
+
+def test_physical_boundaries_launch_count():
+    """Two boundary launches per non-periodic axis after each W(U)."""
+    mesh, ic, c = _turb_case(nx=(16, 16, 16), nb=(2, 1, 1), xorder=2, ng=2)
+    g = StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlld", tlim=1e3,
+                    bc=("reflecting", "outflow", "periodic", "periodic", "outflow",
+                        "outflow"))
+    g.set_state(*ic)
+    g.initialize()
+    g.launch_count(reset=True)
+    g.cycle(3)
+    g.synchronize()
+    assert g.launch_count() / 3 == 2 * (8 + 2 * 2) + 1
+    g.close()
+
+
+def test_invalid_boundary_flags_are_rejected():
+    from athena_gb300.runtime import AthGPUError
+    mesh, ic, c = _turb_case(nx=(16, 16, 16), nb=(1, 1, 1), xorder=2, ng=2)
+    for bad in ((0, 1, 0, 0, 0, 0), (3, 3, 0, 0, 0, 0)):
+        with pytest.raises(AthGPUError):
+            StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlld", bc=bad)

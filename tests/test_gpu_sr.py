@@ -104,3 +104,33 @@ def test_sr_fp32_tracks_fp64_and_keeps_div_b():
            + b2[:, ng:ng + n3, ng + 1:ng + n2 + 1, ng:ng + n1] - b2[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
            + b3[:, ng + 1:ng + n3 + 1, ng:ng + n2, ng:ng + n1] - b3[:, ng:ng + n3, ng:ng + n2, ng:ng + n1])
     assert np.abs(div).max() / np.abs(b1).max() < 1e-13
+
+
+@pytest.mark.parametrize("bc", [(2, 2, 1, 1, 2, 1), (0, 0, 2, 2, 0, 0)])
+def test_sr_physical_boundaries_match_oracle(bc):
+    """Reflecting and outflow mesh faces on the relativistic path (the reflecting
+    function flips the normal 4-velocity): primitives with their ghost zones, interior
+    conserved state and faces equal to the oracle's within the FP64 tolerance."""
+    mesh, ic, w0, c = _sr_kh(nx=(24, 24, 24))
+    g = StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlle", cfl=c["cfl"], tlim=c["tlim"],
+                    relativistic=True, bc=bc)
+    g.set_state(*ic)
+    g.set_prim(w0)
+    g.initialize()
+    g.cycle(3)
+    (u, b1, b2, b3), (w, _) = g.state(), g.prim()
+    g.close()
+    om = O.OracleMesh(mesh, c["gamma"], xorder=2, rsolver="hlle", tlim=c["tlim"],
+                      relativistic=True, bc=bc)
+    om.set_state(*ic)
+    om.set_prim(w0)
+    om.initialize()
+    om.cycle(3)
+    uo, o1, o2, o3 = om.state()
+    wo, _ = om.prim()
+    ui, uoi = mesh.interior(u), mesh.interior(uo)
+    for n in range(5):
+        assert close(ui[:, n], uoi[:, n]), n
+        assert close(w[:, n], wo[:, n], rtol=1e-11), n
+    for a, b in zip((b1, b2, b3), (o1, o2, o3)):
+        assert close(a, b)

@@ -36,7 +36,7 @@ def test_gpu_history_matches_reference_every_cycle():
     rows = h["rows"]
     for prec, tol in (("fp64", 1e-13), ("fp32", 2e-6)):
         g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
-                        precision=prec, cfl=c["cfl"], tlim=c["tlim"])
+                        precision=prec, cfl=c["cfl"], tlim=c["tlim"], bc=c.get("bc"))
         g.set_state(*ic)
         g.initialize()
         for cyc in range(c["ncycle"] + 1):
