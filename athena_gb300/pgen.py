@@ -451,3 +451,83 @@ def sr_isolated_cells(n, seed=20261204, gamma=4.0 / 3.0, lorentz=(1.0, 10.0),
     w = np.stack([d, uvec[:, 0], uvec[:, 1], uvec[:, 2], p], axis=1)
     u = sr_prim_to_cons(w.T, bcc.T, gamma).T
     return w, bcc, u
+
+
+def blast_blocks(mesh, gamma=5.0 / 3.0, radius=0.1, pamb=1.0, damb=1.0, prat=100.0,
+                 drat=1.0, b0=1.0, angle_deg=45.0, center=(0.0, 0.0, 0.0)):
+    """The reference's blast problem generator (pgen/blast.cpp:53-213, Cartesian, no
+    ramp) evaluated on every block of a mesh with per-block coordinates (a
+    MultiLevelMesh): rho = drat*damb and p = prat*pamb inside r < radius, damb and pamb
+    outside, zero velocity, face field (b0 cos a, b0 sin a, 0), E = p/(gamma-1) + b0^2/2.
+    Returns per-block (u, b1, b2, b3), interior cells and faces set, ghosts zero."""
+    ng, (n1, n2, n3) = mesh.ng, mesh.bx
+    gm1 = gamma - 1.0
+    angle = (3.14159265358979323846 / 180.0) * angle_deg   # PI, defs.hpp.in
+    u = np.zeros((mesh.nblocks, 5) + mesh.cell_shape)
+    f = [np.zeros((mesh.nblocks,) + s) for s in mesh.face_shapes]
+    bx, by = b0 * math.cos(angle), b0 * math.sin(angle)
+    for b in range(mesh.nblocks):
+        xv = [mesh.cell_centers(b, d) for d in range(3)]
+        x = xv[0][ng:ng + n1][None, None, :] - center[0]
+        y = xv[1][ng:ng + n2][None, :, None] - center[1]
+        z = xv[2][ng:ng + n3][:, None, None] - center[2]
+        rad = np.sqrt(x * x + y * y + z * z)
+        inside = rad < radius
+        u[b, 0, ng:ng + n3, ng:ng + n2, ng:ng + n1] = np.where(inside, drat * damb, damb)
+        pres = np.where(inside, prat * pamb, pamb)
+        u[b, 4, ng:ng + n3, ng:ng + n2, ng:ng + n1] = pres / gm1 + 0.5 * b0 * b0
+        f[0][b, ng:ng + n3, ng:ng + n2, ng:ng + n1 + 1] = bx
+        f[1][b, ng:ng + n3, ng:ng + n2 + 1, ng:ng + n1] = by
+    return u, f[0], f[1], f[2]
+
+
+def smooth_blocks(mesh, gamma=5.0 / 3.0, seed=7, amp=0.2):
+    """A smooth non-uniform MHD state on every block of a mesh with per-block
+    coordinates: density, pressure and velocity with a few random-phase Fourier modes of
+    the cell-centre position, and a face field sampled from a smooth analytic field at
+    the face centres.  Per-block (u, b1, b2, b3), interior cells and faces set."""
+    rng = np.random.default_rng(seed)
+    ng, (n1, n2, n3) = mesh.ng, mesh.bx
+    L = [mesh.xmax[d] - mesh.xmin[d] for d in range(3)]
+    modes = []
+    for _ in range(4):
+        k = rng.integers(1, 3, size=3) * 2.0 * np.pi / np.array(L)
+        modes.append((k, rng.uniform(0, 2 * np.pi), rng.normal(size=8)))
+
+    def field(x, y, z, c):
+        out = 0.0
+        for k, ph, a in modes:
+            out = out + a[c] * np.sin(k[0] * x + k[1] * y + k[2] * z + ph)
+        return out
+
+    u = np.zeros((mesh.nblocks, 5) + mesh.cell_shape)
+    f = [np.zeros((mesh.nblocks,) + s) for s in mesh.face_shapes]
+    for b in range(mesh.nblocks):
+        xf = [mesh._faces(b, d, False)[0] for d in range(3)]
+        xv = [0.5 * (xf[d][1:] + xf[d][:-1]) for d in range(3)]
+        x = xv[0][ng:ng + n1][None, None, :]
+        y = xv[1][ng:ng + n2][:, None][None]
+        z = xv[2][ng:ng + n3][:, None, None]
+        rho = 1.0 + amp * field(x, y, z, 0) * 0.3
+        p = 1.0 + amp * field(x, y, z, 1) * 0.3
+        v = [amp * field(x, y, z, 2 + c) for c in range(3)]
+        # face fields at face centres: x1 faces at (x1f, x2v, x3v), ...
+        fx = [xf[0][ng:ng + n1 + 1][None, None, :], y, z]
+        b1 = 1.0 + amp * field(fx[0], fx[1], fx[2], 5)
+        fy = [x, xf[1][ng:ng + n2 + 1][None, :, None], z]
+        b2 = 0.5 + amp * field(fy[0], fy[1], fy[2], 6)
+        fz = [x, y, xf[2][ng:ng + n3 + 1][:, None, None]]
+        b3 = 0.25 + amp * field(fz[0], fz[1], fz[2], 7)
+        f[0][b, ng:ng + n3, ng:ng + n2, ng:ng + n1 + 1] = b1
+        f[1][b, ng:ng + n3, ng:ng + n2 + 1, ng:ng + n1] = b2
+        f[2][b, ng:ng + n3 + 1, ng:ng + n2, ng:ng + n1] = b3
+        bc1 = 0.5 * (b1[:, :, 1:] + b1[:, :, :-1])
+        bc2 = 0.5 * (b2[:, 1:, :] + b2[:, :-1, :])
+        bc3 = 0.5 * (b3[1:] + b3[:-1])
+        sl = (b, slice(None), slice(ng, ng + n3), slice(ng, ng + n2), slice(ng, ng + n1))
+        u[sl][0] = rho
+        for c in range(3):
+            u[sl][1 + c] = rho * v[c]
+        u[sl][4] = p / (gamma - 1.0) + 0.5 * rho * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2) + \
+            0.5 * (bc1 ** 2 + bc2 ** 2 + bc3 ** 2)
+    return u, f[0], f[1], f[2]

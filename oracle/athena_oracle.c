@@ -11,6 +11,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -39,7 +40,17 @@ struct orc_mesh {
   long ne1, ne2, ne3;
   double dt, time;
   long c2p_fail;
+  /* multi-level mesh (athena_oracle_ml.c), NULL for a uniform mesh */
+  struct orc_ml *ml;
+  const int *ml_nblev;  /* its [nb][27] neighbour-level table */
+  int rk1;              /* integrator = rk1 (multi-level meshes; diagnostics) */
 };
+
+struct orc_ml;
+static void ml_stage(orc_mesh *m, int stage);
+static void ml_stage_w(orc_mesh *m, double beta, double delta, int order);
+static void ml_initialize(orc_mesh *m);
+static void ml_free(struct orc_ml *ml, int nb);
 
 /* ------------------------------------------------------------------------------------
  * indexing helpers (athena_arrays.hpp:140-143)
@@ -796,6 +807,13 @@ static int nbr_block(const orc_mesh *m, int b, int o1, int o2, int o3) {
   return (l[2] * n[1] + l[1]) * n[0] + l[0];
 }
 
+/* is there a block (or a periodic image) across offset (o1, o2, o3) of block b? */
+static int has_nbr(const orc_mesh *m, int b, int o1, int o2, int o3) {
+  if (m->ml_nblev)
+    return m->ml_nblev[(long)b * 27 + (o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)] != -1;
+  return nbr_block(m, b, o1, o2, o3) >= 0;
+}
+
 /* corrected value of edge component c (0,1,2 = e1,e2,e3) at (k,j,i) of block b */
 static double emf_corrected(const orc_mesh *m, int b, int c, int k, int j, int i) {
   const double *E = (c == 0) ? m->e1 : (c == 1) ? m->e2 : m->e3;
@@ -965,12 +983,12 @@ static long con2prim(orc_mesh *m, int b, double *u, double *prim) {
    * 2206-2212, mesh.cpp:1820-1831); ghosts on physical boundaries come from the boundary
    * functions instead */
   int ng = m->p.ng;
-  int il = m->is - (nbr_block(m, b, -1, 0, 0) >= 0 ? ng : 0);
-  int iu = m->ie + (nbr_block(m, b, 1, 0, 0) >= 0 ? ng : 0);
-  int jl = m->js - (nbr_block(m, b, 0, -1, 0) >= 0 ? ng : 0);
-  int ju = m->je + (nbr_block(m, b, 0, 1, 0) >= 0 ? ng : 0);
-  int kl = m->ks - (nbr_block(m, b, 0, 0, -1) >= 0 ? ng : 0);
-  int ku = m->ke + (nbr_block(m, b, 0, 0, 1) >= 0 ? ng : 0);
+  int il = m->is - (has_nbr(m, b, -1, 0, 0) ? ng : 0);
+  int iu = m->ie + (has_nbr(m, b, 1, 0, 0) ? ng : 0);
+  int jl = m->js - (has_nbr(m, b, 0, -1, 0) ? ng : 0);
+  int ju = m->je + (has_nbr(m, b, 0, 1, 0) ? ng : 0);
+  int kl = m->ks - (has_nbr(m, b, 0, 0, -1) ? ng : 0);
+  int ku = m->ke + (has_nbr(m, b, 0, 0, 1) ? ng : 0);
   cell_centered_field(m, b, il, iu, jl, ju, kl, ku);
   if (m->p.relativistic) return sr_c2p_block(m, b, u, prim, il, iu, jl, ju, kl, ku);
   const double *bcc = m->bcc + (long)b * 3 * m->ncell;
@@ -1457,6 +1475,7 @@ orc_mesh *orc_create(const orc_params *p, const double *x1f, const double *dx1f,
 
 void orc_destroy(orc_mesh *m) {
   if (!m) return;
+  ml_free(m->ml, m->nb);
   free(m->u); free(m->u1); free(m->w); free(m->w1); free(m->bcc); free(m->b1);
   free(m->b2); free(m->b3); free(m->bb1); free(m->bb2); free(m->bb3); free(m->x1f);
   free(m->x2f); free(m->x3f); free(m->dx1f); free(m->dx2f); free(m->dx3f);
@@ -1521,7 +1540,7 @@ static void apply_bcs(orc_mesh *m, int b, double *w) {
   for (int f = 0; f < 6; ++f) {
     int o[3] = {0, 0, 0};
     o[f / 2] = (f & 1) ? 1 : -1;
-    has[f] = nbr_block(m, b, o[0], o[1], o[2]) >= 0;
+    has[f] = has_nbr(m, b, o[0], o[1], o[2]);
   }
   double *wb = w + (long)b * NHYDRO * m->ncell;
   double *fb[3] = {m->b1 + (long)b * m->nf1, m->b2 + (long)b * m->nf2,
@@ -1642,6 +1661,7 @@ static void all_new_dt(orc_mesh *m) {
 }
 
 void orc_initialize(orc_mesh *m) {
+  if (m->ml) { ml_initialize(m); return; }
   /* Mesh::Initialize: boundaries (mesh.cpp:1698-1725), W(U) into w over the whole block
    * (mesh.cpp:1833), NewBlockTimeStep + NewTimeStep (mesh.cpp:1959-1964) */
   exchange(m, m->u, NHYDRO, m->b1, m->b2, m->b3);
@@ -1657,6 +1677,7 @@ void orc_initialize(orc_mesh *m) {
  * averaging, IntegrateHydro/IntegrateField with the register swaps, ghost exchange,
  * Primitives (W(U) into w1 then swap), NewBlockTimeStep on the last stage. */
 void orc_stage(orc_mesh *m, int stage) {
+  if (m->ml) { ml_stage(m, stage); return; }
   const double beta = (stage == 1) ? 0.5 : 1.0;      /* time_integrator.cpp:216-217 */
   const double delta = (stage == 1) ? 1.0 : 0.0;     /* :228-236 */
   const int order = (stage == 1) ? 1 : m->p.xorder;  /* :1700-1703 */
@@ -1724,8 +1745,16 @@ void orc_stage(orc_mesh *m, int stage) {
 }
 
 void orc_cycle(orc_mesh *m) {
+  if (m->rk1) {  /* integrator = rk1: one stage, beta = delta = 1, order xorder */
+    ml_stage_w(m, 1.0, 1.0, m->p.xorder);
+    m->time += m->dt;
+    all_new_dt(m);
+    return;
+  }
   orc_stage(m, 1);
   orc_stage(m, 2);
   m->time += m->dt;  /* main.cpp:535 */
   all_new_dt(m);     /* NewBlockTimeStep (last stage) + Mesh::NewTimeStep */
 }
+
+#include "athena_oracle_ml.c"

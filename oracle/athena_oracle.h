@@ -67,6 +67,21 @@ void orc_stage(orc_mesh *m, int stage);
 /* counts of cells that hit the SR fallback in the last W(U) call */
 long orc_c2p_failures(const orc_mesh *m);
 
+/* Turn the mesh into a multi-level one (SMR/AMR; Newtonian MHD, even NGHOST): the
+ * blocks (p.nbx1 of them, p.nbx2 = p.nbx3 = 1) in the reference's gid order with, per
+ * block, its neighbour list nbr_table[b][56][10] (gid, level, ox1, ox2, ox3, type 0 face /
+ * 1 edge / 2 corner, fi1, fi2, fid, eid), nbr_count[b], the 3x3x3 neighbour levels
+ * nblevel[b][27] (-1: none), loc[b][4] (level, lx1, lx2, lx3) and the coarse-buffer face
+ * coordinates cx?f[b][ncc+1], cdx?f[b][ncc] (ncc = nx/2 + 2 NGHOST).  Returns 0, or <0
+ * for an unsupported configuration. */
+int orc_set_multilevel(orc_mesh *m, const int *nbr_table, const int *nbr_count,
+                       const int *nblevel, const long long *loc, const double *cx1f,
+                       const double *cdx1f, const double *cx2f, const double *cdx2f,
+                       const double *cx3f, const double *cdx3f);
+
+/* use the one-stage rk1 integrator in orc_cycle (multi-level meshes; diagnostics) */
+void orc_set_rk1(orc_mesh *m, int on);
+
 /* per-cell SR conserved->primitive (adiabatic_mhd_sr.cpp:404-522) on independent
  * cells: cons[n][5] (D, E, M1..M3 in the reference's IDN,IEN,IM1..IM3 slots), bcc[n][3],
  * guess pgas[n]; out prim[n][5] and iterations[n] (-1 = not converged). */

@@ -12,8 +12,11 @@ itself without touching the tree:
 * it compiles the same source list as ``Makefile.in:29-75`` with ``g++ -O3 -std=c++11``
   (the flags configure.py uses for g++, configure.py:560-566) straight from the
   reference's ``src/`` into ``oracle/_ref/<variant>/obj`` and links two executables:
-  ``athena_lw`` (the reference's own ``pgen/linear_wave.cpp``) and ``athena_ic``
-  (``oracle/ref_pgen/load_ic.cpp``), both with ``oracle/ref_pgen/dump_hook.cpp``.
+  ``athena_lw`` (the reference's own ``pgen/linear_wave.cpp``), ``athena_blast`` (its
+  own ``pgen/blast.cpp``, used for the multi-level cases), ``athena_ic``
+  (``oracle/ref_pgen/load_ic.cpp``) and ``athena_blocks``
+  (``oracle/ref_pgen/load_blocks.cpp``, per-block initial states of multi-level meshes),
+  all with ``oracle/ref_pgen/dump_hook.cpp``.
 
 Nothing is copied out of the reference tree; all outputs go under ``oracle/_ref/``.
 Usage: ``python oracle/build_ref.py [variant ...]`` (default: all variants).
@@ -35,6 +38,7 @@ VARIANTS = {
     "mhd_hlld_g3": ("hlld", 3, False),
     "mhd_hlle_g2": ("hlle", 2, False),
     "mhd_hlle_g3": ("hlle", 3, False),
+    "mhd_hlld_g4": ("hlld", 4, False),   # PPM with mesh refinement (even NGHOST)
     "srmhd_hlle_g2": ("hlle", 2, True),
 }
 
@@ -126,7 +130,9 @@ def build_variant(name, jobs=None):
     srcs = source_list(flux, sr)
     extra = {"dump_hook": os.path.join(HERE, "ref_pgen/dump_hook.cpp"),
              "load_ic": os.path.join(HERE, "ref_pgen/load_ic.cpp"),
-             "linear_wave": os.path.join(REF, "src/pgen/linear_wave.cpp")}
+             "linear_wave": os.path.join(REF, "src/pgen/linear_wave.cpp"),
+             "blast": os.path.join(REF, "src/pgen/blast.cpp"),
+             "load_blocks": os.path.join(HERE, "ref_pgen/load_blocks.cpp")}
 
     def objname(src):
         rel = os.path.relpath(src, REF).replace("/", "_") if src.startswith(REF) else \
@@ -144,8 +150,9 @@ def build_variant(name, jobs=None):
     with ThreadPoolExecutor(jobs or os.cpu_count()) as ex:
         objs = list(ex.map(compile_one, srcs))
         eobj = dict(zip(extra, ex.map(compile_one, extra.values())))
-    for exe, pg in (("athena_lw", "linear_wave"), ("athena_ic", "load_ic")):
-        if sr and pg == "linear_wave":
+    for exe, pg in (("athena_lw", "linear_wave"), ("athena_ic", "load_ic"),
+                    ("athena_blast", "blast"), ("athena_blocks", "load_blocks")):
+        if sr and pg in ("linear_wave", "blast", "load_blocks"):
             continue
         run(cxx + ["-o", os.path.join(vdir, exe)] + objs + [eobj[pg], eobj["dump_hook"]])
     return vdir

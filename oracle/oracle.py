@@ -15,8 +15,9 @@ SRC = os.path.join(HERE, "athena_oracle.c")
 
 def build(force=False):
     """Compile liboracle.so (plain C, no FMA contraction, OpenMP over MeshBlocks)."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "athena_oracle.h"))):
+    deps = [SRC, os.path.join(HERE, "athena_oracle.h"), os.path.join(HERE, "athena_oracle_ml.c")]
+    if not force and os.path.exists(LIB) and \
+            os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
            "-o", LIB + ".tmp", SRC, "-lm"]
@@ -67,6 +68,11 @@ def lib():
         L.orc_sr_c2p_cells.argtypes = [ctypes.c_long, ctypes.c_double, ctypes.c_double,
                                        dp, dp, dp, dp, ctypes.POINTER(ctypes.c_int)]
         L.orc_sr_prim_to_cons.argtypes = [ctypes.c_long, ctypes.c_double, dp, dp, dp]
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.orc_set_multilevel.argtypes = [ctypes.c_void_p, ip, ip, ip,
+                                         ctypes.POINTER(ctypes.c_longlong)] + [dp] * 6
+        L.orc_set_multilevel.restype = ctypes.c_int
+        L.orc_set_rk1.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -86,7 +92,11 @@ class OracleMesh:
         fmin = float(np.finfo(np.float32).tiny)
         floor = math.sqrt(1024 * fmin)   # adiabatic_mhd.cpp:29-30
         self.mesh = mesh
-        self.p = Params(mesh.nb[0], mesh.nb[1], mesh.nb[2], mesh.bx[0], mesh.bx[1],
+        multilevel = hasattr(mesh, "neighbor_table")
+        if multilevel:
+            bc = mesh.bcs
+        nbl = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
+        self.p = Params(nbl[0], nbl[1], nbl[2], mesh.bx[0], mesh.bx[1],
                         mesh.bx[2], mesh.ng, xorder, 0 if rsolver == "hlld" else 1,
                         1 if relativistic else 0, gamma,
                         floor if dfloor is None else dfloor,
@@ -94,6 +104,18 @@ class OracleMesh:
                         beta_min, gamma_max, (ctypes.c_int * 6)(*bc))
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         self.h = L.orc_create(ctypes.byref(self.p), *[_p(c) for c in self.coords])
+        if multilevel:
+            t, cnt, lv, loc = mesh.neighbor_table()
+            self._ml = [np.ascontiguousarray(a) for a in (t, cnt, lv, loc)]
+            self._cc = [np.ascontiguousarray(c) for c in mesh.coarse_coordinate_arrays()]
+            ip = ctypes.POINTER(ctypes.c_int)
+            rc = L.orc_set_multilevel(
+                self.h, self._ml[0].ctypes.data_as(ip), self._ml[1].ctypes.data_as(ip),
+                self._ml[2].ctypes.data_as(ip),
+                self._ml[3].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                *[_p(c) for c in self._cc])
+            if rc != 0:
+                raise ValueError("unsupported multi-level configuration (%d)" % rc)
         if threads:
             L.orc_num_threads(threads)
 

@@ -11,6 +11,8 @@ inputs and the reference's per-cell outputs:
 
 * ``<case>.npz``: ``ic_*`` (initial state as loaded), ``u``, ``b1``, ``b2``, ``b3``
   (per-block interiors after ``ncycle`` cycles), ``dt`` (the dt of every cycle), ``time``;
+  the multi-level cases (``ml_cases``: static refinement regions, blocks in the
+  reference's gid order) the same;
 * ``golden.json``: case parameters, for the full config-1 linear wave the reference's
   linearwave-errors.dat line plus a SHA-256 of its final state, and the reference's
   history output after every cycle of one case (``history``).
@@ -64,6 +66,74 @@ CASES = {
 # mesh-face boundary flags of the cases that are not periodic
 BCS = {"blastbc_hlld_plm_8blk": (1, 1, 2, 2, 0, 0),
        "blastbc_hlle_ppm_1blk": (2, 1, 1, 2, 2, 1)}
+
+
+# multi-level (static refinement) cases: variant, MultiLevelMesh args (nx, nrbx, ng,
+# xmin, xmax, bcs, regions), problem, problem parameters, xorder, cfl, ncycle
+ML_CASES = {
+    "mlblast_hlle_plm": ("mhd_hlle_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                         (.5, .5, .5), (1, 1, 2, 2, 0, 0),
+                                         [((0.1, 0.1, 0.1), (0.2, 0.2, 0.2), 1)]),
+                         "blast", {"radius": 0.15, "pamb": 0.1, "prat": 100.0, "b0": 1.0,
+                                   "angle": 45.0, "x1_0": 0.25, "x2_0": 0.25,
+                                   "x3_0": 0.25}, 2, 0.3, 6),
+    "mlsmooth_hlld_ppm": ("mhd_hlld_g4", ((16, 16, 16), (2, 2, 2), 4, (-.5, -.5, -.5),
+                                          (.5, .5, .5), (0, 0, 0, 0, 0, 0),
+                                          [((-0.4, -0.4, -0.4), (-0.3, -0.3, -0.3), 1)]),
+                          "smooth", {"seed": 7}, 3, 0.3, 4),
+    "mlsmooth3_hlle_plm": ("mhd_hlle_g2", ((8, 8, 8), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                           (.5, .5, .5), (1, 1, 2, 2, 1, 1),
+                                           [((0.3, 0.3, 0.3), (0.35, 0.35, 0.35), 2)]),
+                           "smooth", {"seed": 11}, 2, 0.3, 4),
+}
+
+
+def ml_mesh(margs):
+    from athena_gb300.meshtree import MultiLevelMesh
+    nx, nrbx, ng, xmin, xmax, bcs, regions = margs
+    return MultiLevelMesh(nx, nrbx, ng, xmin, xmax, bcs=bcs, regions=regions)
+
+
+def run_ml_case(name, spec):
+    """A multi-level case through the reference (static refinement regions): the blast
+    problem through the reference's own pgen/blast.cpp, smooth states through
+    oracle/ref_pgen/load_blocks.cpp.  Stores the initial state as this package generates
+    it (pgen.blast_blocks restates blast.cpp), the reference's interiors after ncycle
+    cycles and every cycle's dt."""
+    variant, margs, problem, prob, xorder, cfl, ncycle = spec
+    mesh = ml_mesh(margs)
+    gamma = 5.0 / 3.0
+    regions = margs[6]
+    if problem == "blast":
+        ic = pgen.blast_blocks(mesh, gamma, radius=prob["radius"], pamb=prob["pamb"],
+                               prat=prob["prat"], b0=prob["b0"], angle_deg=prob["angle"],
+                               center=(prob["x1_0"], prob["x2_0"], prob["x3_0"]))
+        text = ref_run.athinput_multilevel(mesh, gamma, xorder, cfl, ncycle, 1.0e3, prob,
+                                           regions=regions)
+        d, _ = ref_run.run_reference(variant, "athena_blast", text)
+    else:
+        ic = pgen.smooth_blocks(mesh, gamma, seed=prob["seed"])
+        text = ref_run.athinput_multilevel(mesh, gamma, xorder, cfl, ncycle, 1.0e3,
+                                           {"ic_file": "ic.bin"}, regions=regions)
+        d, _ = ref_run.run_reference(variant, "athena_blocks", text, blocks_ic=(mesh,) + ic)
+    dts = []
+    for c in range(1, ncycle + 1):
+        dump = ref_run.read_dump_blocks(os.path.join(d, "dump.%05d.bin" % c))
+        assert dump["locs"] == [(l.level, l.lx1, l.lx2, l.lx3) for l in mesh.locs]
+        dts.append(dump["dt"])
+    fi = mesh.interior_faces
+    u0, b10, b20, b30 = ic
+    np.savez_compressed(
+        os.path.join(OUT, name + ".npz"),
+        ic_u=mesh.interior(u0), ic_b1=fi(b10), ic_b2=fi(b20), ic_b3=fi(b30),
+        u=mesh.interior(dump["u"]), b1=fi(dump["b1"]), b2=fi(dump["b2"]), b3=fi(dump["b3"]),
+        w=mesh.interior(dump["w"]), dt=np.array(dts), time=dump["time"])
+    nx, nrbx, ng, xmin, xmax, bcs, regs = margs
+    return {"variant": variant, "nx": nx, "nrbx": nrbx, "ng": ng, "xmin": xmin,
+            "xmax": xmax, "bc": list(bcs), "regions": regs, "nblocks": mesh.nblocks,
+            "levels": sorted(set(int(v) for v in mesh.levels)), "problem": problem,
+            "xorder": xorder, "rsolver": "hlld" if "hlld" in variant else "hlle",
+            "cfl": cfl, "ncycle": ncycle, "gamma": gamma, "tlim": 1.0e3}
 
 
 def global_ic(problem, mesh):
@@ -168,7 +238,7 @@ def run_history(name="turb_hlld_ppm_8blk"):
 
 
 def main(only=None):
-    for v in sorted({c[0] for c in CASES.values()}):
+    for v in sorted({c[0] for c in CASES.values()} | {c[0] for c in ML_CASES.values()}):
         build_ref.build_variant(v)
     meta = {"cases": {}}
     path = os.path.join(OUT, "golden.json")
@@ -180,6 +250,12 @@ def main(only=None):
             continue
         print("case", name, flush=True)
         meta["cases"][name] = run_case(name, spec)
+    meta.setdefault("ml_cases", {})
+    for name, spec in ML_CASES.items():
+        if only and name not in only:
+            continue
+        print("case", name, flush=True)
+        meta["ml_cases"][name] = run_ml_case(name, spec)
     if not only or "history" in only:
         print("history", flush=True)
         meta["history"] = run_history()

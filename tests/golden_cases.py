@@ -52,3 +52,36 @@ def load_case(name):
 def interior_faces(mesh, b):
     ng = mesh.ng
     return b[:, ng:-ng, ng:-ng, ng:-ng]
+
+
+def ml_case_names():
+    """Names of the multi-level (static refinement) golden cases."""
+    return sorted(meta().get("ml_cases", {}))
+
+
+def load_ml_case(name):
+    """(params, MultiLevelMesh, initial state (u, b1, b2, b3) with ghosts zero,
+    reference outputs)."""
+    from athena_gb300.meshtree import MultiLevelMesh
+    c = meta()["ml_cases"][name]
+    mesh = MultiLevelMesh(tuple(c["nx"]), tuple(c["nrbx"]), c["ng"], tuple(c["xmin"]),
+                          tuple(c["xmax"]), bcs=tuple(c["bc"]),
+                          regions=[(tuple(a), tuple(b), lv) for a, b, lv in c["regions"]])
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ng = mesh.ng
+
+    def pad_cells(a):
+        out = np.zeros((mesh.nblocks, a.shape[1]) + mesh.cell_shape)
+        out[:, :, ng:-ng, ng:-ng, ng:-ng] = a
+        return out
+
+    def pad_faces(a, d):
+        out = np.zeros((mesh.nblocks,) + mesh.face_shapes[d])
+        out[:, ng:-ng, ng:-ng, ng:-ng] = a
+        return out
+
+    ic = (pad_cells(z["ic_u"]), pad_faces(z["ic_b1"], 0), pad_faces(z["ic_b2"], 1),
+          pad_faces(z["ic_b3"], 2))
+    ref = {k: z[k] for k in ("u", "b1", "b2", "b3", "w", "dt")}
+    ref["time"] = float(z["time"])
+    return c, mesh, ic, ref
