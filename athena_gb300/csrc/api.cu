@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "ctx.h"
+#include "ml_plan.h"
 
 using namespace athgpu;
 
@@ -54,6 +55,9 @@ void free_all(athgpu_ctx* c) {
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
                   c->nbr, c->staging, c->c2p_queue, c->c2p_qcount};
   for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->fxv) cudaFree(c->fxv);
+  for (void* p : c->mld.allocs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   if (c->cycle_exec) cudaGraphExecDestroy(c->cycle_exec);
@@ -278,6 +282,21 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     m.plm32 = c->coords32 + plmoff;
   }
 
+  {  // cell centres x?v = (x?f(c+1) + x?f(c))/2 per block (cartesian.cpp:26-28)
+    std::vector<double> hv(nb * (m.nc1 + m.nc2 + m.nc3));
+    i64 o = 0;
+    for (int dd = 0; dd < 3; ++dd)
+      for (i64 b = 0; b < nb; ++b)
+        for (int cc = 0; cc < nc[dd]; ++cc) {
+          const double* f = xf[dd] + b * (nc[dd] + 1);
+          hv[o++] = 0.5 * (f[cc + 1] + f[cc]);
+        }
+    e = cudaMalloc((void**)&c->fxv, sizeof(double) * hv.size());
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc fxv"));
+    e = cudaMemcpy(c->fxv, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy fxv"));
+  }
+
   // neighbour table of the block grid: periodic mesh faces wrap, across a physical mesh
   // face there is no neighbour (-1)
   std::vector<int> hn(nb * 27);
@@ -321,6 +340,145 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "create sync"));
   *out = c;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
+                                    const int* nbr_count, const int* nblevel,
+                                    const long long* loc, const double* cx1f,
+                                    const double* cdx1f, const double* cx2f,
+                                    const double* cdx2f, const double* cx3f,
+                                    const double* cdx3f) {
+  if (!c || !nbr_table || !nbr_count || !nblevel || !loc || !cx1f || !cx2f || !cx3f)
+    return fail(ATHGPU_ERR_ARG, "null argument");
+  (void)cdx1f; (void)cdx2f; (void)cdx3f;
+  if (c->initialized || c->m.ml.on)
+    return fail(ATHGPU_ERR_STATE, "athgpu_set_multilevel must come before athgpu_initialize");
+  if (c->desc.relativistic)
+    return fail(ATHGPU_ERR_UNSUPPORTED, "mesh refinement supports Newtonian MHD only");
+  DevMesh& m = c->m;
+  if (m.ng % 2)
+    return fail(ATHGPU_ERR_ARG, "mesh refinement needs an even nghost (mesh_refinement.cpp:44)");
+  if (m.nx1 % 2 || m.nx2 % 2 || m.nx3 % 2 || m.nx1 / 2 < 2 || m.nx2 / 2 < 2 || m.nx3 / 2 < 2)
+    return fail(ATHGPU_ERR_ARG, "mesh refinement needs even MeshBlock sizes of at least 4");
+  const int nb = m.nb;
+  MlDims dims;
+  dims.nx[0] = m.nx1; dims.nx[1] = m.nx2; dims.nx[2] = m.nx3;
+  dims.ng = m.ng;
+  for (int f = 0; f < 6; ++f) dims.bc[f] = m.bc[f];
+  MlPlan plan;
+  std::string err;
+  if (!build_ml_plan(dims, nb, nbr_table, nbr_count, nblevel, loc, &plan, &err))
+    return fail(ATHGPU_ERR_ARG, err.c_str());
+  auto& al = c->mld.allocs;
+  auto dev = [&](const void* h, size_t bytes, void** out) -> cudaError_t {
+    *out = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e != cudaSuccess) return e;
+    al.push_back(*out);
+    if (h) return cudaMemcpy(*out, h, bytes, cudaMemcpyHostToDevice);
+    return cudaMemsetAsync(*out, 0, bytes, c->stream);
+  };
+  DevML& L = m.ml;
+  const int rb = c->real_bytes;
+  const int cng = (m.ng + 1) / 2 + 1;
+  L.cng = cng;
+  L.ncc1 = m.nx1 / 2 + 2 * m.ng; L.ncc2 = m.nx2 / 2 + 2 * m.ng; L.ncc3 = m.nx3 / 2 + 2 * m.ng;
+  L.cis = m.ng; L.cie = m.ng + m.nx1 / 2 - 1;
+  L.cjs = m.ng; L.cje = m.ng + m.nx2 / 2 - 1;
+  L.cks = m.ng; L.cke = m.ng + m.nx3 / 2 - 1;
+  L.nccell = (i64)L.ncc1 * L.ncc2 * L.ncc3;
+  L.ncf1 = (i64)L.ncc3 * L.ncc2 * (L.ncc1 + 1);
+  L.ncf2 = (i64)L.ncc3 * (L.ncc2 + 1) * L.ncc1;
+  L.ncf3 = (i64)(L.ncc3 + 1) * L.ncc2 * L.ncc1;
+  const int nfa = m.nx2 * m.nx3, nfb = m.nx1 * m.nx3, nfc = m.nx1 * m.nx2;
+  L.nfmax = nfa > nfb ? (nfa > nfc ? nfa : nfc) : (nfb > nfc ? nfb : nfc);
+  // coarse cell centres from the coarse face coordinates
+  std::vector<double> cxv[3];
+  const double* cxf[3] = {cx1f, cx2f, cx3f};
+  const int ncc[3] = {L.ncc1, L.ncc2, L.ncc3};
+  for (int d = 0; d < 3; ++d) {
+    cxv[d].resize((size_t)nb * ncc[d]);
+    for (int b = 0; b < nb; ++b)
+      for (int q = 0; q < ncc[d]; ++q)
+        cxv[d][(size_t)b * ncc[d] + q] = 0.5 * (cxf[d][(size_t)b * (ncc[d] + 1) + q + 1] +
+                                                 cxf[d][(size_t)b * (ncc[d] + 1) + q]);
+  }
+  void* p;
+#define DEV(h, bytes, field) \
+  do { cudaError_t e_ = dev(h, bytes, &p); if (e_ != cudaSuccess) return cuda_fail(e_, "multi-level allocation"); field = (decltype(field))p; } while (0)
+  const void* nullh = nullptr;
+  DEV(nblevel, sizeof(int) * (size_t)nb * 27, L.nblev);
+  DEV(nbr_table, sizeof(int) * (size_t)nb * ML_MAXNB * ML_NF, L.nbrt);
+  DEV(nbr_count, sizeof(int) * (size_t)nb, L.nnbr);
+  DEV(plan.eflag.data(), sizeof(int) * plan.eflag.size(), L.eflag);
+  DEV(plan.nfine.data(), sizeof(int) * plan.nfine.size(), L.nfine);
+  DEV(plan.fmask.data(), sizeof(int) * plan.fmask.size(), L.fmask);
+  DEV(plan.level.data(), sizeof(int) * plan.level.size(), L.level);
+  DEV(nullh, (size_t)nb * 5 * L.nccell * rb, L.ccons);
+  DEV(nullh, (size_t)nb * 5 * L.nccell * rb, L.cprim);
+  DEV(nullh, (size_t)nb * 3 * L.nccell * rb, L.cbcc);
+  DEV(nullh, (size_t)nb * 5 * L.nccell * rb, L.scons);
+  DEV(nullh, (size_t)nb * L.ncf1 * 8, L.cb1);
+  DEV(nullh, (size_t)nb * L.ncf2 * 8, L.cb2);
+  DEV(nullh, (size_t)nb * L.ncf3 * 8, L.cb3);
+  DEV(nullh, (size_t)nb * L.ncf1 * 8, L.sb1);
+  DEV(nullh, (size_t)nb * L.ncf2 * 8, L.sb2);
+  DEV(nullh, (size_t)nb * L.ncf3 * 8, L.sb3);
+  DEV(cxv[0].data(), sizeof(double) * cxv[0].size(), L.cx1v);
+  DEV(cxv[1].data(), sizeof(double) * cxv[1].size(), L.cx2v);
+  DEV(cxv[2].data(), sizeof(double) * cxv[2].size(), L.cx3v);
+  L.fx1v = c->fxv;
+  L.fx2v = c->fxv + (size_t)nb * m.nc1;
+  L.fx3v = c->fxv + (size_t)nb * (m.nc1 + m.nc2);
+  DEV(nullh, (size_t)nb * 6 * L.nfmax * 5 * rb, L.fcorr);
+  DEV(nullh, (size_t)nb * m.ne1 * rb, L.ecorr1);
+  DEV(nullh, (size_t)nb * m.ne2 * rb, L.ecorr2);
+  DEV(nullh, (size_t)nb * m.ne3 * rb, L.ecorr3);
+  MlOpList* lists[3] = {&plan.r, &plan.x, &plan.p};
+  for (int ph = 0; ph < 3; ++ph) {
+    c->mld.nblk[ph] = (int)lists[ph]->blk.size();
+    DEV(lists[ph]->ops.data(), sizeof(MlOp) * lists[ph]->ops.size(), c->mld.ops[ph]);
+    DEV(lists[ph]->off.data(), sizeof(int) * lists[ph]->off.size(), c->mld.off[ph]);
+    DEV(lists[ph]->blk.data(), sizeof(int) * lists[ph]->blk.size(), c->mld.blk[ph]);
+  }
+  c->mld.nflux = (int)plan.flux_tasks.size();
+  DEV(plan.flux_tasks.data(), sizeof(MlFluxTask) * plan.flux_tasks.size(), c->mld.flux_tasks);
+#undef DEV
+  // the 27-entry table now only marks which neighbours exist (the boundary kernels'
+  // has-neighbour test): the block itself for an existing one, -1 for none
+  std::vector<int> hn((size_t)nb * 27);
+  for (int b = 0; b < nb; ++b)
+    for (int q = 0; q < 27; ++q) hn[(size_t)b * 27 + q] = nblevel[(size_t)b * 27 + q] < 0 ? -1 : b;
+  CK(cudaMemcpy(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice));
+  L.on = 1;
+  if (c->cycle_exec) { cudaGraphExecDestroy(c->cycle_exec); c->cycle_exec = nullptr; }
+  if (c->cycle_graph) { cudaGraphDestroy(c->cycle_graph); c->cycle_graph = nullptr; }
+  CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_ml_plan_check(const int* nx, int nghost, const int* bc, int nblocks,
+                                   const int* nbr_table, const int* nbr_count,
+                                   const int* nblevel, const long long* loc,
+                                   long long* counts) {
+  if (!nx || !bc || !nbr_table || !nbr_count || !nblevel || !loc || nblocks < 1)
+    return fail(ATHGPU_ERR_ARG, "null argument");
+  MlDims dims;
+  for (int a = 0; a < 3; ++a) dims.nx[a] = nx[a];
+  dims.ng = nghost;
+  for (int f = 0; f < 6; ++f) dims.bc[f] = bc[f];
+  MlPlan plan;
+  std::string err;
+  if (!build_ml_plan(dims, nblocks, nbr_table, nbr_count, nblevel, loc, &plan, &err))
+    return fail(ATHGPU_ERR_ARG, err.c_str());
+  if (counts) {
+    counts[0] = (long long)plan.r.ops.size();
+    counts[1] = (long long)plan.x.ops.size();
+    counts[2] = (long long)plan.p.ops.size();
+    counts[3] = (long long)plan.flux_tasks.size();
+  }
   return ATHGPU_OK;
 }
 

@@ -63,7 +63,9 @@ __device__ __forceinline__ bool bc_thread(const DevMesh& m, int a, long long t, 
   q.t1 = a == 2 ? 1 : 2;
   const int e0 = ncells(m, q.t0) + 1, e1 = ncells(m, q.t1) + 1;
   const int nbx[3] = {m.nbx1, m.nbx2, m.nbx3};
-  const int nbt = nbx[q.t0] * nbx[q.t1];  // blocks on one mesh face
+  // blocks on one mesh face (multi-level mesh: every block; those without a physical face
+  // on this side return)
+  const int nbt = m.ml.on ? m.nb : nbx[q.t0] * nbx[q.t1];
   const long long per_block = (long long)m.ng * e0 * e1;
   if (t >= 2LL * nbt * per_block) return false;
   long long r = t % per_block;
@@ -74,6 +76,10 @@ __device__ __forceinline__ bool bc_thread(const DevMesh& m, int a, long long t, 
   r /= e0;
   q.p1 = (int)(r % e1);
   q.g = 1 + (int)(r / e1);
+  if (m.ml.on) {
+    q.b = bt;
+    return true;
+  }
   int l[3];
   l[a] = q.side ? nbx[a] - 1 : 0;
   l[q.t0] = bt % nbx[q.t0];
@@ -193,7 +199,8 @@ inline long long bc_threads(const DevMesh& m, int a) {
   const int t0 = a == 0 ? 1 : 0, t1 = a == 2 ? 1 : 2;
   const int nc[3] = {m.nc1, m.nc2, m.nc3};
   const int nbx[3] = {m.nbx1, m.nbx2, m.nbx3};
-  return 2LL * nbx[t0] * nbx[t1] * m.ng * (nc[t0] + 1) * (nc[t1] + 1);
+  const long long nbt = m.ml.on ? (long long)m.nb : (long long)nbx[t0] * nbx[t1];
+  return 2LL * nbt * m.ng * (nc[t0] + 1) * (nc[t1] + 1);
 }
 
 }  // namespace athgpu

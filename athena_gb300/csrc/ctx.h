@@ -29,6 +29,17 @@ struct Registers {
   double *bs1 = nullptr, *bs2 = nullptr, *bs3 = nullptr;
 };
 
+// device copies of the multi-level plan (ml_plan.h)
+struct MlDevice {
+  void* ops[3] = {nullptr, nullptr, nullptr};  // MlOp lists: restriction, exchange, prolongation
+  int* off[3] = {nullptr, nullptr, nullptr};
+  int* blk[3] = {nullptr, nullptr, nullptr};
+  int nblk[3] = {0, 0, 0};
+  void* flux_tasks = nullptr;                  // int4 per task
+  int nflux = 0;
+  std::vector<void*> allocs;                   // everything allocated for the mesh
+};
+
 struct LaunchConfig {
   int seg_x2 = 0, seg_x3 = 0;  // faces per thread along the x2/x3 sweeps (0: default)
   int sr_phase1 = 0;           // SR con2prim: first-solve passes in phase 1 (0: default)
@@ -43,6 +54,8 @@ struct athgpu_ctx {
   athgpu::LaunchConfig lc;
   athgpu::DevClock* clk = nullptr;
   double* coords = nullptr;  // dx1f | dx2f | dx3f | plm coefficients (device)
+  double* fxv = nullptr;     // cell centres x1v | x2v | x3v per block (prolongation)
+  athgpu::MlDevice mld;
   float* coords32 = nullptr; // the same, rounded to FP32, for the FP32 kernels
   int* nbr = nullptr;
   cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -92,6 +105,10 @@ cudaError_t stage_fp64(athgpu_ctx* c, int stage);
 cudaError_t stage_fp32(athgpu_ctx* c, int stage);
 cudaError_t init_fp64(athgpu_ctx* c);
 cudaError_t init_fp32(athgpu_ctx* c);
+// multi-level mesh: the restriction, exchange and prolongation operation lists
+// (phase 0, 1, 2) on the context's stream
+cudaError_t ml_phase_fp64(athgpu_ctx* c, int phase);
+cudaError_t ml_phase_fp32(athgpu_ctx* c, int phase);
 // ghost exchange of U and the face fields (U's ghosts are not kept during the stages)
 cudaError_t exchange_u_fp64(athgpu_ctx* c);
 cudaError_t exchange_u_fp32(athgpu_ctx* c);

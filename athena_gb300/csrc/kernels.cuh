@@ -15,6 +15,34 @@ namespace athgpu {
 
 typedef long long i64;
 
+// Multi-level mesh data (mesh refinement; all zero/null on a uniform mesh).  Coarse
+// buffers hold, per block, the half-resolution arrays that restriction and prolongation
+// use (the reference's coarse_cons_, coarse_prim_, coarse_b_, coarse_bcc_): cells
+// [ncc3][ncc2][ncc1] with ncc = nx/2 + 2 NGHOST, coarse interior cis..cie etc.
+struct DevML {
+  int on;
+  const int* nblev;     // [nb][27] neighbour levels, (ox3+1)*9+(ox2+1)*3+(ox1+1); -1 none
+  const int* nbrt;      // [nb][56][10] neighbour lists (gid, level, ox1..3, type, fi1, fi2, fid, eid)
+  const int* nnbr;      // [nb]
+  const int* eflag;     // [nb][12] block edge touches no finer block
+  const int* nfine;     // [nb][12] blocks of the finest level around the edge
+  const int* fmask;     // [nb] bit f: face f has finer neighbours (flux correction)
+  const int* level;     // [nb]
+  int ncc1, ncc2, ncc3, cis, cie, cjs, cje, cks, cke, cng;
+  i64 nccell, ncf1, ncf2, ncf3;
+  void* ccons;          // coarse U   [nb][5][ncc]   (bulk precision)
+  void* cprim;          // coarse W   [nb][5][ncc]
+  void* cbcc;           // coarse bcc [nb][3][ncc]
+  double *cb1, *cb2, *cb3;   // coarse face field
+  void* scons;          // restricted U as sent to coarser blocks
+  double *sb1, *sb2, *sb3;   // restricted face field as sent
+  const double *cx1v, *cx2v, *cx3v;   // coarse cell centres [nb][ncc?]
+  const double *fx1v, *fx2v, *fx3v;   // fine cell centres [nb][nc?]
+  void* fcorr;          // restricted fine fluxes [nb][6][nfmax][5]
+  int nfmax;            // max over faces of nx_a * nx_b
+  void *ecorr1, *ecorr2, *ecorr3;     // corrected block-boundary edges (edge layout)
+};
+
 struct DevMesh {
   int nb, nbx1, nbx2, nbx3;
   int nx1, nx2, nx3, ng;
@@ -39,6 +67,7 @@ struct DevMesh {
   // 2 reflecting); any_bc is set when one of them is not periodic
   int bc[6];
   int any_bc;
+  DevML ml;
 };
 
 // device-resident scalars of the time integrator
@@ -235,6 +264,21 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   wct[fo] = weight_for_ct<Real>(f[0], wl[IDN], wr[IDN], dx, dt);
 }
 
+// Multi-level meshes: the flux of block b through its face fid (0..5) at transverse
+// position (pa, pb) (pa along the first transverse axis, of extent nta), replaced by the
+// finer blocks' restricted fluxes when that face is shared with finer blocks
+// (flux_correction_cc.cpp:237-286; written by ml_fine_flux_kernel)
+template <typename Real>
+__device__ __forceinline__ bool ml_face_override(const DevMesh& m, int b, int fid, int pa,
+                                                 int pb, int nta, Real* fn) {
+  if (!m.ml.on || !((__ldg(m.ml.fmask + b) >> fid) & 1)) return false;
+  const Real* p = (const Real*)m.ml.fcorr +
+                  (((i64)b * 6 + fid) * m.ml.nfmax + (i64)pb * nta + pa) * NHYDRO;
+#pragma unroll
+  for (int n = 0; n < NHYDRO; ++n) fn[n] = p[n];
+  return true;
+}
+
 // The flux divergence of Hydro::AddFluxDivergence (add_flux_divergence.cpp:50-94) is
 // accumulated by the three sweeps in the reference's order: the x1 sweep stores
 // dflx = A1*F1(i+1) - A1*F1(i), the x2 sweep adds (A2*F2(j+1) - A2*F2(j)), the x3 sweep
@@ -291,6 +335,9 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
     solve_face<Real, 0, RS>(m, wl, qrm, to_real(__ldg(b1 + fo), Real()),
                             __ldg(rdx(m, 0, Real()) + (i64)b * m.nc1 + i), rdt(clk, Real()),
                             fo, fn, e3, e2, wct);
+    if (m.ml.on && (i == m.is || i == m.ie + 1) && j >= m.js && j <= m.je && k >= m.ks &&
+        k <= m.ke)
+      ml_face_override<Real>(m, b, i == m.is ? 0 : 1, j - m.js, k - m.ks, m.nx2, fn);
   }
   Real fp[NHYDRO];
 #pragma unroll
@@ -462,6 +509,9 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     Real fn[NHYDRO];
     solve_face<Real, DIR, RS>(m, wl, qrm, to_real(fbuf[(s & 1) * bd], Real()),
                               __ldg(dxs + s), dt, fo, fn, ey, ez, wct);
+    if (m.ml.on && interior && (s == lo || s == lo + ncellsw))
+      ml_face_override<Real>(m, b, 2 * DIR + (s == lo ? 0 : 1), i - m.is,
+                             trans - (DIR == 1 ? m.ks : m.js), m.nx1, fn);
     cp_async_wait_all();  // this step's aux values and the next step's cell and face
     if (upd) {
       // cell s-1: this direction's flux difference
@@ -647,6 +697,11 @@ __device__ __forceinline__ Real edge_avg(const DevMesh& m, const Real* __restric
   Real own = at(b, k, j, i);
   const int on = (o1 != 0) + (o2 != 0) + (o3 != 0);
   if (on == 0) return own;
+  if (m.ml.on) {  // multi-level mesh: corrected by ml_emf_kernel
+    const Real* ec = (const Real*)(C == 0 ? m.ml.ecorr1 : C == 1 ? m.ml.ecorr2 : m.ml.ecorr3);
+    return ec[C == 0 ? e1idx(m, b, k, j, i) : C == 1 ? e2idx(m, b, k, j, i)
+                                                     : e3idx(m, b, k, j, i)];
+  }
   Real sum = own;
   int count = 1;  // blocks sharing the edge: a physical mesh face contributes none
   // face neighbours in list order: x1 before x2 before x3
@@ -905,6 +960,17 @@ __device__ __forceinline__ i64 src_cell(const DevMesh& m, int b, int k, int j, i
                                         int nvar, bool* ghost) {
   *ghost = i < m.is || i > m.ie || j < m.js || j > m.je || k < m.ks || k > m.ke;
   if (!*ghost) return cidx(m, b, 0, nvar, k, j, i);
+  if (m.ml.on) {
+    // multi-level mesh: the ghost cell's own (exchanged or prolongated) U, over the
+    // ranges of time_integrator.cpp:2206-2212 (ghosts along an axis only where that face
+    // has a neighbour)
+    const int* lv = m.ml.nblev + (i64)b * 27;
+    if ((i < m.is && lv[12] == -1) || (i > m.ie && lv[14] == -1) ||
+        (j < m.js && lv[10] == -1) || (j > m.je && lv[16] == -1) ||
+        (k < m.ks && lv[4] == -1) || (k > m.ke && lv[22] == -1))
+      return -1;
+    return cidx(m, b, 0, nvar, k, j, i);
+  }
   int o1, o2, o3;
   const int si = own_map(i, m.is, m.ie, m.nx1, &o1);
   const int sj = own_map(j, m.js, m.je, m.nx2, &o2);

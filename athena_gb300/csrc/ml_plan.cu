@@ -1,0 +1,664 @@
+// Host planner of the multi-level stage: from the neighbour lists of all MeshBlocks it
+// builds the per-block operation lists that ml_ops_kernel executes (restriction for
+// coarser neighbours, the ghost exchange, ProlongateBoundaries), the flux-correction
+// tasks of ml_fine_flux_kernel and the per-block edge tables of ml_emf_kernel.
+//
+// The index ranges follow the reference's buffer functions, stated per axis:
+// CellCenteredBoundaryVariable (bvals/cc/bvals_cc.cpp:252-540), FaceCenteredBoundary-
+// Variable (bvals/fc/bvals_fc.cpp:344-973), BoundaryValues::ProlongateBoundaries and its
+// helpers (bvals/bvals_refine.cpp:97-637), FaceCenteredBoundaryVariable::CountFineEdges
+// (bvals/fc/bvals_fc.cpp:1129-1196).  A transfer copies a source box to a destination box
+// of the same shape element by element in (k, j, i) order, which is the order the
+// reference packs and unpacks its buffers.
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "ml_plan.h"
+
+namespace athgpu {
+namespace {
+
+struct Box {
+  int s[3], e[3];
+};
+
+struct Ix {
+  int lo[3], hi[3];    // fine interior (is..ie, ...)
+  int clo[3], chi[3];  // coarse interior
+  int n[3];            // nx1, nx2, nx3
+  int ng, cng;
+};
+
+void off3(const MlNbr& q, int o[3]) { o[0] = q.ox1; o[1] = q.ox2; o[2] = q.ox3; }
+
+// the fine-block offset that selects the half of axis a (a has offset 0)
+int half_sel(const MlNbr& q, int a) {
+  if (a == 0) return q.fi1;
+  if (a == 1) return q.ox1 != 0 ? q.fi1 : q.fi2;
+  return (q.ox1 != 0 && q.ox2 != 0) ? q.fi1 : q.fi2;
+}
+
+// ---- cell-centred (U) regions ----
+Box cc_send_same(const Ix& x, const MlNbr& q) {  // LoadBoundaryBufferSameLevel
+  Box r; int o[3]; off3(q, o);
+  for (int a = 0; a < 3; ++a) {
+    r.s[a] = (o[a] > 0) ? x.hi[a] - x.ng + 1 : x.lo[a];
+    r.e[a] = (o[a] < 0) ? x.lo[a] + x.ng - 1 : x.hi[a];
+  }
+  return r;
+}
+Box cc_recv_same(const Ix& x, const MlNbr& q) {  // SetBoundarySameLevel
+  Box r; int o[3]; off3(q, o);
+  for (int a = 0; a < 3; ++a) {
+    if (o[a] == 0) { r.s[a] = x.lo[a]; r.e[a] = x.hi[a]; }
+    else if (o[a] > 0) { r.s[a] = x.hi[a] + 1; r.e[a] = x.hi[a] + x.ng; }
+    else { r.s[a] = x.lo[a] - x.ng; r.e[a] = x.lo[a] - 1; }
+  }
+  return r;
+}
+Box cc_send_coarser(const Ix& x, const MlNbr& q) {  // LoadBoundaryBufferToCoarser
+  Box r; int o[3]; off3(q, o);
+  const int cn = x.ng - 1;
+  for (int a = 0; a < 3; ++a) {
+    r.s[a] = (o[a] > 0) ? x.chi[a] - cn : x.clo[a];
+    r.e[a] = (o[a] < 0) ? x.clo[a] + cn : x.chi[a];
+  }
+  return r;
+}
+Box cc_recv_finer(const Ix& x, const MlNbr& q) {  // SetBoundaryFromFiner
+  Box r; int o[3]; off3(q, o);
+  for (int a = 0; a < 3; ++a) {
+    if (o[a] == 0) {
+      r.s[a] = x.lo[a]; r.e[a] = x.hi[a];
+      if (half_sel(q, a) == 1) r.s[a] += x.n[a] / 2; else r.e[a] -= x.n[a] / 2;
+    } else if (o[a] > 0) { r.s[a] = x.hi[a] + 1; r.e[a] = x.hi[a] + x.ng; }
+    else { r.s[a] = x.lo[a] - x.ng; r.e[a] = x.lo[a] - 1; }
+  }
+  return r;
+}
+Box cc_send_finer(const Ix& x, const MlNbr& q) {  // LoadBoundaryBufferToFiner
+  Box r; int o[3]; off3(q, o);
+  const int cn = x.cng - 1;
+  for (int a = 0; a < 3; ++a) {
+    r.s[a] = (o[a] > 0) ? x.hi[a] - cn : x.lo[a];
+    r.e[a] = (o[a] < 0) ? x.lo[a] + cn : x.hi[a];
+    if (o[a] == 0) {
+      if (half_sel(q, a) == 1) r.s[a] += x.n[a] / 2 - x.cng;
+      else r.e[a] -= x.n[a] / 2 - x.cng;
+    }
+  }
+  return r;
+}
+Box cc_recv_coarser(const Ix& x, const MlNbr& q, const int par[3]) {  // SetBoundaryFromCoarser
+  Box r; int o[3]; off3(q, o);
+  for (int a = 0; a < 3; ++a) {
+    if (o[a] == 0) {
+      r.s[a] = x.clo[a]; r.e[a] = x.chi[a];
+      if (par[a] == 0) r.e[a] += x.cng; else r.s[a] -= x.cng;
+    } else if (o[a] > 0) { r.s[a] = x.chi[a] + 1; r.e[a] = x.chi[a] + x.cng; }
+    else { r.s[a] = x.clo[a] - x.cng; r.e[a] = x.clo[a] - 1; }
+  }
+  return r;
+}
+
+// ---- face-field regions, component d (axis d runs over faces) ----
+Box fc_send_same(const Ix& x, const MlNbr& q, int d) {
+  Box r; int o[3]; off3(q, o);
+  const int ng = x.ng;
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) {
+      if (o[a] == 0) { r.s[a] = x.lo[a]; r.e[a] = x.hi[a] + 1; }
+      else if (o[a] > 0) { r.s[a] = x.hi[a] - ng + 1; r.e[a] = x.hi[a]; }
+      else { r.s[a] = x.lo[a] + 1; r.e[a] = x.lo[a] + ng; }
+      if (q.type != ML_FACE) {  // the overlapping face of edges and corners
+        if (o[a] > 0) r.e[a]++;
+        else if (o[a] < 0) r.s[a]--;
+      }
+    } else {
+      if (o[a] == 0) { r.s[a] = x.lo[a]; r.e[a] = x.hi[a]; }
+      else if (o[a] > 0) { r.s[a] = x.hi[a] - ng + 1; r.e[a] = x.hi[a]; }
+      else { r.s[a] = x.lo[a]; r.e[a] = x.lo[a] + ng - 1; }
+    }
+  }
+  return r;
+}
+Box fc_recv_same(const Ix& x, const MlNbr& q, int d) {
+  Box r; int o[3]; off3(q, o);
+  const int ng = x.ng;
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) {
+      if (o[a] == 0) { r.s[a] = x.lo[a]; r.e[a] = x.hi[a] + 1; }
+      else if (o[a] > 0) { r.s[a] = x.hi[a] + 2; r.e[a] = x.hi[a] + ng + 1; }
+      else { r.s[a] = x.lo[a] - ng; r.e[a] = x.lo[a] - 1; }
+      if (q.type != ML_FACE) {
+        if (o[a] > 0) r.s[a]--;
+        else if (o[a] < 0) r.e[a]++;
+      }
+    } else {
+      if (o[a] == 0) { r.s[a] = x.lo[a]; r.e[a] = x.hi[a]; }
+      else if (o[a] > 0) { r.s[a] = x.hi[a] + 1; r.e[a] = x.hi[a] + ng; }
+      else { r.s[a] = x.lo[a] - ng; r.e[a] = x.lo[a] - 1; }
+    }
+  }
+  return r;
+}
+Box fc_send_coarser(const Ix& x, const MlNbr& q, int d) {  // ghost width NGHOST
+  Box r; int o[3]; off3(q, o);
+  const int cg = x.ng;
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) {
+      if (o[a] == 0) { r.s[a] = x.clo[a]; r.e[a] = x.chi[a] + 1; }
+      else if (o[a] > 0) { r.s[a] = x.chi[a] - cg + 1; r.e[a] = x.chi[a]; }
+      else { r.s[a] = x.clo[a] + 1; r.e[a] = x.clo[a] + cg; }
+      if (q.type != ML_FACE) {
+        if (o[a] > 0) r.e[a]++;
+        else if (o[a] < 0) r.s[a]--;
+      }
+    } else {
+      if (o[a] == 0) { r.s[a] = x.clo[a]; r.e[a] = x.chi[a]; }
+      else if (o[a] > 0) { r.s[a] = x.chi[a] - cg + 1; r.e[a] = x.chi[a]; }
+      else { r.s[a] = x.clo[a]; r.e[a] = x.clo[a] + cg - 1; }
+    }
+  }
+  return r;
+}
+Box fc_recv_finer(const Ix& x, const MlNbr& q, int d) {
+  Box r; int o[3]; off3(q, o);
+  const int ng = x.ng;
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) {
+      if (o[a] == 0) {
+        r.s[a] = x.lo[a]; r.e[a] = x.hi[a] + 1;
+        if (half_sel(q, a) == 1) r.s[a] += x.n[a] / 2; else r.e[a] -= x.n[a] / 2;
+      } else if (o[a] > 0) { r.s[a] = x.hi[a] + 2; r.e[a] = x.hi[a] + ng + 1; }
+      else { r.s[a] = x.lo[a] - ng; r.e[a] = x.lo[a] - 1; }
+      if (q.type != ML_FACE) {
+        if (o[a] > 0) r.s[a]--;
+        else if (o[a] < 0) r.e[a]++;
+      }
+    } else {
+      if (o[a] == 0) {
+        r.s[a] = x.lo[a]; r.e[a] = x.hi[a];
+        if (half_sel(q, a) == 1) r.s[a] += x.n[a] / 2; else r.e[a] -= x.n[a] / 2;
+      } else if (o[a] > 0) { r.s[a] = x.hi[a] + 1; r.e[a] = x.hi[a] + ng; }
+      else { r.s[a] = x.lo[a] - ng; r.e[a] = x.lo[a] - 1; }
+    }
+  }
+  return r;
+}
+Box fc_send_finer(const Ix& x, const MlNbr& q, int d) {
+  Box r; int o[3]; off3(q, o);
+  const int cg = x.cng, cn = x.cng - 1;
+  for (int a = 0; a < 3; ++a) {
+    const int h = x.n[a] / 2 - cg;
+    if (a == d) {
+      if (o[a] == 0) {
+        r.s[a] = x.lo[a]; r.e[a] = x.hi[a] + 1;
+        if (half_sel(q, a) == 1) r.s[a] += h; else r.e[a] -= h;
+      } else if (o[a] > 0) { r.s[a] = x.hi[a] + 1 - cg; r.e[a] = x.hi[a] + 1; }
+      else { r.s[a] = x.lo[a]; r.e[a] = x.lo[a] + cg; }
+    } else {
+      if (o[a] == 0) {
+        r.s[a] = x.lo[a]; r.e[a] = x.hi[a];
+        if (half_sel(q, a) == 1) r.s[a] += h; else r.e[a] -= h;
+      } else if (o[a] > 0) { r.s[a] = x.hi[a] - cn; r.e[a] = x.hi[a]; }
+      else { r.s[a] = x.lo[a]; r.e[a] = x.lo[a] + cn; }
+    }
+  }
+  return r;
+}
+Box fc_recv_coarser(const Ix& x, const MlNbr& q, int d, const int par[3]) {
+  Box r; int o[3]; off3(q, o);
+  const int cg = x.cng;
+  for (int a = 0; a < 3; ++a) {
+    if (a == d) {
+      if (o[a] == 0) {
+        r.s[a] = x.clo[a]; r.e[a] = x.chi[a] + 1;
+        if (par[a] == 0) r.e[a] += cg; else r.s[a] -= cg;
+      } else if (o[a] > 0) { r.s[a] = x.chi[a] + 1; r.e[a] = x.chi[a] + 1 + cg; }
+      else { r.s[a] = x.clo[a] - cg; r.e[a] = x.clo[a]; }
+    } else {
+      if (o[a] == 0) {
+        r.s[a] = x.clo[a]; r.e[a] = x.chi[a];
+        if (par[a] == 0) r.e[a] += cg; else r.s[a] -= cg;
+      } else if (o[a] > 0) { r.s[a] = x.chi[a] + 1; r.e[a] = x.chi[a] + cg; }
+      else { r.s[a] = x.clo[a] - cg; r.e[a] = x.clo[a] - 1; }
+    }
+  }
+  return r;
+}
+
+MlOp make_op(int code, int d, const Box& dst) {
+  MlOp op{};
+  op.code = code;
+  op.d = d;
+  for (int a = 0; a < 3; ++a) { op.s[a] = dst.s[a]; op.e[a] = dst.e[a]; }
+  return op;
+}
+bool same_shape(const Box& a, const Box& b) {
+  for (int q = 0; q < 3; ++q)
+    if (a.e[q] - a.s[q] != b.e[q] - b.s[q]) return false;
+  return true;
+}
+bool empty(const Box& a) {
+  for (int q = 0; q < 3; ++q)
+    if (a.e[q] < a.s[q]) return true;
+  return false;
+}
+
+// Every array index an operation will touch, checked on the host before anything runs on
+// the device (fine arrays: cells 0..nc-1, faces 0..nc along their own axis; coarse
+// buffers: 0..ncc-1, 0..ncc).
+struct Bounds {
+  int nc[3], ncc[3];
+  bool in(int lo, int hi, int n) const { return lo >= 0 && hi <= n - 1 && lo <= hi + 1; }
+  bool cells(const int s[3], const int e[3], bool coarse, int pad) const {
+    for (int a = 0; a < 3; ++a)
+      if (!in(s[a] - pad, e[a] + pad, coarse ? ncc[a] : nc[a])) return false;
+    return true;
+  }
+  bool faces(const int s[3], const int e[3], bool coarse, int d, int pad) const {
+    for (int a = 0; a < 3; ++a) {
+      const int n = (coarse ? ncc[a] : nc[a]) + (a == d ? 1 : 0);
+      if (!in(s[a] - (a == d ? 0 : pad), e[a] + (a == d ? 0 : pad), n)) return false;
+    }
+    return true;
+  }
+};
+
+bool check_op(const MlOp& op, const Ix& x, const Bounds& B) {
+  int e2[3], s2[3], fe[3];
+  for (int a = 0; a < 3; ++a) {
+    s2[a] = op.o[a];
+    e2[a] = op.o[a] + op.e[a] - op.s[a];
+  }
+  switch (op.code) {
+    case ML_COPY_U:
+      return B.cells(op.s, op.e, op.dst_kind == ML_COARSE, 0) &&
+             B.cells(s2, e2, op.src_kind == ML_SEND, 0);
+    case ML_COPY_B:
+      return B.faces(op.s, op.e, op.dst_kind == ML_COARSE, op.d, 0) &&
+             B.faces(s2, e2, op.src_kind == ML_SEND, op.d, 0);
+    case ML_RESTRICT_U: {
+      int fs[3];
+      for (int a = 0; a < 3; ++a) {
+        fs[a] = (op.s[a] - x.clo[a]) * 2 + x.lo[a];
+        fe[a] = (op.e[a] - x.clo[a]) * 2 + x.lo[a] + 1;
+      }
+      return B.cells(op.s, op.e, true, 0) && B.cells(fs, fe, false, 0);
+    }
+    case ML_RESTRICT_B: {
+      int fs[3];
+      for (int a = 0; a < 3; ++a) {
+        fs[a] = (op.s[a] - x.clo[a]) * 2 + x.lo[a];
+        fe[a] = (op.e[a] - x.clo[a]) * 2 + x.lo[a] + (a == op.d ? 0 : 1);
+      }
+      return B.faces(op.s, op.e, true, op.d, 0) && B.faces(fs, fe, false, op.d, 0);
+    }
+    case ML_C2P_COARSE:
+      return B.cells(op.s, op.e, true, 0);
+    case ML_BC_COARSE: {
+      const int f = op.aux & 7, a = f >> 1;
+      int cs[3], ce[3];
+      for (int q = 0; q < 3; ++q) {
+        cs[q] = op.s[q];
+        ce[q] = op.e[q] - (q == a ? 0 : 1);
+      }
+      cs[a] = x.clo[a] - x.ng;
+      ce[a] = x.chi[a] + x.ng;
+      if (!B.cells(cs, ce, true, 0)) return false;
+      for (int d = 0; d < 3; ++d) {
+        int fs[3] = {cs[0], cs[1], cs[2]}, fe2[3] = {ce[0], ce[1], ce[2]};
+        if (d != a) fe2[d] += 1;
+        else fe2[a] += 1;
+        if (!B.faces(fs, fe2, true, d, 0)) return false;
+      }
+      return op.s[a] >= 1 && op.e[a] <= x.ng;
+    }
+    case ML_PROLONG_U: {
+      int fs[3];
+      for (int a = 0; a < 3; ++a) {
+        fs[a] = (op.s[a] - x.clo[a]) * 2 + x.lo[a];
+        fe[a] = (op.e[a] - x.clo[a]) * 2 + x.lo[a] + 1;
+      }
+      return B.cells(op.s, op.e, true, 1) && B.cells(fs, fe, false, 0);
+    }
+    case ML_PROLONG_SHARED: {
+      int fs[3];
+      for (int a = 0; a < 3; ++a) {
+        fs[a] = (op.s[a] - x.clo[a]) * 2 + x.lo[a];
+        fe[a] = (op.e[a] - x.clo[a]) * 2 + x.lo[a] + (a == op.d ? 0 : 1);
+      }
+      // the slopes read the transverse neighbours of the coarse face
+      return B.faces(op.s, op.e, true, op.d, 1) && B.faces(fs, fe, false, op.d, 0);
+    }
+    case ML_PROLONG_INTERNAL: {
+      int fs[3];
+      for (int a = 0; a < 3; ++a) {
+        fs[a] = (op.s[a] - x.clo[a]) * 2 + x.lo[a];
+        fe[a] = (op.e[a] - x.clo[a]) * 2 + x.lo[a] + 2;   // faces fi .. fi+2
+      }
+      for (int d = 0; d < 3; ++d) {
+        int fe2[3] = {fe[0] - 1, fe[1] - 1, fe[2] - 1};
+        fe2[d] += 1;
+        if (!B.faces(fs, fe2, false, d, 0)) return false;
+      }
+      return true;
+    }
+    case ML_FINE_P2C:
+      return B.cells(op.s, op.e, false, 0) && op.e[0] + 1 <= B.nc[0] &&
+             op.e[1] + 1 <= B.nc[1] && op.e[2] + 1 <= B.nc[2];
+    default:
+      return false;
+  }
+}
+
+}  // namespace
+
+bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* nbr_count,
+                   const int* nblevel, const long long* loc, MlPlan* P, std::string* err) {
+  Ix x;
+  const int ng = dims.ng;
+  for (int a = 0; a < 3; ++a) {
+    x.n[a] = dims.nx[a];
+    x.lo[a] = ng;
+    x.hi[a] = ng + dims.nx[a] - 1;
+    x.clo[a] = ng;
+    x.chi[a] = ng + dims.nx[a] / 2 - 1;
+  }
+  x.ng = ng;
+  x.cng = (ng + 1) / 2 + 1;  // meshblock.cpp:93
+  auto nbr = [&](int b, int n) {
+    const int* t = nbr_table + ((long long)b * ML_MAXNB + n) * ML_NF;
+    MlNbr q;
+    q.gid = t[0]; q.level = t[1]; q.ox1 = t[2]; q.ox2 = t[3]; q.ox3 = t[4];
+    q.type = t[5]; q.fi1 = t[6]; q.fi2 = t[7]; q.fid = t[8]; q.eid = t[9];
+    return q;
+  };
+  auto nbl = [&](int b, int o1, int o2, int o3) {
+    return nblevel[(long long)b * 27 + (o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
+  };
+  auto level = [&](int b) { return (int)loc[(long long)b * 4]; };
+  // the entry of s's list that points back at r
+  auto back = [&](int s, int r, const MlNbr& f, MlNbr* out) {
+    for (int n = 0; n < nbr_count[s]; ++n) {
+      MlNbr q = nbr(s, n);
+      if (q.gid == r && q.ox1 == -f.ox1 && q.ox2 == -f.ox2 && q.ox3 == -f.ox3) {
+        *out = q;
+        return true;
+      }
+    }
+    return false;
+  };
+  auto fail = [&](const char* what, int b) {
+    char buf[160];
+    snprintf(buf, sizeof buf, "multi-level plan: %s (block %d)", what, b);
+    *err = buf;
+    return false;
+  };
+  P->level.resize(nb);
+  for (int b = 0; b < nb; ++b) {
+    P->level[b] = level(b);
+    if (nbr_count[b] < 0 || nbr_count[b] > ML_MAXNB) return fail("bad neighbour count", b);
+  }
+  // ---- phase R: restriction for coarser neighbours (into the send and coarse buffers) --
+  P->r.clear(); P->x.clear(); P->p.clear();
+  for (int s = 0; s < nb; ++s) {
+    std::vector<MlOp> ops;
+    for (int n = 0; n < nbr_count[s]; ++n) {
+      MlNbr q = nbr(s, n);
+      if (q.level >= level(s)) continue;
+      MlOp op = make_op(ML_RESTRICT_U, 0, cc_send_coarser(x, q));
+      op.src_kind = ML_SEND;
+      ops.push_back(op);
+      for (int d = 0; d < 3; ++d) {
+        MlOp ob = make_op(ML_RESTRICT_B, d, fc_send_coarser(x, q, d));
+        ob.src_kind = ML_SEND;
+        ops.push_back(ob);
+      }
+    }
+    if (!ops.empty()) P->r.add(s, ops);
+  }
+  // ---- phase X: the ghost exchange, per receiver in neighbour-list order; all U copies
+  // first (SETB_HYD), then all face-field copies (SETB_FLD)
+  for (int r = 0; r < nb; ++r) {
+    std::vector<MlOp> ucopies, bcopies;
+    const int par[3] = {(int)(loc[(long long)r * 4 + 1] & 1), (int)(loc[(long long)r * 4 + 2] & 1),
+                        (int)(loc[(long long)r * 4 + 3] & 1)};
+    for (int n = 0; n < nbr_count[r]; ++n) {
+      MlNbr q = nbr(r, n), qs;
+      const int s = q.gid;
+      if (!back(s, r, q, &qs)) return fail("inconsistent neighbour lists", r);
+      Box du, su;
+      int ud, us;
+      if (q.level == level(r)) {
+        du = cc_recv_same(x, q); su = cc_send_same(x, qs); ud = ML_FINE; us = ML_FINE;
+      } else if (q.level < level(r)) {
+        du = cc_recv_coarser(x, q, par); su = cc_send_finer(x, qs); ud = ML_COARSE;
+        us = ML_FINE;
+      } else {
+        du = cc_recv_finer(x, q); su = cc_send_coarser(x, qs); ud = ML_FINE; us = ML_SEND;
+      }
+      if (!same_shape(du, su)) return fail("mismatched cell transfer boxes", r);
+      MlOp op = make_op(ML_COPY_U, 0, du);
+      op.src_kind = us; op.dst_kind = ud; op.src = s;
+      for (int a = 0; a < 3; ++a) op.o[a] = su.s[a];
+      ucopies.push_back(op);
+      for (int d = 0; d < 3; ++d) {
+        Box db, sb;
+        if (q.level == level(r)) { db = fc_recv_same(x, q, d); sb = fc_send_same(x, qs, d); }
+        else if (q.level < level(r)) {
+          db = fc_recv_coarser(x, q, d, par); sb = fc_send_finer(x, qs, d);
+        } else { db = fc_recv_finer(x, q, d); sb = fc_send_coarser(x, qs, d); }
+        if (!same_shape(db, sb)) return fail("mismatched face transfer boxes", r);
+        MlOp ob = make_op(ML_COPY_B, d, db);
+        ob.src_kind = us; ob.dst_kind = ud; ob.src = s;
+        for (int a = 0; a < 3; ++a) ob.o[a] = sb.s[a];
+        bcopies.push_back(ob);
+      }
+    }
+    std::vector<MlOp> all = ucopies;
+    all.insert(all.end(), bcopies.begin(), bcopies.end());
+    if (!all.empty()) P->x.add(r, all);
+  }
+  // ---- phase P: ProlongateBoundaries per block with coarser neighbours ------------------
+  const int cn = x.cng - 1;
+  for (int b = 0; b < nb; ++b) {
+    const int lev = level(b);
+    std::vector<MlOp> ops;
+    for (int n = 0; n < nbr_count[b]; ++n) {
+      MlNbr q = nbr(b, n);
+      if (q.level >= lev) continue;
+      int o[3]; off3(q, o);
+      int ns[3], ne[3];
+      for (int a = 0; a < 3; ++a) {
+        ns[a] = (o[a] - 1 > -1) ? o[a] - 1 : -1;
+        ne[a] = (o[a] + 1 < 1) ? o[a] + 1 : 1;
+      }
+      // RestrictGhostCellsOnSameLevel (bvals_refine.cpp:262-352)
+      for (int nk = ns[2]; nk <= ne[2]; ++nk)
+        for (int nj = ns[1]; nj <= ne[1]; ++nj)
+          for (int ni = ns[0]; ni <= ne[0]; ++ni) {
+            const int ntype = (ni != 0) + (nj != 0) + (nk != 0);
+            if (ntype == 0 || nbl(b, ni, nj, nk) != lev) continue;
+            const int nn[3] = {ni, nj, nk};
+            Box r;
+            for (int a = 0; a < 3; ++a) {
+              if (nn[a] == 0) {
+                r.s[a] = x.clo[a]; r.e[a] = x.chi[a];
+                if (o[a] == 1) r.s[a] = x.chi[a];
+                else if (o[a] == -1) r.e[a] = x.clo[a];
+              } else if (nn[a] == 1) {
+                r.s[a] = r.e[a] = x.chi[a] + 1;
+              } else {
+                r.s[a] = r.e[a] = x.clo[a] - 1;
+              }
+            }
+            MlOp ru = make_op(ML_RESTRICT_U, 0, r);
+            ru.src_kind = ML_COARSE;
+            ops.push_back(ru);
+            for (int d = 0; d < 3; ++d) {
+              Box rf = r;
+              int rs = r.s[d], re = r.e[d] + 1;
+              int om[3] = {ni, nj, nk}, op3[3] = {ni, nj, nk};
+              om[d] -= 1;
+              op3[d] += 1;
+              if (rs == x.clo[d] && nbl(b, om[0], om[1], om[2]) < lev) rs++;
+              if (re == x.chi[d] + 1 && nbl(b, op3[0], op3[1], op3[2]) < lev) re--;
+              rf.s[d] = rs;
+              rf.e[d] = re;
+              MlOp rb = make_op(ML_RESTRICT_B, d, rf);
+              rb.src_kind = ML_COARSE;
+              if (!empty(rf)) ops.push_back(rb);
+            }
+          }
+      Box c;
+      for (int a = 0; a < 3; ++a) {
+        if (o[a] == 0) {
+          c.s[a] = x.clo[a]; c.e[a] = x.chi[a];
+          if ((loc[(long long)b * 4 + 1 + a] & 1LL) == 0LL) c.e[a] += cn; else c.s[a] -= cn;
+        } else if (o[a] > 0) { c.s[a] = x.chi[a] + 1; c.e[a] = x.chi[a] + cn; }
+        else { c.s[a] = x.clo[a] - cn; c.e[a] = x.clo[a] - 1; }
+      }
+      // ApplyPhysicalBoundariesOnCoarseLevel (bvals_refine.cpp:366-505)
+      Box cx = c;
+      for (int a = 0; a < 3; ++a) {
+        int om[3] = {0, 0, 0}, op3[3] = {0, 0, 0};
+        om[a] = -1; op3[a] = 1;
+        int fm = 1, fp = 1;
+        if (o[a] == 0) {
+          fm = nbl(b, om[0], om[1], om[2]) != -1;
+          fp = nbl(b, op3[0], op3[1], op3[2]) != -1;
+        }
+        cx.s[a] -= fm;
+        cx.e[a] += fp;
+      }
+      ops.push_back(make_op(ML_C2P_COARSE, 0, cx));
+      for (int a = 0; a < 3; ++a) {
+        if (o[a] != 0) continue;
+        for (int side = 0; side < 2; ++side) {
+          int od[3] = {0, 0, 0};
+          od[a] = side ? 1 : -1;
+          if (nbl(b, od[0], od[1], od[2]) != -1) continue;  // not a physical face
+          // box: layers 1..ng along a, transverse ranges of c extended by one (the face
+          // components along a transverse axis have one more entry)
+          Box bx;
+          for (int q3 = 0; q3 < 3; ++q3) {
+            if (q3 == a) { bx.s[q3] = 1; bx.e[q3] = ng; }
+            else { bx.s[q3] = c.s[q3]; bx.e[q3] = c.e[q3] + 1; }
+          }
+          MlOp ob = make_op(ML_BC_COARSE, 0, bx);
+          ob.aux = (2 * a + side) | (dims.bc[2 * a + side] << 4);
+          ops.push_back(ob);
+        }
+      }
+      ops.push_back(make_op(ML_PROLONG_U, 0, c));
+      for (int d = 0; d < 3; ++d) {
+        Box cf = c;
+        int lo = c.s[d], hi = c.e[d] + 1;
+        int om[3] = {o[0], o[1], o[2]}, op3[3] = {o[0], o[1], o[2]};
+        om[d] -= 1;
+        op3[d] += 1;
+        if (o[d] >= 0 && nbl(b, om[0], om[1], om[2]) >= lev) lo++;
+        if (o[d] <= 0 && nbl(b, op3[0], op3[1], op3[2]) >= lev) hi--;
+        cf.s[d] = lo;
+        cf.e[d] = hi;
+        if (!empty(cf)) ops.push_back(make_op(ML_PROLONG_SHARED, d, cf));
+      }
+      ops.push_back(make_op(ML_PROLONG_INTERNAL, 0, c));
+      Box fb;
+      for (int a = 0; a < 3; ++a) {
+        fb.s[a] = (c.s[a] - x.clo[a]) * 2 + x.lo[a];
+        fb.e[a] = (c.e[a] - x.clo[a]) * 2 + x.lo[a] + 1;
+      }
+      ops.push_back(make_op(ML_FINE_P2C, 0, fb));
+    }
+    if (!ops.empty()) P->p.add(b, ops);
+  }
+  // ---- flux correction tasks: (coarse block, finer block, face | fi1 << 4 | fi2 << 5) --
+  P->flux_tasks.clear();
+  P->fmask.assign(nb, 0);
+  for (int b = 0; b < nb; ++b)
+    for (int n = 0; n < nbr_count[b]; ++n) {
+      MlNbr q = nbr(b, n);
+      if (q.type != ML_FACE || q.level != level(b) + 1) continue;
+      P->flux_tasks.push_back(MlFluxTask{b, q.gid, q.fid | (q.fi1 << 4) | (q.fi2 << 5), 0});
+      P->fmask[b] |= 1 << q.fid;
+    }
+  // ---- bounds of every operation ------------------------------------------------------
+  {
+    Bounds B;
+    for (int a = 0; a < 3; ++a) {
+      B.nc[a] = dims.nx[a] + 2 * ng;
+      B.ncc[a] = dims.nx[a] / 2 + 2 * ng;
+    }
+    const MlOpList* lists[3] = {&P->r, &P->x, &P->p};
+    for (const MlOpList* L : lists)
+      for (size_t q = 0; q < L->ops.size(); ++q)
+        if (!check_op(L->ops[q], x, B)) {
+          char buf[200];
+          const MlOp& o = L->ops[q];
+          snprintf(buf, sizeof buf,
+                   "multi-level plan: operation %d (d %d) box [%d..%d, %d..%d, %d..%d] out of bounds",
+                   o.code, o.d, o.s[0], o.e[0], o.s[1], o.e[1], o.s[2], o.e[2]);
+          *err = buf;
+          return false;
+        }
+    for (const MlFluxTask& t : P->flux_tasks)
+      if (t.coarse < 0 || t.coarse >= nb || t.fine < 0 || t.fine >= nb) {
+        *err = "multi-level plan: flux task block out of range";
+        return false;
+      }
+    for (int b = 0; b < nb; ++b)
+      for (int n = 0; n < nbr_count[b]; ++n)
+        if (nbr(b, n).gid < 0 || nbr(b, n).gid >= nb) {
+          *err = "multi-level plan: neighbour gid out of range";
+          return false;
+        }
+  }
+  // ---- CountFineEdges ---------------------------------------------------------------
+  P->eflag.assign((size_t)nb * 12, 0);
+  P->nfine.assign((size_t)nb * 12, 0);
+  for (int b = 0; b < nb; ++b) {
+    const int lev = level(b);
+    int eid = 0;
+    for (int t = 0; t < 3; ++t) {
+      const int a = (t == 2) ? 1 : 0, cax = (t == 0) ? 1 : 2;
+      for (int oc = -1; oc <= 1; oc += 2)
+        for (int oa = -1; oa <= 1; oa += 2) {
+          const int nas = (oa - 1 > -1) ? oa - 1 : -1, nae = (oa + 1 < 1) ? oa + 1 : 1;
+          const int ncs = (oc - 1 > -1) ? oc - 1 : -1, nce = (oc + 1 < 1) ? oc + 1 : 1;
+          int nf = 0, fl = lev;
+          for (int nc = ncs; nc <= nce; ++nc)
+            for (int na = nas; na <= nae; ++na) {
+              int o[3] = {0, 0, 0};
+              o[a] = na;
+              o[cax] = nc;
+              const int l = nbl(b, o[0], o[1], o[2]);
+              if (l > fl) { fl++; nf = 0; }
+              if (l == fl) nf++;
+            }
+          P->eflag[(size_t)b * 12 + eid] = (fl == lev);
+          P->nfine[(size_t)b * 12 + eid] = nf;
+          eid++;
+        }
+    }
+  }
+  return true;
+}
+
+void MlOpList::add(int block, const std::vector<MlOp>& ops) {
+  if (off.empty()) off.push_back(0);
+  blk.push_back(block);
+  this->ops.insert(this->ops.end(), ops.begin(), ops.end());
+  off.push_back((int)this->ops.size());
+}
+
+void MlOpList::clear() {
+  ops.clear();
+  off.clear();
+  blk.clear();
+}
+
+}  // namespace athgpu

@@ -10,6 +10,13 @@ cudaError_t stage_fp32(athgpu_ctx* c, int stage) {
 }
 cudaError_t init_fp32(athgpu_ctx* c) { return run_init<float, 1>(c); }
 cudaError_t exchange_u_fp32(athgpu_ctx* c) {
+  if (c->m.ml.on) {  // multi-level mesh: restriction for coarser blocks, then the exchange
+    float* u = (float*)c->r.u;
+    float* w = (float*)c->r.wbuf[c->r.wsel];
+    launch_ml_phase<float>(c, 0, u, w, c->r.b1, c->r.b2, c->r.b3);
+    launch_ml_phase<float>(c, 1, u, w, c->r.b1, c->r.b2, c->r.b3);
+    return cudaGetLastError();
+  }
   launch_exchange<float>(c, (float*)c->r.u, c->r.b1, c->r.b2, c->r.b3, 1);
   return cudaGetLastError();
 }

@@ -4,6 +4,7 @@
 #pragma once
 #include "ctx.h"
 #include "boundary.cuh"
+#include "multilevel.cuh"
 
 namespace athgpu {
 
@@ -17,6 +18,15 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
   const DevMesh& m = c->m;
   Registers& r = c->r;
   cudaStream_t s = c->stream;
+  if (m.ml.on && c->mld.nflux > 0) {
+    // the finer blocks' fluxes on faces shared with coarser blocks, restricted, before the
+    // sweeps (which use them there)
+    ProfScope ps(c, "ml_fine_flux");
+    const long long n = (long long)c->mld.nflux * (m.ml.nfmax / 4);
+    ml_fine_flux_kernel<Real, ORDER, RS><<<nblk(n, 128), 128, 0, s>>>(
+        m, (const int4*)c->mld.flux_tasks, c->mld.nflux, w, bcc, b1, b2, b3);
+    c->launches += 1;
+  }
   {
     const long long cells = (long long)m.nb * (m.nx3 + 2) * (m.nx2 + 2) * (m.nx1 + 2);
     const long long warps = (cells + 29) / 30;
@@ -77,6 +87,21 @@ static void launch_exchange(athgpu_ctx* c, Real* u, double* b1, double* b2, doub
     exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, st>>>(m, with_u, u, b1, b2, b3);
 }
 
+// Multi-level mesh: one of the three operation lists (0 restriction for coarser
+// neighbours, 1 ghost exchange, 2 prolongation), one CTA per block with work
+template <typename Real>
+static void launch_ml_phase(athgpu_ctx* c, int phase, Real* u, Real* w, double* b1,
+                            double* b2, double* b3) {
+  const int nb = c->mld.nblk[phase];
+  if (nb == 0) return;
+  static const char* names[3] = {"ml_restrict", "ml_exchange", "ml_prolong"};
+  ProfScope ps(c, names[phase]);
+  MlArrays<Real> A{u, w, (Real*)c->r.bcc, b1, b2, b3};
+  ml_ops_kernel<Real><<<nb, 128, 0, c->stream>>>(c->m, A, (const MlOp*)c->mld.ops[phase],
+                                                 c->mld.off[phase], c->mld.blk[phase]);
+  c->launches += 1;
+}
+
 template <typename Real, int KAHAN>
 static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* b2,
                                     double* b3, int do_dt, bool rotate = true,
@@ -90,7 +115,14 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
   // graph); the Newtonian W(U) reads the exchanged faces of its ghost cells and follows
   // the exchange.  The per-kernel profile runs everything one after the other.
   const bool overlap = !c->profiling && c->aux_stream != nullptr && c->desc.relativistic;
-  if (overlap) {
+  if (m.ml.on) {
+    // multi-level mesh: restriction for coarser neighbours, the exchange of U and B, then
+    // ProlongateBoundaries into the current primitives (bvals_refine.cpp:97-256)
+    Real* wcur = (Real*)c->r.wbuf[c->r.wsel];
+    launch_ml_phase<Real>(c, 0, u, wcur, b1, b2, b3);
+    launch_ml_phase<Real>(c, 1, u, wcur, b1, b2, b3);
+    launch_ml_phase<Real>(c, 2, u, wcur, b1, b2, b3);
+  } else if (overlap) {
     cudaEventRecord(c->ev_fork, s);
     cudaStreamWaitEvent(c->aux_stream, c->ev_fork, 0);
     launch_exchange<Real>(c, u, b1, b2, b3, with_u, c->aux_stream);
@@ -133,7 +165,7 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
       c->launches += 1;
     }
   }
-  if (overlap) {
+  if (overlap && !m.ml.on) {
     cudaEventRecord(c->ev_join, c->aux_stream);
     cudaStreamWaitEvent(s, c->ev_join, 0);
   }
@@ -189,6 +221,16 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
         m, (const Real*)r.cce, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f, (Real*)r.e1x2,
         (Real*)r.e3x2, (Real*)r.w2f, (Real*)r.e1x3, (Real*)r.e2x3, (Real*)r.w3f,
         (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
+  }
+  if (m.ml.on) {
+    // EMF correction across levels (flux_correction_fc.cpp)
+    ProfScope ps2(c, "ml_emf");
+    const long long n = (long long)m.nb * ((long long)(m.nx3 + 1) * (m.nx2 + 1) * m.nx1 +
+                                           (long long)(m.nx3 + 1) * m.nx2 * (m.nx1 + 1) +
+                                           (long long)m.nx3 * (m.nx2 + 1) * (m.nx1 + 1));
+    ml_emf_kernel<Real><<<nblk(n, 128), 128, 0, s>>>(m, (const Real*)r.e1, (const Real*)r.e2,
+                                                     (const Real*)r.e3);
+    c->launches += 1;
   }
   double* o1 = (stage == 1) ? r.bs1 : r.b1;
   double* o2 = (stage == 1) ? r.bs2 : r.b2;

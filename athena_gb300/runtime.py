@@ -98,6 +98,13 @@ def load_library(path=LIB_PATH):
         "athgpu_set_sweep_segment": ([vp, ip, ip], ip),
         "athgpu_autotune": ([vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
         "athgpu_history": ([vp, dp], ip),
+        "athgpu_ml_plan_check": ([ctypes.POINTER(ip), ip, ctypes.POINTER(ip), ip,
+                                  ctypes.POINTER(ip), ctypes.POINTER(ip), ctypes.POINTER(ip),
+                                  ctypes.POINTER(ctypes.c_longlong),
+                                  ctypes.POINTER(ctypes.c_longlong)], ip),
+        "athgpu_set_multilevel": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip),
+                                   ctypes.POINTER(ip), ctypes.POINTER(ctypes.c_longlong)] +
+                                  [dp] * 6, ip),
         "athgpu_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
         "athgpu_profile_cycle": ([vp, ip, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ip)], ip),
@@ -145,8 +152,11 @@ class StageUpdate:
         self.mesh = mesh
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         fl = default_floor()
+        multilevel = hasattr(mesh, "neighbor_table")
+        if multilevel:
+            bc = mesh.bcs
         d = MeshDesc()
-        d.nbx1, d.nbx2, d.nbx3 = mesh.nb
+        d.nbx1, d.nbx2, d.nbx3 = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
         d.nx1, d.nx2, d.nx3 = mesh.bx
         d.nghost, d.xorder = mesh.ng, xorder
         d.rsolver = HLLD if rsolver == "hlld" else HLLE
@@ -163,6 +173,16 @@ class StageUpdate:
         h = ctypes.c_void_p()
         _check(L.athgpu_create(ctypes.byref(h), ctypes.byref(d)), "athgpu_create")
         self.h = h
+        if multilevel:
+            t, cnt, lv, loc = mesh.neighbor_table()
+            ml = [np.ascontiguousarray(a) for a in (t, cnt, lv, loc)]
+            cc = [np.ascontiguousarray(c) for c in mesh.coarse_coordinate_arrays()]
+            ipp = ctypes.POINTER(ctypes.c_int)
+            _check(L.athgpu_set_multilevel(
+                h, ml[0].ctypes.data_as(ipp), ml[1].ctypes.data_as(ipp),
+                ml[2].ctypes.data_as(ipp),
+                ml[3].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                *[_dp(c) for c in cc]), "athgpu_set_multilevel")
 
     def close(self):
         if getattr(self, "h", None):
@@ -298,3 +318,20 @@ class StageUpdate:
         _check(load_library().athgpu_device_state_ptrs(self.h, ctypes.byref(s)),
                "athgpu_device_state_ptrs")
         return s
+
+
+def ml_plan_check(mesh):
+    """Build and bounds-check the multi-level operation lists of a MultiLevelMesh on the
+    host (no device needed).  Returns (restriction ops, exchange ops, prolongation ops,
+    flux-correction tasks); raises AthGPUError on an inconsistent mesh."""
+    L = load_library()
+    t, cnt, lv, loc = [np.ascontiguousarray(a) for a in mesh.neighbor_table()]
+    ip = ctypes.POINTER(ctypes.c_int)
+    nx = (ctypes.c_int * 3)(*mesh.bx)
+    bc = (ctypes.c_int * 6)(*mesh.bcs)
+    out = (ctypes.c_longlong * 4)()
+    _check(L.athgpu_ml_plan_check(nx, mesh.ng, bc, mesh.nblocks, t.ctypes.data_as(ip),
+                                  cnt.ctypes.data_as(ip), lv.ctypes.data_as(ip),
+                                  loc.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                                  out), "athgpu_ml_plan_check")
+    return tuple(out)

@@ -74,6 +74,39 @@ typedef struct {
 #define ATHGPU_BC_OUTFLOW 1
 #define ATHGPU_BC_REFLECT 2
 
+/* Host-only check of a multi-level mesh description (no device needed): builds the
+ * operation lists athgpu_set_multilevel would upload and checks every index they touch
+ * against the array bounds.  nx[3] interior cells per block, bc[6] mesh-face flags, the
+ * tables as for athgpu_set_multilevel.  counts (optional, 4 entries): operations of the
+ * restriction, exchange and prolongation lists, flux-correction tasks. */
+athgpu_status athgpu_ml_plan_check(const int* nx, int nghost, const int* bc, int nblocks,
+                                   const int* nbr_table, const int* nbr_count,
+                                   const int* nblevel, const long long* loc,
+                                   long long* counts);
+
+/* Turn the context into a multi-level mesh (static or adaptive mesh refinement;
+ * Newtonian MHD, even nghost, even MeshBlock sizes >= 4).  Call after athgpu_create and
+ * before athgpu_initialize.  The descriptor then lists the MeshBlocks as nbx1 = number of
+ * blocks, nbx2 = nbx3 = 1, in the reference's gid order (MeshBlockTree::GetMeshBlockList,
+ * mesh/meshblock_tree.cpp:336-355) with every block's own coordinates.  Per block:
+ *   nbr_table[b][56][10]  its neighbour list (BoundaryBase::neighbor, bvals/bvals_base.cpp:
+ *                         300-720): gid, level, ox1, ox2, ox3, type (0 face, 1 edge,
+ *                         2 corner), fi1, fi2, fid, eid; nbr_count[b] entries used;
+ *   nblevel[b][27]        neighbour levels at (ox3+1)*9+(ox2+1)*3+(ox1+1), -1 for none
+ *                         (BoundaryBase::nblevel);
+ *   loc[b][4]             level, lx1, lx2, lx3 (LogicalLocation);
+ *   cx?f[b][ncc?+1], cdx?f[b][ncc?]  the coarse-buffer face coordinates (the reference's
+ *                         MeshRefinement::pcoarsec, ncc = nx/2 + 2 nghost).
+ * Replaces: the multilevel branches of TimeIntegratorTaskList (time_integrator.cpp:
+ * 926-1162: flux and EMF correction, PROLONG), BoundaryValues::ProlongateBoundaries
+ * (bvals/bvals_refine.cpp:97) and the buffer functions of bvals/cc and bvals/fc. */
+athgpu_status athgpu_set_multilevel(athgpu_ctx* ctx, const int* nbr_table,
+                                    const int* nbr_count, const int* nblevel,
+                                    const long long* loc, const double* cx1f,
+                                    const double* cdx1f, const double* cx2f,
+                                    const double* cdx2f, const double* cx3f,
+                                    const double* cdx3f);
+
 /* Allocate all device registers of the stage update for the mesh (replaces the
  * Hydro/Field/EquationOfState/Reconstruction constructors, hydro.cpp:31-148,
  * field.cpp:27-105). */

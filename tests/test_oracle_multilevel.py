@@ -59,3 +59,17 @@ def test_tree_balance_and_neighbour_lists():
             back = [e for e in m.nbrs[q.gid] if e.gid == b and
                     (e.ox1, e.ox2, e.ox3) == (-q.ox1, -q.ox2, -q.ox3)]
             assert len(back) == 1, (b, q)
+
+
+def test_gpu_plan_builds_and_stays_in_bounds_on_the_host():
+    """The library's multi-level planner (no device needed) accepts the golden meshes and a
+    three-level periodic mesh, every operation's indices within the array bounds."""
+    from athena_gb300.runtime import ml_plan_check
+    for name in ml_case_names():
+        _, mesh, _, _ = load_ml_case(name)
+        counts = ml_plan_check(mesh)
+        assert counts[1] > 0 and counts[2] > 0 and counts[3] > 0
+    m = MultiLevelMesh((32, 32, 32), (4, 4, 4), 2, (-.5, -.5, -.5), (.5, .5, .5),
+                       bcs=(0, 0, 0, 0, 0, 0),
+                       regions=[((0.3, 0.3, 0.3), (0.35, 0.35, 0.35), 2)])
+    assert ml_plan_check(m)[3] > 0
