@@ -80,6 +80,7 @@ class MeshTree:
             self.root_level += 1
         self.root = _Node(Loc(0, 0, 0, 0))
         self._create_root(self.root)
+        self.nnew = self.ndel = 0   # blocks made and removed (Refine's nnew, Derefine's ndel)
 
     # --- construction (meshblock_tree.cpp:87-258) ----------------------------------
     def _create_root(self, node):
@@ -117,11 +118,19 @@ class MeshTree:
             (((rloc.lx3 >> sh) & 1) << 2)
         self._add(node.leaf[n], rloc)
 
+    def refine(self, node):
+        """MeshBlockTree::Refine (meshblock_tree.cpp:166-258): split a leaf and refine every
+        coarser neighbour so that adjacent blocks differ by at most one level."""
+        self._refine(node)
+
     def _refine(self, node):
         if node.leaf is not None:
             return
-        node.leaf = [_Node(self._child_loc(node.loc, n & 1, (n >> 1) & 1, (n >> 2) & 1))
-                     for n in range(8)]
+        self.nnew += 7
+        # the children inherit the parent's gid (meshblock_tree.cpp:62), which maps the new
+        # blocks back to the old block they were refined from
+        node.leaf = [_Node(self._child_loc(node.loc, n & 1, (n >> 1) & 1, (n >> 2) & 1),
+                           node.gid) for n in range(8)]
         lev = node.loc.level
         nmax = [self.nrbx[d] << (lev - self.root_level) for d in range(3)]
         for oz in (-1, 0, 1):
@@ -182,14 +191,19 @@ class MeshTree:
         """Make a refined node a leaf again (it inherits its first child's gid)."""
         node.gid = node.leaf[0].gid
         node.leaf = None
+        self.ndel += 7
 
     # --- queries (meshblock_tree.cpp:317-487) --------------------------------------
-    def block_list(self):
-        """Leaves in gid order; also stores each leaf's gid."""
+    def block_list(self, old_gids=None):
+        """Leaves in gid order; also stores each leaf's gid.  ``old_gids`` (a list) receives
+        each leaf's previous gid: the block it was refined from, the first child it was
+        derefined from, or itself (GetMeshBlockList's pglist, meshblock_tree.cpp:336-352)."""
         out = []
 
         def walk(node):
             if node.leaf is None:
+                if old_gids is not None:
+                    old_gids.append(node.gid)
                 node.gid = len(out)
                 out.append(node.loc)
             else:
@@ -395,7 +409,9 @@ class MultiLevelMesh:
 
     def rebuild(self):
         """Recompute the block list, neighbour lists and coordinates from the tree."""
-        self.locs = self.tree.block_list()
+        old = []
+        self.locs = self.tree.block_list(old)
+        self.old_gids = np.array(old, dtype=np.int32)
         self.nblocks = len(self.locs)
         self.levels = np.array([l.level for l in self.locs], dtype=np.int32)
         self.nbrs, self.nblevels = [], []

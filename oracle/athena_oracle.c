@@ -1744,17 +1744,25 @@ void orc_stage(orc_mesh *m, int stage) {
   all_bcs(m, m->w);        /* PhysicalBoundary task, :2278-2299 */
 }
 
-void orc_cycle(orc_mesh *m) {
+/* the stages of one cycle and time += dt (main.cpp:535), without the new time step */
+void orc_advance(orc_mesh *m) {
   if (m->rk1) {  /* integrator = rk1: one stage, beta = delta = 1, order xorder */
     ml_stage_w(m, 1.0, 1.0, m->p.xorder);
-    m->time += m->dt;
-    all_new_dt(m);
-    return;
+  } else {
+    orc_stage(m, 1);
+    orc_stage(m, 2);
   }
-  orc_stage(m, 1);
-  orc_stage(m, 2);
-  m->time += m->dt;  /* main.cpp:535 */
-  all_new_dt(m);     /* NewBlockTimeStep (last stage) + Mesh::NewTimeStep */
+  m->time += m->dt;
+}
+
+/* NewBlockTimeStep of every block (last stage) + Mesh::NewTimeStep */
+void orc_new_dt(orc_mesh *m) { all_new_dt(m); }
+
+void orc_set_time(orc_mesh *m, double t) { m->time = t; }
+
+void orc_cycle(orc_mesh *m) {
+  orc_advance(m);
+  all_new_dt(m);
 }
 
 #include "athena_oracle_ml.c"

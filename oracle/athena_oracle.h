@@ -81,6 +81,22 @@ int orc_set_multilevel(orc_mesh *m, const int *nbr_table, const int *nbr_count,
 
 /* use the one-stage rk1 integrator in orc_cycle (multi-level meshes; diagnostics) */
 void orc_set_rk1(orc_mesh *m, int on);
+/* the stages of one cycle and time += dt, without the new time step (adaptive runs
+ * regrid in between); then orc_new_dt: NewBlockTimeStep + Mesh::NewTimeStep */
+void orc_advance(orc_mesh *m);
+void orc_new_dt(orc_mesh *m);
+void orc_set_time(orc_mesh *m, double t);
+/* multi-level mesh: orc_initialize without the time step (one pass of the loop of
+ * Mesh::Initialize with adaptive refinement) */
+void orc_ml_boundaries(orc_mesh *m);
+/* the blast problem's refinement measure per block (max |grad p|/p), maxeps[nb] */
+void orc_refine_eps(const orc_mesh *m, double *maxeps);
+/* fill the new multi-level mesh d from the old mesh s (one rank's
+ * RedistributeAndRefineMeshBlocks): kind[n] 0 kept, 1 restricted from newtoold[n]..+7,
+ * 2 prolongated from newtoold[n] with the face-field corrections ffc[nffc][3] =
+ * (new block, receiving face, old block); copies time and dt. */
+int orc_regrid(orc_mesh *d, orc_mesh *s, const int *newtoold, const int *kind, int nffc,
+               const int *ffc);
 
 /* per-cell SR conserved->primitive (adiabatic_mhd_sr.cpp:404-522) on independent
  * cells: cons[n][5] (D, E, M1..M3 in the reference's IDN,IEN,IM1..IM3 slots), bcc[n][3],

@@ -1394,14 +1394,20 @@ static void ml_stage_w(orc_mesh *m, double beta, double delta, int order) {
   all_bcs(m, m->w);
 }
 
-static void ml_initialize(orc_mesh *m) {
-  /* Mesh::Initialize (mesh.cpp:1698-1964): exchange of U and B, ProlongateBoundaries,
-   * W(U) over the ranges the neighbour levels give, physical boundaries, first dt */
+/* the body of Mesh::Initialize's loop (mesh.cpp:1674-1930): exchange of U and B,
+ * ProlongateBoundaries, W(U) over the ranges the neighbour levels give, physical
+ * boundaries */
+void orc_ml_boundaries(orc_mesh *m) {
   ml_exchange(m, m->u, NHYDRO, m->ml->ccons, m->b1, m->b2, m->b3);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < m->nb; ++b) ml_prolongate_block(m, b, m->w);
   all_con2prim(m, m->w);
   all_bcs(m, m->w);
+}
+
+static void ml_initialize(orc_mesh *m) {
+  /* Mesh::Initialize (mesh.cpp:1698-1964): the boundaries, then the first dt */
+  orc_ml_boundaries(m);
   all_new_dt(m);
 }
 
@@ -1490,3 +1496,134 @@ int orc_set_multilevel(orc_mesh *m, const int *nbr_table, const int *nbr_count,
 }
 
 void orc_set_rk1(orc_mesh *m, int on) { m->rk1 = on; }
+
+/* ---- adaptive refinement ---------------------------------------------------------------- */
+
+/* The blast problem's refinement measure (pgen/blast.cpp:413-443, 3-D branch): per block
+ * the maximum over the interior and one ghost layer of |grad p| / p from centred
+ * differences of the current primitives. */
+void orc_refine_eps(const orc_mesh *m, double *maxeps) {
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < m->nb; ++b) {
+    const double *p = m->w + ((long)b * NHYDRO + IPR) * m->ncell;
+    double mx = 0.0;
+    for (int k = m->ks - 1; k <= m->ke + 1; ++k)
+      for (int j = m->js - 1; j <= m->je + 1; ++j)
+        for (int i = m->is - 1; i <= m->ie + 1; ++i) {
+          double a = 0.5 * (p[CIDX(m, 0, k, j, i + 1)] - p[CIDX(m, 0, k, j, i - 1)]);
+          double c = 0.5 * (p[CIDX(m, 0, k, j + 1, i)] - p[CIDX(m, 0, k, j - 1, i)]);
+          double e = 0.5 * (p[CIDX(m, 0, k + 1, j, i)] - p[CIDX(m, 0, k - 1, j, i)]);
+          double eps = sqrt(SQR(a) + SQR(c) + SQR(e)) / p[CIDX(m, 0, k, j, i)];
+          mx = smax(mx, eps);
+        }
+    maxeps[b] = mx;
+  }
+}
+
+/* Mesh::RedistributeAndRefineMeshBlocks on one rank (amr_loadbalance.cpp:351-660): fill
+ * the new mesh d (multi-level tables already set) from the old mesh s.  Per new block n,
+ * kind[n] 0: the old block newtoold[n] is kept (all its arrays move); 1: restriction of the
+ * eight old children newtoold[n]..+7 into the block's octants (FillSameRankFineToCoarseAMR,
+ * :827-946); 2: the old parent's U and B with a one-cell halo into the coarse buffers
+ * (FillSameRankCoarseToFineAMR, :948-1030), the face-field corrections ffc[nffc][3] =
+ * (new block, receiving face, old block) from old same-level neighbours
+ * (ReceiveAndSetFaceFieldCorrection, :1387-1444), then ProlongateMeshBlock (:1172-1222).
+ * The new blocks start from zero arrays, as newly constructed MeshBlocks do. */
+int orc_regrid(orc_mesh *d, orc_mesh *s, const int *newtoold, const int *kind, int nffc,
+               const int *ffc) {
+  if (!d->ml || !s->ml || d->ncell != s->ncell) return -1;
+  orc_ml *dm = d->ml, *sm = s->ml;
+  const int hx[3] = {d->p.nx1 / 2, d->p.nx2 / 2, d->p.nx3 / 2};
+  double *sfb[3] = {s->b1, s->b2, s->b3}, *dfb[3] = {d->b1, d->b2, d->b3};
+  double *scb[3] = {sm->cb1, sm->cb2, sm->cb3}, *dcb[3] = {dm->cb1, dm->cb2, dm->cb3};
+  long nfs[3] = {d->nf1, d->nf2, d->nf3};
+  const int clo[3] = {dm->cis, dm->cjs, dm->cks}, chi[3] = {dm->cie, dm->cje, dm->cke};
+  const int flo[3] = {d->is, d->js, d->ks}, fhi[3] = {d->ie, d->je, d->ke};
+  for (int n = 0; n < d->nb; ++n) {
+    int on = newtoold[n];
+    if (kind[n] == 0) {
+      memcpy(d->u + (long)n * NHYDRO * d->ncell, s->u + (long)on * NHYDRO * s->ncell,
+             sizeof(double) * NHYDRO * d->ncell);
+      memcpy(d->w + (long)n * NHYDRO * d->ncell, s->w + (long)on * NHYDRO * s->ncell,
+             sizeof(double) * NHYDRO * d->ncell);
+      memcpy(d->bcc + (long)n * 3 * d->ncell, s->bcc + (long)on * 3 * s->ncell,
+             sizeof(double) * 3 * d->ncell);
+      for (int a = 0; a < 3; ++a)
+        memcpy(dfb[a] + n * nfs[a], sfb[a] + on * nfs[a], sizeof(double) * nfs[a]);
+      /* the kept MeshBlock keeps its coarse buffers too */
+      long ncc = dm->nccell, ncf[3] = {dm->ncf1, dm->ncf2, dm->ncf3};
+      memcpy(dm->ccons + n * NHYDRO * ncc, sm->ccons + on * NHYDRO * ncc,
+             sizeof(double) * NHYDRO * ncc);
+      memcpy(dm->cprim + n * NHYDRO * ncc, sm->cprim + on * NHYDRO * ncc,
+             sizeof(double) * NHYDRO * ncc);
+      memcpy(dm->cbcc + n * 3 * ncc, sm->cbcc + on * 3 * ncc, sizeof(double) * 3 * ncc);
+      for (int a = 0; a < 3; ++a)
+        memcpy(dcb[a] + n * ncf[a], scb[a] + on * ncf[a], sizeof(double) * ncf[a]);
+    } else if (kind[n] == 1) {
+      for (int l = 0; l < 8; ++l) {
+        int c = on + l;
+        int o[3];
+        for (int a = 0; a < 3; ++a) o[a] = flo[a] + (int)(ml_lx(s, c, a) & 1LL) * hx[a];
+        box3 cb = {{clo[0], clo[1], clo[2]}, {chi[0], chi[1], chi[2]}};
+        box3 db = {{o[0], o[1], o[2]}, {o[0] + hx[0] - 1, o[1] + hx[1] - 1, o[2] + hx[2] - 1}};
+        for (int v = 0; v < NHYDRO; ++v) {
+          view3 cv = coarse_cc(sm, sm->ccons, c, NHYDRO, v);
+          restrict_cc(s, c, fine_cc(s, s->u, c, NHYDRO, v), cv, cb);
+          copy_box(fine_cc(d, d->u, n, NHYDRO, v), db, cv, cb);
+        }
+        for (int a = 0; a < 3; ++a) {
+          box3 cf = cb, df = db;
+          cf.e[a] += 1; df.e[a] += 1;
+          view3 cv = coarse_fc(sm, a, scb[a], c);
+          restrict_fc(s, c, a, fine_fc(s, a, sfb[a], c), cv, cf);
+          copy_box(fine_fc(d, a, dfb[a], n), df, cv, cf);
+        }
+      }
+    } else {
+      int o[3];
+      for (int a = 0; a < 3; ++a)
+        o[a] = (int)(ml_lx(d, n, a) & 1LL) * hx[a] + flo[a] - 1;
+      box3 cb = {{clo[0] - 1, clo[1] - 1, clo[2] - 1}, {chi[0] + 1, chi[1] + 1, chi[2] + 1}};
+      box3 sb = {{o[0], o[1], o[2]}, {o[0] + hx[0] + 1, o[1] + hx[1] + 1, o[2] + hx[2] + 1}};
+      for (int v = 0; v < NHYDRO; ++v)
+        copy_box(coarse_cc(dm, dm->ccons, n, NHYDRO, v), cb, fine_cc(s, s->u, on, NHYDRO, v),
+                 sb);
+      for (int a = 0; a < 3; ++a) {
+        box3 cf = cb, sf = sb;
+        cf.e[a] += 1; sf.e[a] += 1;
+        copy_box(coarse_fc(dm, a, dcb[a], n), cf, fine_fc(s, a, sfb[a], on), sf);
+      }
+    }
+  }
+  /* face-field corrections: the receiving face of the child from the facing face of the
+   * old same-level neighbour */
+  for (int t = 0; t < nffc; ++t) {
+    int n = ffc[3 * t], f = ffc[3 * t + 1], i = ffc[3 * t + 2], a = f >> 1;
+    box3 rb = {{flo[0], flo[1], flo[2]}, {fhi[0], fhi[1], fhi[2]}}, sb = rb;
+    rb.s[a] = rb.e[a] = (f & 1) ? fhi[a] + 1 : flo[a];
+    sb.s[a] = sb.e[a] = (f & 1) ? flo[a] : fhi[a] + 1;
+    copy_box(fine_fc(d, a, dfb[a], n), rb, fine_fc(s, a, sfb[a], i), sb);
+  }
+  for (int n = 0; n < d->nb; ++n) {
+    if (kind[n] != 2) continue;
+    int got[6] = {0, 0, 0, 0, 0, 0};
+    for (int t = 0; t < nffc; ++t)
+      if (ffc[3 * t] == n) got[ffc[3 * t + 1]] = 1;
+    box3 c = {{clo[0], clo[1], clo[2]}, {chi[0], chi[1], chi[2]}};
+    for (int v = 0; v < NHYDRO; ++v)
+      prolong_cc(d, n, coarse_cc(dm, dm->ccons, n, NHYDRO, v), fine_cc(d, d->u, n, NHYDRO, v),
+                 c);
+    for (int a = 0; a < 3; ++a) {
+      box3 cf = c;
+      cf.e[a] += 1;
+      if (got[2 * a]) cf.s[a]++;
+      if (got[2 * a + 1]) cf.e[a]--;
+      prolong_shared(d, n, a, coarse_fc(dm, a, dcb[a], n), fine_fc(d, a, dfb[a], n), cf);
+    }
+    prolong_internal(d, n, fine_fc(d, 0, d->b1, n), fine_fc(d, 1, d->b2, n),
+                     fine_fc(d, 2, d->b3, n), c);
+  }
+  d->time = s->time;
+  d->dt = s->dt;
+  return 0;
+}

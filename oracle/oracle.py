@@ -73,6 +73,13 @@ def lib():
                                          ctypes.POINTER(ctypes.c_longlong)] + [dp] * 6
         L.orc_set_multilevel.restype = ctypes.c_int
         L.orc_set_rk1.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_advance.argtypes = [ctypes.c_void_p]
+        L.orc_new_dt.argtypes = [ctypes.c_void_p]
+        L.orc_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_ml_boundaries.argtypes = [ctypes.c_void_p]
+        L.orc_refine_eps.argtypes = [ctypes.c_void_p, dp]
+        L.orc_regrid.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ip, ip, ctypes.c_int, ip]
+        L.orc_regrid.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -88,6 +95,10 @@ class OracleMesh:
                  dfloor=None, pfloor=None, relativistic=False, threads=0, sigma_max=0.0,
                  beta_min=0.0, gamma_max=1000.0, bc=(0, 0, 0, 0, 0, 0)):
         L = lib()
+        self.kw = dict(gamma=gamma, xorder=xorder, rsolver=rsolver, cfl=cfl, tlim=tlim,
+                       dfloor=dfloor, pfloor=pfloor, relativistic=relativistic,
+                       threads=threads, sigma_max=sigma_max, beta_min=beta_min,
+                       gamma_max=gamma_max, bc=bc)
         import math
         fmin = float(np.finfo(np.float32).tiny)
         floor = math.sqrt(1024 * fmin)   # adiabatic_mhd.cpp:29-30
@@ -164,6 +175,43 @@ class OracleMesh:
 
     def stage(self, s):
         lib().orc_stage(self.h, s)
+
+    # --- adaptive refinement ---------------------------------------------------------
+    def advance(self):
+        """The stages of one cycle and time += dt, without the new time step."""
+        lib().orc_advance(self.h)
+
+    def new_dt(self):
+        lib().orc_new_dt(self.h)
+
+    def boundaries(self):
+        """Multi-level mesh: initialize() without the time step."""
+        lib().orc_ml_boundaries(self.h)
+
+    def set_clock(self, time, dt):
+        lib().orc_set_time(self.h, time)
+        lib().orc_set_dt(self.h, dt)
+
+    def refine_eps(self):
+        out = np.zeros(self.mesh.nblocks)
+        lib().orc_refine_eps(self.h, _p(out))
+        return out
+
+    def regrid(self, plan):
+        """A new OracleMesh for plan.mesh filled from this one
+        (RedistributeAndRefineMeshBlocks), then Mesh::Initialize(2): ghost exchange,
+        ProlongateBoundaries, W(U), physical boundaries, NewBlockTimeStep +
+        NewTimeStep."""
+        new = OracleMesh(plan.mesh, **self.kw)
+        ip = ctypes.POINTER(ctypes.c_int)
+        arrs = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (plan.newtoold, plan.kind, plan.ffc.reshape(-1))]
+        rc = lib().orc_regrid(new.h, self.h, *[a.ctypes.data_as(ip) for a in arrs[:2]],
+                              int(plan.ffc.shape[0]), arrs[2].ctypes.data_as(ip))
+        if rc != 0:
+            raise ValueError("regrid failed (%d)" % rc)
+        new.initialize()
+        return new
 
 
 def sr_c2p_cells(cons, bcc, guess, gamma):

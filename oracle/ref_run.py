@@ -48,10 +48,11 @@ def athinput(mesh, gamma, xorder, cfl, nlim, tlim, problem, extra_problem=None,
 
 def athinput_multilevel(mesh, gamma, xorder, cfl, nlim, tlim, problem,
                         refinement="static", regions=(), numlevel=None, amr=None,
-                        integrator="vl2"):
+                        integrator="vl2", hydro=None):
     """Text of an athinput file for a multi-level mesh (meshtree.MultiLevelMesh):
     static refinement regions [(xmin3, xmax3, level)] and/or adaptive refinement
-    (numlevel, and the <mesh> AMR keys in amr, e.g. derefine_count)."""
+    (numlevel, and the <mesh> AMR keys in amr, e.g. derefine_count); extra <hydro> keys
+    in hydro (e.g. dfloor, pfloor)."""
     lines = ["<job>", "problem_id = Ref", "<time>", "cfl_number = %r" % cfl,
              "nlim = %d" % nlim, "tlim = %r" % tlim, "integrator = %s" % integrator,
              "xorder = %s" % xorder, "ncycle_out = 100000", "<mesh>"]
@@ -73,7 +74,10 @@ def athinput_multilevel(mesh, gamma, xorder, cfl, nlim, tlim, problem,
         for d, n in enumerate(("1", "2", "3")):
             lines += ["x%smin = %r" % (n, lo[d]), "x%smax = %r" % (n, hi[d])]
         lines.append("level = %d" % lev)
-    lines += ["<hydro>", "gamma = %r" % gamma, "iso_sound_speed = 1.0", "<problem>"]
+    lines += ["<hydro>", "gamma = %r" % gamma, "iso_sound_speed = 1.0"]
+    for k, v in (hydro or {}).items():
+        lines.append("%s = %s" % (k, v))
+    lines.append("<problem>")
     for k, v in (problem or {}).items():
         lines.append("%s = %s" % (k, v))
     return "\n".join(lines) + "\n"

@@ -88,6 +88,77 @@ ML_CASES = {
 }
 
 
+# adaptive (blast pressure-gradient) cases: variant, MultiLevelMesh args (nx, nrbx, ng,
+# xmin, xmax, bcs), blast parameters (with thr), numlevel, derefine_count, xorder, cfl,
+# ncycle.  The floors are given explicitly: with the defaults, the reference's first
+# MeshBlock uses sqrt(1024 FLT_MIN) while every later one reads back the 6-digit string
+# that GetOrAddReal stored (parameter_input.cpp:603-623), and the blast reaches the
+# pressure floor.
+AMR_FLOOR = "3.46945e-18"
+AMR_CASES = {
+    "amrblast_hlle_plm": ("mhd_hlle_g2", ((32, 32, 32), (4, 4, 4), 2, (-.5, -.5, -.5),
+                                          (.5, .5, .5), (0, 0, 0, 0, 0, 0)),
+                          {"radius": 0.1, "pamb": 0.1, "prat": 100.0, "b0": 1.0,
+                           "angle": 45.0, "x1_0": 0.0, "x2_0": 0.0, "x3_0": 0.0,
+                           "thr": 0.5}, 3, 2, 2, 0.3, 10),
+    "amrblast_hlld_ppm": ("mhd_hlld_g4", ((32, 32, 32), (4, 4, 4), 4, (-.5, -.5, -.5),
+                                          (.5, .5, .5), (0, 0, 0, 0, 0, 0)),
+                          {"radius": 0.12, "pamb": 0.1, "prat": 100.0, "b0": 1.0,
+                           "angle": 30.0, "x1_0": 0.3, "x2_0": 0.0, "x3_0": 0.0,
+                           "thr": 1.0}, 3, 1, 3, 0.3, 12),
+}
+
+
+def state_digest(mesh, u, b1, b2, b3):
+    """sha256 of the interior conserved state and face field in block order."""
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(mesh.interior(u)).tobytes())
+    for b in (b1, b2, b3):
+        h.update(np.ascontiguousarray(mesh.interior_faces(b)).tobytes())
+    return h.hexdigest()
+
+
+def run_amr_case(name, spec):
+    """An adaptive blast through the reference's own pgen/blast.cpp with
+    refinement = adaptive.  Stores every cycle's block list (after the stages, before the
+    regrid) and dt, and the last cycle's state as a digest and per-block sums."""
+    from athena_gb300.meshtree import MultiLevelMesh
+    variant, margs, prob, numlevel, dcount, xorder, cfl, ncycle = spec
+    nx, nrbx, ng, xmin, xmax, bcs = margs
+    mesh0 = MultiLevelMesh(nx, nrbx, ng, xmin, xmax, bcs=bcs)
+    gamma = 5.0 / 3.0
+    text = ref_run.athinput_multilevel(mesh0, gamma, xorder, cfl, ncycle, 1.0e3, prob,
+                                       refinement="adaptive", numlevel=numlevel,
+                                       amr={"derefine_count": dcount},
+                                       hydro={"dfloor": AMR_FLOOR, "pfloor": AMR_FLOOR})
+    d, _ = ref_run.run_reference(variant, "athena_blast", text)
+    locs, offs, dts, nregrid, prev = [], [0], [], 0, None
+    for c in range(1, ncycle + 1):
+        dump = ref_run.read_dump_blocks(os.path.join(d, "dump.%05d.bin" % c))
+        locs += dump["locs"]
+        offs.append(len(locs))
+        dts.append(dump["dt"])
+        nregrid += int(prev is not None and prev != dump["locs"])
+        prev = dump["locs"]
+    mesh = MultiLevelMesh(nx, nrbx, ng, xmin, xmax, bcs=bcs)
+    from athena_gb300.meshtree import Loc
+    for lv, a, b, c3 in dump["locs"]:
+        mesh.tree.add_block(Loc(lv, a, b, c3))
+    mesh.rebuild()
+    assert [(l.level, l.lx1, l.lx2, l.lx3) for l in mesh.locs] == dump["locs"]
+    sums = mesh.interior(dump["u"]).sum(axis=(2, 3, 4))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"),
+                        locs=np.array(locs, dtype=np.int32), offsets=np.array(offs),
+                        dt=np.array(dts), usum=sums)
+    return {"variant": variant, "nx": nx, "nrbx": nrbx, "ng": ng, "xmin": xmin,
+            "xmax": xmax, "bc": list(bcs), "problem": prob, "numlevel": numlevel,
+            "derefine_count": dcount, "floor": float(AMR_FLOOR), "xorder": xorder,
+            "rsolver": "hlld" if "hlld" in variant else "hlle", "cfl": cfl,
+            "ncycle": ncycle, "gamma": gamma, "tlim": 1.0e3, "time": dump["time"],
+            "digest": state_digest(mesh, dump["u"], dump["b1"], dump["b2"], dump["b3"]),
+            "nblocks_last": len(dump["locs"]), "regrids": nregrid}
+
+
 def ml_mesh(margs):
     from athena_gb300.meshtree import MultiLevelMesh
     nx, nrbx, ng, xmin, xmax, bcs, regions = margs
@@ -238,7 +309,8 @@ def run_history(name="turb_hlld_ppm_8blk"):
 
 
 def main(only=None):
-    for v in sorted({c[0] for c in CASES.values()} | {c[0] for c in ML_CASES.values()}):
+    for v in sorted({c[0] for c in CASES.values()} | {c[0] for c in ML_CASES.values()}
+                    | {c[0] for c in AMR_CASES.values()}):
         build_ref.build_variant(v)
     meta = {"cases": {}}
     path = os.path.join(OUT, "golden.json")
@@ -256,6 +328,12 @@ def main(only=None):
             continue
         print("case", name, flush=True)
         meta["ml_cases"][name] = run_ml_case(name, spec)
+    meta.setdefault("amr_cases", {})
+    for name, spec in AMR_CASES.items():
+        if only and name not in only:
+            continue
+        print("case", name, flush=True)
+        meta["amr_cases"][name] = run_amr_case(name, spec)
     if not only or "history" in only:
         print("history", flush=True)
         meta["history"] = run_history()

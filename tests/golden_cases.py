@@ -85,3 +85,31 @@ def load_ml_case(name):
     ref = {k: z[k] for k in ("u", "b1", "b2", "b3", "w", "dt")}
     ref["time"] = float(z["time"])
     return c, mesh, ic, ref
+
+
+def amr_case_names():
+    """Names of the adaptive-refinement golden cases."""
+    return sorted(meta().get("amr_cases", {}))
+
+
+def load_amr_case(name):
+    """(params, root MultiLevelMesh, problem generator ic(mesh), reference outputs: per
+    cycle block lists and dt, the last cycle's state digest and per-block sums of U)."""
+    from athena_gb300 import pgen
+    from athena_gb300.meshtree import MultiLevelMesh
+    c = meta()["amr_cases"][name]
+    mesh0 = MultiLevelMesh(tuple(c["nx"]), tuple(c["nrbx"]), c["ng"], tuple(c["xmin"]),
+                           tuple(c["xmax"]), bcs=tuple(c["bc"]))
+    p = c["problem"]
+
+    def ic(mesh):
+        return pgen.blast_blocks(mesh, c["gamma"], radius=p["radius"], pamb=p["pamb"],
+                                 prat=p["prat"], b0=p["b0"], angle_deg=p["angle"],
+                                 center=(p["x1_0"], p["x2_0"], p["x3_0"]))
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    offs = z["offsets"]
+    locs = [[tuple(int(v) for v in r) for r in z["locs"][offs[i]:offs[i + 1]]]
+            for i in range(len(offs) - 1)]
+    ref = {"locs": locs, "dt": z["dt"], "usum": z["usum"], "digest": c["digest"],
+           "time": c["time"]}
+    return c, mesh0, ic, ref
