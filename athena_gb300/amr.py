@@ -59,24 +59,19 @@ class AdaptiveMesh:
         refine flags (1 refine, -1 derefine, 0 keep)."""
         m = self.mesh
         root = m.tree.root_level
+        aret = np.maximum(np.asarray(ret, dtype=np.int32), -1)
+        level = m.levels
+        dc = self.deref_count
+        dc[aret >= 0] = 0
         flags = np.zeros(m.nblocks, dtype=np.int32)
-        for b in range(m.nblocks):
-            aret = max(-1, int(ret[b]))
-            level = m.locs[b].level
-            if aret >= 0:
-                self.deref_count[b] = 0
-            if aret > 0:
-                flags[b] = 0 if level == self.max_level else 1
-            elif aret < 0:
-                if level == root:
-                    self.deref_count[b] = 0
-                else:
-                    self.deref_count[b] += 1
-                    # no derefinement next to a finer block
-                    if (np.asarray(m.nblevels[b]) > level).any():
-                        flags[b] = 0
-                    elif self.deref_count[b] >= self.derefine_count:
-                        flags[b] = -1
+        flags[(aret > 0) & (level != self.max_level)] = 1
+        neg = aret < 0
+        dc[neg & (level == root)] = 0
+        der = neg & (level != root)
+        dc[der] += 1
+        # no derefinement next to a finer block
+        finer = (m.nblevel_array() > level[:, None]).any(axis=1)
+        flags[der & ~finer & (dc >= self.derefine_count)] = -1
         return flags
 
     def update(self, flags):

@@ -29,6 +29,10 @@ UNITS = {
     "history.cu": ["-fmad=false"],
     # host planner of the multi-level stage
     "ml_plan.cu": ["-fmad=false"],
+    # adaptive refinement: refinement measure and regrid (FP64 restriction/prolongation)
+    "regrid.cu": ["-fmad=false"],
+    # adaptive refinement, host side: block tree, neighbour lists, coordinates, flags
+    "amr_host.cu": ["-fmad=false"],
 }
 
 

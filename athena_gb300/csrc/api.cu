@@ -57,6 +57,7 @@ void free_all(athgpu_ctx* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fxv) cudaFree(c->fxv);
+  if (c->eps_buf) cudaFree(c->eps_buf);
   for (void* p : c->mld.allocs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
@@ -98,6 +99,11 @@ athgpu_status download_bulk(athgpu_ctx* c, double* h, const void* dev, const voi
   return ATHGPU_OK;
 }
 }  // namespace
+
+namespace athgpu {
+// the error path of the entry points defined in other translation units
+athgpu_status api_fail(athgpu_status code, const std::string& msg) { return fail(code, msg); }
+}  // namespace athgpu
 
 namespace athgpu {
 // lets other translation units report through athgpu_last_error()
@@ -335,6 +341,8 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   memcpy(&hclk.dtmin_bits, &dmax, 8);
   hclk.c2p_floor_count = 0;
   hclk.dtf = (float)hclk.dt;
+  hclk.dt_prev = DBL_MAX;
+  hclk.dtmin_prev_bits = hclk.dtmin_bits;
   e = cudaMemcpy(c->clk, &hclk, sizeof(hclk), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy clock"));
   e = cudaStreamSynchronize(c->stream);
@@ -409,6 +417,7 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
 #define DEV(h, bytes, field) \
   do { cudaError_t e_ = dev(h, bytes, &p); if (e_ != cudaSuccess) return cuda_fail(e_, "multi-level allocation"); field = (decltype(field))p; } while (0)
   const void* nullh = nullptr;
+  c->mld.hloc.assign(loc, loc + (size_t)nb * 4);
   DEV(nblevel, sizeof(int) * (size_t)nb * 27, L.nblev);
   DEV(nbr_table, sizeof(int) * (size_t)nb * ML_MAXNB * ML_NF, L.nbrt);
   DEV(nbr_count, sizeof(int) * (size_t)nb, L.nnbr);

@@ -38,6 +38,7 @@ struct MlDevice {
   void* flux_tasks = nullptr;                  // int4 per task
   int nflux = 0;
   std::vector<void*> allocs;                   // everything allocated for the mesh
+  std::vector<long long> hloc;                 // host copy of loc[nb][4]
 };
 
 struct LaunchConfig {
@@ -55,6 +56,7 @@ struct athgpu_ctx {
   athgpu::DevClock* clk = nullptr;
   double* coords = nullptr;  // dx1f | dx2f | dx3f | plm coefficients (device)
   double* fxv = nullptr;     // cell centres x1v | x2v | x3v per block (prolongation)
+  double* eps_buf = nullptr; // per-block refinement measure (athgpu_refinement_eps)
   athgpu::MlDevice mld;
   float* coords32 = nullptr; // the same, rounded to FP32, for the FP32 kernels
   int* nbr = nullptr;

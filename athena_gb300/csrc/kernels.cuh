@@ -76,6 +76,8 @@ struct DevClock {
   unsigned long long dtmin_bits;  // min over cells of dx/speed, as ordered bits
   int c2p_floor_count;
   float dtf;                      // dt rounded to FP32 (written with dt)
+  double dt_prev;                 // the dt of the last completed cycle
+  unsigned long long dtmin_prev_bits;  // the minimum the last NewTimeStep used
 };
 
 // The mesh scalars, coordinates and dt in the kernel's arithmetic type: the FP64 kernels
@@ -1280,16 +1282,27 @@ copy_ghost_prims_kernel(DevMesh m, Real* __restrict__ w, Real* __restrict__ bcc,
 
 // Mesh::NewTimeStep (mesh.cpp:1236-1281) after the main loop's time += dt
 // (main.cpp:535): dt = min(2 dt_old, cfl * min cell dt), clipped to tlim.
-static __global__ void advance_clock_kernel(DevClock* clk, double cfl, double tlim, int advance) {
+// mode 0: Mesh::NewTimeStep from the blocks' minimum (mesh.cpp:1236-1281); mode 1: time +=
+// dt first (the end of a main-loop cycle, main.cpp:535-541); mode 2: NewTimeStep again
+// from the minimum the previous call used (the main loop's call after a regrid, whose
+// Initialize(2) made the first one)
+static __global__ void advance_clock_kernel(DevClock* clk, double cfl, double tlim, int mode) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (advance) clk->time = clk->time + clk->dt;
-  double block_dt = __longlong_as_double((long long)clk->dtmin_bits) * cfl;
+  if (mode == 1) {
+    clk->dt_prev = clk->dt;
+    clk->time = clk->time + clk->dt;
+  }
+  const unsigned long long bits = mode == 2 ? clk->dtmin_prev_bits : clk->dtmin_bits;
+  double block_dt = __longlong_as_double((long long)bits) * cfl;
   double dt = 2.0 * clk->dt;
   dt = smin<double>(dt, block_dt);
   if (clk->time < tlim && (tlim - clk->time) < dt) dt = tlim - clk->time;
   clk->dt = dt;
   clk->dtf = (float)dt;
-  clk->dtmin_bits = 0x7fefffffffffffffULL;  // DBL_MAX for the next reduction
+  if (mode != 2) {
+    clk->dtmin_prev_bits = clk->dtmin_bits;
+    clk->dtmin_bits = 0x7fefffffffffffffULL;  // DBL_MAX for the next reduction
+  }
 }
 
 }  // namespace athgpu

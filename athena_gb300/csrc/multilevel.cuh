@@ -253,6 +253,10 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
         break;
       }
       case ML_PROLONG_U: {  // mesh_refinement.cpp:464-540
+        // coarse W into W (ProlongateBoundaries), or with src_kind ML_COARSE the coarse
+        // U into U (ProlongateMeshBlock after a refinement, amr_loadbalance.cpp:1172-1180)
+        const Real* csrc = op.src_kind == ML_COARSE ? cu : cw;
+        Real* fdst = op.src_kind == ML_COARSE ? A.u : A.w;
         const int fk = (k - L.cks) * 2 + m.ks, fj = (j - L.cjs) * 2 + m.js,
                   fi = (i - L.cis) * 2 + m.is;
         const double* cx1 = L.cx1v + (i64)b * L.ncc1;
@@ -269,14 +273,14 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
         const double dx1fm = x1c - fx1[fi], dx1fp = fx1[fi + 1] - x1c;
         for (int n = 0; n < NHYDRO; ++n) {
           auto cv = [&](int kk, int jj, int ii) {
-            return ldr(cw + ccidx(m, b, n, NHYDRO, kk, jj, ii));
+            return ldr(csrc + ccidx(m, b, n, NHYDRO, kk, jj, ii));
           };
           const double cc = cv(k, j, i);
           const double g1 = mm_grad(cv(k, j, i - 1), cc, cv(k, j, i + 1), dx1m, dx1p);
           const double g2 = mm_grad(cv(k, j - 1, i), cc, cv(k, j + 1, i), dx2m, dx2p);
           const double g3 = mm_grad(cv(k - 1, j, i), cc, cv(k + 1, j, i), dx3m, dx3p);
           auto put = [&](int kk, int jj, int ii, double v) {
-            A.w[cidx(m, b, n, NHYDRO, fk + kk, fj + jj, fi + ii)] = (Real)v;
+            fdst[cidx(m, b, n, NHYDRO, fk + kk, fj + jj, fi + ii)] = (Real)v;
           };
           put(0, 0, 0, cc - (g1 * dx1fm + g2 * dx2fm + g3 * dx3fm));
           put(0, 0, 1, cc + (g1 * dx1fp - g2 * dx2fm - g3 * dx3fm));

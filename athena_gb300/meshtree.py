@@ -414,11 +414,19 @@ class MultiLevelMesh:
         self.old_gids = np.array(old, dtype=np.int32)
         self.nblocks = len(self.locs)
         self.levels = np.array([l.level for l in self.locs], dtype=np.int32)
+        self._nblev = None
         self.nbrs, self.nblevels = [], []
         for loc in self.locs:
             nb, lv = self.tree.neighbors(loc)
             self.nbrs.append(nb)
             self.nblevels.append(lv)
+
+    def nblevel_array(self):
+        """The neighbour levels as an int32 array [nblocks][27]."""
+        if getattr(self, "_nblev", None) is None or len(self._nblev) != self.nblocks:
+            self._nblev = np.array([np.asarray(v).ravel() for v in self.nblevels],
+                                   dtype=np.int32).reshape(self.nblocks, 27)
+        return self._nblev
 
     # --- array shapes ----------------------------------------------------------------
     @property

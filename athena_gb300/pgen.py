@@ -454,18 +454,24 @@ def sr_isolated_cells(n, seed=20261204, gamma=4.0 / 3.0, lorentz=(1.0, 10.0),
 
 
 def blast_blocks(mesh, gamma=5.0 / 3.0, radius=0.1, pamb=1.0, damb=1.0, prat=100.0,
-                 drat=1.0, b0=1.0, angle_deg=45.0, center=(0.0, 0.0, 0.0)):
+                 drat=1.0, b0=1.0, angle_deg=45.0, center=(0.0, 0.0, 0.0), bfield=None):
     """The reference's blast problem generator (pgen/blast.cpp:53-213, Cartesian, no
     ramp) evaluated on every block of a mesh with per-block coordinates (a
     MultiLevelMesh): rho = drat*damb and p = prat*pamb inside r < radius, damb and pamb
     outside, zero velocity, face field (b0 cos a, b0 sin a, 0), E = p/(gamma-1) + b0^2/2.
-    Returns per-block (u, b1, b2, b3), interior cells and faces set, ghosts zero."""
+    bfield = (bx, by, bz) replaces the planar field by that uniform field (E then adds
+    |B|^2/2).  Returns per-block (u, b1, b2, b3), interior cells and faces set, ghosts
+    zero."""
     ng, (n1, n2, n3) = mesh.ng, mesh.bx
     gm1 = gamma - 1.0
     angle = (3.14159265358979323846 / 180.0) * angle_deg   # PI, defs.hpp.in
     u = np.zeros((mesh.nblocks, 5) + mesh.cell_shape)
     f = [np.zeros((mesh.nblocks,) + s) for s in mesh.face_shapes]
-    bx, by = b0 * math.cos(angle), b0 * math.sin(angle)
+    bx, by, bz = b0 * math.cos(angle), b0 * math.sin(angle), 0.0
+    emag = 0.5 * b0 * b0
+    if bfield is not None:
+        bx, by, bz = (float(v) for v in bfield)
+        emag = 0.5 * (bx * bx + by * by + bz * bz)
     for b in range(mesh.nblocks):
         xv = [mesh.cell_centers(b, d) for d in range(3)]
         x = xv[0][ng:ng + n1][None, None, :] - center[0]
@@ -475,9 +481,10 @@ def blast_blocks(mesh, gamma=5.0 / 3.0, radius=0.1, pamb=1.0, damb=1.0, prat=100
         inside = rad < radius
         u[b, 0, ng:ng + n3, ng:ng + n2, ng:ng + n1] = np.where(inside, drat * damb, damb)
         pres = np.where(inside, prat * pamb, pamb)
-        u[b, 4, ng:ng + n3, ng:ng + n2, ng:ng + n1] = pres / gm1 + 0.5 * b0 * b0
+        u[b, 4, ng:ng + n3, ng:ng + n2, ng:ng + n1] = pres / gm1 + emag
         f[0][b, ng:ng + n3, ng:ng + n2, ng:ng + n1 + 1] = bx
         f[1][b, ng:ng + n3, ng:ng + n2 + 1, ng:ng + n1] = by
+        f[2][b, ng:ng + n3 + 1, ng:ng + n2, ng:ng + n1] = bz
     return u, f[0], f[1], f[2]
 
 

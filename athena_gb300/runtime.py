@@ -105,6 +105,13 @@ def load_library(path=LIB_PATH):
         "athgpu_set_multilevel": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip),
                                    ctypes.POINTER(ip), ctypes.POINTER(ctypes.c_longlong)] +
                                   [dp] * 6, ip),
+        "athgpu_refinement_eps": ([vp, dp], ip),
+        "athgpu_regrid": ([vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(ip),
+                           ctypes.POINTER(ip), ctypes.POINTER(ip),
+                           ctypes.POINTER(ctypes.c_longlong)] + [dp] * 6 +
+                          [ctypes.POINTER(ip), ctypes.POINTER(ip), ip, ctypes.POINTER(ip),
+                           ip], ip),
+        "athgpu_new_time_step": ([vp], ip),
         "athgpu_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
         "athgpu_profile_cycle": ([vp, ip, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ip)], ip),
@@ -149,40 +156,80 @@ class StageUpdate:
                  cfl=0.3, tlim=1.0e30, dfloor=None, pfloor=None, relativistic=False,
                  sigma_max=0.0, beta_min=0.0, gamma_max=1000.0, bc=None):
         L = load_library()
-        self.mesh = mesh
-        self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
+        self.kw = dict(gamma=gamma, xorder=xorder, rsolver=rsolver, precision=precision,
+                       cfl=cfl, tlim=tlim, dfloor=dfloor, pfloor=pfloor,
+                       relativistic=relativistic, sigma_max=sigma_max, beta_min=beta_min,
+                       gamma_max=gamma_max, bc=bc)
+        multilevel = hasattr(mesh, "neighbor_table")
+        self._describe(mesh)
+        h = ctypes.c_void_p()
+        _check(L.athgpu_create(ctypes.byref(h), ctypes.byref(self.desc)), "athgpu_create")
+        self.h = h
+        if multilevel:
+            ml, cc = self._ml_tables(mesh)
+            _check(L.athgpu_set_multilevel(h, *ml, *cc), "athgpu_set_multilevel")
+
+    def _describe(self, mesh):
+        """The athgpu_mesh_desc of a mesh (keeps the coordinate arrays alive)."""
+        k = self.kw
         fl = default_floor()
         multilevel = hasattr(mesh, "neighbor_table")
-        if multilevel:
-            bc = mesh.bcs
+        bc = mesh.bcs if multilevel else k["bc"]
+        self.mesh = mesh
+        self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         d = MeshDesc()
         d.nbx1, d.nbx2, d.nbx3 = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
         d.nx1, d.nx2, d.nx3 = mesh.bx
-        d.nghost, d.xorder = mesh.ng, xorder
-        d.rsolver = HLLD if rsolver == "hlld" else HLLE
-        d.precision = FP64 if precision == "fp64" else FP32
-        d.relativistic = 1 if relativistic else 0
-        d.sigma_max, d.beta_min, d.gamma_max = sigma_max, beta_min, gamma_max
-        d.gamma = gamma
-        d.dfloor = fl if dfloor is None else dfloor
-        d.pfloor = fl if pfloor is None else pfloor
-        d.cfl_number, d.tlim = cfl, tlim
+        d.nghost, d.xorder = mesh.ng, k["xorder"]
+        d.rsolver = HLLD if k["rsolver"] == "hlld" else HLLE
+        d.precision = FP64 if k["precision"] == "fp64" else FP32
+        d.relativistic = 1 if k["relativistic"] else 0
+        d.sigma_max, d.beta_min, d.gamma_max = k["sigma_max"], k["beta_min"], k["gamma_max"]
+        d.gamma = k["gamma"]
+        d.dfloor = fl if k["dfloor"] is None else k["dfloor"]
+        d.pfloor = fl if k["pfloor"] is None else k["pfloor"]
+        d.cfl_number, d.tlim = k["cfl"], k["tlim"]
         d.bc = (ctypes.c_int * 6)(*bc_codes(bc))
         d.x1f, d.dx1f, d.x2f, d.dx2f, d.x3f, d.dx3f = [_dp(c) for c in self.coords]
         self.desc = d
-        h = ctypes.c_void_p()
-        _check(L.athgpu_create(ctypes.byref(h), ctypes.byref(d)), "athgpu_create")
-        self.h = h
-        if multilevel:
-            t, cnt, lv, loc = mesh.neighbor_table()
-            ml = [np.ascontiguousarray(a) for a in (t, cnt, lv, loc)]
-            cc = [np.ascontiguousarray(c) for c in mesh.coarse_coordinate_arrays()]
-            ipp = ctypes.POINTER(ctypes.c_int)
-            _check(L.athgpu_set_multilevel(
-                h, ml[0].ctypes.data_as(ipp), ml[1].ctypes.data_as(ipp),
-                ml[2].ctypes.data_as(ipp),
-                ml[3].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
-                *[_dp(c) for c in cc]), "athgpu_set_multilevel")
+        return d
+
+    def _ml_tables(self, mesh):
+        """ctypes arguments of the multi-level tables and coarse coordinates of a mesh."""
+        t, cnt, lv, loc = mesh.neighbor_table()
+        self._ml = [np.ascontiguousarray(a) for a in (t, cnt, lv, loc)]
+        self._cc = [np.ascontiguousarray(c) for c in mesh.coarse_coordinate_arrays()]
+        ipp = ctypes.POINTER(ctypes.c_int)
+        ml = [self._ml[0].ctypes.data_as(ipp), self._ml[1].ctypes.data_as(ipp),
+              self._ml[2].ctypes.data_as(ipp),
+              self._ml[3].ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))]
+        return ml, [_dp(c) for c in self._cc]
+
+    # --- adaptive mesh refinement -----------------------------------------------------
+    def refinement_eps(self):
+        """Per-block maximum of |grad p|/p (the blast problem's refinement measure)."""
+        out = np.zeros(self.mesh.nblocks)
+        _check(load_library().athgpu_refinement_eps(self.h, _dp(out)),
+               "athgpu_refinement_eps")
+        return out
+
+    def regrid(self, plan, after_cycle=True):
+        """Move onto plan.mesh (an athena_gb300.amr.RegridPlan): redistribution and
+        Initialize(2); after_cycle takes back the last cycle's NewTimeStep first."""
+        L = load_library()
+        d = self._describe(plan.mesh)
+        ml, cc = self._ml_tables(plan.mesh)
+        ipp = ctypes.POINTER(ctypes.c_int)
+        maps = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (plan.newtoold, plan.kind, plan.ffc.reshape(-1))]
+        _check(L.athgpu_regrid(self.h, ctypes.byref(d), *ml, *cc,
+                               maps[0].ctypes.data_as(ipp), maps[1].ctypes.data_as(ipp),
+                               int(plan.ffc.shape[0]), maps[2].ctypes.data_as(ipp),
+                               1 if after_cycle else 0), "athgpu_regrid")
+
+    def new_time_step(self):
+        """Mesh::NewTimeStep again from the last W(U)'s block time steps."""
+        _check(load_library().athgpu_new_time_step(self.h), "athgpu_new_time_step")
 
     def close(self):
         if getattr(self, "h", None):

@@ -237,6 +237,8 @@ def run_gpu(args, rank, world, local_rank):
                           "steps": e_steps}
         g.close()
     res["linear_wave_l1"] = run_linear_wave()
+    if not args.no_amr:
+        res["amr_blast"] = run_amr_blast(stream)
     if not args.no_learned:
         res["learned_c2p"], net = run_learned_c2p()
         if not args.no_sr:
@@ -415,6 +417,64 @@ def run_sr_kh(n, stream, net):
     return out
 
 
+AMR_ROOT = 128        # root grid cells per direction (8^3 MeshBlocks of 16^3)
+AMR_THR = 0.3        # pressure-gradient threshold of the blast refinement condition
+AMR_WARM = {"fp32": (5, 30), "fp64": (3, 10)}   # warm-up and timed cycles
+
+
+def run_amr_blast(stream):
+    """Adaptive MHD blast (3 refinement levels, 16^3 MeshBlocks): unit cube
+    [-0.5, 0.5]^3 with a 128^3 root grid, rho 1, p 0.1 and p 10 for r < 0.1,
+    B = (1,1,1)/sqrt(2), gamma 5/3, VL2 + PLM + HLLE, CFL 0.3, refinement on the blast's
+    pressure-gradient condition (thr AMR_THR, derefine_count 10) checked every cycle.
+    Zone-cycles/s by the reference's count (the blocks of each cycle times 16^3), timed by
+    the host clock around whole cycles: the CUDA-graph stages, the refinement measure,
+    the host flags and tree update, and every regrid."""
+    import time
+    import torch
+    from athena_gb300 import pgen
+    from athena_gb300.adaptive import AdaptiveStageUpdate
+    from athena_gb300.meshtree import MultiLevelMesh
+    b = 1.0 / np.sqrt(2.0)
+
+    def ic(m):
+        return pgen.blast_blocks(m, 5.0 / 3.0, radius=0.1, pamb=0.1, prat=100.0,
+                                 bfield=(b, b, b))
+    out = {"workload": "adaptive MHD blast, 3 levels of 16^3 MeshBlocks on a %d^3 root "
+                       "grid, VL2 + PLM + HLLE, thr %g" % (AMR_ROOT, AMR_THR)}
+    for prec in ("fp32", "fp64"):
+        warm, cyc = AMR_WARM[prec]
+        mesh0 = MultiLevelMesh((AMR_ROOT,) * 3, (AMR_ROOT // 16,) * 3, 2, (-.5,) * 3,
+                               (.5,) * 3)
+        run = AdaptiveStageUpdate(mesh0, ic, 3, AMR_THR, 10, gamma=5.0 / 3.0, xorder=2,
+                                  rsolver="hlle", precision=prec, cfl=0.3)
+        run.su.set_stream(stream.cuda_stream)
+        run.initialize()
+        nb_init = run.mesh.nblocks
+        run.cycle(warm)
+        torch.cuda.synchronize()
+        r0, tr0, tg0 = run.regrids, run.t_refine, run.t_regrid
+        zc, nbs = 0, []
+        t0 = time.perf_counter()
+        for _ in range(cyc):
+            nbs.append(run.mesh.nblocks)
+            zc += run.mesh.nblocks * 16 ** 3
+            run.cycle(1)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        out[prec] = {"value": zc / t, "unit": "zone-cycles/s", "cycles": cyc,
+                     "ms_per_cycle": t / cyc * 1e3, "blocks_initial": nb_init,
+                     "blocks_min": min(nbs), "blocks_max": max(nbs),
+                     "levels": [int(v) for v in np.bincount(run.mesh.levels)[
+                         run.mesh.tree.root_level:]],
+                     "regrids": run.regrids - r0,
+                     "host_refine_s": run.t_refine - tr0,
+                     "regrid_s": run.t_regrid - tg0}
+        run.close()
+    out["speedup_fp32_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def l1_rel(a, b):
     return [float(np.abs(a[:, n] - b[:, n]).mean() / np.abs(b[:, n]).mean())
             for n in range(a.shape[1])]
@@ -451,6 +511,8 @@ def main():
                     help="skip the isolated learned-con2prim and the SR measurements")
     ap.add_argument("--no-sr", action="store_true",
                     help="skip the relativistic Kelvin-Helmholtz measurement")
+    ap.add_argument("--no-amr", action="store_true",
+                    help="skip the adaptive blast measurement")
     ap.add_argument("--nx", type=int, default=256,
                     help="cells per direction (MeshBlocks of 32^3); 256 is the workload")
     args = ap.parse_args()
@@ -551,6 +613,8 @@ def main():
         line["sr_kh"] = res["sr_kh"]
     if "linear_wave_l1" in res:
         line["linear_wave_l1"] = res["linear_wave_l1"]
+    if "amr_blast" in res:
+        line["amr_blast"] = res["amr_blast"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline((mesh, make_ic(NX, NB)[1]))
     print(json.dumps(line))

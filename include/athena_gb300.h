@@ -107,6 +107,95 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* ctx, const int* nbr_table,
                                     const double* cdx2f, const double* cx3f,
                                     const double* cdx3f);
 
+/* Adaptive mesh refinement (multi-level contexts).
+ * athgpu_refinement_eps: the blast problem's refinement measure (pgen/blast.cpp:413-443)
+ * per MeshBlock from the current primitives: maxeps[b] (HOST, nblocks entries) = the
+ * maximum over the interior and one ghost layer of |grad p| / p with centred
+ * differences, in FP64.  The host turns it into refinement flags
+ * (MeshRefinement::CheckRefinementCondition, mesh/mesh_refinement.cpp:1393-1455) and a new
+ * block tree (Mesh::UpdateMeshBlockTree, mesh/amr_loadbalance.cpp:178-317).  Synchronous. */
+athgpu_status athgpu_refinement_eps(athgpu_ctx* ctx, double* maxeps);
+/* Move the mesh onto a new block list: one rank's Mesh::RedistributeAndRefineMeshBlocks
+ * (mesh/amr_loadbalance.cpp:351-660) followed by its Initialize(2) (ghost exchange,
+ * ProlongateBoundaries, W(U), NewBlockTimeStep + Mesh::NewTimeStep).
+ *   desc        the new mesh (nbx1 = new block count, every block's coordinates; block size,
+ *               nghost, precision, solver and boundary flags unchanged; periodic meshes);
+ *   nbr_table .. cdx3f   the new mesh's tables as for athgpu_set_multilevel;
+ *   newtoold[n] the old block each new block n comes from (MeshBlockTree::GetMeshBlockList's
+ *               previous gids); kind[n] 0: kept; 1: derefined, made from the eight old
+ *               children newtoold[n] .. newtoold[n]+7 by restriction; 2: refined, prolongated
+ *               from the old parent newtoold[n];
+ *   ffc[nffc][3] (new child, receiving face 0..5, old block): the face field a new child
+ *               takes from an old block of its own level across a face of its parent's
+ *               boundary (PrepareAndSendFaceFieldCorrection, amr_loadbalance.cpp:1225-1340).
+ *   after_cycle 1: the call follows athgpu_cycle, whose Mesh::NewTimeStep is taken back
+ *               first (the reference makes it after the regrid: LoadBalancingAndAdaptive-
+ *               MeshRefinement comes between time += dt and NewTimeStep, main.cpp:535-541;
+ *               call athgpu_new_time_step next); 0: the clock is used as it is (the
+ *               regrids of the initial refinement loop, mesh.cpp:1627-1958).
+ * The maps are checked against the old and new locations.  The context handle stays valid;
+ * its CUDA graph is rebuilt on the next athgpu_cycle.  Synchronous. */
+athgpu_status athgpu_regrid(athgpu_ctx* ctx, const athgpu_mesh_desc* desc,
+                            const int* nbr_table, const int* nbr_count, const int* nblevel,
+                            const long long* loc, const double* cx1f, const double* cdx1f,
+                            const double* cx2f, const double* cdx2f, const double* cx3f,
+                            const double* cdx3f, const int* newtoold, const int* kind,
+                            int nffc, const int* ffc, int after_cycle);
+/* Mesh::NewTimeStep again from the block time steps of the last W(U) (the main loop's call
+ * after a regrid, main.cpp:541, or the one after the initial refinement loop).
+ * Synchronous. */
+athgpu_status athgpu_new_time_step(athgpu_ctx* ctx);
+/* ---- Adaptive mesh, host side (native) ----
+ * The block tree of an adaptive mesh (MeshBlockTree, mesh/meshblock_tree.cpp), its block
+ * list in gid order, every block's neighbour list, neighbour levels and fine and coarse
+ * coordinates (BoundaryBase::SearchAndSetNeighbors, bvals/bvals_base.cpp:300-720;
+ * Mesh::SetBlockSizeAndBoundaries, mesh/mesh.cpp:1984-2060; the uniform mesh generator),
+ * the derefinement counters, the refinement flags and the tree update. */
+typedef struct athgpu_amr athgpu_amr;
+/* nx[3]: root-level cells of the mesh (mesh/nx1..3); nrbx[3]: root-grid blocks per
+ * direction (MeshBlock size nx/nrbx, even, >= 4); nghost even; xmin/xmax[3] the mesh
+ * extent; bc[6] the mesh-face flags; numlevel (mesh/numlevel); derefine_count
+ * (mesh/derefine_count, the reference's default 10).  The mesh starts as the root grid. */
+athgpu_status athgpu_amr_create(athgpu_amr** amr, const int* nx, const int* nrbx, int nghost,
+                                const double* xmin, const double* xmax, const int* bc,
+                                int numlevel, int derefine_count);
+athgpu_status athgpu_amr_destroy(athgpu_amr* amr);
+/* MeshBlockTree::AddMeshBlock: make (level, lx1, lx2, lx3) a block (static refinement). */
+athgpu_status athgpu_amr_add_block(athgpu_amr* amr, int level, long long lx1, long long lx2,
+                                   long long lx3);
+athgpu_status athgpu_amr_nblocks(const athgpu_amr* amr, int* nblocks);
+/* The current mesh's tables in the layouts of athgpu_set_multilevel (loc, nbr_table,
+ * nbr_count, nblevel, coarse coordinates) and athgpu_mesh_desc (fine coordinates); any
+ * pointer may be NULL. */
+athgpu_status athgpu_amr_tables(const athgpu_amr* amr, long long* loc, int* nbr_table,
+                                int* nbr_count, int* nblevel, double* x1f, double* dx1f,
+                                double* x2f, double* dx2f, double* x3f, double* dx3f,
+                                double* cx1f, double* cdx1f, double* cx2f, double* cdx2f,
+                                double* cx3f, double* cdx3f);
+/* MeshRefinement::CheckRefinementCondition for every block from the refinement
+ * condition's results ret[b] in {1, 0, -1}: flags[b] (1 refine, -1 derefine, 0 keep);
+ * updates the derefinement counters (mesh/mesh_refinement.cpp:1393-1455). */
+athgpu_status athgpu_amr_flags(athgpu_amr* amr, const int* ret, int* flags);
+/* Mesh::UpdateMeshBlockTree (mesh/amr_loadbalance.cpp:178-317): refinement, then the
+ * derefinement of complete groups of flagged siblings.  *changed = 1 when the tree
+ * changed; the new block list and its maps are then pending until athgpu_amr_accept. */
+athgpu_status athgpu_amr_update(athgpu_amr* amr, const int* flags, int* changed);
+/* Sizes and contents of the pending maps: the new block count, the face-field
+ * corrections; newtoold[n], kind[n] and ffc[nffc][3] as athgpu_regrid takes them, and the
+ * derefinement counters the new blocks carry. */
+athgpu_status athgpu_amr_pending(const athgpu_amr* amr, int* nblocks_new, int* nffc);
+athgpu_status athgpu_amr_pending_maps(const athgpu_amr* amr, int* newtoold, int* kind,
+                                      int* ffc, int* deref_count);
+/* Make the pending block list current (its tables are rebuilt). */
+athgpu_status athgpu_amr_accept(athgpu_amr* amr);
+athgpu_status athgpu_amr_deref_counts(const athgpu_amr* amr, int* deref_count);
+/* The whole end-of-cycle refinement step on a multi-level context that holds this mesh:
+ * the blast problem's refinement measure (athgpu_refinement_eps) with threshold thr
+ * (pgen/blast.cpp:439-441), the flags, the tree update, and on a change the regrid
+ * (athgpu_regrid with after_cycle) and, with after_cycle, athgpu_new_time_step.
+ * *regridded = 1 when the mesh changed.  Synchronous. */
+athgpu_status athgpu_amr_step(athgpu_ctx* ctx, athgpu_amr* amr, double thr, int after_cycle,
+                              int* regridded);
 /* Allocate all device registers of the stage update for the mesh (replaces the
  * Hydro/Field/EquationOfState/Reconstruction constructors, hydro.cpp:31-148,
  * field.cpp:27-105). */
