@@ -112,6 +112,21 @@ def load_library(path=LIB_PATH):
                           [ctypes.POINTER(ip), ctypes.POINTER(ip), ip, ctypes.POINTER(ip),
                            ip], ip),
         "athgpu_new_time_step": ([vp], ip),
+        "athgpu_amr_create": ([ctypes.POINTER(vp), ctypes.POINTER(ip), ctypes.POINTER(ip), ip,
+                               dp, dp, ctypes.POINTER(ip), ip, ip], ip),
+        "athgpu_amr_destroy": ([vp], ip),
+        "athgpu_amr_add_block": ([vp, ip, ctypes.c_longlong, ctypes.c_longlong,
+                                  ctypes.c_longlong], ip),
+        "athgpu_amr_nblocks": ([vp, ctypes.POINTER(ip)], ip),
+        "athgpu_amr_tables": ([vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ip),
+                               ctypes.POINTER(ip), ctypes.POINTER(ip)] + [dp] * 12, ip),
+        "athgpu_amr_flags": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
+        "athgpu_amr_update": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
+        "athgpu_amr_pending": ([vp, ctypes.POINTER(ip), ctypes.POINTER(ip)], ip),
+        "athgpu_amr_pending_maps": ([vp] + [ctypes.POINTER(ip)] * 4, ip),
+        "athgpu_amr_accept": ([vp], ip),
+        "athgpu_amr_deref_counts": ([vp, ctypes.POINTER(ip)], ip),
+        "athgpu_amr_step": ([vp, vp, ctypes.c_double, ip, ctypes.POINTER(ip)], ip),
         "athgpu_launch_count": ([vp, ctypes.POINTER(ctypes.c_longlong), ip], ip),
         "athgpu_profile_cycle": ([vp, ip, ctypes.POINTER(ctypes.c_float),
                                   ctypes.POINTER(ip)], ip),

@@ -1,5 +1,5 @@
 """Adaptive mesh refinement on the GPU (athgpu_refinement_eps, athgpu_regrid,
-athgpu_new_time_step driven by athena_gb300.adaptive).
+athgpu_new_time_step, athgpu_amr_step driven by athena_gb300.adaptive).
 
 * FP64 against the reference's own adaptive blast runs (tests/golden): every cycle's
   block list and dt, the final state digest — bit for bit, through the initial refinement
@@ -16,10 +16,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _adaptive(c, mesh0, ic, precision="fp64"):
+def _adaptive(c, mesh0, ic, precision="fp64", native=True):
     from athena_gb300.adaptive import AdaptiveStageUpdate
     return AdaptiveStageUpdate(mesh0, ic, c["numlevel"], c["problem"]["thr"],
-                               c["derefine_count"], gamma=c["gamma"], xorder=c["xorder"],
+                               c["derefine_count"], native=native, gamma=c["gamma"],
+                               xorder=c["xorder"],
                                rsolver=c["rsolver"], precision=precision, cfl=c["cfl"],
                                tlim=c["tlim"], dfloor=c["floor"], pfloor=c["floor"])
 
@@ -41,11 +42,13 @@ def _names():
     return amr_case_names()
 
 
+@pytest.mark.parametrize("native", [True, False])
 @pytest.mark.parametrize("name", _names())
-def test_gpu_amr_fp64_matches_reference_bitwise(name):
+def test_gpu_amr_fp64_matches_reference_bitwise(name, native):
+    """native: the host side in the library (athgpu_amr_step); else in Python."""
     from golden_cases import load_amr_case
     c, mesh0, ic, ref = load_amr_case(name)
-    run = _adaptive(c, mesh0, ic)
+    run = _adaptive(c, mesh0, ic, native=native)
     run.initialize()
     dts, last = [], {}
 
