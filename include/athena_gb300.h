@@ -164,8 +164,9 @@ athgpu_status athgpu_amr_destroy(athgpu_amr* amr);
 athgpu_status athgpu_amr_add_block(athgpu_amr* amr, int level, long long lx1, long long lx2,
                                    long long lx3);
 athgpu_status athgpu_amr_nblocks(const athgpu_amr* amr, int* nblocks);
-/* The current mesh's tables in the layouts of athgpu_set_multilevel (loc, nbr_table,
- * nbr_count, nblevel, coarse coordinates) and athgpu_mesh_desc (fine coordinates); any
+/* The current mesh's tables in the layouts of athgpu_set_multilevel: loc, nbr_table,
+ * nbr_count, nblevel, coarse coordinates; the fine coordinates as the mesh description
+ * takes them; any
  * pointer may be NULL. */
 athgpu_status athgpu_amr_tables(const athgpu_amr* amr, long long* loc, int* nbr_table,
                                 int* nbr_count, int* nblevel, double* x1f, double* dx1f,
