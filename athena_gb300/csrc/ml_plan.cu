@@ -354,6 +354,137 @@ bool check_op(const MlOp& op, const Ix& x, const Bounds& B) {
   }
 }
 
+// ---- barriers between operations ------------------------------------------------------
+// The arrays an operation reads and writes, as boxes of one block's array, so that runs of
+// operations on disjoint data execute without a barrier between them.
+enum RegArr {
+  RA_U, RA_W, RA_BCC, RA_B1, RA_B2, RA_B3, RA_CU, RA_CW, RA_CBCC, RA_CB1, RA_CB2, RA_CB3,
+  RA_SU, RA_SB1, RA_SB2, RA_SB3
+};
+struct Reg {
+  int arr, blk, s[3], e[3];
+};
+bool overlap(const Reg& a, const Reg& b) {
+  if (a.arr != b.arr || a.blk != b.blk) return false;
+  for (int q = 0; q < 3; ++q)
+    if (a.e[q] < b.s[q] || b.e[q] < a.s[q]) return false;
+  return true;
+}
+Reg reg(int arr, int blk, const int s[3], const int e[3], int pad = 0) {
+  Reg r;
+  r.arr = arr;
+  r.blk = blk;
+  for (int q = 0; q < 3; ++q) { r.s[q] = s[q] - pad; r.e[q] = e[q] + pad; }
+  return r;
+}
+// the fine box under a coarse box (extra: faces beyond the last cell)
+void fine_of(const MlOp& op, const Ix& x, int extra, int fs[3], int fe[3]) {
+  for (int a = 0; a < 3; ++a) {
+    fs[a] = (op.s[a] - x.clo[a]) * 2 + x.lo[a];
+    fe[a] = (op.e[a] - x.clo[a]) * 2 + x.lo[a] + 1 + extra;
+  }
+}
+// conservative read and write sets of one operation of block b
+void op_regions(const MlOp& op, int b, const Ix& x, std::vector<Reg>* rd, std::vector<Reg>* wr) {
+  rd->clear();
+  wr->clear();
+  int fs[3], fe[3], os[3], oe[3];
+  const int all_s[3] = {-1000, -1000, -1000}, all_e[3] = {1000, 1000, 1000};
+  for (int a = 0; a < 3; ++a) {
+    os[a] = op.o[a];
+    oe[a] = op.o[a] + op.e[a] - op.s[a];
+  }
+  switch (op.code) {
+    case ML_COPY_U:
+      wr->push_back(reg(op.dst_kind == ML_COARSE ? RA_CU : RA_U, b, op.s, op.e));
+      rd->push_back(reg(op.src_kind == ML_SEND ? RA_SU : RA_U, op.src, os, oe));
+      break;
+    case ML_COPY_B:
+      wr->push_back(reg((op.dst_kind == ML_COARSE ? RA_CB1 : RA_B1) + op.d, b, op.s, op.e));
+      rd->push_back(reg((op.src_kind == ML_SEND ? RA_SB1 : RA_B1) + op.d, op.src, os, oe));
+      break;
+    case ML_RESTRICT_U:
+      wr->push_back(reg(RA_CU, b, op.s, op.e));
+      if (op.src_kind == ML_SEND) wr->push_back(reg(RA_SU, b, op.s, op.e));
+      fine_of(op, x, 0, fs, fe);
+      rd->push_back(reg(RA_U, b, fs, fe));
+      break;
+    case ML_RESTRICT_B:
+      wr->push_back(reg(RA_CB1 + op.d, b, op.s, op.e));
+      if (op.src_kind == ML_SEND) wr->push_back(reg(RA_SB1 + op.d, b, op.s, op.e));
+      fine_of(op, x, 0, fs, fe);
+      rd->push_back(reg(RA_B1 + op.d, b, fs, fe));
+      break;
+    case ML_C2P_COARSE:
+      wr->push_back(reg(RA_CU, b, op.s, op.e));
+      wr->push_back(reg(RA_CW, b, op.s, op.e));
+      wr->push_back(reg(RA_CBCC, b, op.s, op.e));
+      rd->push_back(reg(RA_CU, b, op.s, op.e));
+      for (int d = 0; d < 3; ++d) rd->push_back(reg(RA_CB1 + d, b, op.s, op.e, 1));
+      break;
+    case ML_PROLONG_U:
+      rd->push_back(reg(op.src_kind == ML_COARSE ? RA_CU : RA_CW, b, op.s, op.e, 1));
+      fine_of(op, x, 0, fs, fe);
+      wr->push_back(reg(op.src_kind == ML_COARSE ? RA_U : RA_W, b, fs, fe));
+      break;
+    case ML_PROLONG_SHARED:
+      rd->push_back(reg(RA_CB1 + op.d, b, op.s, op.e, 1));
+      fine_of(op, x, 0, fs, fe);
+      wr->push_back(reg(RA_B1 + op.d, b, fs, fe));
+      break;
+    case ML_PROLONG_INTERNAL:
+      fine_of(op, x, 1, fs, fe);
+      for (int d = 0; d < 3; ++d) {
+        rd->push_back(reg(RA_B1 + d, b, fs, fe));
+        wr->push_back(reg(RA_B1 + d, b, fs, fe));
+      }
+      break;
+    case ML_FINE_P2C:
+      for (int d = 0; d < 3; ++d) rd->push_back(reg(RA_B1 + d, b, op.s, op.e, 1));
+      rd->push_back(reg(RA_W, b, op.s, op.e));
+      rd->push_back(reg(RA_BCC, b, op.s, op.e));
+      wr->push_back(reg(RA_BCC, b, op.s, op.e));
+      wr->push_back(reg(RA_U, b, op.s, op.e));
+      break;
+    default:  // ML_BC_COARSE and anything else: the whole coarse level of the block
+      for (int arr = RA_CU; arr <= RA_CB3; ++arr) {
+        rd->push_back(reg(arr, b, all_s, all_e));
+        wr->push_back(reg(arr, b, all_s, all_e));
+      }
+      break;
+  }
+}
+
+// mark the operations after which no barrier is needed: an operation joins the current
+// run unless it writes what the run reads or writes, or reads what the run writes
+void mark_runs(MlOpList* L, const Ix& x) {
+  std::vector<Reg> rd, wr, run_rd, run_wr;
+  for (size_t q = 0; q + 1 < L->off.size(); ++q) {
+    const int b = L->blk[q];
+    run_rd.clear();
+    run_wr.clear();
+    for (int i = L->off[q]; i < L->off[q + 1]; ++i) {
+      MlOp& op = L->ops[i];
+      op_regions(op, b, x, &rd, &wr);
+      bool conflict = false;
+      for (const Reg& w : wr) {
+        for (const Reg& r : run_wr) conflict = conflict || overlap(w, r);
+        for (const Reg& r : run_rd) conflict = conflict || overlap(w, r);
+      }
+      for (const Reg& r : rd)
+        for (const Reg& w : run_wr) conflict = conflict || overlap(r, w);
+      if (conflict && i > L->off[q]) {
+        L->ops[i - 1].nosync = 0;
+        run_rd.clear();
+        run_wr.clear();
+      }
+      run_rd.insert(run_rd.end(), rd.begin(), rd.end());
+      run_wr.insert(run_wr.end(), wr.begin(), wr.end());
+      op.nosync = 1;
+    }
+  }
+}
+
 }  // namespace
 
 bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* nbr_count,
@@ -605,6 +736,9 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
           *err = buf;
           return false;
         }
+    mark_runs(&P->r, x);
+    mark_runs(&P->x, x);
+    mark_runs(&P->p, x);
     for (const MlFluxTask& t : P->flux_tasks)
       if (t.coarse < 0 || t.coarse >= nb || t.fine < 0 || t.fine >= nb) {
         *err = "multi-level plan: flux task block out of range";

@@ -29,6 +29,8 @@ struct MlOp {
   int aux;        // boundary face and kind (ML_BC_COARSE)
   int s[3], e[3]; // destination box (inclusive), index 0 = i
   int o[3];       // source box origin (copies)
+  int nosync;     // 1: the next operation touches nothing this one writes or reads
+                  // (no barrier between them); 0 (the default): barrier
 };
 
 // a neighbour-list entry as the host passes it (BoundaryBase::neighbor, bvals_base.cpp)

@@ -67,25 +67,29 @@ __device__ __forceinline__ void box_pos(const MlOp& op, int t, int& k, int& j, i
 __device__ __forceinline__ double ldr(const double* p) { return *p; }
 __device__ __forceinline__ double ldr(const float* p) { return (double)*p; }
 
-__device__ __forceinline__ double mm_grad(double cm, double c0, double cp, double dxm,
-                                          double dxp) {
-  const double gm = (c0 - cm) / dxm, gp = (cp - c0) / dxp;
-  const double sg = ((gm < 0.0) ? -1.0 : 1.0) + ((gp < 0.0) ? -1.0 : 1.0);
-  const double am = fabs(gm), ap = fabs(gp);
-  return 0.5 * sg * ((ap < am) ? ap : am);
+template <typename T>
+__device__ __forceinline__ T mm_grad(T cm, T c0, T cp, T dxm, T dxp) {
+  const T gm = (c0 - cm) / dxm, gp = (cp - c0) / dxp;
+  const T sg = ((gm < T(0)) ? T(-1) : T(1)) + ((gp < T(0)) ? T(-1) : T(1));
+  const T am = fabs(gm), ap = fabs(gp);
+  return T(0.5) * sg * ((ap < am) ? ap : am);
 }
 
 // ---- the per-block operation executor ------------------------------------------------
-template <typename Real>
-__device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const MlOp& op) {
+// CODE: the operation code as a template parameter, so that each instance keeps only its
+// own branch of the element loop
+template <typename Real, int CODE>
+__device__ __forceinline__ void ml_op_code(const DevMesh& m, const MlArrays<Real>& A, int b,
+                                           const MlOp& op) {
   const DevML& L = m.ml;
   const int nel = box_count(op);
   const double* dx[3] = {m.dx1f + (i64)b * m.nc1, m.dx2f + (i64)b * m.nc2,
                          m.dx3f + (i64)b * m.nc3};
   const int clo[3] = {L.cis, L.cjs, L.cks}, flo[3] = {m.is, m.js, m.ks};
-  double* fb[3] = {A.b1, A.b2, A.b3};
-  double* cbs[3] = {L.cb1, L.cb2, L.cb3};
-  double* sbs[3] = {L.sb1, L.sb2, L.sb3};
+  // face arrays by component (selected, not indexed: no local-memory pointer tables)
+  auto FB = [&](int d) -> double* { return d == 0 ? A.b1 : d == 1 ? A.b2 : A.b3; };
+  auto CBS = [&](int d) -> double* { return d == 0 ? L.cb1 : d == 1 ? L.cb2 : L.cb3; };
+  auto SBS = [&](int d) -> double* { return d == 0 ? L.sb1 : d == 1 ? L.sb2 : L.sb3; };
   Real* cu = (Real*)L.ccons;
   Real* su = (Real*)L.scons;
   Real* cw = (Real*)L.cprim;
@@ -93,58 +97,65 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
   for (int t = threadIdx.x; t < nel; t += blockDim.x) {
     int k, j, i;
     box_pos(op, t, k, j, i);
-    switch (op.code) {
+    switch (CODE) {
       case ML_COPY_U: {
         const int sk = op.o[2] + (k - op.s[2]), sj = op.o[1] + (j - op.s[1]),
                   si = op.o[0] + (i - op.s[0]);
-        for (int n = 0; n < NHYDRO; ++n) {
-          Real v = op.src_kind == ML_SEND ? su[ccidx(m, op.src, n, NHYDRO, sk, sj, si)]
-                                          : A.u[cidx(m, op.src, n, NHYDRO, sk, sj, si)];
-          if (op.dst_kind == ML_COARSE) cu[ccidx(m, b, n, NHYDRO, k, j, i)] = v;
-          else A.u[cidx(m, b, n, NHYDRO, k, j, i)] = v;
-        }
+        const bool ssend = op.src_kind == ML_SEND, dcoarse = op.dst_kind == ML_COARSE;
+        const Real* sp = ssend ? su + ccidx(m, op.src, 0, NHYDRO, sk, sj, si)
+                               : A.u + cidx(m, op.src, 0, NHYDRO, sk, sj, si);
+        Real* dp = dcoarse ? cu + ccidx(m, b, 0, NHYDRO, k, j, i)
+                           : A.u + cidx(m, b, 0, NHYDRO, k, j, i);
+        const i64 svs = ssend ? L.nccell : m.ncell, dvs = dcoarse ? L.nccell : m.ncell;
+#pragma unroll
+        for (int n = 0; n < NHYDRO; ++n) dp[n * dvs] = sp[n * svs];
         break;
       }
       case ML_COPY_B: {
         const int sk = op.o[2] + (k - op.s[2]), sj = op.o[1] + (j - op.s[1]),
                   si = op.o[0] + (i - op.s[0]);
         const double v = op.src_kind == ML_SEND
-                             ? sbs[op.d][fcidx(m, true, op.d, op.src, sk, sj, si)]
-                             : fb[op.d][fcidx(m, false, op.d, op.src, sk, sj, si)];
-        if (op.dst_kind == ML_COARSE) cbs[op.d][fcidx(m, true, op.d, b, k, j, i)] = v;
-        else fb[op.d][fcidx(m, false, op.d, b, k, j, i)] = v;
+                             ? SBS(op.d)[fcidx(m, true, op.d, op.src, sk, sj, si)]
+                             : FB(op.d)[fcidx(m, false, op.d, op.src, sk, sj, si)];
+        if (op.dst_kind == ML_COARSE) CBS(op.d)[fcidx(m, true, op.d, b, k, j, i)] = v;
+        else FB(op.d)[fcidx(m, false, op.d, b, k, j, i)] = v;
         break;
       }
       case ML_RESTRICT_U: {  // mesh_refinement.cpp:116-189, CellVolume = dx1 dx2 dx3
+        // cell-centred operations compute in the bulk precision (FP64: the reference's
+        // arithmetic; FP32 path: FP32)
+        using Acc = Real;
         const int fk = (k - L.cks) * 2 + m.ks, fj = (j - L.cjs) * 2 + m.js,
                   fi = (i - L.cis) * 2 + m.is;
-        const double d1a = dx[0][fi], d1b = dx[0][fi + 1], d2a = dx[1][fj],
-                     d2b = dx[1][fj + 1], d3a = dx[2][fk], d3b = dx[2][fk + 1];
-        const double v000 = d1a * d2a * d3a, v001 = d1b * d2a * d3a;
-        const double v010 = d1a * d2b * d3a, v011 = d1b * d2b * d3a;
-        const double v100 = d1a * d2a * d3b, v101 = d1b * d2a * d3b;
-        const double v110 = d1a * d2b * d3b, v111 = d1b * d2b * d3b;
-        const double tvol = ((v000 + v010) + (v001 + v011)) + ((v100 + v110) + (v101 + v111));
+        const Acc d1a = (Acc)dx[0][fi], d1b = (Acc)dx[0][fi + 1], d2a = (Acc)dx[1][fj],
+                  d2b = (Acc)dx[1][fj + 1], d3a = (Acc)dx[2][fk], d3b = (Acc)dx[2][fk + 1];
+        const Acc v000 = d1a * d2a * d3a, v001 = d1b * d2a * d3a;
+        const Acc v010 = d1a * d2b * d3a, v011 = d1b * d2b * d3a;
+        const Acc v100 = d1a * d2a * d3b, v101 = d1b * d2a * d3b;
+        const Acc v110 = d1a * d2b * d3b, v111 = d1b * d2b * d3b;
+        const Acc tvol = ((v000 + v010) + (v001 + v011)) + ((v100 + v110) + (v101 + v111));
         // ML_SEND: the values sent to coarser blocks, also kept in the coarse buffer as the
         // prolongation stencil's inner side (LoadBoundaryBufferToCoarser restricts into it)
         const bool both = op.src_kind == ML_SEND;
+        const i64 pj = m.nc1, pk = (i64)m.nc1 * m.nc2;
+        const Real* ub = A.u + cidx(m, b, 0, NHYDRO, fk, fj, fi);
+        const i64 cb0 = ccidx(m, b, 0, NHYDRO, k, j, i);
         for (int n = 0; n < NHYDRO; ++n) {
-          auto f = [&](int kk, int jj, int ii) {
-            return ldr(A.u + cidx(m, b, n, NHYDRO, fk + kk, fj + jj, fi + ii));
-          };
-          const double v = (((f(0, 0, 0) * v000 + f(0, 1, 0) * v010) +
-                             (f(0, 0, 1) * v001 + f(0, 1, 1) * v011)) +
-                            ((f(1, 0, 0) * v100 + f(1, 1, 0) * v110) +
-                             (f(1, 0, 1) * v101 + f(1, 1, 1) * v111))) / tvol;
-          cu[ccidx(m, b, n, NHYDRO, k, j, i)] = (Real)v;
-          if (both) su[ccidx(m, b, n, NHYDRO, k, j, i)] = (Real)v;
+          const Real* un = ub + n * m.ncell;
+          auto f = [&](int kk, int jj, int ii) { return un[kk * pk + jj * pj + ii]; };
+          const Acc v = (((f(0, 0, 0) * v000 + f(0, 1, 0) * v010) +
+                          (f(0, 0, 1) * v001 + f(0, 1, 1) * v011)) +
+                         ((f(1, 0, 0) * v100 + f(1, 1, 0) * v110) +
+                          (f(1, 0, 1) * v101 + f(1, 1, 1) * v111))) / tvol;
+          cu[cb0 + n * L.nccell] = (Real)v;
+          if (both) su[cb0 + n * L.nccell] = (Real)v;
         }
         break;
       }
       case ML_RESTRICT_B: {  // mesh_refinement.cpp:272-463
         const int fk = (k - L.cks) * 2 + m.ks, fj = (j - L.cjs) * 2 + m.js,
                   fi = (i - L.cis) * 2 + m.is;
-        const double* F = fb[op.d];
+        const double* F = FB(op.d);
         auto f = [&](int kk, int jj, int ii) {
           return F[fcidx(m, false, op.d, b, fk + kk, fj + jj, fi + ii)];
         };
@@ -165,38 +176,38 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
           const double tarea = s0i + s0p + s1i + s1p;
           v = (f(0, 0, 0) * s0i + f(0, 0, 1) * s0p + f(0, 1, 0) * s1i + f(0, 1, 1) * s1p) / tarea;
         }
-        cbs[op.d][fcidx(m, true, op.d, b, k, j, i)] = v;
-        if (op.src_kind == ML_SEND) sbs[op.d][fcidx(m, true, op.d, b, k, j, i)] = v;
+        CBS(op.d)[fcidx(m, true, op.d, b, k, j, i)] = v;
+        if (op.src_kind == ML_SEND) SBS(op.d)[fcidx(m, true, op.d, b, k, j, i)] = v;
         break;
       }
       case ML_C2P_COARSE: {  // adiabatic_mhd.cpp:41-90 with field.cpp:112-180
+        using Acc = Real;
         const i64 vs = L.nccell;
         const i64 c = ccidx(m, b, 0, NHYDRO, k, j, i);
         const i64 cb = ccidx(m, b, 0, 3, k, j, i);
         const double lw = 0.5, rw = 0.5;
-        const double bc1 = lw * L.cb1[fcidx(m, true, 0, b, k, j, i)] +
-                           rw * L.cb1[fcidx(m, true, 0, b, k, j, i + 1)];
-        const double bc2 = lw * L.cb2[fcidx(m, true, 1, b, k, j, i)] +
-                           rw * L.cb2[fcidx(m, true, 1, b, k, j + 1, i)];
-        const double bc3 = lw * L.cb3[fcidx(m, true, 2, b, k, j, i)] +
-                           rw * L.cb3[fcidx(m, true, 2, b, k + 1, j, i)];
+        const Acc bc1 = (Acc)(lw * L.cb1[fcidx(m, true, 0, b, k, j, i)] +
+                              rw * L.cb1[fcidx(m, true, 0, b, k, j, i + 1)]);
+        const Acc bc2 = (Acc)(lw * L.cb2[fcidx(m, true, 1, b, k, j, i)] +
+                              rw * L.cb2[fcidx(m, true, 1, b, k, j + 1, i)]);
+        const Acc bc3 = (Acc)(lw * L.cb3[fcidx(m, true, 2, b, k, j, i)] +
+                              rw * L.cb3[fcidx(m, true, 2, b, k + 1, j, i)]);
         cbcc[cb] = (Real)bc1;
         cbcc[cb + vs] = (Real)bc2;
         cbcc[cb + 2 * vs] = (Real)bc3;
-        const double gm1 = m.gamma - 1.0, dfl = m.dfloor, pfl = m.pfloor;
-        double u_d = ldr(cu + c), u_e = ldr(cu + c + 4 * vs);
-        const double u_m1 = ldr(cu + c + vs), u_m2 = ldr(cu + c + 2 * vs),
-                     u_m3 = ldr(cu + c + 3 * vs);
+        const Acc gm1 = (Acc)(m.gamma - 1.0), dfl = (Acc)m.dfloor, pfl = (Acc)m.pfloor;
+        Acc u_d = cu[c], u_e = cu[c + 4 * vs];
+        const Acc u_m1 = cu[c + vs], u_m2 = cu[c + 2 * vs], u_m3 = cu[c + 3 * vs];
         u_d = (u_d > dfl) ? u_d : dfl;
         cu[c] = (Real)u_d;
-        const double di = 1.0 / u_d;
+        const Acc di = Acc(1) / u_d;
         cw[c] = (Real)u_d;
         cw[c + vs] = (Real)(u_m1 * di);
         cw[c + 2 * vs] = (Real)(u_m2 * di);
         cw[c + 3 * vs] = (Real)(u_m3 * di);
-        const double pb = 0.5 * (bc1 * bc1 + bc2 * bc2 + bc3 * bc3);
-        const double e_k = 0.5 * di * (u_m1 * u_m1 + u_m2 * u_m2 + u_m3 * u_m3);
-        const double w_p = gm1 * (u_e - e_k - pb);
+        const Acc pb = Acc(0.5) * (bc1 * bc1 + bc2 * bc2 + bc3 * bc3);
+        const Acc e_k = Acc(0.5) * di * (u_m1 * u_m1 + u_m2 * u_m2 + u_m3 * u_m3);
+        const Acc w_p = gm1 * (u_e - e_k - pb);
         cu[c + 4 * vs] = (Real)((w_p > pfl) ? u_e : ((pfl / gm1) + e_k + pb));
         cw[c + 4 * vs] = (Real)((w_p > pfl) ? w_p : pfl);
         break;
@@ -247,14 +258,15 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
             c3[a] = dst;
             s3[a] = srcc;
           }
-          const double v = cbs[d][fcidx(m, true, d, b, s3[2], s3[1], s3[0])];
-          cbs[d][fcidx(m, true, d, b, c3[2], c3[1], c3[0])] = sgn < 0.0 ? -v : v;
+          const double v = CBS(d)[fcidx(m, true, d, b, s3[2], s3[1], s3[0])];
+          CBS(d)[fcidx(m, true, d, b, c3[2], c3[1], c3[0])] = sgn < 0.0 ? -v : v;
         }
         break;
       }
       case ML_PROLONG_U: {  // mesh_refinement.cpp:464-540
         // coarse W into W (ProlongateBoundaries), or with src_kind ML_COARSE the coarse
         // U into U (ProlongateMeshBlock after a refinement, amr_loadbalance.cpp:1172-1180)
+        using Acc = Real;
         const Real* csrc = op.src_kind == ML_COARSE ? cu : cw;
         Real* fdst = op.src_kind == ML_COARSE ? A.u : A.w;
         const int fk = (k - L.cks) * 2 + m.ks, fj = (j - L.cjs) * 2 + m.js,
@@ -265,22 +277,27 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
         const double* fx1 = L.fx1v + (i64)b * m.nc1;
         const double* fx2 = L.fx2v + (i64)b * m.nc2;
         const double* fx3 = L.fx3v + (i64)b * m.nc3;
-        const double x3c = cx3[k], dx3m = x3c - cx3[k - 1], dx3p = cx3[k + 1] - x3c;
-        const double dx3fm = x3c - fx3[fk], dx3fp = fx3[fk + 1] - x3c;
-        const double x2c = cx2[j], dx2m = x2c - cx2[j - 1], dx2p = cx2[j + 1] - x2c;
-        const double dx2fm = x2c - fx2[fj], dx2fp = fx2[fj + 1] - x2c;
-        const double x1c = cx1[i], dx1m = x1c - cx1[i - 1], dx1p = cx1[i + 1] - x1c;
-        const double dx1fm = x1c - fx1[fi], dx1fp = fx1[fi + 1] - x1c;
+        // coordinate differences in FP64 (exact in the FP64 path), then the bulk precision
+        const Acc dx3m = (Acc)(cx3[k] - cx3[k - 1]), dx3p = (Acc)(cx3[k + 1] - cx3[k]);
+        const Acc dx3fm = (Acc)(cx3[k] - fx3[fk]), dx3fp = (Acc)(fx3[fk + 1] - cx3[k]);
+        const Acc dx2m = (Acc)(cx2[j] - cx2[j - 1]), dx2p = (Acc)(cx2[j + 1] - cx2[j]);
+        const Acc dx2fm = (Acc)(cx2[j] - fx2[fj]), dx2fp = (Acc)(fx2[fj + 1] - cx2[j]);
+        const Acc dx1m = (Acc)(cx1[i] - cx1[i - 1]), dx1p = (Acc)(cx1[i + 1] - cx1[i]);
+        const Acc dx1fm = (Acc)(cx1[i] - fx1[fi]), dx1fp = (Acc)(fx1[fi + 1] - cx1[i]);
+        const i64 cj = L.ncc1, ck = (i64)L.ncc1 * L.ncc2;
+        const i64 fj1 = m.nc1, fk1 = (i64)m.nc1 * m.nc2;
+        const Real* cbase = csrc + ccidx(m, b, 0, NHYDRO, k, j, i);
+        Real* fbase = fdst + cidx(m, b, 0, NHYDRO, fk, fj, fi);
         for (int n = 0; n < NHYDRO; ++n) {
-          auto cv = [&](int kk, int jj, int ii) {
-            return ldr(csrc + ccidx(m, b, n, NHYDRO, kk, jj, ii));
-          };
-          const double cc = cv(k, j, i);
-          const double g1 = mm_grad(cv(k, j, i - 1), cc, cv(k, j, i + 1), dx1m, dx1p);
-          const double g2 = mm_grad(cv(k, j - 1, i), cc, cv(k, j + 1, i), dx2m, dx2p);
-          const double g3 = mm_grad(cv(k - 1, j, i), cc, cv(k + 1, j, i), dx3m, dx3p);
-          auto put = [&](int kk, int jj, int ii, double v) {
-            fdst[cidx(m, b, n, NHYDRO, fk + kk, fj + jj, fi + ii)] = (Real)v;
+          const Real* cn = cbase + n * L.nccell;
+          Real* fn = fbase + n * m.ncell;
+          auto cv = [&](int kk, int jj, int ii) -> Acc { return cn[kk * ck + jj * cj + ii]; };
+          const Acc cc = cv(0, 0, 0);
+          const Acc g1 = mm_grad<Acc>(cv(0, 0, -1), cc, cv(0, 0, 1), dx1m, dx1p);
+          const Acc g2 = mm_grad<Acc>(cv(0, -1, 0), cc, cv(0, 1, 0), dx2m, dx2p);
+          const Acc g3 = mm_grad<Acc>(cv(-1, 0, 0), cc, cv(1, 0, 0), dx3m, dx3p);
+          auto put = [&](int kk, int jj, int ii, Acc v) {
+            fn[kk * fk1 + jj * fj1 + ii] = (Real)v;
           };
           put(0, 0, 0, cc - (g1 * dx1fm + g2 * dx2fm + g3 * dx3fm));
           put(0, 0, 1, cc + (g1 * dx1fp - g2 * dx2fm - g3 * dx3fm));
@@ -303,7 +320,7 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
         const int cidx3[3] = {i, j, k};
         int f3[3];
         for (int a = 0; a < 3; ++a) f3[a] = (cidx3[a] - clo[a]) * 2 + flo[a];
-        const double* C = cbs[d];
+        const double* C = CBS(d);
         auto cv = [&](int kk, int jj, int ii) { return C[fcidx(m, true, d, b, kk, jj, ii)]; };
         const double cc = cv(k, j, i);
         double g[3] = {0, 0, 0}, am[3] = {0, 0, 0}, ap[3] = {0, 0, 0};
@@ -318,7 +335,7 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
           am[a] = xc - fxs[a][f3[a]];
           ap[a] = fxs[a][f3[a] + 1] - xc;
         }
-        double* F = fb[d];
+        double* F = FB(d);
         for (int ob = 0; ob < 2; ++ob)
           for (int oa = 0; oa < 2; ++oa) {
             int ff[3] = {f3[0], f3[1], f3[2]};
@@ -415,18 +432,19 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
         A.bcc[cb] = (Real)bc1;
         A.bcc[cb + vs] = (Real)bc2;
         A.bcc[cb + 2 * vs] = (Real)bc3;
-        const double igm1 = 1.0 / (m.gamma - 1.0);
-        const double w_d = ldr(A.w + c), w_vx = ldr(A.w + c + vs), w_vy = ldr(A.w + c + 2 * vs),
-                     w_vz = ldr(A.w + c + 3 * vs), w_p = ldr(A.w + c + 4 * vs);
+        using Acc = Real;   // U(W) in the bulk precision
+        const Acc igm1 = Acc(1) / (Acc)(m.gamma - 1.0);
+        const Acc w_d = A.w[c], w_vx = A.w[c + vs], w_vy = A.w[c + 2 * vs],
+                  w_vz = A.w[c + 3 * vs], w_p = A.w[c + 4 * vs];
         // the FP32 path's cell-centred field is the FP32 rounding of the FP64 average
-        const double b1c = ldr(A.bcc + cb), b2c = ldr(A.bcc + cb + vs),
-                     b3c = ldr(A.bcc + cb + 2 * vs);
+        const Acc b1c = A.bcc[cb], b2c = A.bcc[cb + vs], b3c = A.bcc[cb + 2 * vs];
         A.u[c] = (Real)w_d;
         A.u[c + vs] = (Real)(w_vx * w_d);
         A.u[c + 2 * vs] = (Real)(w_vy * w_d);
         A.u[c + 3 * vs] = (Real)(w_vz * w_d);
-        A.u[c + 4 * vs] = (Real)(w_p * igm1 + 0.5 * (w_d * (w_vx * w_vx + w_vy * w_vy + w_vz * w_vz) +
-                                                    (b1c * b1c + b2c * b2c + b3c * b3c)));
+        A.u[c + 4 * vs] = (Real)(w_p * igm1 + Acc(0.5) * (w_d * (w_vx * w_vx + w_vy * w_vy +
+                                                                 w_vz * w_vz) +
+                                                          (b1c * b1c + b2c * b2c + b3c * b3c)));
         break;
       }
       default:
@@ -436,14 +454,33 @@ __device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const Ml
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(128)
+__device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const MlOp& op) {
+  switch (op.code) {
+    case ML_COPY_U: ml_op_code<Real, ML_COPY_U>(m, A, b, op); break;
+    case ML_COPY_B: ml_op_code<Real, ML_COPY_B>(m, A, b, op); break;
+    case ML_RESTRICT_U: ml_op_code<Real, ML_RESTRICT_U>(m, A, b, op); break;
+    case ML_RESTRICT_B: ml_op_code<Real, ML_RESTRICT_B>(m, A, b, op); break;
+    case ML_C2P_COARSE: ml_op_code<Real, ML_C2P_COARSE>(m, A, b, op); break;
+    case ML_BC_COARSE: ml_op_code<Real, ML_BC_COARSE>(m, A, b, op); break;
+    case ML_PROLONG_U: ml_op_code<Real, ML_PROLONG_U>(m, A, b, op); break;
+    case ML_PROLONG_SHARED: ml_op_code<Real, ML_PROLONG_SHARED>(m, A, b, op); break;
+    case ML_PROLONG_INTERNAL: ml_op_code<Real, ML_PROLONG_INTERNAL>(m, A, b, op); break;
+    case ML_FINE_P2C: ml_op_code<Real, ML_FINE_P2C>(m, A, b, op); break;
+    default: break;
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(128, 4)
 ml_ops_kernel(DevMesh m, MlArrays<Real> A, const MlOp* __restrict__ ops,
               const int* __restrict__ off, const int* __restrict__ blk) {
   const int b = blk[blockIdx.x];
   for (int q = off[blockIdx.x]; q < off[blockIdx.x + 1]; ++q) {
     const MlOp op = ops[q];
     ml_op<Real>(m, A, b, op);
-    __syncthreads();
+    // runs of operations on disjoint data proceed without a barrier (the planner marks
+    // them); the flag is the same for every thread of the CTA
+    if (!op.nosync) __syncthreads();
   }
 }
 
@@ -552,41 +589,14 @@ ml_fine_flux_kernel(DevMesh m, const int4* __restrict__ tasks, int ntasks,
 }
 
 // ---- EMF correction across levels ---------------------------------------------------
-// One thread per (block, edge component c, edge position); positions off the block
-// boundary return.  Same-level contributions in neighbour-list order, clearing of the
-// positions shared with finer blocks, the finer blocks' restricted values in list order,
-// then the averaging (flux_correction_fc.cpp:689-1545).
 template <typename Real>
-__global__ void __launch_bounds__(128)
-ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e2,
-              const Real* __restrict__ e3) {
+__device__ __forceinline__ void ml_emf_position(const DevMesh& m, const Real* __restrict__ e1,
+                                                const Real* __restrict__ e2,
+                                                const Real* __restrict__ e3, int b, int c,
+                                                int k, int j, int i, const int* nt, int nn,
+                                                const int* s_lev, const int* s_ef,
+                                                const int* s_nf) {
   const int nx1 = m.nx1, nx2 = m.nx2, nx3 = m.nx3;
-  // positions per block: e1 (nx3+1)(nx2+1)nx1, e2 (nx3+1)nx2(nx1+1), e3 nx3(nx2+1)(nx1+1)
-  const i64 n1c = (i64)(nx3 + 1) * (nx2 + 1) * nx1, n2c = (i64)(nx3 + 1) * nx2 * (nx1 + 1),
-            n3c = (i64)nx3 * (nx2 + 1) * (nx1 + 1);
-  const i64 per = n1c + n2c + n3c;
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= per * m.nb) return;
-  const int b = (int)(t / per);
-  i64 r = t - (i64)b * per;
-  int c, k, j, i;
-  if (r < n1c) {
-    c = 0;
-    i = m.is + (int)(r % nx1); r /= nx1;
-    j = m.js + (int)(r % (nx2 + 1));
-    k = m.ks + (int)(r / (nx2 + 1));
-  } else if ((r -= n1c) < n2c) {
-    c = 1;
-    i = m.is + (int)(r % (nx1 + 1)); r /= (nx1 + 1);
-    j = m.js + (int)(r % nx2);
-    k = m.ks + (int)(r / nx2);
-  } else {
-    r -= n2c;
-    c = 2;
-    i = m.is + (int)(r % (nx1 + 1)); r /= (nx1 + 1);
-    j = m.js + (int)(r % (nx2 + 1));
-    k = m.ks + (int)(r / (nx2 + 1));
-  }
   const int p3[3] = {i, j, k};
   const int lo[3] = {m.is, m.js, m.ks}, hi[3] = {m.ie + 1, m.je + 1, m.ke + 1};
   // faces this position lies on: along the two axes other than c
@@ -612,8 +622,6 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
     eid = base + (((onf[ta] + 1) >> 1) | ((onf[tb] + 1) & 2));
   }
   Real val = E[eidx(b, k, j, i)];
-  const int* nt = L.nbrt + (i64)b * 56 * 10;
-  const int nn = __ldg(L.nnbr + b);
   // same level
   for (int q = 0; q < nn; ++q) {
     const int* e = nt + q * 10;
@@ -628,7 +636,7 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
       s3[a] = o[a] > 0 ? lo[a] : hi[a];          // the neighbour's face facing me
       val += E[eidx(e[0], s3[2], s3[1], s3[0])];
     } else {
-      if (!on_edge || e[9] != eid || !L.eflag[b * 12 + eid]) continue;
+      if (!on_edge || e[9] != eid || !s_ef[eid]) continue;
       int s3[3] = {i, j, k};
       s3[ta] = o[ta] > 0 ? lo[ta] : hi[ta];
       s3[tb] = o[tb] > 0 ? lo[tb] : hi[tb];
@@ -641,7 +649,7 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
     if (a == c || onf[a] == 0) continue;
     int o[3] = {0, 0, 0};
     o[a] = onf[a];
-    if (__ldg(L.nblev + (i64)b * 27 + (o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1)) <= lev)
+    if ((s_lev[(o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1)]) <= lev)
       continue;
     // the face-interior range of component c on face a (block edges excluded)
     bool inside = true;
@@ -649,7 +657,7 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
       if (q != a && q != c && (p3[q] == lo[q] || p3[q] == hi[q])) inside = false;
     if (inside) cleared = true;
   }
-  if (on_edge && !L.eflag[b * 12 + eid]) cleared = true;
+  if (on_edge && !s_ef[eid]) cleared = true;
   if (cleared) val = Real(0);
   // finer blocks
   const double* fdx[3];
@@ -710,7 +718,7 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
   }
   // AverageFluxBoundary
   if (on_edge) {
-    const int nf = L.nfine[b * 12 + eid];
+    const int nf = s_nf[eid];
     if (nf != 1) val *= (Real)(1.0 / (double)nf);
   } else {
     // the one face this position lies on
@@ -719,7 +727,7 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
       if (q != c && onf[q] != 0) a = q;
     int o[3] = {0, 0, 0};
     o[a] = onf[a];
-    const int nl = __ldg(L.nblev + (i64)b * 27 + (o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1));
+    const int nl = (s_lev[(o[2] + 1) * 9 + (o[1] + 1) * 3 + (o[0] + 1)]);
     if (nl == lev) {
       val *= Real(0.5);
     } else if (nl > lev) {
@@ -731,5 +739,67 @@ ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e
   Real* out = (Real*)(c == 0 ? L.ecorr1 : c == 1 ? L.ecorr2 : L.ecorr3);
   out[eidx(b, k, j, i)] = val;
 }
+
+// Grid (blocks, position chunks): the CTAs of block blockIdx.x stage its neighbour list
+// and levels in shared memory; a thread takes edge positions on the block boundary (for
+// component c, the positions with a transverse index on the block's first or last face).
+// Same-level contributions in neighbour-list order, clearing of the positions shared with
+// finer blocks, the finer blocks' restricted values in list order, then the averaging
+// (flux_correction_fc.cpp:689-1545).
+__host__ __device__ __forceinline__ i64 ml_emf_positions(const DevMesh& m) {
+  // per component c: nx_c cells times the perimeter 2 (nx_ta + nx_tb) of the transverse
+  // rectangle of (nx_ta + 1) x (nx_tb + 1) positions
+  return (i64)m.nx1 * 2 * (m.nx2 + m.nx3) + (i64)m.nx2 * 2 * (m.nx1 + m.nx3) +
+         (i64)m.nx3 * 2 * (m.nx1 + m.nx2);
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(128)
+ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e2,
+              const Real* __restrict__ e3) {
+  const int nx1 = m.nx1, nx2 = m.nx2, nx3 = m.nx3;
+  const int b = blockIdx.x;
+  __shared__ int s_nt[56 * 10];
+  __shared__ int s_lev[27];
+  __shared__ int s_ef[12], s_nf[12];
+  const DevML& L = m.ml;
+  const int nn = __ldg(L.nnbr + b);
+  for (int q = threadIdx.x; q < nn * 10; q += blockDim.x) s_nt[q] = __ldg(L.nbrt + (i64)b * 560 + q);
+  if (threadIdx.x < 27) s_lev[threadIdx.x] = __ldg(L.nblev + (i64)b * 27 + threadIdx.x);
+  if (threadIdx.x < 12) {
+    s_ef[threadIdx.x] = __ldg(L.eflag + b * 12 + threadIdx.x);
+    s_nf[threadIdx.x] = __ldg(L.nfine + b * 12 + threadIdx.x);
+  }
+  __syncthreads();
+  const i64 npos = ml_emf_positions(m);
+  for (i64 r0 = (i64)blockIdx.y * blockDim.x + threadIdx.x; r0 < npos;
+       r0 += (i64)gridDim.y * blockDim.x) {
+    // component c, cell index along c, perimeter index of the transverse rectangle
+    const int nxs[3] = {nx1, nx2, nx3};
+    int c = 0;
+    i64 r = r0;
+    for (; c < 2; ++c) {
+      const int ta_ = c == 0 ? 1 : 0, tb_ = c == 2 ? 1 : 2;
+      const i64 nc = (i64)nxs[c] * 2 * (nxs[ta_] + nxs[tb_]);
+      if (r < nc) break;
+      r -= nc;
+    }
+    const int ta0 = c == 0 ? 1 : 0, tb0 = c == 2 ? 1 : 2;
+    const int na = nxs[ta0], nbt = nxs[tb0];
+    const int per = 2 * (na + nbt);
+    const int pc = (int)(r / per);
+    int pr = (int)(r % per), pa, pb;
+    if (pr < na + 1) { pa = pr; pb = 0; }
+    else if ((pr -= na + 1) < na + 1) { pa = pr; pb = nbt; }
+    else { pr -= na + 1; pa = (pr & 1) ? na : 0; pb = 1 + (pr >> 1); }
+    int q3[3];
+    q3[c] = pc;
+    q3[ta0] = pa;
+    q3[tb0] = pb;
+    const int i = m.is + q3[0], j = m.js + q3[1], k = m.ks + q3[2];
+    ml_emf_position<Real>(m, e1, e2, e3, b, c, k, j, i, s_nt, nn, s_lev, s_ef, s_nf);
+  }
+}
+
 
 }  // namespace athgpu

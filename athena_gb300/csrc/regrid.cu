@@ -40,35 +40,37 @@ using namespace athgpu;
 
 // ---- refinement measure ---------------------------------------------------------------
 // pgen/blast.cpp:413-443: per block the maximum over the interior and one ghost layer of
-// sqrt(sum_d (0.5 (p(+1) - p(-1)))^2) / p, in FP64.  One CTA per block.
+// sqrt(sum_d (0.5 (p(+1) - p(-1)))^2) / p, in the bulk precision (FP64: the reference's
+// arithmetic).  One CTA per block.
 template <typename Real>
 __global__ void __launch_bounds__(256)
 refine_eps_kernel(DevMesh m, const Real* __restrict__ w, double* __restrict__ out) {
+  using Acc = Real;
   const int b = blockIdx.x;
   const int n1 = m.nx1 + 2, n2 = m.nx2 + 2, n3 = m.nx3 + 2;
   const int tot = n1 * n2 * n3;
   const Real* p = w + ((i64)b * NHYDRO + IPR) * m.ncell;
   const i64 sj = m.nc1, sk = (i64)m.nc1 * m.nc2;
-  double mx = 0.0;
+  Acc mx = Acc(0);
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     const int i = m.is - 1 + t % n1, j = m.js - 1 + (t / n1) % n2, k = m.ks - 1 + t / (n1 * n2);
     const i64 c = k * sk + j * sj + i;
-    const double a = 0.5 * ((double)p[c + 1] - (double)p[c - 1]);
-    const double e = 0.5 * ((double)p[c + sj] - (double)p[c - sj]);
-    const double f = 0.5 * ((double)p[c + sk] - (double)p[c - sk]);
-    const double eps = sqrt(a * a + e * e + f * f) / (double)p[c];
+    const Acc a = Acc(0.5) * (p[c + 1] - p[c - 1]);
+    const Acc e = Acc(0.5) * (p[c + sj] - p[c - sj]);
+    const Acc f = Acc(0.5) * (p[c + sk] - p[c - sk]);
+    const Acc eps = sqrt(a * a + e * e + f * f) / p[c];
     mx = (mx < eps) ? eps : mx;
   }
-  __shared__ double red[256 / 32];
+  __shared__ Acc red[256 / 32];
   for (int o = 16; o > 0; o >>= 1) {
-    const double v = __shfl_down_sync(0xffffffffu, mx, o);
+    const Acc v = __shfl_down_sync(0xffffffffu, mx, o);
     mx = (mx < v) ? v : mx;
   }
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int q = 1; q < (int)(blockDim.x >> 5); ++q) mx = (mx < red[q]) ? red[q] : mx;
-    out[b] = mx;
+    out[b] = (double)mx;
   }
 }
 

@@ -225,11 +225,10 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   if (m.ml.on) {
     // EMF correction across levels (flux_correction_fc.cpp)
     ProfScope ps2(c, "ml_emf");
-    const long long n = (long long)m.nb * ((long long)(m.nx3 + 1) * (m.nx2 + 1) * m.nx1 +
-                                           (long long)(m.nx3 + 1) * m.nx2 * (m.nx1 + 1) +
-                                           (long long)m.nx3 * (m.nx2 + 1) * (m.nx1 + 1));
-    ml_emf_kernel<Real><<<nblk(n, 128), 128, 0, s>>>(m, (const Real*)r.e1, (const Real*)r.e2,
-                                                     (const Real*)r.e3);
+    const long long chunks = (ml_emf_positions(m) + 127) / 128;
+    dim3 grid(m.nb, (unsigned)(chunks < 65535 ? chunks : 65535));
+    ml_emf_kernel<Real><<<grid, 128, 0, s>>>(m, (const Real*)r.e1, (const Real*)r.e2,
+                                             (const Real*)r.e3);
     c->launches += 1;
   }
   double* o1 = (stage == 1) ? r.bs1 : r.b1;
