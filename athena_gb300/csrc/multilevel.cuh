@@ -80,7 +80,7 @@ __device__ __forceinline__ T mm_grad(T cm, T c0, T cp, T dxm, T dxp) {
 // own branch of the element loop
 template <typename Real, int CODE>
 __device__ __forceinline__ void ml_op_code(const DevMesh& m, const MlArrays<Real>& A, int b,
-                                           const MlOp& op) {
+                                           const MlOp& op, int t0, int dt) {
   const DevML& L = m.ml;
   const int nel = box_count(op);
   const double* dx[3] = {m.dx1f + (i64)b * m.nc1, m.dx2f + (i64)b * m.nc2,
@@ -94,7 +94,61 @@ __device__ __forceinline__ void ml_op_code(const DevMesh& m, const MlArrays<Real
   Real* su = (Real*)L.scons;
   Real* cw = (Real*)L.cprim;
   Real* cbcc = (Real*)L.cbcc;
-  for (int t = threadIdx.x; t < nel; t += blockDim.x) {
+  if (CODE == ML_COPY_U || CODE == ML_COPY_B) {
+    // copies: four elements per thread per pass, all loads issued before the stores
+    // (the copies are latency-bound reads of other blocks' data)
+    constexpr int U = 4;
+    const bool ssend = op.src_kind == ML_SEND, dcoarse = op.dst_kind == ML_COARSE;
+    for (int t = t0; t < nel; t += U * dt) {
+      i64 sidx[U], didx[U];
+      bool ok[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int tt = t + u * dt;
+        ok[u] = tt < nel;
+        int k, j, i;
+        box_pos(op, ok[u] ? tt : t, k, j, i);
+        const int sk = op.o[2] + (k - op.s[2]), sj = op.o[1] + (j - op.s[1]),
+                  si = op.o[0] + (i - op.s[0]);
+        if (CODE == ML_COPY_U) {
+          sidx[u] = ssend ? ccidx(m, op.src, 0, NHYDRO, sk, sj, si)
+                          : cidx(m, op.src, 0, NHYDRO, sk, sj, si);
+          didx[u] = dcoarse ? ccidx(m, b, 0, NHYDRO, k, j, i) : cidx(m, b, 0, NHYDRO, k, j, i);
+        } else {
+          sidx[u] = fcidx(m, ssend, op.d, op.src, sk, sj, si);
+          didx[u] = fcidx(m, dcoarse, op.d, b, k, j, i);
+        }
+      }
+      if (CODE == ML_COPY_U) {
+        const Real* sp = ssend ? su : A.u;
+        Real* dp = dcoarse ? cu : A.u;
+        const i64 svs = ssend ? L.nccell : m.ncell, dvs = dcoarse ? L.nccell : m.ncell;
+        Real v[U][NHYDRO];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int n = 0; n < NHYDRO; ++n)
+            if (ok[u]) v[u][n] = sp[sidx[u] + n * svs];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int n = 0; n < NHYDRO; ++n)
+            if (ok[u]) dp[didx[u] + n * dvs] = v[u][n];
+      } else {
+        const double* sp = ssend ? SBS(op.d) : FB(op.d);
+        double* dp = dcoarse ? CBS(op.d) : FB(op.d);
+        double v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) v[u] = sp[sidx[u]];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) dp[didx[u]] = v[u];
+      }
+    }
+    return;
+  }
+  for (int t = t0; t < nel; t += dt) {
     int k, j, i;
     box_pos(op, t, k, j, i);
     switch (CODE) {
@@ -453,34 +507,67 @@ __device__ __forceinline__ void ml_op_code(const DevMesh& m, const MlArrays<Real
   }
 }
 
-template <typename Real>
-__device__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b, const MlOp& op) {
+// the operation codes of one list: 0 the restriction list (RESTRICT_U/B), 1 the exchange
+// list (COPY_U/B), 2 any code (ProlongateBoundaries, the regrid); the first two compile to
+// small kernels (few registers, high occupancy)
+template <typename Real, int LIST>
+__device__ __forceinline__ void ml_op(const DevMesh& m, const MlArrays<Real>& A, int b,
+                                      const MlOp& op, int t0, int dt) {
+  if (LIST == 0) {
+    if (op.code == ML_RESTRICT_U) ml_op_code<Real, ML_RESTRICT_U>(m, A, b, op, t0, dt);
+    else if (op.code == ML_RESTRICT_B) ml_op_code<Real, ML_RESTRICT_B>(m, A, b, op, t0, dt);
+    return;
+  }
+  if (LIST == 1) {
+    if (op.code == ML_COPY_U) ml_op_code<Real, ML_COPY_U>(m, A, b, op, t0, dt);
+    else if (op.code == ML_COPY_B) ml_op_code<Real, ML_COPY_B>(m, A, b, op, t0, dt);
+    return;
+  }
   switch (op.code) {
-    case ML_COPY_U: ml_op_code<Real, ML_COPY_U>(m, A, b, op); break;
-    case ML_COPY_B: ml_op_code<Real, ML_COPY_B>(m, A, b, op); break;
-    case ML_RESTRICT_U: ml_op_code<Real, ML_RESTRICT_U>(m, A, b, op); break;
-    case ML_RESTRICT_B: ml_op_code<Real, ML_RESTRICT_B>(m, A, b, op); break;
-    case ML_C2P_COARSE: ml_op_code<Real, ML_C2P_COARSE>(m, A, b, op); break;
-    case ML_BC_COARSE: ml_op_code<Real, ML_BC_COARSE>(m, A, b, op); break;
-    case ML_PROLONG_U: ml_op_code<Real, ML_PROLONG_U>(m, A, b, op); break;
-    case ML_PROLONG_SHARED: ml_op_code<Real, ML_PROLONG_SHARED>(m, A, b, op); break;
-    case ML_PROLONG_INTERNAL: ml_op_code<Real, ML_PROLONG_INTERNAL>(m, A, b, op); break;
-    case ML_FINE_P2C: ml_op_code<Real, ML_FINE_P2C>(m, A, b, op); break;
+    case ML_COPY_U: ml_op_code<Real, ML_COPY_U>(m, A, b, op, t0, dt); break;
+    case ML_COPY_B: ml_op_code<Real, ML_COPY_B>(m, A, b, op, t0, dt); break;
+    case ML_RESTRICT_U: ml_op_code<Real, ML_RESTRICT_U>(m, A, b, op, t0, dt); break;
+    case ML_RESTRICT_B: ml_op_code<Real, ML_RESTRICT_B>(m, A, b, op, t0, dt); break;
+    case ML_C2P_COARSE: ml_op_code<Real, ML_C2P_COARSE>(m, A, b, op, t0, dt); break;
+    case ML_BC_COARSE: ml_op_code<Real, ML_BC_COARSE>(m, A, b, op, t0, dt); break;
+    case ML_PROLONG_U: ml_op_code<Real, ML_PROLONG_U>(m, A, b, op, t0, dt); break;
+    case ML_PROLONG_SHARED: ml_op_code<Real, ML_PROLONG_SHARED>(m, A, b, op, t0, dt); break;
+    case ML_PROLONG_INTERNAL: ml_op_code<Real, ML_PROLONG_INTERNAL>(m, A, b, op, t0, dt); break;
+    case ML_FINE_P2C: ml_op_code<Real, ML_FINE_P2C>(m, A, b, op, t0, dt); break;
     default: break;
   }
 }
 
-template <typename Real>
-__global__ void __launch_bounds__(128, 4)
+// One CTA per block.  The restriction and exchange lists (LIST 0, 1: many small
+// operations) give each operation of a barrier-free run to one warp (lanes over its
+// elements); ProlongateBoundaries (LIST 2: larger, mostly dependent operations) spreads
+// every operation over the whole CTA.  A barrier closes each run.
+template <typename Real, int LIST>
+__global__ void __launch_bounds__(128, LIST == 2 ? 4 : 1)
 ml_ops_kernel(DevMesh m, MlArrays<Real> A, const MlOp* __restrict__ ops,
               const int* __restrict__ off, const int* __restrict__ blk) {
   const int b = blk[blockIdx.x];
-  for (int q = off[blockIdx.x]; q < off[blockIdx.x + 1]; ++q) {
-    const MlOp op = ops[q];
-    ml_op<Real>(m, A, b, op);
-    // runs of operations on disjoint data proceed without a barrier (the planner marks
-    // them); the flag is the same for every thread of the CTA
-    if (!op.nosync) __syncthreads();
+  const int qe = off[blockIdx.x + 1];
+  if (LIST == 2) {
+    for (int q = off[blockIdx.x]; q < qe; ++q) {
+      const MlOp op = ops[q];
+      ml_op<Real, LIST>(m, A, b, op, threadIdx.x, blockDim.x);
+      // the flag is the same for every thread of the CTA
+      if (!op.nosync) __syncthreads();
+    }
+    return;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  int q = off[blockIdx.x];
+  while (q < qe) {
+    int r = q;   // the run: q .. r (r the first operation followed by a barrier)
+    while (r < qe - 1 && ops[r].nosync) ++r;
+    for (int p = q + warp; p <= r; p += nwarps) {
+      const MlOp op = ops[p];
+      ml_op<Real, LIST>(m, A, b, op, lane, 32);
+    }
+    __syncthreads();
+    q = r + 1;
   }
 }
 

@@ -182,7 +182,7 @@ cudaError_t run_ops(athgpu_ctx* c, const MlOpList& L) {
   if (e != cudaSuccess) return e;
   MlArrays<Real> A{(Real*)c->r.u, (Real*)c->r.wbuf[c->r.wsel], (Real*)c->r.bcc, c->r.b1,
                    c->r.b2, c->r.b3};
-  ml_ops_kernel<Real><<<(int)L.blk.size(), 128, 0, s>>>(c->m, A, ops, off, blk);
+  ml_ops_kernel<Real, 2><<<(int)L.blk.size(), 128, 0, s>>>(c->m, A, ops, off, blk);
   c->launches += 1;
   e = cudaGetLastError();
   cudaFreeAsync(ops, s);

@@ -97,8 +97,16 @@ static void launch_ml_phase(athgpu_ctx* c, int phase, Real* u, Real* w, double* 
   static const char* names[3] = {"ml_restrict", "ml_exchange", "ml_prolong"};
   ProfScope ps(c, names[phase]);
   MlArrays<Real> A{u, w, (Real*)c->r.bcc, b1, b2, b3};
-  ml_ops_kernel<Real><<<nb, 128, 0, c->stream>>>(c->m, A, (const MlOp*)c->mld.ops[phase],
-                                                 c->mld.off[phase], c->mld.blk[phase]);
+  const MlOp* ops = (const MlOp*)c->mld.ops[phase];
+  if (phase == 0)
+    ml_ops_kernel<Real, 0><<<nb, 128, 0, c->stream>>>(c->m, A, ops, c->mld.off[phase],
+                                                      c->mld.blk[phase]);
+  else if (phase == 1)
+    ml_ops_kernel<Real, 1><<<nb, 128, 0, c->stream>>>(c->m, A, ops, c->mld.off[phase],
+                                                      c->mld.blk[phase]);
+  else
+    ml_ops_kernel<Real, 2><<<nb, 128, 0, c->stream>>>(c->m, A, ops, c->mld.off[phase],
+                                                      c->mld.blk[phase]);
   c->launches += 1;
 }
 

@@ -88,25 +88,36 @@ class ClockSampler:
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(
-                    ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                     "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                    timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        # one nvidia-smi process in loop mode (-lms): a sample every 25 ms without the
+        # start-up cost of a process per sample
+        try:
+            self._p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "25"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        for line in self._p.stdout:
+            if self._stop.is_set():
+                break
+            line = line.strip()
+            if line:
+                self.samples.append([x.strip() for x in line.split(",")])
 
     def __enter__(self):
+        self._p = None
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
         return self
 
     def __exit__(self, *a):
         self._stop.set()
+        if self._p is not None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
         self._t.join(timeout=10)
 
     def summary(self):
@@ -238,7 +249,7 @@ def run_gpu(args, rank, world, local_rank):
         g.close()
     res["linear_wave_l1"] = run_linear_wave()
     if not args.no_amr:
-        res["amr_blast"] = run_amr_blast(stream)
+        res["amr_blast"] = run_amr_blast(stream, cpu=not args.no_cpu_baseline)
     if not args.no_learned:
         res["learned_c2p"], net = run_learned_c2p()
         if not args.no_sr:
@@ -420,9 +431,10 @@ def run_sr_kh(n, stream, net):
 AMR_ROOT = 128        # root grid cells per direction (8^3 MeshBlocks of 16^3)
 AMR_THR = 0.3        # pressure-gradient threshold of the blast refinement condition
 AMR_WARM = {"fp32": (5, 30), "fp64": (3, 10)}   # warm-up and timed cycles
+AMR_ACC_CYCLES = 12
 
 
-def run_amr_blast(stream):
+def run_amr_blast(stream, cpu=True):
     """Adaptive MHD blast (3 refinement levels, 16^3 MeshBlocks): unit cube
     [-0.5, 0.5]^3 with a 128^3 root grid, rho 1, p 0.1 and p 10 for r < 0.1,
     B = (1,1,1)/sqrt(2), gamma 5/3, VL2 + PLM + HLLE, CFL 0.3, refinement on the blast's
@@ -481,7 +493,82 @@ def run_amr_blast(stream):
         out[prec]["stages_blocks"] = run.mesh.nblocks
         run.close()
     out["speedup_fp32_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # accuracy: FP32 against FP64 after AMR_ACC_CYCLES cycles from the same start
+    finals = {}
+    for prec in ("fp32", "fp64"):
+        mesh0 = MultiLevelMesh((AMR_ROOT,) * 3, (AMR_ROOT // 16,) * 3, 2, (-.5,) * 3,
+                               (.5,) * 3)
+        run = AdaptiveStageUpdate(mesh0, ic, 3, AMR_THR, 10, gamma=5.0 / 3.0, xorder=2,
+                                  rsolver="hlle", precision=prec, cfl=0.3)
+        run.initialize()
+        run.cycle(AMR_ACC_CYCLES)
+        finals[prec] = ([(l.level, l.lx1, l.lx2, l.lx3) for l in run.mesh.locs],
+                        run.mesh.interior(run.state()[0]))
+        run.close()
+    if finals["fp32"][0] == finals["fp64"][0]:
+        l1 = l1_rel(finals["fp32"][1], finals["fp64"][1])
+        out["l1_rel_fp32_vs_fp64"] = {"cycles": AMR_ACC_CYCLES, "d": l1[0], "m1": l1[1],
+                                      "m2": l1[2], "m3": l1[3], "e": l1[4]}
+    else:
+        out["l1_rel_fp32_vs_fp64"] = {"cycles": AMR_ACC_CYCLES,
+                                      "note": "the FP32 and FP64 runs refined differently"}
+    if cpu:
+        out["cpu_baseline"] = amr_cpu_baseline(ic)
     return out
+
+
+def amr_profile_cycle(precision="fp32", warm=2):
+    """One cycle of the adaptive blast without the CUDA graph, every kernel timed with CUDA
+    events, between cudaProfilerStart and cudaProfilerStop (for ncu
+    --profile-from-start off); returns per-kernel launches and milliseconds."""
+    import torch
+    from athena_gb300 import pgen
+    from athena_gb300.adaptive import AdaptiveStageUpdate
+    from athena_gb300.meshtree import MultiLevelMesh
+    b = 1.0 / np.sqrt(2.0)
+    mesh0 = MultiLevelMesh((AMR_ROOT,) * 3, (AMR_ROOT // 16,) * 3, 2, (-.5,) * 3, (.5,) * 3)
+    run = AdaptiveStageUpdate(
+        mesh0, lambda m: pgen.blast_blocks(m, 5.0 / 3.0, radius=0.1, pamb=0.1, prat=100.0,
+                                           bfield=(b, b, b)),
+        3, AMR_THR, 10, gamma=5.0 / 3.0, xorder=2, rsolver="hlle", precision=precision,
+        cfl=0.3)
+    run.initialize()
+    run.cycle(warm)
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStart()
+    prof = run.su.profile_cycle()
+    torch.cuda.synchronize()
+    torch.cuda.cudart().cudaProfilerStop()
+    agg = {}
+    for name, ms in prof:
+        n, t = agg.get(name, (0, 0.0))
+        agg[name] = (n + 1, t + ms)
+    out = {"workload": "adaptive blast %s, %d blocks" % (precision, run.mesh.nblocks),
+           "cycle_ms": sum(ms for _, ms in prof),
+           "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in agg.items()}}
+    run.close()
+    return out
+
+
+def amr_cpu_baseline(ic, threads=None):
+    """The oracle (C port of the reference algorithm, FP64, OpenMP over MeshBlocks) on the
+    host cores: the adaptive initial loop, then one timed cycle with its refinement step
+    (a bounded sample of the adaptive blast workload)."""
+    import time
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import amr_run
+    from athena_gb300.meshtree import MultiLevelMesh
+    threads = threads or os.cpu_count()
+    mesh0 = MultiLevelMesh((AMR_ROOT,) * 3, (AMR_ROOT // 16,) * 3, 2, (-.5,) * 3, (.5,) * 3)
+    amr, om = amr_run.initialize(mesh0, ic, 3, AMR_THR, 10, gamma=5.0 / 3.0, xorder=2,
+                                 rsolver="hlle", cfl=0.3, threads=threads)
+    zones = amr.mesh.nblocks * 16 ** 3
+    t0 = time.perf_counter()
+    om = amr_run.cycle(amr, om, AMR_THR)
+    t = time.perf_counter() - t0
+    return {"value": zones / t, "unit": "zone-cycles/s", "cores": threads, "kind": "port",
+            "sample": "1 cycle (with its refinement step) of the %d-block mesh after the "
+                      "adaptive initial loop" % (zones // 16 ** 3)}
 
 
 def l1_rel(a, b):
@@ -512,7 +599,7 @@ def cpu_baseline(mesh_ic, cycles=2, threads=None):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -524,7 +611,14 @@ def main():
                     help="skip the adaptive blast measurement")
     ap.add_argument("--nx", type=int, default=256,
                     help="cells per direction (MeshBlocks of 32^3); 256 is the workload")
+    ap.add_argument("--amr-profile-cycle", action="store_true",
+                    help="only: one profiled cycle of the adaptive blast (FP32)")
     args = ap.parse_args()
+    if args.amr_profile_cycle:
+        from athena_gb300 import build
+        build.build()
+        print(json.dumps(amr_profile_cycle()))
+        return
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
