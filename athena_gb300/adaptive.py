@@ -38,6 +38,7 @@ class AdaptiveStageUpdate:
         self.condition = condition or blast_condition
         self.regrids = 0
         self.t_refine = 0.0   # host seconds in the refinement steps (regrids included)
+        self.regrid_ms = []   # milliseconds of each main-loop refinement step that regridded
         if self.native:
             self.namr = NativeAmr(mesh0.nx, mesh0.nrbx, mesh0.ng, mesh0.xmin, mesh0.xmax,
                                   mesh0.bcs, numlevel, derefine_count)
@@ -105,10 +106,11 @@ class AdaptiveStageUpdate:
                 after_stages(self)
             su.synchronize()   # the step below synchronizes anyway: time only the step
             t0 = time.perf_counter()
+            changed = False
             if self.native:
                 if self.namr.step(su, self.thr, after_cycle=True):
                     self._set_mesh(NativeMesh(self.namr))
-                    self.regrids += 1
+                    changed = True
             else:
                 plan = self.amr.update(self.amr.check_refinement(
                     self.condition(su.refinement_eps(), self.thr)))
@@ -116,8 +118,12 @@ class AdaptiveStageUpdate:
                     su.regrid(plan, after_cycle=True)
                     self.amr.accept(plan)
                     su.new_time_step()
-                    self.regrids += 1
-            self.t_refine += time.perf_counter() - t0
+                    changed = True
+            dt = time.perf_counter() - t0
+            self.t_refine += dt
+            if changed:
+                self.regrids += 1
+                self.regrid_ms.append(dt * 1e3)
 
     # the state accessors of StageUpdate
     def state(self):

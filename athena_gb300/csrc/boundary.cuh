@@ -1,9 +1,10 @@
 // Physical mesh boundaries: BoundaryValues::ApplyPhysicalBoundaries (bvals/bvals.cpp:
 // 453-680) for outflow and reflecting faces, on the primitives (bvals/cc/outflow_cc.cpp,
 // bvals/cc/hydro/reflect_hydro.cpp), the face field (bvals/fc/outflow_fc.cpp,
-// bvals/fc/reflect_fc.cpp) and then the cell-centred field of the filled ghost cells
-// (bvals.cpp:516-520), axis by axis (x1, x2, x3), after W(U).  The conserved state of
-// those ghost cells (bvals.cpp:521-522) is not formed: nothing on the path reads it.
+// bvals/fc/reflect_fc.cpp), then the cell-centred field and (Newtonian) the conserved
+// state of the filled ghost cells (bvals.cpp:508-515), axis by axis (x1, x2, x3), after
+// W(U).  A refined parent's halo reads that conserved state (a regrid); the relativistic
+// path reads no ghost U and does not form it.
 //
 // Per axis a two launches: bc_fill_kernel (primitives and face field of both sides), then
 // bc_cc_kernel (cell-centred field and cell-centred E of the filled ghost cells, from the
@@ -156,7 +157,7 @@ template <typename Real, bool SR>
 __global__ void __launch_bounds__(256)
 bc_cc_kernel(DevMesh m, int a, const Real* __restrict__ w, const double* __restrict__ b1,
              const double* __restrict__ b2, const double* __restrict__ b3,
-             Real* __restrict__ bcc, Real* __restrict__ cc) {
+             Real* __restrict__ bcc, Real* __restrict__ cc, Real* __restrict__ u) {
   BcThread q;
   if (!bc_thread(m, a, (long long)blockIdx.x * blockDim.x + threadIdx.x, q)) return;
   if (has_nbr(m, q.b, 2 * a + q.side)) return;
@@ -192,6 +193,17 @@ bc_cc_kernel(DevMesh m, int a, const Real* __restrict__ w, const double* __restr
   bcc[cb + 2 * vs] = c3;
   store_cce<Real, SR>(cc, cb, vs, w[cw + IVX * vs], w[cw + IVY * vs], w[cw + IVZ * vs], c1,
                       c2, c3);
+  if (!SR) {  // PrimitiveToConserved (adiabatic_mhd.cpp:99-133), bulk precision
+    const Real igm1 = Real(1) / (Real)(m.gamma - 1.0);
+    const Real w_d = w[cw], w_vx = w[cw + IVX * vs], w_vy = w[cw + IVY * vs],
+               w_vz = w[cw + IVZ * vs], w_p = w[cw + IPR * vs];
+    u[cw] = w_d;
+    u[cw + vs] = w_vx * w_d;
+    u[cw + 2 * vs] = w_vy * w_d;
+    u[cw + 3 * vs] = w_vz * w_d;
+    u[cw + 4 * vs] = w_p * igm1 + Real(0.5) * (w_d * (w_vx * w_vx + w_vy * w_vy + w_vz * w_vz) +
+                                               (c1 * c1 + c2 * c2 + c3 * c3));
+  }
 }
 
 // threads of one axis-a launch

@@ -242,10 +242,8 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     return api_fail(ATHGPU_ERR_ARG, "the new mesh must keep the block size, nghost, "
                                        "precision and solver of the old one");
   for (int f = 0; f < 6; ++f)
-    if (desc->bc[f] != ATHGPU_BC_PERIODIC)
-      return api_fail(ATHGPU_ERR_UNSUPPORTED,
-                         "regridding is implemented for periodic meshes (a refined parent's "
-                         "halo would need U in its physical ghost cells)");
+    if (desc->bc[f] != od.bc[f])
+      return api_fail(ATHGPU_ERR_ARG, "the new mesh must keep the boundary flags");
   const int onb = om.nb, nnb = desc->nbx1;
   const std::vector<long long>& ol = c->mld.hloc;
   // the block maps must describe a refinement or derefinement of the old tree

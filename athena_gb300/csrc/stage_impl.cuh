@@ -187,7 +187,7 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
       bc_fill_kernel<Real><<<nblk(n, 256), 256, 0, s>>>(m, a, wout, b1, b2, b3);
       auto cck = c->desc.relativistic ? bc_cc_kernel<Real, true> : bc_cc_kernel<Real, false>;
       cck<<<nblk(n, 256), 256, 0, s>>>(m, a, wout, b1, b2, b3, (Real*)c->r.bcc,
-                                       (Real*)c->r.cce);
+                                       (Real*)c->r.cce, u);
       c->launches += 2;
     }
   }

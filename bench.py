@@ -481,7 +481,10 @@ def run_amr_blast(stream, cpu=True):
                      "levels": [int(v) for v in np.bincount(run.mesh.levels)[
                          run.mesh.tree.root_level:]],
                      "regrids": run.regrids - r0,
-                     "refine_step_s": run.t_refine - tr0}
+                     "refine_step_s": run.t_refine - tr0,
+                     # every main-loop regrid of the run (warm-up included): the whole
+                     # refinement step, device data movement and re-initialisation
+                     "regrid_ms": [round(v, 2) for v in run.regrid_ms]}
         # the stages alone (CUDA graph replays) on the final mesh
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         run.su.cycle(2)

@@ -119,7 +119,7 @@ athgpu_status athgpu_refinement_eps(athgpu_ctx* ctx, double* maxeps);
  * (mesh/amr_loadbalance.cpp:351-660) followed by its Initialize(2) (ghost exchange,
  * ProlongateBoundaries, W(U), NewBlockTimeStep + Mesh::NewTimeStep).
  *   desc        the new mesh (nbx1 = new block count, every block's coordinates; block size,
- *               nghost, precision, solver and boundary flags unchanged; periodic meshes);
+ *               nghost, precision, solver and boundary flags unchanged);
  *   nbr_table .. cdx3f   the new mesh's tables as for athgpu_set_multilevel;
  *   newtoold[n] the old block each new block n comes from (MeshBlockTree::GetMeshBlockList's
  *               previous gids); kind[n] 0: kept; 1: derefined, made from the eight old

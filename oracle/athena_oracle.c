@@ -1533,6 +1533,31 @@ long orc_c2p_failures(const orc_mesh *m) { return m->c2p_fail; }
  * state of those ghost cells (bvals.cpp:521-522) is not formed: nothing on the path
  * reads it.
  */
+/* EquationOfState::PrimitiveToConserved, Newtonian MHD (adiabatic_mhd.cpp:99-133), over
+ * a cell range of block b (from w and the cell-centred field) */
+static void p2c_range(orc_mesh *m, int b, const double *w, int i0, int i1, int j0, int j1,
+                      int k0, int k1) {
+  double igm1 = 1.0 / (m->p.gamma - 1.0);
+  double *ub = m->u + (long)b * NHYDRO * m->ncell;
+  const double *wb = w + (long)b * NHYDRO * m->ncell;
+  const double *bc = m->bcc + (long)b * 3 * m->ncell;
+  long nc = m->ncell;
+  for (int k = k0; k <= k1; ++k)
+    for (int j = j0; j <= j1; ++j)
+      for (int i = i0; i <= i1; ++i) {
+        long q = CIDX(m, 0, k, j, i);
+        double w_d = wb[q], w_vx = wb[q + nc], w_vy = wb[q + 2 * nc], w_vz = wb[q + 3 * nc],
+               w_p = wb[q + 4 * nc];
+        double bcc1 = bc[q], bcc2 = bc[q + nc], bcc3 = bc[q + 2 * nc];
+        ub[q] = w_d;
+        ub[q + nc] = w_vx * w_d;
+        ub[q + 2 * nc] = w_vy * w_d;
+        ub[q + 3 * nc] = w_vz * w_d;
+        ub[q + 4 * nc] = w_p * igm1 + 0.5 * (w_d * (SQR(w_vx) + SQR(w_vy) + SQR(w_vz)) +
+                                             (SQR(bcc1) + SQR(bcc2) + SQR(bcc3)));
+      }
+}
+
 static void apply_bcs(orc_mesh *m, int b, double *w) {
   int ng = m->p.ng;
   int lo[3] = {m->is, m->js, m->ks}, hi[3] = {m->ie, m->je, m->ke};
@@ -1626,6 +1651,9 @@ static void apply_bcs(orc_mesh *m, int b, double *w) {
       c0[a] = side ? hi[a] + 1 : lo[a] - ng;
       c1[a] = side ? hi[a] + ng : lo[a] - 1;
       cell_centered_field(m, b, c0[0], c1[0], c0[1], c1[1], c0[2], c1[2]);
+      /* the conserved state of those ghost cells (bvals.cpp:514-515); the relativistic
+       * path reads no ghost U and does not form it */
+      if (!m->p.relativistic) p2c_range(m, b, w, c0[0], c1[0], c0[1], c1[1], c0[2], c1[2]);
     }
   }
   (void)nc;

@@ -106,6 +106,12 @@ AMR_CASES = {
                           {"radius": 0.12, "pamb": 0.1, "prat": 100.0, "b0": 1.0,
                            "angle": 30.0, "x1_0": 0.3, "x2_0": 0.0, "x3_0": 0.0,
                            "thr": 1.0}, 3, 1, 3, 0.3, 12),
+    # outflow x1 faces, reflecting x2 faces, periodic x3; the blast near a corner
+    "amrblastbc_hlle_plm": ("mhd_hlle_g2", ((32, 32, 32), (4, 4, 4), 2, (-.5, -.5, -.5),
+                                            (.5, .5, .5), (1, 1, 2, 2, 0, 0)),
+                            {"radius": 0.1, "pamb": 0.1, "prat": 100.0, "b0": 1.0,
+                             "angle": 60.0, "x1_0": 0.38, "x2_0": -0.4, "x3_0": 0.45,
+                             "thr": 0.5}, 3, 2, 2, 0.3, 10),
 }
 
 
