@@ -165,6 +165,37 @@ def run_amr_case(name, spec):
             "nblocks_last": len(dump["locs"]), "regrids": nregrid}
 
 
+def run_restart_case():
+    """A restart through the reference: the linear wave on one 8x4x4 MeshBlock runs 3
+    cycles and writes its final restart file (outputs/restart.cpp); a second run restarts
+    from that file (``-r``) to cycle 6.  Stores the restart file itself and the restarted
+    run's dts and final interior state."""
+    import shutil
+    import subprocess
+    mesh = MeshSpec((8, 4, 4), (1, 1, 1), 2, (0., 0., 0.), (3.0, 1.5, 1.5))
+    text = ref_run.athinput(mesh, GAMMA_LW, 2, 0.3, 3, 1.0e3, {
+        "compute_error": "false", "wave_flag": 0, "amp": 1.0e-6, "vflow": 0.0})
+    text += "<output9>\nfile_type = rst\ndt = 1.0e9\n"
+    d, _ = ref_run.run_reference("mhd_hlld_g2", "athena_lw", text)
+    exe = os.path.join(ref_run.REF_OUT, "mhd_hlld_g2", "athena_lw")
+    # the restarted run writes its own final restart file: keep the first one apart
+    shutil.copyfile(os.path.join(d, "Ref.final.rst"), os.path.join(d, "cycle3.rst"))
+    shutil.copyfile(os.path.join(d, "Ref.final.rst"), os.path.join(OUT, "restart_lw.rst"))
+    r = subprocess.run([exe, "-r", "cycle3.rst", "time/nlim=6"], cwd=d,
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
+    dts = []
+    for c in range(4, 7):
+        dump = ref_run.read_dump(os.path.join(d, "dump.%05d.bin" % c), mesh)
+        dts.append(dump["dt"])
+    np.savez_compressed(os.path.join(OUT, "restart_lw_after.npz"),
+                        u=mesh.interior(dump["u"]), dt=np.array(dts), time=dump["time"])
+    return {"variant": "mhd_hlld_g2", "nx": [8, 4, 4], "nb": [1, 1, 1], "ng": 2,
+            "xmin": [0., 0., 0.], "xmax": [3.0, 1.5, 1.5], "gamma": GAMMA_LW, "xorder": 2,
+            "rsolver": "hlld", "cfl": 0.3, "cycles_before": 3, "cycles_after": 3}
+
+
 def ml_mesh(margs):
     from athena_gb300.meshtree import MultiLevelMesh
     nx, nrbx, ng, xmin, xmax, bcs, regions = margs
@@ -340,6 +371,9 @@ def main(only=None):
             continue
         print("case", name, flush=True)
         meta["amr_cases"][name] = run_amr_case(name, spec)
+    if not only or "restart" in only:
+        print("restart", flush=True)
+        meta["restart"] = run_restart_case()
     if not only or "history" in only:
         print("history", flush=True)
         meta["history"] = run_history()
