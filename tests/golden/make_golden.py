@@ -196,6 +196,25 @@ def run_restart_case():
             "rsolver": "hlld", "cfl": 0.3, "cycles_before": 3, "cycles_after": 3}
 
 
+def run_vtk_case():
+    """The reference's VTK outputs (prim as out8, cons as out7) of the initial state of the
+    linear wave on two MeshBlocks of 4^3 (the outputs written at t = 0, after
+    Mesh::Initialize)."""
+    import shutil
+    mesh = MeshSpec((8, 4, 4), (2, 1, 1), 2, (0., 0., 0.), (3.0, 1.5, 1.5))
+    text = ref_run.athinput(mesh, GAMMA_LW, 2, 0.3, 1, 1.0e3, {
+        "compute_error": "false", "wave_flag": 0, "amp": 1.0e-6, "vflow": 0.0})
+    text += ("<output8>\nfile_type = vtk\nvariable = prim\ndt = 1.0e9\n"
+             "<output7>\nfile_type = vtk\nvariable = cons\ndt = 1.0e9\n")
+    d, _ = ref_run.run_reference("mhd_hlld_g2", "athena_lw", text)
+    os.makedirs(os.path.join(OUT, "vtk"), exist_ok=True)
+    files = sorted(f for f in os.listdir(d) if f.endswith(".vtk"))
+    for f in files:
+        shutil.copyfile(os.path.join(d, f), os.path.join(OUT, "vtk", f))
+    return {"nx": [8, 4, 4], "nb": [2, 1, 1], "ng": 2, "xmin": [0., 0., 0.],
+            "xmax": [3.0, 1.5, 1.5], "gamma": GAMMA_LW, "files": files}
+
+
 def ml_mesh(margs):
     from athena_gb300.meshtree import MultiLevelMesh
     nx, nrbx, ng, xmin, xmax, bcs, regions = margs
@@ -371,6 +390,9 @@ def main(only=None):
             continue
         print("case", name, flush=True)
         meta["amr_cases"][name] = run_amr_case(name, spec)
+    if not only or "vtk" in only:
+        print("vtk", flush=True)
+        meta["vtk"] = run_vtk_case()
     if not only or "restart" in only:
         print("restart", flush=True)
         meta["restart"] = run_restart_case()
