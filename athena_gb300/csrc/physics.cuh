@@ -268,6 +268,54 @@ __device__ __forceinline__ void hlld(Real gamma, const Real* wli, const Real* wr
   }
 }
 
+// local Lax-Friedrichs, hydro/rsolvers/mhd/llf_mhd.cpp:29-153 (adiabatic branch)
+template <typename Real>
+__device__ __forceinline__ void llf(Real gamma, const Real* wli, const Real* wri, Real bxi,
+                                    Real* flxi) {
+  const Real gm1 = gamma - RC(1.0);
+  Real fl[NWAVE], fr[NWAVE], du[NWAVE];
+  const Real cfl = fast_ms(gamma, wli[IDN], wli[IPR], wli[IBY], wli[IBZ], bxi);
+  const Real cfr = fast_ms(gamma, wri[IDN], wri[IPR], wri[IBY], wri[IBZ], bxi);
+  const Real a = RC(0.5) * smax(fabs(wli[IVX]) + cfl, fabs(wri[IVX]) + cfr);
+  const Real mxl = wli[IDN] * wli[IVX];
+  const Real mxr = wri[IDN] * wri[IVX];
+  const Real pbl = RC(0.5) * (bxi * bxi + wli[IBY] * wli[IBY] + wli[IBZ] * wli[IBZ]);
+  const Real pbr = RC(0.5) * (bxi * bxi + wri[IBY] * wri[IBY] + wri[IBZ] * wri[IBZ]);
+  fl[IDN] = mxl;
+  fr[IDN] = mxr;
+  fl[IVX] = mxl * wli[IVX] + pbl - bxi * bxi;
+  fr[IVX] = mxr * wri[IVX] + pbr - bxi * bxi;
+  fl[IVY] = mxl * wli[IVY] - bxi * wli[IBY];
+  fr[IVY] = mxr * wri[IVY] - bxi * wri[IBY];
+  fl[IVZ] = mxl * wli[IVZ] - bxi * wli[IBZ];
+  fr[IVZ] = mxr * wri[IVZ] - bxi * wri[IBZ];
+  const Real el = wli[IPR] / gm1 +
+                  RC(0.5) * wli[IDN] *
+                      (wli[IVX] * wli[IVX] + wli[IVY] * wli[IVY] + wli[IVZ] * wli[IVZ]) + pbl;
+  const Real er = wri[IPR] / gm1 +
+                  RC(0.5) * wri[IDN] *
+                      (wri[IVX] * wri[IVX] + wri[IVY] * wri[IVY] + wri[IVZ] * wri[IVZ]) + pbr;
+  fl[IVX] += wli[IPR];
+  fr[IVX] += wri[IPR];
+  fl[IPR] = (el + wli[IPR] + pbl - bxi * bxi) * wli[IVX];
+  fr[IPR] = (er + wri[IPR] + pbr - bxi * bxi) * wri[IVX];
+  fl[IPR] -= bxi * (wli[IBY] * wli[IVY] + wli[IBZ] * wli[IVZ]);
+  fr[IPR] -= bxi * (wri[IBY] * wri[IVY] + wri[IBZ] * wri[IVZ]);
+  fl[IBY] = wli[IBY] * wli[IVX] - bxi * wli[IVY];
+  fr[IBY] = wri[IBY] * wri[IVX] - bxi * wri[IVY];
+  fl[IBZ] = wli[IBZ] * wli[IVX] - bxi * wli[IVZ];
+  fr[IBZ] = wri[IBZ] * wri[IVX] - bxi * wri[IVZ];
+  du[IDN] = wri[IDN] - wli[IDN];
+  du[IVX] = wri[IDN] * wri[IVX] - wli[IDN] * wli[IVX];
+  du[IVY] = wri[IDN] * wri[IVY] - wli[IDN] * wli[IVY];
+  du[IVZ] = wri[IDN] * wri[IVZ] - wli[IDN] * wli[IVZ];
+  du[IPR] = er - el;
+  du[IBY] = wri[IBY] - wli[IBY];
+  du[IBZ] = wri[IBZ] - wli[IBZ];
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) flxi[n] = RC(0.5) * (fl[n] + fr[n]) - a * du[n];
+}
+
 // HLLE, hydro/rsolvers/mhd/hlle_mhd.cpp:25-182
 template <typename Real>
 __device__ __forceinline__ void hlle(Real gamma, const Real* wli, const Real* wri, Real bxi,

@@ -19,7 +19,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libathgpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300.h")
 
-HLLD, HLLE = 0, 1
+HLLD, HLLE, LLF = 0, 1, 2
+_RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF}
 FP64, FP32 = 0, 1
 
 
@@ -196,7 +197,7 @@ class StageUpdate:
         d.nbx1, d.nbx2, d.nbx3 = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
         d.nx1, d.nx2, d.nx3 = mesh.bx
         d.nghost, d.xorder = mesh.ng, k["xorder"]
-        d.rsolver = HLLD if k["rsolver"] == "hlld" else HLLE
+        d.rsolver = _RSOLVERS[k["rsolver"]]
         d.precision = FP64 if k["precision"] == "fp64" else FP32
         d.relativistic = 1 if k["relativistic"] else 0
         d.sigma_max, d.beta_min, d.gamma_max = k["sigma_max"], k["beta_min"], k["gamma_max"]

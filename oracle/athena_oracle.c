@@ -408,6 +408,51 @@ static void sr_fast_speeds(double gamma_adi, double wgas, double pgas, double u0
   *lm = (a1 >= 0.0) ? (-a1 - s) / 2.0 : -2.0 * a0 / (a1 - s);
 }
 
+/* local Lax-Friedrichs, hydro/rsolvers/mhd/llf_mhd.cpp:29-153 (adiabatic).  Local order
+ * as for hlld(). */
+static void llf(double gamma, const double *wli, const double *wri, double bxi,
+                double *flxi) {
+  double gm1 = gamma - 1.0;
+  double fl[NWAVE], fr[NWAVE], du[NWAVE];
+  double cfl = fast_ms(gamma, wli, bxi);
+  double cfr = fast_ms(gamma, wri, bxi);
+  double a = 0.5 * smax(fabs(wli[IVX]) + cfl, fabs(wri[IVX]) + cfr);
+  double mxl = wli[IDN] * wli[IVX];
+  double mxr = wri[IDN] * wri[IVX];
+  double pbl = 0.5 * (bxi * bxi + SQR(wli[IBY]) + SQR(wli[IBZ]));
+  double pbr = 0.5 * (bxi * bxi + SQR(wri[IBY]) + SQR(wri[IBZ]));
+  fl[IDN] = mxl;
+  fr[IDN] = mxr;
+  fl[IVX] = mxl * wli[IVX] + pbl - SQR(bxi);
+  fr[IVX] = mxr * wri[IVX] + pbr - SQR(bxi);
+  fl[IVY] = mxl * wli[IVY] - bxi * wli[IBY];
+  fr[IVY] = mxr * wri[IVY] - bxi * wri[IBY];
+  fl[IVZ] = mxl * wli[IVZ] - bxi * wli[IBZ];
+  fr[IVZ] = mxr * wri[IVZ] - bxi * wri[IBZ];
+  double el = wli[IPR] / gm1 +
+              0.5 * wli[IDN] * (SQR(wli[IVX]) + SQR(wli[IVY]) + SQR(wli[IVZ])) + pbl;
+  double er = wri[IPR] / gm1 +
+              0.5 * wri[IDN] * (SQR(wri[IVX]) + SQR(wri[IVY]) + SQR(wri[IVZ])) + pbr;
+  fl[IVX] += wli[IPR];
+  fr[IVX] += wri[IPR];
+  fl[IPR] = (el + wli[IPR] + pbl - bxi * bxi) * wli[IVX];
+  fr[IPR] = (er + wri[IPR] + pbr - bxi * bxi) * wri[IVX];
+  fl[IPR] -= bxi * (wli[IBY] * wli[IVY] + wli[IBZ] * wli[IVZ]);
+  fr[IPR] -= bxi * (wri[IBY] * wri[IVY] + wri[IBZ] * wri[IVZ]);
+  fl[IBY] = wli[IBY] * wli[IVX] - bxi * wli[IVY];
+  fr[IBY] = wri[IBY] * wri[IVX] - bxi * wri[IVY];
+  fl[IBZ] = wli[IBZ] * wli[IVX] - bxi * wli[IVZ];
+  fr[IBZ] = wri[IBZ] * wri[IVX] - bxi * wri[IVZ];
+  du[IDN] = wri[IDN] - wli[IDN];
+  du[IVX] = wri[IDN] * wri[IVX] - wli[IDN] * wli[IVX];
+  du[IVY] = wri[IDN] * wri[IVY] - wli[IDN] * wli[IVY];
+  du[IVZ] = wri[IDN] * wri[IVZ] - wli[IDN] * wli[IVZ];
+  du[IPR] = er - el;
+  du[IBY] = wri[IBY] - wli[IBY];
+  du[IBZ] = wri[IBZ] - wli[IBZ];
+  for (int n = 0; n < NWAVE; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) - a * du[n];
+}
+
 /* SR frame-transforming HLLE, hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330 (SR branch).
  * Local order as for hlld(); velocities are the spatial 4-velocity u^i. */
 static void hlle_sr(double gamma_adi, const double *wli, const double *wri, double bb1,
@@ -622,6 +667,7 @@ static void riemann(const orc_mesh *m, int dir, const double *wl, const double *
   double wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
   if (m->p.relativistic) hlle_sr(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
+  else if (m->p.rsolver == 2) llf(m->p.gamma, wli, wri, bx, flx7);
   else hlle(m->p.gamma, wli, wri, bx, flx7);
 }
 

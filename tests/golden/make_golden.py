@@ -52,6 +52,11 @@ CASES = {
                                             (.5, .5, .5)), "blast", 2, 0.3, 3),
     "blast_hlle_ppm_8blk": ("mhd_hlle_g3", ((16, 16, 16), (2, 2, 2), 3, (-.5, -.5, -.5),
                                             (.5, .5, .5)), "blast", 3, 0.3, 3),
+    # local Lax-Friedrichs (--flux=llf)
+    "blast_llf_plm_8blk": ("mhd_llf_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                          (.5, .5, .5)), "blast", 2, 0.3, 3),
+    "turb_llf_plm_8blk": ("mhd_llf_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                         (1., 1., 1.)), "turbulence", 2, 0.3, 3),
     # special-relativistic MHD (-s -b --flux=hlle): relativistic Kelvin-Helmholtz layer
     "srkh_hlle_plm_8blk": ("srmhd_hlle_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
                                             (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
@@ -159,7 +164,7 @@ def run_amr_case(name, spec):
     return {"variant": variant, "nx": nx, "nrbx": nrbx, "ng": ng, "xmin": xmin,
             "xmax": xmax, "bc": list(bcs), "problem": prob, "numlevel": numlevel,
             "derefine_count": dcount, "floor": float(AMR_FLOOR), "xorder": xorder,
-            "rsolver": "hlld" if "hlld" in variant else "hlle", "cfl": cfl,
+            "rsolver": variant.split("_")[1], "cfl": cfl,
             "ncycle": ncycle, "gamma": gamma, "tlim": 1.0e3, "time": dump["time"],
             "digest": state_digest(mesh, dump["u"], dump["b1"], dump["b2"], dump["b3"]),
             "nblocks_last": len(dump["locs"]), "regrids": nregrid}
@@ -259,7 +264,7 @@ def run_ml_case(name, spec):
     return {"variant": variant, "nx": nx, "nrbx": nrbx, "ng": ng, "xmin": xmin,
             "xmax": xmax, "bc": list(bcs), "regions": regs, "nblocks": mesh.nblocks,
             "levels": sorted(set(int(v) for v in mesh.levels)), "problem": problem,
-            "xorder": xorder, "rsolver": "hlld" if "hlld" in variant else "hlle",
+            "xorder": xorder, "rsolver": variant.split("_")[1],
             "cfl": cfl, "ncycle": ncycle, "gamma": gamma, "tlim": 1.0e3}
 
 
@@ -330,7 +335,7 @@ def run_case(name, spec):
     return {"variant": variant, "nx": mesh.nx, "nb": mesh.nb, "ng": mesh.ng,
             "relativistic": problem == "sr_kh",
             "xmin": mesh.xmin, "xmax": mesh.xmax, "problem": problem, "xorder": xorder,
-            "rsolver": "hlld" if "hlld" in variant else "hlle", "cfl": cfl,
+            "rsolver": variant.split("_")[1], "cfl": cfl,
             "ncycle": ncycle, "gamma": gamma, "tlim": tlim, "bc": list(BCS.get(name, (0,) * 6))}
 
 
