@@ -48,18 +48,47 @@ __global__ void join_kernel(const float* __restrict__ hi, const float* __restric
 
 long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
+}  // namespace
+
+namespace athgpu {
+// Device memory of the contexts comes from the device's stream-ordered pool, configured to
+// keep what is freed (no release threshold): a regrid allocates the new mesh's registers
+// while the old ones exist and frees the old ones after, so from the second regrid on the
+// pool serves both without a cudaMalloc/cudaFree through the driver.
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s) {
+  static int configured_device = -1;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (configured_device != dev) {
+    cudaMemPool_t pool;
+    e = cudaDeviceGetDefaultMemPool(&pool, dev);
+    if (e != cudaSuccess) return e;
+    unsigned long long thr = ~0ULL;   // cudaMemPoolAttrReleaseThreshold takes a uint64
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (e != cudaSuccess) return e;
+    configured_device = dev;
+  }
+  return cudaMallocAsync(p, bytes, s);
+}
+}  // namespace athgpu
+
+namespace {
+
 void free_all(athgpu_ctx* c) {
   Registers& r = c->r;
   void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.cce, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
-                  c->nbr, c->staging, c->c2p_queue, c->c2p_qcount};
+                  c->nbr, c->staging, c->c2p_queue, c->c2p_qcount, c->fxv, c->eps_buf};
+  // the context's device memory returns to the stream-ordered pool (pool_alloc)
+  cudaStream_t s = c->own_stream;
+  if (s) cudaStreamSynchronize(c->stream ? c->stream : s);
   for (void* p : ptrs)
-    if (p) cudaFree(p);
-  if (c->fxv) cudaFree(c->fxv);
-  if (c->eps_buf) cudaFree(c->eps_buf);
+    if (p) cudaFreeAsync(p, s);
   for (void* p : c->mld.allocs)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
+  if (s) cudaStreamSynchronize(s);
   for (cudaEvent_t e : c->prof_events) cudaEventDestroy(e);
   if (c->cycle_exec) cudaGraphExecDestroy(c->cycle_exec);
   if (c->cycle_graph) cudaGraphDestroy(c->cycle_graph);
@@ -236,8 +265,8 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   allocs.push_back({(void**)&c->c2p_queue, nb * m.nx1 * m.nx2 * m.nx3 * (i64)sizeof(int)});
   allocs.push_back({(void**)&c->c2p_qcount, (i64)sizeof(unsigned)});
   for (auto& a : allocs) {
-    e = cudaMalloc(a.p, a.bytes);
-    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
+    e = pool_alloc(a.p, a.bytes, c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync"));
     e = cudaMemsetAsync(*a.p, 0, a.bytes, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemset"));
   }
@@ -267,8 +296,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
         hc[plmoff + ((b * 3 + dd) * 2 + 0) * m.ncmax + cc] = (f[cc + 1] - xv) / df[cc];
         hc[plmoff + ((b * 3 + dd) * 2 + 1) * m.ncmax + cc] = (xv - f[cc]) / df[cc];
       }
-  e = cudaMalloc((void**)&c->coords, sizeof(double) * ncoord);
-  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc coords"));
+  e = pool_alloc((void**)&c->coords, sizeof(double) * ncoord, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync coords"));
   e = cudaMemcpy(c->coords, hc.data(), sizeof(double) * ncoord, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy coords"));
   m.dx1f = c->coords + dxoff[0];
@@ -278,8 +308,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   {  // FP32 copies: the FP32 kernels read these instead of converting on the FP64 pipe
     std::vector<float> hf(ncoord);
     for (i64 q = 0; q < ncoord; ++q) hf[q] = (float)hc[q];
-    e = cudaMalloc((void**)&c->coords32, sizeof(float) * ncoord);
-    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc coords32"));
+    e = pool_alloc((void**)&c->coords32, sizeof(float) * ncoord, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync coords32"));
     e = cudaMemcpy(c->coords32, hf.data(), sizeof(float) * ncoord, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy coords32"));
     m.dx1f32 = c->coords32 + dxoff[0];
@@ -297,8 +328,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
           const double* f = xf[dd] + b * (nc[dd] + 1);
           hv[o++] = 0.5 * (f[cc + 1] + f[cc]);
         }
-    e = cudaMalloc((void**)&c->fxv, sizeof(double) * hv.size());
-    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc fxv"));
+    e = pool_alloc((void**)&c->fxv, sizeof(double) * hv.size(), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync fxv"));
     e = cudaMemcpy(c->fxv, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy fxv"));
   }
@@ -328,8 +360,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
               none ? -1 : (a[2] * m.nbx2 + a[1]) * m.nbx1 + a[0];
         }
   }
-  e = cudaMalloc((void**)&c->nbr, sizeof(int) * hn.size());
-  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc nbr"));
+  e = pool_alloc((void**)&c->nbr, sizeof(int) * hn.size(), c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync nbr"));
   e = cudaMemcpy(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy nbr"));
   m.nbr = c->nbr;
@@ -382,10 +415,11 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
   auto dev = [&](const void* h, size_t bytes, void** out) -> cudaError_t {
     *out = nullptr;
     if (bytes == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(out, bytes);
+    cudaError_t e = pool_alloc(out, bytes, c->stream);
     if (e != cudaSuccess) return e;
     al.push_back(*out);
-    if (h) return cudaMemcpy(*out, h, bytes, cudaMemcpyHostToDevice);
+    // stream-ordered after the allocation; the host data live until the final sync
+    if (h) return cudaMemcpyAsync(*out, h, bytes, cudaMemcpyHostToDevice, c->stream);
     return cudaMemsetAsync(*out, 0, bytes, c->stream);
   };
   DevML& L = m.ml;
@@ -460,7 +494,9 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
   std::vector<int> hn((size_t)nb * 27);
   for (int b = 0; b < nb; ++b)
     for (int q = 0; q < 27; ++q) hn[(size_t)b * 27 + q] = nblevel[(size_t)b * 27 + q] < 0 ? -1 : b;
-  CK(cudaMemcpy(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   L.on = 1;
   if (c->cycle_exec) { cudaGraphExecDestroy(c->cycle_exec); c->cycle_exec = nullptr; }
   if (c->cycle_graph) { cudaGraphDestroy(c->cycle_graph); c->cycle_graph = nullptr; }

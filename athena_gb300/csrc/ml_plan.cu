@@ -10,8 +10,12 @@
 // (bvals/fc/bvals_fc.cpp:1129-1196).  A transfer copies a source box to a destination box
 // of the same shape element by element in (k, j, i) order, which is the order the
 // reference packs and unpacks its buffers.
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ml_plan.h"
@@ -455,34 +459,62 @@ void op_regions(const MlOp& op, int b, const Ix& x, std::vector<Reg>* rd, std::v
   }
 }
 
-// mark the operations after which no barrier is needed: an operation joins the current
-// run unless it writes what the run reads or writes, or reads what the run writes
+// mark the operations after which no barrier is needed.  An operation joins the current
+// run unless it writes an array of its block that the run writes or reads, or reads an
+// array of its block that the run writes (whole arrays, not boxes: a conservative test
+// that costs O(1) per operation; the per-neighbour groups of the restriction and exchange
+// lists, which write distinct arrays, form runs).
+template <typename F>
+bool for_blocks(int nb, F f);
+
 void mark_runs(MlOpList* L, const Ix& x) {
-  std::vector<Reg> rd, wr, run_rd, run_wr;
-  for (size_t q = 0; q + 1 < L->off.size(); ++q) {
+  const int nq = L->off.empty() ? 0 : (int)L->off.size() - 1;
+  for_blocks(nq, [&](int q) {
+    std::vector<Reg> rd, wr;
     const int b = L->blk[q];
-    run_rd.clear();
-    run_wr.clear();
+    unsigned run_wr = 0, run_rd = 0;
     for (int i = L->off[q]; i < L->off[q + 1]; ++i) {
       MlOp& op = L->ops[i];
       op_regions(op, b, x, &rd, &wr);
-      bool conflict = false;
-      for (const Reg& w : wr) {
-        for (const Reg& r : run_wr) conflict = conflict || overlap(w, r);
-        for (const Reg& r : run_rd) conflict = conflict || overlap(w, r);
-      }
-      for (const Reg& r : rd)
-        for (const Reg& w : run_wr) conflict = conflict || overlap(r, w);
+      unsigned w = 0, r = 0;
+      for (const Reg& g : wr) w |= 1u << g.arr;          // writes are all of block b
+      for (const Reg& g : rd)
+        if (g.blk == b) r |= 1u << g.arr;                // reads of other blocks: no hazard
+      const bool conflict = (w & (run_wr | run_rd)) || (r & run_wr);
       if (conflict && i > L->off[q]) {
         L->ops[i - 1].nosync = 0;
-        run_rd.clear();
-        run_wr.clear();
+        run_wr = run_rd = 0;
       }
-      run_rd.insert(run_rd.end(), rd.begin(), rd.end());
-      run_wr.insert(run_wr.end(), wr.begin(), wr.end());
+      run_wr |= w;
+      run_rd |= r;
       op.nosync = 1;
     }
-  }
+    return true;
+  });
+}
+
+// f(b) for every block on the host's cores (chunks of 32 blocks); false if any call
+// returned false
+template <typename F>
+bool for_blocks(int nb, F f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = std::max(1, std::min<int>(hw ? (int)hw : 1, std::min(16, nb / 64 + 1)));
+  std::atomic<int> next{0};
+  std::atomic<bool> ok{true};
+  auto work = [&]() {
+    for (;;) {
+      const int b0 = next.fetch_add(32);
+      if (b0 >= nb) return;
+      const int b1 = std::min(nb, b0 + 32);
+      for (int b = b0; b < b1; ++b)
+        if (!f(b)) ok = false;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+  return ok;
 }
 
 }  // namespace
@@ -511,32 +543,28 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
     return nblevel[(long long)b * 27 + (o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1)];
   };
   auto level = [&](int b) { return (int)loc[(long long)b * 4]; };
-  // the entry of s's list that points back at r
-  auto back = [&](int s, int r, const MlNbr& f, MlNbr* out) {
-    for (int n = 0; n < nbr_count[s]; ++n) {
-      MlNbr q = nbr(s, n);
-      if (q.gid == r && q.ox1 == -f.ox1 && q.ox2 == -f.ox2 && q.ox3 == -f.ox3) {
-        *out = q;
-        return true;
-      }
-    }
-    return false;
-  };
+  std::mutex err_mu;
   auto fail = [&](const char* what, int b) {
     char buf[160];
     snprintf(buf, sizeof buf, "multi-level plan: %s (block %d)", what, b);
-    *err = buf;
+    std::lock_guard<std::mutex> lk(err_mu);
+    if (err->empty()) *err = buf;
     return false;
   };
+  err->clear();
   P->level.resize(nb);
   for (int b = 0; b < nb; ++b) {
     P->level[b] = level(b);
     if (nbr_count[b] < 0 || nbr_count[b] > ML_MAXNB) return fail("bad neighbour count", b);
+    for (int n = 0; n < nbr_count[b]; ++n)
+      if (nbr(b, n).gid < 0 || nbr(b, n).gid >= nb)
+        return fail("neighbour gid out of range", b);
   }
   // ---- phase R: restriction for coarser neighbours (into the send and coarse buffers) --
   P->r.clear(); P->x.clear(); P->p.clear();
-  for (int s = 0; s < nb; ++s) {
-    std::vector<MlOp> ops;
+  std::vector<std::vector<MlOp>> per(nb);
+  for_blocks(nb, [&](int s) {
+    std::vector<MlOp>& ops = per[s];
     for (int n = 0; n < nbr_count[s]; ++n) {
       MlNbr q = nbr(s, n);
       if (q.level >= level(s)) continue;
@@ -549,18 +577,52 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
         ops.push_back(ob);
       }
     }
-    if (!ops.empty()) P->r.add(s, ops);
+    return true;
+  });
+  {
+    size_t tot = 0;
+    for (const auto& v : per) tot += v.size();
+    P->r.ops.reserve(tot);
+    P->r.off.reserve(nb + 1);
+    P->r.blk.reserve(nb);
   }
+  for (int s = 0; s < nb; ++s)
+    if (!per[s].empty()) P->r.add(s, per[s]);
   // ---- phase X: the ghost exchange, per receiver in neighbour-list order; all U copies
   // first (SETB_HYD), then all face-field copies (SETB_FLD)
-  for (int r = 0; r < nb; ++r) {
+  // the entry of each block's list by (neighbour gid, offset), sorted, for the lookups of
+  // the sender's entry that points back at the receiver
+  std::vector<std::vector<std::pair<long long, int>>> keys(nb);
+  auto key = [](long long gid, int o1, int o2, int o3) {
+    return (gid << 5) | (long long)((o3 + 1) * 9 + (o2 + 1) * 3 + (o1 + 1));
+  };
+  for_blocks(nb, [&](int s) {
+    auto& k = keys[s];
+    k.reserve(nbr_count[s]);
+    for (int n = 0; n < nbr_count[s]; ++n) {
+      const MlNbr q = nbr(s, n);
+      k.push_back({key(q.gid, q.ox1, q.ox2, q.ox3), n});
+    }
+    std::sort(k.begin(), k.end());
+    return true;
+  });
+  auto back_fast = [&](int s, int r, const MlNbr& f, MlNbr* out) {
+    const auto& k = keys[s];
+    const long long want = key(r, -f.ox1, -f.ox2, -f.ox3);
+    auto it = std::lower_bound(k.begin(), k.end(), std::make_pair(want, -1));
+    if (it == k.end() || it->first != want) return false;
+    *out = nbr(s, it->second);
+    return true;
+  };
+  for (auto& v : per) v.clear();
+  const bool xok = for_blocks(nb, [&](int r) {
     std::vector<MlOp> ucopies, bcopies;
     const int par[3] = {(int)(loc[(long long)r * 4 + 1] & 1), (int)(loc[(long long)r * 4 + 2] & 1),
                         (int)(loc[(long long)r * 4 + 3] & 1)};
     for (int n = 0; n < nbr_count[r]; ++n) {
       MlNbr q = nbr(r, n), qs;
       const int s = q.gid;
-      if (!back(s, r, q, &qs)) return fail("inconsistent neighbour lists", r);
+      if (!back_fast(s, r, q, &qs)) return fail("inconsistent neighbour lists", r);
       Box du, su;
       int ud, us;
       if (q.level == level(r)) {
@@ -589,15 +651,27 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
         bcopies.push_back(ob);
       }
     }
-    std::vector<MlOp> all = ucopies;
+    std::vector<MlOp>& all = per[r];
+    all = ucopies;
     all.insert(all.end(), bcopies.begin(), bcopies.end());
-    if (!all.empty()) P->x.add(r, all);
+    return true;
+  });
+  if (!xok) return false;
+  {
+    size_t tot = 0;
+    for (const auto& v : per) tot += v.size();
+    P->x.ops.reserve(tot);
+    P->x.off.reserve(nb + 1);
+    P->x.blk.reserve(nb);
   }
+  for (int r = 0; r < nb; ++r)
+    if (!per[r].empty()) P->x.add(r, per[r]);
   // ---- phase P: ProlongateBoundaries per block with coarser neighbours ------------------
   const int cn = x.cng - 1;
-  for (int b = 0; b < nb; ++b) {
+  for (auto& v : per) v.clear();
+  for_blocks(nb, [&](int b) {
     const int lev = level(b);
-    std::vector<MlOp> ops;
+    std::vector<MlOp>& ops = per[b];
     for (int n = 0; n < nbr_count[b]; ++n) {
       MlNbr q = nbr(b, n);
       if (q.level >= lev) continue;
@@ -705,8 +779,17 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
       }
       ops.push_back(make_op(ML_FINE_P2C, 0, fb));
     }
-    if (!ops.empty()) P->p.add(b, ops);
+    return true;
+  });
+  {
+    size_t tot = 0;
+    for (const auto& v : per) tot += v.size();
+    P->p.ops.reserve(tot);
+    P->p.off.reserve(nb + 1);
+    P->p.blk.reserve(nb);
   }
+  for (int b = 0; b < nb; ++b)
+    if (!per[b].empty()) P->p.add(b, per[b]);
   // ---- flux correction tasks: (coarse block, finer block, face | fi1 << 4 | fi2 << 5) --
   P->flux_tasks.clear();
   P->fmask.assign(nb, 0);
@@ -725,17 +808,24 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
       B.ncc[a] = dims.nx[a] / 2 + 2 * ng;
     }
     const MlOpList* lists[3] = {&P->r, &P->x, &P->p};
-    for (const MlOpList* L : lists)
-      for (size_t q = 0; q < L->ops.size(); ++q)
-        if (!check_op(L->ops[q], x, B)) {
-          char buf[200];
-          const MlOp& o = L->ops[q];
-          snprintf(buf, sizeof buf,
-                   "multi-level plan: operation %d (d %d) box [%d..%d, %d..%d, %d..%d] out of bounds",
-                   o.code, o.d, o.s[0], o.e[0], o.s[1], o.e[1], o.s[2], o.e[2]);
-          *err = buf;
-          return false;
-        }
+    for (const MlOpList* L : lists) {
+      const int nq = L->off.empty() ? 0 : (int)L->off.size() - 1;
+      const bool ok = for_blocks(nq, [&](int q) {
+        for (int i = L->off[q]; i < L->off[q + 1]; ++i)
+          if (!check_op(L->ops[i], x, B)) {
+            char buf[200];
+            const MlOp& o = L->ops[i];
+            snprintf(buf, sizeof buf,
+                     "multi-level plan: operation %d (d %d) box [%d..%d, %d..%d, %d..%d] out "
+                     "of bounds", o.code, o.d, o.s[0], o.e[0], o.s[1], o.e[1], o.s[2], o.e[2]);
+            std::lock_guard<std::mutex> lk(err_mu);
+            if (err->empty()) *err = buf;
+            return false;
+          }
+        return true;
+      });
+      if (!ok) return false;
+    }
     mark_runs(&P->r, x);
     mark_runs(&P->x, x);
     mark_runs(&P->p, x);
@@ -744,12 +834,6 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
         *err = "multi-level plan: flux task block out of range";
         return false;
       }
-    for (int b = 0; b < nb; ++b)
-      for (int n = 0; n < nbr_count[b]; ++n)
-        if (nbr(b, n).gid < 0 || nbr(b, n).gid >= nb) {
-          *err = "multi-level plan: neighbour gid out of range";
-          return false;
-        }
   }
   // ---- CountFineEdges ---------------------------------------------------------------
   P->eflag.assign((size_t)nb * 12, 0);

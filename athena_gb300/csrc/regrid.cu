@@ -22,6 +22,7 @@
 // The arithmetic of steps 1 and 3 is the executor's (FP64, the reference's operand order),
 // so the FP64 path stays bit-identical to the reference.
 #include <cfloat>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <utility>
@@ -33,10 +34,18 @@
 
 namespace athgpu {
 athgpu_status api_fail(athgpu_status code, const std::string& msg);
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
 }
 
 namespace {
 using namespace athgpu;
+
+// host wall time of the phases of the last regrid (athgpu_regrid_profile)
+double g_phase_ms[8];
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(
+             std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 // ---- refinement measure ---------------------------------------------------------------
 // pgen/blast.cpp:413-443: per block the maximum over the interior and one ghost layer of
@@ -207,7 +216,7 @@ athgpu_status athgpu_refinement_eps(athgpu_ctx* c, double* maxeps) {
   if (!c->initialized) return api_fail(ATHGPU_ERR_STATE, "athgpu_initialize not called");
   const DevMesh& m = c->m;
   cudaError_t e = cudaSuccess;
-  if (!c->eps_buf) e = cudaMalloc((void**)&c->eps_buf, sizeof(double) * (size_t)m.nb);
+  if (!c->eps_buf) e = pool_alloc((void**)&c->eps_buf, sizeof(double) * (size_t)m.nb, c->stream);
   if (e != cudaSuccess) return api_fail(ATHGPU_ERR_CUDA, cudaGetErrorString(e));
   const void* w = c->r.wbuf[c->r.wsel];
   if (c->real_bytes == 8)
@@ -279,13 +288,22 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
 
   // the new context: registers, coordinates and the multi-level plan
   athgpu_ctx* nc = nullptr;
+  double tp = now_ms();
+  for (int q = 0; q < 8; ++q) g_phase_ms[q] = 0.0;
+  auto phase = [&](int q) {
+    const double t = now_ms();
+    g_phase_ms[q] += t - tp;
+    tp = t;
+  };
   athgpu_status st = athgpu_create(&nc, desc);
+  phase(0);
   if (st != ATHGPU_OK) return st;
   st = athgpu_set_multilevel(nc, nbr_table, nbr_count, nblevel, loc, cx1f, cdx1f, cx2f, cdx2f,
                              cx3f, cdx3f);
   if (st != ATHGPU_OK) { athgpu_destroy(nc); return st; }
   cudaError_t e = cudaStreamSynchronize(nc->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  phase(1);
   nc->lc = c->lc;
   const DevMesh& nm = nc->m;
   const int rb = c->real_bytes;
@@ -320,6 +338,7 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     if (e != cudaSuccess) return fail_cleanup(e, "regrid restriction");
   }
 
+  phase(2);
   // 2. box copies old -> new
   std::vector<RgCopy> tasks;
   bool boxes_ok = true;
@@ -455,6 +474,7 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     if (e != cudaSuccess) return fail_cleanup(e, "regrid clock");
   }
 
+  phase(3);
   // 3. new mesh: ProlongateMeshBlock of every new child
   {
     MlOpList L;
@@ -481,6 +501,7 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     if (e != cudaSuccess) return fail_cleanup(e, "regrid prolongation");
   }
 
+  phase(4);
   // the new context takes the old one's place behind the caller's handle
   const bool user_stream = c->stream != c->own_stream;
   cudaStream_t us = c->stream;
@@ -490,8 +511,17 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
   c->launches = launches;
   if (user_stream) c->stream = us;
 
+  phase(5);
   // 4. Initialize(2)
-  return athgpu_initialize(c);
+  st = athgpu_initialize(c);
+  phase(6);
+  return st;
+}
+
+athgpu_status athgpu_regrid_profile(double* ms) {
+  if (!ms) return api_fail(ATHGPU_ERR_ARG, "null argument");
+  for (int q = 0; q < 8; ++q) ms[q] = g_phase_ms[q];
+  return ATHGPU_OK;
 }
 
 namespace athgpu {

@@ -113,6 +113,7 @@ def load_library(path=LIB_PATH):
                           [ctypes.POINTER(ip), ctypes.POINTER(ip), ip, ctypes.POINTER(ip),
                            ip], ip),
         "athgpu_new_time_step": ([vp], ip),
+        "athgpu_regrid_profile": ([dp], ip),
         "athgpu_amr_create": ([ctypes.POINTER(vp), ctypes.POINTER(ip), ctypes.POINTER(ip), ip,
                                dp, dp, ctypes.POINTER(ip), ip, ip], ip),
         "athgpu_amr_destroy": ([vp], ip),

@@ -428,7 +428,7 @@ def run_sr_kh(n, stream, net):
     return out
 
 
-AMR_ROOT = 128        # root grid cells per direction (8^3 MeshBlocks of 16^3)
+AMR_ROOT = 160        # root grid cells per direction (10^3 MeshBlocks of 16^3)
 AMR_THR = 0.3        # pressure-gradient threshold of the blast refinement condition
 AMR_WARM = {"fp32": (5, 30), "fp64": (3, 10)}   # warm-up and timed cycles
 AMR_ACC_CYCLES = 12
