@@ -459,11 +459,10 @@ void op_regions(const MlOp& op, int b, const Ix& x, std::vector<Reg>* rd, std::v
   }
 }
 
-// mark the operations after which no barrier is needed.  An operation joins the current
-// run unless it writes an array of its block that the run writes or reads, or reads an
-// array of its block that the run writes (whole arrays, not boxes: a conservative test
-// that costs O(1) per operation; the per-neighbour groups of the restriction and exchange
-// lists, which write distinct arrays, form runs).
+// mark the operations after which no barrier is needed: an operation joins the current
+// run unless it writes a box of its block's arrays that the run writes or reads, or reads
+// one that the run writes.  Boxes are compared only within the same array of the block
+// (reads of other blocks cannot conflict: a list writes its own block's arrays only).
 template <typename F>
 bool for_blocks(int nb, F f);
 
@@ -471,22 +470,29 @@ void mark_runs(MlOpList* L, const Ix& x) {
   const int nq = L->off.empty() ? 0 : (int)L->off.size() - 1;
   for_blocks(nq, [&](int q) {
     std::vector<Reg> rd, wr;
+    std::vector<Reg> run_w[RA_SB3 + 1], run_r[RA_SB3 + 1];
+    unsigned used = 0;
     const int b = L->blk[q];
-    unsigned run_wr = 0, run_rd = 0;
     for (int i = L->off[q]; i < L->off[q + 1]; ++i) {
       MlOp& op = L->ops[i];
       op_regions(op, b, x, &rd, &wr);
-      unsigned w = 0, r = 0;
-      for (const Reg& g : wr) w |= 1u << g.arr;          // writes are all of block b
-      for (const Reg& g : rd)
-        if (g.blk == b) r |= 1u << g.arr;                // reads of other blocks: no hazard
-      const bool conflict = (w & (run_wr | run_rd)) || (r & run_wr);
+      bool conflict = false;
+      for (const Reg& w : wr) {
+        for (const Reg& g : run_w[w.arr]) conflict = conflict || overlap(w, g);
+        for (const Reg& g : run_r[w.arr]) conflict = conflict || overlap(w, g);
+      }
+      for (const Reg& r : rd)
+        if (r.blk == b)
+          for (const Reg& g : run_w[r.arr]) conflict = conflict || overlap(r, g);
       if (conflict && i > L->off[q]) {
         L->ops[i - 1].nosync = 0;
-        run_wr = run_rd = 0;
+        for (int a = 0; a <= RA_SB3; ++a)
+          if (used & (1u << a)) { run_w[a].clear(); run_r[a].clear(); }
+        used = 0;
       }
-      run_wr |= w;
-      run_rd |= r;
+      for (const Reg& w : wr) { run_w[w.arr].push_back(w); used |= 1u << w.arr; }
+      for (const Reg& r : rd)
+        if (r.blk == b) { run_r[r.arr].push_back(r); used |= 1u << r.arr; }
       op.nosync = 1;
     }
     return true;
