@@ -1,5 +1,5 @@
 // History output of the MHD state (HistoryOutput::WriteOutputFile, outputs/history.cpp:
-// 77-140 for the quantities this build evolves): volume-weighted sums over the interior
+// 77-140 for the quantities the path evolves): volume-weighted sums over the interior
 // cells of all MeshBlocks of
 //   mass, 1-mom, 2-mom, 3-mom, 1-KE, 2-KE, 3-KE, tot-E, 1-ME, 2-ME, 3-ME
 // with vol = dx1f(i) dx2f(j) dx3f(k) (coordinates.cpp:536-545), KE_d = 0.5 M_d^2 / D and

@@ -349,7 +349,7 @@ SR_ACC_CYCLES = 5
 
 
 def run_sr_kh(n, stream, net):
-    """Relativistic Kelvin-Helmholtz shear layer (SURVEY config 5 workload): n^3 periodic
+    """Relativistic Kelvin-Helmholtz shear layer (the full SR step workload): n^3 periodic
     box as (n/32)^3 MeshBlocks, gamma 4/3, v_x = +-0.5c with tanh width 0.01, rho 1 / 0.1,
     p = 1, uniform B_x with sigma 0.1, seeded 1e-3 velocity noise, VL2 + PLM + HLLE.
     Zone-cycles/s of the FP32 and FP64 SR stage paths (CUDA events, state resident), their
