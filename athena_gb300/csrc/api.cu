@@ -159,7 +159,8 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
                                 "(reconstruction.cpp:117-127)");
   if (d->nx1 < d->nghost || d->nx2 < d->nghost || d->nx3 < d->nghost)
     return fail(ATHGPU_ERR_ARG, "MeshBlock smaller than the ghost width");
-  if (d->rsolver != ATHGPU_HLLD && d->rsolver != ATHGPU_HLLE && d->rsolver != ATHGPU_LLF)
+  if (d->rsolver != ATHGPU_HLLD && d->rsolver != ATHGPU_HLLE && d->rsolver != ATHGPU_LLF &&
+      d->rsolver != ATHGPU_ROE)
     return fail(ATHGPU_ERR_ARG, "unknown Riemann solver");
   if (d->precision != ATHGPU_FP64 && d->precision != ATHGPU_FP32)
     return fail(ATHGPU_ERR_ARG, "unknown precision");

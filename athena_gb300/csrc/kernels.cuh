@@ -256,6 +256,7 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
   else if (RS == 1) hlle<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
+  else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);
   else hlle_sr<Real>(gam, wli, wri, bx, f);  // RS 2: special relativity
   fn[IDN] = f[0];
   fn[ivx] = f[1];

@@ -594,6 +594,7 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const Real* __restri
   const Real bx = to_real(__ldg(bn + fo), Real());
   if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
+  else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);
   else hlle<Real>(gam, wli, wri, bx, f);
   fn[IDN] = f[0];
   fn[ivx] = f[1];

@@ -208,8 +208,10 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   const double* bb3 = (stage == 1) ? r.b3 : r.bs3;
   const Real* w = (const Real*)r.wbuf[r.wsel];
   const Real* bcc = (const Real*)r.bcc;
-  // solver template index: 0 HLLD, 1 HLLE, 2 relativistic HLLE, 3 LLF
-  const int rs = c->desc.relativistic ? 2 : c->desc.rsolver == ATHGPU_LLF ? 3 : c->desc.rsolver;
+  // solver template index: 0 HLLD, 1 HLLE, 2 relativistic HLLE, 3 LLF, 4 Roe
+  const int rs = c->desc.relativistic ? 2
+                 : c->desc.rsolver == ATHGPU_LLF ? 3
+                 : c->desc.rsolver == ATHGPU_ROE ? 4 : c->desc.rsolver;
   Real* uout = (stage == 1) ? (Real*)r.ustar : (Real*)r.u;
   UpdateArgs ua;
   ua.beta = beta;
@@ -218,16 +220,15 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   ua.uout = uout;
   ua.ulo = r.ulo;
 #define FLUX(O, R) launch_fluxes<Real, O, R, KAHAN>(c, w, bcc, bb1, bb2, bb3, ua)
-  if (order == 1) {
-    if (rs == 0) FLUX(1, 0); else if (rs == 1) FLUX(1, 1); else if (rs == 3) FLUX(1, 3);
-    else FLUX(1, 2);
-  } else if (order == 2) {
-    if (rs == 0) FLUX(2, 0); else if (rs == 1) FLUX(2, 1); else if (rs == 3) FLUX(2, 3);
-    else FLUX(2, 2);
-  } else {
-    if (rs == 0) FLUX(3, 0); else if (rs == 1) FLUX(3, 1); else if (rs == 3) FLUX(3, 3);
-    else FLUX(3, 2);
-  }
+#define FLUX_RS(O)                                                                   \
+  do {                                                                               \
+    if (rs == 0) FLUX(O, 0); else if (rs == 1) FLUX(O, 1); else if (rs == 3) FLUX(O, 3); \
+    else if (rs == 4) FLUX(O, 4); else FLUX(O, 2);                                   \
+  } while (0)
+  if (order == 1) FLUX_RS(1);
+  else if (order == 2) FLUX_RS(2);
+  else FLUX_RS(3);
+#undef FLUX_RS
 #undef FLUX
   {
     const long long n = (long long)m.nb * (m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);

@@ -19,8 +19,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libathgpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300.h")
 
-HLLD, HLLE, LLF = 0, 1, 2
-_RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF}
+HLLD, HLLE, LLF, ROE = 0, 1, 2, 3
+_RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF, "roe": ROE}
 FP64, FP32 = 0, 1
 
 

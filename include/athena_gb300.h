@@ -35,6 +35,7 @@ typedef int athgpu_status;
 #define ATHGPU_HLLD 0            /* --flux=hlld  (hydro/rsolvers/mhd/hlld.cpp) */
 #define ATHGPU_HLLE 1            /* --flux=hlle  (hydro/rsolvers/mhd/hlle_mhd.cpp) */
 #define ATHGPU_LLF 2             /* --flux=llf   (hydro/rsolvers/mhd/llf_mhd.cpp) */
+#define ATHGPU_ROE 3             /* --flux=roe   (hydro/rsolvers/mhd/roe_mhd.cpp) */
 #define ATHGPU_FP64 0            /* every operation in FP64: bit-identical to the reference */
 #define ATHGPU_FP32 1            /* FP32 reconstruction/Riemann/divergence, compensated
                                     (Kahan) conserved update, FP64 CT and time step */
@@ -50,7 +51,7 @@ typedef struct {
   int nx1, nx2, nx3;      /* interior cells per MeshBlock (meshblock/nx1..3) */
   int nghost;             /* NGHOST: 2 for PLM, >= 3 for PPM (reconstruction.cpp:117-127) */
   int xorder;             /* time/xorder: 2 = PLM, 3 = PPM (stage 1 is donor cell) */
-  int rsolver;            /* ATHGPU_HLLD, ATHGPU_HLLE or ATHGPU_LLF */
+  int rsolver;            /* ATHGPU_HLLD, ATHGPU_HLLE, ATHGPU_LLF or ATHGPU_ROE */
   int precision;          /* ATHGPU_FP64 or ATHGPU_FP32 */
   int relativistic;       /* 1: special-relativistic MHD (-s): HLLE solver only, FP64
                              Newman-Hamlin con2prim (adiabatic_mhd_sr.cpp) */

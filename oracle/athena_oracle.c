@@ -453,6 +453,244 @@ static void llf(double gamma, const double *wli, const double *wri, double bxi,
   for (int n = 0; n < NWAVE; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) - a * du[n];
 }
 
+/* Roe's linearised solver for adiabatic MHD, hydro/rsolvers/mhd/roe_mhd.cpp:45-221 (the
+ * driver) and :223-460 (RoeFlux: the eigensystem of Stone et al. 2008, ApJS 178, 137,
+ * appendix B, eqs. B17-B29).  The sums over waves follow the reference's order term by
+ * term, which fixes the rounding.  Upwind fluxes replace the Roe flux outside the fan; the
+ * LLF flux replaces the hydro components (not the field ones) when an intermediate density
+ * of the fan is negative. */
+static void roe(double gamma, const double *wli, const double *wri, double bxi,
+                double *flxi) {
+  const double gm1 = gamma - 1.0;
+  double fl[NWAVE], fr[NWAVE], du[NWAVE], ev[NWAVE], a[NWAVE], cf_[NWAVE];
+  /* Roe averages (density-weighted velocity, inverse-weighted transverse field, enthalpy) */
+  double sl = sqrt(wli[IDN]), sr = sqrt(wri[IDN]);
+  double isum = 1.0 / (sl + sr);
+  double d = sl * sr;
+  double v1 = (sl * wli[IVX] + sr * wri[IVX]) * isum;
+  double v2 = (sl * wli[IVY] + sr * wri[IVY]) * isum;
+  double v3 = (sl * wli[IVZ] + sr * wri[IVZ]) * isum;
+  double b2 = (sr * wli[IBY] + sl * wri[IBY]) * isum;
+  double b3 = (sr * wli[IBZ] + sl * wri[IBZ]) * isum;
+  double x = 0.5 * (SQR(wli[IBY] - wri[IBY]) + SQR(wli[IBZ] - wri[IBZ])) / SQR(sl + sr);
+  double y = 0.5 * (wli[IDN] + wri[IDN]) / d;
+  double pbl = 0.5 * (bxi * bxi + SQR(wli[IBY]) + SQR(wli[IBZ]));
+  double pbr = 0.5 * (bxi * bxi + SQR(wri[IBY]) + SQR(wri[IBZ]));
+  double el = wli[IPR] / gm1 +
+              0.5 * wli[IDN] * (SQR(wli[IVX]) + SQR(wli[IVY]) + SQR(wli[IVZ])) + pbl;
+  double er = wri[IPR] / gm1 +
+              0.5 * wri[IDN] * (SQR(wri[IVX]) + SQR(wri[IVY]) + SQR(wri[IVZ])) + pbr;
+  double h = ((el + wli[IPR] + pbl) / sl + (er + wri[IPR] + pbr) / sr) * isum;
+  /* left and right physical fluxes */
+  double mxl = wli[IDN] * wli[IVX], mxr = wri[IDN] * wri[IVX];
+  fl[IDN] = mxl;
+  fr[IDN] = mxr;
+  fl[IVX] = mxl * wli[IVX] + pbl - SQR(bxi);
+  fr[IVX] = mxr * wri[IVX] + pbr - SQR(bxi);
+  fl[IVY] = mxl * wli[IVY] - bxi * wli[IBY];
+  fr[IVY] = mxr * wri[IVY] - bxi * wri[IBY];
+  fl[IVZ] = mxl * wli[IVZ] - bxi * wli[IBZ];
+  fr[IVZ] = mxr * wri[IVZ] - bxi * wri[IBZ];
+  fl[IVX] += wli[IPR];
+  fr[IVX] += wri[IPR];
+  fl[IPR] = (el + wli[IPR] + pbl - bxi * bxi) * wli[IVX];
+  fr[IPR] = (er + wri[IPR] + pbr - bxi * bxi) * wri[IVX];
+  fl[IPR] -= bxi * (wli[IBY] * wli[IVY] + wli[IBZ] * wli[IVZ]);
+  fr[IPR] -= bxi * (wri[IBY] * wri[IVY] + wri[IBZ] * wri[IVZ]);
+  fl[IBY] = wli[IBY] * wli[IVX] - bxi * wli[IVY];
+  fr[IBY] = wri[IBY] * wri[IVX] - bxi * wri[IVY];
+  fl[IBZ] = wli[IBZ] * wli[IVX] - bxi * wli[IVZ];
+  fr[IBZ] = wri[IBZ] * wri[IVX] - bxi * wri[IVZ];
+  /* jump in the conserved variables */
+  du[IDN] = wri[IDN] - wli[IDN];
+  du[IVX] = wri[IDN] * wri[IVX] - wli[IDN] * wli[IVX];
+  du[IVY] = wri[IDN] * wri[IVY] - wli[IDN] * wli[IVY];
+  du[IVZ] = wri[IDN] * wri[IVZ] - wli[IDN] * wli[IVZ];
+  du[IPR] = er - el;
+  du[IBY] = wri[IBY] - wli[IBY];
+  du[IBZ] = wri[IBZ] - wli[IBZ];
+  for (int n = 0; n < NWAVE; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]);
+
+  /* wave speeds of the Roe matrix (eq. B17-B18) */
+  double di = 1.0 / d;
+  double btsq = b2 * b2 + b3 * b3;
+  double vaxsq = bxi * bxi * di;
+  double vsq = v1 * v1 + v2 * v2 + v3 * v3;
+  double hp = h - (vaxsq + btsq * di);
+  double ystar = gm1 - (gm1 - 1.0) * y;
+  double bt_starsq = ystar * btsq;
+  double csq = smax((gm1 * (hp - 0.5 * vsq) - (gm1 - 1.0) * x), 1.0e-20);
+  double ct2 = bt_starsq * di;
+  double tsum = vaxsq + ct2 + csq;
+  double tdif = vaxsq + ct2 - csq;
+  double root = sqrt(tdif * tdif + 4.0 * csq * ct2);
+  double cfsq = 0.5 * (tsum + root);
+  double cf = sqrt(cfsq);
+  double cssq = csq * vaxsq / cfsq;
+  double cs = sqrt(cssq);
+  /* transverse-field directions (eq. A17, B20, B28) */
+  double bt = sqrt(btsq), bt_star = sqrt(bt_starsq);
+  double be2 = 0.0, be3 = 0.0;
+  if (bt != 0.0) {
+    be2 = b2 / bt;
+    be3 = b3 / bt;
+  }
+  double be2s = be2 / sqrt(ystar);
+  double be3s = be3 / sqrt(ystar);
+  double bes_sq = be2s * be2s + be3s * be3s;
+  double vbet = v2 * be2s + v3 * be3s;
+  double q2s = 0.0, q3s = 0.0;
+  if (bes_sq != 0.0) {
+    q2s = be2s / bes_sq;
+    q3s = be3s / bes_sq;
+  }
+  /* fast/slow normalisations (eq. A16), with their degenerate limits */
+  double af_, as_;
+  if ((cfsq - cssq) <= 0.0) { af_ = 1.0; as_ = 0.0; }
+  else if ((csq - cssq) <= 0.0) { af_ = 0.0; as_ = 1.0; }
+  else if ((cfsq - csq) <= 0.0) { af_ = 1.0; as_ = 0.0; }
+  else {
+    af_ = sqrt((csq - cssq) / (cfsq - cssq));
+    as_ = sqrt((cfsq - csq) / (cfsq - cssq));
+  }
+  double sqd = sqrt(d), isqd = 1.0 / sqd;
+  double sgn = (bxi < 0.0) ? -1.0 : 1.0;
+  double c = sqrt(csq);
+  double qf = cf * af_ * sgn, qs = cs * as_ * sgn;
+  double afp = c * af_ * isqd, asp = c * as_ * isqd;
+  double afpbb = afp * bt_star * bes_sq, aspbb = asp * bt_star * bes_sq;
+  double vq = (v2 * q2s + v3 * q3s);
+  double vax = sqrt(vaxsq);
+  double nrm = 0.5 / csq;
+  double cff = nrm * af_ * cf, css = nrm * as_ * cs;
+  double qfh = qf * nrm, qsh = qs * nrm;
+  double afd = nrm * afp * d, asd = nrm * asp * d;
+  double afpb = nrm * afp * bt_star, aspb = nrm * asp * bt_star;
+  ev[0] = v1 - cf;
+  ev[1] = v1 - vax;
+  ev[2] = v1 - cs;
+  ev[3] = v1;
+  ev[4] = v1 + cs;
+  ev[5] = v1 + vax;
+  ev[6] = v1 + cf;
+  /* projection of du on the left eigenvectors (eq. B29), term by term */
+  double afb = af_ * gm1 * nrm, asb = as_ * gm1 * nrm;
+  double gm1a = gm1 / csq;
+  a[0] = du[0] * (afb * (vsq - hp) + cff * (cf + v1) - qsh * vq - aspb);
+  a[0] -= du[1] * (afb * v1 + cff);
+  a[0] -= du[2] * (afb * v2 - qsh * q2s);
+  a[0] -= du[3] * (afb * v3 - qsh * q3s);
+  a[0] += du[4] * afb;
+  a[0] += du[5] * (asd * q2s - afb * b2);
+  a[0] += du[6] * (asd * q3s - afb * b3);
+  a[1] = du[0] * (v2 * be3 - v3 * be2);
+  a[1] -= du[2] * be3;
+  a[1] += du[3] * be2;
+  a[1] -= du[5] * sqd * be3 * sgn;
+  a[1] += du[6] * sqd * be2 * sgn;
+  a[1] *= 0.5;
+  a[2] = du[0] * (asb * (vsq - hp) + css * (cs + v1) + qfh * vq + afpb);
+  a[2] -= du[1] * (asb * v1 + css);
+  a[2] -= du[2] * (asb * v2 + qfh * q2s);
+  a[2] -= du[3] * (asb * v3 + qfh * q3s);
+  a[2] += du[4] * asb;
+  a[2] -= du[5] * (afd * q2s + asb * b2);
+  a[2] -= du[6] * (afd * q3s + asb * b3);
+  a[3] = du[0] * (1.0 - gm1a * (0.5 * vsq - (gm1 - 1.0) * x / gm1));
+  a[3] += du[1] * gm1a * v1;
+  a[3] += du[2] * gm1a * v2;
+  a[3] += du[3] * gm1a * v3;
+  a[3] -= du[4] * gm1a;
+  a[3] += du[5] * gm1a * b2;
+  a[3] += du[6] * gm1a * b3;
+  a[4] = du[0] * (asb * (vsq - hp) + css * (cs - v1) - qfh * vq + afpb);
+  a[4] -= du[1] * (asb * v1 - css);
+  a[4] -= du[2] * (asb * v2 - qfh * q2s);
+  a[4] -= du[3] * (asb * v3 - qfh * q3s);
+  a[4] += du[4] * asb;
+  a[4] -= du[5] * (afd * q2s + asb * b2);
+  a[4] -= du[6] * (afd * q3s + asb * b3);
+  a[5] = du[0] * (v3 * be2 - v2 * be3);
+  a[5] += du[2] * be3;
+  a[5] -= du[3] * be2;
+  a[5] -= du[5] * sqd * be3 * sgn;
+  a[5] += du[6] * sqd * be2 * sgn;
+  a[5] *= 0.5;
+  a[6] = du[0] * (afb * (vsq - hp) + cff * (cf - v1) + qsh * vq - aspb);
+  a[6] -= du[1] * (afb * v1 - cff);
+  a[6] -= du[2] * (afb * v2 + qsh * q2s);
+  a[6] -= du[3] * (afb * v3 + qsh * q3s);
+  a[6] += du[4] * afb;
+  a[6] += du[5] * (asd * q2s - afb * b2);
+  a[6] += du[6] * (asd * q3s - afb * b3);
+  for (int n = 0; n < NWAVE; ++n) cf_[n] = -0.5 * fabs(ev[n]) * a[n];
+  /* density of the intermediate states left to right (first row of the right
+   * eigenvectors): a negative one selects the LLF flux below */
+  int neg = 0;
+  double dens = wli[IDN] + a[0] * af_;
+  neg |= dens < 0.0;
+  dens += a[2] * as_;
+  neg |= dens < 0.0;
+  dens += a[3];
+  neg |= dens < 0.0;
+  dens += a[4] * as_;
+  neg |= dens < 0.0;
+  /* dissipation: sum of the waves times the right eigenvectors (eq. B21) */
+  flxi[0] += cf_[0] * af_;
+  flxi[0] += cf_[2] * as_;
+  flxi[0] += cf_[3];
+  flxi[0] += cf_[4] * as_;
+  flxi[0] += cf_[6] * af_;
+  flxi[1] += cf_[0] * (af_ * (v1 - cf));
+  flxi[1] += cf_[2] * (as_ * (v1 - cs));
+  flxi[1] += cf_[3] * v1;
+  flxi[1] += cf_[4] * (as_ * (v1 + cs));
+  flxi[1] += cf_[6] * (af_ * (v1 + cf));
+  flxi[2] += cf_[0] * (af_ * v2 + qs * be2s);
+  flxi[2] -= cf_[1] * be3;
+  flxi[2] += cf_[2] * (as_ * v2 - qf * be2s);
+  flxi[2] += cf_[3] * v2;
+  flxi[2] += cf_[4] * (as_ * v2 + qf * be2s);
+  flxi[2] += cf_[5] * be3;
+  flxi[2] += cf_[6] * (af_ * v2 - qs * be2s);
+  flxi[3] += cf_[0] * (af_ * v3 + qs * be3s);
+  flxi[3] += cf_[1] * be2;
+  flxi[3] += cf_[2] * (as_ * v3 - qf * be3s);
+  flxi[3] += cf_[3] * v3;
+  flxi[3] += cf_[4] * (as_ * v3 + qf * be3s);
+  flxi[3] -= cf_[5] * be2;
+  flxi[3] += cf_[6] * (af_ * v3 - qs * be3s);
+  flxi[4] += cf_[0] * (af_ * (hp - v1 * cf) + qs * vbet + aspbb);
+  flxi[4] -= cf_[1] * (v2 * be3 - v3 * be2);
+  flxi[4] += cf_[2] * (as_ * (hp - v1 * cs) - qf * vbet - afpbb);
+  flxi[4] += cf_[3] * (0.5 * vsq + (gm1 - 1.0) * x / gm1);
+  flxi[4] += cf_[4] * (as_ * (hp + v1 * cs) + qf * vbet - afpbb);
+  flxi[4] += cf_[5] * (v1 * be3 - v3 * be2);
+  flxi[4] += cf_[6] * (af_ * (hp + v1 * cf) - qs * vbet + aspbb);
+  flxi[5] += cf_[0] * asp * be2s;
+  flxi[5] -= cf_[1] * be3 * sgn * isqd;
+  flxi[5] -= cf_[2] * afp * be2s;
+  flxi[5] -= cf_[4] * afp * be2s;
+  flxi[5] -= cf_[5] * be3 * sgn * isqd;
+  flxi[5] += cf_[6] * asp * be2s;
+  flxi[6] += cf_[0] * asp * be3s;
+  flxi[6] += cf_[1] * be2 * sgn * isqd;
+  flxi[6] -= cf_[2] * afp * be3s;
+  flxi[6] -= cf_[4] * afp * be3s;
+  flxi[6] += cf_[5] * be2 * sgn * isqd;
+  flxi[6] += cf_[6] * asp * be3s;
+  /* supersonic: the upwind flux */
+  if (ev[0] >= 0.0)
+    for (int n = 0; n < NWAVE; ++n) flxi[n] = fl[n];
+  if (ev[NWAVE - 1] <= 0.0)
+    for (int n = 0; n < NWAVE; ++n) flxi[n] = fr[n];
+  if (neg) {
+    double cl = fast_ms(gamma, wli, bxi), cr = fast_ms(gamma, wri, bxi);
+    double s = 0.5 * smax((fabs(wli[IVX]) + cl), (fabs(wri[IVX]) + cr));
+    for (int n = 0; n < NHYDRO; ++n) flxi[n] = 0.5 * (fl[n] + fr[n]) - s * du[n];
+  }
+}
+
 /* SR frame-transforming HLLE, hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330 (SR branch).
  * Local order as for hlld(); velocities are the spatial 4-velocity u^i. */
 static void hlle_sr(double gamma_adi, const double *wli, const double *wri, double bb1,
@@ -668,6 +906,7 @@ static void riemann(const orc_mesh *m, int dir, const double *wl, const double *
   if (m->p.relativistic) hlle_sr(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 2) llf(m->p.gamma, wli, wri, bx, flx7);
+  else if (m->p.rsolver == 3) roe(m->p.gamma, wli, wri, bx, flx7);
   else hlle(m->p.gamma, wli, wri, bx, flx7);
 }
 

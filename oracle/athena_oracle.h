@@ -27,7 +27,7 @@ typedef struct {
   int nx1, nx2, nx3;      /* interior cells per MeshBlock */
   int ng;                 /* ghost layers (NGHOST) */
   int xorder;             /* 2 = PLM, 3 = PPM in the second VL2 stage */
-  int rsolver;            /* 0 = HLLD, 1 = HLLE */
+  int rsolver;            /* 0 = HLLD, 1 = HLLE, 2 = LLF, 3 = Roe */
   int relativistic;       /* 0 = Newtonian adiabatic MHD, 1 = special relativistic */
   double gamma, dfloor, pfloor, cfl_number, tlim;
   double sigma_max, beta_min, gamma_max; /* SR floors (adiabatic_mhd_sr.cpp:46-48) */

@@ -40,6 +40,7 @@ VARIANTS = {
     "mhd_hlle_g3": ("hlle", 3, False),
     "mhd_hlld_g4": ("hlld", 4, False),   # PPM with mesh refinement (even NGHOST)
     "mhd_llf_g2": ("llf", 2, False),     # local Lax-Friedrichs (llf_mhd.cpp)
+    "mhd_roe_g2": ("roe", 2, False),     # Roe linearisation (roe_mhd.cpp)
     "srmhd_hlle_g2": ("hlle", 2, True),
 }
 

@@ -108,7 +108,7 @@ class OracleMesh:
             bc = mesh.bcs
         nbl = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
         self.p = Params(nbl[0], nbl[1], nbl[2], mesh.bx[0], mesh.bx[1],
-                        mesh.bx[2], mesh.ng, xorder, {"hlld": 0, "hlle": 1, "llf": 2}[rsolver],
+                        mesh.bx[2], mesh.ng, xorder, {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3}[rsolver],
                         1 if relativistic else 0, gamma,
                         floor if dfloor is None else dfloor,
                         floor if pfloor is None else pfloor, cfl, tlim, sigma_max,

@@ -87,7 +87,9 @@ def _turb_case(nx=(32, 32, 32), nb=(2, 2, 2), ng=3, xorder=3, rsolver="hlld", se
 
 @pytest.mark.parametrize("xorder,rsolver,nb", [(3, "hlld", (2, 2, 2)),
                                                (2, "hlle", (4, 2, 1)),
-                                               (2, "hlld", (1, 1, 1))])
+                                               (2, "hlld", (1, 1, 1)),
+                                               (3, "roe", (2, 1, 2)),
+                                               (2, "llf", (1, 2, 1))])
 def test_fp64_matches_oracle_bitwise(xorder, rsolver, nb):
     mesh, ic, c = _turb_case(nb=nb, xorder=xorder, rsolver=rsolver,
                              ng=3 if xorder == 3 else 2)
@@ -118,8 +120,9 @@ def _div_b(mesh, b1, b2, b3):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_div_b_stays_at_roundoff(precision):
-    mesh, ic, c = _turb_case()
+@pytest.mark.parametrize("rsolver", ["hlld", "roe"])
+def test_div_b_stays_at_roundoff(precision, rsolver):
+    mesh, ic, c = _turb_case(rsolver=rsolver)
     (u, b1, b2, b3), _, _, _ = _run_gpu(mesh, c, ic, 5, precision=precision)
     div = np.abs(_div_b(mesh, b1, b2, b3)).max()
     bmax = max(np.abs(b1).max(), np.abs(b2).max(), np.abs(b3).max())
