@@ -151,6 +151,8 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "mesh sizes must be positive");
   if (d->nx2 < 2 || d->nx3 < 2)
     return fail(ATHGPU_ERR_UNSUPPORTED, "only 3-D meshes (nx2, nx3 > 1) are supported");
+  if (d->ppm_fast && d->xorder != 3)
+    return fail(ATHGPU_ERR_ARG, "ppm_fast needs xorder 3");
   if (d->xorder < 1 || d->xorder > 3)
     return fail(ATHGPU_ERR_UNSUPPORTED, "xorder must be 1, 2 or 3");
   const int need_ng = d->xorder == 3 ? 3 : 2;
@@ -218,6 +220,7 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.ne3 = (i64)m.nc3 * (m.nc2 + 1) * (m.nc1 + 1);
   m.gamma = d->gamma; m.dfloor = d->dfloor; m.pfloor = d->pfloor;
   m.gammaf = (float)d->gamma; m.dfloorf = (float)d->dfloor; m.pfloorf = (float)d->pfloor;
+  m.ppmf = d->ppm_fast ? 1 : 0;
   m.any_bc = 0;
   for (int f = 0; f < 6; ++f) {
     m.bc[f] = d->bc[f];

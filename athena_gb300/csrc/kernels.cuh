@@ -67,6 +67,7 @@ struct DevMesh {
   // 2 reflecting); any_bc is set when one of them is not periodic
   int bc[6];
   int any_bc;
+  int ppmf;  // time/xorder = 3f: PPM with the fast limiter and no floors (ppm_fast.cpp)
   DevML ml;
 };
 
@@ -186,10 +187,10 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
                     __ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
     } else {
       ppm_one<Real>(__ldg(src + o - 2 * sw), __ldg(src + o - sw), __ldg(src + o),
-                    __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n]);
+                    __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n], m.ppmf);
     }
   }
-  if (ORDER == 3) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
+  if (ORDER == 3 && !m.ppmf) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
     const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
     qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
     qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
@@ -212,6 +213,7 @@ __device__ __forceinline__ void load_wave(const Real* __restrict__ wp,
 // ApplyPrimitiveFloors on the PPM face states (adiabatic_mhd.cpp:162-172, ppm.cpp:326-331)
 template <typename Real>
 __device__ __forceinline__ void ppm_floors(const DevMesh& m, Real* qlp, Real* qrm) {
+  if (m.ppmf) return;  // time/floor_ppm_fast defaults to false (reconstruction.cpp:42)
   const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
   qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
   qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
@@ -233,7 +235,8 @@ __device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)
     } else if (ORDER == 2) {
       plm_one<Real>(win[0][n], win[1][n], win[2][n], cp, cm, qlp[n], qrm[n]);
     } else {
-      ppm_one<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qlp[n], qrm[n]);
+      ppm_one<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qlp[n], qrm[n],
+                    m.ppmf);
     }
   }
   if (ORDER == 3) ppm_floors(m, qlp, qrm);
@@ -460,7 +463,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
         const Real lo = ppm_face<Real>(win[0][n], win[1][n], win[2][n], win[3][n]);
         dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
         ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo, dphc[n],
-                         wl[n], qrm[n]);
+                         wl[n], qrm[n], m.ppmf);
       }
       ppm_floors(m, wl, qrm);
     } else {
@@ -501,7 +504,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
           const Real lo = dphc[n];
           dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
           ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo,
-                           dphc[n], qlp[n], qrm[n]);
+                           dphc[n], qlp[n], qrm[n], m.ppmf);
         }
         ppm_floors(m, qlp, qrm);
       } else {

@@ -688,7 +688,22 @@ __device__ __forceinline__ Real ppm_face(Real q_im2, Real q_im1, Real qc, Real q
 template <typename Real>
 __device__ __forceinline__ void ppm_finish(Real q_im2, Real q_im1, Real qc, Real q_ip1,
                                            Real q_ip2, Real dph, Real dph_ip1, Real& qlp,
-                                           Real& qrm) {
+                                           Real& qrm, bool fast) {
+  if (fast) {  // time/xorder = 3f: Mignone's limiter (ppm_fast.cpp:142-165), ratios 2 on a
+               // uniform Cartesian mesh (reconstruction.cpp:490-491)
+    const Real dqm = qc - dph, dqp = dph_ip1 - qc;
+    Real qm = dph, qp = dph_ip1;
+    if (dqm * dqp <= RC(0.0)) {
+      qm = qc;
+      qp = qc;
+    } else {
+      if (dabs(dqm) >= RC(2.0) * dabs(dqp)) qm = qc - RC(2.0) * dqp;
+      if (dabs(dqp) >= RC(2.0) * dabs(dqm)) qp = qc + RC(2.0) * dqm;
+    }
+    qlp = qp;
+    qrm = qm;
+    return;
+  }
   const Real C2 = RC(1.25);
   Real d2qc_im1 = q_im2 + qc - RC(2.0) * q_im1;
   Real d2qc = q_im1 + q_ip1 - RC(2.0) * qc;
@@ -727,9 +742,9 @@ __device__ __forceinline__ void ppm_finish(Real q_im2, Real q_im1, Real qc, Real
 
 template <typename Real>
 __device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_ip1,
-                                        Real q_ip2, Real& qlp, Real& qrm) {
+                                        Real q_ip2, Real& qlp, Real& qrm, bool fast) {
   ppm_finish<Real>(q_im2, q_im1, qc, q_ip1, q_ip2, ppm_face<Real>(q_im2, q_im1, qc, q_ip1),
-                   ppm_face<Real>(q_im1, qc, q_ip1, q_ip2), qlp, qrm);
+                   ppm_face<Real>(q_im1, qc, q_ip1, q_ip2), qlp, qrm, fast);
 }
 
 

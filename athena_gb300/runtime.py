@@ -43,7 +43,8 @@ class MeshDesc(ctypes.Structure):
                 ("x3f", ctypes.POINTER(ctypes.c_double)),
                 ("dx3f", ctypes.POINTER(ctypes.c_double)),
                 ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
-                ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6)]
+                ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6),
+                ("ppm_fast", ctypes.c_int)]
 
 
 BC_PERIODIC, BC_OUTFLOW, BC_REFLECT = 0, 1, 2
@@ -197,7 +198,9 @@ class StageUpdate:
         d = MeshDesc()
         d.nbx1, d.nbx2, d.nbx3 = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
         d.nx1, d.nx2, d.nx3 = mesh.bx
-        d.nghost, d.xorder = mesh.ng, k["xorder"]
+        # time/xorder: 1, 2, 3 or "3f" (PPM with the fast limiter, ppm_fast.cpp)
+        d.nghost = mesh.ng
+        d.xorder, d.ppm_fast = (3, 1) if str(k["xorder"]) == "3f" else (int(k["xorder"]), 0)
         d.rsolver = _RSOLVERS[k["rsolver"]]
         d.precision = FP64 if k["precision"] == "fp64" else FP32
         d.relativistic = 1 if k["relativistic"] else 0

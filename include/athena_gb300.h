@@ -71,6 +71,10 @@ typedef struct {
    * bvals/cc/hydro/reflect_hydro.cpp, bvals/fc/outflow_fc.cpp, bvals/fc/reflect_fc.cpp,
    * applied as BoundaryValues::ApplyPhysicalBoundaries does, bvals/bvals.cpp:453-680). */
   int bc[6];
+  /* 1: time/xorder = 3f, PiecewiseParabolicFast (reconstruct/ppm_fast.cpp): the PPM
+   * interface values with Mignone's limiter and no floors (time/floor_ppm_fast false);
+   * needs xorder 3.  0 (the zero-initialized default): the standard PPM. */
+  int ppm_fast;
 } athgpu_mesh_desc;
 #define ATHGPU_BC_PERIODIC 0
 #define ATHGPU_BC_OUTFLOW 1

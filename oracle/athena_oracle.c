@@ -764,11 +764,13 @@ static void plm_cell(const double *qm, const double *q0, const double *qp, doubl
   }
 }
 
-/* PiecewiseParabolicX1/2/3 uniform-Cartesian CS08 branch, ppm.cpp:113-315,
+/* PiecewiseParabolicX1/2/3 uniform-Cartesian CS08 branch, ppm.cpp:113-315, or with
+ * fast != 0 PiecewiseParabolicFastX1/2/3 (ppm_fast.cpp: the same interface values, the
+ * Mignone limiter, no floors);
  * coefficients c1..c6 = 1/2,1/2,1/2,1/2,1/6,-1/6 (reconstruction.cpp:499-504);
  * floors ppm.cpp:326-331.  q[0..4] = cells i-2..i+2. */
-static void ppm_cell(const double *const q[5], double dfloor, double pfloor, double *qlp,
-                     double *qrm) {
+static void ppm_cell(const double *const q[5], double dfloor, double pfloor, int fast,
+                     double *qlp, double *qrm) {
   const double C2 = 1.25;
   const double c1 = 0.5, c2 = 0.5, c3 = 0.5, c4 = 0.5, c5 = 1.0 / 6.0, c6 = -1.0 / 6.0;
   for (int n = 0; n < NWAVE; ++n) {
@@ -805,10 +807,23 @@ static void ppm_cell(const double *const q[5], double dfloor, double pfloor, dou
       double dphip1_tmp = 0.5 * (qc + q_ip1) - d / 6.0;
       if (qa_tmp * qb_tmp < 0.0) dph_ip1 = dphip1_tmp;
     }
-    double d2qf = 6.0 * (dph + dph_ip1 - 2.0 * qc);
     double qminus = dph, qplus = dph_ip1;
     double dqf_minus = qc - qminus;
     double dqf_plus = qplus - qc;
+    if (fast) { /* time/xorder = 3f: Mignone's limiter of the parabola (ppm_fast.cpp:142-165,
+                 * ratios 2 on a uniform Cartesian mesh, reconstruction.cpp:490-491) */
+      if (dqf_minus * dqf_plus <= 0.0) {
+        qminus = qc;
+        qplus = qc;
+      } else {
+        if (fabs(dqf_minus) >= 2.0 * fabs(dqf_plus)) qminus = qc - 2.0 * dqf_plus;
+        if (fabs(dqf_plus) >= 2.0 * fabs(dqf_minus)) qplus = qc + 2.0 * dqf_minus;
+      }
+      qlp[n] = qplus;
+      qrm[n] = qminus;
+      continue;
+    }
+    double d2qf = 6.0 * (dph + dph_ip1 - 2.0 * qc);
     { /* CS limiter, ppm.cpp:234-288 */
       double qa_tmp = dqf_minus * dqf_plus;
       double qb_tmp = (q_ip1 - qc) * (qc - q_im1);
@@ -836,6 +851,7 @@ static void ppm_cell(const double *const q[5], double dfloor, double pfloor, dou
     qlp[n] = qplus;
     qrm[n] = qminus;
   }
+  if (fast) return; /* time/floor_ppm_fast defaults to false (reconstruction.cpp:42) */
   /* ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 */
   qlp[IDN] = (qlp[IDN] > dfloor) ? qlp[IDN] : dfloor;
   qlp[IPR] = (qlp[IPR] > pfloor) ? qlp[IPR] : pfloor;
@@ -892,7 +908,7 @@ static void recon_cell(const orc_mesh *m, int b, const double *w, const double *
       load_wave(m, w, bcc, dir, k + (s - 2) * dk, j + (s - 2) * dj, i + (s - 2) * di, qs[s]);
       qp[s] = qs[s];
     }
-    ppm_cell(qp, m->p.dfloor, m->p.pfloor, qlp, qrm);
+    ppm_cell(qp, m->p.dfloor, m->p.pfloor, m->p.ppm_fast, qlp, qrm);
   }
 }
 

@@ -35,6 +35,7 @@ typedef struct {
    * 2 reflecting (bvals/cc/outflow_cc.cpp, bvals/cc/hydro/reflect_hydro.cpp,
    * bvals/fc/outflow_fc.cpp, bvals/fc/reflect_fc.cpp) */
   int bc[6];
+  int ppm_fast;           /* time/xorder = 3f: PiecewiseParabolicFast (ppm_fast.cpp) */
 } orc_params;
 
 typedef struct orc_mesh orc_mesh;

@@ -34,7 +34,8 @@ class Params(ctypes.Structure):
                 ("dfloor", ctypes.c_double), ("pfloor", ctypes.c_double),
                 ("cfl_number", ctypes.c_double), ("tlim", ctypes.c_double),
                 ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
-                ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6)]
+                ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6),
+                ("ppm_fast", ctypes.c_int)]
 
 
 _lib = None
@@ -107,12 +108,15 @@ class OracleMesh:
         if multilevel:
             bc = mesh.bcs
         nbl = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
+        # time/xorder: 1, 2, 3 or "3f" (PPM with the fast limiter, ppm_fast.cpp)
+        xo, ppmf = (3, 1) if str(xorder) == "3f" else (int(xorder), 0)
+        rs = {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3}[rsolver]
         self.p = Params(nbl[0], nbl[1], nbl[2], mesh.bx[0], mesh.bx[1],
-                        mesh.bx[2], mesh.ng, xorder, {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3}[rsolver],
+                        mesh.bx[2], mesh.ng, xo, rs,
                         1 if relativistic else 0, gamma,
                         floor if dfloor is None else dfloor,
                         floor if pfloor is None else pfloor, cfl, tlim, sigma_max,
-                        beta_min, gamma_max, (ctypes.c_int * 6)(*bc))
+                        beta_min, gamma_max, (ctypes.c_int * 6)(*bc), ppmf)
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         self.h = L.orc_create(ctypes.byref(self.p), *[_p(c) for c in self.coords])
         if multilevel:

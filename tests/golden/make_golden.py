@@ -57,6 +57,11 @@ CASES = {
                                           (.5, .5, .5)), "blast", 2, 0.3, 3),
     "turb_llf_plm_8blk": ("mhd_llf_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
                                          (1., 1., 1.)), "turbulence", 2, 0.3, 3),
+    # PPM with the fast limiter (time/xorder = 3f, ppm_fast.cpp)
+    "turb_hlld_ppmf_8blk": ("mhd_hlld_g3", ((16, 16, 16), (2, 2, 2), 3, (0., 0., 0.),
+                                            (1., 1., 1.)), "turbulence", "3f", 0.3, 3),
+    "blast_hlle_ppmf_8blk": ("mhd_hlle_g3", ((16, 16, 16), (2, 2, 2), 3, (-.5, -.5, -.5),
+                                             (.5, .5, .5)), "blast", "3f", 0.3, 4),
     # Roe's linearisation (--flux=roe)
     "blast_roe_plm_8blk": ("mhd_roe_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
                                           (.5, .5, .5)), "blast", 2, 0.3, 4),

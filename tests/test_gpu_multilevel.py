@@ -58,7 +58,8 @@ def _smooth_case(ng=2, xorder=2, rsolver="hlle", bcs=(0, 0, 0, 0, 0, 0)):
 @pytest.mark.parametrize("ng,xorder,rsolver,bcs", [(2, 2, "hlle", (0, 0, 0, 0, 0, 0)),
                                                    (4, 3, "hlld", (1, 1, 2, 2, 1, 2)),
                                                    (2, 2, "roe", (2, 1, 0, 0, 1, 1)),
-                                                   (2, 2, "llf", (0, 0, 1, 2, 0, 0))])
+                                                   (2, 2, "llf", (0, 0, 1, 2, 0, 0)),
+                                                   (4, "3f", "hlle", (1, 2, 0, 0, 2, 1))])
 def test_multilevel_fp64_matches_oracle_with_ghosts(ng, xorder, rsolver, bcs):
     """Three levels, 127+ blocks: the state after three cycles equals the oracle's bit for
     bit, ghost zones of W and B included."""

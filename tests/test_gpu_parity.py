@@ -89,10 +89,11 @@ def _turb_case(nx=(32, 32, 32), nb=(2, 2, 2), ng=3, xorder=3, rsolver="hlld", se
                                                (2, "hlle", (4, 2, 1)),
                                                (2, "hlld", (1, 1, 1)),
                                                (3, "roe", (2, 1, 2)),
-                                               (2, "llf", (1, 2, 1))])
+                                               (2, "llf", (1, 2, 1)),
+                                               ("3f", "hlld", (2, 2, 1))])
 def test_fp64_matches_oracle_bitwise(xorder, rsolver, nb):
     mesh, ic, c = _turb_case(nb=nb, xorder=xorder, rsolver=rsolver,
-                             ng=3 if xorder == 3 else 2)
+                             ng=3 if xorder in (3, "3f") else 2)
     (u, b1, b2, b3), dts, w, bcc = _run_gpu(mesh, c, ic, 4)
     om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"])
     om.set_state(*ic)
@@ -232,7 +233,7 @@ def test_physical_boundaries_match_oracle_bitwise(bc, xorder, rsolver, nb):
     the EMF averaging along them: every primitive, cell-centred field and face value,
     ghost zones included, equals the oracle's after four cycles."""
     mesh, ic, c = _turb_case(nx=(24, 24, 24), nb=nb, xorder=xorder, rsolver=rsolver,
-                             ng=3 if xorder == 3 else 2)
+                             ng=3 if xorder in (3, "3f") else 2)
     c["bc"] = bc
     (u, b1, b2, b3), dts, w, bcc = _run_gpu(mesh, c, ic, 4)
     om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"],
