@@ -220,7 +220,6 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.ne3 = (i64)m.nc3 * (m.nc2 + 1) * (m.nc1 + 1);
   m.gamma = d->gamma; m.dfloor = d->dfloor; m.pfloor = d->pfloor;
   m.gammaf = (float)d->gamma; m.dfloorf = (float)d->dfloor; m.pfloorf = (float)d->pfloor;
-  m.ppmf = d->ppm_fast ? 1 : 0;
   m.any_bc = 0;
   for (int f = 0; f < 6; ++f) {
     m.bc[f] = d->bc[f];

@@ -67,7 +67,6 @@ struct DevMesh {
   // 2 reflecting); any_bc is set when one of them is not periodic
   int bc[6];
   int any_bc;
-  int ppmf;  // time/xorder = 3f: PPM with the fast limiter and no floors (ppm_fast.cpp)
   DevML ml;
 };
 
@@ -187,10 +186,10 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
                     __ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
     } else {
       ppm_one<Real>(__ldg(src + o - 2 * sw), __ldg(src + o - sw), __ldg(src + o),
-                    __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n], m.ppmf);
+                    __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n], ORDER == 4);
     }
   }
-  if (ORDER == 3 && !m.ppmf) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
+  if (ORDER == 3) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
     const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
     qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
     qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
@@ -213,7 +212,6 @@ __device__ __forceinline__ void load_wave(const Real* __restrict__ wp,
 // ApplyPrimitiveFloors on the PPM face states (adiabatic_mhd.cpp:162-172, ppm.cpp:326-331)
 template <typename Real>
 __device__ __forceinline__ void ppm_floors(const DevMesh& m, Real* qlp, Real* qrm) {
-  if (m.ppmf) return;  // time/floor_ppm_fast defaults to false (reconstruction.cpp:42)
   const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
   qlp[IDN] = (qlp[IDN] > dfl) ? qlp[IDN] : dfl;
   qlp[IPR] = (qlp[IPR] > pfl) ? qlp[IPR] : pfl;
@@ -236,7 +234,7 @@ __device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)
       plm_one<Real>(win[0][n], win[1][n], win[2][n], cp, cm, qlp[n], qrm[n]);
     } else {
       ppm_one<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qlp[n], qrm[n],
-                    m.ppmf);
+                    ORDER == 4);
     }
   }
   if (ORDER == 3) ppm_floors(m, qlp, qrm);
@@ -407,7 +405,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   //  * fbuf: the normal face field of faces s and s+1 (FP64, double-buffered);
   //  * aux: the divergence register (x2) or divergence, U^n and compensation (x3) of the
   //    cell updated in this step, copied in before the face solve.
-  constexpr int R = ORDER == 3 ? 2 : ORDER == 2 ? 1 : 0;
+  constexpr int R = ORDER >= 3 ? 2 : ORDER == 2 ? 1 : 0;
   constexpr int WN = 2 * R + 1;
   constexpr int NS = WN + 1;
   constexpr int NAUX = DIR == 1 ? NHYDRO : 3 * NHYDRO;
@@ -453,19 +451,19 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
   Real wl[NWAVE], qlp[NWAVE], qrm[NWAVE];
   Real fprev[NHYDRO];
-  Real dphc[ORDER == 3 ? NWAVE : 1];  // PPM: limited lower interface of the current cell
+  Real dphc[ORDER >= 3 ? NWAVE : 1];  // PPM: limited lower interface of the current cell
   {
     Real win[WN][NWAVE];
     window(0, win);
-    if constexpr (ORDER == 3) {
+    if constexpr (ORDER >= 3) {
 #pragma unroll
       for (int n = 0; n < NWAVE; ++n) {
         const Real lo = ppm_face<Real>(win[0][n], win[1][n], win[2][n], win[3][n]);
         dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
         ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo, dphc[n],
-                         wl[n], qrm[n], m.ppmf);
+                         wl[n], qrm[n], ORDER == 4);
       }
-      ppm_floors(m, wl, qrm);
+      if (ORDER == 3) ppm_floors(m, wl, qrm);  // time/floor_ppm_fast is false
     } else {
       recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + c0 - 1) : Real(0),
                                 ORDER == 2 ? __ldg(pc + m.ncmax + c0 - 1) : Real(0), wl,
@@ -498,15 +496,15 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     {
       Real win[WN][NWAVE];
       window(rel0, win);
-      if constexpr (ORDER == 3) {  // the lower interface is the previous cell's upper one
+      if constexpr (ORDER >= 3) {  // the lower interface is the previous cell's upper one
 #pragma unroll
         for (int n = 0; n < NWAVE; ++n) {
           const Real lo = dphc[n];
           dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
           ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo,
-                           dphc[n], qlp[n], qrm[n], m.ppmf);
+                           dphc[n], qlp[n], qrm[n], ORDER == 4);
         }
-        ppm_floors(m, qlp, qrm);
+        if (ORDER == 3) ppm_floors(m, qlp, qrm);
       } else {
         recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + s) : Real(0),
                                   ORDER == 2 ? __ldg(pc + m.ncmax + s) : Real(0), qlp, qrm);
@@ -568,7 +566,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
 // shared-memory bytes of the x2/x3 sweep's staging for a CTA of `threads` threads
 __host__ __device__ inline int sweep_smem_bytes(int dir, int order, int real_bytes,
                                                 int threads) {
-  const int r = order == 3 ? 2 : order == 2 ? 1 : 0;
+  const int r = order >= 3 ? 2 : order == 2 ? 1 : 0;
   const int naux = dir == 1 ? NHYDRO : 3 * NHYDRO;
   return 2 * 8 * threads + ((2 * r + 2) * NWAVE + naux) * threads * real_bytes;
 }

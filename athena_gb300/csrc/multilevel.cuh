@@ -644,15 +644,15 @@ ml_fine_flux_kernel(DevMesh m, const int4* __restrict__ tasks, int ntasks,
       if (ax == 0) {
         if (ORDER == 1) face_flux<Real, 0, 1, RS>(m, w, bcc, b1, fbk, p[2], p[1], p[0], F[ob][oa]);
         else if (ORDER == 2) face_flux<Real, 0, 2, RS>(m, w, bcc, b1, fbk, p[2], p[1], p[0], F[ob][oa]);
-        else face_flux<Real, 0, 3, RS>(m, w, bcc, b1, fbk, p[2], p[1], p[0], F[ob][oa]);
+        else face_flux<Real, 0, ORDER, RS>(m, w, bcc, b1, fbk, p[2], p[1], p[0], F[ob][oa]);
       } else if (ax == 1) {
         if (ORDER == 1) face_flux<Real, 1, 1, RS>(m, w, bcc, b2, fbk, p[2], p[1], p[0], F[ob][oa]);
         else if (ORDER == 2) face_flux<Real, 1, 2, RS>(m, w, bcc, b2, fbk, p[2], p[1], p[0], F[ob][oa]);
-        else face_flux<Real, 1, 3, RS>(m, w, bcc, b2, fbk, p[2], p[1], p[0], F[ob][oa]);
+        else face_flux<Real, 1, ORDER, RS>(m, w, bcc, b2, fbk, p[2], p[1], p[0], F[ob][oa]);
       } else {
         if (ORDER == 1) face_flux<Real, 2, 1, RS>(m, w, bcc, b3, fbk, p[2], p[1], p[0], F[ob][oa]);
         else if (ORDER == 2) face_flux<Real, 2, 2, RS>(m, w, bcc, b3, fbk, p[2], p[1], p[0], F[ob][oa]);
-        else face_flux<Real, 2, 3, RS>(m, w, bcc, b3, fbk, p[2], p[1], p[0], F[ob][oa]);
+        else face_flux<Real, 2, ORDER, RS>(m, w, bcc, b3, fbk, p[2], p[1], p[0], F[ob][oa]);
       }
     }
   // areas of the four fine faces, in the bulk precision (as the coarse block's own

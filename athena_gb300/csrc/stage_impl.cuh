@@ -200,7 +200,8 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   const DevMesh& m = c->m;
   Registers& r = c->r;
   cudaStream_t s = c->stream;
-  const int order = (stage == 1) ? 1 : c->desc.xorder;
+  // reconstruction template index: 1 DC, 2 PLM, 3 PPM, 4 fast PPM (time/xorder = 3f)
+  const int order = (stage == 1) ? 1 : c->desc.ppm_fast ? 4 : c->desc.xorder;
   const double beta = (stage == 1) ? 0.5 : 1.0;
   // stage 1 reads U^n, B^n and writes U*, B*; stage 2 reads W*, B* and updates U, B
   const double* bb1 = (stage == 1) ? r.b1 : r.bs1;
@@ -227,7 +228,8 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   } while (0)
   if (order == 1) FLUX_RS(1);
   else if (order == 2) FLUX_RS(2);
-  else FLUX_RS(3);
+  else if (order == 3) FLUX_RS(3);
+  else FLUX_RS(4);
 #undef FLUX_RS
 #undef FLUX
   {
