@@ -44,7 +44,7 @@ def _desc(mesh, **kw):
 @pytest.mark.parametrize("field,value,code", [
     ("xorder", 4, -3), ("xorder", 0, -3), ("nghost", 1, -1), ("rsolver", 7, -1),
     ("precision", 9, -1), ("relativistic", 1, -3), ("gamma", 1.0, -1),
-    ("cfl_number", 0.0, -1), ("nx1", 0, -1)])
+    ("cfl_number", 0.0, -1), ("nx1", 0, -1), ("ppm_fast", 1, -1)])
 def test_invalid_meshes_are_rejected(lib, field, value, code):
     mesh = MeshSpec((16, 8, 8), (1, 1, 1), 2)
     d, keep = _desc(mesh, **{field: value})
