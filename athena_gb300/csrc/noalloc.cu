@@ -9,8 +9,10 @@
 // computation needs — the per-CTA partial minima of the two-pass time-step reduction —
 // lives in the file-scope array g_noalloc_partial below, of fixed size.  Every GPU that
 // loads the library holds that array (about 0.5 MB) until the process exits.
+#include <cuda.h>  // CUcontext and the driver-call types (the calls are fetched at run time)
 #include <cuda_runtime.h>
 #include <float.h>
+#include <limits.h>
 
 #include <mutex>
 #include <string>
@@ -34,9 +36,19 @@ static_assert(kMaxCells == ATHGPU_NOALLOC_MAX_CELLS, "header limit out of date")
 // overwrites every entry it reads before reading it.
 static __device__ __align__(256) double g_noalloc_partial[kMaxPartials + 32];
 
-constexpr int kMaxDevices = 64;
+// The device address of g_noalloc_partial belongs to a CUDA context, not to a device: a
+// host that makes its own driver context current, or a process that reset the device,
+// sees the array at another address.  The lookups are cached per context, keyed by the
+// context's process-unique ID (cuCtxGetId), which a re-created context never reuses.
+constexpr int kMaxContexts = 64;
+struct SymbolEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
 std::mutex g_mu;
-double* g_symbol_addr[kMaxDevices] = {nullptr};  // device address of g_noalloc_partial
+SymbolEntry g_symbol_cache[kMaxContexts];
+int g_symbol_used = 0;
+int g_symbol_next = 0;  // slot replaced next once the cache is full
 
 
 __device__ __forceinline__ long long f1(int nc1, int nc2, long long nf, int b, int k, int j,
@@ -170,6 +182,79 @@ athgpu_status noalloc_fail(athgpu_status s, const std::string& msg) {
   return s;
 }
 
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// The process-unique ID of the calling thread's current CUDA context.  The two driver
+// calls are fetched through the runtime, so the library needs no link against libcuda.
+// With no context current yet, the runtime's primary context of the current device is
+// made current first (cudaSetDevice initialises it; it allocates nothing).
+athgpu_status current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                                      cudaEnableDefault, &q1);
+    cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000,
+                                                      cudaEnableDefault, &q2);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+        q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return noalloc_fail(ATHGPU_ERR_CUDA,
+                          "con2prim_timestep_noalloc: cuCtxGetCurrent/cuCtxGetId unavailable");
+    get_current = (CtxGetCurrentFn)f1;
+    get_id = (CtxGetIdFn)f2;
+  }
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS)
+    return noalloc_fail(ATHGPU_ERR_CUDA, "con2prim_timestep_noalloc: cuCtxGetCurrent failed");
+  if (!c) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaSetDevice(dev);
+    if (e != cudaSuccess)
+      return noalloc_fail(ATHGPU_ERR_CUDA,
+                          std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    if (get_current(&c) != CUDA_SUCCESS || !c)
+      return noalloc_fail(ATHGPU_ERR_CUDA, "con2prim_timestep_noalloc: no current context");
+  }
+  if (get_id(c, id) != CUDA_SUCCESS)
+    return noalloc_fail(ATHGPU_ERR_CUDA, "con2prim_timestep_noalloc: cuCtxGetId failed");
+  return ATHGPU_OK;
+}
+
+// Device address of the scratch array in the current context.  Set-up, once per context:
+// cudaGetSymbolAddress with that context current (the array's host-side name is only a
+// stand-in and must never reach a kernel).
+athgpu_status scratch_address(double** out) {
+  unsigned long long id = 0;
+  athgpu_status st = current_context_id(&id);
+  if (st != ATHGPU_OK) return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (int q = 0; q < g_symbol_used; ++q)
+    if (g_symbol_cache[q].ctx_id == id) {
+      *out = g_symbol_cache[q].addr;
+      return ATHGPU_OK;
+    }
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partial);
+  if (e != cudaSuccess || !p)
+    return noalloc_fail(ATHGPU_ERR_CUDA,
+                        std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  int slot;
+  if (g_symbol_used < kMaxContexts) {
+    slot = g_symbol_used++;
+  } else {  // full: replace the oldest entry
+    slot = g_symbol_next;
+    g_symbol_next = (g_symbol_next + 1) % kMaxContexts;
+  }
+  g_symbol_cache[slot] = {id, (double*)p};
+  *out = (double*)p;
+  return ATHGPU_OK;
+}
+
 }  // namespace
 
 extern "C" athgpu_status athgpu_con2prim_timestep_noalloc(
@@ -179,52 +264,50 @@ extern "C" athgpu_status athgpu_con2prim_timestep_noalloc(
     double* w, double* bcc, double* dt_out, void* stream) {
   if (nblocks < 1 || nx1 < 1 || nx2 < 1 || nx3 < 1 || nghost < 1)
     return noalloc_fail(ATHGPU_ERR_ARG, "con2prim_timestep_noalloc: sizes must be positive");
+  // the same mesh shapes as athgpu_create: 3-D only (a 2-D array of the reference has
+  // nc3 = 1 and no x3 ghosts, which this layout would read past)
+  if (nx2 < 2 || nx3 < 2)
+    return noalloc_fail(ATHGPU_ERR_UNSUPPORTED,
+                        "con2prim_timestep_noalloc: only 3-D meshes (nx2, nx3 > 1) are "
+                        "supported");
   if (!dx1f || !dx2f || !dx3f || !b1 || !b2 || !b3 || !u || !w || !bcc || !dt_out)
     return noalloc_fail(ATHGPU_ERR_ARG, "con2prim_timestep_noalloc: null pointer");
   if (!(gamma > 1.0) || !(cfl_number > 0.0))
     return noalloc_fail(ATHGPU_ERR_ARG, "con2prim_timestep_noalloc: bad gamma or cfl");
+  // sizes in 64-bit first: nx + 2 nghost must fit the kernels' int indices
+  const long long lc1 = (long long)nx1 + 2LL * nghost;
+  const long long lc2 = (long long)nx2 + 2LL * nghost;
+  const long long lc3 = (long long)nx3 + 2LL * nghost;
+  if (lc1 > INT_MAX || lc2 > INT_MAX || lc3 > INT_MAX)
+    return noalloc_fail(ATHGPU_ERR_ARG, "con2prim_timestep_noalloc: block too large");
+  // each factor is below 2^31, so lc1 * lc2 < 2^62; checked against the limit before the
+  // third factor (then ncell < 2^55) and before the block count, so nothing overflows
+  const long long ncell = (lc1 * lc2 > kMaxCells) ? kMaxCells + 1 : lc1 * lc2 * lc3;
+  if (ncell > kMaxCells || (long long)nblocks > kMaxCells / ncell)
+    return noalloc_fail(ATHGPU_ERR_ARG,
+                        "con2prim_timestep_noalloc: " + std::to_string(nblocks) +
+                            " blocks of " + std::to_string(ncell) +
+                            " cells (ghosts included) exceed the no-allocation limit of " +
+                            std::to_string(kMaxCells) + " cells per call");
   Geometry g;
   g.nb = nblocks;
   g.nx1 = nx1; g.nx2 = nx2; g.nx3 = nx3; g.ng = nghost;
-  g.nc1 = nx1 + 2 * nghost; g.nc2 = nx2 + 2 * nghost; g.nc3 = nx3 + 2 * nghost;
-  g.ncell = (long long)g.nc1 * g.nc2 * g.nc3;
+  g.nc1 = (int)lc1; g.nc2 = (int)lc2; g.nc3 = (int)lc3;
+  g.ncell = ncell;
   g.nf1 = (long long)g.nc3 * g.nc2 * (g.nc1 + 1);
   g.nf2 = (long long)g.nc3 * (g.nc2 + 1) * g.nc1;
   g.nf3 = (long long)(g.nc3 + 1) * g.nc2 * g.nc1;
   g.gamma = gamma; g.dfloor = dfloor; g.pfloor = pfloor;
-  const long long cells = (long long)nblocks * g.ncell;
-  if (cells > kMaxCells)
-    return noalloc_fail(ATHGPU_ERR_ARG,
-                        "con2prim_timestep_noalloc: " + std::to_string(cells) +
-                            " cells (ghosts included) exceed the no-allocation limit of " +
-                            std::to_string(kMaxCells) + " cells per call");
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess)
-    return noalloc_fail(ATHGPU_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices)
-    return noalloc_fail(ATHGPU_ERR_UNSUPPORTED, "con2prim_timestep_noalloc: device index");
+  const long long cells = (long long)nblocks * ncell;
   double* partial = nullptr;
-  {
-    // one-time set-up per device, with that device current: the device address of the
-    // scratch array (its host-side name is only a stand-in)
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_symbol_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_partial);
-      if (e != cudaSuccess)
-        return noalloc_fail(ATHGPU_ERR_CUDA,
-                            std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      g_symbol_addr[dev] = (double*)p;
-    }
-    partial = g_symbol_addr[dev];
-  }
+  athgpu_status st = scratch_address(&partial);
+  if (st != ATHGPU_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const int nparts = (int)((cells + kThreads - 1) / kThreads);
   c2p_dt_partial_kernel<<<nparts, kThreads, 0, s>>>(g, dx1f, dx2f, dx3f, b1, b2, b3, u, w,
                                                     bcc, partial);
   dt_finalize_kernel<<<1, 1024, 0, s>>>(partial, nparts, cfl_number, dt_out);
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return noalloc_fail(ATHGPU_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
   return ATHGPU_OK;

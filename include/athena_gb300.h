@@ -414,9 +414,11 @@ athgpu_status athgpu_selftest_conversions(long long n, const double *d, const fl
  * reduction's scratch is a fixed array of 65,536 doubles inside the library, held by every
  * GPU that loads it until the process exits, so a call covers at most
  * ATHGPU_NOALLOC_MAX_CELLS cells (ghosts included, all blocks) and larger meshes are
- * rejected with ATHGPU_ERR_ARG.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call before
- * any stream capture.  Every call on a device shares the one array, which keeps the last
+ * rejected with ATHGPU_ERR_ARG; meshes with nx2 or nx3 < 2 are rejected with
+ * ATHGPU_ERR_UNSUPPORTED, as by athgpu_create.  The first call in each CUDA context (per
+ * device, normally the runtime's primary context) looks up the array's device address
+ * (cudaGetSymbolAddress) with that context current; make that first call before any
+ * stream capture.  Every call on a device shares the one array, which keeps the last
  * call's contents: calls that overlap on the GPU (different streams, no ordering) race;
  * order them on one stream or with events. */
 #define ATHGPU_NOALLOC_MAX_CELLS 16777216LL
