@@ -43,12 +43,22 @@ struct orc_mesh {
   /* multi-level mesh (athena_oracle_ml.c), NULL for a uniform mesh */
   struct orc_ml *ml;
   const int *ml_nblev;  /* its [nb][27] neighbour-level table */
-  int rk1;              /* integrator = rk1 (multi-level meshes; diagnostics) */
+  int integ;            /* time/integrator: ORC_VL2, ORC_RK2 or ORC_RK1 */
 };
 
+/* The stage weights of TimeIntegratorTaskList (time_integrator.cpp:111-236 vl2,
+ * :338-465 rk2; rk1 one stage with beta = delta = 1): beta scales dt in the flux
+ * divergence and CT, delta the first register average (u1 += delta*u), and
+ * gamma = (g1, g2, 0) the second, a register swap when (0, 1, 0) (:1814-1821). */
+typedef struct {
+  double beta, delta, g1, g2;
+  int order;  /* reconstruction: donor cell on the first vl2 stage (:1700-1703) */
+  int swap;   /* gamma = (0, 1, 0) */
+} stage_w;
+
 struct orc_ml;
+static stage_w stage_weights(const orc_mesh *m, int stage);
 static void ml_stage(orc_mesh *m, int stage);
-static void ml_stage_w(orc_mesh *m, double beta, double delta, int order);
 static void ml_initialize(orc_mesh *m);
 static void ml_free(struct orc_ml *ml, int nb);
 
@@ -2001,15 +2011,68 @@ void orc_initialize(orc_mesh *m) {
 
 #define SWAP(a, b) do { double *t_ = (a); (a) = (b); (b) = t_; } while (0)
 
-/* one VL2 stage of TimeIntegratorTaskList for MHD (time_integrator.cpp:1606-2318):
- * StartupTaskList zeroing, CalculateHydroFlux (DC on stage 1), CalculateEMF, EMF
- * averaging, IntegrateHydro/IntegrateField with the register swaps, ghost exchange,
- * Primitives (W(U) into w1 then swap), NewBlockTimeStep on the last stage. */
+static stage_w stage_weights(const orc_mesh *m, int stage) {
+  stage_w w;
+  w.g1 = 0.0; w.g2 = 1.0; w.swap = 1;
+  w.order = m->p.xorder;
+  if (m->integ == ORC_RK1) {           /* one stage */
+    w.beta = 1.0; w.delta = 1.0;
+  } else if (m->integ == ORC_RK2) {    /* :338-465: Heun / SSPRK(2,2) */
+    if (stage == 1) { w.beta = 1.0; w.delta = 1.0; }
+    else { w.beta = 0.5; w.delta = 0.0; w.g1 = 0.5; w.g2 = 0.5; w.swap = 0; }
+  } else {                             /* vl2, :111-236 */
+    w.beta = (stage == 1) ? 0.5 : 1.0;
+    w.delta = (stage == 1) ? 1.0 : 0.0;
+    if (stage == 1) w.order = 1;
+  }
+  return w;
+}
+
+/* WeightedAve(u1, u, ..., {1, delta, 0, 0, 0}) then, unless the registers swap,
+ * WeightedAve(u, u1, ..., {g1, g2, 0, 0, 0}) (weighted_ave.cpp:35-230) over the interior
+ * of one block; returns the register IntegrateHydro then updates (the pointer swap itself
+ * happens after all blocks, so with a swap that register is u1). */
+static double *hydro_registers(orc_mesh *m, const stage_w *sw, double *u, double *u1) {
+  if (sw->delta != 0.0)
+    for (int n = 0; n < NHYDRO; ++n)
+      for (int k = m->ks; k <= m->ke; ++k)
+        for (int j = m->js; j <= m->je; ++j)
+          for (int i = m->is; i <= m->ie; ++i)
+            u1[CIDX(m, n, k, j, i)] += sw->delta * u[CIDX(m, n, k, j, i)];
+  if (sw->swap) return u1;
+  for (int n = 0; n < NHYDRO; ++n)
+    for (int k = m->ks; k <= m->ke; ++k)
+      for (int j = m->js; j <= m->je; ++j)
+        for (int i = m->is; i <= m->ie; ++i)
+          u[CIDX(m, n, k, j, i)] = sw->g1 * u[CIDX(m, n, k, j, i)] +
+                                   sw->g2 * u1[CIDX(m, n, k, j, i)];
+  return u;
+}
+
+/* the same for the face field of one block (weighted_ave.cpp:360-560: x1 faces
+ * [is, ie+1], x2 faces [js, je+1], x3 faces [ks, ke+1]); f = b1 registers, g = b */
+static void field_registers(orc_mesh *m, const stage_w *sw, double *const f[3],
+                            double *const g[3]) {
+  int iu[3] = {1, 0, 0}, ju[3] = {0, 1, 0}, ku[3] = {0, 0, 1};
+  for (int d = 0; d < 3; ++d)
+    for (int k = m->ks; k <= m->ke + ku[d]; ++k)
+      for (int j = m->js; j <= m->je + ju[d]; ++j)
+        for (int i = m->is; i <= m->ie + iu[d]; ++i) {
+          const long o = d == 0 ? F1IDX(m, k, j, i) : d == 1 ? F2IDX(m, k, j, i)
+                                                             : F3IDX(m, k, j, i);
+          if (sw->delta != 0.0) f[d][o] += sw->delta * g[d][o];
+          if (!sw->swap) g[d][o] = sw->g1 * g[d][o] + sw->g2 * f[d][o];
+        }
+}
+
+/* one stage of TimeIntegratorTaskList for MHD (time_integrator.cpp:1606-2318):
+ * StartupTaskList zeroing, CalculateHydroFlux (DC on the first vl2 stage),
+ * CalculateEMF, EMF averaging, IntegrateHydro/IntegrateField with the register
+ * averages, ghost exchange, Primitives (W(U) into w1 then swap), NewBlockTimeStep on the
+ * last stage. */
 void orc_stage(orc_mesh *m, int stage) {
   if (m->ml) { ml_stage(m, stage); return; }
-  const double beta = (stage == 1) ? 0.5 : 1.0;      /* time_integrator.cpp:216-217 */
-  const double delta = (stage == 1) ? 1.0 : 0.0;     /* :228-236 */
-  const int order = (stage == 1) ? 1 : m->p.xorder;  /* :1700-1703 */
+  const stage_w sw = stage_weights(m, stage);
   long nb = m->nb;
   if (stage == 1) { /* StartupTaskList, :1606-1625 */
     memset(m->u1, 0, sizeof(double) * nb * NHYDRO * m->ncell);
@@ -2024,49 +2087,30 @@ void orc_stage(orc_mesh *m, int stage) {
     /* phase A: fluxes, corner EMFs, hydro register average + flux divergence */
 #pragma omp for schedule(dynamic, 1)
     for (int b = 0; b < m->nb; ++b) {
-      calculate_fluxes(m, b, order, &s);
+      calculate_fluxes(m, b, sw.order, &s);
       corner_e(m, b, &s);
       double *u = m->u + (long)b * NHYDRO * m->ncell;
       double *u1 = m->u1 + (long)b * NHYDRO * m->ncell;
-      /* WeightedAve(u1, u, ..., {1, delta, 0, 0, 0}), weighted_ave.cpp:35-95 */
-      if (delta != 0.0)
-        for (int n = 0; n < NHYDRO; ++n)
-          for (int k = m->ks; k <= m->ke; ++k)
-            for (int j = m->js; j <= m->je; ++j)
-              for (int i = m->is; i <= m->ie; ++i)
-                u1[CIDX(m, n, k, j, i)] += delta * u[CIDX(m, n, k, j, i)];
-      /* gamma = (0, 1, 0): the registers swap (time_integrator.cpp:1815-1817); the
-       * pointer swap happens after the loops, so the register updated here is u1 */
-      add_flux_divergence(m, b, beta * m->dt, u1, &s);
+      add_flux_divergence(m, b, sw.beta * m->dt, hydro_registers(m, &sw, u, u1), &s);
     }
     /* phase B: EMF correction (needs every block's edges), field registers + CT */
 #pragma omp for schedule(dynamic, 1)
     for (int b = 0; b < m->nb; ++b) {
-      double *f[3] = {m->bb1 + b * m->nf1, m->bb2 + b * m->nf2, m->bb3 + b * m->nf3};
-      const double *g[3] = {m->b1 + b * m->nf1, m->b2 + b * m->nf2, m->b3 + b * m->nf3};
-      if (delta != 0.0) { /* WeightedAve for FaceField, weighted_ave.cpp:360-420 */
-        for (int k = m->ks; k <= m->ke; ++k)
-          for (int j = m->js; j <= m->je; ++j)
-            for (int i = m->is; i <= m->ie + 1; ++i)
-              f[0][F1IDX(m, k, j, i)] += delta * g[0][F1IDX(m, k, j, i)];
-        for (int k = m->ks; k <= m->ke; ++k)
-          for (int j = m->js; j <= m->je + 1; ++j)
-            for (int i = m->is; i <= m->ie; ++i)
-              f[1][F2IDX(m, k, j, i)] += delta * g[1][F2IDX(m, k, j, i)];
-        for (int k = m->ks; k <= m->ke + 1; ++k)
-          for (int j = m->js; j <= m->je; ++j)
-            for (int i = m->is; i <= m->ie; ++i)
-              f[2][F3IDX(m, k, j, i)] += delta * g[2][F3IDX(m, k, j, i)];
-      }
+      double *const f[3] = {m->bb1 + b * m->nf1, m->bb2 + b * m->nf2, m->bb3 + b * m->nf3};
+      double *const g[3] = {m->b1 + b * m->nf1, m->b2 + b * m->nf2, m->b3 + b * m->nf3};
+      field_registers(m, &sw, f, g);
       corrected_edges(m, b, &s);
-      ct_update(m, b, beta * m->dt, f[0], f[1], f[2], &s);
+      double *const *t = sw.swap ? f : g;
+      ct_update(m, b, sw.beta * m->dt, t[0], t[1], t[2], &s);
     }
     scratch_free(&s);
   }
-  SWAP(m->u, m->u1);
-  SWAP(m->b1, m->bb1);
-  SWAP(m->b2, m->bb2);
-  SWAP(m->b3, m->bb3);
+  if (sw.swap) {
+    SWAP(m->u, m->u1);
+    SWAP(m->b1, m->bb1);
+    SWAP(m->b2, m->bb2);
+    SWAP(m->b3, m->bb3);
+  }
   exchange(m, m->u, NHYDRO, m->b1, m->b2, m->b3);
   all_con2prim(m, m->w1);  /* ConservedToPrimitive(u, w, b, w1, ...) (:2221-2223) */
   SWAP(m->w, m->w1);       /* :2269 */
@@ -2075,12 +2119,8 @@ void orc_stage(orc_mesh *m, int stage) {
 
 /* the stages of one cycle and time += dt (main.cpp:535), without the new time step */
 void orc_advance(orc_mesh *m) {
-  if (m->rk1) {  /* integrator = rk1: one stage, beta = delta = 1, order xorder */
-    ml_stage_w(m, 1.0, 1.0, m->p.xorder);
-  } else {
-    orc_stage(m, 1);
-    orc_stage(m, 2);
-  }
+  orc_stage(m, 1);
+  if (m->integ != ORC_RK1) orc_stage(m, 2);
   m->time += m->dt;
 }
 

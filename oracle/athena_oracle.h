@@ -80,8 +80,12 @@ int orc_set_multilevel(orc_mesh *m, const int *nbr_table, const int *nbr_count,
                        const double *cdx1f, const double *cx2f, const double *cdx2f,
                        const double *cx3f, const double *cdx3f);
 
-/* use the one-stage rk1 integrator in orc_cycle (multi-level meshes; diagnostics) */
-void orc_set_rk1(orc_mesh *m, int on);
+/* time/integrator (task_list/time_integrator.cpp): ORC_VL2 (the default), ORC_RK2, or
+ * ORC_RK1 (one stage; diagnostics) */
+#define ORC_VL2 0
+#define ORC_RK2 1
+#define ORC_RK1 2
+void orc_set_integrator(orc_mesh *m, int integrator);
 /* the stages of one cycle and time += dt, without the new time step (adaptive runs
  * regrid in between); then orc_new_dt: NewBlockTimeStep + Mesh::NewTimeStep */
 void orc_advance(orc_mesh *m);

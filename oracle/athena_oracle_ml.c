@@ -1321,22 +1321,18 @@ static void ml_prolongate_block(orc_mesh *m, int b, double *w) {
 
 /* ---- the multi-level stage and initialization ------------------------------------------ */
 
+/* one stage on a multi-level mesh, the register averages of stage_weights */
 static void ml_stage(orc_mesh *m, int stage) {
-  ml_stage_w(m, (stage == 1) ? 0.5 : 1.0, (stage == 1) ? 1.0 : 0.0,
-             (stage == 1) ? 1 : m->p.xorder);
-}
-
-/* one stage with weights beta (flux divergence and CT) and delta (register average);
- * delta != 0 starts a cycle (StartupTaskList zeroes the registers) */
-static void ml_stage_w(orc_mesh *m, double beta, double delta, int order) {
+  const stage_w sw = stage_weights(m, stage);
   orc_ml *ml = m->ml;
   long nb = m->nb;
-  if (delta != 0.0) {
+  if (stage == 1) {  /* StartupTaskList zeroes the registers */
     memset(m->u1, 0, sizeof(double) * nb * NHYDRO * m->ncell);
     memset(m->bb1, 0, sizeof(double) * nb * m->nf1);
     memset(m->bb2, 0, sizeof(double) * nb * m->nf2);
     memset(m->bb3, 0, sizeof(double) * nb * m->nf3);
   }
+  const int order = sw.order;
   /* CalculateHydroFlux, CalculateEMF (corner EMFs into m->e1..e3) */
 #pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < m->nb; ++b) {
@@ -1350,41 +1346,25 @@ static void ml_stage_w(orc_mesh *m, double beta, double delta, int order) {
   for (int b = 0; b < m->nb; ++b) {
     double *u = m->u + (long)b * NHYDRO * m->ncell;
     double *u1 = m->u1 + (long)b * NHYDRO * m->ncell;
-    if (delta != 0.0)
-      for (int n = 0; n < NHYDRO; ++n)
-        for (int k = m->ks; k <= m->ke; ++k)
-          for (int j = m->js; j <= m->je; ++j)
-            for (int i = m->is; i <= m->ie; ++i)
-              u1[CIDX(m, n, k, j, i)] += delta * u[CIDX(m, n, k, j, i)];
-    add_flux_divergence(m, b, beta * m->dt, u1, &ml->sb[b]);
+    add_flux_divergence(m, b, sw.beta * m->dt, hydro_registers(m, &sw, u, u1), &ml->sb[b]);
   }
   /* SEND/RECV_FLDFLX (EMF correction) and IntegrateField */
 #pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < m->nb; ++b) {
     scratch *s = &ml->sb[b];
-    double *f[3] = {m->bb1 + b * m->nf1, m->bb2 + b * m->nf2, m->bb3 + b * m->nf3};
-    const double *g[3] = {m->b1 + b * m->nf1, m->b2 + b * m->nf2, m->b3 + b * m->nf3};
-    if (delta != 0.0) {
-      for (int k = m->ks; k <= m->ke; ++k)
-        for (int j = m->js; j <= m->je; ++j)
-          for (int i = m->is; i <= m->ie + 1; ++i)
-            f[0][F1IDX(m, k, j, i)] += delta * g[0][F1IDX(m, k, j, i)];
-      for (int k = m->ks; k <= m->ke; ++k)
-        for (int j = m->js; j <= m->je + 1; ++j)
-          for (int i = m->is; i <= m->ie; ++i)
-            f[1][F2IDX(m, k, j, i)] += delta * g[1][F2IDX(m, k, j, i)];
-      for (int k = m->ks; k <= m->ke + 1; ++k)
-        for (int j = m->js; j <= m->je; ++j)
-          for (int i = m->is; i <= m->ie; ++i)
-            f[2][F3IDX(m, k, j, i)] += delta * g[2][F3IDX(m, k, j, i)];
-    }
+    double *const f[3] = {m->bb1 + b * m->nf1, m->bb2 + b * m->nf2, m->bb3 + b * m->nf3};
+    double *const g[3] = {m->b1 + b * m->nf1, m->b2 + b * m->nf2, m->b3 + b * m->nf3};
+    field_registers(m, &sw, f, g);
     ml_emf_correct_block(m, b, s->e1, s->e2, s->e3);
-    ct_update(m, b, beta * m->dt, f[0], f[1], f[2], s);
+    double *const *t = sw.swap ? f : g;
+    ct_update(m, b, sw.beta * m->dt, t[0], t[1], t[2], s);
   }
-  SWAP(m->u, m->u1);
-  SWAP(m->b1, m->bb1);
-  SWAP(m->b2, m->bb2);
-  SWAP(m->b3, m->bb3);
+  if (sw.swap) {
+    SWAP(m->u, m->u1);
+    SWAP(m->b1, m->bb1);
+    SWAP(m->b2, m->bb2);
+    SWAP(m->b3, m->bb3);
+  }
   /* SEND/RECV/SETB_HYD and _FLD, PROLONG, CONS2PRIM, PHY_BVAL */
   ml_exchange(m, m->u, NHYDRO, ml->ccons, m->b1, m->b2, m->b3);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -1495,7 +1475,7 @@ int orc_set_multilevel(orc_mesh *m, const int *nbr_table, const int *nbr_count,
   return 0;
 }
 
-void orc_set_rk1(orc_mesh *m, int on) { m->rk1 = on; }
+void orc_set_integrator(orc_mesh *m, int integrator) { m->integ = integrator; }
 
 /* ---- adaptive refinement ---------------------------------------------------------------- */
 

@@ -26,6 +26,10 @@ def build(force=False):
     return LIB
 
 
+# time/integrator values (athena_oracle.h ORC_VL2, ORC_RK2, ORC_RK1)
+INTEGRATORS = {"vl2": 0, "rk2": 1, "rk1": 2}
+
+
 class Params(ctypes.Structure):
     _fields_ = [("nbx1", ctypes.c_int), ("nbx2", ctypes.c_int), ("nbx3", ctypes.c_int),
                 ("nx1", ctypes.c_int), ("nx2", ctypes.c_int), ("nx3", ctypes.c_int),
@@ -73,7 +77,7 @@ def lib():
         L.orc_set_multilevel.argtypes = [ctypes.c_void_p, ip, ip, ip,
                                          ctypes.POINTER(ctypes.c_longlong)] + [dp] * 6
         L.orc_set_multilevel.restype = ctypes.c_int
-        L.orc_set_rk1.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_set_integrator.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_advance.argtypes = [ctypes.c_void_p]
         L.orc_new_dt.argtypes = [ctypes.c_void_p]
         L.orc_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double]
@@ -94,12 +98,12 @@ class OracleMesh:
 
     def __init__(self, mesh, gamma, xorder=2, rsolver="hlld", cfl=0.3, tlim=1e30,
                  dfloor=None, pfloor=None, relativistic=False, threads=0, sigma_max=0.0,
-                 beta_min=0.0, gamma_max=1000.0, bc=(0, 0, 0, 0, 0, 0)):
+                 beta_min=0.0, gamma_max=1000.0, bc=(0, 0, 0, 0, 0, 0), integrator="vl2"):
         L = lib()
         self.kw = dict(gamma=gamma, xorder=xorder, rsolver=rsolver, cfl=cfl, tlim=tlim,
                        dfloor=dfloor, pfloor=pfloor, relativistic=relativistic,
                        threads=threads, sigma_max=sigma_max, beta_min=beta_min,
-                       gamma_max=gamma_max, bc=bc)
+                       gamma_max=gamma_max, bc=bc, integrator=integrator)
         import math
         fmin = float(np.finfo(np.float32).tiny)
         floor = math.sqrt(1024 * fmin)   # adiabatic_mhd.cpp:29-30
@@ -119,6 +123,7 @@ class OracleMesh:
                         beta_min, gamma_max, (ctypes.c_int * 6)(*bc), ppmf)
         self.coords = [np.ascontiguousarray(c) for c in mesh.coordinate_arrays()]
         self.h = L.orc_create(ctypes.byref(self.p), *[_p(c) for c in self.coords])
+        L.orc_set_integrator(self.h, INTEGRATORS[integrator])
         if multilevel:
             t, cnt, lv, loc = mesh.neighbor_table()
             self._ml = [np.ascontiguousarray(a) for a in (t, cnt, lv, loc)]

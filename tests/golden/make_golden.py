@@ -77,7 +77,15 @@ CASES = {
                                               (.5, .5, .5)), "blast", 2, 0.3, 4),
     "blastbc_hlle_ppm_1blk": ("mhd_hlle_g3", ((16, 16, 16), (1, 1, 1), 3, (-.5, -.5, -.5),
                                               (.5, .5, .5)), "blast", 3, 0.3, 4),
+    # time/integrator = rk2 (Heun / SSPRK(2,2), time_integrator.cpp:338-465)
+    "turbrk2_hlld_plm_8blk": ("mhd_hlld_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                              (1., 1., 1.)), "turbulence", 2, 0.6, 3),
+    "blastrk2_hlle_ppm_8blk": ("mhd_hlle_g3", ((16, 16, 16), (2, 2, 2), 3, (-.5, -.5, -.5),
+                                               (.5, .5, .5)), "blast", 3, 0.4, 3),
 }
+# time/integrator of the cases that do not use vl2
+INTEGRATOR = {"turbrk2_hlld_plm_8blk": "rk2", "blastrk2_hlle_ppm_8blk": "rk2",
+              "mlblastrk2_hlle_plm": "rk2"}
 # mesh-face boundary flags of the cases that are not periodic
 BCS = {"blastbc_hlld_plm_8blk": (1, 1, 2, 2, 0, 0),
        "blastbc_hlle_ppm_1blk": (2, 1, 1, 2, 2, 1)}
@@ -100,6 +108,12 @@ ML_CASES = {
                                            (.5, .5, .5), (1, 1, 2, 2, 1, 1),
                                            [((0.3, 0.3, 0.3), (0.35, 0.35, 0.35), 2)]),
                            "smooth", {"seed": 11}, 2, 0.3, 4),
+    "mlblastrk2_hlle_plm": ("mhd_hlle_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                            (.5, .5, .5), (1, 1, 0, 0, 2, 2),
+                                            [((-0.2, 0.1, -0.2), (-0.1, 0.2, -0.1), 1)]),
+                            "blast", {"radius": 0.15, "pamb": 0.1, "prat": 100.0,
+                                      "b0": 1.0, "angle": 30.0, "x1_0": -0.2,
+                                      "x2_0": 0.2, "x3_0": -0.1}, 2, 0.5, 5),
 }
 
 
@@ -251,12 +265,14 @@ def run_ml_case(name, spec):
                                prat=prob["prat"], b0=prob["b0"], angle_deg=prob["angle"],
                                center=(prob["x1_0"], prob["x2_0"], prob["x3_0"]))
         text = ref_run.athinput_multilevel(mesh, gamma, xorder, cfl, ncycle, 1.0e3, prob,
-                                           regions=regions)
+                                           regions=regions,
+                                           integrator=INTEGRATOR.get(name, "vl2"))
         d, _ = ref_run.run_reference(variant, "athena_blast", text)
     else:
         ic = pgen.smooth_blocks(mesh, gamma, seed=prob["seed"])
         text = ref_run.athinput_multilevel(mesh, gamma, xorder, cfl, ncycle, 1.0e3,
-                                           {"ic_file": "ic.bin"}, regions=regions)
+                                           {"ic_file": "ic.bin"}, regions=regions,
+                                           integrator=INTEGRATOR.get(name, "vl2"))
         d, _ = ref_run.run_reference(variant, "athena_blocks", text, blocks_ic=(mesh,) + ic)
     dts = []
     for c in range(1, ncycle + 1):
@@ -275,7 +291,8 @@ def run_ml_case(name, spec):
             "xmax": xmax, "bc": list(bcs), "regions": regs, "nblocks": mesh.nblocks,
             "levels": sorted(set(int(v) for v in mesh.levels)), "problem": problem,
             "xorder": xorder, "rsolver": variant.split("_")[1],
-            "cfl": cfl, "ncycle": ncycle, "gamma": gamma, "tlim": 1.0e3}
+            "cfl": cfl, "ncycle": ncycle, "gamma": gamma, "tlim": 1.0e3,
+            "integrator": INTEGRATOR.get(name, "vl2")}
 
 
 def global_ic(problem, mesh):
@@ -327,7 +344,8 @@ def run_case(name, spec):
         u0 = mesh.scatter_cells(gu)
         b10, b20, b30 = mesh.scatter_faces(g1, g2, g3)
         text = ref_run.athinput(mesh, gamma, xorder, cfl, ncycle, 1.0e3,
-                                {"ic_file": "ic.bin"}, bc=BCS.get(name, (0,) * 6))
+                                {"ic_file": "ic.bin"}, bc=BCS.get(name, (0,) * 6),
+                                integrator=INTEGRATOR.get(name, "vl2"))
         d, _ = ref_run.run_reference(variant, "athena_ic", text, ic=(0, gu, g1, g2, g3))
         tlim = 1.0e3
     dts = []
@@ -346,7 +364,8 @@ def run_case(name, spec):
             "relativistic": problem == "sr_kh",
             "xmin": mesh.xmin, "xmax": mesh.xmax, "problem": problem, "xorder": xorder,
             "rsolver": variant.split("_")[1], "cfl": cfl,
-            "ncycle": ncycle, "gamma": gamma, "tlim": tlim, "bc": list(BCS.get(name, (0,) * 6))}
+            "ncycle": ncycle, "gamma": gamma, "tlim": tlim, "bc": list(BCS.get(name, (0,) * 6)),
+            "integrator": INTEGRATOR.get(name, "vl2")}
 
 
 def run_config1():

@@ -16,7 +16,8 @@ def test_oracle_matches_reference_bitwise(name):
     c, mesh, ic, ref = load_case(name)
     om = O.OracleMesh(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
                       cfl=c["cfl"], tlim=c["tlim"], relativistic=c.get("relativistic", False),
-                      bc=tuple(c.get("bc", (0,) * 6)))
+                      bc=tuple(c.get("bc", (0,) * 6)),
+                      integrator=c.get("integrator", "vl2"))
     om.set_state(*ic)
     if "ic_w" in c:
         om.set_prim(c["ic_w"])

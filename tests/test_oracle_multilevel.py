@@ -19,7 +19,7 @@ from golden_cases import load_ml_case, ml_case_names
 def test_oracle_multilevel_matches_reference_bitwise(name):
     c, mesh, ic, ref = load_ml_case(name)
     om = O.OracleMesh(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
-                      cfl=c["cfl"], tlim=c["tlim"])
+                      cfl=c["cfl"], tlim=c["tlim"], integrator=c.get("integrator", "vl2"))
     om.set_state(*ic)
     om.initialize()
     dts = []
