@@ -27,6 +27,8 @@ UNITS = {
     "sr_learned.cu": ["-fmad=false"],
     "selftest.cu": ["-fmad=false"],
     "history.cu": ["-fmad=false"],
+    # div B diagnostic (the reference's per-cell arithmetic) and run statistics
+    "diagnostics.cu": ["-fmad=false"],
     # host planner of the multi-level stage
     "ml_plan.cu": ["-fmad=false"],
     # adaptive refinement: refinement measure and regrid (FP64 restriction/prolongation)

@@ -80,7 +80,8 @@ void free_all(athgpu_ctx* c) {
   void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.cce, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
-                  c->nbr, c->staging, c->c2p_queue, c->c2p_qcount, c->fxv, c->eps_buf};
+                  c->nbr, c->staging, c->c2p_queue, c->c2p_qcount, c->fxv, c->eps_buf,
+                  c->c2p_qstart, c->c2p_net, c->c2p_net_err};
   // the context's device memory returns to the stream-ordered pool (pool_alloc)
   cudaStream_t s = c->own_stream;
   if (s) cudaStreamSynchronize(c->stream ? c->stream : s);
@@ -175,6 +176,13 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "coordinate arrays are required");
   if (!(d->gamma > 1.0) || !(d->cfl_number > 0.0))
     return fail(ATHGPU_ERR_ARG, "gamma must exceed 1 and cfl_number be positive");
+  if (d->integrator != ATHGPU_VL2 && d->integrator != ATHGPU_RK2)
+    return fail(ATHGPU_ERR_ARG, "unknown integrator (ATHGPU_VL2 or ATHGPU_RK2)");
+  // the integrator's CFL limit in 3-D (time_integrator.cpp:219-222, 445, checked at
+  // :894-900)
+  if (d->cfl_number > (d->integrator == ATHGPU_RK2 ? 1.0 : 0.5))
+    return fail(ATHGPU_ERR_ARG, "cfl_number exceeds the integrator's limit (0.5 for vl2, "
+                                "1.0 for rk2 in 3-D)");
   for (int f = 0; f < 6; ++f) {
     if (d->bc[f] < ATHGPU_BC_PERIODIC || d->bc[f] > ATHGPU_BC_REFLECT)
       return fail(ATHGPU_ERR_ARG, "bc flags must be periodic (0), outflow (1) or reflecting (2)");
@@ -267,6 +275,14 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   // floors' rewrite of U (Newtonian)
   allocs.push_back({(void**)&c->c2p_queue, nb * m.nx1 * m.nx2 * m.nx3 * (i64)sizeof(int)});
   allocs.push_back({(void**)&c->c2p_qcount, (i64)sizeof(unsigned)});
+  if (d->relativistic) {
+    // the start pressure of each deferred SR solve, and the network start's error flag
+    allocs.push_back({(void**)&c->c2p_qstart, nb * m.nx1 * m.nx2 * m.nx3 * (i64)sizeof(double)});
+    allocs.push_back({(void**)&c->c2p_net_err, (i64)sizeof(int)});
+  }
+  // the FP32 path starts the SR solve from the stale pressure refined in FP32, the FP64
+  // path from the stale pressure itself (the reference's start)
+  c->c2p_start = rb == 4 ? C2P_START_REFINED : C2P_START_STALE;
   for (auto& a : allocs) {
     e = pool_alloc(a.p, a.bytes, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync"));
@@ -371,6 +387,7 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.nbr = c->nbr;
 
   DevClock hclk;
+  memset(&hclk, 0, sizeof(hclk));
   hclk.dt = DBL_MAX;  // mesh.cpp:100
   hclk.time = 0.0;
   double dmax = DBL_MAX;
@@ -721,6 +738,41 @@ athgpu_status athgpu_device_state_ptrs(athgpu_ctx* c, athgpu_device_state* out) 
   out->b2 = c->r.b2;
   out->b3 = c->r.b3;
   out->real_bytes = c->real_bytes;
+  return ATHGPU_OK;
+}
+
+static_assert(ATHGPU_C2P_START_STALE == C2P_START_STALE &&
+                  ATHGPU_C2P_START_REFINED == C2P_START_REFINED &&
+                  ATHGPU_C2P_START_NETWORK == C2P_START_NETWORK,
+              "con2prim start codes out of date");
+
+athgpu_status athgpu_set_c2p_start(athgpu_ctx* c, int start, const float* params) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (!c->desc.relativistic)
+    return fail(ATHGPU_ERR_UNSUPPORTED, "the con2prim start applies to relativistic MHD");
+  if (start != ATHGPU_C2P_START_STALE && start != ATHGPU_C2P_START_REFINED &&
+      start != ATHGPU_C2P_START_NETWORK)
+    return fail(ATHGPU_ERR_ARG, "unknown con2prim start");
+  if (start == ATHGPU_C2P_START_NETWORK) {
+    if (!params) return fail(ATHGPU_ERR_ARG, "the network start needs the parameters");
+    if (!c->c2p_net) {
+      cudaError_t e = pool_alloc((void**)&c->c2p_net, sizeof(float) * ATHGPU_MLP_NPARAM,
+                                 c->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync network");
+    }
+    // host or device memory (unified addressing)
+    CK(cudaMemcpyAsync(c->c2p_net, params, sizeof(float) * ATHGPU_MLP_NPARAM,
+                       cudaMemcpyDefault, c->stream));
+    CK(cudaMemsetAsync(c->c2p_net_err, 0, sizeof(int), c->stream));
+  }
+  c->c2p_start = start;
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->cycle_exec) {  // re-capture with the new con2prim kernel
+    cudaGraphExecDestroy(c->cycle_exec);
+    c->cycle_exec = nullptr;
+    cudaGraphDestroy(c->cycle_graph);
+    c->cycle_graph = nullptr;
+  }
   return ATHGPU_OK;
 }
 

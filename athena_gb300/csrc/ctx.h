@@ -75,6 +75,12 @@ struct athgpu_ctx {
   double* staging = nullptr;  // device staging of FP64 host data in FP32 mode
   int* c2p_queue = nullptr;      // SR con2prim: interior cells deferred to phase 2
   unsigned* c2p_qcount = nullptr;
+  double* c2p_qstart = nullptr;  // SR con2prim: the start pressure of each queued cell
+  // SR con2prim start (athgpu_set_c2p_start): C2P_START_STALE / _REFINED / _NETWORK, the
+  // network's parameters (device, ATHGPU_MLP_NPARAM floats) and its tensor-core error flag
+  int c2p_start = 0;
+  float* c2p_net = nullptr;
+  int* c2p_net_err = nullptr;
   // per-kernel timing of one non-graph cycle (athgpu_profile_cycle)
   bool profiling = false;
   std::vector<std::string> prof_names;

@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "physics.cuh"
+#include "c2p_net.cuh"
 
 namespace athgpu {
 
@@ -78,6 +79,10 @@ struct DevClock {
   float dtf;                      // dt rounded to FP32 (written with dt)
   double dt_prev;                 // the dt of the last completed cycle
   unsigned long long dtmin_prev_bits;  // the minimum the last NewTimeStep used
+  // relativistic con2prim statistics since the last reset (athgpu_stats): cells solved,
+  // FP64 Newman-Hamlin passes over all attempts, cells re-solved from the reference's
+  // start after their own start failed, cells left unconverged
+  unsigned long long sr_cells, sr_passes, sr_fallbacks, sr_unconverged;
 };
 
 // The mesh scalars, coordinates and dt in the kernel's arithmetic type: the FP64 kernels
@@ -290,11 +295,16 @@ __device__ __forceinline__ bool ml_face_override(const DevMesh& m, int b, int fi
 // adds (A3*F3(k+1) - A3*F3(k)) and applies u_out = u_in - wght*dflx/vol.  So no flux
 // array is stored.  Cartesian areas and volumes, coordinates.cpp:448-548.
 struct UpdateArgs {
-  double beta;            // stage weight (time_integrator.cpp:216-217)
+  double beta;            // stage weight (time_integrator.cpp:216-217 vl2, :441-444 rk2)
   int stage;
   const void* uin;        // U^n
   void* uout;             // U* (stage 1) or U^n+1 (stage 2; may alias uin)
   void* ulo;              // compensation of U (FP32 path)
+  // rk2 stage 2: the register average u = g1*U* + g2*U^n (WeightedAve with gamma =
+  // (1/2, 1/2, 0), weighted_ave.cpp:161-230) before the flux divergence; NULL otherwise
+  // (vl2's gamma = (0, 1, 0) is a register swap)
+  const void* uavg;
+  double g1, g2;
 };
 
 // x1 sweep: rows (b, k in [ks-1,ke+1], j in [js-1,je+1]) of cells i in [is-1, ie+1],
@@ -473,6 +483,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   const Real* uin = (const Real*)ua.uin;
   Real* uout = (Real*)ua.uout;
   Real* ulo = (Real*)ua.ulo;
+  const Real* uavg = (const Real*)ua.uavg;
   for (int s = c0; s <= c1 + 1; ++s) {
     const int rel0 = s - R - cfirst;  // window = cells s-R..s+R
     const bool upd = s > c0 && interior;  // this step finishes cell s-1
@@ -540,10 +551,20 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
           Real d = aux[n * bd];
           d += (area * fn[n] - area * fprev[n]);
           if (KAHAN == 0) {
-            uout[cc] = aux[(NHYDRO + n) * bd] - wght * d / vol;
+            Real base = aux[(NHYDRO + n) * bd];
+            if (uavg) base = (Real)ua.g1 * uavg[cc] + (Real)ua.g2 * base;
+            uout[cc] = base - wght * d / vol;
           } else {
             const Real du = -(wght * d / vol);
-            const Real hi = aux[(NHYDRO + n) * bd], lw = aux[(2 * NHYDRO + n) * bd];
+            Real hi = aux[(NHYDRO + n) * bd], lw = aux[(2 * NHYDRO + n) * bd];
+            if (uavg) {
+              // g1*U* + g2*(hi + lw) as a new (hi, lw) pair: the products are exact
+              // (g = 1/2), their sum's rounding error is recovered (two-sum) into lw
+              const Real a = (Real)ua.g1 * uavg[cc], c = (Real)ua.g2 * hi;
+              const Real sum = a + c, bv = sum - a;
+              lw = ((a - (sum - bv)) + (c - bv)) + (Real)ua.g2 * lw;
+              hi = sum;
+            }
             if (ua.stage == 1) {
               uout[cc] = hi + (lw + du);
             } else {
@@ -745,9 +766,10 @@ __device__ __forceinline__ double edge_value(const DevMesh& m, const Real* __res
   return widen(edge_avg<Real, C>(m, e, b, k, j, i));
 }
 
-// Field::CT, field/ct.cpp:31-116, plus the VL2 register average (weighted_ave.cpp),
-// which for VL2 reduces to out = in on the first stage and an in-place update on the
-// second.  blockIdx.y is the MeshBlock; the CTA computes the block's (wght/area) factors
+// Field::CT, field/ct.cpp:31-116, plus the register average (weighted_ave.cpp), which
+// for VL2 and the first RK2 stage reduces to out = in and an in-place update on the
+// second VL2 stage; on the second RK2 stage the face starts from g1*B* + g2*B^n (bavg =
+// B*, bin = B^n; NULL bavg: no average).  blockIdx.y is the MeshBlock; the CTA computes the block's (wght/area) factors
 // once (areas and edge lengths are constant on a uniform block).  A thread owns the cell
 // point (k,j,i) of [ks,ke+1]x[js,je+1]x[is,ie+1] and updates the faces whose lower corner
 // it is: x1 face (k,j,i) for j<=je, k<=ke; x2 face for i<=ie, k<=ke; x3 face for i<=ie,
@@ -762,7 +784,9 @@ __global__ void __launch_bounds__(256)
 ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
           const Real* __restrict__ e1, const Real* __restrict__ e2,
           const Real* __restrict__ e3, const double* b1in, const double* b2in,
-          const double* b3in, double* b1out, double* b2out, double* b3out) {
+          const double* b3in, double* b1out, double* b2out, double* b3out,
+          const double* b1avg, const double* b2avg, const double* b3avg, double g1,
+          double g2) {
   const int b = blockIdx.y;
   const double* dx1f = m.dx1f + (i64)b * m.nc1;
   const double* dx2f = m.dx2f + (i64)b * m.nc2;
@@ -802,6 +826,7 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   if (f1) {
     const i64 o = f1idx(m, b, k, j, i);
     double v = b1in[o];
+    if (b1avg) v = g1 * b1avg[o] + g2 * v;
     v -= term(q[0], l3, ql[0], edge_value<Real, 2>(m, e3, b, k, j + 1, i), e3c);
     v += term(q[0], l2, ql[1], edge_value<Real, 1>(m, e2, b, k + 1, j, i), e2c);
     b1out[o] = v;
@@ -809,6 +834,7 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   if (f2) {
     const i64 o = f2idx(m, b, k, j, i);
     double v = b2in[o];
+    if (b2avg) v = g1 * b2avg[o] + g2 * v;
     v += term(q[1], l3, ql[2], edge_value<Real, 2>(m, e3, b, k, j, i + 1), e3c);
     v -= term(q[1], l1, ql[3], edge_value<Real, 0>(m, e1, b, k + 1, j, i), e1c);
     b2out[o] = v;
@@ -816,6 +842,7 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   if (f3) {
     const i64 o = f3idx(m, b, k, j, i);
     double v = b3in[o];
+    if (b3avg) v = g1 * b3avg[o] + g2 * v;
     v -= term(q[2], l2, ql[4], edge_value<Real, 1>(m, e2, b, k, j, i + 1), e2c);
     v += term(q[2], l1, ql[5], edge_value<Real, 0>(m, e1, b, k, j + 1, i), e1c);
     b3out[o] = v;
@@ -1147,76 +1174,127 @@ c2p_floor_writeback_kernel(DevMesh m, const double* __restrict__ b1,
 // interior cells, in FP64: the Newman-Hamlin solve of every cell is seeded from the output
 // array's previous contents (wout holds the primitives of two con2prim calls ago, the
 // reference's w1 register, :143-154 and time_integrator.cpp:2221-2269).  In FP32 mode the
-// conserved input is hi + lo, a re-synced conserved state is split back, and (REFINE) the
-// stale pressure is first refined by FP32 iterations of the same scheme, which the FP64
-// solve then finishes.  When do_dt is set the interior cells contribute
-// min(dx1, dx2, dx3) to the CFL reduction (the SR branch of new_blockdt.cpp:74 keeps the
-// widths: signal speed 1).
+// conserved input is hi + lo and a re-synced conserved state is split back.  When do_dt
+// is set the interior cells contribute min(dx1, dx2, dx3) to the CFL reduction (the SR
+// branch of new_blockdt.cpp:74 keeps the widths: signal speed 1).
+//
+// The start of the FP64 solve (START):
+//   C2P_START_STALE    the stale pressure, the reference's start (the FP64 path);
+//   C2P_START_REFINED  the stale pressure refined by FP32 iterations of the same scheme;
+//   C2P_START_NETWORK  the con2prim network's pressure for the cell (BF16 tcgen05
+//                      evaluation of the CTA's 128 cells, c2p_net.cuh), refined in FP32.
+// A start other than the stale pressure that does not converge within the reference's 15
+// passes is followed by the reference's own solve from the stale pressure (sr_c2p_cell).
 //
 // Warp-coherent two-phase schedule: the iteration count varies from cell to cell and a
-// warp runs as long as its slowest lane, so phase 1 (queue != null on input, phase == 1)
-// caps the first solve at max_first passes and appends each cell still iterating to the
-// queue; phase 2 runs the whole con2prim of the queued cells (grid-stride over the
-// count).  The solve is deterministic, so the result equals one uncapped pass.  Ghost
-// cells are not solved: a ghost's primitives equal its owner's (same conserved state, same
-// stale guess, both kept equal since initialization), so copy_ghost_prims_kernel copies
-// them afterwards.
-template <typename Real, int KAHAN, int REFINE>
+// warp runs as long as its slowest lane, so phase 1 caps the first solve at max_first
+// passes and appends each cell still iterating to the queue (with its start pressure in
+// qstart); phase 2 runs the whole con2prim of the queued cells again from that start
+// (grid-stride over the count).  The solve is deterministic, so the result equals one
+// uncapped pass.  Ghost cells are not solved: a ghost's primitives equal its owner's (same
+// conserved state, same stale guess, both kept equal since initialization), so
+// copy_ghost_prims_kernel copies them afterwards.  Every finished cell adds to the
+// con2prim statistics of the clock (warp-aggregated).
+constexpr int C2P_START_STALE = 0, C2P_START_REFINED = 1, C2P_START_NETWORK = 2;
+
+template <typename Real, int KAHAN, int START>
 __global__ void __launch_bounds__(128)
 c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
               const double* __restrict__ b2, const double* __restrict__ b3, Real* u,
               Real* ulo, Real* __restrict__ wout, Real* __restrict__ bcc,
               Real* __restrict__ cc, DevClock* clk, int phase, int max_first,
-              int* __restrict__ queue, unsigned* __restrict__ qcount) {
+              int* __restrict__ queue, unsigned* __restrict__ qcount,
+              double* __restrict__ qstart, const float* __restrict__ net,
+              int* __restrict__ net_err) {
   const int n1 = m.nx1, n2 = m.nx2, n3 = m.nx3;
   const long long ninterior = (long long)m.nb * n1 * n2 * n3;
   long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long count = phase == 1 ? ninterior : (long long)*qcount;
+  // the network's operands in shared memory (phase 1 of the network start only)
+  extern __shared__ __align__(128) unsigned char c2p_smem[];
+  c2pnet::TcNet& tnet = *reinterpret_cast<c2pnet::TcNet*>(c2p_smem);
+  const bool with_net = START == C2P_START_NETWORK && phase == 1;
+  if (with_net) c2pnet::tc_setup(net, tnet);
   // phase 1 runs one pass over the cells (with the CTA-wide dt reduction at the end);
   // phase 2 strides over the queue
   for (; phase == 2 ? e < count : true; e += stride) {
     double cell_dt = 1.0e300;
-    bool enqueue = false;
+    bool enqueue = false, finished = false, fell_back = false, failed = false;
+    int passes = 0;
     long long t = -1;
     if (e < count) t = phase == 1 ? e : (long long)queue[e];
+    int b = 0, i = 0, j = 0, k = 0;
+    double bc1 = 0.0, bc2 = 0.0, bc3 = 0.0;
+    double cons[NHYDRO] = {1.0, 0.0, 0.0, 0.0, 2.0}, prim[NHYDRO];
+    i64 c = 0, cb = 0;
+    const i64 vs = m.ncell;
     if (t >= 0) {
-      const int b = (int)(t / ((long long)n1 * n2 * n3));
+      b = (int)(t / ((long long)n1 * n2 * n3));
       int r = (int)(t - (long long)b * n1 * n2 * n3);
-      const int i = m.is + r % n1;
+      i = m.is + r % n1;
       r /= n1;
-      const int j = m.js + r % n2;
-      const int k = m.ks + r / n2;
+      j = m.js + r % n2;
+      k = m.ks + r / n2;
       const double lw = 0.5, rw = 0.5;
-      const double bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
-      const double bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
-      const double bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
-      const i64 vs = m.ncell;
-      const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
-      const i64 cb = cidx(m, b, 0, 3, k, j, i);
-      double cons[NHYDRO], prim[NHYDRO];
+      bc1 = lw * b1[f1idx(m, b, k, j, i)] + rw * b1[f1idx(m, b, k, j, i + 1)];
+      bc2 = lw * b2[f2idx(m, b, k, j, i)] + rw * b2[f2idx(m, b, k, j + 1, i)];
+      bc3 = lw * b3[f3idx(m, b, k, j, i)] + rw * b3[f3idx(m, b, k + 1, j, i)];
+      c = cidx(m, b, 0, NHYDRO, k, j, i);
+      cb = cidx(m, b, 0, 3, k, j, i);
 #pragma unroll
       for (int n = 0; n < NHYDRO; ++n) {
         cons[n] = (double)u[c + n * vs] + ((KAHAN && ulo) ? (double)ulo[c + n * vs] : 0.0);
         prim[n] = (double)wout[c + n * vs];
       }
-      double pstart = 0.0;
-      if (REFINE) {  // the stale pressure refined in FP32 (raw conserved state)
-        const double mm_sq = cons[IVX] * cons[IVX] + cons[IVY] * cons[IVY] +
-                             cons[IVZ] * cons[IVZ];
-        const double bb_sq = bc1 * bc1 + bc2 * bc2 + bc3 * bc3;
-        const double tt = cons[IVX] * bc1 + cons[IVY] * bc2 + cons[IVZ] * bc3;
-        int it32;
-        pstart = sr_refine_f32(fp.gamma_adi, cons[IDN], cons[IPR], mm_sq, bb_sq, tt,
-                               smax(prim[IPR], fp.pfloor), 12, 1.0e-6f, &it32);
+    }
+    double pstart = 0.0;
+    if (START != C2P_START_STALE) {
+      const double mm_sq = cons[IVX] * cons[IVX] + cons[IVY] * cons[IVY] +
+                           cons[IVZ] * cons[IVZ];
+      const double bb_sq = bc1 * bc1 + bc2 * bc2 + bc3 * bc3;
+      const double tt = cons[IVX] * bc1 + cons[IVY] * bc2 + cons[IVZ] * bc3;
+      if (phase == 2) {
+        pstart = qstart[e];  // the start phase 1 used
+      } else if (START == C2P_START_REFINED) {
+        if (t >= 0) {
+          int it32;
+          pstart = sr_refine_f32(fp.gamma_adi, cons[IDN], cons[IPR], mm_sq, bb_sq, tt,
+                                 smax(prim[IPR], fp.pfloor), 12, 1.0e-6f, &it32);
+        }
+      } else {
+        // every thread of the CTA takes part in the tensor-core evaluation (a thread
+        // without a cell evaluates the network on a dummy state)
+        float f[c2pnet::NIN], xin[c2pnet::NIN], y[c2pnet::NOUT];
+        const double uu[5] = {cons[IDN], cons[IVX], cons[IVY], cons[IVZ], cons[IPR]};
+        const double bb[3] = {bc1, bc2, bc3};
+        c2pnet::features(uu, bb, f);
+#pragma unroll
+        for (int q = 0; q < c2pnet::NIN; ++q) xin[q] = (f[q] - tnet.xm[q]) / tnet.xs[q];
+        uint32_t ph = 0;
+        c2pnet::tc_infer_tile(tnet, xin, y, ph, net_err);
+        c2pnet::tc_teardown(tnet);
+        if (t >= 0) {
+          int it32;
+          double guess = cons[IPR] * (double)__expf(y[0]);
+          if (!(guess > fp.pfloor)) guess = smax(prim[IPR], fp.pfloor);  // NaN: no result
+          pstart = sr_refine_f32(fp.gamma_adi, cons[IDN], cons[IPR], mm_sq, bb_sq, tt, guess,
+                                 12, 1.0e-6f, &it32);
+        }
       }
+      if (!(pstart > fp.pfloor)) pstart = smax(prim[IPR], fp.pfloor);
+    }
+    if (t >= 0) {
       bool fixed = false, deferred = false;
       int it = 0;
       const bool ok = sr_c2p_cell(fp, cons, bc1, bc2, bc3, prim, &fixed, &it, pstart,
-                                  phase == 1 ? max_first : 15, &deferred);
+                                  phase == 1 ? max_first : 15, &deferred, &passes,
+                                  &fell_back);
       if (deferred) {
         enqueue = true;
       } else {
+        finished = true;
+        failed = !ok;
 #pragma unroll
         for (int n = 0; n < NHYDRO; ++n) wout[c + n * vs] = (Real)prim[n];
         bcc[cb] = (Real)bc1;
@@ -1240,7 +1318,29 @@ c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
         cell_dt = smin<double>(smin<double>(dt1, dt2), dt3);
       }
     }
-    if (phase == 2) continue;
+    if (phase == 2) {  // statistics of the queued cells: per thread (few cells)
+      if (finished) {
+        atomicAdd(&clk->sr_cells, 1ull);
+        atomicAdd(&clk->sr_passes, (unsigned long long)passes);
+        if (fell_back) atomicAdd(&clk->sr_fallbacks, 1ull);
+        if (failed) atomicAdd(&clk->sr_unconverged, 1ull);
+      }
+      continue;
+    }
+    // phase 1 (every lane runs this body once): statistics of the cells finished here,
+    // one atomic per counter and warp
+    {
+      const unsigned nfin = __popc(__ballot_sync(0xffffffffu, finished));
+      const unsigned psum = __reduce_add_sync(0xffffffffu, finished ? (unsigned)passes : 0u);
+      const unsigned nfb = __popc(__ballot_sync(0xffffffffu, finished && fell_back));
+      const unsigned nfail = __popc(__ballot_sync(0xffffffffu, failed));
+      if ((threadIdx.x & 31) == 0 && nfin) {
+        atomicAdd(&clk->sr_cells, (unsigned long long)nfin);
+        atomicAdd(&clk->sr_passes, (unsigned long long)psum);
+        if (nfb) atomicAdd(&clk->sr_fallbacks, (unsigned long long)nfb);
+        if (nfail) atomicAdd(&clk->sr_unconverged, (unsigned long long)nfail);
+      }
+    }
     // phase 1: warp-aggregated append of the deferred cells, then the dt reduction
     const unsigned mask = __ballot_sync(0xffffffffu, enqueue);
     if (mask) {
@@ -1248,7 +1348,11 @@ c2p_sr_kernel(DevMesh m, SRFloors fp, int do_dt, const double* __restrict__ b1,
       unsigned base = 0;
       if (lane == leader) base = atomicAdd(qcount, (unsigned)__popc(mask));
       base = __shfl_sync(0xffffffffu, base, leader);
-      if (enqueue) queue[base + __popc(mask & ((1u << lane) - 1u))] = (int)t;
+      if (enqueue) {
+        const unsigned slot = base + __popc(mask & ((1u << lane) - 1u));
+        queue[slot] = (int)t;
+        if (START != C2P_START_STALE) qstart[slot] = pstart;
+      }
     }
     if (do_dt) cta_min_to_clock<double>(cell_dt, clk);
     break;

@@ -989,10 +989,17 @@ struct SRFloors { double gamma_adi, dfloor, pfloor, sigma_max, beta_min, gamma_m
 // caps the first solve: a cell that has not converged by then returns with *deferred set
 // and prim, cons untouched, to be solved again in full by a later pass (the solve is
 // deterministic, so the result is the same as one uncapped call).
+//
+// When the first solve starts from pstart and fails within the reference's 15 passes, the
+// cell is solved again from the reference's own start, the stale pressure (*fallback_out
+// set): the reference's solve is the per-cell fallback of any other start.  *passes_out
+// (may be NULL) receives the FP64 loop passes of every solve the cell ran.
 __device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, double bc1,
                                             double bc2, double bc3, double* prim,
                                             bool* fixed_out, int* iters, double pstart = 0.0,
-                                            int max_first = 15, bool* deferred = nullptr) {
+                                            int max_first = 15, bool* deferred = nullptr,
+                                            int* passes_out = nullptr,
+                                            bool* fallback_out = nullptr) {
   const double gamma_adi = fp.gamma_adi;
   const double mm_sq_ee_sq_max = 1.0 - 1.0e-12;
   double dd = cons[IDN], ee = cons[IPR];
@@ -1025,6 +1032,15 @@ __device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, do
     *fixed_out = false;
     return false;
   }
+  int passes = *iters < 15 ? *iters + 1 : 15;
+  if (!success && pstart > 0.0) {  // the reference's start, the stale pressure
+    int it_ref;
+    success = sr_normal_t<double>(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2,
+                                  bc3, tt, pgas_old, prim, &gamma, &pmag, &it_ref, 15,
+                                  1.0e-12, false);
+    passes += it_ref < 15 ? it_ref + 1 : 15;
+    if (fallback_out) *fallback_out = true;
+  }
   if (!success) {
     prim[IDN] = rho_old; prim[IPR] = pgas_old;
     prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;
@@ -1043,6 +1059,7 @@ __device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, do
     int it2;
     success = sr_normal(gamma_adi, dd, ee, mm_sq, mm1, mm2, mm3, bb_sq, bc1, bc2, bc3, tt,
                         pgas_old, prim, &gamma, &pmag, &it2);
+    passes += it2 < 15 ? it2 + 1 : 15;
     if (!success) {
       prim[IDN] = rho_old; prim[IPR] = pgas_old;
       prim[IVX] = u1_old; prim[IVY] = u2_old; prim[IVZ] = u3_old;
@@ -1093,6 +1110,7 @@ __device__ __forceinline__ bool sr_c2p_cell(const SRFloors& fp, double* cons, do
     cons[IVZ] = wtot * gamma * u3 - b0 * b3;
   }
   *fixed_out = fixed;
+  if (passes_out) *passes_out = passes;
   return success;
 }
 

@@ -248,9 +248,9 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
   if (desc->nbx2 != 1 || desc->nbx3 != 1 || desc->nx1 != od.nx1 || desc->nx2 != od.nx2 ||
       desc->nx3 != od.nx3 || desc->nghost != od.nghost || desc->precision != od.precision ||
       desc->xorder != od.xorder || desc->ppm_fast != od.ppm_fast ||
-      desc->rsolver != od.rsolver || desc->relativistic)
+      desc->rsolver != od.rsolver || desc->relativistic || desc->integrator != od.integrator)
     return api_fail(ATHGPU_ERR_ARG, "the new mesh must keep the block size, nghost, "
-                                       "precision and solver of the old one");
+                                       "precision, solver and integrator of the old one");
   for (int f = 0; f < 6; ++f)
     if (desc->bc[f] != od.bc[f])
       return api_fail(ATHGPU_ERR_ARG, "the new mesh must keep the boundary flags");

@@ -148,17 +148,34 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
     if (c->desc.relativistic) {
       SRFloors fp{c->desc.gamma, c->desc.dfloor, c->desc.pfloor, c->desc.sigma_max,
                   c->desc.beta_min, c->desc.gamma_max};
-      constexpr int REFINE = sizeof(Real) == 4;  // FP32 path: FP32-refined start
-      const int n1 = c->lc.sr_phase1 > 0 ? c->lc.sr_phase1 : (REFINE ? 5 : 7);
+      // the start of the FP64 solve (athgpu_set_c2p_start): 0 the stale pressure, 1 that
+      // pressure refined in FP32, 2 the network's pressure refined in FP32
+      const int start = c->c2p_start;
+      const int n1 = c->lc.sr_phase1 > 0 ? c->lc.sr_phase1 : (start ? 5 : 7);
       const long long ni = (long long)m.nb * m.nx1 * m.nx2 * m.nx3;
+      auto kern = start == C2P_START_NETWORK ? c2p_sr_kernel<Real, KAHAN, C2P_START_NETWORK>
+                  : start == C2P_START_REFINED ? c2p_sr_kernel<Real, KAHAN, C2P_START_REFINED>
+                                               : c2p_sr_kernel<Real, KAHAN, C2P_START_STALE>;
+      // the network start: its operands in shared memory, padded so that at most four
+      // CTAs (4 x 128 tensor-memory columns) share an SM
+      const int smem = start == C2P_START_NETWORK
+                           ? (int)sizeof(c2pnet::TcNet) + c2pnet::TC_SMEM_PAD : 0;
+      if (smem) {
+        static bool attr = false;  // opt in above 48 KB once per instantiation
+        if (!attr) {
+          cudaFuncSetAttribute(c2p_sr_kernel<Real, KAHAN, C2P_START_NETWORK>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+          attr = true;
+        }
+      }
       cudaMemsetAsync(c->c2p_qcount, 0, sizeof(unsigned), s);
-      c2p_sr_kernel<Real, KAHAN, REFINE><<<nblk(ni, 128), 128, 0, s>>>(
+      kern<<<nblk(ni, 128), 128, smem, s>>>(
           m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk,
-          1, n1, c->c2p_queue, c->c2p_qcount);
+          1, n1, c->c2p_queue, c->c2p_qcount, c->c2p_qstart, c->c2p_net, c->c2p_net_err);
       const long long g2 = nblk(ni, 128) < 2048 ? nblk(ni, 128) : 2048;
-      c2p_sr_kernel<Real, KAHAN, REFINE><<<g2, 128, 0, s>>>(
+      kern<<<g2, 128, 0, s>>>(
           m, fp, do_dt, b1, b2, b3, u, lo, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk,
-          2, 15, c->c2p_queue, c->c2p_qcount);
+          2, 15, c->c2p_queue, c->c2p_qcount, c->c2p_qstart, c->c2p_net, c->c2p_net_err);
       const long long ng = ((long long)m.ncell - (long long)m.nx1 * m.nx2 * m.nx3) * m.nb;
       copy_ghost_prims_kernel<Real><<<nblk(ng, 256), 256, 0, s>>>(
           m, wout, (Real*)c->r.bcc, (Real*)c->r.cce);
@@ -200,9 +217,16 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   const DevMesh& m = c->m;
   Registers& r = c->r;
   cudaStream_t s = c->stream;
+  // Stage weights of TimeIntegratorTaskList (time_integrator.cpp:111-236 vl2, :338-465
+  // rk2).  vl2: donor cell on stage 1, beta = 1/2, 1, register swaps; rk2: xorder on both
+  // stages, beta = 1, 1/2, and on stage 2 the register average g1*U* + g2*U^n.
+  const bool rk2 = c->desc.integrator == ATHGPU_RK2;
   // reconstruction template index: 1 DC, 2 PLM, 3 PPM, 4 fast PPM (time/xorder = 3f)
-  const int order = (stage == 1) ? 1 : c->desc.ppm_fast ? 4 : c->desc.xorder;
-  const double beta = (stage == 1) ? 0.5 : 1.0;
+  const int xo = c->desc.ppm_fast ? 4 : c->desc.xorder;
+  const int order = (stage == 1 && !rk2) ? 1 : xo;
+  const double beta = rk2 ? (stage == 1 ? 1.0 : 0.5) : (stage == 1 ? 0.5 : 1.0);
+  const bool avg = rk2 && stage == 2;
+  const double g1 = 0.5, g2 = 0.5;
   // stage 1 reads U^n, B^n and writes U*, B*; stage 2 reads W*, B* and updates U, B
   const double* bb1 = (stage == 1) ? r.b1 : r.bs1;
   const double* bb2 = (stage == 1) ? r.b2 : r.bs2;
@@ -220,6 +244,9 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   ua.uin = r.u;
   ua.uout = uout;
   ua.ulo = r.ulo;
+  ua.uavg = avg ? r.ustar : nullptr;
+  ua.g1 = g1;
+  ua.g2 = g2;
 #define FLUX(O, R) launch_fluxes<Real, O, R, KAHAN>(c, w, bcc, bb1, bb2, bb3, ua)
 #define FLUX_RS(O)                                                                   \
   do {                                                                               \
@@ -259,7 +286,9 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
     ProfScope ps(c, "ct");
     ct_kernel<Real><<<grid, 256, 0, s>>>(m, beta, c->clk, (const Real*)r.e1,
                                          (const Real*)r.e2, (const Real*)r.e3, r.b1, r.b2,
-                                         r.b3, o1, o2, o3);
+                                         r.b3, o1, o2, o3, avg ? r.bs1 : nullptr,
+                                         avg ? r.bs2 : nullptr, avg ? r.bs3 : nullptr, g1,
+                                         g2);
   }
   c->launches += 2;
   launch_exchange_and_c2p<Real, KAHAN>(c, uout, o1, o2, o3, stage == 2);

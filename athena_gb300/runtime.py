@@ -22,10 +22,21 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300.h")
 HLLD, HLLE, LLF, ROE = 0, 1, 2, 3
 _RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF, "roe": ROE}
 FP64, FP32 = 0, 1
+VL2, RK2 = 0, 1
+_INTEGRATORS = {"vl2": VL2, "rk2": RK2}
 
 
 class AthGPUError(RuntimeError):
     pass
+
+
+class RunStats(ctypes.Structure):
+    """athgpu_run_stats"""
+    _fields_ = [("divb_sum", ctypes.c_double), ("divb_max", ctypes.c_double),
+                ("divb_cells", ctypes.c_longlong), ("floor_cells", ctypes.c_longlong),
+                ("sr_cells", ctypes.c_longlong), ("sr_passes", ctypes.c_longlong),
+                ("sr_fallbacks", ctypes.c_longlong), ("sr_unconverged", ctypes.c_longlong),
+                ("net_error", ctypes.c_int)]
 
 
 class MeshDesc(ctypes.Structure):
@@ -44,7 +55,7 @@ class MeshDesc(ctypes.Structure):
                 ("dx3f", ctypes.POINTER(ctypes.c_double)),
                 ("sigma_max", ctypes.c_double), ("beta_min", ctypes.c_double),
                 ("gamma_max", ctypes.c_double), ("bc", ctypes.c_int * 6),
-                ("ppm_fast", ctypes.c_int)]
+                ("ppm_fast", ctypes.c_int), ("integrator", ctypes.c_int)]
 
 
 BC_PERIODIC, BC_OUTFLOW, BC_REFLECT = 0, 1, 2
@@ -172,12 +183,12 @@ class StageUpdate:
 
     def __init__(self, mesh: MeshSpec, gamma, xorder=2, rsolver="hlld", precision="fp64",
                  cfl=0.3, tlim=1.0e30, dfloor=None, pfloor=None, relativistic=False,
-                 sigma_max=0.0, beta_min=0.0, gamma_max=1000.0, bc=None):
+                 sigma_max=0.0, beta_min=0.0, gamma_max=1000.0, bc=None, integrator="vl2"):
         L = load_library()
         self.kw = dict(gamma=gamma, xorder=xorder, rsolver=rsolver, precision=precision,
                        cfl=cfl, tlim=tlim, dfloor=dfloor, pfloor=pfloor,
                        relativistic=relativistic, sigma_max=sigma_max, beta_min=beta_min,
-                       gamma_max=gamma_max, bc=bc)
+                       gamma_max=gamma_max, bc=bc, integrator=integrator)
         multilevel = hasattr(mesh, "neighbor_table")
         self._describe(mesh)
         h = ctypes.c_void_p()
@@ -210,6 +221,7 @@ class StageUpdate:
         d.pfloor = fl if k["pfloor"] is None else k["pfloor"]
         d.cfl_number, d.tlim = k["cfl"], k["tlim"]
         d.bc = (ctypes.c_int * 6)(*bc_codes(bc))
+        d.integrator = _INTEGRATORS[k["integrator"]]
         d.x1f, d.dx1f, d.x2f, d.dx2f, d.x3f, d.dx3f = [_dp(c) for c in self.coords]
         self.desc = d
         return d
@@ -363,6 +375,38 @@ class StageUpdate:
         out = np.zeros(len(self.HISTORY_NAMES))
         _check(load_library().athgpu_history(self.h, _dp(out)), "athgpu_history")
         return dict(zip(self.HISTORY_NAMES, out.tolist()))
+
+    def divb(self):
+        """The reference's |div B| diagnostic (WAbsDivergenceB): (sum over interior cells,
+        maximum, cells counted)."""
+        out = np.zeros(3)
+        _check(load_library().athgpu_divb(self.h, _dp(out)), "athgpu_divb")
+        return float(out[0]), float(out[1]), int(out[2])
+
+    def stats(self, reset=False):
+        """Run statistics (athgpu_stats) as a dict."""
+        st = RunStats()
+        _check(load_library().athgpu_stats(self.h, ctypes.byref(st), int(reset)),
+               "athgpu_stats")
+        return {name: getattr(st, name) for name, _ in RunStats._fields_}
+
+    C2P_STARTS = {"stale": 0, "refined": 1, "network": 2}
+
+    def set_c2p_start(self, start, params=None):
+        """Start of the relativistic con2prim solve: "stale" (the reference's), "refined"
+        (that pressure refined in FP32) or "network" (params: the network's
+        ATHGPU_MLP_NPARAM floats, a device tensor or a numpy array)."""
+        ptr = None
+        if params is not None:
+            if hasattr(params, "data_ptr"):
+                ptr = ctypes.c_void_p(params.data_ptr())
+            else:
+                self._net_host = np.ascontiguousarray(params, dtype=np.float32)
+                ptr = self._net_host.ctypes.data_as(ctypes.c_void_p)
+        L = load_library()
+        L.athgpu_set_c2p_start.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        _check(L.athgpu_set_c2p_start(self.h, self.C2P_STARTS[start], ptr),
+               "athgpu_set_c2p_start")
 
     def autotune(self, cycles=2):
         """Pick the x2/x3 sweep segment lengths by timing (state left unchanged);

@@ -75,7 +75,15 @@ typedef struct {
    * interface values with Mignone's limiter and no floors (time/floor_ppm_fast false);
    * needs xorder 3.  0 (the zero-initialized default): the standard PPM. */
   int ppm_fast;
+  /* time/integrator (task_list/time_integrator.cpp): ATHGPU_VL2 (0, the zero-initialized
+   * default: van Leer predictor-corrector, donor cell on stage 1, :111-236) or ATHGPU_RK2
+   * (Heun / SSPRK(2,2): xorder on both stages, stage weights beta = 1, 1/2 and the
+   * register average u = (u* + u^n)/2 on stage 2, :338-465).  cfl_number must not
+   * exceed the integrator's limit in 3-D (0.5 for vl2, 1.0 for rk2, :219-222, :445). */
+  int integrator;
 } athgpu_mesh_desc;
+#define ATHGPU_VL2 0
+#define ATHGPU_RK2 1
 #define ATHGPU_BC_PERIODIC 0
 #define ATHGPU_BC_OUTFLOW 1
 #define ATHGPU_BC_REFLECT 2
@@ -280,6 +288,27 @@ typedef struct {
 } athgpu_device_state;
 athgpu_status athgpu_device_state_ptrs(athgpu_ctx *ctx, athgpu_device_state *out);
 
+/* Start of the relativistic con2prim solve in the stage's W(U) (the Newman-Hamlin
+ * iteration of adiabatic_mhd_sr.cpp:404-522, seeded by the reference from the stale
+ * pressure, :143-154):
+ *   ATHGPU_C2P_START_STALE    the stale pressure (the reference's start; FP64 default);
+ *   ATHGPU_C2P_START_REFINED  the stale pressure refined by FP32 iterations of the same
+ *                             scheme (FP32 default);
+ *   ATHGPU_C2P_START_NETWORK  the con2prim network's pressure (see athgpu_mlp_infer_tc;
+ *                             BF16 tcgen05 evaluation of each 128-cell tile inside the
+ *                             W(U) kernel), refined in FP32; params = ATHGPU_MLP_NPARAM
+ *                             floats in host or device memory, copied into the context.
+ * Any start other than the stale pressure that does not converge within the reference's 15
+ * passes is followed by the reference's solve from the stale pressure, so the per-cell
+ * outcome is the reference's whenever its start converges; the results of the starts
+ * agree to the solver's tolerance (absolute 1e-12 on the pressure).  Relativistic contexts
+ * only.  No counterpart in the reference (the start is a solver detail there).
+ * Synchronous; the next athgpu_cycle captures its graph again. */
+#define ATHGPU_C2P_START_STALE 0
+#define ATHGPU_C2P_START_REFINED 1
+#define ATHGPU_C2P_START_NETWORK 2
+athgpu_status athgpu_set_c2p_start(athgpu_ctx *ctx, int start, const float *params);
+
 /* Launch tiling of the x2/x3 flux sweeps: faces per thread along the sweep (the
  * autotuner's knob); 0 = heuristic default. */
 athgpu_status athgpu_set_sweep_segment(athgpu_ctx *ctx, int seg_x2, int seg_x3);
@@ -291,6 +320,37 @@ athgpu_status athgpu_set_sweep_segment(athgpu_ctx *ctx, int seg_x2, int seg_x3);
  * reference's sequential sum).  Synchronous. */
 #define ATHGPU_NHISTORY 11
 athgpu_status athgpu_history(athgpu_ctx *ctx, double *out);
+
+/* |div B| diagnostic of the face field (the reference's history diagnostic
+ * WAbsDivergenceB, pgen/field_loop_poles.cpp:634-672): over the interior cells of all
+ * MeshBlocks, |(sum over faces of +-area * B_normal) / volume| / (|B| / dl) with dl the
+ * smallest edge length and |B| from the cell-centred field, cells with |B| = 0 skipped.
+ * out[3] (HOST): the sum over cells (the reference's "wabsdivB" column summed over
+ * blocks), the maximum, and the number of cells counted.  FP64 in both precision modes
+ * (the face field is FP64); each cell's value is the reference's bit for bit, the sum is
+ * reduced deterministically (the same bits on every call, not the reference's summation
+ * order).  Synchronous. */
+athgpu_status athgpu_divb(athgpu_ctx *ctx, double *out);
+
+/* Run statistics (athgpu_stats): the div B diagnostic above, the cells floored by the
+ * conserved->primitive calls that computed a time step (athgpu_floor_count), and the
+ * relativistic con2prim counters of every W(U) call since the last reset: cells solved,
+ * FP64 Newman-Hamlin loop passes summed over all attempts, cells re-solved from the
+ * reference's start (the previous pressure) because their own start (FP32-refined or
+ * learned) did not converge within the reference's 15 passes, and cells left unconverged
+ * (the reference's failure branch: old primitives and floors, adiabatic_mhd_sr.cpp:
+ * 156-164).  Replaces the diagnostics the reference prints or writes to history files;
+ * the reference counts no con2prim iterations.  reset = 1 zeroes the counters after
+ * reading them.  Synchronous. */
+typedef struct {
+  double divb_sum, divb_max;
+  long long divb_cells;
+  long long floor_cells;
+  long long sr_cells, sr_passes, sr_fallbacks, sr_unconverged;
+  int net_error;  /* 1: a tensor-core wait of the network start timed out (its cells then
+                     started from the stale pressure) */
+} athgpu_run_stats;
+athgpu_status athgpu_stats(athgpu_ctx *ctx, athgpu_run_stats *out, int reset);
 
 /* Autotuner of the sweep tiling: times `cycles` cycles (after one warm-up) for each
  * candidate segment length of the x2 sweep (the whole column, then halves down to 4

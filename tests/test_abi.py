@@ -44,7 +44,8 @@ def _desc(mesh, **kw):
 @pytest.mark.parametrize("field,value,code", [
     ("xorder", 4, -3), ("xorder", 0, -3), ("nghost", 1, -1), ("rsolver", 7, -1),
     ("precision", 9, -1), ("relativistic", 1, -3), ("gamma", 1.0, -1),
-    ("cfl_number", 0.0, -1), ("nx1", 0, -1), ("ppm_fast", 1, -1)])
+    ("cfl_number", 0.0, -1), ("nx1", 0, -1), ("ppm_fast", 1, -1), ("integrator", 2, -1),
+    ("cfl_number", 0.6, -1)])
 def test_invalid_meshes_are_rejected(lib, field, value, code):
     mesh = MeshSpec((16, 8, 8), (1, 1, 1), 2)
     d, keep = _desc(mesh, **{field: value})
@@ -60,6 +61,17 @@ def test_ppm_needs_three_ghosts(lib):
     h = ctypes.c_void_p()
     assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -1
     assert b"nghost" in lib.athgpu_last_error()
+
+
+def test_integrator_cfl_limits(lib):
+    """The integrators' CFL limits in 3-D (time_integrator.cpp:219-222, 445): 0.5 for
+    vl2, 1.0 for rk2."""
+    mesh = MeshSpec((16, 8, 8), (1, 1, 1), 2)
+    for integ, cfl in ((rt.VL2, 0.51), (rt.RK2, 1.01)):
+        d, keep = _desc(mesh, integrator=integ, cfl_number=cfl)
+        h = ctypes.c_void_p()
+        assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -1
+        assert b"limit" in lib.athgpu_last_error()
 
 
 def test_null_context_calls_fail(lib):

@@ -24,7 +24,8 @@ def _built():
 
 def _run(mesh, c, ic, ncycle, precision="fp64"):
     g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
-                    precision=precision, cfl=c["cfl"], tlim=c["tlim"])
+                    precision=precision, cfl=c["cfl"], tlim=c["tlim"],
+                    integrator=c.get("integrator", "vl2"))
     g.set_state(*ic)
     g.initialize()
     dts = []
@@ -55,17 +56,18 @@ def _smooth_case(ng=2, xorder=2, rsolver="hlle", bcs=(0, 0, 0, 0, 0, 0)):
     return mesh, pgen.smooth_blocks(mesh, seed=5), c
 
 
-@pytest.mark.parametrize("ng,xorder,rsolver,bcs", [(2, 2, "hlle", (0, 0, 0, 0, 0, 0)),
-                                                   (4, 3, "hlld", (1, 1, 2, 2, 1, 2)),
-                                                   (2, 2, "roe", (2, 1, 0, 0, 1, 1)),
-                                                   (2, 2, "llf", (0, 0, 1, 2, 0, 0)),
-                                                   (4, "3f", "hlle", (1, 2, 0, 0, 2, 1))])
-def test_multilevel_fp64_matches_oracle_with_ghosts(ng, xorder, rsolver, bcs):
+@pytest.mark.parametrize("ng,xorder,rsolver,bcs,integ", [
+    (2, 2, "hlle", (0, 0, 0, 0, 0, 0), "vl2"), (4, 3, "hlld", (1, 1, 2, 2, 1, 2), "vl2"),
+    (2, 2, "roe", (2, 1, 0, 0, 1, 1), "vl2"), (2, 2, "llf", (0, 0, 1, 2, 0, 0), "vl2"),
+    (4, "3f", "hlle", (1, 2, 0, 0, 2, 1), "vl2"), (4, 3, "hlld", (2, 1, 0, 0, 1, 2), "rk2")])
+def test_multilevel_fp64_matches_oracle_with_ghosts(ng, xorder, rsolver, bcs, integ):
     """Three levels, 127+ blocks: the state after three cycles equals the oracle's bit for
     bit, ghost zones of W and B included."""
     mesh, ic, c = _smooth_case(ng, xorder, rsolver, bcs)
+    c["integrator"] = integ
     (u, b1, b2, b3), dts, w, bcc = _run(mesh, c, ic, 3)
-    om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"])
+    om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"],
+                      integrator=integ)
     om.set_state(*ic)
     om.initialize()
     odts = []

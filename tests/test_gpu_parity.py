@@ -28,7 +28,8 @@ def _faces(mesh, bs):
 
 def _run_gpu(mesh, c, ic, ncycle, precision="fp64"):
     g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
-                    precision=precision, cfl=c["cfl"], tlim=c["tlim"], bc=c.get("bc"))
+                    precision=precision, cfl=c["cfl"], tlim=c["tlim"], bc=c.get("bc"),
+                    integrator=c.get("integrator", "vl2"))
     g.set_state(*ic)
     g.initialize()
     dts = []
@@ -252,6 +253,49 @@ def test_physical_boundaries_match_oracle_bitwise(bc, xorder, rsolver, nb):
     assert np.array_equal(bcc, bcco)
     for a, b in zip((b1, b2, b3), (o1, o2, o3)):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("xorder,rsolver,nb,bc", [(3, "hlld", (2, 2, 2), (0,) * 6),
+                                                  (2, "roe", (1, 2, 3), (2, 1, 0, 0, 1, 2)),
+                                                  ("3f", "hlle", (2, 1, 2), (1, 1, 2, 2, 0, 0))])
+def test_rk2_fp64_matches_oracle_bitwise(xorder, rsolver, nb, bc):
+    """time/integrator = rk2 (xorder on both stages, beta 1 and 1/2, the register average
+    (U* + U^n)/2 on stage 2): every primitive, cell-centred field and face value, ghost
+    zones included, equals the oracle's after four cycles at CFL 0.8."""
+    mesh, ic, c = _turb_case(nx=(24, 24, 24), nb=nb, xorder=xorder, rsolver=rsolver,
+                             ng=3 if xorder in (3, "3f") else 2)
+    c.update(bc=bc, integrator="rk2", cfl=0.8)
+    (u, b1, b2, b3), dts, w, bcc = _run_gpu(mesh, c, ic, 4)
+    om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver=rsolver, tlim=c["tlim"],
+                      bc=bc, integrator="rk2", cfl=0.8)
+    om.set_state(*ic)
+    om.initialize()
+    odts = []
+    for _ in range(4):
+        odts.append(om.dt)
+        om.cycle()
+    uo, o1, o2, o3 = om.state()
+    wo, bcco = om.prim()
+    assert np.array_equal(dts, np.array(odts))
+    assert np.array_equal(mesh.interior(u), mesh.interior(uo))
+    assert np.array_equal(w, wo)
+    assert np.array_equal(bcc, bcco)
+    for a, b in zip((b1, b2, b3), (o1, o2, o3)):
+        assert np.array_equal(a, b)
+
+
+def test_rk2_fp32_tracks_fp64_and_keeps_div_b():
+    mesh, ic, c = _turb_case()
+    c.update(integrator="rk2", cfl=0.6)
+    (u64, *_), dt64, _, _ = _run_gpu(mesh, c, ic, 5, "fp64")
+    (u32, f1, f2, f3), dt32, _, _ = _run_gpu(mesh, c, ic, 5, "fp32")
+    a, b = mesh.interior(u64), mesh.interior(u32)
+    for n in range(5):
+        rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(a[:, n]).mean()
+        assert rel < 2e-5, (n, rel)
+    assert np.allclose(dt32, dt64, rtol=1e-5)
+    div = np.abs(_div_b(mesh, f1, f2, f3)).max()
+    assert div / max(np.abs(f).max() for f in (f1, f2, f3)) < 1e-13
 
 
 def test_physical_boundaries_fp32_tracks_fp64():

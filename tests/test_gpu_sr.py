@@ -32,9 +32,26 @@ def close(a, b, rtol=1e-12):
     return bool(np.all(np.abs(a - b) <= rtol * np.abs(b) + rtol * scale))
 
 
-def _run(mesh, c, ic, w0, ncycle, precision="fp64"):
+_NET = {}
+
+
+def _network():
+    """A con2prim network trained here on solver-made pairs (a small fit: the FP64 polish
+    makes the result independent of the start to the solver's tolerance)."""
+    if "p" not in _NET:
+        from athena_gb300.learned_c2p import LearnedC2P
+        net = LearnedC2P(4.0 / 3.0, seed=0)
+        net.fit(n=1 << 16, steps=1500, batch=2048, seed=5)
+        _NET["p"] = net.params.clone()
+    return _NET["p"]
+
+
+def _run(mesh, c, ic, w0, ncycle, precision="fp64", start=None, stats=None):
     g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver="hlle",
-                    precision=precision, cfl=c["cfl"], tlim=c["tlim"], relativistic=True)
+                    precision=precision, cfl=c["cfl"], tlim=c["tlim"], relativistic=True,
+                    integrator=c.get("integrator", "vl2"))
+    if start is not None:
+        g.set_c2p_start(start, _network() if start == "network" else None)
     g.set_state(*ic)
     g.set_prim(w0)
     g.initialize()
@@ -44,6 +61,8 @@ def _run(mesh, c, ic, w0, ncycle, precision="fp64"):
         g.cycle(1)
     out = g.state()
     w, bcc = g.prim()
+    if stats is not None:
+        stats.update(g.stats())
     g.close()
     return out, w, np.array(dts)
 
@@ -63,6 +82,30 @@ def test_sr_fp64_matches_reference(name):
         assert close(interior_faces(mesh, got), want)
 
 
+@pytest.mark.parametrize("start", ["stale", "refined", "network"])
+@pytest.mark.parametrize("name", SR_CASES)
+def test_sr_starts_reproduce_reference(name, start):
+    """The three starts of the FP64 solve (the reference's stale pressure, that pressure
+    refined in FP32, the network's pressure refined in FP32, the network evaluated on
+    tcgen05 inside W(U)) reproduce the reference's relativistic runs within 1e-12: the
+    polish's absolute stopping rule makes the result independent of the start to the
+    solver's tolerance.  None unconverged."""
+    c, mesh, ic, ref = load_case(name)
+    st = {}
+    (u, b1, b2, b3), w, dts = _run(mesh, c, ic, c["ic_w"], c["ncycle"], start=start, stats=st)
+    assert np.array_equal(dts, ref["dt"])
+    ui = mesh.interior(u)
+    for n in range(5):
+        assert close(ui[:, n], ref["u"][:, n]), n
+    wi = mesh.interior(w)
+    for n in range(5):
+        assert close(wi[:, n], ref["w"][:, n], rtol=1e-11), n
+    for got, want in zip((b1, b2, b3), (ref["b1"], ref["b2"], ref["b3"])):
+        assert close(interior_faces(mesh, got), want)
+    assert st["sr_unconverged"] == 0 and st["net_error"] == 0, st
+    assert st["sr_cells"] > 0
+
+
 def _sr_kh(nx=(32, 32, 32), nb=(2, 2, 2), seed=4):
     mesh = MeshSpec(nx, nb, 2)
     gw, f1, f2, f3 = pgen.sr_kelvin_helmholtz(nx, seed=seed, noise=0.02)
@@ -72,11 +115,13 @@ def _sr_kh(nx=(32, 32, 32), nb=(2, 2, 2), seed=4):
     return mesh, ic, mesh.scatter_cells(gw), c
 
 
-def test_sr_fp64_matches_oracle():
+@pytest.mark.parametrize("integ", ["vl2", "rk2"])
+def test_sr_fp64_matches_oracle(integ):
     mesh, ic, w0, c = _sr_kh()
+    c["integrator"] = integ
     (u, *_), w, dts = _run(mesh, c, ic, w0, 4)
     om = O.OracleMesh(mesh, c["gamma"], xorder=2, rsolver="hlle", tlim=c["tlim"],
-                      relativistic=True)
+                      relativistic=True, integrator=integ)
     om.set_state(*ic)
     om.set_prim(w0)
     om.initialize()
