@@ -29,6 +29,8 @@ UNITS = {
     "history.cu": ["-fmad=false"],
     # div B diagnostic (the reference's per-cell arithmetic) and run statistics
     "diagnostics.cu": ["-fmad=false"],
+    # per-operator entry points on one MeshBlock (FP64, the reference's rounding)
+    "operators.cu": ["-fmad=false"],
     # host planner of the multi-level stage
     "ml_plan.cu": ["-fmad=false"],
     # adaptive refinement: refinement measure and regrid (FP64 restriction/prolongation)

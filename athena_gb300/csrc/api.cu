@@ -1,6 +1,7 @@
 // C ABI of the stage update (include/athena_gb300.h).
 #include <cuda_runtime.h>
 #include <float.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -48,6 +49,72 @@ __global__ void join_kernel(const float* __restrict__ hi, const float* __restric
 
 long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
+// The same conversions reading or writing page-locked host memory in place (the GPU reaches
+// it over the host link): one pass instead of a copy into device staging plus a kernel.
+// Each thread moves four consecutive elements per step, so several requests are in flight
+// per thread and the link's latency is hidden; grid-stride over the array.
+__global__ void __launch_bounds__(256)
+split_from_host_kernel(const double* __restrict__ src, float* __restrict__ hi,
+                       float* __restrict__ lo, long long n) {
+  const long long n4 = n / 4;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4;
+       q += (long long)gridDim.x * blockDim.x) {
+    const double2 a = reinterpret_cast<const double2*>(src)[2 * q];
+    const double2 b = reinterpret_cast<const double2*>(src)[2 * q + 1];
+    const float4 h = make_float4((float)a.x, (float)a.y, (float)b.x, (float)b.y);
+    reinterpret_cast<float4*>(hi)[q] = h;
+    if (lo)
+      reinterpret_cast<float4*>(lo)[q] =
+          make_float4((float)(a.x - (double)h.x), (float)(a.y - (double)h.y),
+                      (float)(b.x - (double)h.z), (float)(b.y - (double)h.w));
+  }
+  // the tail (n not a multiple of 4)
+  const long long t = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0 && t < n) {
+    const double v = src[t];
+    const float h = (float)v;
+    hi[t] = h;
+    if (lo) lo[t] = (float)(v - (double)h);
+  }
+}
+__global__ void __launch_bounds__(256)
+join_to_host_kernel(const float* __restrict__ hi, const float* __restrict__ lo,
+                    double* __restrict__ dst, long long n) {
+  const long long n4 = n / 4;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float4 h = reinterpret_cast<const float4*>(hi)[q];
+    float4 l = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lo) l = reinterpret_cast<const float4*>(lo)[q];
+    reinterpret_cast<double2*>(dst)[2 * q] =
+        make_double2((double)h.x + (double)l.x, (double)h.y + (double)l.y);
+    reinterpret_cast<double2*>(dst)[2 * q + 1] =
+        make_double2((double)h.z + (double)l.z, (double)h.w + (double)l.w);
+  }
+  const long long t = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0 && t < n) dst[t] = (double)hi[t] + (lo ? (double)lo[t] : 0.0);
+}
+
+// The device address of page-locked host memory (cudaHostAlloc / cudaHostRegister, mapped
+// under unified addressing), or nullptr for other memory.  Both kernels above need 16-byte
+// alignment of the host array.
+const void* pinned_device_ptr(const void* h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();  // clear the error of an unknown pointer
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  if (((uintptr_t)a.devicePointer & 15u) != 0) return nullptr;
+  return a.devicePointer;
+}
+
+// grid of the host-link conversion kernels: enough CTAs for many requests in flight
+unsigned link_grid(long long n) {
+  const long long want = ceil_div(ceil_div(n, 4), 256);
+  return (unsigned)(want < 152 * 16 ? (want > 0 ? want : 1) : 152 * 16);
+}
+
 }  // namespace
 
 namespace athgpu {
@@ -81,7 +148,7 @@ void free_all(athgpu_ctx* c) {
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
                   c->nbr, c->staging, c->c2p_queue, c->c2p_qcount, c->fxv, c->eps_buf,
-                  c->c2p_qstart, c->c2p_net, c->c2p_net_err};
+                  c->c2p_qstart, c->c2p_net, c->c2p_net_err, c->op_flx, c->op_words};
   // the context's device memory returns to the stream-ordered pool (pool_alloc)
   cudaStream_t s = c->own_stream;
   if (s) cudaStreamSynchronize(c->stream ? c->stream : s);
@@ -105,8 +172,13 @@ cudaError_t run_stage_dispatch(athgpu_ctx* c, int stage) {
 
 // host copy of a double array into a bulk-precision device register
 athgpu_status upload_bulk(athgpu_ctx* c, const double* h, void* dev, void* lo, long long n) {
+  const double* hd = c->real_bytes == 4 ? (const double*)pinned_device_ptr(h) : nullptr;
   if (c->real_bytes == 8) {
     CK(cudaMemcpyAsync(dev, h, n * 8, cudaMemcpyHostToDevice, c->stream));
+  } else if (hd) {  // page-locked host array: converted while it is read over the link
+    split_from_host_kernel<<<link_grid(n), 256, 0, c->stream>>>(hd, (float*)dev, (float*)lo,
+                                                                n);
+    CK(cudaGetLastError());
   } else {
     CK(cudaMemcpyAsync(c->staging, h, n * 8, cudaMemcpyHostToDevice, c->stream));
     split_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(c->staging, (float*)dev,
@@ -118,8 +190,13 @@ athgpu_status upload_bulk(athgpu_ctx* c, const double* h, void* dev, void* lo, l
 
 athgpu_status download_bulk(athgpu_ctx* c, double* h, const void* dev, const void* lo,
                             long long n) {
+  double* hd = c->real_bytes == 4 ? (double*)pinned_device_ptr(h) : nullptr;
   if (c->real_bytes == 8) {
     CK(cudaMemcpyAsync(h, dev, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  } else if (hd) {  // page-locked host array: written in place over the link
+    join_to_host_kernel<<<link_grid(n), 256, 0, c->stream>>>((const float*)dev,
+                                                             (const float*)lo, hd, n);
+    CK(cudaGetLastError());
   } else {
     join_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(
         (const float*)dev, (const float*)lo, c->staging, n);

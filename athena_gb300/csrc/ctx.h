@@ -81,6 +81,9 @@ struct athgpu_ctx {
   int c2p_start = 0;
   float* c2p_net = nullptr;
   int* c2p_net_err = nullptr;
+  // per-operator calls (operators.cu): the three flux arrays [5][nf1] | [5][nf2] | [5][nf3]
+  double* op_flx = nullptr;
+  unsigned long long* op_words = nullptr;  // [0] floored-cell count, [1] dt minimum bits
   // per-kernel timing of one non-graph cycle (athgpu_profile_cycle)
   bool profiling = false;
   std::vector<std::string> prof_names;
@@ -108,6 +111,8 @@ struct ProfScope {
 };
 
 namespace athgpu {
+// device memory of the contexts, from the stream-ordered pool (api.cu)
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
 // stage drivers, one per precision translation unit
 cudaError_t stage_fp64(athgpu_ctx* c, int stage);
 cudaError_t stage_fp32(athgpu_ctx* c, int stage);

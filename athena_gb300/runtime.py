@@ -30,6 +30,14 @@ class AthGPUError(RuntimeError):
     pass
 
 
+class FaceEmfs(ctypes.Structure):
+    """athgpu_face_emfs: e3_x1f, e2_x1f, wght_x1f, e1_x2f, e3_x2f, wght_x2f, e1_x3f,
+    e2_x3f, wght_x3f"""
+    _fields_ = [(n, ctypes.POINTER(ctypes.c_double)) for n in (
+        "e3_x1f", "e2_x1f", "wght_x1f", "e1_x2f", "e3_x2f", "wght_x2f", "e1_x3f", "e2_x3f",
+        "wght_x3f")]
+
+
 class RunStats(ctypes.Structure):
     """athgpu_run_stats"""
     _fields_ = [("divb_sum", ctypes.c_double), ("divb_max", ctypes.c_double),
@@ -446,3 +454,73 @@ def ml_plan_check(mesh):
                                   loc.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
                                   out), "athgpu_ml_plan_check")
     return tuple(out)
+
+
+class BlockOperators:
+    """The per-operator entry points (athgpu_op_*) on ONE MeshBlock: the reference's
+    member functions of the stage update, one call each, on numpy arrays in the block's
+    AthenaArray layout (ghosts included).  mesh: a MeshSpec of one block."""
+
+    def __init__(self, mesh, gamma, rsolver="hlld", xorder=2, relativistic=False, **kw):
+        if mesh.nblocks != 1:
+            raise ValueError("BlockOperators takes a mesh of one MeshBlock")
+        self.mesh = mesh
+        self.su = StageUpdate(mesh, gamma, xorder=xorder, rsolver=rsolver, precision="fp64",
+                              relativistic=relativistic, **kw)
+        L = load_library()
+        dp, vp = ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
+        L.athgpu_op_calculate_fluxes.argtypes = [vp, ctypes.c_int, ctypes.c_double] + \
+            [dp] * 8 + [ctypes.POINTER(FaceEmfs)]
+        L.athgpu_op_corner_e.argtypes = [vp, dp, dp, ctypes.POINTER(FaceEmfs), dp, dp, dp]
+        L.athgpu_op_add_flux_divergence.argtypes = [vp, ctypes.c_double, dp, dp, dp, dp]
+        L.athgpu_op_ct.argtypes = [vp, ctypes.c_double] + [dp] * 6
+        L.athgpu_op_con2prim.argtypes = [vp] + [dp] * 6 + [ctypes.c_int] * 6 + \
+            [ctypes.POINTER(ctypes.c_longlong)]
+        L.athgpu_op_new_block_dt.argtypes = [vp] + [dp] * 5 + [dp]
+        self.L = L
+
+    @staticmethod
+    def _emfs(emf):
+        e = FaceEmfs()
+        for (name, _), a in zip(FaceEmfs._fields_, emf):
+            setattr(e, name, _dp(a))
+        return e
+
+    def calculate_fluxes(self, order, dt, w, bcc, b, flx, emf):
+        e = self._emfs(emf)
+        _check(self.L.athgpu_op_calculate_fluxes(
+            self.su.h, order, dt, _dp(w), _dp(bcc), _dp(b[0]), _dp(b[1]), _dp(b[2]),
+            _dp(flx[0]), _dp(flx[1]), _dp(flx[2]), ctypes.byref(e)),
+            "athgpu_op_calculate_fluxes")
+
+    def corner_e(self, w, bcc, emf, e):
+        fe = self._emfs(emf)
+        _check(self.L.athgpu_op_corner_e(self.su.h, _dp(w), _dp(bcc), ctypes.byref(fe),
+                                         _dp(e[0]), _dp(e[1]), _dp(e[2])),
+               "athgpu_op_corner_e")
+
+    def add_flux_divergence(self, wght, flx, u):
+        _check(self.L.athgpu_op_add_flux_divergence(self.su.h, wght, _dp(flx[0]),
+                                                    _dp(flx[1]), _dp(flx[2]), _dp(u)),
+               "athgpu_op_add_flux_divergence")
+
+    def ct(self, wght, e, b):
+        _check(self.L.athgpu_op_ct(self.su.h, wght, _dp(e[0]), _dp(e[1]), _dp(e[2]),
+                                   _dp(b[0]), _dp(b[1]), _dp(b[2])), "athgpu_op_ct")
+
+    def con2prim(self, cons, b, prim, bcc, rng):
+        n = ctypes.c_longlong()
+        _check(self.L.athgpu_op_con2prim(self.su.h, _dp(cons), _dp(b[0]), _dp(b[1]),
+                                         _dp(b[2]), _dp(prim), _dp(bcc), *rng,
+                                         ctypes.byref(n)), "athgpu_op_con2prim")
+        return n.value
+
+    def new_block_dt(self, w, bcc, b):
+        out = ctypes.c_double()
+        _check(self.L.athgpu_op_new_block_dt(self.su.h, _dp(w), _dp(bcc), _dp(b[0]),
+                                             _dp(b[1]), _dp(b[2]), ctypes.byref(out)),
+               "athgpu_op_new_block_dt")
+        return out.value
+
+    def close(self):
+        self.su.close()

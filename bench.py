@@ -33,7 +33,8 @@ METRIC = ("zone-cycles/s on 1 GB300: FP32+learned c2p vs plain FP64 GPU at equal
           "error")
 NX, NB, NG = (256, 256, 256), (8, 8, 8), 3
 BYTES_PER_ZONE_CYCLE = {"fp32": 260.0, "fp64": 320.0}  # algorithmic HBM bytes
-ACC_CYCLES = 10   # cycles run by both paths for the FP32-vs-FP64 L1 comparison
+ACC_CYCLES = 100  # cycles run by both paths for the FP32-vs-FP64 comparison (the
+                  # workload's 100 steps): per-variable L1 and energy spectra
 PROFILE_CYCLES = 3
 
 # Dominant kernel of the FP32 cycle: the stage-2 x1 sweep (PPM + HLLD), the largest single
@@ -71,6 +72,39 @@ def make_ic(nx=NX, nb=NB, ng=NG, seed=20261204):
     u = mesh.scatter_cells(gu)
     b1, b2, b3 = mesh.scatter_faces(f1, f2, f3)
     return mesh, (u, b1, b2, b3)
+
+
+# ------------------------------------------------------------------------------------
+def energy_spectra(mesh, w, bcc, kmax):
+    """Shell-averaged kinetic and magnetic energy spectra of a periodic state:
+    E_K(k) = sum over |k'| in [k - 1/2, k + 1/2) of |FFT(sqrt(rho) v)|^2 / 2 and
+    E_M(k) the same of the cell-centred field (FFT normalised by the cell count),
+    k = 1..kmax in units of the box wavenumber.  w, bcc: per-block primitives and
+    cell-centred field with ghosts.  Evaluated with torch's FFT on the device (analysis of
+    the outputs, not part of the timed path)."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    gw = torch.from_numpy(mesh.gather_cells(w)).to(dev)
+    gb = torch.from_numpy(mesh.gather_cells(bcc)).to(dev)
+    n3, n2, n1 = gw.shape[1:]
+    ncell = n1 * n2 * n3
+    k1 = torch.fft.fftfreq(n1, d=1.0 / n1, device=dev, dtype=torch.float64)
+    k2 = torch.fft.fftfreq(n2, d=1.0 / n2, device=dev, dtype=torch.float64)
+    k3 = torch.fft.fftfreq(n3, d=1.0 / n3, device=dev, dtype=torch.float64)
+    kk = torch.sqrt(k3[:, None, None] ** 2 + k2[None, :, None] ** 2 + k1[None, None, :] ** 2)
+    shell = torch.round(kk).to(torch.int64).ravel()
+
+    def spec(fields):
+        power = torch.zeros(n3 * n2 * n1, dtype=torch.float64, device=dev)
+        for f in fields:
+            fk = torch.fft.fftn(f) / ncell
+            power += 0.5 * (fk.real ** 2 + fk.imag ** 2).ravel()
+        e = torch.bincount(shell, weights=power, minlength=kmax + 1)
+        return e[1:kmax + 1].cpu().numpy()
+    sq = torch.sqrt(gw[0])
+    ek = spec([sq * gw[1], sq * gw[2], sq * gw[3]])
+    em = spec([gb[0], gb[1], gb[2]])
+    return ek, em
 
 
 # ------------------------------------------------------------------------------------
@@ -157,6 +191,30 @@ def time_device_cycles(g, stream, steps, warmup):
     return s.elapsed_time(e) / 1e3
 
 
+def link_ceiling(dev, nbytes, reps=3):
+    """The host link's ceiling for the e2e copies: one plain cudaMemcpyAsync (torch copy_)
+    of a pinned host buffer of nbytes to the device and back, CUDA events, best of reps."""
+    import torch
+    h = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    h.fill_(1.0)
+    d = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
+    out = {}
+    for name, (dst, src) in (("h2d_gbs", (d, h)), ("d2h_gbs", (h, d))):
+        best = 1e30
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+        out[name] = nbytes / best / 1e9
+    out["bytes"] = nbytes
+    out["how"] = "one cudaMemcpyAsync of a pinned host buffer each way, CUDA events"
+    del h, d
+    return out
+
+
 def run_gpu(args, rank, world, local_rank):
     global NX, NB
     NX = (args.nx,) * 3
@@ -196,12 +254,19 @@ def run_gpu(args, rank, world, local_rank):
             dt = float(t.item())
         res[prec] = {"seconds": dt, "steps": steps, "value": world * zones * steps / dt,
                      "ms_per_step": dt / steps * 1e3}
+        if prec == "fp32":  # |div B| after the timed cycles (the reference's diagnostic)
+            s_, m_, c_ = g.divb()
+            res["divb"] = {"max": m_, "mean": s_ / max(c_, 1), "cells": c_,
+                           "after_cycles": args.warmup + steps + 2}
         # accuracy: the same number of cycles from the same initial state in each path
         g.set_state(*ic)
         g.set_clock(0.0, 1.7976931348623157e308)
         g.initialize()
         g.cycle(ACC_CYCLES)
         res["u_" + prec] = mesh.interior(g.state()[0])
+        w_acc, bcc_acc = g.prim()
+        res["spec_" + prec] = energy_spectra(mesh, w_acc, bcc_acc, NX[0] // 2)
+        del w_acc, bcc_acc
         if prec == "fp64":
             res["profile64"] = g.profile_cycle()
         else:
@@ -245,7 +310,8 @@ def run_gpu(args, rank, world, local_rank):
                 te = float(t.item())
             res["e2e"] = {"value": world * zones * e_steps / te, "unit": "zone-cycles/s",
                           "h2d_bytes_per_step": ebytes, "d2h_bytes_per_step": ebytes,
-                          "steps": e_steps}
+                          "steps": e_steps, "ms_per_step": te / e_steps * 1e3,
+                          "link_ceiling": link_ceiling(dev, ebytes)}
         g.close()
     res["linear_wave_l1"] = run_linear_wave()
     if not args.no_amr:
@@ -353,10 +419,13 @@ def run_sr_kh(n, stream, net):
     box as (n/32)^3 MeshBlocks, gamma 4/3, v_x = +-0.5c with tanh width 0.01, rho 1 / 0.1,
     p = 1, uniform B_x with sigma 0.1, seeded 1e-3 velocity noise, VL2 + PLM + HLLE.
     Zone-cycles/s of the FP32 and FP64 SR stage paths (CUDA events, state resident), their
-    relative L1 difference after SR_ACC_CYCLES cycles, and the con2prim start study: the
-    conserved state of one cycle solved per cell from the previous cycle's pressure (the
-    reference's start, and the FP32 stage's start: that pressure refined in FP32) and from
-    the network refined in FP32."""
+    relative L1 difference after SR_ACC_CYCLES cycles.  Inside the stage each start of the
+    FP64 con2prim solve is timed (the stale pressure, that pressure refined in FP32, the
+    network evaluated on tcgen05 in the W(U) kernel and refined in FP32) with its mean FP64
+    passes, fallbacks and unconverged cells from the run statistics, also for the first
+    W(U) without stale primitives (as after a restart).  The con2prim start study solves
+    the conserved state of one cycle per cell with the isolated-cell entry point from the
+    previous cycle's pressure, that pressure refined in FP32, and the network."""
     import torch
     from athena_gb300 import pgen
     from athena_gb300.learned_c2p import MODE_LEARNED_FP32, MODE_PLAIN, MODE_REFINED
@@ -375,16 +444,43 @@ def run_sr_kh(n, stream, net):
                        "32^3, gamma 4/3, shear +-0.5c, sigma 0.1, VL2 + PLM + HLLE" %
                        (n, nb[0] * nb[1] * nb[2])}
     finals = {}
+    wzero = np.zeros_like(w0)
     for prec in ("fp32", "fp64"):
         g = StageUpdate(mesh, gam, xorder=2, rsolver="hlle", precision=prec, cfl=0.3,
                         relativistic=True)
         g.set_stream(stream.cuda_stream)
-        g.set_state(*ic)
-        g.set_prim(w0)
-        g.initialize()
-        t = time_device_cycles(g, stream, SR_CYCLES[prec], 3)
-        out[prec] = {"value": zones * SR_CYCLES[prec] / t, "unit": "zone-cycles/s",
-                     "ms_per_step": t / SR_CYCLES[prec] * 1e3, "steps": SR_CYCLES[prec]}
+        # every start of the FP64 solve inside the stage: the default first (FP32 path: the
+        # stale pressure refined in FP32; FP64 path: the stale pressure, the reference's)
+        starts = ("refined", "network", "stale") if prec == "fp32" else ("stale", "network")
+        by_start, cold = {}, {}
+        for start in starts:
+            g.set_c2p_start(start, net.params if start == "network" else None)
+            # the first W(U) with no stale primitives (w = 0, as after a restart, whose
+            # file holds U and B only): the stale start is the pressure floor
+            g.set_state(*ic)
+            g.set_prim(wzero)
+            g.initialize()
+            st = g.stats(reset=True)
+            cold[start] = {"mean_fp64_passes": st["sr_passes"] / max(st["sr_cells"], 1),
+                           "unconverged": st["sr_unconverged"],
+                           "fallbacks": st["sr_fallbacks"]}
+            # the timed run from the initial primitives
+            g.set_state(*ic)
+            g.set_prim(w0)
+            g.set_clock(0.0, 1.7976931348623157e308)
+            g.initialize()
+            g.stats(reset=True)
+            t = time_device_cycles(g, stream, SR_CYCLES[prec], 3)
+            st = g.stats(reset=True)
+            by_start[start] = {"value": zones * SR_CYCLES[prec] / t, "unit": "zone-cycles/s",
+                               "ms_per_step": t / SR_CYCLES[prec] * 1e3,
+                               "mean_fp64_passes": st["sr_passes"] / max(st["sr_cells"], 1),
+                               "unconverged": st["sr_unconverged"],
+                               "fallbacks": st["sr_fallbacks"], "net_error": st["net_error"]}
+        out[prec] = dict(by_start[starts[0]], steps=SR_CYCLES[prec], start=starts[0])
+        out[prec]["in_stage_starts"] = by_start
+        out[prec]["first_c2p_without_stale_primitives"] = cold
+        g.set_c2p_start(starts[0])
         g.set_state(*ic)
         g.set_prim(w0)
         g.set_clock(0.0, 1.7976931348623157e308)
@@ -685,6 +781,18 @@ def main():
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     sm_hz = (res["clocks"].get("sm_mhz") or 2070.0) * 1e6
     l1 = l1_rel(res["u_fp32"], res["u_fp64"])
+    # energy spectra after ACC_CYCLES cycles: the largest relative difference over the
+    # resolved band (k <= N/8, i.e. at least 8 cells per wavelength) and over all k
+    (ek32, em32), (ek64, em64) = res["spec_fp32"], res["spec_fp64"]
+    kres = NX[0] // 8
+    spectra = {"cycles": ACC_CYCLES, "k": "1..%d" % (NX[0] // 2),
+               "resolved_band": "1..%d" % kres,
+               "max_rel_diff_kinetic_resolved": float(np.max(np.abs(ek32[:kres] / ek64[:kres] - 1))),
+               "max_rel_diff_magnetic_resolved": float(np.max(np.abs(em32[:kres] / em64[:kres] - 1))),
+               "max_rel_diff_kinetic_all": float(np.max(np.abs(ek32 / ek64 - 1))),
+               "max_rel_diff_magnetic_all": float(np.max(np.abs(em32 / em64 - 1))),
+               "E_kinetic_fp64": [float(v) for v in ek64[:16]],
+               "E_magnetic_fp64": [float(v) for v in em64[:16]]}
     line = {"metric": METRIC, "value": r32["value"], "unit": "zone-cycles/s",
             "n_gpus": world, "steps": r32["steps"], "warmup": args.warmup,
             "ms_per_step": r32["ms_per_step"], "higher_is_better": True,
@@ -695,6 +803,8 @@ def main():
             "speedup_fp32_vs_fp64_gpu": r32["value"] / r64["value"],
             "l1_rel_fp32_vs_fp64": {"cycles": ACC_CYCLES, "d": l1[0], "m1": l1[1],
                                     "m2": l1[2], "m3": l1[3], "e": l1[4]},
+            "energy_spectra_fp32_vs_fp64": spectra,
+            "divb": res.get("divb"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "traffic": DOMINANT_TRAFFIC_PER_ZONE * zones,
@@ -723,6 +833,8 @@ def main():
         line["amr_blast"] = res["amr_blast"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline((mesh, make_ic(NX, NB)[1]))
+        # like for like: the plain FP64 GPU path against the FP64 CPU baseline
+        line["fp64_gpu"]["vs_cpu_baseline"] = r64["value"] / line["cpu_baseline"]["value"]
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

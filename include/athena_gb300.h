@@ -374,6 +374,67 @@ athgpu_status athgpu_launch_count(athgpu_ctx *ctx, long long *count, int reset);
 const char *athgpu_last_error(void);
 const char *athgpu_version(void);
 
+/* ---- Per-operator entry points (one MeshBlock per call) ----
+ * The bodies of the reference's per-MeshBlock member functions of the stage update, for a
+ * caller that keeps its own TimeIntegratorTaskList, boundary exchange and EMF averaging
+ * and replaces only these operators (the shim in athena_gb300/shim/ does so inside the
+ * reference).  ctx: a context of ONE MeshBlock (athgpu_create with nbx1 = nbx2 = nbx3 = 1
+ * and that block's coordinates, FP64; athgpu_initialize is not needed).  Arrays are the
+ * block's AthenaArrays (ghosts included, layouts at the top of this file; fluxes
+ * flx? [5][nc3][nc2][nc1+1] etc., edge EMFs e1 [nc3+1][nc2+1][nc1], e2 [nc3+1][nc2][nc1+1],
+ * e3 [nc3][nc2+1][nc1+1]) in host or device memory.  Outputs are written over the
+ * reference's index ranges only (their other elements come back unchanged).  Results are
+ * the reference's bit for bit.  Synchronous. */
+typedef struct {
+  /* the face EMFs and CT weights Hydro::CalculateFluxes writes and Field::ComputeCornerE
+   * reads (pfield->e3_x1f, e2_x1f, wght.x1f, e1_x2f, e3_x2f, wght.x2f, e1_x3f, e2_x3f,
+   * wght.x3f; each shaped like the face field of its direction) */
+  double *e3_x1f, *e2_x1f, *wght_x1f;
+  double *e1_x2f, *e3_x2f, *wght_x2f;
+  double *e1_x3f, *e2_x3f, *wght_x3f;
+} athgpu_face_emfs;
+/* Hydro::CalculateFluxes(w, b, bcc, order) (hydro.hpp:72-73, calculate_fluxes.cpp:38-415):
+ * reconstruction of order 1 (donor cell), 2 (PLM), 3 (PPM, or fast PPM when the context
+ * has ppm_fast) or 4 (fast PPM, time/xorder = 3f) and the context's Riemann solver on every
+ * face the reference solves;
+ * fluxes into flx1..3, face EMFs and CT weights into emfs.  dt = Mesh::dt (the CT weights,
+ * hydro.cpp:154-158). */
+athgpu_status athgpu_op_calculate_fluxes(athgpu_ctx *ctx, int order, double dt,
+                                         const double *w, const double *bcc,
+                                         const double *b1, const double *b2,
+                                         const double *b3, double *flx1, double *flx2,
+                                         double *flx3, athgpu_face_emfs *emfs);
+/* Field::ComputeCornerE(w, bcc) (field.hpp:66, calculate_corner_e.cpp:28-236): the edge
+ * EMFs e1, e2, e3 (pfield->e.x1e, x2e, x3e) from the face EMFs and weights and the
+ * cell-centred E of w and bcc. */
+athgpu_status athgpu_op_corner_e(athgpu_ctx *ctx, const double *w, const double *bcc,
+                                 const athgpu_face_emfs *emfs, double *e1, double *e2,
+                                 double *e3);
+/* Hydro::AddFluxDivergence(wght, u_out) (hydro.hpp:67, add_flux_divergence.cpp:39-96):
+ * u -= wght * div(flux) / vol over the interior. */
+athgpu_status athgpu_op_add_flux_divergence(athgpu_ctx *ctx, double wght, const double *flx1,
+                                            const double *flx2, const double *flx3,
+                                            double *u);
+/* Field::CT(wght, b_out) (field.hpp:63, ct.cpp:31-116): the face fields b1..b3 updated
+ * in place from the edge EMFs. */
+athgpu_status athgpu_op_ct(athgpu_ctx *ctx, double wght, const double *e1, const double *e2,
+                           const double *e3, double *b1, double *b2, double *b3);
+/* EquationOfState::ConservedToPrimitive(cons, prim_old, b, prim, bcc, pco, il, iu, jl, ju,
+ * kl, ku) (eos.hpp:37-40; adiabatic_mhd.cpp:41-90, relativistic: adiabatic_mhd_sr.cpp:
+ * 72-272, seeded from prim's previous contents): bcc from the faces, prim, and cons
+ * rewritten where floors apply, over the given cell range.  *nfloored (may be NULL):
+ * cells whose floors applied (relativistic: also failed solves). */
+athgpu_status athgpu_op_con2prim(athgpu_ctx *ctx, double *cons, const double *b1,
+                                 const double *b2, const double *b3, double *prim,
+                                 double *bcc, int il, int iu, int jl, int ju, int kl, int ku,
+                                 long long *nfloored);
+/* Hydro::NewBlockTimeStep() (hydro.hpp:66, new_blockdt.cpp:45-230), ideal MHD or SR:
+ * *dt_out = cfl_number times the minimum over interior cells of dx_d / (|v_d| + c_f)
+ * (the value the reference stores in MeshBlock::new_block_dt_). */
+athgpu_status athgpu_op_new_block_dt(athgpu_ctx *ctx, const double *w, const double *bcc,
+                                     const double *b1, const double *b2, const double *b3,
+                                     double *dt_out);
+
 /* ---- Learned initial guess for the special-relativistic con2prim ----
  * A 5 -> 64 -> 64 -> 2 SiLU network predicts (log(p_gas/E), log(Lorentz factor)) from the
  * features of athgpu_sr_features; its start replaces the previous-pressure start of the

@@ -1289,6 +1289,9 @@ static void cell_centered_field(orc_mesh *m, int b, int il, int iu, int jl, int 
 static long sr_c2p_block(orc_mesh *m, int b, double *u, double *prim, int il, int iu,
                          int jl, int ju, int kl, int ku);
 
+static long con2prim_range(orc_mesh *m, int b, double *u, double *prim, int il, int iu,
+                           int jl, int ju, int kl, int ku);
+
 static long con2prim(orc_mesh *m, int b, double *u, double *prim) {
   /* the interior plus the ghost layers that have a neighbour (time_integrator.cpp:
    * 2206-2212, mesh.cpp:1820-1831); ghosts on physical boundaries come from the boundary
@@ -1300,6 +1303,13 @@ static long con2prim(orc_mesh *m, int b, double *u, double *prim) {
   int ju = m->je + (has_nbr(m, b, 0, 1, 0) ? ng : 0);
   int kl = m->ks - (has_nbr(m, b, 0, 0, -1) ? ng : 0);
   int ku = m->ke + (has_nbr(m, b, 0, 0, 1) ? ng : 0);
+  return con2prim_range(m, b, u, prim, il, iu, jl, ju, kl, ku);
+}
+
+/* EquationOfState::ConservedToPrimitive over [il,iu]x[jl,ju]x[kl,ku] of block b, with the
+ * cell-centred field of the same range first */
+static long con2prim_range(orc_mesh *m, int b, double *u, double *prim, int il, int iu,
+                           int jl, int ju, int kl, int ku) {
   cell_centered_field(m, b, il, iu, jl, ju, kl, ku);
   if (m->p.relativistic) return sr_c2p_block(m, b, u, prim, il, iu, jl, ju, kl, ku);
   const double *bcc = m->bcc + (long)b * 3 * m->ncell;
@@ -2133,5 +2143,93 @@ void orc_cycle(orc_mesh *m) {
   orc_advance(m);
   all_new_dt(m);
 }
+
+/* ------------------------------------------------------------------------------------
+ * Per-operator restatements on block b of the oracle's mesh (checkers of the library's
+ * per-operator entry points): each runs one member function of the reference on the
+ * mesh's own arrays (w, bcc, b, u) and copies its outputs.  Test infrastructure only.
+ */
+
+/* Hydro::CalculateFluxes (calculate_fluxes.cpp:38-415) with dt for the CT weights:
+ * flx? [5][face] and emf[9] = e3_x1f, e2_x1f, wght.x1f, e1_x2f, e3_x2f, wght.x2f, e1_x3f,
+ * e2_x3f, wght.x3f */
+void orc_op_fluxes(orc_mesh *m, int b, int order, double dt, double *flx1, double *flx2,
+                   double *flx3, double *const emf[9]) {
+  scratch s;
+  scratch_alloc(m, &s);
+  double dt_keep = m->dt;
+  m->dt = dt;
+  calculate_fluxes(m, b, order, &s);
+  m->dt = dt_keep;
+  long n1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1), n2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1,
+       n3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  memcpy(flx1, s.flx1, sizeof(double) * NHYDRO * n1);
+  memcpy(flx2, s.flx2, sizeof(double) * NHYDRO * n2);
+  memcpy(flx3, s.flx3, sizeof(double) * NHYDRO * n3);
+  const double *src[9] = {s.e3x1, s.e2x1, s.w1f, s.e1x2, s.e3x2, s.w2f, s.e1x3, s.e2x3, s.w3f};
+  const long len[9] = {n1, n1, n1, n2, n2, n2, n3, n3, n3};
+  for (int q = 0; q < 9; ++q) memcpy(emf[q], src[q], sizeof(double) * len[q]);
+  scratch_free(&s);
+}
+
+/* Field::ComputeCornerE (calculate_corner_e.cpp:28-236) from the face EMFs emf[9] (as
+ * orc_op_fluxes gives them) and the mesh's w, bcc: the edge EMFs before any averaging */
+void orc_op_corner_e(orc_mesh *m, int b, const double *const emf[9], double *e1, double *e2,
+                     double *e3) {
+  scratch s;
+  scratch_alloc(m, &s);
+  long n1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1), n2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1,
+       n3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  double *dst[9] = {s.e3x1, s.e2x1, s.w1f, s.e1x2, s.e3x2, s.w2f, s.e1x3, s.e2x3, s.w3f};
+  const long len[9] = {n1, n1, n1, n2, n2, n2, n3, n3, n3};
+  for (int q = 0; q < 9; ++q) memcpy(dst[q], emf[q], sizeof(double) * len[q]);
+  /* corner_e writes the mesh's own edge arrays of block b: start them from e1..e3 */
+  double *me1 = m->e1 + (long)b * m->ne1, *me2 = m->e2 + (long)b * m->ne2,
+         *me3 = m->e3 + (long)b * m->ne3;
+  memcpy(me1, e1, sizeof(double) * m->ne1);
+  memcpy(me2, e2, sizeof(double) * m->ne2);
+  memcpy(me3, e3, sizeof(double) * m->ne3);
+  corner_e(m, b, &s);
+  memcpy(e1, me1, sizeof(double) * m->ne1);
+  memcpy(e2, me2, sizeof(double) * m->ne2);
+  memcpy(e3, me3, sizeof(double) * m->ne3);
+  scratch_free(&s);
+}
+
+/* Hydro::AddFluxDivergence (add_flux_divergence.cpp:39-96) on u (one block's array) */
+void orc_op_add_flux_divergence(orc_mesh *m, int b, double wght, const double *flx1,
+                                const double *flx2, const double *flx3, double *u) {
+  scratch s;
+  scratch_alloc(m, &s);
+  long n1 = (long)m->nc3 * m->nc2 * (m->nc1 + 1), n2 = (long)m->nc3 * (m->nc2 + 1) * m->nc1,
+       n3 = (long)(m->nc3 + 1) * m->nc2 * m->nc1;
+  memcpy(s.flx1, flx1, sizeof(double) * NHYDRO * n1);
+  memcpy(s.flx2, flx2, sizeof(double) * NHYDRO * n2);
+  memcpy(s.flx3, flx3, sizeof(double) * NHYDRO * n3);
+  add_flux_divergence(m, b, wght, u, &s);
+  scratch_free(&s);
+}
+
+/* Field::CT (ct.cpp:31-116) with the given edge EMFs on b1..b3 (one block's arrays) */
+void orc_op_ct(orc_mesh *m, int b, double wght, const double *e1, const double *e2,
+               const double *e3, double *b1, double *b2, double *b3) {
+  scratch s;
+  scratch_alloc(m, &s);
+  memcpy(s.e1, e1, sizeof(double) * (m->nc3 + 1) * (m->nc2 + 1) * m->nc1);
+  memcpy(s.e2, e2, sizeof(double) * (m->nc3 + 1) * m->nc2 * (m->nc1 + 1));
+  memcpy(s.e3, e3, sizeof(double) * m->nc3 * (m->nc2 + 1) * (m->nc1 + 1));
+  ct_update(m, b, wght, b1, b2, b3, &s);
+  scratch_free(&s);
+}
+
+/* EquationOfState::ConservedToPrimitive over a range, on the mesh's own u, w, bcc and b of
+ * block b (prim = the mesh's w); returns the relativistic failures */
+long orc_op_con2prim(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl, int ku) {
+  return con2prim_range(m, b, m->u + (long)b * NHYDRO * m->ncell,
+                        m->w + (long)b * NHYDRO * m->ncell, il, iu, jl, ju, kl, ku);
+}
+
+/* Hydro::NewBlockTimeStep (new_blockdt.cpp:45-230) of block b: cfl times the minimum */
+double orc_op_new_block_dt(orc_mesh *m, int b) { return new_block_dt(m, b); }
 
 #include "athena_oracle_ml.c"

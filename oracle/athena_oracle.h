@@ -86,6 +86,19 @@ int orc_set_multilevel(orc_mesh *m, const int *nbr_table, const int *nbr_count,
 #define ORC_RK2 1
 #define ORC_RK1 2
 void orc_set_integrator(orc_mesh *m, int integrator);
+
+/* per-operator restatements on block b (the member functions of one stage, one at a
+ * time; see athena_oracle.c) */
+void orc_op_fluxes(orc_mesh *m, int b, int order, double dt, double *flx1, double *flx2,
+                   double *flx3, double *const emf[9]);
+void orc_op_corner_e(orc_mesh *m, int b, const double *const emf[9], double *e1, double *e2,
+                     double *e3);
+void orc_op_add_flux_divergence(orc_mesh *m, int b, double wght, const double *flx1,
+                                const double *flx2, const double *flx3, double *u);
+void orc_op_ct(orc_mesh *m, int b, double wght, const double *e1, const double *e2,
+               const double *e3, double *b1, double *b2, double *b3);
+long orc_op_con2prim(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl, int ku);
+double orc_op_new_block_dt(orc_mesh *m, int b);
 /* the stages of one cycle and time += dt, without the new time step (adaptive runs
  * regrid in between); then orc_new_dt: NewBlockTimeStep + Mesh::NewTimeStep */
 void orc_advance(orc_mesh *m);

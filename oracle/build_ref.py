@@ -160,6 +160,80 @@ def build_variant(name, jobs=None):
     return vdir
 
 
+# The reference with the library's per-operator shim (athena_gb300/shim/): the member
+# functions the shim defines, and the reference object files that define them
+SHIM = os.path.join(os.path.dirname(HERE), "athena_gb300", "shim", "athgpu_operator_shim.cpp")
+SHIM_REPLACES = {
+    "src_hydro_calculate_fluxes.o": "Hydro::CalculateFluxes(",
+    "src_hydro_add_flux_divergence.o": "Hydro::AddFluxDivergence(",
+    "src_hydro_new_blockdt.o": "Hydro::NewBlockTimeStep(",
+    "src_field_calculate_corner_e.o": "Field::ComputeCornerE(",
+    "src_field_ct.o": "Field::CT(",
+    "src_eos_adiabatic_mhd.o": "EquationOfState::ConservedToPrimitive(",
+}
+
+
+def defined_symbols(obj):
+    """(mangled, demangled) names of the functions an object file defines (nm of an
+    object compiled here from the reference's sources)."""
+    raw = subprocess.run(["nm", "--defined-only", obj], capture_output=True, text=True,
+                         check=True).stdout.splitlines()
+    dem = subprocess.run(["nm", "-C", "--defined-only", obj], capture_output=True, text=True,
+                         check=True).stdout.splitlines()
+    out = []
+    for a, b in zip(raw, dem):
+        pa, pb = a.split(None, 2), b.split(None, 2)
+        if len(pa) == 3 and pa[1] in "TtWw":
+            out.append((pa[2], pb[2]))
+    return out
+
+
+def build_gpu_variant(base="mhd_hlld_g2", lib_dir=None):
+    """The reference linked with the operator shim: the base variant's objects, the six
+    replaced member functions made weak (objcopy --weaken-symbol) so that the shim's
+    definitions take their place, the shim compiled against the reference's headers and
+    this repository's include/, linked with libathgpu.so.  Writes
+    oracle/_ref/<base>_gpu/athena_lw (the reference's linear_wave problem generator and
+    the state dump hook).  Needs libathgpu.so built (athena_gb300/build.py)."""
+    flux, ng, sr = VARIANTS[base]
+    bdir = build_variant(base)
+    vdir = os.path.join(OUT, base + "_gpu")
+    wobj = os.path.join(vdir, "obj")
+    os.makedirs(wobj, exist_ok=True)
+    repo = os.path.dirname(HERE)
+    lib_dir = lib_dir or os.path.join(repo, "athena_gb300")
+    gen = os.path.join(bdir, "gen")
+    cxx = ["g++", "-O3", "-std=c++11", "-ffp-contract=off", "-I", gen,
+           "-I", os.path.join(gen, "a"), "-I", os.path.join(gen, "a", "b"),
+           "-I", os.path.join(gen, "a", "b", "c", "d"), "-I", os.path.join(REF, "src"),
+           "-I", os.path.join(repo, "include")]
+    objs = []
+    for o in sorted(glob.glob(os.path.join(bdir, "obj", "src_*.o"))):
+        name = os.path.basename(o)
+        if name.startswith("src_pgen_") and name != "src_pgen_default_pgen.o":
+            continue
+        if name in SHIM_REPLACES:
+            want = SHIM_REPLACES[name]
+            syms = [m for m, d in defined_symbols(o) if d.startswith(want)]
+            if len(syms) != 1:
+                raise RuntimeError("%s: %d definitions of %s" % (name, len(syms), want))
+            w = os.path.join(wobj, name)
+            run(["objcopy", "--weaken-symbol=" + syms[0], o, w])
+            objs.append(w)
+        else:
+            objs.append(o)
+    shim_o = os.path.join(wobj, "athgpu_operator_shim.o")
+    run(cxx + ["-c", SHIM, "-o", shim_o])
+    extra = [os.path.join(bdir, "obj", "src_pgen_linear_wave.o"),
+             os.path.join(bdir, "obj", "dump_hook.o")]
+    exe = os.path.join(vdir, "athena_lw")
+    cuda_lib = "/usr/local/cuda/lib64"
+    run(cxx + ["-o", exe] + objs + [shim_o] + extra +
+        ["-L", lib_dir, "-lathgpu", "-Wl,-rpath," + lib_dir, "-L", cuda_lib,
+         "-Wl,-rpath-link," + cuda_lib, "-lcudart"])
+    return exe
+
+
 def main(argv):
     names = argv or list(VARIANTS)
     for n in names:

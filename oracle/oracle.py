@@ -85,6 +85,17 @@ def lib():
         L.orc_refine_eps.argtypes = [ctypes.c_void_p, dp]
         L.orc_regrid.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ip, ip, ctypes.c_int, ip]
         L.orc_regrid.restype = ctypes.c_int
+        vp = ctypes.c_void_p
+        L.orc_op_fluxes.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, dp,
+                                    dp, ctypes.POINTER(dp)]
+        L.orc_op_corner_e.argtypes = [vp, ctypes.c_int, ctypes.POINTER(dp), dp, dp, dp]
+        L.orc_op_add_flux_divergence.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, dp,
+                                                 dp, dp]
+        L.orc_op_ct.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp, dp, dp, dp, dp, dp]
+        L.orc_op_con2prim.argtypes = [vp, ctypes.c_int] + [ctypes.c_int] * 6
+        L.orc_op_con2prim.restype = ctypes.c_long
+        L.orc_op_new_block_dt.argtypes = [vp, ctypes.c_int]
+        L.orc_op_new_block_dt.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -184,6 +195,32 @@ class OracleMesh:
 
     def stage(self, s):
         lib().orc_stage(self.h, s)
+
+    # --- per-operator restatements (block b; the checkers of the operator calls) ----
+    def _emf_ptrs(self, emf):
+        return (ctypes.POINTER(ctypes.c_double) * 9)(*[_p(a) for a in emf])
+
+    def op_fluxes(self, b, order, dt, flx, emf):
+        """Hydro::CalculateFluxes of block b into flx (3 arrays) and emf (9 arrays)."""
+        lib().orc_op_fluxes(self.h, b, order, dt, _p(flx[0]), _p(flx[1]), _p(flx[2]),
+                            self._emf_ptrs(emf))
+
+    def op_corner_e(self, b, emf, e):
+        lib().orc_op_corner_e(self.h, b, self._emf_ptrs(emf), _p(e[0]), _p(e[1]), _p(e[2]))
+
+    def op_add_flux_divergence(self, b, wght, flx, u):
+        lib().orc_op_add_flux_divergence(self.h, b, wght, _p(flx[0]), _p(flx[1]), _p(flx[2]),
+                                         _p(u))
+
+    def op_ct(self, b, wght, e, bf):
+        lib().orc_op_ct(self.h, b, wght, _p(e[0]), _p(e[1]), _p(e[2]), _p(bf[0]), _p(bf[1]),
+                        _p(bf[2]))
+
+    def op_con2prim(self, b, rng):
+        return lib().orc_op_con2prim(self.h, b, *rng)
+
+    def op_new_block_dt(self, b):
+        return lib().orc_op_new_block_dt(self.h, b)
 
     # --- adaptive refinement ---------------------------------------------------------
     def advance(self):

@@ -131,6 +131,13 @@ def test_div_b_stays_at_roundoff(precision, rsolver):
     assert div / bmax < 1e-13
 
 
+# FP32-vs-FP64 gates: about ten times the distances measured on GB300 for these cases
+# (relative L1 after 5 cycles 0.4e-7 .. 1.4e-7, rk2 1.2e-7 .. 2.9e-7; dt 1.5e-7)
+FP32_L1_GATE = 2e-6
+FP32_L1_GATE_RK2 = 3e-6
+FP32_DT_GATE = 2e-6
+
+
 def test_fp32_tracks_fp64():
     """FP32 bulk + compensated update + FP64 CT stays within a small relative L1
     distance of the FP64 path on a Mach-2 turbulent state after 5 cycles."""
@@ -140,8 +147,8 @@ def test_fp32_tracks_fp64():
     a, b = mesh.interior(u64), mesh.interior(u32)
     for n in range(5):
         rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(a[:, n]).mean()
-        assert rel < 2e-5, (n, rel)
-    assert np.allclose(dt32, dt64, rtol=1e-5)
+        assert rel < FP32_L1_GATE, (n, rel)
+    assert np.allclose(dt32, dt64, rtol=FP32_DT_GATE, atol=0)
 
 
 def test_sweep_segments_do_not_change_results():
@@ -292,8 +299,8 @@ def test_rk2_fp32_tracks_fp64_and_keeps_div_b():
     a, b = mesh.interior(u64), mesh.interior(u32)
     for n in range(5):
         rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(a[:, n]).mean()
-        assert rel < 2e-5, (n, rel)
-    assert np.allclose(dt32, dt64, rtol=1e-5)
+        assert rel < FP32_L1_GATE_RK2, (n, rel)
+    assert np.allclose(dt32, dt64, rtol=FP32_DT_GATE, atol=0)
     div = np.abs(_div_b(mesh, f1, f2, f3)).max()
     assert div / max(np.abs(f).max() for f in (f1, f2, f3)) < 1e-13
 
@@ -306,8 +313,8 @@ def test_physical_boundaries_fp32_tracks_fp64():
     a, b = mesh.interior(u64), mesh.interior(u32)
     for n in range(5):
         rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(a[:, n]).mean()
-        assert rel < 2e-5, (n, rel)
-    assert np.allclose(dt32, dt64, rtol=1e-5)
+        assert rel < FP32_L1_GATE, (n, rel)
+    assert np.allclose(dt32, dt64, rtol=FP32_DT_GATE, atol=0)
 
 
 def test_physical_boundaries_launch_count():
