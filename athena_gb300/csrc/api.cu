@@ -162,6 +162,10 @@ void free_all(athgpu_ctx* c) {
   if (c->cycle_graph) cudaGraphDestroy(c->cycle_graph);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   if (c->aux_stream) cudaStreamDestroy(c->aux_stream);
+  for (cudaStream_t cs : c->copy_stream)
+    if (cs) cudaStreamDestroy(cs);
+  for (cudaEvent_t ce : c->copy_ev)
+    if (ce) cudaEventDestroy(ce);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
 }
@@ -170,38 +174,101 @@ cudaError_t run_stage_dispatch(athgpu_ctx* c, int stage) {
   return c->desc.precision == ATHGPU_FP64 ? stage_fp64(c, stage) : stage_fp32(c, stage);
 }
 
-// host copy of a double array into a bulk-precision device register
-athgpu_status upload_bulk(athgpu_ctx* c, const double* h, void* dev, void* lo, long long n) {
-  const double* hd = c->real_bytes == 4 ? (const double*)pinned_device_ptr(h) : nullptr;
-  if (c->real_bytes == 8) {
-    CK(cudaMemcpyAsync(dev, h, n * 8, cudaMemcpyHostToDevice, c->stream));
-  } else if (hd) {  // page-locked host array: converted while it is read over the link
+// ---- host <-> device copies of the state ----------------------------------------------
+// Copy-engine mode (host_copy_mode 0, the default): each array moves in chunks of
+// COPY_CHUNK bytes spread round-robin over the context's copy streams, so several DMA
+// copies run at once; in FP32 mode every chunk's conversion (split/join) runs on the
+// context's stream, ordered after (upload) or before (download) its own copy by an event,
+// so conversions overlap the remaining copies.  Host-link mode (1): the conversion kernels
+// read or write page-locked host arrays in place over the link (FP32 contexts).
+constexpr long long COPY_CHUNK = 64LL << 20;
+
+cudaEvent_t next_copy_event(athgpu_ctx* c) {
+  cudaEvent_t e = c->copy_ev[c->copy_ev_next];
+  c->copy_ev_next = (c->copy_ev_next + 1) % athgpu_ctx::NCOPY_EV;
+  return e;
+}
+
+// the copy streams start after everything queued on the context's stream
+cudaError_t fork_copies(athgpu_ctx* c) {
+  cudaEvent_t ev = next_copy_event(c);
+  cudaError_t e = cudaEventRecord(ev, c->stream);
+  for (int q = 0; q < athgpu_ctx::NCOPY && e == cudaSuccess; ++q)
+    e = cudaStreamWaitEvent(c->copy_stream[q], ev, 0);
+  return e;
+}
+// the context's stream continues after every copy
+cudaError_t join_copies(athgpu_ctx* c) {
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < athgpu_ctx::NCOPY && e == cudaSuccess; ++q) {
+    cudaEvent_t ev = next_copy_event(c);
+    e = cudaEventRecord(ev, c->copy_stream[q]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, ev, 0);
+  }
+  return e;
+}
+
+// plain FP64 array, host <-> device, chunked over the copy streams (after fork_copies)
+athgpu_status copy_chunked(athgpu_ctx* c, void* dst, const void* src, long long bytes,
+                           cudaMemcpyKind kind, int* rr) {
+  for (long long off = 0; off < bytes; off += COPY_CHUNK) {
+    const long long nb = bytes - off < COPY_CHUNK ? bytes - off : COPY_CHUNK;
+    CK(cudaMemcpyAsync((char*)dst + off, (const char*)src + off, nb, kind,
+                       c->copy_stream[(*rr)++ % athgpu_ctx::NCOPY]));
+  }
+  return ATHGPU_OK;
+}
+
+// host copy of a double array into a bulk-precision device register (after fork_copies)
+athgpu_status upload_bulk(athgpu_ctx* c, const double* h, void* dev, void* lo, long long n,
+                          int* rr) {
+  if (c->real_bytes == 8)
+    return copy_chunked(c, dev, h, n * 8, cudaMemcpyHostToDevice, rr);
+  const double* hd = c->host_copy_mode == 1 ? (const double*)pinned_device_ptr(h) : nullptr;
+  if (hd) {  // page-locked host array: converted while it is read over the link
     split_from_host_kernel<<<link_grid(n), 256, 0, c->stream>>>(hd, (float*)dev, (float*)lo,
                                                                 n);
     CK(cudaGetLastError());
-  } else {
-    CK(cudaMemcpyAsync(c->staging, h, n * 8, cudaMemcpyHostToDevice, c->stream));
-    split_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(c->staging, (float*)dev,
-                                                                     (float*)lo, n);
+    return ATHGPU_OK;
+  }
+  const long long chunk = COPY_CHUNK / 8;
+  for (long long off = 0; off < n; off += chunk) {
+    const long long cn = n - off < chunk ? n - off : chunk;
+    cudaStream_t cs = c->copy_stream[(*rr)++ % athgpu_ctx::NCOPY];
+    CK(cudaMemcpyAsync(c->staging + off, h + off, cn * 8, cudaMemcpyHostToDevice, cs));
+    cudaEvent_t ev = next_copy_event(c);
+    CK(cudaEventRecord(ev, cs));
+    CK(cudaStreamWaitEvent(c->stream, ev, 0));
+    split_kernel<<<(unsigned)ceil_div(cn, 256), 256, 0, c->stream>>>(
+        c->staging + off, (float*)dev + off, lo ? (float*)lo + off : nullptr, cn);
     CK(cudaGetLastError());
   }
   return ATHGPU_OK;
 }
 
+// device register to a host double array (after fork_copies; the caller joins)
 athgpu_status download_bulk(athgpu_ctx* c, double* h, const void* dev, const void* lo,
-                            long long n) {
-  double* hd = c->real_bytes == 4 ? (double*)pinned_device_ptr(h) : nullptr;
-  if (c->real_bytes == 8) {
-    CK(cudaMemcpyAsync(h, dev, n * 8, cudaMemcpyDeviceToHost, c->stream));
-  } else if (hd) {  // page-locked host array: written in place over the link
+                            long long n, int* rr) {
+  if (c->real_bytes == 8)
+    return copy_chunked(c, h, dev, n * 8, cudaMemcpyDeviceToHost, rr);
+  double* hd = c->host_copy_mode == 1 ? (double*)pinned_device_ptr(h) : nullptr;
+  if (hd) {  // page-locked host array: written in place over the link
     join_to_host_kernel<<<link_grid(n), 256, 0, c->stream>>>((const float*)dev,
                                                              (const float*)lo, hd, n);
     CK(cudaGetLastError());
-  } else {
-    join_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(
-        (const float*)dev, (const float*)lo, c->staging, n);
+    return ATHGPU_OK;
+  }
+  const long long chunk = COPY_CHUNK / 8;
+  for (long long off = 0; off < n; off += chunk) {
+    const long long cn = n - off < chunk ? n - off : chunk;
+    join_kernel<<<(unsigned)ceil_div(cn, 256), 256, 0, c->stream>>>(
+        (const float*)dev + off, lo ? (const float*)lo + off : nullptr, c->staging + off, cn);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h, c->staging, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    cudaEvent_t ev = next_copy_event(c);
+    CK(cudaEventRecord(ev, c->stream));
+    cudaStream_t cs = c->copy_stream[(*rr)++ % athgpu_ctx::NCOPY];
+    CK(cudaStreamWaitEvent(cs, ev, 0));
+    CK(cudaMemcpyAsync(h + off, c->staging + off, cn * 8, cudaMemcpyDeviceToHost, cs));
   }
   return ATHGPU_OK;
 }
@@ -244,9 +311,10 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "unknown Riemann solver");
   if (d->precision != ATHGPU_FP64 && d->precision != ATHGPU_FP32)
     return fail(ATHGPU_ERR_ARG, "unknown precision");
-  if (d->relativistic && d->rsolver != ATHGPU_HLLE)
+  if (d->relativistic && d->rsolver != ATHGPU_HLLE && d->rsolver != ATHGPU_LLF)
     return fail(ATHGPU_ERR_UNSUPPORTED,
-                "relativistic MHD supports the HLLE solver (hlle_mhd_rel.cpp) only");
+                "relativistic MHD supports the HLLE and LLF solvers (hlle_mhd_rel.cpp, "
+                "llf_mhd_rel.cpp) only");
   if (d->relativistic && !(d->gamma_max > 1.0))
     return fail(ATHGPU_ERR_ARG, "gamma_max must exceed 1 (adiabatic_mhd_sr.cpp:48)");
   if (!d->x1f || !d->dx1f || !d->x2f || !d->dx2f || !d->x3f || !d->dx3f)
@@ -327,6 +395,11 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
   e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
+  for (int q = 0; q < athgpu_ctx::NCOPY && e == cudaSuccess; ++q)
+    e = cudaStreamCreateWithFlags(&c->copy_stream[q], cudaStreamNonBlocking);
+  for (int q = 0; q < athgpu_ctx::NCOPY_EV && e == cudaSuccess; ++q)
+    e = cudaEventCreateWithFlags(&c->copy_ev[q], cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "copy streams"));
 
   const i64 nb = m.nb, rb = c->real_bytes;
   Registers& r = c->r;
@@ -644,11 +717,18 @@ athgpu_status athgpu_upload_state(athgpu_ctx* c, const double* u, const double* 
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   const DevMesh& m = c->m;
   athgpu_status s;
-  if (u && (s = upload_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
+  int rr = 0;
+  CK(fork_copies(c));
+  // the face fields first: plain copies that need no conversion
+  if (b1 && (s = copy_chunked(c, c->r.b1, b1, m.nb * m.nf1 * 8, cudaMemcpyHostToDevice, &rr)))
     return s;
-  if (b1) CK(cudaMemcpyAsync(c->r.b1, b1, m.nb * m.nf1 * 8, cudaMemcpyHostToDevice, c->stream));
-  if (b2) CK(cudaMemcpyAsync(c->r.b2, b2, m.nb * m.nf2 * 8, cudaMemcpyHostToDevice, c->stream));
-  if (b3) CK(cudaMemcpyAsync(c->r.b3, b3, m.nb * m.nf3 * 8, cudaMemcpyHostToDevice, c->stream));
+  if (b2 && (s = copy_chunked(c, c->r.b2, b2, m.nb * m.nf2 * 8, cudaMemcpyHostToDevice, &rr)))
+    return s;
+  if (b3 && (s = copy_chunked(c, c->r.b3, b3, m.nb * m.nf3 * 8, cudaMemcpyHostToDevice, &rr)))
+    return s;
+  if (u && (s = upload_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell, &rr)))
+    return s;
+  CK(join_copies(c));
   CK(cudaStreamSynchronize(c->stream));
   return ATHGPU_OK;
 }
@@ -657,8 +737,13 @@ athgpu_status athgpu_upload_prim(athgpu_ctx* c, const double* w) {
   if (!c || !w) return fail(ATHGPU_ERR_ARG, "null argument");
   const i64 n = (i64)c->m.nb * 5 * c->m.ncell;
   athgpu_status s;
-  for (int q = 0; q < 2; ++q)
-    if ((s = upload_bulk(c, w, c->r.wbuf[q], nullptr, n)) != ATHGPU_OK) return s;
+  int rr = 0;
+  CK(fork_copies(c));
+  if ((s = upload_bulk(c, w, c->r.wbuf[0], nullptr, n, &rr)) != ATHGPU_OK) return s;
+  CK(join_copies(c));
+  // the second primitive buffer: the same values, copied on the device
+  CK(cudaMemcpyAsync(c->r.wbuf[1], c->r.wbuf[0], n * c->real_bytes, cudaMemcpyDeviceToDevice,
+                     c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return ATHGPU_OK;
 }
@@ -668,14 +753,20 @@ athgpu_status athgpu_download_state(athgpu_ctx* c, double* u, double* b1, double
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   const DevMesh& m = c->m;
   athgpu_status s;
-  if (u) {  // the stages do not keep U's ghost cells: refresh them from their owners
-    CK(c->desc.precision == ATHGPU_FP64 ? exchange_u_fp64(c) : exchange_u_fp32(c));
-    if ((s = download_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell)) != ATHGPU_OK)
-      return s;
-  }
-  if (b1) CK(cudaMemcpyAsync(b1, c->r.b1, m.nb * m.nf1 * 8, cudaMemcpyDeviceToHost, c->stream));
-  if (b2) CK(cudaMemcpyAsync(b2, c->r.b2, m.nb * m.nf2 * 8, cudaMemcpyDeviceToHost, c->stream));
-  if (b3) CK(cudaMemcpyAsync(b3, c->r.b3, m.nb * m.nf3 * 8, cudaMemcpyDeviceToHost, c->stream));
+  int rr = 0;
+  // the stages do not keep U's ghost cells: refresh them from their owners first (the
+  // exchange also rewrites the face fields' ghosts), then every copy follows it
+  if (u) CK(c->desc.precision == ATHGPU_FP64 ? exchange_u_fp64(c) : exchange_u_fp32(c));
+  CK(fork_copies(c));
+  if (b1 && (s = copy_chunked(c, b1, c->r.b1, m.nb * m.nf1 * 8, cudaMemcpyDeviceToHost, &rr)))
+    return s;
+  if (b2 && (s = copy_chunked(c, b2, c->r.b2, m.nb * m.nf2 * 8, cudaMemcpyDeviceToHost, &rr)))
+    return s;
+  if (b3 && (s = copy_chunked(c, b3, c->r.b3, m.nb * m.nf3 * 8, cudaMemcpyDeviceToHost, &rr)))
+    return s;
+  if (u && (s = download_bulk(c, u, c->r.u, c->r.ulo, (i64)m.nb * 5 * m.ncell, &rr)))
+    return s;
+  CK(join_copies(c));
   CK(cudaStreamSynchronize(c->stream));
   return ATHGPU_OK;
 }
@@ -684,13 +775,25 @@ athgpu_status athgpu_download_prim(athgpu_ctx* c, double* w, double* bcc) {
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   const DevMesh& m = c->m;
   athgpu_status s;
-  if (w && (s = download_bulk(c, w, c->r.wbuf[c->r.wsel], nullptr, (i64)m.nb * 5 * m.ncell)) !=
-               ATHGPU_OK)
+  int rr = 0;
+  CK(fork_copies(c));
+  if (w && (s = download_bulk(c, w, c->r.wbuf[c->r.wsel], nullptr, (i64)m.nb * 5 * m.ncell,
+                              &rr)) != ATHGPU_OK)
     return s;
-  if (bcc && (s = download_bulk(c, bcc, c->r.bcc, nullptr, (i64)m.nb * 3 * m.ncell)) !=
+  // FP32: bcc's conversions reuse the staging buffer once w's copies out of it are done
+  if (w && bcc && c->real_bytes == 4) CK(join_copies(c));
+  if (bcc && (s = download_bulk(c, bcc, c->r.bcc, nullptr, (i64)m.nb * 3 * m.ncell, &rr)) !=
                  ATHGPU_OK)
     return s;
+  CK(join_copies(c));
   CK(cudaStreamSynchronize(c->stream));
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_host_copy(athgpu_ctx* c, int mode) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (mode != 0 && mode != 1) return fail(ATHGPU_ERR_ARG, "host copy mode must be 0 or 1");
+  c->host_copy_mode = mode;
   return ATHGPU_OK;
 }
 

@@ -63,6 +63,13 @@ struct athgpu_ctx {
   cudaStream_t own_stream = nullptr, stream = nullptr;
   // second stream for the ghost exchange beside W(U), forked and joined with events
   cudaStream_t aux_stream = nullptr;
+  // host <-> device state copies: chunks spread over these streams (copy engines), each
+  // chunk's conversion ordered after its copy with an event from the pool
+  static const int NCOPY = 4, NCOPY_EV = 64;
+  cudaStream_t copy_stream[NCOPY] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t copy_ev[NCOPY_EV] = {};
+  int copy_ev_next = 0;
+  int host_copy_mode = 0;  // athgpu_set_host_copy
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t cycle_exec = nullptr;
   cudaGraph_t cycle_graph = nullptr;

@@ -263,7 +263,8 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   else if (RS == 1) hlle<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
   else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);
-  else hlle_sr<Real>(gam, wli, wri, bx, f);  // RS 2: special relativity
+  else if (RS == 5) llf_sr<Real>(gam, wli, wri, bx, f);  // special relativity, LLF
+  else hlle_sr<Real>(gam, wli, wri, bx, f);  // RS 2: special relativity, HLLE
   fn[IDN] = f[0];
   fn[ivx] = f[1];
   fn[ivy] = f[2];

@@ -770,13 +770,13 @@ __device__ __forceinline__ void sr_fast_speeds(Real gamma_adi, Real wgas, Real p
   *lm = (a1 >= RC(0.0)) ? (-a1 - s) / RC(2.0) : RC(-2.0) * a0 / (a1 - s);
 }
 
-// Frame-transforming HLLE (Mignone & Bodo 2005), SR branch of
-// hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330.  Local order as for hlld().
+// The L and R states of the SR frame-transforming solvers (Mignone & Bodo 2005; the same
+// operations in hlle_mhd_rel.cpp:160-260 and llf_mhd_rel.cpp:136-220): conserved state and
+// flux of each side (MUB 8, 15) and its fast speeds.  Local order as for hlld().
 template <typename Real>
-__device__ __forceinline__ void hlle_sr(Real gamma_adi, const Real* wli, const Real* wri,
-                                        Real bb1, Real* f) {
-  Real cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
-  Real lml, lpl, lmr, lpr;
+__device__ __forceinline__ void sr_states(Real gamma_adi, const Real* wli, const Real* wri,
+                                          Real bb1, Real* cl, Real* cr, Real* fl, Real* fr,
+                                          Real& lml, Real& lpl, Real& lmr, Real& lpr) {
 #pragma unroll
   for (int sd = 0; sd < 2; ++sd) {
     const Real* w = sd == 0 ? wli : wri;
@@ -810,6 +810,15 @@ __device__ __forceinline__ void hlle_sr(Real gamma_adi, const Real* wli, const R
     ff[5] = b2 * u1 - b1 * u2;
     ff[6] = b3 * u1 - b1 * u3;
   }
+}
+
+// SR frame-transforming HLLE, hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330 (SR branch)
+template <typename Real>
+__device__ __forceinline__ void hlle_sr(Real gamma_adi, const Real* wli, const Real* wri,
+                                        Real bb1, Real* f) {
+  Real cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  Real lml, lpl, lmr, lpr;
+  sr_states<Real>(gamma_adi, wli, wri, bb1, cl, cr, fl, fr, lml, lpl, lmr, lpr);
   Real lambda_l = smin(lml, lmr);
   Real lambda_r = smax(lpl, lpr);
   Real lambda_diff_inv = RC(1.0) / (lambda_r - lambda_l);
@@ -821,6 +830,21 @@ __device__ __forceinline__ void hlle_sr(Real gamma_adi, const Real* wli, const R
     else f[n] = (lambda_r * fl[n] - lambda_l * fr[n] + lambda_l * lambda_r * (cr[n] - cl[n])) *
                 lambda_diff_inv;
   }
+}
+
+// SR frame-transforming LLF, hydro/rsolvers/mhd/llf_mhd_rel.cpp:101-280 (SR branch):
+// lambda = max(lambda_r, -lambda_l) (MB 55), F = (F_l + F_r - lambda (U_r - U_l)) / 2
+template <typename Real>
+__device__ __forceinline__ void llf_sr(Real gamma_adi, const Real* wli, const Real* wri,
+                                       Real bb1, Real* f) {
+  Real cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  Real lml, lpl, lmr, lpr;
+  sr_states<Real>(gamma_adi, wli, wri, bb1, cl, cr, fl, fr, lml, lpl, lmr, lpr);
+  Real lambda_l = smin(lml, lmr);
+  Real lambda_r = smax(lpl, lpr);
+  Real lambda = smax(lambda_r, -lambda_l);
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) f[n] = RC(0.5) * (fl[n] + fr[n] - lambda * (cr[n] - cl[n]));
 }
 
 // Newman & Hamlin (2014) fixed-point con2prim with Aitken acceleration,

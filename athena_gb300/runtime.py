@@ -428,6 +428,11 @@ class StageUpdate:
         _check(load_library().athgpu_set_sweep_segment(self.h, seg_x2, seg_x3),
                "athgpu_set_sweep_segment")
 
+    def set_host_copy(self, mode):
+        """0: chunked DMA over several copy streams (default); 1: conversion kernels on
+        page-locked host memory."""
+        _check(load_library().athgpu_set_host_copy(self.h, int(mode)), "athgpu_set_host_copy")
+
     def set_stream(self, stream_ptr):
         _check(load_library().athgpu_set_stream(self.h, ctypes.c_void_p(stream_ptr)),
                "athgpu_set_stream")

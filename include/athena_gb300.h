@@ -34,7 +34,8 @@ typedef int athgpu_status;
 
 #define ATHGPU_HLLD 0            /* --flux=hlld  (hydro/rsolvers/mhd/hlld.cpp) */
 #define ATHGPU_HLLE 1            /* --flux=hlle  (hydro/rsolvers/mhd/hlle_mhd.cpp) */
-#define ATHGPU_LLF 2             /* --flux=llf   (hydro/rsolvers/mhd/llf_mhd.cpp) */
+#define ATHGPU_LLF 2             /* --flux=llf   (hydro/rsolvers/mhd/llf_mhd.cpp; relativistic:
+                                    llf_mhd_rel.cpp) */
 #define ATHGPU_ROE 3             /* --flux=roe   (hydro/rsolvers/mhd/roe_mhd.cpp) */
 #define ATHGPU_FP64 0            /* every operation in FP64: bit-identical to the reference */
 #define ATHGPU_FP32 1            /* FP32 reconstruction/Riemann/divergence, compensated
@@ -53,8 +54,9 @@ typedef struct {
   int xorder;             /* time/xorder: 2 = PLM, 3 = PPM (stage 1 is donor cell) */
   int rsolver;            /* ATHGPU_HLLD, ATHGPU_HLLE, ATHGPU_LLF or ATHGPU_ROE */
   int precision;          /* ATHGPU_FP64 or ATHGPU_FP32 */
-  int relativistic;       /* 1: special-relativistic MHD (-s): HLLE solver only, FP64
-                             Newman-Hamlin con2prim (adiabatic_mhd_sr.cpp) */
+  int relativistic;       /* 1: special-relativistic MHD (-s): the HLLE or LLF solver
+                             (hlle_mhd_rel.cpp, llf_mhd_rel.cpp), FP64 Newman-Hamlin
+                             con2prim (adiabatic_mhd_sr.cpp) */
   double gamma;           /* hydro/gamma */
   double dfloor, pfloor;  /* hydro/dfloor, hydro/pfloor (adiabatic_mhd.cpp:29-30) */
   double cfl_number;      /* time/cfl_number */
@@ -232,6 +234,13 @@ athgpu_status athgpu_upload_state(athgpu_ctx *ctx, const double *u, const double
                                   const double *b2, const double *b3);
 athgpu_status athgpu_download_state(athgpu_ctx *ctx, double *u, double *b1, double *b2,
                                     double *b3);
+/* How the state calls above move data between host and device memory.  mode 0 (the
+ * default): DMA copies in 64 MB chunks spread over several streams (copy engines), the
+ * FP32 conversions on the device overlapping the remaining copies; mode 1: for FP32
+ * contexts and page-locked host arrays, conversion kernels that read or write the host
+ * arrays in place over the host link (no device staging).  Results are identical. */
+athgpu_status athgpu_set_host_copy(athgpu_ctx *ctx, int mode);
+
 /* Initial primitives W = phydro->w (relativistic runs: also the initial guess of the
  * con2prim solve, which the reference seeds from its w / w1 registers,
  * adiabatic_mhd_sr.cpp:143-154).  Synchronous. */

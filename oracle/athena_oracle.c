@@ -701,14 +701,15 @@ static void roe(double gamma, const double *wli, const double *wri, double bxi,
   }
 }
 
-/* SR frame-transforming HLLE, hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330 (SR branch).
- * Local order as for hlld(); velocities are the spatial 4-velocity u^i. */
-static void hlle_sr(double gamma_adi, const double *wli, const double *wri, double bb1,
-                    double *f) {
-  double cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
-  double lml, lpl, lmr, lpr;
+/* The L and R states of the SR frame-transforming solvers (hlle_mhd_rel.cpp:160-260,
+ * llf_mhd_rel.cpp:136-220, the same operations): conserved state and flux (MUB 8, 15) of
+ * each side and its fast speeds.  Local order as for hlld(); velocities are the spatial
+ * 4-velocity u^i. */
+static void sr_states(double gamma_adi, const double *wli, const double *wri, double bb1,
+                      double *cl, double *cr, double *fl, double *fr, double *lml,
+                      double *lpl, double *lmr, double *lpr) {
   const double *wv[2] = {wli, wri};
-  double *cv[2] = {cl, cr}, *fv[2] = {fl, fr}, *lm[2] = {&lml, &lmr}, *lp[2] = {&lpl, &lpr};
+  double *cv[2] = {cl, cr}, *fv[2] = {fl, fr}, *lm[2] = {lml, lmr}, *lp[2] = {lpl, lpr};
   for (int s = 0; s < 2; ++s) {
     const double *w = wv[s];
     double rho = w[IDN], pgas = w[IPR];
@@ -742,6 +743,14 @@ static void hlle_sr(double gamma_adi, const double *wli, const double *wri, doub
     f[5] = b[2] * u[1] - b[1] * u[2];
     f[6] = b[3] * u[1] - b[1] * u[3];
   }
+}
+
+/* SR frame-transforming HLLE, hydro/rsolvers/mhd/hlle_mhd_rel.cpp:103-330 (SR branch) */
+static void hlle_sr(double gamma_adi, const double *wli, const double *wri, double bb1,
+                    double *f) {
+  double cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  double lml, lpl, lmr, lpr;
+  sr_states(gamma_adi, wli, wri, bb1, cl, cr, fl, fr, &lml, &lpl, &lmr, &lpr);
   double lambda_l = smin(lml, lmr);
   double lambda_r = smax(lpl, lpr);
   double lambda_diff_inv = 1.0 / (lambda_r - lambda_l);
@@ -752,6 +761,19 @@ static void hlle_sr(double gamma_adi, const double *wli, const double *wri, doub
     else f[n] = (lambda_r * fl[n] - lambda_l * fr[n] + lambda_l * lambda_r * (cr[n] - cl[n])) *
                 lambda_diff_inv;
   }
+}
+
+/* SR frame-transforming LLF, hydro/rsolvers/mhd/llf_mhd_rel.cpp:101-280 (SR branch):
+ * lambda = max(lambda_r, -lambda_l) (MB 55), F = (F_l + F_r - lambda (U_r - U_l)) / 2 */
+static void llf_sr(double gamma_adi, const double *wli, const double *wri, double bb1,
+                   double *f) {
+  double cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  double lml, lpl, lmr, lpr;
+  sr_states(gamma_adi, wli, wri, bb1, cl, cr, fl, fr, &lml, &lpl, &lmr, &lpr);
+  double lambda_l = smin(lml, lmr);
+  double lambda_r = smax(lpl, lpr);
+  double lambda = smax(lambda_r, -lambda_l);
+  for (int n = 0; n < NWAVE; ++n) f[n] = 0.5 * (fl[n] + fr[n] - lambda * (cr[n] - cl[n]));
 }
 
 /* ------------------------------------------------------------------------------------
@@ -929,7 +951,8 @@ static void riemann(const orc_mesh *m, int dir, const double *wl, const double *
   int ivx = IVX + dir, ivy = IVX + (dir + 1) % 3, ivz = IVX + (dir + 2) % 3;
   double wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
   double wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
-  if (m->p.relativistic) hlle_sr(m->p.gamma, wli, wri, bx, flx7);
+  if (m->p.relativistic && m->p.rsolver == 2) llf_sr(m->p.gamma, wli, wri, bx, flx7);
+  else if (m->p.relativistic) hlle_sr(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 2) llf(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 3) roe(m->p.gamma, wli, wri, bx, flx7);

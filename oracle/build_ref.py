@@ -30,6 +30,11 @@ from concurrent.futures import ThreadPoolExecutor
 
 REF = os.environ.get("ATHENA_REF_SRC", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def reference_present():
+    """True where the reference's source tree is available (this recipe can build)."""
+    return os.path.isdir(os.path.join(REF, "src"))
 OUT = os.path.join(HERE, "_ref")
 
 # variant -> (riemann solver, nghost, relativistic)
@@ -42,6 +47,7 @@ VARIANTS = {
     "mhd_llf_g2": ("llf", 2, False),     # local Lax-Friedrichs (llf_mhd.cpp)
     "mhd_roe_g2": ("roe", 2, False),     # Roe linearisation (roe_mhd.cpp)
     "srmhd_hlle_g2": ("hlle", 2, True),
+    "srmhd_llf_g2": ("llf", 2, True),    # relativistic LLF (llf_mhd_rel.cpp)
 }
 
 

@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the reference source tree (default /root/reference):
+Run where the reference source tree is present (oracle/build_ref.py says where):
 
     python tests/golden/make_golden.py
 
@@ -72,6 +72,11 @@ CASES = {
                                             (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
     "srkh_hlle_plm_1blk": ("srmhd_hlle_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
                                             (1., 1., 1.)), "sr_kh", 2, 0.4, 4),
+    # relativistic LLF (-s -b --flux=llf, llf_mhd_rel.cpp)
+    "srkh_llf_plm_8blk": ("srmhd_llf_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                          (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
+    "srkh_llf_plm_1blk": ("srmhd_llf_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
+                                          (1., 1., 1.)), "sr_kh", 2, 0.4, 4),
     # physical boundaries (flags inner/outer x1, x2, x3: 1 outflow, 2 reflecting)
     "blastbc_hlld_plm_8blk": ("mhd_hlld_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
                                               (.5, .5, .5)), "blast", 2, 0.3, 4),

@@ -338,3 +338,37 @@ def test_invalid_boundary_flags_are_rejected():
     for bad in ((0, 1, 0, 0, 0, 0), (3, 3, 0, 0, 0, 0)):
         with pytest.raises(AthGPUError):
             StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlld", bc=bad)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_host_copy_modes_agree(precision):
+    """The two host-copy modes (chunked DMA over several streams; conversion kernels on
+    page-locked host memory) move the same bits, from pageable and pinned host arrays."""
+    import torch
+    mesh, ic, c = _turb_case(nx=(48, 32, 32), nb=(3, 2, 2), xorder=2, ng=2)
+    outs = []
+    for mode in (0, 1):
+        for pinned in (False, True):
+            g = StageUpdate(mesh, c["gamma"], xorder=2, rsolver="hlld", precision=precision,
+                            tlim=1e3)
+            g.set_host_copy(mode)
+            src = ic
+            if pinned:
+                src = [torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+                       for a in ic]
+                for p, a in zip(src, ic):
+                    p[...] = a
+            g.set_state(*src)
+            g.initialize()
+            g.cycle(2)
+            dst = None
+            if pinned:
+                dst = [torch.zeros(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+                       for a in ic]
+            out = [np.array(a) for a in g.state(out=dst)]
+            w, bcc = g.prim()
+            outs.append(out + [w, bcc])
+            g.close()
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert np.array_equal(a, b)

@@ -47,7 +47,7 @@ def _network():
 
 
 def _run(mesh, c, ic, w0, ncycle, precision="fp64", start=None, stats=None):
-    g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver="hlle",
+    g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c.get("rsolver", "hlle"),
                     precision=precision, cfl=c["cfl"], tlim=c["tlim"], relativistic=True,
                     integrator=c.get("integrator", "vl2"))
     if start is not None:
@@ -149,6 +149,31 @@ def test_sr_fp32_tracks_fp64_and_keeps_div_b():
            + b2[:, ng:ng + n3, ng + 1:ng + n2 + 1, ng:ng + n1] - b2[:, ng:ng + n3, ng:ng + n2, ng:ng + n1]
            + b3[:, ng + 1:ng + n3 + 1, ng:ng + n2, ng:ng + n1] - b3[:, ng:ng + n3, ng:ng + n2, ng:ng + n1])
     assert np.abs(div).max() / np.abs(b1).max() < 1e-13
+
+
+def test_sr_llf_matches_oracle_rk2():
+    """The relativistic LLF solver (llf_mhd_rel.cpp) under RK2 with PPM: within 1e-12 of
+    the oracle per cell."""
+    mesh = MeshSpec((32, 32, 32), (2, 2, 2), 3)
+    gw, f1, f2, f3 = pgen.sr_kelvin_helmholtz(mesh.nx, seed=6, noise=0.02)
+    gu = pgen.sr_prim_to_cons(gw, pgen.cell_centered(f1, f2, f3), 4.0 / 3.0)
+    ic = (mesh.scatter_cells(gu),) + mesh.scatter_faces(f1, f2, f3)
+    w0 = mesh.scatter_cells(gw)
+    c = {"gamma": 4.0 / 3.0, "xorder": 3, "cfl": 0.5, "tlim": 1e3, "rsolver": "llf",
+         "integrator": "rk2"}
+    (u, *_), w, dts = _run(mesh, c, ic, w0, 3)
+    om = O.OracleMesh(mesh, c["gamma"], xorder=3, rsolver="llf", tlim=c["tlim"], cfl=0.5,
+                      relativistic=True, integrator="rk2")
+    om.set_state(*ic)
+    om.set_prim(w0)
+    om.initialize()
+    om.cycle(3)
+    a, b = mesh.interior(u), mesh.interior(om.state()[0])
+    for n in range(5):
+        assert close(a[:, n], b[:, n]), n
+    aw, bw = mesh.interior(w), mesh.interior(om.prim()[0])
+    for n in range(5):
+        assert close(aw[:, n], bw[:, n], rtol=1e-11), n
 
 
 @pytest.mark.parametrize("bc", [(2, 2, 1, 1, 2, 1), (0, 0, 2, 2, 0, 0)])

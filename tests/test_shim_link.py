@@ -27,7 +27,7 @@ def _sizes(path):
     return sizes
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(build_ref.REF, "src")),
+@pytest.mark.skipif(not build_ref.reference_present(),
                     reason="the reference source tree is not present")
 def test_shim_replaces_the_stage_operators():
     from athena_gb300 import build
