@@ -118,6 +118,16 @@ unsigned link_grid(long long n) {
 }  // namespace
 
 namespace athgpu {
+// whether the x3 sweep's TMA bulk staging can run on this context (stage_impl.cuh's rule
+// without the selection flag)
+bool x3_bulk_eligible(const athgpu_ctx* c) {
+  const DevMesh& m = c->m;
+  if (m.ml.on) return false;
+  const long long plane = (long long)m.nc1 * m.nc2, row0 = (long long)(m.js - 1) * m.nc1;
+  return (plane * c->real_bytes) % 16 == 0 && (row0 * c->real_bytes) % 16 == 0 &&
+         (plane * 8) % 16 == 0 && (row0 * 8) % 16 == 0;
+}
+
 // Device memory of the contexts comes from the device's stream-ordered pool, configured to
 // keep what is freed (no release threshold): a regrid allocates the new mesh's registers
 // while the old ones exist and frees the old ones after, so from the second regrid on the
@@ -434,6 +444,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   // path from the stale pressure itself (the reference's start)
   c->c2p_start = rb == 4 ? C2P_START_REFINED : C2P_START_STALE;
   for (auto& a : allocs) {
+    // 4 KB beyond every register: the x3 sweep's bulk staging copies whole 128-element rows,
+    // and the last CTA of the last k-plane of an array overhangs its end (never used)
+    a.bytes += 4096;
     e = pool_alloc(a.p, a.bytes, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync"));
     e = cudaMemsetAsync(*a.p, 0, a.bytes, c->stream);
@@ -956,6 +969,26 @@ athgpu_status athgpu_set_c2p_start(athgpu_ctx* c, int start, const float* params
   return ATHGPU_OK;
 }
 
+athgpu_status athgpu_get_x3_staging(athgpu_ctx* c, int* bulk) {
+  if (!c || !bulk) return fail(ATHGPU_ERR_ARG, "null argument");
+  *bulk = (c->lc.x3_bulk && x3_bulk_eligible(c)) ? 1 : 0;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_x3_staging(athgpu_ctx* c, int bulk) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (bulk != 0 && bulk != 1) return fail(ATHGPU_ERR_ARG, "x3 staging must be 0 or 1");
+  c->lc.x3_bulk = bulk;
+  if (c->cycle_exec) {  // re-capture with the other kernel
+    CK(cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(c->cycle_exec);
+    c->cycle_exec = nullptr;
+    cudaGraphDestroy(c->cycle_graph);
+    c->cycle_graph = nullptr;
+  }
+  return ATHGPU_OK;
+}
+
 athgpu_status athgpu_set_sweep_segment(athgpu_ctx* c, int seg_x2, int seg_x3) {
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   if (seg_x2 < 0 || seg_x3 < 0) return fail(ATHGPU_ERR_ARG, "negative segment");
@@ -1100,6 +1133,23 @@ athgpu_status athgpu_autotune(athgpu_ctx* c, int cycles, int* seg_x2, int* seg_x
       }
     }
   }
+  // the x3 sweep's staging (per-thread cp.async or TMA bulk copies) at those segments
+  int best_bulk = c->lc.x3_bulk;
+  if (st == ATHGPU_OK) {
+    c->lc.seg_x2 = best2;
+    c->lc.seg_x3 = best3;
+    float best_ms = 3.0e38f;
+    for (int bulk = 0; bulk <= 1 && st == ATHGPU_OK; ++bulk) {
+      c->lc.x3_bulk = bulk;
+      if (bulk && !x3_bulk_eligible(c)) break;
+      float ms = 0.0f;
+      if ((st = time_cycles(c, cycles, &ms)) != ATHGPU_OK) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_bulk = bulk;
+      }
+    }
+  }
   athgpu_status st2 = restore(c, &sn);
   if (st != ATHGPU_OK) {
     c->lc = keep;
@@ -1107,6 +1157,7 @@ athgpu_status athgpu_autotune(athgpu_ctx* c, int cycles, int* seg_x2, int* seg_x
   }
   if (st2 != ATHGPU_OK) return st2;
   c->lc = keep;
+  c->lc.x3_bulk = best_bulk;
   st = athgpu_set_sweep_segment(c, best2, best3);  // also drops the captured graph
   if (seg_x2) *seg_x2 = best2;
   if (seg_x3) *seg_x3 = best3;

@@ -44,6 +44,7 @@ struct MlDevice {
 struct LaunchConfig {
   int seg_x2 = 0, seg_x3 = 0;  // faces per thread along the x2/x3 sweeps (0: default)
   int sr_phase1 = 0;           // SR con2prim: first-solve passes in phase 1 (0: default)
+  int x3_bulk = 0;             // x3 sweep staged by TMA bulk copies (athgpu_set_x3_staging)
 };
 
 }  // namespace athgpu
@@ -120,6 +121,9 @@ struct ProfScope {
 namespace athgpu {
 // device memory of the contexts, from the stream-ordered pool (api.cu)
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
+// the x3 sweep's TMA bulk staging can run here: uniform mesh, 16-byte aligned k-planes and
+// first staged rows (api.cu)
+bool x3_bulk_eligible(const athgpu_ctx* c);
 // stage drivers, one per precision translation unit
 cudaError_t stage_fp64(athgpu_ctx* c, int stage);
 cudaError_t stage_fp32(athgpu_ctx* c, int stage);

@@ -171,6 +171,7 @@ extern "C" athgpu_status athgpu_stats(athgpu_ctx* c, athgpu_run_stats* out, int 
   out->sr_fallbacks = (long long)h.sr_fallbacks;
   out->sr_unconverged = (long long)h.sr_unconverged;
   out->net_error = 0;
+  out->sweep_timeout = h.sweep_timeout;
   if (c->c2p_net_err) {
     e = cudaMemcpyAsync(&out->net_error, c->c2p_net_err, sizeof(int), cudaMemcpyDeviceToHost,
                         c->stream);
@@ -182,6 +183,7 @@ extern "C" athgpu_status athgpu_stats(athgpu_ctx* c, athgpu_run_stats* out, int 
     // zero the counters: the floor count and the four SR counters
     h.c2p_floor_count = 0;
     h.sr_cells = h.sr_passes = h.sr_fallbacks = h.sr_unconverged = 0;
+    h.sweep_timeout = 0;
     e = cudaMemcpyAsync((char*)c->clk + offsetof(DevClock, c2p_floor_count),
                         &h.c2p_floor_count, sizeof(int), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess)
@@ -189,6 +191,9 @@ extern "C" athgpu_status athgpu_stats(athgpu_ctx* c, athgpu_run_stats* out, int 
                           4 * sizeof(unsigned long long), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && c->c2p_net_err)
       e = cudaMemsetAsync(c->c2p_net_err, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync((char*)c->clk + offsetof(DevClock, sweep_timeout), 0, sizeof(int),
+                          c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return diag_fail(ATHGPU_ERR_CUDA, std::string("stats reset: ") +
                                                                 cudaGetErrorString(e));

@@ -83,6 +83,7 @@ struct DevClock {
   // FP64 Newman-Hamlin passes over all attempts, cells re-solved from the reference's
   // start after their own start failed, cells left unconverged
   unsigned long long sr_cells, sr_passes, sr_fallbacks, sr_unconverged;
+  int sweep_timeout;  // a bulk-copy wait of a sweep timed out (athgpu_stats)
 };
 
 // The mesh scalars, coordinates and dt in the kernel's arithmetic type: the FP64 kernels
@@ -155,6 +156,56 @@ __device__ __forceinline__ void cp_async_commit() {
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Bulk copies of the tensor-memory-access (TMA) unit: one thread moves a contiguous row
+// global -> shared (16-byte aligned addresses, size a multiple of 16), completion counted
+// in bytes on an mbarrier.  A CTA's consumers wait on the mbarrier's phase with a bounded
+// spin (about 0.1 s of SM clock) that records a timeout in *err instead of hanging.
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gsrc, unsigned bytes,
+                                         unsigned long long* mbar) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar);
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+      "[%3];\n" ::"r"(d),
+      "l"(gsrc), "r"(bytes), "r"(mb)
+      : "memory");
+}
+__device__ __forceinline__ void mbar_init_1(unsigned long long* mbar) {
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// the single producer arrival of a phase, announcing `bytes` of copies to come
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long* mbar, unsigned bytes) {
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_parity(unsigned long long* mbar, unsigned parity) {
+  const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar);
+  unsigned done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(mb), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ void mbar_wait_bounded(unsigned long long* mbar, unsigned parity,
+                                                  int* err) {
+  if (mbar_try_parity(mbar, parity)) return;
+  const long long t0 = clock64();
+  while (!mbar_try_parity(mbar, parity)) {
+    if (clock64() - t0 > 200000000LL) {  // about 0.1 s: record and stop waiting
+      if (err) atomicExch(err, 1);
+      return;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -306,6 +357,7 @@ struct UpdateArgs {
   // (vl2's gamma = (0, 1, 0) is a register swap)
   const void* uavg;
   double g1, g2;
+  int* err;               // set when a bulk-copy wait of a sweep timed out
 };
 
 // x1 sweep: rows (b, k in [ks-1,ke+1], j in [js-1,je+1]) of cells i in [is-1, ie+1],
@@ -373,33 +425,64 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
 // calculate_fluxes.cpp:184-237 and :304-356).  Columns: x2: k in [ks-1,ke+1],
 // i in [is-1,ie+1]; x3: j in [js-1,je+1], i in [is-1,ie+1].  A segment of cells
 // [c0,c1] solves faces c0..c1+1, so neighbouring segments share one face.
-template <typename Real, int DIR, int ORDER, int RS, int KAHAN>
+//
+// BULK (x3 only, uniform meshes): the stencil cells, the face field and the update
+// operands are staged by the TMA unit instead of per-thread cp.async.  The CTA's threads
+// then own consecutive positions of a k-plane (rows js-1..je+1 at full width nc1, columns
+// outside [is-1,ie+1] idle), so every staged row is one contiguous 16-byte-aligned range
+// that one thread copies with cp.async.bulk, completion counted on an mbarrier; a CTA
+// barrier per step frees the ring slot the next copy overwrites.  Same arithmetic and
+// results as the cp.async staging.
+template <typename Real, int DIR, int ORDER, int RS, int KAHAN, int BULK = 0>
 __global__ void __launch_bounds__(128, sizeof(Real) == 4 ? 4 : 1)
 flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                   const Real* __restrict__ bcc, const double* __restrict__ bn,
                   const DevClock* __restrict__ clk, Real* __restrict__ dflx,
                   Real* __restrict__ ey, Real* __restrict__ ez, Real* __restrict__ wct,
                   UpdateArgs ua) {
+  static_assert(!BULK || DIR == 2, "bulk staging is the x3 sweep's");
   const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
   const int ni = m.nx1 + 2;
   const int nt = (DIR == 1) ? m.nx3 + 2 : m.nx2 + 2;
   const int ncellsw = (DIR == 1) ? m.nx2 : m.nx3;
   const int nseg = (ncellsw + seg - 1) / seg;
-  const i64 total = (i64)nseg * m.nb * nt * ni;
-  if (t >= total) return;
-  const int ii = (int)(t % ni);
-  i64 r = t / ni;
-  const int tt = (int)(r % nt);
-  r /= nt;
-  const int b = (int)(r % m.nb);
-  const int sg = (int)(r / m.nb);
+  int ii, tt, b, sg;
+  bool active = true;
+  int bq = 0;  // BULK: this CTA's first plane position
+  if (BULK) {
+    const int np = nt * m.nc1;                   // plane positions of rows js-1..je+1
+    const int nq = (np + blockDim.x - 1) / blockDim.x;
+    if ((i64)blockIdx.x >= (i64)nq * m.nb * nseg) return;  // whole CTA
+    const int q = (int)(blockIdx.x % nq);
+    const int r2 = (int)(blockIdx.x / nq);
+    b = r2 % m.nb;
+    sg = r2 / m.nb;
+    bq = q * blockDim.x;
+    const int p = bq + threadIdx.x;
+    tt = p / m.nc1;
+    ii = p % m.nc1 - (m.is - 1);
+    active = p < np && ii >= 0 && ii < ni;
+    if (!active) {  // idle column: keep every index in range (nothing is stored)
+      tt = 0;
+      ii = 0;
+    }
+  } else {
+    const i64 total = (i64)nseg * m.nb * nt * ni;
+    if (t >= total) return;
+    ii = (int)(t % ni);
+    i64 r = t / ni;
+    tt = (int)(r % nt);
+    r /= nt;
+    b = (int)(r % m.nb);
+    sg = (int)(r / m.nb);
+  }
   const int i = m.is - 1 + ii;
   const int lo = (DIR == 1) ? m.js : m.ks;
   const int c0 = lo + sg * seg;
   const int c1 = min(c0 + seg - 1, lo + ncellsw - 1);
   const int trans = (DIR == 1 ? m.ks : m.js) - 1 + tt;  // k for x2, j for x3
-  const bool interior = ii >= 1 && ii <= m.nx1 && trans >= (DIR == 1 ? m.ks : m.js) &&
-                        trans <= (DIR == 1 ? m.ke : m.je);
+  const bool interior = active && ii >= 1 && ii <= m.nx1 &&
+                        trans >= (DIR == 1 ? m.ks : m.js) && trans <= (DIR == 1 ? m.ke : m.je);
   const Real dt = rdt(clk, Real());
   const Real* dxs = rdx(m, DIR, Real()) + (i64)b * (DIR == 1 ? m.nc2 : m.nc3);
   // area of this direction's faces (the same for every face of a uniform block)
@@ -432,8 +515,29 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
                                    : cidx(m, b, 0, NHYDRO, cfirst, j0, i));
   const Real* bp = bcc + ((DIR == 1) ? cidx(m, b, 0, 3, k0, cfirst, i)
                                      : cidx(m, b, 0, 3, cfirst, j0, i));
+  // BULK: the CTA's rows start at plane position bq of row js-1 (column 0); thread 0 issues
+  // every copy of a step, counted on the CTA's mbarrier
+  __shared__ unsigned long long sweep_mbar;
+  unsigned mbar_phase = 0;
+  const i64 prow = BULK ? (i64)(m.js - 1) * m.nc1 + bq : 0;
+  Real* ring0 = ring - threadIdx.x;  // the CTA's row starts (BULK)
+  double* fbuf0 = fbuf - threadIdx.x;
+  Real* aux0 = aux - threadIdx.x;
+  const unsigned rowb = (unsigned)(bd * sizeof(Real));
   auto issue = [&](int rel) {  // cell cfirst + rel -> slot rel % NS
     const int slot = rel % NS;
+    if (BULK) {
+      if (threadIdx.x != 0) return;
+      const int c = cfirst + rel;
+#pragma unroll
+      for (int n = 0; n < NWAVE; ++n) {
+        const Real* src = n < NHYDRO ? w + cidx(m, b, n, NHYDRO, c, 0, 0) + prow
+                                     : bcc + cidx(m, b, (DIR + 1 + (n - NHYDRO)) % 3, 3, c,
+                                                  0, 0) + prow;
+        bulk_g2s(ring0 + (slot * NWAVE + n) * bd, src, rowb, &sweep_mbar);
+      }
+      return;
+    }
     const Real* wc = wp + rel * sw;
     const Real* bc = bp + rel * sw;
 #pragma unroll
@@ -444,8 +548,24 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     }
   };
   auto issue_face = [&](int f) {  // normal field of face f
+    if (BULK) {
+      if (threadIdx.x != 0) return;
+      bulk_g2s(fbuf0 + (f & 1) * bd, bn + f3idx(m, b, f, 0, 0) + prow,
+               (unsigned)(bd * sizeof(double)), &sweep_mbar);
+      return;
+    }
     const i64 fo = (DIR == 1) ? f2idx(m, b, k0, f, i) : f3idx(m, b, f, j0, i);
     cp_async_elem<double>(fbuf + (f & 1) * bd, bn + fo);
+  };
+  // BULK: the producer's arrival of a step, announcing its bytes, comes before its copies
+  const unsigned cell_bytes = NWAVE * rowb, face_bytes = (unsigned)(bd * sizeof(double));
+  const unsigned aux_bytes = (KAHAN ? 3 : 2) * NHYDRO * rowb;
+  auto bulk_expect = [&](unsigned bytes) {
+    if (threadIdx.x == 0) mbar_arrive_tx(&sweep_mbar, bytes);
+  };
+  auto bulk_wait = [&]() {
+    mbar_wait_bounded(&sweep_mbar, mbar_phase, ua.err);
+    mbar_phase ^= 1u;
   };
   auto window = [&](int rel0, Real (*win)[NWAVE]) {  // cells cfirst+rel0 .. +WN-1
 #pragma unroll
@@ -455,10 +575,19 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
       for (int n = 0; n < NWAVE; ++n) win[q][n] = ring[(slot * NWAVE + n) * bd];
     }
   };
+  if (BULK) {
+    if (threadIdx.x == 0) mbar_init_1(&sweep_mbar);
+    __syncthreads();
+    bulk_expect((WN + 1) * cell_bytes + face_bytes);
+  }
   for (int q = 0; q <= WN; ++q) issue(q);  // cells c0-1-R .. c0+R
   issue_face(c0);
-  cp_async_commit();
-  cp_async_wait_all();
+  if (BULK) {
+    bulk_wait();
+  } else {
+    cp_async_commit();
+    cp_async_wait_all();
+  }
   const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
   Real wl[NWAVE], qlp[NWAVE], qrm[NWAVE];
   Real fprev[NHYDRO];
@@ -490,21 +619,42 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     const bool upd = s > c0 && interior;  // this step finishes cell s-1
     const int kc = (DIR == 1) ? k0 : s - 1, jc = (DIR == 1) ? s - 1 : j0;
     const i64 cc0 = cidx(m, b, 0, NHYDRO, kc, jc, i);
+    // BULK: every thread is done with the slot, the face buffer and the update operands
+    // of the previous step before they are overwritten
+    if (BULK) {
+      __syncthreads();
+      bulk_expect((s <= c1 ? cell_bytes + face_bytes : 0u) + (s > c0 ? aux_bytes : 0u));
+    }
     if (s <= c1) {  // prefetch cell s+R+1 into the slot of cell s-R-1, and face s+1
       issue(rel0 + WN);
       issue_face(s + 1);
     }
-    if (upd) {
+    if (BULK) {
+      if (s > c0 && threadIdx.x == 0) {  // the update operands of cell s-1, whole rows
 #pragma unroll
-      for (int n = 0; n < NHYDRO; ++n) {
-        cp_async_elem<Real>(aux + n * bd, dflx + cc0 + n * vs);
-        if (DIR == 2) {
-          cp_async_elem<Real>(aux + (NHYDRO + n) * bd, uin + cc0 + n * vs);
-          if (KAHAN) cp_async_elem<Real>(aux + (2 * NHYDRO + n) * bd, ulo + cc0 + n * vs);
+        for (int n = 0; n < NHYDRO; ++n) {
+          bulk_g2s(aux0 + n * bd, dflx + cidx(m, b, n, NHYDRO, s - 1, 0, 0) + prow, rowb,
+                   &sweep_mbar);
+          bulk_g2s(aux0 + (NHYDRO + n) * bd, uin + cidx(m, b, n, NHYDRO, s - 1, 0, 0) + prow,
+                   rowb, &sweep_mbar);
+          if (KAHAN)
+            bulk_g2s(aux0 + (2 * NHYDRO + n) * bd,
+                     ulo + cidx(m, b, n, NHYDRO, s - 1, 0, 0) + prow, rowb, &sweep_mbar);
         }
       }
+    } else {
+      if (upd) {
+#pragma unroll
+        for (int n = 0; n < NHYDRO; ++n) {
+          cp_async_elem<Real>(aux + n * bd, dflx + cc0 + n * vs);
+          if (DIR == 2) {
+            cp_async_elem<Real>(aux + (NHYDRO + n) * bd, uin + cc0 + n * vs);
+            if (KAHAN) cp_async_elem<Real>(aux + (2 * NHYDRO + n) * bd, ulo + cc0 + n * vs);
+          }
+        }
+      }
+      cp_async_commit();
     }
-    cp_async_commit();
     {
       Real win[WN][NWAVE];
       window(rel0, win);
@@ -524,12 +674,19 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     }
     const i64 fo = (DIR == 1) ? f2idx(m, b, k0, s, i) : f3idx(m, b, s, j0, i);
     Real fn[NHYDRO];
-    solve_face<Real, DIR, RS>(m, wl, qrm, to_real(fbuf[(s & 1) * bd], Real()),
-                              __ldg(dxs + s), dt, fo, fn, ey, ez, wct);
+    if (active) {
+      solve_face<Real, DIR, RS>(m, wl, qrm, to_real(fbuf[(s & 1) * bd], Real()),
+                                __ldg(dxs + s), dt, fo, fn, ey, ez, wct);
+    } else {
+#pragma unroll
+      for (int n = 0; n < NHYDRO; ++n) fn[n] = Real(0);
+    }
     if (m.ml.on && interior && (s == lo || s == lo + ncellsw))
       ml_face_override<Real>(m, b, 2 * DIR + (s == lo ? 0 : 1), i - m.is,
                              trans - (DIR == 1 ? m.ks : m.js), m.nx1, fn);
-    cp_async_wait_all();  // this step's aux values and the next step's cell and face
+    // this step's aux values and the next step's cell and face
+    if (BULK) bulk_wait();
+    else cp_async_wait_all();
     if (upd) {
       // cell s-1: this direction's flux difference
       if (DIR == 1) {

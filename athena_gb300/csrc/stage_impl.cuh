@@ -12,6 +12,14 @@ static inline unsigned nblk(long long n, int tpb) {
   return (unsigned)((n + tpb - 1) / tpb);
 }
 
+// The x3 sweep's TMA bulk staging applies when selected and when every staged row is
+// 16-byte aligned: the k-plane (nc1 nc2 elements) and the first staged row ((js-1) nc1)
+// of the bulk-precision arrays and of the FP64 face field, on a uniform mesh (the
+// registers of a uniform mesh are padded for the last CTA's overhanging row).
+static inline bool x3_bulk_ok(const athgpu_ctx* c) {
+  return c->lc.x3_bulk && x3_bulk_eligible(c);
+}
+
 template <typename Real, int ORDER, int RS, int KAHAN>
 static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const double* b1,
                           const double* b2, const double* b3, const UpdateArgs& ua) {
@@ -56,15 +64,30 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
     const long long n = nseg * m.nb * (m.nx2 + 2) * (long long)(m.nx1 + 2);
     ProfScope ps(c, "flux_x3_update");
     const int smem = sweep_smem_bytes(2, ORDER, sizeof(Real), 128);
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      attr = true;
+    if (x3_bulk_ok(c)) {
+      // TMA bulk staging: CTAs over consecutive k-plane positions of rows js-1..je+1
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN, 1>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+      }
+      const long long nq = ((long long)(m.nx2 + 2) * m.nc1 + 127) / 128;
+      flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN, 1><<<(unsigned)(nq * m.nb * nseg), 128,
+                                                        smem, s>>>(
+          m, seg, w, bcc, b3, c->clk, (Real*)r.dflx, (Real*)r.e2x3, (Real*)r.e1x3,
+          (Real*)r.w3f, ua);
+    } else {
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr = true;
+      }
+      flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN><<<nblk(n, 128), 128, smem, s>>>(
+          m, seg, w, bcc, b3, c->clk, (Real*)r.dflx, (Real*)r.e2x3, (Real*)r.e1x3,
+          (Real*)r.w3f, ua);
     }
-    flux_sweep_kernel<Real, 2, ORDER, RS, KAHAN><<<nblk(n, 128), 128, smem, s>>>(
-        m, seg, w, bcc, b3, c->clk, (Real*)r.dflx, (Real*)r.e2x3, (Real*)r.e1x3,
-        (Real*)r.w3f, ua);
   }
   c->launches += 3;
 }
@@ -248,6 +271,7 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   ua.uavg = avg ? r.ustar : nullptr;
   ua.g1 = g1;
   ua.g2 = g2;
+  ua.err = (int*)((char*)c->clk + offsetof(DevClock, sweep_timeout));
 #define FLUX(O, R) launch_fluxes<Real, O, R, KAHAN>(c, w, bcc, bb1, bb2, bb3, ua)
 #define FLUX_RS(O)                                                                   \
   do {                                                                               \

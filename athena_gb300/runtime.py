@@ -44,7 +44,7 @@ class RunStats(ctypes.Structure):
                 ("divb_cells", ctypes.c_longlong), ("floor_cells", ctypes.c_longlong),
                 ("sr_cells", ctypes.c_longlong), ("sr_passes", ctypes.c_longlong),
                 ("sr_fallbacks", ctypes.c_longlong), ("sr_unconverged", ctypes.c_longlong),
-                ("net_error", ctypes.c_int)]
+                ("net_error", ctypes.c_int), ("sweep_timeout", ctypes.c_int)]
 
 
 class MeshDesc(ctypes.Structure):
@@ -432,6 +432,17 @@ class StageUpdate:
         """0: chunked DMA over several copy streams (default); 1: conversion kernels on
         page-locked host memory."""
         _check(load_library().athgpu_set_host_copy(self.h, int(mode)), "athgpu_set_host_copy")
+
+    def set_x3_staging(self, bulk):
+        """x3 sweep staging: 0 per-thread cp.async, 1 TMA bulk copies."""
+        _check(load_library().athgpu_set_x3_staging(self.h, int(bulk)),
+               "athgpu_set_x3_staging")
+
+    def x3_staging(self):
+        v = ctypes.c_int()
+        _check(load_library().athgpu_get_x3_staging(self.h, ctypes.byref(v)),
+               "athgpu_get_x3_staging")
+        return v.value
 
     def set_stream(self, stream_ptr):
         _check(load_library().athgpu_set_stream(self.h, ctypes.c_void_p(stream_ptr)),

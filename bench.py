@@ -237,6 +237,7 @@ def run_gpu(args, rank, world, local_rank):
         g.initialize()
         if prec == "fp32":  # sweep tiling picked by the autotuner (state left unchanged)
             res["tiling"] = dict(zip(("seg_x2", "seg_x3"), g.autotune(cycles=2)))
+            res["tiling"]["x3_staging"] = "tma_bulk" if g.x3_staging() else "cp_async"
         steps = args.steps if prec == "fp32" else max(3, min(args.steps, 10))
         sampler = ClockSampler(local_rank) if prec == "fp32" else None
         if world > 1:
@@ -667,6 +668,29 @@ def amr_profile_cycle(precision="fp32", warm=2):
     return out
 
 
+def x3_staging_cycles(n=128):
+    """One cycle (per-kernel CUDA events, no graph) of the n^3 turbulence workload in FP32
+    with each staging of the x3 sweep: per-thread cp.async, then TMA bulk copies."""
+    from athena_gb300 import build
+    from athena_gb300.runtime import StageUpdate
+    build.build()
+    mesh, ic = make_ic((n,) * 3, (n // 32,) * 3)
+    g = StageUpdate(mesh, 5.0 / 3.0, xorder=3, rsolver="hlld", precision="fp32", cfl=0.3)
+    g.set_state(*ic)
+    g.initialize()
+    out = {}
+    for bulk in (0, 1):
+        g.set_x3_staging(bulk)
+        prof = g.profile_cycle()
+        out["tma_bulk" if bulk else "cp_async"] = [ms for name, ms in prof
+                                                   if name == "flux_x3_update"]
+    st = g.stats()
+    g.close()
+    if st["sweep_timeout"]:
+        raise RuntimeError("a bulk-copy wait timed out")
+    return out
+
+
 def amr_cpu_baseline(ic, threads=None):
     """The oracle (C port of the reference algorithm, FP64, OpenMP over MeshBlocks) on the
     host cores: the adaptive initial loop, then one timed cycle with its refinement step
@@ -730,11 +754,17 @@ def main():
                     help="cells per direction (MeshBlocks of 32^3); 256 is the workload")
     ap.add_argument("--amr-profile-cycle", action="store_true",
                     help="only: one profiled cycle of the adaptive blast (FP32)")
+    ap.add_argument("--x3-staging-cycles", action="store_true",
+                    help="only: one non-graph FP32 cycle of the 128^3 workload with each x3 "
+                         "staging (per-thread cp.async, TMA bulk copies), for ncu")
     args = ap.parse_args()
     if args.amr_profile_cycle:
         from athena_gb300 import build
         build.build()
         print(json.dumps(amr_profile_cycle()))
+        return
+    if args.x3_staging_cycles:
+        print(json.dumps(x3_staging_cycles()))
         return
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", 0))

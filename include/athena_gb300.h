@@ -322,6 +322,15 @@ athgpu_status athgpu_set_c2p_start(athgpu_ctx *ctx, int start, const float *para
  * autotuner's knob); 0 = heuristic default. */
 athgpu_status athgpu_set_sweep_segment(athgpu_ctx *ctx, int seg_x2, int seg_x3);
 
+/* Staging of the x3 sweep's stencil cells, face field and update operands in shared
+ * memory: 0 (default) per-thread asynchronous copies (cp.async); 1 the TMA unit's bulk
+ * copies (cp.async.bulk, one thread per CTA, completion on an mbarrier), on uniform meshes
+ * whose k-planes and rows are 16-byte aligned (otherwise the call is accepted and the
+ * sweep keeps per-thread copies).  Results are identical; athgpu_autotune times both. */
+athgpu_status athgpu_set_x3_staging(athgpu_ctx *ctx, int bulk);
+/* The staging the x3 sweep uses now (1: TMA bulk copies). */
+athgpu_status athgpu_get_x3_staging(athgpu_ctx *ctx, int *bulk);
+
 /* History output (HistoryOutput::WriteOutputFile, outputs/history.cpp:77-140): out[11]
  * (HOST) = volume-weighted sums over the interior cells of all MeshBlocks of mass, 1-mom,
  * 2-mom, 3-mom, 1-KE, 2-KE, 3-KE, tot-E, 1-ME, 2-ME, 3-ME, in FP64, reduced
@@ -358,13 +367,15 @@ typedef struct {
   long long sr_cells, sr_passes, sr_fallbacks, sr_unconverged;
   int net_error;  /* 1: a tensor-core wait of the network start timed out (its cells then
                      started from the stale pressure) */
+  int sweep_timeout;  /* 1: a bulk-copy wait of the x3 sweep timed out (results invalid) */
 } athgpu_run_stats;
 athgpu_status athgpu_stats(athgpu_ctx *ctx, athgpu_run_stats *out, int reset);
 
 /* Autotuner of the sweep tiling: times `cycles` cycles (after one warm-up) for each
  * candidate segment length of the x2 sweep (the whole column, then halves down to 4
- * cells), keeps the fastest, then does the same for the x3 sweep, and applies the pair
- * (*seg_x2, *seg_x3 receive it; either may be NULL).  The simulation state, the clock and
+ * cells), keeps the fastest, then does the same for the x3 sweep, then times the x3
+ * sweep's two stagings (athgpu_set_x3_staging) at those segments, and applies the choice
+ * (*seg_x2, *seg_x3 receive the segments; either may be NULL).  The simulation state, the clock and
  * the primitive-buffer rotation are snapshotted on the device before and restored after,
  * so the call does not advance the run.  Allocates the snapshot (one copy of the state)
  * for the duration of the call.  Synchronous. */
