@@ -321,10 +321,10 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     return fail(ATHGPU_ERR_ARG, "unknown Riemann solver");
   if (d->precision != ATHGPU_FP64 && d->precision != ATHGPU_FP32)
     return fail(ATHGPU_ERR_ARG, "unknown precision");
-  if (d->relativistic && d->rsolver != ATHGPU_HLLE && d->rsolver != ATHGPU_LLF)
+  if (d->relativistic && d->rsolver == ATHGPU_ROE)
     return fail(ATHGPU_ERR_UNSUPPORTED,
-                "relativistic MHD supports the HLLE and LLF solvers (hlle_mhd_rel.cpp, "
-                "llf_mhd_rel.cpp) only");
+                "relativistic MHD supports the HLLD, HLLE and LLF solvers (hlld_rel.cpp, "
+                "hlle_mhd_rel.cpp, llf_mhd_rel.cpp) only");
   if (d->relativistic && !(d->gamma_max > 1.0))
     return fail(ATHGPU_ERR_ARG, "gamma_max must exceed 1 (adiabatic_mhd_sr.cpp:48)");
   if (!d->x1f || !d->dx1f || !d->x2f || !d->dx2f || !d->x3f || !d->dx3f)

@@ -315,6 +315,7 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
   else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);
   else if (RS == 5) llf_sr<Real>(gam, wli, wri, bx, f);  // special relativity, LLF
+  else if (RS == 6) hlld_sr<Real>(gam, wli, wri, bx, f);  // special relativity, HLLD
   else hlle_sr<Real>(gam, wli, wri, bx, f);  // RS 2: special relativity, HLLE
   fn[IDN] = f[0];
   fn[ivx] = f[1];

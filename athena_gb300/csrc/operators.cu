@@ -320,7 +320,8 @@ athgpu_status op_flux_scratch(athgpu_ctx* c) {
 }
 
 int solver_index(const athgpu_ctx* c) {
-  return c->desc.relativistic ? (c->desc.rsolver == ATHGPU_LLF ? 5 : 2)
+  return c->desc.relativistic ? (c->desc.rsolver == ATHGPU_LLF    ? 5
+                                 : c->desc.rsolver == ATHGPU_HLLD ? 6 : 2)
          : c->desc.rsolver == ATHGPU_LLF ? 3
          : c->desc.rsolver == ATHGPU_ROE ? 4 : c->desc.rsolver;
 }
@@ -351,6 +352,7 @@ void launch_op_fluxes_rs(athgpu_ctx* c, int rs, double dt, double* f1, double* f
   else if (rs == 2) launch_op_fluxes<ORDER, 2>(c, dt, f1, f2, f3);
   else if (rs == 3) launch_op_fluxes<ORDER, 3>(c, dt, f1, f2, f3);
   else if (rs == 5) launch_op_fluxes<ORDER, 5>(c, dt, f1, f2, f3);
+  else if (rs == 6) launch_op_fluxes<ORDER, 6>(c, dt, f1, f2, f3);
   else launch_op_fluxes<ORDER, 4>(c, dt, f1, f2, f3);
 }
 

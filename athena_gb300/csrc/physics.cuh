@@ -847,6 +847,327 @@ __device__ __forceinline__ void llf_sr(Real gamma_adi, const Real* wli, const Re
   for (int n = 0; n < NWAVE; ++n) f[n] = RC(0.5) * (fl[n] + fr[n] - lambda * (cr[n] - cl[n]));
 }
 
+// Relativistic HLLD (Mignone, Ugliano & Bodo 2009, "MUB"), hydro/rsolvers/mhd/
+// hlld_rel.cpp:116-890 (SR branch), with the enthalpy residual of Mignone & McKinney 2007
+// ("MM") at hlld_rel.cpp:928-975.  Same steps, constants and operand order as the
+// reference: HLL state (MB 29, 31); its total pressure from two Newton steps on W
+// (MM A26-A27 start); the initial total pressure (MUB 53-55); four secant steps on the
+// contact condition (MUB 48); the aL, aR (MUB 21-35, 43) and contact (MUB 45-52) states;
+// the fan region at the interface; HLL wherever the HLLD states are not finite.
+template <typename Real>
+__device__ __forceinline__ Real hlldsr_eres(Real w_guess, Real dd, Real ee, Real m_sq,
+                                            Real bb_sq, Real ss_sq, Real gamma_prime) {
+  Real v_sq = (m_sq + ss_sq / (w_guess * w_guess) * (RC(2.0) * w_guess + bb_sq)) /
+              ((w_guess + bb_sq) * (w_guess + bb_sq));
+  Real gamma_sq = RC(1.0) / (RC(1.0) - v_sq);
+  Real gamma_lorentz = dsqrt(gamma_sq);
+  Real chi = (RC(1.0) - v_sq) * (w_guess - gamma_lorentz * dd);
+  Real pgas = chi / gamma_prime;
+  Real ee_calc = w_guess - pgas + RC(0.5) * bb_sq * (RC(1.0) + v_sq) -
+                 ss_sq / (RC(2.0) * (w_guess * w_guess));
+  return ee_calc - ee;
+}
+
+template <typename Real>
+__device__ __forceinline__ Real hlldsr_eres_prime(Real w_guess, Real dd, Real m_sq,
+                                                  Real bb_sq, Real ss_sq, Real gamma_prime) {
+  Real v_sq = (m_sq + ss_sq / (w_guess * w_guess) * (RC(2.0) * w_guess + bb_sq)) /
+              ((w_guess + bb_sq) * (w_guess + bb_sq));
+  Real gamma_sq = RC(1.0) / (RC(1.0) - v_sq);
+  Real gamma_lorentz = dsqrt(gamma_sq);
+  Real chi = (RC(1.0) - v_sq) * (w_guess - gamma_lorentz * dd);
+  Real w_cu = (w_guess * w_guess) * w_guess;
+  Real w_b_cu = ((w_guess + bb_sq) * (w_guess + bb_sq)) * (w_guess + bb_sq);
+  Real dv_sq_dw = RC(-2.0) / (w_cu * w_b_cu) *
+                  (ss_sq * (RC(3.0) * w_guess * (w_guess + bb_sq) + bb_sq * bb_sq) +
+                   m_sq * w_cu);
+  Real dchi_dw = RC(1.0) - v_sq -
+                 gamma_lorentz / RC(2.0) * (dd + RC(2.0) * gamma_lorentz * chi) * dv_sq_dw;
+  Real drho_dw = -gamma_lorentz * dd / RC(2.0) * dv_sq_dw;
+  Real dpgas_dchi = RC(1.0) / gamma_prime;
+  Real dpgas_drho = RC(0.0);
+  // the zero term stays: it makes a non-finite drho_dw reach the result as it does there
+  Real dpgas_dw = dpgas_dchi * dchi_dw + dpgas_drho * drho_dw;
+  return RC(1.0) - dpgas_dw + RC(0.5) * bb_sq * dv_sq_dw + ss_sq / w_cu;
+}
+
+// The Alfven-region quantities at one total pressure and the contact-condition residual
+// (MUB 21-49; hlld_rel.cpp:437-517, the same steps at :521-598 and :618-697)
+template <typename Real>
+struct HlldSrAlfven {
+  Real vx_al, vy_al, vz_al, vx_ar, vy_ar, vz_ar;
+  Real by_al, bz_al, by_ar, bz_ar;
+  Real kx_l, ky_l, kz_l, kx_r, ky_r, kz_r, eta_l, eta_r;
+};
+
+template <typename Real>
+__device__ __forceinline__ Real hlldsr_residual(Real ptot, Real bbx, Real lambda_l,
+                                                Real lambda_r, const Real* r_l,
+                                                const Real* r_r, HlldSrAlfven<Real>& a) {
+  const Real delta_kx_aug = RC(1.0e-12);
+  const Real bbx_sq = bbx * bbx;
+  {
+    Real al = r_l[1] - lambda_l * r_l[4] + ptot * (RC(1.0) - lambda_l * lambda_l);
+    Real gl = r_l[5] * r_l[5] + r_l[6] * r_l[6];
+    Real cl = r_l[2] * r_l[5] + r_l[3] * r_l[6];
+    Real ql = -al - gl + bbx_sq * (RC(1.0) - lambda_l * lambda_l);
+    Real xl_inv = RC(1.0) / (bbx * (al * lambda_l * bbx + cl) -
+                             (al + gl) * (lambda_l * ptot + r_l[4]));
+    a.vx_al = (bbx * (al * bbx + lambda_l * cl) - (al + gl) * (ptot + r_l[1])) * xl_inv;
+    Real tl = cl + bbx * (lambda_l * r_l[1] - r_l[4]);
+    a.vy_al = (ql * r_l[2] + r_l[5] * tl) * xl_inv;
+    a.vz_al = (ql * r_l[3] + r_l[6] * tl) * xl_inv;
+  }
+  {
+    Real ar = r_r[1] - lambda_r * r_r[4] + ptot * (RC(1.0) - lambda_r * lambda_r);
+    Real gr = r_r[5] * r_r[5] + r_r[6] * r_r[6];
+    Real cr = r_r[2] * r_r[5] + r_r[3] * r_r[6];
+    Real qr = -ar - gr + bbx_sq * (RC(1.0) - lambda_r * lambda_r);
+    Real xr_inv = RC(1.0) / (bbx * (ar * lambda_r * bbx + cr) -
+                             (ar + gr) * (lambda_r * ptot + r_r[4]));
+    a.vx_ar = (bbx * (ar * bbx + lambda_r * cr) - (ar + gr) * (ptot + r_r[1])) * xr_inv;
+    Real tr = cr + bbx * (lambda_r * r_r[1] - r_r[4]);
+    a.vy_ar = (qr * r_r[2] + r_r[5] * tr) * xr_inv;
+    a.vz_ar = (qr * r_r[3] + r_r[6] * tr) * xr_inv;
+  }
+  a.by_al = (r_l[5] - bbx * a.vy_al) / (lambda_l - a.vx_al);
+  a.bz_al = (r_l[6] - bbx * a.vz_al) / (lambda_l - a.vx_al);
+  a.by_ar = (r_r[5] - bbx * a.vy_ar) / (lambda_r - a.vx_ar);
+  a.bz_ar = (r_r[6] - bbx * a.vz_ar) / (lambda_r - a.vx_ar);
+  Real v_rm_l = a.vx_al * r_l[1] + a.vy_al * r_l[2] + a.vz_al * r_l[3];
+  Real wtot_al = ptot + (r_l[4] - v_rm_l) / (lambda_l - a.vx_al);
+  Real v_rm_r = a.vx_ar * r_r[1] + a.vy_ar * r_r[2] + a.vz_ar * r_r[3];
+  Real wtot_ar = ptot + (r_r[4] - v_rm_r) / (lambda_r - a.vx_ar);
+  a.eta_l = -copysign(dsqrt(wtot_al), bbx);
+  a.eta_r = copysign(dsqrt(wtot_ar), bbx);
+  Real dl_inv = RC(1.0) / (lambda_l * ptot + r_l[4] + bbx * a.eta_l);
+  a.kx_l = (r_l[1] + ptot + lambda_l * bbx * a.eta_l) * dl_inv;
+  a.ky_l = (r_l[2] + r_l[5] * a.eta_l) * dl_inv;
+  a.kz_l = (r_l[3] + r_l[6] * a.eta_l) * dl_inv;
+  Real dr_inv = RC(1.0) / (lambda_r * ptot + r_r[4] + bbx * a.eta_r);
+  a.kx_r = (r_r[1] + ptot + lambda_r * bbx * a.eta_r) * dr_inv;
+  a.ky_r = (r_r[2] + r_r[5] * a.eta_r) * dr_inv;
+  a.kz_r = (r_r[3] + r_r[6] * a.eta_r) * dr_inv;
+  // the Alfven speeds are kx_l and kx_r
+  Real delta_kx = a.kx_r - a.kx_l + delta_kx_aug;
+  Real bbx_c = bbx * delta_kx;
+  Real by_c = a.by_ar * (a.kx_r - a.vx_ar) - a.by_al * (a.kx_l - a.vx_al) +
+              bbx * (a.vy_ar - a.vy_al);
+  Real bz_c = a.bz_ar * (a.kx_r - a.vx_ar) - a.bz_al * (a.kx_l - a.vx_al) +
+              bbx * (a.vz_ar - a.vz_al);
+  Real k_sq_l = a.kx_l * a.kx_l + a.ky_l * a.ky_l + a.kz_l * a.kz_l;
+  Real y_l = (RC(1.0) - k_sq_l) /
+             (a.eta_l * delta_kx - (a.kx_l * bbx_c + a.ky_l * by_c + a.kz_l * bz_c));
+  Real k_sq_r = a.kx_r * a.kx_r + a.ky_r * a.ky_r + a.kz_r * a.kz_r;
+  Real y_r = (RC(1.0) - k_sq_r) /
+             (a.eta_r * delta_kx - (a.kx_r * bbx_c + a.ky_r * by_c + a.kz_r * bz_c));
+  return delta_kx * (RC(1.0) - bbx * (y_r - y_l));
+}
+
+template <typename Real>
+__device__ __forceinline__ bool all_finite7(const Real* c, const Real* f) {
+  bool ok = true;
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) ok = ok && isfinite(c[n]) && isfinite(f[n]);
+  return ok;
+}
+
+template <typename Real>
+__device__ __forceinline__ void hlld_sr(Real gamma_adi, const Real* wli, const Real* wri,
+                                        Real bbx, Real* f) {
+  const Real p_transition = RC(0.01), vc_extension = RC(1.0e-6);
+  const Real delta_kx_aug = RC(1.0e-12), initial_offset = RC(1.0e-5), tol_res = RC(1.0e-12);
+  const Real gamma_prime = gamma_adi / (gamma_adi - RC(1.0));
+  Real cl[NWAVE], cr[NWAVE], fl[NWAVE], fr[NWAVE];
+  Real lml, lpl, lmr, lpr;
+  sr_states<Real>(gamma_adi, wli, wri, bbx, cl, cr, fl, fr, lml, lpl, lmr, lpr);
+  const Real lambda_l = smin(lml, lmr);
+  const Real lambda_r = smax(lpl, lpr);
+  // A face outside the fan takes the L or R flux whatever the fan holds, unless that state
+  // is not finite (then the reference's choice depends on the fan: the full path below).
+  if (lambda_l >= RC(0.0) && all_finite7(cl, fl)) {
+#pragma unroll
+    for (int n = 0; n < NWAVE; ++n) f[n] = fl[n];
+    return;
+  }
+  if (lambda_r <= RC(0.0) && lambda_l < RC(0.0) && all_finite7(cr, fr)) {
+#pragma unroll
+    for (int n = 0; n < NWAVE; ++n) f[n] = fr[n];
+    return;
+  }
+  Real r_l[NWAVE], r_r[NWAVE], u_hll[NWAVE], f_hll[NWAVE];
+  const Real lambda_diff_inv = RC(1.0) / (lambda_r - lambda_l);
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    r_l[n] = lambda_l * cl[n] - fl[n];
+    r_r[n] = lambda_r * cr[n] - fr[n];
+    u_hll[n] = (r_r[n] - r_l[n]) * lambda_diff_inv;
+    f_hll[n] = (lambda_l * r_r[n] - lambda_r * r_l[n]) * lambda_diff_inv;
+  }
+  // total pressure of the HLL state (MM A26-A27 start, two Newton steps, MM A3-A17, MM 2)
+  Real ptot_hll;
+  {
+    Real m_sq = u_hll[1] * u_hll[1] + u_hll[2] * u_hll[2] + u_hll[3] * u_hll[3];
+    Real bb_sq = bbx * bbx + u_hll[5] * u_hll[5] + u_hll[6] * u_hll[6];
+    Real m_dot_bb = u_hll[1] * bbx + u_hll[2] * u_hll[5] + u_hll[3] * u_hll[6];
+    Real ss_sq = m_dot_bb * m_dot_bb;
+    Real a1 = RC(4.0) / RC(3.0) * (bb_sq - u_hll[4]);
+    Real a0 = RC(0.33333333333333333) * (m_sq + bb_sq * (bb_sq - RC(2.0) * u_hll[4]));
+    Real s2 = a1 * a1 - RC(4.0) * a0;
+    Real s = (s2 < RC(0.0)) ? RC(0.0) : dsqrt(s2);
+    Real w = (s2 >= RC(0.0) && a1 >= RC(0.0)) ? RC(-2.0) * a0 / (a1 + s)
+                                              : RC(0.5) * (-a1 + s);
+    Real res = hlldsr_eres(w, u_hll[0], u_hll[4], m_sq, bb_sq, ss_sq, gamma_prime);
+#pragma unroll
+    for (int n = 0; n < 2; ++n) {
+      Real derivative = hlldsr_eres_prime(w, u_hll[0], m_sq, bb_sq, ss_sq, gamma_prime);
+      w = w + -res / derivative;
+      res = hlldsr_eres(w, u_hll[0], u_hll[4], m_sq, bb_sq, ss_sq, gamma_prime);
+    }
+    Real v_sq = (m_sq + ss_sq / (w * w) * (RC(2.0) * w + bb_sq)) / ((w + bb_sq) * (w + bb_sq));
+    Real gamma_lor_sq = RC(1.0) / (RC(1.0) - v_sq);
+    Real gamma_lor = dsqrt(gamma_lor_sq);
+    Real chi = (RC(1.0) - v_sq) * (w - gamma_lor * u_hll[0]);
+    Real pgas = RC(1.0) / gamma_prime * chi;
+    Real vx = (u_hll[1] + m_dot_bb / w * bbx) / (w + bb_sq);
+    Real vy = (u_hll[2] + m_dot_bb / w * u_hll[5]) / (w + bb_sq);
+    Real vz = (u_hll[3] + m_dot_bb / w * u_hll[6]) / (w + bb_sq);
+    Real v_bb = vx * bbx + vy * u_hll[5] + vz * u_hll[6];
+    Real b_sq = bb_sq / gamma_lor_sq + v_bb * v_bb;
+    ptot_hll = pgas + RC(0.5) * b_sq;
+  }
+  Real ptot_init;
+  if (bbx * bbx / ptot_hll < p_transition) {  // weak field (MUB 55)
+    Real a1 = u_hll[4] - f_hll[1];
+    Real a0 = u_hll[1] * f_hll[4] - f_hll[1] * u_hll[4];
+    Real s2 = a1 * a1 - RC(4.0) * a0;
+    Real s = (s2 < RC(0.0)) ? RC(0.0) : dsqrt(s2);
+    ptot_init = (s2 >= RC(0.0) && a1 >= RC(0.0)) ? RC(-2.0) * a0 / (a1 + s)
+                                                 : (-a1 + s) / RC(2.0);
+  } else {
+    ptot_init = ptot_hll;
+  }
+  bool to_hll = !isfinite(ptot_init) || ptot_init <= RC(0.0);
+  // secant iteration on the contact condition
+  HlldSrAlfven<Real> a;
+  Real ptot_last = ptot_init;
+  Real res_last = hlldsr_residual(ptot_last, bbx, lambda_l, lambda_r, r_l, r_r, a);
+  Real ptot_n = ptot_init * (RC(1.0) + initial_offset);
+  Real res_n = hlldsr_residual(ptot_n, bbx, lambda_l, lambda_r, r_l, r_r, a);
+  // FP64: the reference's stopping tests.  FP32: the pressure test at 1e-6 (eight ulps;
+  // 1e-8 is below one) and no step when the two residuals are equal, so that a secant
+  // that has reached the rounding noise of FP32 stops instead of dividing by zero and
+  // sending the face to the HLL fallback that FP64 does not take.
+  constexpr bool kFp64 = sizeof(Real) == 8;
+  const Real tol_ptot = (kFp64 ? RC(1.0e-8) : RC(1.0e-6)) * ptot_init;
+#pragma unroll 1
+  for (int n = 0; n < 4; ++n) {
+    const Real ptot_old = ptot_last, res_old = res_last;
+    ptot_last = ptot_n;
+    res_last = res_n;
+    if (dabs(res_last) > tol_res && dabs(ptot_last - ptot_old) > tol_ptot &&
+        (kFp64 || res_last != res_old))
+      ptot_n = (res_last * ptot_old - res_old * ptot_last) / (res_last - res_old);
+    else
+      ptot_n = ptot_last;
+    res_n = hlldsr_residual(ptot_n, bbx, lambda_l, lambda_r, r_l, r_r, a);
+  }
+  const Real ptot_c = ptot_n;
+  const Real lambda_al = a.kx_l, lambda_ar = a.kx_r;
+  if (!isfinite(lambda_al) || !isfinite(lambda_ar) || !isfinite(ptot_c) || ptot_c <= RC(0.0))
+    to_hll = true;
+  // aL and aR states (MUB 32-34) and fluxes (MUB 11-12)
+  Real u_al[NWAVE], u_ar[NWAVE];
+  u_al[5] = a.by_al;
+  u_al[6] = a.bz_al;
+  u_ar[5] = a.by_ar;
+  u_ar[6] = a.bz_ar;
+  {
+    Real v_bb = a.vx_al * bbx + a.vy_al * u_al[5] + a.vz_al * u_al[6];
+    u_al[0] = r_l[0] / (lambda_l - a.vx_al);
+    u_al[4] = (r_l[4] + ptot_c * a.vx_al - v_bb * bbx) / (lambda_l - a.vx_al);
+    u_al[1] = (u_al[4] + ptot_c) * a.vx_al - v_bb * bbx;
+    u_al[2] = (u_al[4] + ptot_c) * a.vy_al - v_bb * u_al[5];
+    u_al[3] = (u_al[4] + ptot_c) * a.vz_al - v_bb * u_al[6];
+  }
+  {
+    Real v_bb = a.vx_ar * bbx + a.vy_ar * u_ar[5] + a.vz_ar * u_ar[6];
+    u_ar[0] = r_r[0] / (lambda_r - a.vx_ar);
+    u_ar[4] = (r_r[4] + ptot_c * a.vx_ar - v_bb * bbx) / (lambda_r - a.vx_ar);
+    u_ar[1] = (u_ar[4] + ptot_c) * a.vx_ar - v_bb * bbx;
+    u_ar[2] = (u_ar[4] + ptot_c) * a.vy_ar - v_bb * u_ar[5];
+    u_ar[3] = (u_ar[4] + ptot_c) * a.vz_ar - v_bb * u_ar[6];
+  }
+  // contact field (MUB 45) and velocity (MUB 47, the mean of the L and R estimates)
+  Real u_c[NWAVE];
+  {
+    Real denom_c_inv = RC(1.0) / (lambda_ar - lambda_al + delta_kx_aug);
+    Real nl = u_al[5] * (lambda_al - a.vx_al) + bbx * a.vy_al;
+    Real nr = u_ar[5] * (lambda_ar - a.vx_ar) + bbx * a.vy_ar;
+    u_c[5] = (nr - nl) * denom_c_inv;
+    nl = u_al[6] * (lambda_al - a.vx_al) + bbx * a.vz_al;
+    nr = u_ar[6] * (lambda_ar - a.vx_ar) + bbx * a.vz_ar;
+    u_c[6] = (nr - nl) * denom_c_inv;
+  }
+  Real vx_c, vy_c, vz_c;
+  {
+    Real k_sq_l = a.kx_l * a.kx_l + a.ky_l * a.ky_l + a.kz_l * a.kz_l;
+    Real k_bc_l = a.kx_l * bbx + a.ky_l * u_c[5] + a.kz_l * u_c[6];
+    Real vx_cl = a.kx_l - bbx * (RC(1.0) - k_sq_l) / (a.eta_l - k_bc_l);
+    Real vy_cl = a.ky_l - u_c[5] * (RC(1.0) - k_sq_l) / (a.eta_l - k_bc_l);
+    Real vz_cl = a.kz_l - u_c[6] * (RC(1.0) - k_sq_l) / (a.eta_l - k_bc_l);
+    Real k_sq_r = a.kx_r * a.kx_r + a.ky_r * a.ky_r + a.kz_r * a.kz_r;
+    Real k_bc_r = a.kx_r * bbx + a.ky_r * u_c[5] + a.kz_r * u_c[6];
+    Real vx_cr = a.kx_r - bbx * (RC(1.0) - k_sq_r) / (a.eta_r - k_bc_r);
+    Real vy_cr = a.ky_r - u_c[5] * (RC(1.0) - k_sq_r) / (a.eta_r - k_bc_r);
+    Real vz_cr = a.kz_r - u_c[6] * (RC(1.0) - k_sq_r) / (a.eta_r - k_bc_r);
+    vx_c = RC(0.5) * (vx_cl + vx_cr);
+    vy_c = RC(0.5) * (vy_cl + vy_cr);
+    vz_c = RC(0.5) * (vz_cl + vz_cr);
+  }
+  // the contact state on the side of the contact that vx_c names (MUB 50-52)
+  const bool c_left = vx_c >= RC(0.0);
+  const Real lam_s = c_left ? lambda_al : lambda_ar;
+  const Real vx_s = c_left ? a.vx_al : a.vx_ar;
+  Real u_s[NWAVE], f_s[NWAVE];
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    u_s[n] = c_left ? u_al[n] : u_ar[n];
+    // flux of the aL / aR state (MUB 11-12)
+    f_s[n] = c_left ? lambda_l * u_al[n] - r_l[n] : lambda_r * u_ar[n] - r_r[n];
+  }
+  {
+    Real v_bb = vx_c * bbx + vy_c * u_c[5] + vz_c * u_c[6];
+    u_c[0] = u_s[0] * (lam_s - vx_s) / (lam_s - vx_c);
+    u_c[4] = (lam_s * u_s[4] - u_s[1] + ptot_c * vx_c - v_bb * bbx) / (lam_s - vx_c);
+    u_c[1] = (u_c[4] + ptot_c) * vx_c - v_bb * bbx;
+    u_c[2] = (u_c[4] + ptot_c) * vy_c - v_bb * u_c[5];
+    u_c[3] = (u_c[4] + ptot_c) * vz_c - v_bb * u_c[6];
+  }
+  // region of the fan at the interface (v_interface = 0 in SR): 0 L, 1 R, 2 HLL, 3 aL,
+  // 4 aR, 5 contact
+  const int region = lambda_l >= RC(0.0) ? 0
+                     : lambda_r <= RC(0.0) ? 1
+                     : to_hll ? 2
+                     : lambda_al >= RC(0.0) - vc_extension ? 3
+                     : lambda_ar <= RC(0.0) + vc_extension ? 4 : 5;
+  Real ui[NWAVE], fi[NWAVE];
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    Real f_al = lambda_l * u_al[n] - r_l[n];
+    Real f_ar = lambda_r * u_ar[n] - r_r[n];
+    Real f_c = f_s[n] + lam_s * (u_c[n] - u_s[n]);
+    ui[n] = region == 0 ? cl[n] : region == 1 ? cr[n] : region == 2 ? u_hll[n]
+            : region == 3 ? u_al[n] : region == 4 ? u_ar[n] : u_c[n];
+    fi[n] = region == 0 ? fl[n] : region == 1 ? fr[n] : region == 2 ? f_hll[n]
+            : region == 3 ? f_al : region == 4 ? f_ar : f_c;
+  }
+  // HLL where the chosen state is not finite (an HLL, L or R choice under to_hll stands)
+  const bool hll = !to_hll && !all_finite7(ui, fi);
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) f[n] = hll ? f_hll[n] : fi[n];
+}
+
 // Newman & Hamlin (2014) fixed-point con2prim with Aitken acceleration,
 // ConservedToPrimitiveNormal, eos/adiabatic_mhd_sr.cpp:404-522.  prim[5] in natural
 // slots (rho, u1, u2, u3, p).  *iters = loop index at exit.  The FP64 instantiation is the

@@ -28,7 +28,70 @@ __global__ void conversion_check_kernel(long long n, const double* __restrict__ 
   if (bad64) atomicAdd(mismatches + 1, 1ull);
 }
 
+// One Riemann solve per face in the solvers' local order (d, v_n, v_t1, v_t2, p, B_t1,
+// B_t2), FP64: wl/wr [n][7], bx [n], flux [n][7].
+template <int RS>
+__global__ void riemann_check_kernel(long long n, double gamma, const double* __restrict__ wl,
+                                     const double* __restrict__ wr,
+                                     const double* __restrict__ bx, double* __restrict__ flux) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double a[athgpu::NWAVE], b[athgpu::NWAVE], f[athgpu::NWAVE];
+#pragma unroll
+  for (int v = 0; v < athgpu::NWAVE; ++v) {
+    a[v] = wl[q * athgpu::NWAVE + v];
+    b[v] = wr[q * athgpu::NWAVE + v];
+  }
+  if (RS == 0) athgpu::hlld<double>(gamma, a, b, bx[q], f);
+  else if (RS == 1) athgpu::hlle<double>(gamma, a, b, bx[q], f);
+  else if (RS == 2) athgpu::hlle_sr<double>(gamma, a, b, bx[q], f);
+  else if (RS == 3) athgpu::llf<double>(gamma, a, b, bx[q], f);
+  else if (RS == 4) athgpu::roe<double>(gamma, a, b, bx[q], f);
+  else if (RS == 5) athgpu::llf_sr<double>(gamma, a, b, bx[q], f);
+  else athgpu::hlld_sr<double>(gamma, a, b, bx[q], f);
+#pragma unroll
+  for (int v = 0; v < athgpu::NWAVE; ++v) flux[q * athgpu::NWAVE + v] = f[v];
+}
+
 }  // namespace
+
+extern "C" athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, double gamma,
+                                                 long long n, const double* wl,
+                                                 const double* wr, const double* bx,
+                                                 double* flux, void* stream) {
+  if (n < 0 || (n > 0 && (!wl || !wr || !bx || !flux)) ||
+      rsolver < ATHGPU_HLLD || rsolver > ATHGPU_ROE ||
+      (relativistic && rsolver == ATHGPU_ROE) || !(gamma > 1.0)) {
+    athgpu::set_last_error("selftest_riemann: bad arguments");
+    return ATHGPU_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (n > 0) {
+    if (relativistic) {
+      if (rsolver == ATHGPU_HLLD)
+        riemann_check_kernel<6><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+      else if (rsolver == ATHGPU_LLF)
+        riemann_check_kernel<5><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+      else
+        riemann_check_kernel<2><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+    } else if (rsolver == ATHGPU_HLLD) {
+      riemann_check_kernel<0><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+    } else if (rsolver == ATHGPU_HLLE) {
+      riemann_check_kernel<1><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+    } else if (rsolver == ATHGPU_LLF) {
+      riemann_check_kernel<3><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+    } else {
+      riemann_check_kernel<4><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    athgpu::set_last_error(std::string("selftest_riemann: ") + cudaGetErrorString(e));
+    return ATHGPU_ERR_CUDA;
+  }
+  return ATHGPU_OK;
+}
 
 extern "C" athgpu_status athgpu_selftest_conversions(long long n, const double* d,
                                                      const float* f,

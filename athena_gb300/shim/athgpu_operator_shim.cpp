@@ -97,7 +97,7 @@ athgpu_ctx *ContextOf(MeshBlock *pmb, const ShimPhysics &phys) {
   // the reconstruction order comes with each flux call; the largest one the ghost width
   // allows here
   d.xorder = NGHOST >= 3 ? 3 : 2;
-  d.rsolver = RELATIVISTIC_DYNAMICS ? ATHGPU_HLLE : SolverCode();
+  d.rsolver = SolverCode();
   d.precision = ATHGPU_FP64;
   d.relativistic = RELATIVISTIC_DYNAMICS ? 1 : 0;
   d.gamma = pmb->peos->GetGamma();

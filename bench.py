@@ -438,7 +438,8 @@ def run_sr_kh(n, stream, net):
     box as (n/32)^3 MeshBlocks, gamma 4/3, v_x = +-0.5c with tanh width 0.01, rho 1 / 0.1,
     p = 1, uniform B_x with sigma 0.1, seeded 1e-3 velocity noise, VL2 + PLM + HLLE.
     Zone-cycles/s of the FP32 and FP64 SR stage paths (CUDA events, state resident), their
-    relative L1 difference after SR_ACC_CYCLES cycles.  Inside the stage each start of the
+    relative L1 difference after SR_ACC_CYCLES cycles, and the same step with the LLF and
+    HLLD solvers in place of HLLE.  Inside the stage each start of the
     FP64 con2prim solve is timed (the stale pressure, that pressure refined in FP32, the
     network evaluated on tcgen05 in the W(U) kernel and refined in FP32) with its mean FP64
     passes, fallbacks and unconverged cells from the run statistics, also for the first
@@ -514,6 +515,26 @@ def run_sr_kh(n, stream, net):
             _, bcc_new = g.prim()
         g.close()
     out["speedup_fp32_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    # the same workload with each relativistic Riemann solver (default con2prim start)
+    out["by_solver"] = {"hlle": {p: {"value": out[p]["value"],
+                                     "ms_per_step": out[p]["ms_per_step"]}
+                                 for p in ("fp32", "fp64")}}
+    for rs in ("llf", "hlld"):
+        out["by_solver"][rs] = {}
+        for prec in ("fp32", "fp64"):
+            g = StageUpdate(mesh, gam, xorder=2, rsolver=rs, precision=prec, cfl=0.3,
+                            relativistic=True)
+            g.set_stream(stream.cuda_stream)
+            g.set_state(*ic)
+            g.set_prim(w0)
+            g.set_clock(0.0, 1.7976931348623157e308)
+            g.initialize()
+            t = time_device_cycles(g, stream, SR_CYCLES[prec], 3)
+            st = g.stats()
+            out["by_solver"][rs][prec] = {"value": zones * SR_CYCLES[prec] / t,
+                                          "ms_per_step": t / SR_CYCLES[prec] * 1e3,
+                                          "unconverged": st["sr_unconverged"]}
+            g.close()
     l1 = l1_rel(finals["fp32"], finals["fp64"])
     out["l1_rel_fp32_vs_fp64"] = {"cycles": SR_ACC_CYCLES, "d": l1[0], "m1": l1[1],
                                   "m2": l1[2], "m3": l1[3], "e": l1[4]}

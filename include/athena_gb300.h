@@ -32,7 +32,8 @@ typedef int athgpu_status;
 #define ATHGPU_ERR_UNSUPPORTED (-3)
 #define ATHGPU_ERR_STATE (-4)    /* call out of order (e.g. stage before initialize) */
 
-#define ATHGPU_HLLD 0            /* --flux=hlld  (hydro/rsolvers/mhd/hlld.cpp) */
+#define ATHGPU_HLLD 0            /* --flux=hlld  (hydro/rsolvers/mhd/hlld.cpp; relativistic:
+                                    hlld_rel.cpp) */
 #define ATHGPU_HLLE 1            /* --flux=hlle  (hydro/rsolvers/mhd/hlle_mhd.cpp) */
 #define ATHGPU_LLF 2             /* --flux=llf   (hydro/rsolvers/mhd/llf_mhd.cpp; relativistic:
                                     llf_mhd_rel.cpp) */
@@ -54,9 +55,9 @@ typedef struct {
   int xorder;             /* time/xorder: 2 = PLM, 3 = PPM (stage 1 is donor cell) */
   int rsolver;            /* ATHGPU_HLLD, ATHGPU_HLLE, ATHGPU_LLF or ATHGPU_ROE */
   int precision;          /* ATHGPU_FP64 or ATHGPU_FP32 */
-  int relativistic;       /* 1: special-relativistic MHD (-s): the HLLE or LLF solver
-                             (hlle_mhd_rel.cpp, llf_mhd_rel.cpp), FP64 Newman-Hamlin
-                             con2prim (adiabatic_mhd_sr.cpp) */
+  int relativistic;       /* 1: special-relativistic MHD (-s): the HLLD, HLLE or LLF
+                             solver (hlld_rel.cpp, hlle_mhd_rel.cpp, llf_mhd_rel.cpp),
+                             FP64 Newman-Hamlin con2prim (adiabatic_mhd_sr.cpp) */
   double gamma;           /* hydro/gamma */
   double dfloor, pfloor;  /* hydro/dfloor, hydro/pfloor (adiabatic_mhd.cpp:29-30) */
   double cfl_number;      /* time/cfl_number */
@@ -535,6 +536,19 @@ athgpu_status athgpu_mlp_train(const float *features, const float *targets, long
  * widening of f[q].  No counterpart in the reference. */
 athgpu_status athgpu_selftest_conversions(long long n, const double *d, const float *f,
                                           unsigned long long *mismatches, void *stream);
+
+/* Self-check of the Riemann solvers on arbitrary face states: for device arrays wl[n][7],
+ * wr[n][7] (primitive states in the solvers' local order: density, normal and two
+ * transverse velocities (relativistic: spatial 4-velocity), gas pressure, two transverse
+ * fields), bx[n] (normal field), flux[n][7] (device) receives each face's flux in the same
+ * order (mass, three momenta, energy, then the two transverse-field fluxes, before the
+ * EMF sign flip of the caller).  rsolver as in athgpu_mesh_desc; FP64.  Replaces no
+ * reference interface: the solvers' own entry points are the per-pencil RiemannSolver
+ * functions (hydro/rsolvers/mhd/*.cpp), which this applies one face at a time.
+ * Asynchronous on `stream`. */
+athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, double gamma,
+                                      long long n, const double *wl, const double *wr,
+                                      const double *bx, double *flux, void *stream);
 
 /* Conserved->primitive over whole MeshBlocks plus the first CFL time step, for callers
  * that cannot let a library allocate device memory: hosts whose device memory belongs

@@ -776,6 +776,280 @@ static void llf_sr(double gamma_adi, const double *wli, const double *wri, doubl
   for (int n = 0; n < NWAVE; ++n) f[n] = 0.5 * (fl[n] + fr[n] - lambda * (cr[n] - cl[n]));
 }
 
+/* 1/3 as the reference writes it (defs.hpp.in:144, ONE_3RD); the nearest double to 1/3 */
+#define ORC_ONE_3RD 0.33333333333333333
+
+/* the enthalpy residual and its derivative of the HLL state's total-pressure estimate
+ * (Mignone & McKinney 2007 A1, A3, A11, A14-A18), hlld_rel.cpp:928-975 */
+static double hlldsr_eres(double w_guess, double dd, double ee, double m_sq, double bb_sq, double ss_sq,
+                    double gamma_prime) {
+  double v_sq = (m_sq + ss_sq / SQR(w_guess) * (2.0 * w_guess + bb_sq)) / SQR(w_guess + bb_sq);
+  double gamma_sq = 1.0 / (1.0 - v_sq);
+  double gamma_lorentz = sqrt(gamma_sq);
+  double chi = (1.0 - v_sq) * (w_guess - gamma_lorentz * dd);
+  double pgas = chi / gamma_prime;
+  double ee_calc = w_guess - pgas + 0.5 * bb_sq * (1.0 + v_sq) -
+                 ss_sq / (2.0 * SQR(w_guess));
+  return ee_calc - ee;
+}
+
+static double hlldsr_eres_prime(double w_guess, double dd, double m_sq, double bb_sq, double ss_sq,
+                          double gamma_prime) {
+  double v_sq = (m_sq + ss_sq / SQR(w_guess) * (2.0 * w_guess + bb_sq)) / SQR(w_guess + bb_sq);
+  double gamma_sq = 1.0 / (1.0 - v_sq);
+  double gamma_lorentz = sqrt(gamma_sq);
+  double chi = (1.0 - v_sq) * (w_guess - gamma_lorentz * dd);
+  double w_cu = SQR(w_guess) * w_guess;
+  double w_b_cu = SQR(w_guess + bb_sq) * (w_guess + bb_sq);
+  double dv_sq_dw = -2.0 / (w_cu * w_b_cu) *
+                  (ss_sq * (3.0 * w_guess * (w_guess + bb_sq) + SQR(bb_sq)) + m_sq * w_cu);
+  double dchi_dw = 1.0 - v_sq - gamma_lorentz / 2.0 * (dd + 2.0 * gamma_lorentz * chi) *
+                                     dv_sq_dw;
+  double drho_dw = -gamma_lorentz * dd / 2.0 * dv_sq_dw;
+  double dpgas_dchi = 1.0 / gamma_prime;
+  double dpgas_drho = 0.0;
+  double dpgas_dw = dpgas_dchi * dchi_dw + dpgas_drho * drho_dw;
+  return 1.0 - dpgas_dw + 0.5 * bb_sq * dv_sq_dw + ss_sq / w_cu;
+}
+
+/* the Alfven-region states of one total pressure ptot (MUB 21-49): the normal velocities
+ * vx, vy, vz and transverse fields of the aL and aR regions, eta, K and the residual of
+ * the contact condition (MUB 48), hlld_rel.cpp:437-517 (repeated at :521-598, :618-697) */
+typedef struct {
+  double vx_al, vy_al, vz_al, vx_ar, vy_ar, vz_ar;
+  double kx_l, ky_l, kz_l, kx_r, ky_r, kz_r, eta_l, eta_r;
+  double by_al, bz_al, by_ar, bz_ar, lambda_al, lambda_ar;
+} hlldsr_alfven;
+
+static double hlldsr_residual(double ptot, double bbx, double lambda_l, double lambda_r, const double *r_l,
+                        const double *r_r, hlldsr_alfven *s) {
+  const double delta_kx_aug = 1.0e-12;
+  double al = r_l[1] - lambda_l * r_l[4] + ptot * (1.0 - SQR(lambda_l));
+  double gl = SQR(r_l[5]) + SQR(r_l[6]);
+  double cl = r_l[2] * r_l[5] + r_l[3] * r_l[6];
+  double ql = -al - gl + SQR(bbx) * (1.0 - SQR(lambda_l));
+  double xl_inv = 1.0 / (bbx * (al * lambda_l * bbx + cl) - (al + gl) * (lambda_l * ptot + r_l[4]));
+  s->vx_al = (bbx * (al * bbx + lambda_l * cl) - (al + gl) * (ptot + r_l[1])) * xl_inv;
+  s->vy_al = (ql * r_l[2] + r_l[5] * (cl + bbx * (lambda_l * r_l[1] - r_l[4]))) * xl_inv;
+  s->vz_al = (ql * r_l[3] + r_l[6] * (cl + bbx * (lambda_l * r_l[1] - r_l[4]))) * xl_inv;
+  double ar = r_r[1] - lambda_r * r_r[4] + ptot * (1.0 - SQR(lambda_r));
+  double gr = SQR(r_r[5]) + SQR(r_r[6]);
+  double cr = r_r[2] * r_r[5] + r_r[3] * r_r[6];
+  double qr = -ar - gr + SQR(bbx) * (1.0 - SQR(lambda_r));
+  double xr_inv = 1.0 / (bbx * (ar * lambda_r * bbx + cr) - (ar + gr) * (lambda_r * ptot + r_r[4]));
+  s->vx_ar = (bbx * (ar * bbx + lambda_r * cr) - (ar + gr) * (ptot + r_r[1])) * xr_inv;
+  s->vy_ar = (qr * r_r[2] + r_r[5] * (cr + bbx * (lambda_r * r_r[1] - r_r[4]))) * xr_inv;
+  s->vz_ar = (qr * r_r[3] + r_r[6] * (cr + bbx * (lambda_r * r_r[1] - r_r[4]))) * xr_inv;
+  s->by_al = (r_l[5] - bbx * s->vy_al) / (lambda_l - s->vx_al);
+  s->bz_al = (r_l[6] - bbx * s->vz_al) / (lambda_l - s->vx_al);
+  s->by_ar = (r_r[5] - bbx * s->vy_ar) / (lambda_r - s->vx_ar);
+  s->bz_ar = (r_r[6] - bbx * s->vz_ar) / (lambda_r - s->vx_ar);
+  double v_rm_l = s->vx_al * r_l[1] + s->vy_al * r_l[2] + s->vz_al * r_l[3];
+  double wtot_al = ptot + (r_l[4] - v_rm_l) / (lambda_l - s->vx_al);
+  double v_rm_r = s->vx_ar * r_r[1] + s->vy_ar * r_r[2] + s->vz_ar * r_r[3];
+  double wtot_ar = ptot + (r_r[4] - v_rm_r) / (lambda_r - s->vx_ar);
+  s->eta_l = -copysign(sqrt(wtot_al), bbx);
+  s->eta_r = copysign(sqrt(wtot_ar), bbx);
+  double denom_al_inv = 1.0 / (lambda_l * ptot + r_l[4] + bbx * s->eta_l);
+  s->kx_l = (r_l[1] + ptot + lambda_l * bbx * s->eta_l) * denom_al_inv;
+  s->ky_l = (r_l[2] + r_l[5] * s->eta_l) * denom_al_inv;
+  s->kz_l = (r_l[3] + r_l[6] * s->eta_l) * denom_al_inv;
+  double denom_ar_inv = 1.0 / (lambda_r * ptot + r_r[4] + bbx * s->eta_r);
+  s->kx_r = (r_r[1] + ptot + lambda_r * bbx * s->eta_r) * denom_ar_inv;
+  s->ky_r = (r_r[2] + r_r[5] * s->eta_r) * denom_ar_inv;
+  s->kz_r = (r_r[3] + r_r[6] * s->eta_r) * denom_ar_inv;
+  s->lambda_al = s->kx_l;
+  s->lambda_ar = s->kx_r;
+  double delta_kx = s->kx_r - s->kx_l + delta_kx_aug;
+  double bbx_c_delta_kx = bbx * delta_kx;
+  double by_c_delta_kx = s->by_ar * (s->lambda_ar - s->vx_ar) - s->by_al * (s->lambda_al - s->vx_al) +
+                       bbx * (s->vy_ar - s->vy_al);
+  double bz_c_delta_kx = s->bz_ar * (s->lambda_ar - s->vx_ar) - s->bz_al * (s->lambda_al - s->vx_al) +
+                       bbx * (s->vz_ar - s->vz_al);
+  double k_sq_l = SQR(s->kx_l) + SQR(s->ky_l) + SQR(s->kz_l);
+  double k_dot_bc_delta_kx = s->kx_l * bbx_c_delta_kx + s->ky_l * by_c_delta_kx +
+                           s->kz_l * bz_c_delta_kx;
+  double y_l = (1.0 - k_sq_l) / (s->eta_l * delta_kx - k_dot_bc_delta_kx);
+  double k_sq_r = SQR(s->kx_r) + SQR(s->ky_r) + SQR(s->kz_r);
+  k_dot_bc_delta_kx = s->kx_r * bbx_c_delta_kx + s->ky_r * by_c_delta_kx +
+                      s->kz_r * bz_c_delta_kx;
+  double y_r = (1.0 - k_sq_r) / (s->eta_r * delta_kx - k_dot_bc_delta_kx);
+  return delta_kx * (1.0 - bbx * (y_r - y_l));
+}
+
+/* SR frame-transforming HLLD (Mignone, Ugliano & Bodo 2009), hydro/rsolvers/mhd/
+ * hlld_rel.cpp:116-890 (SR branch): L, R and HLL states, the HLL total pressure from two
+ * Newton steps on the enthalpy (MM A26-A27), the initial total pressure (MUB 53-55), four
+ * secant steps on the contact condition, the aL, aR and contact states, the region of the
+ * fan at the interface, HLL where anything is not finite. */
+static void hlld_sr(double gamma_adi, const double *wli, const double *wri, double bbx, double *f) {
+  const double p_transition = 0.01, vc_extension = 1.0e-6;
+  const double delta_kx_aug = 1.0e-12;
+  const double gamma_prime = gamma_adi / (gamma_adi - 1.0);
+  const int num_secant = 4;
+  const double initial_offset = 1.0e-5, tol_res = 1.0e-12;
+  double cons_l[7], flux_l[7], cons_r[7], flux_r[7], r_l[7], r_r[7], cons_hll[7], flux_hll[7];
+  double cons_al[7], flux_al[7], cons_ar[7], flux_ar[7], cons_c[7], flux_c[7];
+  double lml, lpl, lmr, lpr;
+  sr_states(gamma_adi, wli, wri, bbx, cons_l, cons_r, flux_l, flux_r, &lml, &lpl, &lmr, &lpr);
+  const double lambda_l = smin(lml, lmr);
+  const double lambda_r = smax(lpl, lpr);
+  for (int n = 0; n < 7; ++n) r_l[n] = lambda_l * cons_l[n] - flux_l[n];
+  for (int n = 0; n < 7; ++n) r_r[n] = lambda_r * cons_r[n] - flux_r[n];
+  double lambda_diff_inv = 1.0 / (lambda_r - lambda_l);
+  for (int n = 0; n < 7; ++n) cons_hll[n] = (r_r[n] - r_l[n]) * lambda_diff_inv;
+  for (int n = 0; n < 7; ++n) flux_hll[n] = (lambda_l * r_r[n] - lambda_r * r_l[n]) * lambda_diff_inv;
+  /* total pressure of the HLL state */
+  double ptot_hll;
+  {
+    double m_sq = SQR(cons_hll[1]) + SQR(cons_hll[2]) + SQR(cons_hll[3]);
+    double bb_sq = SQR(bbx) + SQR(cons_hll[5]) + SQR(cons_hll[6]);
+    double m_dot_bb = cons_hll[1] * bbx + cons_hll[2] * cons_hll[5] + cons_hll[3] * cons_hll[6];
+    double ss_sq = SQR(m_dot_bb);
+    double a1 = 4.0 / 3.0 * (bb_sq - cons_hll[4]);
+    double a0 = ORC_ONE_3RD * (m_sq + bb_sq * (bb_sq - 2.0 * cons_hll[4]));
+    double s2 = SQR(a1) - 4.0 * a0;
+    double s = (s2 < 0.0) ? 0.0 : sqrt(s2);
+    double w_init = (s2 >= 0.0 && a1 >= 0.0) ? -2.0 * a0 / (a1 + s) : 0.5 * (-a1 + s);
+    double w_new = w_init;
+    double res_new = hlldsr_eres(w_new, cons_hll[0], cons_hll[4], m_sq, bb_sq, ss_sq, gamma_prime);
+    for (int n = 0; n < 2; ++n) {
+      double w_old = w_new;
+      double res_old = res_new;
+      double derivative = hlldsr_eres_prime(w_old, cons_hll[0], m_sq, bb_sq, ss_sq, gamma_prime);
+      double delta = -res_old / derivative;
+      w_new = w_old + delta;
+      res_new = hlldsr_eres(w_new, cons_hll[0], cons_hll[4], m_sq, bb_sq, ss_sq, gamma_prime);
+    }
+    double w = w_new;
+    double v_sq = (m_sq + ss_sq / SQR(w) * (2.0 * w + bb_sq)) / SQR(w + bb_sq);
+    double gamma_lor_sq = 1.0 / (1.0 - v_sq);
+    double gamma_lor = sqrt(gamma_lor_sq);
+    double chi = (1.0 - v_sq) * (w - gamma_lor * cons_hll[0]);
+    double pgas = 1.0 / gamma_prime * chi;
+    double vx = (cons_hll[1] + m_dot_bb / w * bbx) / (w + bb_sq);
+    double vy = (cons_hll[2] + m_dot_bb / w * cons_hll[5]) / (w + bb_sq);
+    double vz = (cons_hll[3] + m_dot_bb / w * cons_hll[6]) / (w + bb_sq);
+    double v_bb = vx * bbx + vy * cons_hll[5] + vz * cons_hll[6];
+    double b_sq = bb_sq / gamma_lor_sq + SQR(v_bb);
+    ptot_hll = pgas + 0.5 * b_sq;
+  }
+  double ptot_init;
+  if (SQR(bbx) / ptot_hll < p_transition) {  /* weak field (MUB 55) */
+    double a1 = cons_hll[4] - flux_hll[1];
+    double a0 = cons_hll[1] * flux_hll[4] - flux_hll[1] * cons_hll[4];
+    double s2 = SQR(a1) - 4.0 * a0;
+    double s = (s2 < 0.0) ? 0.0 : sqrt(s2);
+    ptot_init = (s2 >= 0.0 && a1 >= 0.0) ? -2.0 * a0 / (a1 + s) : (-a1 + s) / 2.0;
+  } else {
+    ptot_init = ptot_hll;
+  }
+  int switch_to_hlle = 0;
+  if (!isfinite(ptot_init) || ptot_init <= 0.0) switch_to_hlle = 1;
+  /* secant iteration on the total pressure (MUB 48) */
+  hlldsr_alfven st;
+  double ptot_0 = ptot_init;
+  double res_0 = hlldsr_residual(ptot_0, bbx, lambda_l, lambda_r, r_l, r_r, &st);
+  double ptot_1 = ptot_init * (1.0 + initial_offset);
+  double res_1 = hlldsr_residual(ptot_1, bbx, lambda_l, lambda_r, r_l, r_r, &st);
+  double ptot_last = ptot_0, ptot_n = ptot_1, res_last = res_0, res_n = res_1;
+  const double tol_ptot = 1.0e-8 * ptot_init;
+  for (int n = 0; n < num_secant; ++n) {
+    double ptot_old = ptot_last;
+    ptot_last = ptot_n;
+    double res_old = res_last;
+    res_last = res_n;
+    int need_to_iterate = fabs(res_last) > tol_res && fabs(ptot_last - ptot_old) > tol_ptot;
+    if (need_to_iterate)
+      ptot_n = (res_last * ptot_old - res_old * ptot_last) / (res_last - res_old);
+    else
+      ptot_n = ptot_last;
+    res_n = hlldsr_residual(ptot_n, bbx, lambda_l, lambda_r, r_l, r_r, &st);
+  }
+  const double ptot_c = ptot_n;
+  const double lambda_al = st.lambda_al, lambda_ar = st.lambda_ar;
+  if (!isfinite(lambda_al) || !isfinite(lambda_ar) || !isfinite(ptot_c) || ptot_c <= 0.0)
+    switch_to_hlle = 1;
+  const double vx_al = st.vx_al, vy_al = st.vy_al, vz_al = st.vz_al;
+  const double vx_ar = st.vx_ar, vy_ar = st.vy_ar, vz_ar = st.vz_ar;
+  cons_al[5] = st.by_al;
+  cons_al[6] = st.bz_al;
+  cons_ar[5] = st.by_ar;
+  cons_ar[6] = st.bz_ar;
+  /* the aL and aR states (MUB 32-34) */
+  double v_bb_al = vx_al * bbx + vy_al * cons_al[5] + vz_al * cons_al[6];
+  cons_al[0] = r_l[0] / (lambda_l - vx_al);
+  cons_al[4] = (r_l[4] + ptot_c * vx_al - v_bb_al * bbx) / (lambda_l - vx_al);
+  cons_al[1] = (cons_al[4] + ptot_c) * vx_al - v_bb_al * bbx;
+  cons_al[2] = (cons_al[4] + ptot_c) * vy_al - v_bb_al * cons_al[5];
+  cons_al[3] = (cons_al[4] + ptot_c) * vz_al - v_bb_al * cons_al[6];
+  double v_bb_ar = vx_ar * bbx + vy_ar * cons_ar[5] + vz_ar * cons_ar[6];
+  cons_ar[0] = r_r[0] / (lambda_r - vx_ar);
+  cons_ar[4] = (r_r[4] + ptot_c * vx_ar - v_bb_ar * bbx) / (lambda_r - vx_ar);
+  cons_ar[1] = (cons_ar[4] + ptot_c) * vx_ar - v_bb_ar * bbx;
+  cons_ar[2] = (cons_ar[4] + ptot_c) * vy_ar - v_bb_ar * cons_ar[5];
+  cons_ar[3] = (cons_ar[4] + ptot_c) * vz_ar - v_bb_ar * cons_ar[6];
+  for (int n = 0; n < 7; ++n) flux_al[n] = lambda_l * cons_al[n] - r_l[n];
+  for (int n = 0; n < 7; ++n) flux_ar[n] = lambda_r * cons_ar[n] - r_r[n];
+  /* the contact state (MUB 45, 47, 50-52) */
+  double denom_c_inv = 1.0 / (lambda_ar - lambda_al + delta_kx_aug);
+  double numer_al = cons_al[5] * (lambda_al - vx_al) + bbx * vy_al;
+  double numer_ar = cons_ar[5] * (lambda_ar - vx_ar) + bbx * vy_ar;
+  cons_c[5] = (numer_ar - numer_al) * denom_c_inv;
+  numer_al = cons_al[6] * (lambda_al - vx_al) + bbx * vz_al;
+  numer_ar = cons_ar[6] * (lambda_ar - vx_ar) + bbx * vz_ar;
+  cons_c[6] = (numer_ar - numer_al) * denom_c_inv;
+  const double kx_l = st.kx_l, ky_l = st.ky_l, kz_l = st.kz_l, eta_l = st.eta_l;
+  const double kx_r = st.kx_r, ky_r = st.ky_r, kz_r = st.kz_r, eta_r = st.eta_r;
+  double k_sq_l = SQR(kx_l) + SQR(ky_l) + SQR(kz_l);
+  double k_bc_l = kx_l * bbx + ky_l * cons_c[5] + kz_l * cons_c[6];
+  double vx_cl = kx_l - bbx * (1.0 - k_sq_l) / (eta_l - k_bc_l);
+  double vy_cl = ky_l - cons_c[5] * (1.0 - k_sq_l) / (eta_l - k_bc_l);
+  double vz_cl = kz_l - cons_c[6] * (1.0 - k_sq_l) / (eta_l - k_bc_l);
+  double k_sq_r = SQR(kx_r) + SQR(ky_r) + SQR(kz_r);
+  double k_bc_r = kx_r * bbx + ky_r * cons_c[5] + kz_r * cons_c[6];
+  double vx_cr = kx_r - bbx * (1.0 - k_sq_r) / (eta_r - k_bc_r);
+  double vy_cr = ky_r - cons_c[5] * (1.0 - k_sq_r) / (eta_r - k_bc_r);
+  double vz_cr = kz_r - cons_c[6] * (1.0 - k_sq_r) / (eta_r - k_bc_r);
+  double vx_c = 0.5 * (vx_cl + vx_cr);
+  double vy_c = 0.5 * (vy_cl + vy_cr);
+  double vz_c = 0.5 * (vz_cl + vz_cr);
+  double v_bb_c = vx_c * bbx + vy_c * cons_c[5] + vz_c * cons_c[6];
+  if (vx_c >= 0.0) {
+    cons_c[0] = cons_al[0] * (lambda_al - vx_al) / (lambda_al - vx_c);
+    cons_c[4] = (lambda_al * cons_al[4] - cons_al[1] + ptot_c * vx_c - v_bb_c * bbx) /
+                (lambda_al - vx_c);
+  } else {
+    cons_c[0] = cons_ar[0] * (lambda_ar - vx_ar) / (lambda_ar - vx_c);
+    cons_c[4] = (lambda_ar * cons_ar[4] - cons_ar[1] + ptot_c * vx_c - v_bb_c * bbx) /
+                (lambda_ar - vx_c);
+  }
+  cons_c[1] = (cons_c[4] + ptot_c) * vx_c - v_bb_c * bbx;
+  cons_c[2] = (cons_c[4] + ptot_c) * vy_c - v_bb_c * cons_c[5];
+  cons_c[3] = (cons_c[4] + ptot_c) * vz_c - v_bb_c * cons_c[6];
+  for (int n = 0; n < 7; ++n) {
+    if (vx_c >= 0.0)
+      flux_c[n] = flux_al[n] + lambda_al * (cons_c[n] - cons_al[n]);
+    else
+      flux_c[n] = flux_ar[n] + lambda_ar * (cons_c[n] - cons_ar[n]);
+  }
+  /* the region of the fan at the interface (v_interface = 0 in SR) */
+  const double v_interface = 0.0;
+  const double *ci, *fi;
+  if (lambda_l >= v_interface) { ci = cons_l; fi = flux_l; }
+  else if (lambda_r <= v_interface) { ci = cons_r; fi = flux_r; }
+  else if (switch_to_hlle) { ci = cons_hll; fi = flux_hll; }
+  else if (lambda_al >= v_interface - vc_extension) { ci = cons_al; fi = flux_al; }
+  else if (lambda_ar <= v_interface + vc_extension) { ci = cons_ar; fi = flux_ar; }
+  else { ci = cons_c; fi = flux_c; }
+  if (!switch_to_hlle) {
+    for (int n = 0; n < 7; ++n)
+      if (!isfinite(ci[n]) || !isfinite(fi[n])) switch_to_hlle = 1;
+    if (switch_to_hlle) { ci = cons_hll; fi = flux_hll; }
+  }
+  for (int n = 0; n < 7; ++n) f[n] = fi[n];
+}
+
 /* ------------------------------------------------------------------------------------
  * Reconstruction of one cell along a direction: given the 7-component wave vector of the
  * cell and its neighbours, return the value at its upper face (qlp, becomes wl of the
@@ -952,6 +1226,7 @@ static void riemann(const orc_mesh *m, int dir, const double *wl, const double *
   double wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
   double wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
   if (m->p.relativistic && m->p.rsolver == 2) llf_sr(m->p.gamma, wli, wri, bx, flx7);
+  else if (m->p.relativistic && m->p.rsolver == 0) hlld_sr(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.relativistic) hlle_sr(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 2) llf(m->p.gamma, wli, wri, bx, flx7);
@@ -2254,5 +2529,16 @@ long orc_op_con2prim(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl,
 
 /* Hydro::NewBlockTimeStep (new_blockdt.cpp:45-230) of block b: cfl times the minimum */
 double orc_op_new_block_dt(orc_mesh *m, int b) { return new_block_dt(m, b); }
+
+void orc_riemann_face(int rsolver, int relativistic, double gamma, const double *wli,
+                      const double *wri, double bx, double *flx7) {
+  if (relativistic && rsolver == 2) llf_sr(gamma, wli, wri, bx, flx7);
+  else if (relativistic && rsolver == 0) hlld_sr(gamma, wli, wri, bx, flx7);
+  else if (relativistic) hlle_sr(gamma, wli, wri, bx, flx7);
+  else if (rsolver == 0) hlld(gamma, wli, wri, bx, flx7);
+  else if (rsolver == 2) llf(gamma, wli, wri, bx, flx7);
+  else if (rsolver == 3) roe(gamma, wli, wri, bx, flx7);
+  else hlle(gamma, wli, wri, bx, flx7);
+}
 
 #include "athena_oracle_ml.c"

@@ -99,6 +99,12 @@ void orc_op_ct(orc_mesh *m, int b, double wght, const double *e1, const double *
                const double *e3, double *b1, double *b2, double *b3);
 long orc_op_con2prim(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl, int ku);
 double orc_op_new_block_dt(orc_mesh *m, int b);
+
+/* One Riemann solve on a face, states in the solvers' local order (d, v_n, v_t1, v_t2, p,
+ * B_t1, B_t2); rsolver 0 HLLD, 1 HLLE, 2 LLF, 3 Roe; relativistic selects the SR solvers
+ * (hlld_rel.cpp, hlle_mhd_rel.cpp, llf_mhd_rel.cpp).  flx7 in the same local order. */
+void orc_riemann_face(int rsolver, int relativistic, double gamma, const double *wli,
+                      const double *wri, double bx, double *flx7);
 /* the stages of one cycle and time += dt, without the new time step (adaptive runs
  * regrid in between); then orc_new_dt: NewBlockTimeStep + Mesh::NewTimeStep */
 void orc_advance(orc_mesh *m);

@@ -48,6 +48,7 @@ VARIANTS = {
     "mhd_roe_g2": ("roe", 2, False),     # Roe linearisation (roe_mhd.cpp)
     "srmhd_hlle_g2": ("hlle", 2, True),
     "srmhd_llf_g2": ("llf", 2, True),    # relativistic LLF (llf_mhd_rel.cpp)
+    "srmhd_hlld_g2": ("hlld", 2, True),  # relativistic HLLD (hlld_rel.cpp)
 }
 
 

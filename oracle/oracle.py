@@ -96,6 +96,8 @@ def lib():
         L.orc_op_con2prim.restype = ctypes.c_long
         L.orc_op_new_block_dt.argtypes = [vp, ctypes.c_int]
         L.orc_op_new_block_dt.restype = ctypes.c_double
+        L.orc_riemann_face.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, dp,
+                                       ctypes.c_double, dp]
         _lib = L
     return _lib
 
@@ -281,3 +283,17 @@ def sr_prim_to_cons(w, bcc, gamma):
     u = np.zeros((n, 5))
     lib().orc_sr_prim_to_cons(n, gamma, _p(w), _p(bcc), _p(u))
     return u
+
+
+def riemann_faces(rsolver, wl, wr, bx, gamma, relativistic=False):
+    """One Riemann solve per face: wl, wr [n, 7] primitive states in the solvers' local
+    order (d, v_n, v_t1, v_t2, p, B_t1, B_t2), bx [n] -> flux [n, 7] in the same order."""
+    rs = {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3}[rsolver]
+    wl = np.ascontiguousarray(wl, dtype=np.float64)
+    wr = np.ascontiguousarray(wr, dtype=np.float64)
+    out = np.zeros((wl.shape[0], 7))
+    L = lib()
+    for q in range(wl.shape[0]):
+        L.orc_riemann_face(rs, 1 if relativistic else 0, gamma, _p(wl[q]), _p(wr[q]),
+                           float(bx[q]), _p(out[q]))
+    return out

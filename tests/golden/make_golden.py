@@ -77,6 +77,11 @@ CASES = {
                                           (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
     "srkh_llf_plm_1blk": ("srmhd_llf_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
                                           (1., 1., 1.)), "sr_kh", 2, 0.4, 4),
+    # relativistic HLLD (-s -b --flux=hlld, hlld_rel.cpp)
+    "srkh_hlld_plm_8blk": ("srmhd_hlld_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
+                                            (1., 1., 1.)), "sr_kh", 2, 0.3, 3),
+    "srkh_hlld_plm_1blk": ("srmhd_hlld_g2", ((16, 8, 8), (1, 1, 1), 2, (0., 0., 0.),
+                                            (1., 1., 1.)), "sr_kh", 2, 0.4, 4),
     # physical boundaries (flags inner/outer x1, x2, x3: 1 outflow, 2 reflecting)
     "blastbc_hlld_plm_8blk": ("mhd_hlld_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
                                               (.5, .5, .5)), "blast", 2, 0.3, 4),

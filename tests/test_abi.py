@@ -43,7 +43,7 @@ def _desc(mesh, **kw):
 
 @pytest.mark.parametrize("field,value,code", [
     ("xorder", 4, -3), ("xorder", 0, -3), ("nghost", 1, -1), ("rsolver", 7, -1),
-    ("precision", 9, -1), ("relativistic", 1, -3), ("gamma", 1.0, -1),
+    ("precision", 9, -1), ("gamma", 1.0, -1),
     ("cfl_number", 0.0, -1), ("nx1", 0, -1), ("ppm_fast", 1, -1), ("integrator", 2, -1),
     ("cfl_number", 0.6, -1)])
 def test_invalid_meshes_are_rejected(lib, field, value, code):
@@ -96,7 +96,7 @@ def test_non_uniform_spacing_is_rejected(lib):
 def test_relativistic_options_are_checked(lib):
     mesh = MeshSpec((16, 8, 8), (1, 1, 1), 2)
     h = ctypes.c_void_p()
-    d, keep = _desc(mesh, relativistic=1, rsolver=0)      # SR + HLLD: not provided
+    d, keep = _desc(mesh, relativistic=1, rsolver=3)      # SR + Roe: no such solver
     assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -3
     d, keep = _desc(mesh, relativistic=1, rsolver=1, gamma_max=0.5)
     assert lib.athgpu_create(ctypes.byref(h), ctypes.byref(d)) == -1

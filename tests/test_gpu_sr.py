@@ -176,6 +176,54 @@ def test_sr_llf_matches_oracle_rk2():
         assert close(aw[:, n], bw[:, n], rtol=1e-11), n
 
 
+@pytest.mark.parametrize("xorder,integ,noise,rtol", [(3, "rk2", 0.02, 1e-12),
+                                                     (2, "vl2", 0.3, 1e-10)])
+def test_sr_hlld_matches_oracle(xorder, integ, noise, rtol):
+    """The relativistic HLLD solver (hlld_rel.cpp) against the oracle per cell: PPM under
+    RK2 within 1e-12; PLM under VL2 on a strongly perturbed layer within 1e-10.  The solver
+    itself is bit-exact face by face (the per-face and per-operator tests); over whole
+    cycles the con2prim's last-bit differences (acos, cos, cbrt) reach its secant stopping
+    tests (|residual| > 1e-12, |dp| > 1e-8 p), whose flips move a face's total pressure at
+    the 1e-12 level: measured 5.5e-12 after one to three cycles on the perturbed layer, not
+    growing (HLLE on the same run: 7.6e-14)."""
+    mesh = MeshSpec((32, 32, 32), (2, 2, 2), 3)
+    gw, f1, f2, f3 = pgen.sr_kelvin_helmholtz(mesh.nx, seed=7, noise=noise)
+    gu = pgen.sr_prim_to_cons(gw, pgen.cell_centered(f1, f2, f3), 4.0 / 3.0)
+    ic = (mesh.scatter_cells(gu),) + mesh.scatter_faces(f1, f2, f3)
+    w0 = mesh.scatter_cells(gw)
+    c = {"gamma": 4.0 / 3.0, "xorder": xorder, "cfl": 0.4, "tlim": 1e3, "rsolver": "hlld",
+         "integrator": integ}
+    (u, b1, b2, b3), w, dts = _run(mesh, c, ic, w0, 3)
+    om = O.OracleMesh(mesh, c["gamma"], xorder=xorder, rsolver="hlld", tlim=c["tlim"],
+                      cfl=0.4, relativistic=True, integrator=integ)
+    om.set_state(*ic)
+    om.set_prim(w0)
+    om.initialize()
+    om.cycle(3)
+    uo, o1, o2, o3 = om.state()
+    a, b = mesh.interior(u), mesh.interior(uo)
+    for n in range(5):
+        assert close(a[:, n], b[:, n], rtol), n
+    for got, want in zip((b1, b2, b3), (o1, o2, o3)):
+        assert close(interior_faces(mesh, got), interior_faces(mesh, want), rtol)
+    aw, bw = mesh.interior(w), mesh.interior(om.prim()[0])
+    for n in range(5):
+        assert close(aw[:, n], bw[:, n], rtol=10 * rtol), n
+
+
+def test_sr_hlld_fp32_tracks_fp64():
+    """The FP32 path with the relativistic HLLD solver stays within 1e-4 (mean relative)
+    of the FP64 path after four cycles."""
+    mesh, ic, w0, c = _sr_kh(nx=(32, 32, 32), nb=(1, 1, 1))
+    c = dict(c, rsolver="hlld")
+    (u64, *_), _, _ = _run(mesh, c, ic, w0, 4, "fp64")
+    (u32, *_), _, _ = _run(mesh, c, ic, w0, 4, "fp32")
+    a, b = mesh.interior(u32), mesh.interior(u64)
+    for n in range(5):
+        rel = np.abs(a[:, n] - b[:, n]).mean() / np.abs(b[:, n]).mean()
+        assert rel < 1e-4, (n, rel)
+
+
 @pytest.mark.parametrize("bc", [(2, 2, 1, 1, 2, 1), (0, 0, 2, 2, 0, 0)])
 def test_sr_physical_boundaries_match_oracle(bc):
     """Reflecting and outflow mesh faces on the relativistic path (the reflecting
