@@ -152,13 +152,82 @@ cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s) {
 
 namespace {
 
+// The ghost elements of one MeshBlock in the order exchange_plan_kernel visits them: the
+// cells, then the x1-, x2- and x3-face layouts, each k-major over the whole array; per
+// element its in-block offset and (bits 27-31) the offset index of the neighbour owning
+// it, as own_map classifies it (below the own range: -1, above: +1; a face layout's own
+// range along its normal ends one later).  delta[what][dir] is the in-block shift from a
+// ghost element to the owner's (src = dst - delta).  False when an offset needs more
+// than 27 bits.
+bool build_exchange_plan(const DevMesh& m, std::vector<unsigned>& plan, int n[4],
+                         std::vector<int>& delta) {
+  for (int what = 0; what < 4; ++what) {
+    const int N1 = m.nc1 + (what == 1), N2 = m.nc2 + (what == 2), N3 = m.nc3 + (what == 3);
+    if ((long long)N1 * N2 * N3 >= (1LL << 27)) return false;
+    const int hi1 = m.ie + (what == 1), hi2 = m.je + (what == 2), hi3 = m.ke + (what == 3);
+    const size_t start = plan.size();
+    for (int k = 0; k < N3; ++k)
+      for (int j = 0; j < N2; ++j)
+        for (int i = 0; i < N1; ++i) {
+          const int o1 = i < m.is ? -1 : i > hi1 ? 1 : 0;
+          const int o2 = j < m.js ? -1 : j > hi2 ? 1 : 0;
+          const int o3 = k < m.ks ? -1 : k > hi3 ? 1 : 0;
+          if (o1 == 0 && o2 == 0 && o3 == 0) continue;
+          const unsigned dir = (unsigned)(((o3 + 1) * 3 + (o2 + 1)) * 3 + (o1 + 1));
+          plan.push_back((unsigned)((k * N2 + j) * N1 + i) | (dir << 27));
+        }
+    n[what] = (int)(plan.size() - start);
+    for (int dir = 0; dir < 27; ++dir) {
+      const int o1 = dir % 3 - 1, o2 = (dir / 3) % 3 - 1, o3 = dir / 9 - 1;
+      delta.push_back(o1 * m.nx1 + o2 * m.nx2 * N1 + o3 * m.nx3 * N1 * N2);
+    }
+  }
+  return true;
+}
+
+// The own edges of one MeshBlock that lie on block faces, as edge_fix_kernel visits them:
+// x1-directed, then x2- and x3-directed, each k-major.  Per edge its in-block offset and
+// the neighbours edge_avg adds, in its order: the face neighbours across x1, x2, x3 (those
+// whose face the edge lies on), then for an edge on two faces the edge neighbour; each as
+// (offset index << 27) | the edge's offset in that neighbour, ~0 when absent.  An edge of
+// direction C has own range [s, e] along C and [s, e + 1] across.
+void build_edge_plan(const DevMesh& m, std::vector<int4>& plan, int n[3]) {
+  for (int C = 0; C < 3; ++C) {
+    const int N1 = m.nc1 + (C != 0), N2 = m.nc2 + (C != 1);
+    const size_t start = plan.size();
+    for (int k = m.ks; k <= m.ke + (C != 2); ++k)
+      for (int j = m.js; j <= m.je + (C != 1); ++j)
+        for (int i = m.is; i <= m.ie + (C != 0); ++i) {
+          const int o1 = C == 0 ? 0 : i == m.is ? -1 : i == m.ie + 1 ? 1 : 0;
+          const int o2 = C == 1 ? 0 : j == m.js ? -1 : j == m.je + 1 ? 1 : 0;
+          const int o3 = C == 2 ? 0 : k == m.ks ? -1 : k == m.ke + 1 ? 1 : 0;
+          if (o1 == 0 && o2 == 0 && o3 == 0) continue;
+          unsigned cand[3] = {~0u, ~0u, ~0u};
+          int nc = 0;
+          auto add = [&](int p1, int p2, int p3) {
+            const unsigned dir = (unsigned)(((p3 + 1) * 3 + (p2 + 1)) * 3 + (p1 + 1));
+            const int off = ((k - p3 * m.nx3) * N2 + (j - p2 * m.nx2)) * N1 + (i - p1 * m.nx1);
+            cand[nc++] = (dir << 27) | (unsigned)off;
+          };
+          if (o1 != 0) add(o1, 0, 0);
+          if (o2 != 0) add(0, o2, 0);
+          if (o3 != 0) add(0, 0, o3);
+          if ((o1 != 0) + (o2 != 0) + (o3 != 0) == 2) add(o1, o2, o3);
+          plan.push_back(make_int4((k * N2 + j) * N1 + i, (int)cand[0], (int)cand[1],
+                                   (int)cand[2]));
+        }
+    n[C] = (int)(plan.size() - start);
+  }
+}
+
 void free_all(athgpu_ctx* c) {
   Registers& r = c->r;
   void* ptrs[] = {r.u, r.ustar, r.ulo, r.wbuf[0], r.wbuf[1], r.bcc, r.cce, r.dflx, r.e3x1, r.e2x1,
                   r.w1f, r.e1x2, r.e3x2, r.w2f, r.e1x3, r.e2x3, r.w3f, r.e1, r.e2, r.e3,
                   r.b1, r.b2, r.b3, r.bs1, r.bs2, r.bs3, c->clk, c->coords, c->coords32,
                   c->nbr, c->staging, c->c2p_queue, c->c2p_qcount, c->fxv, c->eps_buf,
-                  c->c2p_qstart, c->c2p_net, c->c2p_net_err, c->op_flx, c->op_words};
+                  c->c2p_qstart, c->c2p_net, c->c2p_net_err, c->op_flx, c->op_words,
+                  c->xplan, c->xdelta, c->eplan, c->escratch};
   // the context's device memory returns to the stream-ordered pool (pool_alloc)
   cudaStream_t s = c->own_stream;
   if (s) cudaStreamSynchronize(c->stream ? c->stream : s);
@@ -375,6 +444,10 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.js = m.ng; m.je = m.ng + m.nx2 - 1;
   m.ks = m.ng; m.ke = m.ng + m.nx3 - 1;
   m.ncell = (i64)m.nc1 * m.nc2 * m.nc3;
+  m.fd_nc1 = make_fastdiv(m.nc1);
+  m.fd_nc2 = make_fastdiv(m.nc2);
+  m.fd_n1 = make_fastdiv(m.nx1 + 1);
+  m.fd_n2 = make_fastdiv(m.nx2 + 1);
   m.nf1 = (i64)m.nc3 * m.nc2 * (m.nc1 + 1);
   m.nf2 = (i64)m.nc3 * (m.nc2 + 1) * m.nc1;
   m.nf3 = (i64)(m.nc3 + 1) * m.nc2 * m.nc1;
@@ -548,6 +621,36 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   e = cudaMemcpy(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy nbr"));
   m.nbr = c->nbr;
+
+  {  // the blocks' ghost plan for the same-level exchange (exchange_plan_kernel)
+    std::vector<unsigned> plan;
+    std::vector<int> delta;
+    if (!build_exchange_plan(m, plan, c->xplan_n, delta))
+      return bail(fail(ATHGPU_ERR_UNSUPPORTED, "MeshBlock too large for the ghost plan"));
+    e = pool_alloc((void**)&c->xplan, sizeof(unsigned) * plan.size(), c->stream);
+    if (e == cudaSuccess)
+      e = pool_alloc((void**)&c->xdelta, sizeof(int) * delta.size(), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c->xplan, plan.data(), sizeof(unsigned) * plan.size(),
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c->xdelta, delta.data(), sizeof(int) * delta.size(),
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "ghost plan"));
+  }
+  {  // the blocks' face edges for the same-level edge averaging (edge_fix_kernel)
+    std::vector<int4> plan;
+    build_edge_plan(m, plan, c->eplan_n);
+    e = pool_alloc((void**)&c->eplan, sizeof(int4) * plan.size(), c->stream);
+    if (e == cudaSuccess)
+      e = pool_alloc(&c->escratch, (size_t)c->real_bytes * plan.size() * nb, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c->eplan, plan.data(), sizeof(int4) * plan.size(),
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "edge plan"));
+  }
 
   DevClock hclk;
   memset(&hclk, 0, sizeof(hclk));

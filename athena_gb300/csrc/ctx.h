@@ -61,6 +61,16 @@ struct athgpu_ctx {
   athgpu::MlDevice mld;
   float* coords32 = nullptr; // the same, rounded to FP32, for the FP32 kernels
   int* nbr = nullptr;
+  // ghost plan of a same-level mesh's blocks (exchange_plan_kernel): plan words of the
+  // cell, x1-, x2- and x3-face ghosts, their counts, and the owner shifts [4][27]
+  unsigned* xplan = nullptr;
+  int xplan_n[4] = {0, 0, 0, 0};
+  int* xdelta = nullptr;
+  // block-face edges of a same-level mesh's blocks (edge_fix_kernel): (offset, k, j, i) of
+  // the x1-, x2- and x3-directed ones, their counts, and the averages' scratch [nb][n]
+  int4* eplan = nullptr;
+  int eplan_n[3] = {0, 0, 0};
+  void* escratch = nullptr;
   cudaStream_t own_stream = nullptr, stream = nullptr;
   // second stream for the ghost exchange beside W(U), forked and joined with events
   cudaStream_t aux_stream = nullptr;

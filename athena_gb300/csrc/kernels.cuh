@@ -44,12 +44,34 @@ struct DevML {
   void *ecorr1, *ecorr2, *ecorr3;     // corrected block-boundary edges (edge layout)
 };
 
+// Division of an int in [0, 2^31) by a divisor d >= 2 fixed when the mesh is set up, in
+// two instructions instead of the ~20 of a division by a run-time value: with
+// l = ceil(log2 d), mul = ceil(2^(31+l) / d) < 2^32 and x < 2^31, floor(x * mul / 2^(31+l))
+// = floor(x / d) (the round-up multiplier's error x (mul - 2^(31+l)/d) / 2^(31+l) stays
+// below 2^-l <= 1/d, so it never reaches the next multiple of d).
+struct FastDiv {
+  unsigned mul;
+  int shift;  // l - 1
+};
+inline FastDiv make_fastdiv(int d) {
+  int l = 0;
+  while ((1LL << l) < d) ++l;
+  FastDiv f;
+  f.mul = (unsigned)(((1ULL << (31 + l)) + (unsigned long long)d - 1) / (unsigned long long)d);
+  f.shift = l - 1;
+  return f;
+}
+__device__ __forceinline__ int fdiv(int x, FastDiv f) {
+  return (int)(__umulhi((unsigned)x, f.mul) >> f.shift);
+}
+
 struct DevMesh {
   int nb, nbx1, nbx2, nbx3;
   int nx1, nx2, nx3, ng;
   int nc1, nc2, nc3;
   int is, ie, js, je, ks, ke;
   i64 ncell, nf1, nf2, nf3, ne1, ne2, ne3;  // per-block element counts
+  FastDiv fd_nc1, fd_nc2, fd_n1, fd_n2;     // divisors nc1, nc2, nx1 + 1, nx2 + 1
   double gamma, dfloor, pfloor, cfl, tlim;
   const double* dx1f;  // [nb][nc1]
   const double* dx2f;  // [nb][nc2]
@@ -782,26 +804,44 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ cc, const Real* __restrict__
                 const Real* __restrict__ e1x3, const Real* __restrict__ e2x3,
                 const Real* __restrict__ w3f, Real* __restrict__ e1, Real* __restrict__ e2,
                 Real* __restrict__ e3) {
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  // blockIdx.y (strided) is the MeshBlock, blockIdx.x/threadIdx.x the corner point of it;
+  // every array is read at a 32-bit offset from the block's base, relative to (k,j,i)
   const int n1 = m.nx1 + 1, n2 = m.nx2 + 1, n3 = m.nx3 + 1;
-  if (t >= (i64)m.nb * n3 * n2 * n1) return;
-  const int i = m.is + (int)(t % n1);
-  i64 r = t / n1;
-  const int j = m.js + (int)(r % n2);
-  r /= n2;
-  const int k = m.ks + (int)(r % n3);
-  const int b = (int)(r / n3);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n1 * n2 * n3) return;
+  const int q = fdiv(r, m.fd_n1);
+  const int kq = fdiv(q, m.fd_n2);
+  const int i = m.is + (r - q * n1), j = m.js + (q - kq * n2), k = m.ks + kq;
+  const int c1 = m.nc1, c2 = m.nc2;
+  // in-block offsets of (k,j,i) and the (k, j, i) strides of each layout
+  const int of1 = (k * c2 + j) * (c1 + 1) + i, s1j = c1 + 1, s1k = c2 * (c1 + 1);
+  const int of2 = (k * (c2 + 1) + j) * c1 + i, s2j = c1, s2k = (c2 + 1) * c1;
+  const int of3 = (k * c2 + j) * c1 + i, s3j = c1, s3k = c2 * c1;
   const Real one = Real(1.0), quarter = Real(0.25);
-#define W1F(kk, jj, ii) __ldg(w1f + f1idx(m, b, kk, jj, ii))
-#define W2F(kk, jj, ii) __ldg(w2f + f2idx(m, b, kk, jj, ii))
-#define W3F(kk, jj, ii) __ldg(w3f + f3idx(m, b, kk, jj, ii))
-#define E3X1(kk, jj, ii) __ldg(e3x1 + f1idx(m, b, kk, jj, ii))
-#define E2X1(kk, jj, ii) __ldg(e2x1 + f1idx(m, b, kk, jj, ii))
-#define E1X2(kk, jj, ii) __ldg(e1x2 + f2idx(m, b, kk, jj, ii))
-#define E3X2(kk, jj, ii) __ldg(e3x2 + f2idx(m, b, kk, jj, ii))
-#define E1X3(kk, jj, ii) __ldg(e1x3 + f3idx(m, b, kk, jj, ii))
-#define E2X3(kk, jj, ii) __ldg(e2x3 + f3idx(m, b, kk, jj, ii))
-#define CC(n, kk, jj, ii) __ldg(cc + cidx(m, b, n, 3, kk, jj, ii))
+  for (int b = blockIdx.y; b < m.nb; b += gridDim.y) {
+  const Real* W1 = w1f + (i64)b * m.nf1;
+  const Real* W2 = w2f + (i64)b * m.nf2;
+  const Real* W3 = w3f + (i64)b * m.nf3;
+  const Real* A3X1 = e3x1 + (i64)b * m.nf1;
+  const Real* A2X1 = e2x1 + (i64)b * m.nf1;
+  const Real* A1X2 = e1x2 + (i64)b * m.nf2;
+  const Real* A3X2 = e3x2 + (i64)b * m.nf2;
+  const Real* A1X3 = e1x3 + (i64)b * m.nf3;
+  const Real* A2X3 = e2x3 + (i64)b * m.nf3;
+  const Real* CB = cc + (i64)b * 3 * m.ncell;
+#define OF1(kk, jj, ii) (of1 + ((kk) - k) * s1k + ((jj) - j) * s1j + ((ii) - i))
+#define OF2(kk, jj, ii) (of2 + ((kk) - k) * s2k + ((jj) - j) * s2j + ((ii) - i))
+#define OF3(kk, jj, ii) (of3 + ((kk) - k) * s3k + ((jj) - j) * s3j + ((ii) - i))
+#define W1F(kk, jj, ii) __ldg(W1 + OF1(kk, jj, ii))
+#define W2F(kk, jj, ii) __ldg(W2 + OF2(kk, jj, ii))
+#define W3F(kk, jj, ii) __ldg(W3 + OF3(kk, jj, ii))
+#define E3X1(kk, jj, ii) __ldg(A3X1 + OF1(kk, jj, ii))
+#define E2X1(kk, jj, ii) __ldg(A2X1 + OF1(kk, jj, ii))
+#define E1X2(kk, jj, ii) __ldg(A1X2 + OF2(kk, jj, ii))
+#define E3X2(kk, jj, ii) __ldg(A3X2 + OF2(kk, jj, ii))
+#define E1X3(kk, jj, ii) __ldg(A1X3 + OF3(kk, jj, ii))
+#define E2X3(kk, jj, ii) __ldg(A2X3 + OF3(kk, jj, ii))
+#define CC(n, kk, jj, ii) __ldg(CB + (i64)(n) * m.ncell + OF3(kk, jj, ii))
   if (i <= m.ie) {
     Real de1_l3 = (one - W2F(k - 1, j, i)) * (E1X3(k, j, i) - CC(0, k - 1, j, i)) +
                   (W2F(k - 1, j, i)) * (E1X3(k, j - 1, i) - CC(0, k - 1, j - 1, i));
@@ -811,7 +851,7 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ cc, const Real* __restrict__
                   (W3F(k, j - 1, i)) * (E1X2(k - 1, j, i) - CC(0, k - 1, j - 1, i));
     Real de1_r2 = (one - W3F(k, j, i)) * (E1X2(k, j, i) - CC(0, k, j, i)) +
                   (W3F(k, j, i)) * (E1X2(k - 1, j, i) - CC(0, k - 1, j, i));
-    e1[e1idx(m, b, k, j, i)] =
+    e1[(i64)b * m.ne1 + (k * (c2 + 1) + j) * c1 + i] =
         quarter * (de1_l3 + de1_r3 + de1_l2 + de1_r2 + E1X2(k - 1, j, i) + E1X2(k, j, i) +
                    E1X3(k, j - 1, i) + E1X3(k, j, i));
   }
@@ -824,7 +864,7 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ cc, const Real* __restrict__
                   (W3F(k, j, i - 1)) * (E2X1(k - 1, j, i) - CC(1, k - 1, j, i - 1));
     Real de2_r1 = (one - W3F(k, j, i)) * (E2X1(k, j, i) - CC(1, k, j, i)) +
                   (W3F(k, j, i)) * (E2X1(k - 1, j, i) - CC(1, k - 1, j, i));
-    e2[e2idx(m, b, k, j, i)] =
+    e2[(i64)b * m.ne2 + (k * c2 + j) * (c1 + 1) + i] =
         quarter * (de2_l3 + de2_r3 + de2_l1 + de2_r1 + E2X3(k, j, i - 1) + E2X3(k, j, i) +
                    E2X1(k - 1, j, i) + E2X1(k, j, i));
   }
@@ -837,10 +877,14 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ cc, const Real* __restrict__
                   (W2F(k, j, i - 1)) * (E3X1(k, j - 1, i) - CC(2, k, j - 1, i - 1));
     Real de3_r1 = (one - W2F(k, j, i)) * (E3X1(k, j, i) - CC(2, k, j, i)) +
                   (W2F(k, j, i)) * (E3X1(k, j - 1, i) - CC(2, k, j - 1, i));
-    e3[e3idx(m, b, k, j, i)] =
+    e3[(i64)b * m.ne3 + (k * (c2 + 1) + j) * (c1 + 1) + i] =
         quarter * (de3_l1 + de3_r1 + de3_l2 + de3_r2 + E3X2(k, j, i - 1) + E3X2(k, j, i) +
                    E3X1(k, j - 1, i) + E3X1(k, j, i));
   }
+  }
+#undef OF1
+#undef OF2
+#undef OF3
 #undef W1F
 #undef W2F
 #undef W3F
@@ -924,6 +968,108 @@ __device__ __forceinline__ double edge_value(const DevMesh& m, const Real* __res
                                              int b, int k, int j, int i) {
   return widen(edge_avg<Real, C>(m, e, b, k, j, i));
 }
+// The same, reading an edge off the block's faces at in-block offset off from the block's
+// base eb (no neighbour logic, no 64-bit index arithmetic); ML = false: the stored value
+// everywhere (a same-level mesh's block-face edges hold their averages already)
+template <typename Real, int C, bool ML>
+__device__ __forceinline__ double edge_value_at(const DevMesh& m, const Real* __restrict__ e,
+                                                const Real* __restrict__ eb, int off, int b,
+                                                int k, int j, int i) {
+  if (!ML) return widen(__ldg(eb + off));
+  const bool on_face = (C != 0 && (i == m.is || i == m.ie + 1)) ||
+                       (C != 1 && (j == m.js || j == m.je + 1)) ||
+                       (C != 2 && (k == m.ks || k == m.ke + 1));
+  if (!on_face) return widen(__ldg(eb + off));
+  return edge_value<Real, C>(m, e, b, k, j, i);
+}
+
+// The average of the block-face edges over the blocks sharing them (edge_avg above) on a
+// same-level mesh, done before CT in two launches so that every value averaged is a
+// pre-average one: edge_fix_kernel writes the averages of the plan's edges into scratch,
+// edge_put_kernel stores them into the edge arrays.  The plan (edge_plan, built when the
+// mesh is set up) lists per block its own edges on block faces, x1-directed (n0), then
+// x2- (n1) and x3-directed (n2): the in-block offset, then the candidates to add in
+// edge_avg's order (x1-, x2-, x3-face neighbour, then the edge neighbour for an edge on
+// two faces), each as (offset index << 27) | offset in the neighbour, ~0u past the last.
+// blockIdx.x covers the plan, blockIdx.y the MeshBlocks: EB per thread, their loads
+// issued together.
+constexpr int EB = 4;
+template <typename Real>
+__global__ void __launch_bounds__(128)
+edge_fix_kernel(DevMesh m, const int4* __restrict__ plan, int n0, int n1, int n2,
+                const Real* __restrict__ e1, const Real* __restrict__ e2,
+                const Real* __restrict__ e3, Real* __restrict__ scratch) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = n0 + n1 + n2;
+  if (p >= np) return;
+  const int4 q = __ldg(plan + p);
+  const Real* e = p < n0 ? e1 : p < n0 + n1 ? e2 : e3;
+  const i64 ne = p < n0 ? m.ne1 : p < n0 + n1 ? m.ne2 : m.ne3;
+  const unsigned cand[3] = {(unsigned)q.y, (unsigned)q.z, (unsigned)q.w};
+  const bool two = cand[1] != ~0u;  // an edge on two block faces: three candidates
+  for (int b0 = blockIdx.y; b0 < m.nb; b0 += EB * gridDim.y) {
+    Real own[EB], v[EB][3];
+    int ok[EB][3];
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      const int b = b0 + u * gridDim.y;
+      const bool live = b < m.nb;
+      own[u] = live ? __ldg(e + (i64)b * ne + q.x) : Real(0);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int nb = (live && cand[c] != ~0u)
+                           ? __ldg(m.nbr + (i64)b * 27 + (int)(cand[c] >> 27)) : -1;
+        ok[u][c] = nb >= 0;
+        v[u][c] = nb >= 0 ? __ldg(e + (i64)nb * ne + (int)(cand[c] & 0x7ffffffu)) : Real(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      const int b = b0 + u * gridDim.y;
+      if (b >= m.nb) break;
+      Real sum = own[u];
+      int count = 1;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        if (ok[u][c]) { sum += v[u][c]; ++count; }
+      Real r;
+      if (two) {
+        // an edge shared by four blocks is scaled by 1/4; along a physical mesh face by
+        // 1/count (flux_correction_fc.cpp:1477-1481)
+        r = count == 4 ? sum * Real(0.25) : count == 1 ? own[u]
+                                                       : sum * (Real(1.0) / Real(count));
+      } else {
+        r = count == 2 ? sum * Real(0.5) : own[u];  // (flux_correction_fc.cpp:1362-1380)
+      }
+      scratch[(i64)b * np + p] = r;
+    }
+  }
+}
+template <typename Real>
+__global__ void __launch_bounds__(128)
+edge_put_kernel(DevMesh m, const int4* __restrict__ plan, int n0, int n1, int n2,
+                Real* __restrict__ e1, Real* __restrict__ e2, Real* __restrict__ e3,
+                const Real* __restrict__ scratch) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = n0 + n1 + n2;
+  if (p >= np) return;
+  const int off = __ldg(plan + p).x;
+  Real* e = p < n0 ? e1 : p < n0 + n1 ? e2 : e3;
+  const i64 ne = p < n0 ? m.ne1 : p < n0 + n1 ? m.ne2 : m.ne3;
+  for (int b0 = blockIdx.y; b0 < m.nb; b0 += EB * gridDim.y) {
+    Real v[EB];
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      const int b = b0 + u * gridDim.y;
+      v[u] = b < m.nb ? scratch[(i64)b * np + p] : Real(0);
+    }
+#pragma unroll
+    for (int u = 0; u < EB; ++u) {
+      const int b = b0 + u * gridDim.y;
+      if (b < m.nb) e[(i64)b * ne + off] = v[u];
+    }
+  }
+}
 
 // Field::CT, field/ct.cpp:31-116, plus the register average (weighted_ave.cpp), which
 // for VL2 and the first RK2 stage reduces to out = in and an in-place update on the
@@ -938,7 +1084,10 @@ __device__ __forceinline__ double edge_value(const DevMesh& m, const Real* __res
 // FP32 path: the corner EMFs are FP32, widened exactly, and the update is
 // ((wght/area)*len)*(e(+) - e(-)) in FP64 (the difference of two floats is exact in FP64).
 // bin/bout may alias.
-template <typename Real>
+// ML: a multi-level mesh, whose block-face edges take the corrected values
+// (edge_value_at).  On a same-level mesh the block-face edges already hold their averages
+// (edge_fix_kernel, edge_put_kernel), so the kernel reads plain edges.
+template <typename Real, bool ML>
 __global__ void __launch_bounds__(256)
 ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
           const Real* __restrict__ e1, const Real* __restrict__ e2,
@@ -967,9 +1116,11 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const int n1 = m.nx1 + 1, n2 = m.nx2 + 1, n3 = m.nx3 + 1;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n1 * n2 * n3) return;
-  const int i = m.is + r % n1;
-  const int j = m.js + (r / n1) % n2;
-  const int k = m.ks + r / (n1 * n2);
+  const int qr = fdiv(r, m.fd_n1);
+  const int kq = fdiv(qr, m.fd_n2);
+  const int i = m.is + (r - qr * n1);
+  const int j = m.js + (qr - kq * n2);
+  const int k = m.ks + kq;
   const bool f1 = j <= m.je && k <= m.ke;
   const bool f2 = i <= m.ie && k <= m.ke;
   const bool f3 = i <= m.ie && j <= m.je;
@@ -978,32 +1129,46 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   auto term = [&](double qd, double len, double qlen, double ep, double em) -> double {
     return exact ? qd * (len * ep - len * em) : qlen * (ep - em);
   };
+  // in-block offsets of the edges at (k,j,i) and the block bases of the edge arrays
+  const int c1 = m.nc1, c2 = m.nc2;
+  const int oe1 = (k * (c2 + 1) + j) * c1 + i;
+  const int oe2 = (k * c2 + j) * (c1 + 1) + i;
+  const int oe3 = (k * (c2 + 1) + j) * (c1 + 1) + i;
+  const Real* E1 = e1 + (i64)b * m.ne1;
+  const Real* E2 = e2 + (i64)b * m.ne2;
+  const Real* E3 = e3 + (i64)b * m.ne3;
   // the shared edges, each read once (and only where a face of this thread uses it)
-  const double e1c = (f2 || f3) ? edge_value<Real, 0>(m, e1, b, k, j, i) : 0.0;
-  const double e2c = (f1 || f3) ? edge_value<Real, 1>(m, e2, b, k, j, i) : 0.0;
-  const double e3c = (f1 || f2) ? edge_value<Real, 2>(m, e3, b, k, j, i) : 0.0;
+  const double e1c = (f2 || f3) ? edge_value_at<Real, 0, ML>(m, e1, E1, oe1, b, k, j, i) : 0.0;
+  const double e2c = (f1 || f3) ? edge_value_at<Real, 1, ML>(m, e2, E2, oe2, b, k, j, i) : 0.0;
+  const double e3c = (f1 || f2) ? edge_value_at<Real, 2, ML>(m, e3, E3, oe3, b, k, j, i) : 0.0;
   if (f1) {
-    const i64 o = f1idx(m, b, k, j, i);
+    const i64 o = (i64)b * m.nf1 + (k * c2 + j) * (c1 + 1) + i;
     double v = b1in[o];
     if (b1avg) v = g1 * b1avg[o] + g2 * v;
-    v -= term(q[0], l3, ql[0], edge_value<Real, 2>(m, e3, b, k, j + 1, i), e3c);
-    v += term(q[0], l2, ql[1], edge_value<Real, 1>(m, e2, b, k + 1, j, i), e2c);
+    v -= term(q[0], l3, ql[0],
+              edge_value_at<Real, 2, ML>(m, e3, E3, oe3 + (c1 + 1), b, k, j + 1, i), e3c);
+    v += term(q[0], l2, ql[1],
+              edge_value_at<Real, 1, ML>(m, e2, E2, oe2 + c2 * (c1 + 1), b, k + 1, j, i), e2c);
     b1out[o] = v;
   }
   if (f2) {
-    const i64 o = f2idx(m, b, k, j, i);
+    const i64 o = (i64)b * m.nf2 + (k * (c2 + 1) + j) * c1 + i;
     double v = b2in[o];
     if (b2avg) v = g1 * b2avg[o] + g2 * v;
-    v += term(q[1], l3, ql[2], edge_value<Real, 2>(m, e3, b, k, j, i + 1), e3c);
-    v -= term(q[1], l1, ql[3], edge_value<Real, 0>(m, e1, b, k + 1, j, i), e1c);
+    v += term(q[1], l3, ql[2], edge_value_at<Real, 2, ML>(m, e3, E3, oe3 + 1, b, k, j, i + 1),
+              e3c);
+    v -= term(q[1], l1, ql[3],
+              edge_value_at<Real, 0, ML>(m, e1, E1, oe1 + (c2 + 1) * c1, b, k + 1, j, i), e1c);
     b2out[o] = v;
   }
   if (f3) {
-    const i64 o = f3idx(m, b, k, j, i);
+    const i64 o = (i64)b * m.nf3 + (k * c2 + j) * c1 + i;
     double v = b3in[o];
     if (b3avg) v = g1 * b3avg[o] + g2 * v;
-    v -= term(q[2], l2, ql[4], edge_value<Real, 1>(m, e2, b, k, j, i + 1), e2c);
-    v += term(q[2], l1, ql[5], edge_value<Real, 0>(m, e1, b, k, j + 1, i), e1c);
+    v -= term(q[2], l2, ql[4], edge_value_at<Real, 1, ML>(m, e2, E2, oe2 + 1, b, k, j, i + 1),
+              e2c);
+    v += term(q[2], l1, ql[5], edge_value_at<Real, 0, ML>(m, e1, E1, oe1 + c1, b, k, j + 1, i),
+              e1c);
     b3out[o] = v;
   }
 }
@@ -1101,6 +1266,56 @@ exchange_kernel(DevMesh m, int with_u, T* __restrict__ u, double* __restrict__ b
   }
 }
 
+// The same exchange from the block's ghost plan (exchange_plan, built when the mesh is set
+// up): plan element p is one ghost element of a block, its in-block offset in bits 0-26
+// and in bits 27-31 the offset index ((o3+1)*3 + (o2+1))*3 + (o1+1) of the neighbour that
+// owns it; the owner's element is at offset dst - delta[what][dir].  The plan holds the
+// cell ghosts (n0), then the x1 (n1), x2 (n2) and x3 (n3) face ghosts; blockIdx.x covers
+// the plan from p0 (0 with U's ghosts, n0 without), blockIdx.y the MeshBlocks (strided).
+// No index division: one plan word and one neighbour-table word per copy.
+template <typename T>
+__global__ void __launch_bounds__(256)
+exchange_plan_kernel(DevMesh m, const unsigned* __restrict__ plan, int p0, int n0, int n1,
+                     int n2, int n3, const int* __restrict__ delta, T* u, double* b1,
+                     double* b2, double* b3) {
+  const int p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n0 + n1 + n2 + n3) return;
+  const unsigned wd = __ldg(plan + p);
+  const int dst = (int)(wd & 0x7ffffffu), dir = (int)(wd >> 27);
+  const int what = p < n0 ? 0 : p < n0 + n1 ? 1 : p < n0 + n1 + n2 ? 2 : 3;
+  const int src = dst - __ldg(delta + what * 27 + dir);
+  if (what == 0) {
+    for (int b = blockIdx.y; b < m.nb; b += gridDim.y) {
+      const int sb = __ldg(m.nbr + (i64)b * 27 + dir);
+      if (sb < 0) continue;  // a physical mesh face: the boundary functions fill it
+#pragma unroll
+      for (int n = 0; n < NHYDRO; ++n)
+        u[((i64)b * NHYDRO + n) * m.ncell + dst] = u[((i64)sb * NHYDRO + n) * m.ncell + src];
+    }
+    return;
+  }
+  // face fields: XB blocks per thread (blockIdx.y + q gridDim.y), their neighbour words
+  // and values all loaded before the stores, so the loads overlap (an owner's element is
+  // never a ghost, so no store here changes a value loaded here)
+  double* f = what == 1 ? b1 : what == 2 ? b2 : b3;
+  const i64 nf = what == 1 ? m.nf1 : what == 2 ? m.nf2 : m.nf3;
+  constexpr int XB = 4;
+  for (int b0 = blockIdx.y; b0 < m.nb; b0 += XB * gridDim.y) {
+    int sb[XB];
+    double v[XB];
+#pragma unroll
+    for (int q = 0; q < XB; ++q) {
+      const int b = b0 + q * gridDim.y;
+      sb[q] = b < m.nb ? __ldg(m.nbr + (i64)b * 27 + dir) : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < XB; ++q) v[q] = sb[q] >= 0 ? f[(i64)sb[q] * nf + src] : 0.0;
+#pragma unroll
+    for (int q = 0; q < XB; ++q)
+      if (sb[q] >= 0) f[(i64)(b0 + q * gridDim.y) * nf + dst] = v[q];
+  }
+}
+
 // ---------------------------------------------------------------------------------------
 // Reductions for the CFL time step of W(U) (Hydro::NewBlockTimeStep): warp shuffles, a
 // CTA reduction in shared memory and one atomicMin per CTA on the order-preserving bit
@@ -1179,18 +1394,12 @@ struct C2POne {
   Real u_d, u_e, vx, vy, vz, w_p, bcc1, bcc2, bcc3, b1lr, b2lr, b3lr;
   bool dfloored, pfloored;
 };
+// W(U) of one cell from its six face values and its conserved state at u[cs + n ncell]
 template <typename Real>
-__device__ __forceinline__ C2POne<Real> c2p_one(const DevMesh& m, int b, int k, int j, int i,
-                                                const double* __restrict__ b1,
-                                                const double* __restrict__ b2,
-                                                const double* __restrict__ b3,
-                                                const Real* u, i64 cs, bool ghost) {
+__device__ __forceinline__ C2POne<Real> c2p_cell(const DevMesh& m, double b1l, double b1r,
+                                                 double b2l, double b2r, double b3l,
+                                                 double b3r, const Real* u, i64 cs) {
   C2POne<Real> o;
-  // the face fields after the ghost exchange: a ghost cell's faces hold its owner's values
-  (void)ghost;
-  const double b1l = __ldg(b1 + f1idx(m, b, k, j, i)), b1r = __ldg(b1 + f1idx(m, b, k, j, i + 1));
-  const double b2l = __ldg(b2 + f2idx(m, b, k, j, i)), b2r = __ldg(b2 + f2idx(m, b, k, j + 1, i));
-  const double b3l = __ldg(b3 + f3idx(m, b, k, j, i)), b3r = __ldg(b3 + f3idx(m, b, k + 1, j, i));
   // the lower faces in the bulk precision (also the dt's |b_face - bcc| term)
   o.b1lr = to_real(b1l, Real());
   o.b2lr = to_real(b2l, Real());
@@ -1225,6 +1434,19 @@ __device__ __forceinline__ C2POne<Real> c2p_one(const DevMesh& m, int b, int k, 
   o.u_d = u_d;
   return o;
 }
+// the same at cell (b,k,j,i), reading the face fields after the ghost exchange (a ghost
+// cell's faces hold its owner's values)
+template <typename Real>
+__device__ __forceinline__ C2POne<Real> c2p_one(const DevMesh& m, int b, int k, int j, int i,
+                                                const double* __restrict__ b1,
+                                                const double* __restrict__ b2,
+                                                const double* __restrict__ b3,
+                                                const Real* u, i64 cs) {
+  return c2p_cell<Real>(m, __ldg(b1 + f1idx(m, b, k, j, i)), __ldg(b1 + f1idx(m, b, k, j, i + 1)),
+                        __ldg(b2 + f2idx(m, b, k, j, i)), __ldg(b2 + f2idx(m, b, k, j + 1, i)),
+                        __ldg(b3 + f3idx(m, b, k, j, i)), __ldg(b3 + f3idx(m, b, k + 1, j, i)),
+                        u, cs);
+}
 
 // W(U) over whole blocks (ghosts included: a ghost cell reads its conserved state from the
 // block that owns it, its faces from the exchanged face fields), fused with
@@ -1239,58 +1461,68 @@ c2p_kernel(DevMesh m, int do_dt, const double* __restrict__ b1,
            const double* __restrict__ b2, const double* __restrict__ b3, const Real* u,
            Real* __restrict__ w, Real* __restrict__ bcc, Real* __restrict__ cc,
            DevClock* clk, int* __restrict__ flist, unsigned* __restrict__ fcount) {
-  const i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+  // blockIdx.y (strided) is the MeshBlock, blockIdx.x/threadIdx.x the cell r of it:
+  // r = (k nc2 + j) nc1 + i, so q = r / nc1 = k nc2 + j, and the face offsets follow from
+  // r, q and k without 64-bit arithmetic
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
   Real cell_dt = big_dt(Real());
-  if (t < (i64)m.nb * m.ncell) {
-    const int b = (int)(t / m.ncell);
-    i64 r = t - (i64)b * m.ncell;
-    const int i = (int)(r % m.nc1);
-    r /= m.nc1;
-    const int j = (int)(r % m.nc2);
-    const int k = (int)(r / m.nc2);
-    bool ghost;
-    const i64 cs = src_cell(m, b, k, j, i, NHYDRO, &ghost);
-    if (cs >= 0) {  // not a physical-boundary ghost
-    const C2POne<Real> o = c2p_one<Real>(m, b, k, j, i, b1, b2, b3, u, cs, ghost);
-    const i64 vs = m.ncell;
-    const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
-    const i64 cb = cidx(m, b, 0, 3, k, j, i);
-    if ((o.dfloored || o.pfloored) && !ghost) {
-      const unsigned slot = atomicAdd(fcount, 1u);
-      flist[slot] = (int)(((i64)b * m.nx3 + (k - m.ks)) * m.nx2 * m.nx1 +
-                          (i64)(j - m.js) * m.nx1 + (i - m.is));
-    }
-    if ((o.dfloored || o.pfloored) && do_dt) atomicAdd(&clk->c2p_floor_count, 1);
-    w[c] = o.u_d;
-    w[c + vs] = o.vx;
-    w[c + 2 * vs] = o.vy;
-    w[c + 3 * vs] = o.vz;
-    w[c + 4 * vs] = o.w_p;
-    bcc[cb] = o.bcc1;
-    bcc[cb + vs] = o.bcc2;
-    bcc[cb + 2 * vs] = o.bcc3;
-    store_cce<Real, false>(cc, cb, vs, o.vx, o.vy, o.vz, o.bcc1, o.bcc2, o.bcc3);
-    if (do_dt && !ghost) {
-      // new_blockdt.cpp:80-103, in the bulk precision on the stored primitives (FP64
-      // path: the reference's arithmetic; FP32 path: FP32, reduced in FP64)
-      const Real gam = rgamma(m, Real());
-      Real dt1 = rdx(m, 0, Real())[(i64)b * m.nc1 + i],
-           dt2 = rdx(m, 1, Real())[(i64)b * m.nc2 + j],
-           dt3 = rdx(m, 2, Real())[(i64)b * m.nc3 + k];
-      Real bx = o.bcc1 + dabs(o.b1lr - o.bcc1);
-      Real cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc2, o.bcc3, bx);
-      Real speed = smax<Real>(Real(0.0), (dabs(o.vx) + cf));
-      dt1 /= (speed);
-      bx = o.bcc2 + dabs(o.b2lr - o.bcc2);
-      cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc3, o.bcc1, bx);
-      speed = smax<Real>(Real(0.0), (dabs(o.vy) + cf));
-      dt2 /= (speed);
-      bx = o.bcc3 + dabs(o.b3lr - o.bcc3);
-      cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc1, o.bcc2, bx);
-      speed = smax<Real>(Real(0.0), (dabs(o.vz) + cf));
-      dt3 /= (speed);
-      cell_dt = smin<Real>(smin<Real>(dt1, dt2), dt3);
-    }
+  if (r < (int)m.ncell) {
+    const int q = fdiv(r, m.fd_nc1);
+    const int i = r - q * m.nc1;
+    const int k = fdiv(q, m.fd_nc2);
+    const int j = q - k * m.nc2;
+    const bool ghost =
+        i < m.is || i > m.ie || j < m.js || j > m.je || k < m.ks || k > m.ke;
+    for (int b = blockIdx.y; b < m.nb; b += gridDim.y) {
+      bool gh;
+      const i64 cs = ghost ? src_cell(m, b, k, j, i, NHYDRO, &gh)
+                           : (i64)b * NHYDRO * m.ncell + r;
+      if (cs < 0) continue;  // a physical-boundary ghost
+      const double* f1 = b1 + (i64)b * m.nf1 + (r + q);
+      const double* f2 = b2 + (i64)b * m.nf2 + (r + k * m.nc1);
+      const double* f3 = b3 + (i64)b * m.nf3 + r;
+      const C2POne<Real> o = c2p_cell<Real>(m, __ldg(f1), __ldg(f1 + 1), __ldg(f2),
+                                            __ldg(f2 + m.nc1), __ldg(f3),
+                                            __ldg(f3 + (i64)m.nc2 * m.nc1), u, cs);
+      const i64 vs = m.ncell;
+      const i64 c = (i64)b * NHYDRO * m.ncell + r;
+      const i64 cb = (i64)b * 3 * m.ncell + r;
+      if ((o.dfloored || o.pfloored) && !ghost) {
+        const unsigned slot = atomicAdd(fcount, 1u);
+        flist[slot] = (int)(((i64)b * m.nx3 + (k - m.ks)) * m.nx2 * m.nx1 +
+                            (i64)(j - m.js) * m.nx1 + (i - m.is));
+      }
+      if ((o.dfloored || o.pfloored) && do_dt) atomicAdd(&clk->c2p_floor_count, 1);
+      w[c] = o.u_d;
+      w[c + vs] = o.vx;
+      w[c + 2 * vs] = o.vy;
+      w[c + 3 * vs] = o.vz;
+      w[c + 4 * vs] = o.w_p;
+      bcc[cb] = o.bcc1;
+      bcc[cb + vs] = o.bcc2;
+      bcc[cb + 2 * vs] = o.bcc3;
+      store_cce<Real, false>(cc, cb, vs, o.vx, o.vy, o.vz, o.bcc1, o.bcc2, o.bcc3);
+      if (do_dt && !ghost) {
+        // new_blockdt.cpp:80-103, in the bulk precision on the stored primitives (FP64
+        // path: the reference's arithmetic; FP32 path: FP32, reduced in FP64)
+        const Real gam = rgamma(m, Real());
+        Real dt1 = rdx(m, 0, Real())[(i64)b * m.nc1 + i],
+             dt2 = rdx(m, 1, Real())[(i64)b * m.nc2 + j],
+             dt3 = rdx(m, 2, Real())[(i64)b * m.nc3 + k];
+        Real bx = o.bcc1 + dabs(o.b1lr - o.bcc1);
+        Real cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc2, o.bcc3, bx);
+        Real speed = smax<Real>(Real(0.0), (dabs(o.vx) + cf));
+        dt1 /= (speed);
+        bx = o.bcc2 + dabs(o.b2lr - o.bcc2);
+        cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc3, o.bcc1, bx);
+        speed = smax<Real>(Real(0.0), (dabs(o.vy) + cf));
+        dt2 /= (speed);
+        bx = o.bcc3 + dabs(o.b3lr - o.bcc3);
+        cf = fast_ms<Real>(gam, o.u_d, o.w_p, o.bcc1, o.bcc2, bx);
+        speed = smax<Real>(Real(0.0), (dabs(o.vz) + cf));
+        dt3 /= (speed);
+        cell_dt = smin<Real>(cell_dt, smin<Real>(smin<Real>(dt1, dt2), dt3));
+      }
     }
   }
   if (do_dt) cta_min_to_clock<Real>(cell_dt, clk);  // reduced in the bulk precision
@@ -1316,7 +1548,7 @@ c2p_floor_writeback_kernel(DevMesh m, const double* __restrict__ b1,
     const int j = m.js + r % m.nx2;
     const int k = m.ks + r / m.nx2;
     const i64 c = cidx(m, b, 0, NHYDRO, k, j, i);
-    const C2POne<Real> o = c2p_one<Real>(m, b, k, j, i, b1, b2, b3, u, c, false);
+    const C2POne<Real> o = c2p_one<Real>(m, b, k, j, i, b1, b2, b3, u, c);
     const i64 vs = m.ncell;
     if (o.dfloored) {
       u[c] = o.u_d;

@@ -442,8 +442,9 @@ athgpu_status athgpu_op_corner_e(athgpu_ctx* c, const double* w, const double* b
                                                       c->stream>>>(
       m, (const double*)r.wbuf[0], (const double*)r.bcc, (double*)r.cce);
   const long long n = (long long)(m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
-  (sr ? corner_e_kernel<double, true> : corner_e_kernel<double, false>)<<<grid_of(n, 128),
-                                                                         128, 0, c->stream>>>(
+  (sr ? corner_e_kernel<double, true>
+      : corner_e_kernel<double, false>)<<<dim3(grid_of(n, 128), m.nb < 65535 ? m.nb : 65535),
+                                          128, 0, c->stream>>>(
       m, (const double*)r.cce, (double*)r.e3x1, (double*)r.e2x1, (double*)r.w1f,
       (double*)r.e1x2, (double*)r.e3x2, (double*)r.w2f, (double*)r.e1x3, (double*)r.e2x3,
       (double*)r.w3f, (double*)r.e1, (double*)r.e2, (double*)r.e3);

@@ -104,7 +104,16 @@ static void launch_exchange(athgpu_ctx* c, Real* u, double* b1, double* b2, doub
   const long long g2 = m.nf2 - (long long)m.nx1 * (m.nx2 + 1) * m.nx3;
   const long long g3 = m.nf3 - (long long)m.nx1 * m.nx2 * (m.nx3 + 1);
   const long long n = (gc + g1 + g2 + g3) * m.nb;
-  if (n < (1LL << 31) - 256)
+  if (c->xplan) {
+    const int* xn = c->xplan_n;
+    const int p0 = with_u ? 0 : xn[0];
+    const long long cnt = (long long)xn[0] + xn[1] + xn[2] + xn[3] - p0;
+    // four MeshBlocks per thread (exchange_plan_kernel's XB)
+    const long long gy = (m.nb + 3) / 4;
+    exchange_plan_kernel<Real><<<dim3(nblk(cnt, 256), gy < 65535 ? gy : 65535), 256, 0,
+                                 st>>>(m, c->xplan, p0, xn[0], xn[1], xn[2], xn[3],
+                                       c->xdelta, u, b1, b2, b3);
+  } else if (n < (1LL << 31) - 256)
     exchange_kernel<Real, int><<<nblk(n, 256), 256, 0, st>>>(m, with_u, u, b1, b2, b3);
   else
     exchange_kernel<Real, long long><<<nblk(n, 256), 256, 0, st>>>(m, with_u, u, b1, b2, b3);
@@ -205,7 +214,8 @@ static void launch_exchange_and_c2p(athgpu_ctx* c, Real* u, double* b1, double* 
       c->launches += 2;
     } else {
       cudaMemsetAsync(c->c2p_qcount, 0, sizeof(unsigned), s);
-      c2p_kernel<Real, KAHAN><<<nblk(nc, 128), 128, 0, s>>>(
+      const dim3 grid(nblk(m.ncell, 128), m.nb < 65535 ? m.nb : 65535);
+      c2p_kernel<Real, KAHAN><<<grid, 128, 0, s>>>(
           m, do_dt, b1, b2, b3, u, wout, (Real*)c->r.bcc, (Real*)c->r.cce, c->clk,
           c->c2p_queue, c->c2p_qcount);
       c2p_floor_writeback_kernel<Real, KAHAN><<<64, 128, 0, s>>>(
@@ -287,15 +297,29 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
 #undef FLUX_RS
 #undef FLUX
   {
-    const long long n = (long long)m.nb * (m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
+    const long long n = (long long)(m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
     ProfScope ps(c, "corner_e");
     auto kern = c->desc.relativistic ? corner_e_kernel<Real, true> : corner_e_kernel<Real, false>;
-    kern<<<nblk(n, 128), 128, 0, s>>>(
+    kern<<<dim3(nblk(n, 128), m.nb < 65535 ? m.nb : 65535), 128, 0, s>>>(
         m, (const Real*)r.cce, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f, (Real*)r.e1x2,
         (Real*)r.e3x2, (Real*)r.w2f, (Real*)r.e1x3, (Real*)r.e2x3, (Real*)r.w3f,
         (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
   }
-  if (m.ml.on) {
+  if (!m.ml.on) {
+    // same-level edge averaging of the block-face edges (flux_correction_fc.cpp)
+    ProfScope ps2(c, "edge_avg");
+    const int* en = c->eplan_n;
+    const long long ne = (long long)en[0] + en[1] + en[2];
+    const long long gy = (m.nb + EB - 1) / EB;
+    const dim3 grid(nblk(ne, 128), gy < 65535 ? gy : 65535);
+    edge_fix_kernel<Real><<<grid, 128, 0, s>>>(m, c->eplan, en[0], en[1], en[2],
+                                               (const Real*)r.e1, (const Real*)r.e2,
+                                               (const Real*)r.e3, (Real*)c->escratch);
+    edge_put_kernel<Real><<<grid, 128, 0, s>>>(m, c->eplan, en[0], en[1], en[2], (Real*)r.e1,
+                                               (Real*)r.e2, (Real*)r.e3,
+                                               (const Real*)c->escratch);
+    c->launches += 2;
+  } else {
     // EMF correction across levels (flux_correction_fc.cpp)
     ProfScope ps2(c, "ml_emf");
     const long long chunks = (ml_emf_positions(m) + 127) / 128;
@@ -311,11 +335,10 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
     const long long per = (long long)(m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
     dim3 grid(nblk(per, 256), m.nb);
     ProfScope ps(c, "ct");
-    ct_kernel<Real><<<grid, 256, 0, s>>>(m, beta, c->clk, (const Real*)r.e1,
-                                         (const Real*)r.e2, (const Real*)r.e3, r.b1, r.b2,
-                                         r.b3, o1, o2, o3, avg ? r.bs1 : nullptr,
-                                         avg ? r.bs2 : nullptr, avg ? r.bs3 : nullptr, g1,
-                                         g2);
+    (m.ml.on ? ct_kernel<Real, true> : ct_kernel<Real, false>)<<<grid, 256, 0, s>>>(
+        m, beta, c->clk, (const Real*)r.e1, (const Real*)r.e2, (const Real*)r.e3, r.b1, r.b2,
+        r.b3, o1, o2, o3, avg ? r.bs1 : nullptr, avg ? r.bs2 : nullptr,
+        avg ? r.bs3 : nullptr, g1, g2);
   }
   c->launches += 2;
   launch_exchange_and_c2p<Real, KAHAN>(c, uout, o1, o2, o3, stage == 2);

@@ -199,9 +199,9 @@ def test_graph_replay_counts_launches():
     g.cycle(3)
     g.synchronize()
     per = g.launch_count() / 3
-    # two stages of 8 kernels (3 sweeps, corner EMFs, CT, ghost exchange, W(U), the
-    # floors' write-back of U), one clock update
-    assert per == 2 * 8 + 1
+    # two stages of 10 kernels (3 sweeps, corner EMFs, the block-face edge average and
+    # its store, CT, ghost exchange, W(U), the floors' write-back of U), one clock update
+    assert per == 2 * 10 + 1
 
 
 def test_autotune_keeps_the_state_and_the_results():
@@ -328,7 +328,7 @@ def test_physical_boundaries_launch_count():
     g.launch_count(reset=True)
     g.cycle(3)
     g.synchronize()
-    assert g.launch_count() / 3 == 2 * (8 + 2 * 2) + 1
+    assert g.launch_count() / 3 == 2 * (10 + 2 * 2) + 1
     g.close()
 
 
