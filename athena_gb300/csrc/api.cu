@@ -448,6 +448,8 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   m.fd_nc2 = make_fastdiv(m.nc2);
   m.fd_n1 = make_fastdiv(m.nx1 + 1);
   m.fd_n2 = make_fastdiv(m.nx2 + 1);
+  m.fd_r1 = make_fastdiv(m.nx1 + 2);
+  m.fd_r2 = make_fastdiv(m.nx2 + 2);
   m.nf1 = (i64)m.nc3 * m.nc2 * (m.nc1 + 1);
   m.nf2 = (i64)m.nc3 * (m.nc2 + 1) * m.nc1;
   m.nf3 = (i64)(m.nc3 + 1) * m.nc2 * m.nc1;

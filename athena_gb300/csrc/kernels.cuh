@@ -72,6 +72,7 @@ struct DevMesh {
   int is, ie, js, je, ks, ke;
   i64 ncell, nf1, nf2, nf3, ne1, ne2, ne3;  // per-block element counts
   FastDiv fd_nc1, fd_nc2, fd_n1, fd_n2;     // divisors nc1, nc2, nx1 + 1, nx2 + 1
+  FastDiv fd_r1, fd_r2;                     // divisors nx1 + 2, nx2 + 2
   double gamma, dfloor, pfloor, cfl, tlim;
   const double* dx1f;  // [nb][nc1]
   const double* dx2f;  // [nb][nc2]
@@ -383,10 +384,10 @@ struct UpdateArgs {
   int* err;               // set when a bulk-copy wait of a sweep timed out
 };
 
-// x1 sweep: rows (b, k in [ks-1,ke+1], j in [js-1,je+1]) of cells i in [is-1, ie+1],
-// flattened over rows.  A warp reconstructs 32 consecutive cells: lane L > 0 solves the
-// left face of its cell with the upper-face state of lane L-1 (shuffle up), and lanes
-// 1..30 form their cell's x1 flux difference with the face flux of lane L+1 (shuffle
+// x1 sweep: rows (k in [ks-1,ke+1], j in [js-1,je+1]) of cells i in [is-1, ie+1] of block
+// blockIdx.y, flattened over rows.  A warp reconstructs 32 consecutive cells: lane L > 0
+// solves the left face of its cell with the upper-face state of lane L-1 (shuffle up), and
+// lanes 1..30 form their cell's x1 flux difference with the face flux of lane L+1 (shuffle
 // down).  Warps advance by 30 cells, so every cell is reconstructed at most twice, every
 // face solved at most twice (identical duplicate stores) and every difference formed once.
 template <typename Real, int ORDER, int RS>
@@ -396,20 +397,20 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
                Real* __restrict__ dflx, Real* __restrict__ e3, Real* __restrict__ e2,
                Real* __restrict__ wct) {
   const int lane = threadIdx.x & 31;
-  const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int ncr = m.nx1 + 2, nrj = m.nx2 + 2, nrk = m.nx3 + 2;
-  const i64 total = (i64)m.nb * nrk * nrj * ncr;
-  const i64 g = warp * 30 + lane - 1;
-  const bool valid = (g >= 0) && (g < total);
+  const int per = nrk * nrj * ncr;
+  const int g = warp * 30 + lane - 1;
+  const bool valid = (g >= 0) && (g < per);
   Real qlp[NWAVE], qrm[NWAVE];
-  int b = 0, k = 0, j = 0, c = 0;
+  const int b = blockIdx.y;
+  int k = 0, j = 0, c = 0;
   if (valid) {
-    i64 row = g / ncr;
-    c = (int)(g - row * ncr);
-    j = (int)(row % nrj) + m.js - 1;
-    i64 r2 = row / nrj;
-    k = (int)(r2 % nrk) + m.ks - 1;
-    b = (int)(r2 / nrk);
+    const int row = fdiv(g, m.fd_r1);
+    c = g - row * ncr;
+    const int kq = fdiv(row, m.fd_r2);
+    j = row - kq * nrj + m.js - 1;
+    k = kq + m.ks - 1;
     recon_cell<Real, 0, ORDER>(m, w, bcc, b, k, j, m.is - 1 + c, qlp, qrm);
   } else {
 #pragma unroll

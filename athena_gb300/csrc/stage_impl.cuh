@@ -36,10 +36,10 @@ static void launch_fluxes(athgpu_ctx* c, const Real* w, const Real* bcc, const d
     c->launches += 1;
   }
   {
-    const long long cells = (long long)m.nb * (m.nx3 + 2) * (m.nx2 + 2) * (m.nx1 + 2);
-    const long long warps = (cells + 29) / 30;
+    const long long cells = (long long)(m.nx3 + 2) * (m.nx2 + 2) * (m.nx1 + 2);
+    const long long warps = (cells + 29) / 30;  // per MeshBlock (blockIdx.y)
     ProfScope ps(c, "flux_x1");
-    flux_x1_kernel<Real, ORDER, RS><<<nblk(warps * 32, 128), 128, 0, s>>>(
+    flux_x1_kernel<Real, ORDER, RS><<<dim3(nblk(warps * 32, 128), m.nb), 128, 0, s>>>(
         m, w, bcc, b1, c->clk, (Real*)r.dflx, (Real*)r.e3x1, (Real*)r.e2x1, (Real*)r.w1f);
   }
   {
