@@ -695,7 +695,7 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
   dims.nx[0] = m.nx1; dims.nx[1] = m.nx2; dims.nx[2] = m.nx3;
   dims.ng = m.ng;
   for (int f = 0; f < 6; ++f) dims.bc[f] = m.bc[f];
-  MlPlan plan;
+  MlPlan& plan = c->mlplan;
   std::string err;
   if (!build_ml_plan(dims, nb, nbr_table, nbr_count, nblevel, loc, &plan, &err))
     return fail(ATHGPU_ERR_ARG, err.c_str());

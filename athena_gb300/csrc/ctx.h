@@ -7,6 +7,7 @@
 
 #include "../../include/athena_gb300.h"
 #include "kernels.cuh"
+#include "ml_plan.h"
 
 namespace athgpu {
 
@@ -59,6 +60,9 @@ struct athgpu_ctx {
   double* fxv = nullptr;     // cell centres x1v | x2v | x3v per block (prolongation)
   double* eps_buf = nullptr; // per-block refinement measure (athgpu_refinement_eps)
   athgpu::MlDevice mld;
+  // the host side of the multi-level plan, kept so that a regrid's new plan reuses its
+  // storage (no fresh pages for tens of MB of operation lists)
+  athgpu::MlPlan mlplan;
   float* coords32 = nullptr; // the same, rounded to FP32, for the FP32 kernels
   int* nbr = nullptr;
   // ghost plan of a same-level mesh's blocks (exchange_plan_kernel): plan words of the

@@ -12,7 +12,10 @@
 // reference packs and unpacks its buffers.
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <cstdio>
+#include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -499,28 +502,119 @@ void mark_runs(MlOpList* L, const Ix& x) {
   });
 }
 
-// f(b) for every block on the host's cores (chunks of 32 blocks); false if any call
-// returned false
+// Host threads kept for the planner's parallel loops: creating threads costs tens of
+// microseconds each, several times per regrid otherwise.  run(n, f) calls f(i) for
+// i in [0, n) in chunks of 32 on the pool's threads and the caller's; one run at a time.
+class PlanPool {
+ public:
+  static PlanPool& get() {
+    static PlanPool pool;
+    return pool;
+  }
+  void run(int n, const std::function<void(int)>& f) {
+    std::lock_guard<std::mutex> one(run_mu_);
+    const int nt = std::min<int>((int)workers_.size() + 1, n / 64 + 1);
+    if (nt <= 1) {
+      for (int i = 0; i < n; ++i) f(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &f;
+      n_ = n;
+      next_.store(0);
+      helpers_ = nt - 1;
+      busy_ = nt - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    work(f, n);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return busy_ == 0; });
+    job_ = nullptr;
+  }
+  ~PlanPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+  }
+
+ private:
+  PlanPool() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nw = std::max(0, std::min(16, hw ? (int)hw : 1) - 1);
+    for (int t = 0; t < nw; ++t) workers_.emplace_back([this] { loop(); });
+  }
+  void work(const std::function<void(int)>& f, int n) {
+    for (;;) {
+      const int i0 = next_.fetch_add(32);
+      if (i0 >= n) return;
+      const int i1 = std::min(n, i0 + 32);
+      for (int i = i0; i < i1; ++i) f(i);
+    }
+  }
+  void loop() {
+    unsigned long long seen = 0;
+    for (;;) {
+      const std::function<void(int)>* f;
+      int n;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || (gen_ != seen && helpers_ > 0); });
+        if (stop_) return;
+        seen = gen_;
+        --helpers_;  // this run takes at most nt - 1 helpers
+        f = job_;
+        n = n_;
+      }
+      work(*f, n);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--busy_ == 0) done_cv_.notify_one();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* job_ = nullptr;
+  int n_ = 0, helpers_ = 0, busy_ = 0;
+  unsigned long long gen_ = 0;
+  bool stop_ = false;
+  std::atomic<int> next_{0};
+};
+
+// f(b) for every block on the host's cores; false if any call returned false
 template <typename F>
 bool for_blocks(int nb, F f) {
-  const unsigned hw = std::thread::hardware_concurrency();
-  const int nt = std::max(1, std::min<int>(hw ? (int)hw : 1, std::min(16, nb / 64 + 1)));
-  std::atomic<int> next{0};
   std::atomic<bool> ok{true};
-  auto work = [&]() {
-    for (;;) {
-      const int b0 = next.fetch_add(32);
-      if (b0 >= nb) return;
-      const int b1 = std::min(nb, b0 + 32);
-      for (int b = b0; b < b1; ++b)
-        if (!f(b)) ok = false;
-    }
-  };
-  std::vector<std::thread> th;
-  for (int t = 1; t < nt; ++t) th.emplace_back(work);
-  work();
-  for (auto& t : th) t.join();
+  PlanPool::get().run(nb, [&](int b) {
+    if (!f(b)) ok = false;
+  });
   return ok;
+}
+
+// the per-block lists in block order as one operation list (blocks with no operations
+// left out), copied in parallel
+void gather(const std::vector<std::vector<MlOp>>& per, MlOpList* L) {
+  const int nb = (int)per.size();
+  L->clear();
+  std::vector<size_t> start(nb + 1, 0);
+  for (int b = 0; b < nb; ++b) start[b + 1] = start[b] + per[b].size();
+  L->ops.resize(start[nb]);
+  L->off.push_back(0);
+  for (int b = 0; b < nb; ++b)
+    if (!per[b].empty()) {
+      L->blk.push_back(b);
+      L->off.push_back((int)start[b + 1]);
+    }
+  for_blocks(nb, [&](int b) {
+    if (!per[b].empty())
+      memcpy(L->ops.data() + start[b], per[b].data(), per[b].size() * sizeof(MlOp));
+    return true;
+  });
 }
 
 }  // namespace
@@ -568,7 +662,9 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
   }
   // ---- phase R: restriction for coarser neighbours (into the send and coarse buffers) --
   P->r.clear(); P->x.clear(); P->p.clear();
-  std::vector<std::vector<MlOp>> per(nb);
+  std::vector<std::vector<MlOp>>& per = P->per;
+  per.resize(nb);
+  for (auto& v : per) v.clear();
   for_blocks(nb, [&](int s) {
     std::vector<MlOp>& ops = per[s];
     for (int n = 0; n < nbr_count[s]; ++n) {
@@ -585,15 +681,7 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
     }
     return true;
   });
-  {
-    size_t tot = 0;
-    for (const auto& v : per) tot += v.size();
-    P->r.ops.reserve(tot);
-    P->r.off.reserve(nb + 1);
-    P->r.blk.reserve(nb);
-  }
-  for (int s = 0; s < nb; ++s)
-    if (!per[s].empty()) P->r.add(s, per[s]);
+  gather(per, &P->r);
   // ---- phase X: the ghost exchange, per receiver in neighbour-list order; all U copies
   // first (SETB_HYD), then all face-field copies (SETB_FLD)
   // the entry of each block's list by (neighbour gid, offset), sorted, for the lookups of
@@ -622,7 +710,11 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
   };
   for (auto& v : per) v.clear();
   const bool xok = for_blocks(nb, [&](int r) {
-    std::vector<MlOp> ucopies, bcopies;
+    // U copies into the list, face-field copies behind them (at most 3 per neighbour)
+    std::vector<MlOp>& all = per[r];
+    all.reserve(4 * nbr_count[r]);
+    MlOp bcopies[3 * ML_MAXNB];
+    int nbc = 0;
     const int par[3] = {(int)(loc[(long long)r * 4 + 1] & 1), (int)(loc[(long long)r * 4 + 2] & 1),
                         (int)(loc[(long long)r * 4 + 3] & 1)};
     for (int n = 0; n < nbr_count[r]; ++n) {
@@ -643,7 +735,7 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
       MlOp op = make_op(ML_COPY_U, 0, du);
       op.src_kind = us; op.dst_kind = ud; op.src = s;
       for (int a = 0; a < 3; ++a) op.o[a] = su.s[a];
-      ucopies.push_back(op);
+      all.push_back(op);
       for (int d = 0; d < 3; ++d) {
         Box db, sb;
         if (q.level == level(r)) { db = fc_recv_same(x, q, d); sb = fc_send_same(x, qs, d); }
@@ -654,24 +746,14 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
         MlOp ob = make_op(ML_COPY_B, d, db);
         ob.src_kind = us; ob.dst_kind = ud; ob.src = s;
         for (int a = 0; a < 3; ++a) ob.o[a] = sb.s[a];
-        bcopies.push_back(ob);
+        bcopies[nbc++] = ob;
       }
     }
-    std::vector<MlOp>& all = per[r];
-    all = ucopies;
-    all.insert(all.end(), bcopies.begin(), bcopies.end());
+    all.insert(all.end(), bcopies, bcopies + nbc);
     return true;
   });
   if (!xok) return false;
-  {
-    size_t tot = 0;
-    for (const auto& v : per) tot += v.size();
-    P->x.ops.reserve(tot);
-    P->x.off.reserve(nb + 1);
-    P->x.blk.reserve(nb);
-  }
-  for (int r = 0; r < nb; ++r)
-    if (!per[r].empty()) P->x.add(r, per[r]);
+  gather(per, &P->x);
   // ---- phase P: ProlongateBoundaries per block with coarser neighbours ------------------
   const int cn = x.cng - 1;
   for (auto& v : per) v.clear();
@@ -787,15 +869,7 @@ bool build_ml_plan(const MlDims& dims, int nb, const int* nbr_table, const int* 
     }
     return true;
   });
-  {
-    size_t tot = 0;
-    for (const auto& v : per) tot += v.size();
-    P->p.ops.reserve(tot);
-    P->p.off.reserve(nb + 1);
-    P->p.blk.reserve(nb);
-  }
-  for (int b = 0; b < nb; ++b)
-    if (!per[b].empty()) P->p.add(b, per[b]);
+  gather(per, &P->p);
   // ---- flux correction tasks: (coarse block, finer block, face | fi1 << 4 | fi2 << 5) --
   P->flux_tasks.clear();
   P->fmask.assign(nb, 0);

@@ -169,8 +169,8 @@ RgCopy box_copy(const void* sbase, ArrDims sd, long long slim, const void* dbase
   return t;
 }
 
-template <typename T>
-cudaError_t upload(const std::vector<T>& h, T** d, cudaStream_t s) {
+template <typename T, typename A>
+cudaError_t upload(const std::vector<T, A>& h, T** d, cudaStream_t s) {
   *d = nullptr;
   if (h.empty()) return cudaSuccess;
   cudaError_t e = cudaMallocAsync((void**)d, sizeof(T) * h.size(), s);

@@ -314,11 +314,14 @@ def run_gpu(args, rank, world, local_rank):
             if world > 1:
                 dist.barrier()
             t0 = time.perf_counter()
+            step_ms = []
             for _ in range(e_steps):
+                ts = time.perf_counter()
                 g.set_state(*pinned)    # host -> device (pinned) every step
                 g.initialize()          # W(U), ghosts and the time step of that state
                 g.cycle(1)
                 out = g.state(out=pinned_out)   # device -> host (pinned) every step
+                step_ms.append((time.perf_counter() - ts) * 1e3)  # the download syncs
             torch.cuda.synchronize()
             te = time.perf_counter() - t0
             if world > 1:
@@ -329,6 +332,8 @@ def run_gpu(args, rank, world, local_rank):
                           "h2d_bytes_per_step": ebytes, "d2h_bytes_per_step": ebytes,
                           "steps": e_steps, "ms_per_step": te / e_steps * 1e3,
                           "host_copy_mode": host_mode,
+                          "step_ms": {"min": min(step_ms), "median": float(np.median(step_ms)),
+                                      "max": max(step_ms)},
                           "upload_download_ms_by_mode": mode_ms,
                           "link_ceiling": link_ceiling(dev, ebytes)}
         g.close()
