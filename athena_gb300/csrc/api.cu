@@ -386,11 +386,11 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   if (d->nx1 < d->nghost || d->nx2 < d->nghost || d->nx3 < d->nghost)
     return fail(ATHGPU_ERR_ARG, "MeshBlock smaller than the ghost width");
   if (d->rsolver != ATHGPU_HLLD && d->rsolver != ATHGPU_HLLE && d->rsolver != ATHGPU_LLF &&
-      d->rsolver != ATHGPU_ROE)
+      d->rsolver != ATHGPU_ROE && d->rsolver != ATHGPU_LHLLD)
     return fail(ATHGPU_ERR_ARG, "unknown Riemann solver");
   if (d->precision != ATHGPU_FP64 && d->precision != ATHGPU_FP32)
     return fail(ATHGPU_ERR_ARG, "unknown precision");
-  if (d->relativistic && d->rsolver == ATHGPU_ROE)
+  if (d->relativistic && (d->rsolver == ATHGPU_ROE || d->rsolver == ATHGPU_LHLLD))
     return fail(ATHGPU_ERR_UNSUPPORTED,
                 "relativistic MHD supports the HLLD, HLLE and LLF solvers (hlld_rel.cpp, "
                 "hlle_mhd_rel.cpp, llf_mhd_rel.cpp) only");
@@ -685,6 +685,9 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
     return fail(ATHGPU_ERR_STATE, "athgpu_set_multilevel must come before athgpu_initialize");
   if (c->desc.relativistic)
     return fail(ATHGPU_ERR_UNSUPPORTED, "mesh refinement supports Newtonian MHD only");
+  if (c->desc.rsolver == ATHGPU_LHLLD)
+    return fail(ATHGPU_ERR_UNSUPPORTED,
+                "mesh refinement supports the HLLD, HLLE, LLF and Roe solvers");
   DevMesh& m = c->m;
   if (m.ng % 2)
     return fail(ATHGPU_ERR_ARG, "mesh refinement needs an even nghost (mesh_refinement.cpp:44)");

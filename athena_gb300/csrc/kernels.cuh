@@ -319,14 +319,39 @@ __device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)
   if (ORDER == 3) ppm_floors(m, qlp, qrm);
 }
 
+// The per-cell parts of Hydro::CalculateVelocityDifferences
+// (hydro/calculate_velocity_differences.cpp:23-64, 3-D) for faces normal to DIR: the
+// normal velocity vn and, for the transverse axes a1 = (DIR+1)%3 and a2 = (DIR+2)%3, the
+// smaller one-sided difference of that axis's velocity along that axis (t1, t2).  The face
+// between cells c-1 and c then has dvn = vn(c) - vn(c-1) and
+// dvt = min(min(t1(c-1), t1(c)), min(t2(c-1), t2(c))), the reference's dvl, dvr, dwl, dwr.
+template <typename Real, int DIR>
+__device__ __forceinline__ void vel_cell(const DevMesh& m, const Real* __restrict__ w, int b,
+                                         int k, int j, int i, Real& vn, Real& t1, Real& t2) {
+  const Real* p = w + cidx(m, b, 0, NHYDRO, k, j, i);
+  const i64 vs = m.ncell;
+  constexpr int a1 = (DIR + 1) % 3, a2 = (DIR + 2) % 3;
+  const i64 s1 = a1 == 0 ? 1 : a1 == 1 ? (i64)m.nc1 : (i64)m.nc1 * m.nc2;
+  const i64 s2 = a2 == 0 ? 1 : a2 == 1 ? (i64)m.nc1 : (i64)m.nc1 * m.nc2;
+  vn = __ldg(p + (IVX + DIR) * vs);
+  const Real* q1 = p + (IVX + a1) * vs;
+  const Real c1 = __ldg(q1);
+  t1 = smin(__ldg(q1 + s1) - c1, c1 - __ldg(q1 - s1));
+  const Real* q2 = p + (IVX + a2) * vs;
+  const Real c2 = __ldg(q2);
+  t2 = smin(__ldg(q2 + s2) - c2, c2 - __ldg(q2 - s2));
+}
+
 // Riemann solve on one face of direction DIR: stores the two face EMFs and the CT weight
 // (calculate_fluxes.cpp:102/:221/:340; hlld.cpp:372-376) and returns the five hydro
 // fluxes in natural slots (IDN, IM1, IM2, IM3, IEN).
+// RS 7 (LHLLD) also takes the face's velocity differences dvn, dvt (vel_cell below).
 template <typename Real, int DIR, int RS>
 __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, const Real* wr,
                                            Real bx, Real dx, Real dt, i64 fo, Real* fn,
                                            Real* __restrict__ ey, Real* __restrict__ ez,
-                                           Real* __restrict__ wct) {
+                                           Real* __restrict__ wct, Real dvn = Real(0),
+                                           Real dvt = Real(0)) {
   // local order: d, v_normal, v_t1, v_t2, p, By, Bz (hlld.cpp:42-43)
   const int ivx = IVX + DIR, ivy = IVX + (DIR + 1) % 3, ivz = IVX + (DIR + 2) % 3;
   Real wli[NWAVE] = {wl[IDN], wl[ivx], wl[ivy], wl[ivz], wl[IPR], wl[IBY], wl[IBZ]};
@@ -337,6 +362,7 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   else if (RS == 1) hlle<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
   else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);
+  else if (RS == 7) hlld<Real, true>(gam, wli, wri, bx, f, dvn, dvt);  // low-dissipation
   else if (RS == 5) llf_sr<Real>(gam, wli, wri, bx, f);  // special relativity, LLF
   else if (RS == 6) hlld_sr<Real>(gam, wli, wri, bx, f);  // special relativity, HLLD
   else hlle_sr<Real>(gam, wli, wri, bx, f);  // RS 2: special relativity, HLLE
@@ -419,6 +445,17 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
   Real wl[NWAVE];
 #pragma unroll
   for (int n = 0; n < NWAVE; ++n) wl[n] = __shfl_up_sync(0xffffffffu, qlp[n], 1);
+  // LHLLD: the face's velocity differences from this cell and the one of lane L-1
+  Real dvn = Real(0), dvt = Real(0);
+  if (RS == 7) {
+    Real vn = Real(0), t1 = Real(0), t2 = Real(0);
+    if (valid) vel_cell<Real, 0>(m, w, b, k, j, m.is - 1 + c, vn, t1, t2);
+    const Real vnl = __shfl_up_sync(0xffffffffu, vn, 1);
+    const Real t1l = __shfl_up_sync(0xffffffffu, t1, 1);
+    const Real t2l = __shfl_up_sync(0xffffffffu, t2, 1);
+    dvn = vn - vnl;
+    dvt = smin(smin(t1l, t1), smin(t2l, t2));
+  }
   const int i = m.is - 1 + c;
   Real fn[NHYDRO] = {Real(0), Real(0), Real(0), Real(0), Real(0)};
   const bool has_face = valid && lane > 0 && c > 0;
@@ -426,7 +463,7 @@ flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ b
     const i64 fo = f1idx(m, b, k, j, i);
     solve_face<Real, 0, RS>(m, wl, qrm, to_real(__ldg(b1 + fo), Real()),
                             __ldg(rdx(m, 0, Real()) + (i64)b * m.nc1 + i), rdt(clk, Real()),
-                            fo, fn, e3, e2, wct);
+                            fo, fn, e3, e2, wct, dvn, dvt);
     if (m.ml.on && (i == m.is || i == m.ie + 1) && j >= m.js && j <= m.je && k >= m.ks &&
         k <= m.ke)
       ml_face_override<Real>(m, b, i == m.is ? 0 : 1, j - m.js, k - m.ks, m.nx2, fn);
@@ -638,6 +675,11 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
   Real* uout = (Real*)ua.uout;
   Real* ulo = (Real*)ua.ulo;
   const Real* uavg = (const Real*)ua.uavg;
+  // LHLLD: the velocity-difference parts of the cell below the next face (vel_cell)
+  Real vn_p = Real(0), t1_p = Real(0), t2_p = Real(0);
+  if (RS == 7 && active)
+    vel_cell<Real, DIR>(m, w, b, DIR == 1 ? k0 : c0 - 1, DIR == 1 ? c0 - 1 : j0, i, vn_p,
+                        t1_p, t2_p);
   for (int s = c0; s <= c1 + 1; ++s) {
     const int rel0 = s - R - cfirst;  // window = cells s-R..s+R
     const bool upd = s > c0 && interior;  // this step finishes cell s-1
@@ -699,8 +741,18 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     const i64 fo = (DIR == 1) ? f2idx(m, b, k0, s, i) : f3idx(m, b, s, j0, i);
     Real fn[NHYDRO];
     if (active) {
+      Real dvn = Real(0), dvt = Real(0);
+      if (RS == 7) {
+        Real vn, t1, t2;
+        vel_cell<Real, DIR>(m, w, b, DIR == 1 ? k0 : s, DIR == 1 ? s : j0, i, vn, t1, t2);
+        dvn = vn - vn_p;
+        dvt = smin(smin(t1_p, t1), smin(t2_p, t2));
+        vn_p = vn;
+        t1_p = t1;
+        t2_p = t2;
+      }
       solve_face<Real, DIR, RS>(m, wl, qrm, to_real(fbuf[(s & 1) * bd], Real()),
-                                __ldg(dxs + s), dt, fo, fn, ey, ez, wct);
+                                __ldg(dxs + s), dt, fo, fn, ey, ez, wct, dvn, dvt);
     } else {
 #pragma unroll
       for (int n = 0; n < NHYDRO; ++n) fn[n] = Real(0);

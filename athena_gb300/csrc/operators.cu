@@ -80,7 +80,16 @@ op_flux_kernel(DevMesh m, double dt, const double* __restrict__ w,
   const int c = DIR == 0 ? i : DIR == 1 ? j : k;
   const double dxw = (DIR == 0 ? m.dx1f : DIR == 1 ? m.dx2f : m.dx3f)[c];
   double fn[NHYDRO];
-  solve_face<double, DIR, RS>(m, wl, wr, bn[fo], dxw, dt, fo, fn, ey, ez, wct);
+  double dvn = 0.0, dvt = 0.0;
+  if (RS == 7) {  // LHLLD: the face's velocity differences (vel_cell)
+    double vnl, t1l, t2l, vnr, t1r, t2r;
+    vel_cell<double, DIR>(m, w, 0, k - (DIR == 2), j - (DIR == 1), i - (DIR == 0), vnl, t1l,
+                          t2l);
+    vel_cell<double, DIR>(m, w, 0, k, j, i, vnr, t1r, t2r);
+    dvn = vnr - vnl;
+    dvt = smin(smin(t1l, t1r), smin(t2l, t2r));
+  }
+  solve_face<double, DIR, RS>(m, wl, wr, bn[fo], dxw, dt, fo, fn, ey, ez, wct, dvn, dvt);
   const i64 nf = DIR == 0 ? m.nf1 : DIR == 1 ? m.nf2 : m.nf3;
 #pragma unroll
   for (int n = 0; n < NHYDRO; ++n) flx[n * nf + fo] = fn[n];
@@ -322,8 +331,9 @@ athgpu_status op_flux_scratch(athgpu_ctx* c) {
 int solver_index(const athgpu_ctx* c) {
   return c->desc.relativistic ? (c->desc.rsolver == ATHGPU_LLF    ? 5
                                  : c->desc.rsolver == ATHGPU_HLLD ? 6 : 2)
-         : c->desc.rsolver == ATHGPU_LLF ? 3
-         : c->desc.rsolver == ATHGPU_ROE ? 4 : c->desc.rsolver;
+         : c->desc.rsolver == ATHGPU_LLF   ? 3
+         : c->desc.rsolver == ATHGPU_ROE   ? 4
+         : c->desc.rsolver == ATHGPU_LHLLD ? 7 : c->desc.rsolver;
 }
 
 template <int ORDER, int RS>
@@ -353,6 +363,7 @@ void launch_op_fluxes_rs(athgpu_ctx* c, int rs, double dt, double* f1, double* f
   else if (rs == 3) launch_op_fluxes<ORDER, 3>(c, dt, f1, f2, f3);
   else if (rs == 5) launch_op_fluxes<ORDER, 5>(c, dt, f1, f2, f3);
   else if (rs == 6) launch_op_fluxes<ORDER, 6>(c, dt, f1, f2, f3);
+  else if (rs == 7) launch_op_fluxes<ORDER, 7>(c, dt, f1, f2, f3);
   else launch_op_fluxes<ORDER, 4>(c, dt, f1, f2, f3);
 }
 

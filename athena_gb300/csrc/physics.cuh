@@ -95,10 +95,14 @@ __device__ __forceinline__ Real weight_for_ct(Real dflx, Real rhol, Real rhor, R
 template <typename Real>
 struct Cons1D { Real d, mx, my, mz, e, by, bz; };
 
-// HLLD (Miyoshi & Kusano 2005), hydro/rsolvers/mhd/hlld.cpp:36-376
-template <typename Real>
+// HLLD (Miyoshi & Kusano 2005), hydro/rsolvers/mhd/hlld.cpp:36-376.  LD: the
+// low-dissipation HLLD of Minoshima et al. 2021, hydro/rsolvers/mhd/lhlld.cpp:33-380,
+// which scales the pressure jump in the middle speed by the shock detector th of the
+// face's velocity differences dvn, dvt (:157-163), takes the star total pressure with the
+// low-Mach factor phi (:184-188) and groups a few products as sdld = sdl*ul.d (:153-234).
+template <typename Real, bool LD = false>
 __device__ __forceinline__ void hlld(Real gamma, const Real* wli, const Real* wri, Real bxi,
-                                     Real* f) {
+                                     Real* f, Real dvn = RC(0.0), Real dvt = RC(0.0)) {
   const Real SMALL_NUMBER = RC(1.0e-4);
   Real igm1 = RC(1.0) / (gamma - RC(1.0));
   Cons1D<Real> ul, ur, ulst, uldst, urdst, urst, fl, fr;
@@ -149,7 +153,15 @@ __device__ __forceinline__ void hlld(Real gamma, const Real* wli, const Real* wr
 
   Real sdl = spd[0] - wli[IVX];
   Real sdr = spd[4] - wri[IVX];
-  spd[2] = (sdr * ur.mx - sdl * ul.mx + (ptl - ptr)) / (sdr * ur.d - sdl * ul.d);
+  const Real sdld = sdl * ul.d, sdrd = sdr * ur.d;
+  const Real cfmax = smax(cfl, cfr);
+  if (LD) {
+    const Real th1 = smin(RC(1.0), (cfmax - smin(dvn, RC(0.0))) / (cfmax - smin(dvt, RC(0.0))));
+    const Real th = th1 * th1 * th1 * th1;
+    spd[2] = (sdr * ur.mx - sdl * ul.mx + th * (ptl - ptr)) / (sdrd - sdld);
+  } else {
+    spd[2] = (sdr * ur.mx - sdl * ul.mx + (ptl - ptr)) / (sdr * ur.d - sdl * ul.d);
+  }
   Real sdml = spd[0] - spd[2];
   Real sdmr = spd[4] - spd[2];
   Real sdml_inv = RC(1.0) / sdml;
@@ -163,9 +175,21 @@ __device__ __forceinline__ void hlld(Real gamma, const Real* wli, const Real* wr
   spd[1] = spd[2] - dabs(bxi) / sqrtdl;
   spd[3] = spd[2] + dabs(bxi) / sqrtdr;
 
-  Real ptstl = ptl + ul.d * sdl * (spd[2] - wli[IVX]);
-  Real ptstr = ptr + ur.d * sdr * (spd[2] - wri[IVX]);
-  Real ptst = RC(0.5) * (ptstr + ptstl);
+  Real ptst;
+  if (LD) {
+    const Real clsq =
+        ((pbl + kel) + dsqrt((pbl + kel) * (pbl + kel) - RC(2.0) * kel * bxsq)) / ul.d;
+    const Real crsq =
+        ((pbr + ker) + dsqrt((pbr + ker) * (pbr + ker) - RC(2.0) * ker * bxsq)) / ur.d;
+    const Real chi = smin(RC(1.0), dsqrt(smax(clsq, crsq)) / cfmax);
+    const Real phi = chi * (RC(2.0) - chi);
+    ptst = (sdrd * ptl - sdld * ptr + phi * sdrd * sdld * (wri[IVX] - wli[IVX])) /
+           (sdrd - sdld);
+  } else {
+    Real ptstl = ptl + ul.d * sdl * (spd[2] - wli[IVX]);
+    Real ptstr = ptr + ur.d * sdr * (spd[2] - wri[IVX]);
+    ptst = RC(0.5) * (ptstr + ptstl);
+  }
 
   ulst.mx = ulst.d * spd[2];
   if (dabs(ul.d * sdl * sdml - bxsq) < (SMALL_NUMBER)*ptst) {
@@ -177,7 +201,7 @@ __device__ __forceinline__ void hlld(Real gamma, const Real* wli, const Real* wr
     Real tmp = bxi * (sdl - sdml) / (ul.d * sdl * sdml - bxsq);
     ulst.my = ulst.d * (wli[IVY] - ul.by * tmp);
     ulst.mz = ulst.d * (wli[IVZ] - ul.bz * tmp);
-    tmp = (ul.d * (sdl * sdl) - bxsq) / (ul.d * sdl * sdml - bxsq);
+    tmp = (LD ? sdld * sdl - bxsq : ul.d * (sdl * sdl) - bxsq) / (ul.d * sdl * sdml - bxsq);
     ulst.by = ul.by * tmp;
     ulst.bz = ul.bz * tmp;
   }
@@ -196,7 +220,7 @@ __device__ __forceinline__ void hlld(Real gamma, const Real* wli, const Real* wr
     Real tmp = bxi * (sdr - sdmr) / (ur.d * sdr * sdmr - bxsq);
     urst.my = urst.d * (wri[IVY] - ur.by * tmp);
     urst.mz = urst.d * (wri[IVZ] - ur.bz * tmp);
-    tmp = (ur.d * (sdr * sdr) - bxsq) / (ur.d * sdr * sdmr - bxsq);
+    tmp = (LD ? sdrd * sdr - bxsq : ur.d * (sdr * sdr) - bxsq) / (ur.d * sdr * sdmr - bxsq);
     urst.by = ur.by * tmp;
     urst.bz = ur.bz * tmp;
   }

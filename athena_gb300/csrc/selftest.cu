@@ -33,7 +33,9 @@ __global__ void conversion_check_kernel(long long n, const double* __restrict__ 
 template <int RS>
 __global__ void riemann_check_kernel(long long n, double gamma, const double* __restrict__ wl,
                                      const double* __restrict__ wr,
-                                     const double* __restrict__ bx, double* __restrict__ flux) {
+                                     const double* __restrict__ bx,
+                                     const double* __restrict__ dv,
+                                     double* __restrict__ flux) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
   double a[athgpu::NWAVE], b[athgpu::NWAVE], f[athgpu::NWAVE];
@@ -48,6 +50,9 @@ __global__ void riemann_check_kernel(long long n, double gamma, const double* __
   else if (RS == 3) athgpu::llf<double>(gamma, a, b, bx[q], f);
   else if (RS == 4) athgpu::roe<double>(gamma, a, b, bx[q], f);
   else if (RS == 5) athgpu::llf_sr<double>(gamma, a, b, bx[q], f);
+  else if (RS == 7)
+    athgpu::hlld<double, true>(gamma, a, b, bx[q], f, dv ? dv[2 * q] : 0.0,
+                               dv ? dv[2 * q + 1] : 0.0);
   else athgpu::hlld_sr<double>(gamma, a, b, bx[q], f);
 #pragma unroll
   for (int v = 0; v < athgpu::NWAVE; ++v) flux[q * athgpu::NWAVE + v] = f[v];
@@ -58,10 +63,12 @@ __global__ void riemann_check_kernel(long long n, double gamma, const double* __
 extern "C" athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, double gamma,
                                                  long long n, const double* wl,
                                                  const double* wr, const double* bx,
-                                                 double* flux, void* stream) {
+                                                 const double* dv, double* flux,
+                                                 void* stream) {
   if (n < 0 || (n > 0 && (!wl || !wr || !bx || !flux)) ||
-      rsolver < ATHGPU_HLLD || rsolver > ATHGPU_ROE ||
-      (relativistic && rsolver == ATHGPU_ROE) || !(gamma > 1.0)) {
+      rsolver < ATHGPU_HLLD || rsolver > ATHGPU_LHLLD ||
+      (relativistic && (rsolver == ATHGPU_ROE || rsolver == ATHGPU_LHLLD)) ||
+      !(gamma > 1.0)) {
     athgpu::set_last_error("selftest_riemann: bad arguments");
     return ATHGPU_ERR_ARG;
   }
@@ -70,19 +77,21 @@ extern "C" athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, 
   if (n > 0) {
     if (relativistic) {
       if (rsolver == ATHGPU_HLLD)
-        riemann_check_kernel<6><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+        riemann_check_kernel<6><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
       else if (rsolver == ATHGPU_LLF)
-        riemann_check_kernel<5><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+        riemann_check_kernel<5><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
       else
-        riemann_check_kernel<2><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+        riemann_check_kernel<2><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
     } else if (rsolver == ATHGPU_HLLD) {
-      riemann_check_kernel<0><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+      riemann_check_kernel<0><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
     } else if (rsolver == ATHGPU_HLLE) {
-      riemann_check_kernel<1><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+      riemann_check_kernel<1><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
     } else if (rsolver == ATHGPU_LLF) {
-      riemann_check_kernel<3><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+      riemann_check_kernel<3><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
+    } else if (rsolver == ATHGPU_LHLLD) {
+      riemann_check_kernel<7><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
     } else {
-      riemann_check_kernel<4><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, flux);
+      riemann_check_kernel<4><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
     }
   }
   cudaError_t e = cudaGetLastError();

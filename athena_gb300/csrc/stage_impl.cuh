@@ -267,11 +267,12 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   const Real* w = (const Real*)r.wbuf[r.wsel];
   const Real* bcc = (const Real*)r.bcc;
   // solver template index: 0 HLLD, 1 HLLE, 2 relativistic HLLE, 3 LLF, 4 Roe,
-  // 5 relativistic LLF, 6 relativistic HLLD
+  // 5 relativistic LLF, 6 relativistic HLLD, 7 low-dissipation HLLD
   const int rs = c->desc.relativistic ? (c->desc.rsolver == ATHGPU_LLF    ? 5
                                          : c->desc.rsolver == ATHGPU_HLLD ? 6 : 2)
-                 : c->desc.rsolver == ATHGPU_LLF ? 3
-                 : c->desc.rsolver == ATHGPU_ROE ? 4 : c->desc.rsolver;
+                 : c->desc.rsolver == ATHGPU_LLF   ? 3
+                 : c->desc.rsolver == ATHGPU_ROE   ? 4
+                 : c->desc.rsolver == ATHGPU_LHLLD ? 7 : c->desc.rsolver;
   Real* uout = (stage == 1) ? (Real*)r.ustar : (Real*)r.u;
   UpdateArgs ua;
   ua.beta = beta;
@@ -288,7 +289,7 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
   do {                                                                               \
     if (rs == 0) FLUX(O, 0); else if (rs == 1) FLUX(O, 1); else if (rs == 3) FLUX(O, 3); \
     else if (rs == 4) FLUX(O, 4); else if (rs == 5) FLUX(O, 5);                      \
-    else if (rs == 6) FLUX(O, 6); else FLUX(O, 2);                                   \
+    else if (rs == 6) FLUX(O, 6); else if (rs == 7) FLUX(O, 7); else FLUX(O, 2);      \
   } while (0)
   if (order == 1) FLUX_RS(1);
   else if (order == 2) FLUX_RS(2);

@@ -19,8 +19,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libathgpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300.h")
 
-HLLD, HLLE, LLF, ROE = 0, 1, 2, 3
-_RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF, "roe": ROE}
+HLLD, HLLE, LLF, ROE, LHLLD = 0, 1, 2, 3, 4
+_RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF, "roe": ROE, "lhlld": LHLLD}
 FP64, FP32 = 0, 1
 VL2, RK2 = 0, 1
 _INTEGRATORS = {"vl2": VL2, "rk2": RK2}

@@ -72,6 +72,7 @@ int SolverCode() {
   if (rs == "hlle") return ATHGPU_HLLE;
   if (rs == "llf") return ATHGPU_LLF;
   if (rs == "roe") return ATHGPU_ROE;
+  if (rs == "lhlld") return ATHGPU_LHLLD;
   throw std::runtime_error("### FATAL ERROR in athgpu shim: unsupported Riemann solver " + rs);
 }
 

@@ -38,6 +38,9 @@ typedef int athgpu_status;
 #define ATHGPU_LLF 2             /* --flux=llf   (hydro/rsolvers/mhd/llf_mhd.cpp; relativistic:
                                     llf_mhd_rel.cpp) */
 #define ATHGPU_ROE 3             /* --flux=roe   (hydro/rsolvers/mhd/roe_mhd.cpp) */
+#define ATHGPU_LHLLD 4           /* --flux=lhlld (hydro/rsolvers/mhd/lhlld.cpp, with
+                                    hydro/calculate_velocity_differences.cpp); uniform
+                                    meshes, Newtonian MHD */
 #define ATHGPU_FP64 0            /* every operation in FP64: bit-identical to the reference */
 #define ATHGPU_FP32 1            /* FP32 reconstruction/Riemann/divergence, compensated
                                     (Kahan) conserved update, FP64 CT and time step */
@@ -53,7 +56,8 @@ typedef struct {
   int nx1, nx2, nx3;      /* interior cells per MeshBlock (meshblock/nx1..3) */
   int nghost;             /* NGHOST: 2 for PLM, >= 3 for PPM (reconstruction.cpp:117-127) */
   int xorder;             /* time/xorder: 2 = PLM, 3 = PPM (stage 1 is donor cell) */
-  int rsolver;            /* ATHGPU_HLLD, ATHGPU_HLLE, ATHGPU_LLF or ATHGPU_ROE */
+  int rsolver;            /* ATHGPU_HLLD, ATHGPU_HLLE, ATHGPU_LLF, ATHGPU_ROE or
+                             ATHGPU_LHLLD */
   int precision;          /* ATHGPU_FP64 or ATHGPU_FP32 */
   int relativistic;       /* 1: special-relativistic MHD (-s): the HLLD, HLLE or LLF
                              solver (hlld_rel.cpp, hlle_mhd_rel.cpp, llf_mhd_rel.cpp),
@@ -542,13 +546,16 @@ athgpu_status athgpu_selftest_conversions(long long n, const double *d, const fl
  * transverse velocities (relativistic: spatial 4-velocity), gas pressure, two transverse
  * fields), bx[n] (normal field), flux[n][7] (device) receives each face's flux in the same
  * order (mass, three momenta, energy, then the two transverse-field fluxes, before the
- * EMF sign flip of the caller).  rsolver as in athgpu_mesh_desc; FP64.  Replaces no
+ * EMF sign flip of the caller).  dv[n][2] (device, may be NULL for zeros): each face's
+ * velocity differences (dvn, dvt) that ATHGPU_LHLLD reads (the other solvers ignore them).
+ * rsolver as in athgpu_mesh_desc; FP64.  Replaces no
  * reference interface: the solvers' own entry points are the per-pencil RiemannSolver
  * functions (hydro/rsolvers/mhd/*.cpp), which this applies one face at a time.
  * Asynchronous on `stream`. */
 athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, double gamma,
                                       long long n, const double *wl, const double *wr,
-                                      const double *bx, double *flux, void *stream);
+                                      const double *bx, const double *dv, double *flux,
+                                      void *stream);
 
 /* Conserved->primitive over whole MeshBlocks plus the first CFL time step, for callers
  * that cannot let a library allocate device memory: hosts whose device memory belongs

@@ -143,8 +143,13 @@ static double weight_for_ct(double dflx, double rhol, double rhor, double dx, do
 /* HLLD, hydro/rsolvers/mhd/hlld.cpp:36-376 (Miyoshi & Kusano 2005) */
 typedef struct { double d, mx, my, mz, e, by, bz; } cons1d;
 
-static void hlld(double gamma, const double *wli, const double *wri, double bxi,
-                 double *flxi) {
+/* ld = 0: HLLD.  ld = 1: the low-dissipation HLLD of Minoshima et al. 2021,
+ * hydro/rsolvers/mhd/lhlld.cpp:33-380, which differs in the middle speed (the pressure
+ * jump scaled by the shock detector th from the face's velocity differences dvn, dvt,
+ * :157-163), the star total pressure (the low-Mach factor phi, :184-188) and the grouping
+ * of a few products (sdld = sdl*ul.d, :153-154, :192-234). */
+static void hlld_core(double gamma, const double *wli, const double *wri, double bxi,
+                      int ld, double dvn, double dvt, double *flxi) {
   const double SMALL_NUMBER = 1.0e-4;
   double igm1 = 1.0 / (gamma - 1.0);
   cons1d ul, ur, ulst, uldst, urdst, urst, fl, fr;
@@ -200,7 +205,16 @@ static void hlld(double gamma, const double *wli, const double *wri, double bxi,
   /* middle and Alfven speeds, hlld.cpp:144-171 */
   double sdl = spd[0] - wli[IVX];
   double sdr = spd[4] - wri[IVX];
-  spd[2] = (sdr * ur.mx - sdl * ul.mx + (ptl - ptr)) / (sdr * ur.d - sdl * ul.d);
+  double sdld = sdl * ul.d, sdrd = sdr * ur.d;
+  double cfmax = smax(cfl, cfr);
+  if (ld) {
+    /* shock detector, lhlld.cpp:158-163 */
+    double th1 = smin(1.0, (cfmax - smin(dvn, 0.0)) / (cfmax - smin(dvt, 0.0)));
+    double th = th1 * th1 * th1 * th1;
+    spd[2] = (sdr * ur.mx - sdl * ul.mx + th * (ptl - ptr)) / (sdrd - sdld);
+  } else {
+    spd[2] = (sdr * ur.mx - sdl * ul.mx + (ptl - ptr)) / (sdr * ur.d - sdl * ul.d);
+  }
   double sdml = spd[0] - spd[2];
   double sdmr = spd[4] - spd[2];
   double sdml_inv = 1.0 / sdml;
@@ -215,9 +229,19 @@ static void hlld(double gamma, const double *wli, const double *wri, double bxi,
   spd[3] = spd[2] + fabs(bxi) / sqrtdr;
 
   /* intermediate states, hlld.cpp:173-300 */
-  double ptstl = ptl + ul.d * sdl * (spd[2] - wli[IVX]);
-  double ptstr = ptr + ur.d * sdr * (spd[2] - wri[IVX]);
-  double ptst = 0.5 * (ptstr + ptstl);
+  double ptst;
+  if (ld) {  /* lhlld.cpp:184-188 */
+    double clsq = ((pbl + kel) + sqrt(SQR(pbl + kel) - 2.0 * kel * bxsq)) / ul.d;
+    double crsq = ((pbr + ker) + sqrt(SQR(pbr + ker) - 2.0 * ker * bxsq)) / ur.d;
+    double chi = smin(1.0, sqrt(smax(clsq, crsq)) / cfmax);
+    double phi = chi * (2.0 - chi);
+    ptst = (sdrd * ptl - sdld * ptr + phi * sdrd * sdld * (wri[IVX] - wli[IVX])) /
+           (sdrd - sdld);
+  } else {
+    double ptstl = ptl + ul.d * sdl * (spd[2] - wli[IVX]);
+    double ptstr = ptr + ur.d * sdr * (spd[2] - wri[IVX]);
+    ptst = 0.5 * (ptstr + ptstl);
+  }
 
   ulst.mx = ulst.d * spd[2];
   if (fabs(ul.d * sdl * sdml - bxsq) < (SMALL_NUMBER)*ptst) {
@@ -229,7 +253,7 @@ static void hlld(double gamma, const double *wli, const double *wri, double bxi,
     double tmp = bxi * (sdl - sdml) / (ul.d * sdl * sdml - bxsq);
     ulst.my = ulst.d * (wli[IVY] - ul.by * tmp);
     ulst.mz = ulst.d * (wli[IVZ] - ul.bz * tmp);
-    tmp = (ul.d * SQR(sdl) - bxsq) / (ul.d * sdl * sdml - bxsq);
+    tmp = (ld ? sdld * sdl - bxsq : ul.d * SQR(sdl) - bxsq) / (ul.d * sdl * sdml - bxsq);
     ulst.by = ul.by * tmp;
     ulst.bz = ul.bz * tmp;
   }
@@ -248,7 +272,7 @@ static void hlld(double gamma, const double *wli, const double *wri, double bxi,
     double tmp = bxi * (sdr - sdmr) / (ur.d * sdr * sdmr - bxsq);
     urst.my = urst.d * (wri[IVY] - ur.by * tmp);
     urst.mz = urst.d * (wri[IVZ] - ur.bz * tmp);
-    tmp = (ur.d * SQR(sdr) - bxsq) / (ur.d * sdr * sdmr - bxsq);
+    tmp = (ld ? sdrd * sdr - bxsq : ur.d * SQR(sdr) - bxsq) / (ur.d * sdr * sdmr - bxsq);
     urst.by = ur.by * tmp;
     urst.bz = ur.bz * tmp;
   }
@@ -325,6 +349,11 @@ static void hlld(double gamma, const double *wli, const double *wri, double bxi,
   }
   flxi[0] = f.d; flxi[1] = f.mx; flxi[2] = f.my; flxi[3] = f.mz; flxi[4] = f.e;
   flxi[5] = f.by; flxi[6] = f.bz;
+}
+
+static void hlld(double gamma, const double *wli, const double *wri, double bxi,
+                 double *flxi) {
+  hlld_core(gamma, wli, wri, bxi, 0, 0.0, 0.0, flxi);
 }
 
 /* HLLE, hydro/rsolvers/mhd/hlle_mhd.cpp:25-182 */
@@ -1218,8 +1247,54 @@ static void recon_cell(const orc_mesh *m, int b, const double *w, const double *
   }
 }
 
+/* Hydro::CalculateVelocityDifferences, hydro/calculate_velocity_differences.cpp:20-64
+ * (3-D branch): at the face between cells c-1 and c along dir (c = (k, j, i)), dvn is the
+ * jump of the normal velocity and dvt the smallest one-sided transverse derivative of the
+ * transverse velocities in the two cells.  w: the block's primitives [5][nc3][nc2][nc1]. */
+static void vel_diffs(const orc_mesh *m, const double *w, int dir, int k, int j, int i,
+                      double *dvn, double *dvt) {
+  long vs = m->ncell, sj = m->nc1, sk = (long)m->nc1 * m->nc2;
+#define W(n, kk, jj, ii) w[(n) * vs + (kk) * sk + (jj) * sj + (ii)]
+  if (dir == 0) {
+    *dvn = W(IVX, k, j, i) - W(IVX, k, j, i - 1);
+    double dvl = smin(W(IVY, k, j + 1, i - 1) - W(IVY, k, j, i - 1),
+                      W(IVY, k, j, i - 1) - W(IVY, k, j - 1, i - 1));
+    double dvr = smin(W(IVY, k, j + 1, i) - W(IVY, k, j, i),
+                      W(IVY, k, j, i) - W(IVY, k, j - 1, i));
+    double dwl = smin(W(IVZ, k + 1, j, i - 1) - W(IVZ, k, j, i - 1),
+                      W(IVZ, k, j, i - 1) - W(IVZ, k - 1, j, i - 1));
+    double dwr = smin(W(IVZ, k + 1, j, i) - W(IVZ, k, j, i),
+                      W(IVZ, k, j, i) - W(IVZ, k - 1, j, i));
+    *dvt = smin(smin(dvl, dvr), smin(dwl, dwr));
+  } else if (dir == 1) {
+    *dvn = W(IVY, k, j, i) - W(IVY, k, j - 1, i);
+    double dvl = smin(W(IVZ, k + 1, j - 1, i) - W(IVZ, k, j - 1, i),
+                      W(IVZ, k, j - 1, i) - W(IVZ, k - 1, j - 1, i));
+    double dvr = smin(W(IVZ, k + 1, j, i) - W(IVZ, k, j, i),
+                      W(IVZ, k, j, i) - W(IVZ, k - 1, j, i));
+    double dwl = smin(W(IVX, k, j - 1, i + 1) - W(IVX, k, j - 1, i),
+                      W(IVX, k, j - 1, i) - W(IVX, k, j - 1, i - 1));
+    double dwr = smin(W(IVX, k, j, i + 1) - W(IVX, k, j, i),
+                      W(IVX, k, j, i) - W(IVX, k, j, i - 1));
+    *dvt = smin(smin(dvl, dvr), smin(dwl, dwr));
+  } else {
+    *dvn = W(IVZ, k, j, i) - W(IVZ, k - 1, j, i);
+    double dvl = smin(W(IVX, k - 1, j, i + 1) - W(IVX, k - 1, j, i),
+                      W(IVX, k - 1, j, i) - W(IVX, k - 1, j, i - 1));
+    double dvr = smin(W(IVX, k, j, i + 1) - W(IVX, k, j, i),
+                      W(IVX, k, j, i) - W(IVX, k, j, i - 1));
+    double dwl = smin(W(IVY, k - 1, j + 1, i) - W(IVY, k - 1, j, i),
+                      W(IVY, k - 1, j, i) - W(IVY, k - 1, j - 1, i));
+    double dwr = smin(W(IVY, k, j + 1, i) - W(IVY, k, j, i),
+                      W(IVY, k, j, i) - W(IVY, k, j - 1, i));
+    *dvt = smin(smin(dvl, dvr), smin(dwl, dwr));
+  }
+#undef W
+}
+
+/* dvn, dvt: the face's velocity differences (vel_diffs; read by LHLLD only) */
 static void riemann(const orc_mesh *m, int dir, const double *wl, const double *wr,
-                    double bx, double *flx7) {
+                    double bx, double dvn, double dvt, double *flx7) {
   /* local order: IDN, v_normal, v_t1, v_t2, p, IBY, IBZ; ivx = IVX+dir,
    * ivy = IVX+(dir+1)%3, ivz = IVX+(dir+2)%3 (hlld.cpp:42-43, 59-75) */
   int ivx = IVX + dir, ivy = IVX + (dir + 1) % 3, ivz = IVX + (dir + 2) % 3;
@@ -1231,6 +1306,7 @@ static void riemann(const orc_mesh *m, int dir, const double *wl, const double *
   else if (m->p.rsolver == 0) hlld(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 2) llf(m->p.gamma, wli, wri, bx, flx7);
   else if (m->p.rsolver == 3) roe(m->p.gamma, wli, wri, bx, flx7);
+  else if (m->p.rsolver == 4) hlld_core(m->p.gamma, wli, wri, bx, 1, dvn, dvt, flx7);
   else hlle(m->p.gamma, wli, wri, bx, flx7);
 }
 
@@ -1254,7 +1330,9 @@ static void calculate_fluxes(orc_mesh *m, int b, int order, scratch *s) {
         recon_cell(m, b, w, bcc, order, 0, k, j, i - 1, wl, tmp);
         recon_cell(m, b, w, bcc, order, 0, k, j, i, tmp, wr);
         long fi = F1IDX(m, k, j, i);
-        riemann(m, 0, wl, wr, b1[fi], f);
+        double dvn = 0.0, dvt = 0.0;
+        if (m->p.rsolver == 4) vel_diffs(m, w, 0, k, j, i, &dvn, &dvt);
+        riemann(m, 0, wl, wr, b1[fi], dvn, dvt, f);
         s->flx1[0 * n1 + fi] = f[0];
         s->flx1[1 * n1 + fi] = f[1];
         s->flx1[2 * n1 + fi] = f[2];
@@ -1271,7 +1349,9 @@ static void calculate_fluxes(orc_mesh *m, int b, int order, scratch *s) {
         recon_cell(m, b, w, bcc, order, 1, k, j - 1, i, wl, tmp);
         recon_cell(m, b, w, bcc, order, 1, k, j, i, tmp, wr);
         long fi = F2IDX(m, k, j, i);
-        riemann(m, 1, wl, wr, b2[fi], f);
+        double dvn = 0.0, dvt = 0.0;
+        if (m->p.rsolver == 4) vel_diffs(m, w, 1, k, j, i, &dvn, &dvt);
+        riemann(m, 1, wl, wr, b2[fi], dvn, dvt, f);
         /* flux slots: IDN, ivx=IVY, ivy=IVZ, ivz=IVX, IEN */
         s->flx2[0 * n2 + fi] = f[0];
         s->flx2[2 * n2 + fi] = f[1];
@@ -1289,7 +1369,9 @@ static void calculate_fluxes(orc_mesh *m, int b, int order, scratch *s) {
         recon_cell(m, b, w, bcc, order, 2, k - 1, j, i, wl, tmp);
         recon_cell(m, b, w, bcc, order, 2, k, j, i, tmp, wr);
         long fi = F3IDX(m, k, j, i);
-        riemann(m, 2, wl, wr, b3[fi], f);
+        double dvn = 0.0, dvt = 0.0;
+        if (m->p.rsolver == 4) vel_diffs(m, w, 2, k, j, i, &dvn, &dvt);
+        riemann(m, 2, wl, wr, b3[fi], dvn, dvt, f);
         /* flux slots: IDN, ivx=IVZ, ivy=IVX, ivz=IVY, IEN */
         s->flx3[0 * n3 + fi] = f[0];
         s->flx3[3 * n3 + fi] = f[1];
@@ -2531,13 +2613,14 @@ long orc_op_con2prim(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl,
 double orc_op_new_block_dt(orc_mesh *m, int b) { return new_block_dt(m, b); }
 
 void orc_riemann_face(int rsolver, int relativistic, double gamma, const double *wli,
-                      const double *wri, double bx, double *flx7) {
+                      const double *wri, double bx, double dvn, double dvt, double *flx7) {
   if (relativistic && rsolver == 2) llf_sr(gamma, wli, wri, bx, flx7);
   else if (relativistic && rsolver == 0) hlld_sr(gamma, wli, wri, bx, flx7);
   else if (relativistic) hlle_sr(gamma, wli, wri, bx, flx7);
   else if (rsolver == 0) hlld(gamma, wli, wri, bx, flx7);
   else if (rsolver == 2) llf(gamma, wli, wri, bx, flx7);
   else if (rsolver == 3) roe(gamma, wli, wri, bx, flx7);
+  else if (rsolver == 4) hlld_core(gamma, wli, wri, bx, 1, dvn, dvt, flx7);
   else hlle(gamma, wli, wri, bx, flx7);
 }
 

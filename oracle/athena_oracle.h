@@ -27,7 +27,7 @@ typedef struct {
   int nx1, nx2, nx3;      /* interior cells per MeshBlock */
   int ng;                 /* ghost layers (NGHOST) */
   int xorder;             /* 2 = PLM, 3 = PPM in the second VL2 stage */
-  int rsolver;            /* 0 = HLLD, 1 = HLLE, 2 = LLF, 3 = Roe */
+  int rsolver;            /* 0 = HLLD, 1 = HLLE, 2 = LLF, 3 = Roe, 4 = LHLLD */
   int relativistic;       /* 0 = Newtonian adiabatic MHD, 1 = special relativistic */
   double gamma, dfloor, pfloor, cfl_number, tlim;
   double sigma_max, beta_min, gamma_max; /* SR floors (adiabatic_mhd_sr.cpp:46-48) */
@@ -101,10 +101,11 @@ long orc_op_con2prim(orc_mesh *m, int b, int il, int iu, int jl, int ju, int kl,
 double orc_op_new_block_dt(orc_mesh *m, int b);
 
 /* One Riemann solve on a face, states in the solvers' local order (d, v_n, v_t1, v_t2, p,
- * B_t1, B_t2); rsolver 0 HLLD, 1 HLLE, 2 LLF, 3 Roe; relativistic selects the SR solvers
- * (hlld_rel.cpp, hlle_mhd_rel.cpp, llf_mhd_rel.cpp).  flx7 in the same local order. */
+ * B_t1, B_t2); rsolver 0 HLLD, 1 HLLE, 2 LLF, 3 Roe, 4 LHLLD (with the face's velocity
+ * differences dvn, dvt); relativistic selects the SR solvers (hlld_rel.cpp,
+ * hlle_mhd_rel.cpp, llf_mhd_rel.cpp).  flx7 in the same local order. */
 void orc_riemann_face(int rsolver, int relativistic, double gamma, const double *wli,
-                      const double *wri, double bx, double *flx7);
+                      const double *wri, double bx, double dvn, double dvt, double *flx7);
 /* the stages of one cycle and time += dt, without the new time step (adaptive runs
  * regrid in between); then orc_new_dt: NewBlockTimeStep + Mesh::NewTimeStep */
 void orc_advance(orc_mesh *m);

@@ -46,6 +46,8 @@ VARIANTS = {
     "mhd_hlld_g4": ("hlld", 4, False),   # PPM with mesh refinement (even NGHOST)
     "mhd_llf_g2": ("llf", 2, False),     # local Lax-Friedrichs (llf_mhd.cpp)
     "mhd_roe_g2": ("roe", 2, False),     # Roe linearisation (roe_mhd.cpp)
+    "mhd_lhlld_g2": ("lhlld", 2, False),  # low-dissipation HLLD (lhlld.cpp)
+    "mhd_lhlld_g3": ("lhlld", 3, False),
     "srmhd_hlle_g2": ("hlle", 2, True),
     "srmhd_llf_g2": ("llf", 2, True),    # relativistic LLF (llf_mhd_rel.cpp)
     "srmhd_hlld_g2": ("hlld", 2, True),  # relativistic HLLD (hlld_rel.cpp)

@@ -97,7 +97,7 @@ def lib():
         L.orc_op_new_block_dt.argtypes = [vp, ctypes.c_int]
         L.orc_op_new_block_dt.restype = ctypes.c_double
         L.orc_riemann_face.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, dp,
-                                       ctypes.c_double, dp]
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]
         _lib = L
     return _lib
 
@@ -127,7 +127,7 @@ class OracleMesh:
         nbl = (mesh.nblocks, 1, 1) if multilevel else mesh.nb
         # time/xorder: 1, 2, 3 or "3f" (PPM with the fast limiter, ppm_fast.cpp)
         xo, ppmf = (3, 1) if str(xorder) == "3f" else (int(xorder), 0)
-        rs = {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3}[rsolver]
+        rs = {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3, "lhlld": 4}[rsolver]
         self.p = Params(nbl[0], nbl[1], nbl[2], mesh.bx[0], mesh.bx[1],
                         mesh.bx[2], mesh.ng, xo, rs,
                         1 if relativistic else 0, gamma,
@@ -285,15 +285,17 @@ def sr_prim_to_cons(w, bcc, gamma):
     return u
 
 
-def riemann_faces(rsolver, wl, wr, bx, gamma, relativistic=False):
+def riemann_faces(rsolver, wl, wr, bx, gamma, relativistic=False, dv=None):
     """One Riemann solve per face: wl, wr [n, 7] primitive states in the solvers' local
-    order (d, v_n, v_t1, v_t2, p, B_t1, B_t2), bx [n] -> flux [n, 7] in the same order."""
-    rs = {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3}[rsolver]
+    order (d, v_n, v_t1, v_t2, p, B_t1, B_t2), bx [n], dv [n, 2] the faces' velocity
+    differences (dvn, dvt; LHLLD only) -> flux [n, 7] in the same order."""
+    rs = {"hlld": 0, "hlle": 1, "llf": 2, "roe": 3, "lhlld": 4}[rsolver]
     wl = np.ascontiguousarray(wl, dtype=np.float64)
     wr = np.ascontiguousarray(wr, dtype=np.float64)
     out = np.zeros((wl.shape[0], 7))
     L = lib()
+    dv = np.zeros((wl.shape[0], 2)) if dv is None else np.asarray(dv, dtype=np.float64)
     for q in range(wl.shape[0]):
         L.orc_riemann_face(rs, 1 if relativistic else 0, gamma, _p(wl[q]), _p(wr[q]),
-                           float(bx[q]), _p(out[q]))
+                           float(bx[q]), float(dv[q, 0]), float(dv[q, 1]), _p(out[q]))
     return out

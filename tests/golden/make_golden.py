@@ -67,6 +67,11 @@ CASES = {
                                           (.5, .5, .5)), "blast", 2, 0.3, 4),
     "turb_roe_plm_8blk": ("mhd_roe_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
                                          (1., 1., 1.)), "turbulence", 2, 0.3, 3),
+    # low-dissipation HLLD (--flux=lhlld, lhlld.cpp, with calculate_velocity_differences.cpp)
+    "blast_lhlld_plm_8blk": ("mhd_lhlld_g2", ((16, 16, 16), (2, 2, 2), 2, (-.5, -.5, -.5),
+                                              (.5, .5, .5)), "blast", 2, 0.3, 4),
+    "turb_lhlld_ppm_8blk": ("mhd_lhlld_g3", ((16, 16, 16), (2, 2, 2), 3, (0., 0., 0.),
+                                             (1., 1., 1.)), "turbulence", 3, 0.3, 3),
     # special-relativistic MHD (-s -b --flux=hlle): relativistic Kelvin-Helmholtz layer
     "srkh_hlle_plm_8blk": ("srmhd_hlle_g2", ((16, 16, 16), (2, 2, 2), 2, (0., 0., 0.),
                                             (1., 1., 1.)), "sr_kh", 2, 0.3, 3),

@@ -63,3 +63,13 @@ def faces(family, n, seed=0):
         wr = wl.copy()
         bx = rng.normal(0, .5, n)
     return wl, wr, bx
+
+
+def face_velocity_differences(wl, wr, seed=0):
+    """(dvn, dvt) per face for the low-dissipation HLLD: the normal-velocity jump of the
+    two states and a seeded transverse difference, both sides of zero (compression and
+    expansion; the shock detector saturates for dvt >= dvn)."""
+    rng = np.random.default_rng([seed, 99])
+    dvn = wr[:, 1] - wl[:, 1]
+    dvt = rng.normal(0.0, 0.5, wl.shape[0]) * (1.0 + np.abs(dvn))
+    return np.column_stack([dvn, dvt])

@@ -45,7 +45,7 @@ def _edges(mesh):
 CASES = [("hlld", 2, False, 2), ("hlld", 3, False, 3), ("hlle", 1, False, 2),
          ("roe", 2, False, 2), ("llf", 3, False, 3), ("hlld", "3f", False, 3),
          ("hlle", 2, True, 2), ("llf", 3, True, 3), ("hlld", 2, True, 2),
-         ("hlld", 3, True, 3)]
+         ("hlld", 3, True, 3), ("lhlld", 2, False, 2), ("lhlld", 3, False, 3)]
 
 
 @pytest.mark.parametrize("rsolver,order,sr,ng", CASES)

@@ -91,7 +91,9 @@ def _turb_case(nx=(32, 32, 32), nb=(2, 2, 2), ng=3, xorder=3, rsolver="hlld", se
                                                (2, "hlld", (1, 1, 1)),
                                                (3, "roe", (2, 1, 2)),
                                                (2, "llf", (1, 2, 1)),
-                                               ("3f", "hlld", (2, 2, 1))])
+                                               ("3f", "hlld", (2, 2, 1)),
+                                               (3, "lhlld", (2, 1, 2)),
+                                               (2, "lhlld", (1, 1, 1))])
 def test_fp64_matches_oracle_bitwise(xorder, rsolver, nb):
     mesh, ic, c = _turb_case(nb=nb, xorder=xorder, rsolver=rsolver,
                              ng=3 if xorder in (3, "3f") else 2)
@@ -122,7 +124,7 @@ def _div_b(mesh, b1, b2, b3):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("rsolver", ["hlld", "roe"])
+@pytest.mark.parametrize("rsolver", ["hlld", "roe", "lhlld"])
 def test_div_b_stays_at_roundoff(precision, rsolver):
     mesh, ic, c = _turb_case(rsolver=rsolver)
     (u, b1, b2, b3), _, _, _ = _run_gpu(mesh, c, ic, 5, precision=precision)
@@ -235,7 +237,8 @@ BC_SETS = [(1, 1, 1, 1, 1, 1), (2, 2, 2, 2, 2, 2), (2, 1, 0, 0, 1, 2), (0, 0, 2,
 
 @pytest.mark.parametrize("bc", BC_SETS)
 @pytest.mark.parametrize("xorder,rsolver,nb", [(3, "hlld", (2, 2, 2)),
-                                               (2, "hlle", (1, 2, 3))])
+                                               (2, "hlle", (1, 2, 3)),
+                                               (2, "lhlld", (2, 1, 1))])
 def test_physical_boundaries_match_oracle_bitwise(bc, xorder, rsolver, nb):
     """Outflow and reflecting mesh faces (ApplyPhysicalBoundaries, bvals.cpp:453-680) and
     the EMF averaging along them: every primitive, cell-centred field and face value,

@@ -10,12 +10,12 @@ import pytest
 import oracle as O
 from athena_gb300 import build
 from athena_gb300.runtime import _RSOLVERS, _check, load_library
-from riemann_faces import FAMILIES, faces
+from riemann_faces import FAMILIES, face_velocity_differences, faces
 
 pytestmark = pytest.mark.gpu
 
 SOLVERS = [("hlld", False), ("hlle", False), ("llf", False), ("roe", False),
-           ("hlld", True), ("hlle", True), ("llf", True)]
+           ("lhlld", False), ("hlld", True), ("hlle", True), ("llf", True)]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -24,20 +24,21 @@ def _built():
     O.build()
 
 
-def _gpu_faces(rsolver, sr, gamma, wl, wr, bx):
+def _gpu_faces(rsolver, sr, gamma, wl, wr, bx, dv):
     import torch
     L = load_library()
     f = L.athgpu_selftest_riemann
     f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_longlong] + \
-        [ctypes.c_void_p] * 5
+        [ctypes.c_void_p] * 6
     f.restype = ctypes.c_int
     dev = torch.device("cuda", 0)
     tl = torch.from_numpy(np.ascontiguousarray(wl)).to(dev)
     tr = torch.from_numpy(np.ascontiguousarray(wr)).to(dev)
     tb = torch.from_numpy(np.ascontiguousarray(bx)).to(dev)
+    td = torch.from_numpy(np.ascontiguousarray(dv)).to(dev)
     out = torch.full((wl.shape[0], 7), float("nan"), dtype=torch.float64, device=dev)
     _check(f(_RSOLVERS[rsolver], 1 if sr else 0, gamma, wl.shape[0], tl.data_ptr(),
-             tr.data_ptr(), tb.data_ptr(), out.data_ptr(),
+             tr.data_ptr(), tb.data_ptr(), td.data_ptr(), out.data_ptr(),
              torch.cuda.current_stream().cuda_stream), "athgpu_selftest_riemann")
     torch.cuda.synchronize()
     return out.cpu().numpy()
@@ -48,7 +49,8 @@ def test_riemann_faces_match_oracle_bitwise(rsolver, sr):
     gamma = 4.0 / 3.0 if sr else 5.0 / 3.0
     for fam in FAMILIES:
         wl, wr, bx = faces(fam, 1500, seed=11)
-        got = _gpu_faces(rsolver, sr, gamma, wl, wr, bx)
-        want = O.riemann_faces(rsolver, wl, wr, bx, gamma, sr)
+        dv = face_velocity_differences(wl, wr, seed=11)
+        got = _gpu_faces(rsolver, sr, gamma, wl, wr, bx, dv)
+        want = O.riemann_faces(rsolver, wl, wr, bx, gamma, sr, dv)
         same = (got == want) | (np.isnan(got) & np.isnan(want))
         assert same.all(), (fam, int((~same).sum()), np.argwhere(~same)[:3].tolist())

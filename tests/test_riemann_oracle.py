@@ -8,7 +8,7 @@ import oracle as O
 from riemann_faces import FAMILIES, faces
 
 SOLVERS = [("hlld", False), ("hlle", False), ("llf", False), ("roe", False),
-           ("hlld", True), ("hlle", True), ("llf", True)]
+           ("lhlld", False), ("hlld", True), ("hlle", True), ("llf", True)]
 
 
 @pytest.fixture(scope="module", autouse=True)
