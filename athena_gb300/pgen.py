@@ -394,6 +394,36 @@ def sr_prim_to_cons(w, bcc, gamma):
     return u
 
 
+def sr_shock_tube(nx, xmin, xmax, left, right, shock_pos=0.0):
+    """Relativistic MHD shock tube along x1 (pgen/gr_shock_tube.cpp:44-330, SR branch):
+    left/right = (rho, p, v^x, v^y, v^z, B^x, B^y, B^z) with 3-velocities, cell (k,j,i) on
+    the left where x1v(i) < shock_pos.  The face fields take the state of the cell of the
+    same index (x1v(i) decides face i too, :248-262, the last face that of the next ghost
+    cell).  Returns global primitives w[5, NX3, NX2, NX1] (4-velocity u^i = u^0 v^i) and
+    the face fields (f1, f2, f3)."""
+    n1, n2, n3 = nx
+    dx = (xmax[0] - xmin[0]) / n1
+    xf = xmin[0] + dx * np.arange(n1 + 2)
+    x1v = 0.5 * (xf[:-1] + xf[1:])            # cell centres of cells 0..n1 (n1: ghost)
+    side = x1v < shock_pos                    # True: left state
+
+    def state(q):
+        rho, p, vx, vy, vz, bx, by, bz = q
+        ut = np.sqrt(1.0 / (1.0 - (vx * vx + vy * vy + vz * vz)))
+        return rho, p, ut * vx, ut * vy, ut * vz, bx, by, bz
+
+    L, R = state(left), state(right)
+    cols = np.array([L if s else R for s in side])   # [n1+1, 8]
+    w = np.empty((5, n3, n2, n1))
+    for n in range(5):
+        src = {0: 0, 1: 2, 2: 3, 3: 4, 4: 1}[n]      # rho, u1, u2, u3, p
+        w[n] = cols[:n1, src][None, None, :]
+    f1 = np.broadcast_to(cols[:, 5][None, None, :], (n3, n2, n1 + 1)).copy()
+    f2 = np.broadcast_to(cols[:n1, 6][None, None, :], (n3, n2 + 1, n1)).copy()
+    f3 = np.broadcast_to(cols[:n1, 7][None, None, :], (n3 + 1, n2, n1)).copy()
+    return w, f1, f2, f3
+
+
 def sr_kelvin_helmholtz(nx, seed=20261204, gamma=4.0 / 3.0, vshear=0.5, width=0.01,
                         rho_in=1.0, rho_out=0.1, p0=1.0, sigma=0.1, noise=1.0e-3):
     """Relativistic Kelvin-Helmholtz shear layer on a periodic unit box: v_x = +vshear
