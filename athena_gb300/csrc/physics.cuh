@@ -63,10 +63,6 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // kernel is not bound by the FP64 pipe, F2F costs fewer issue slots than d2f_rn)
 __device__ __forceinline__ double to_real(double x, double) { return x; }
 __device__ __forceinline__ float to_real(double x, float) { return (float)x; }
-// the same on the integer pipe (d2f_rn, the hardware's bits), for a kernel whose FP64 pipe
-// the conversions would otherwise bound (W(U): six face values per cell)
-__device__ __forceinline__ double to_real_ip(double x, double) { return x; }
-__device__ __forceinline__ float to_real_ip(double x, float) { return d2f_rn(x); }
 
 // EquationOfState::FastMagnetosonicSpeed, eos/adiabatic_mhd.cpp:149-156
 template <typename Real>
