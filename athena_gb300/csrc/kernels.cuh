@@ -962,9 +962,7 @@ __device__ __forceinline__ int nbr_of(const DevMesh& m, int b, int o1, int o2, i
 
 // The corner EMF of edge (b,k,j,i) as CT uses it: the value itself, or on a block face /
 // edge the average over the blocks that share it (flux_correction_fc.cpp), formed in the
-// bulk precision; returned widened to FP64 (exactly; on the integer pipe for FP32).
-__device__ __forceinline__ double widen(double x) { return x; }
-__device__ __forceinline__ double widen(float x) { return f2d_exact(x); }
+// bulk precision.
 template <typename Real, int C>
 __device__ __forceinline__ Real edge_avg(const DevMesh& m, const Real* __restrict__ e,
                                          int b, int k, int j, int i) {
@@ -1016,24 +1014,19 @@ __device__ __forceinline__ Real edge_avg(const DevMesh& m, const Real* __restric
   return count == 2 ? sum * Real(0.5) : own;
 }
 
-template <typename Real, int C>
-__device__ __forceinline__ double edge_value(const DevMesh& m, const Real* __restrict__ e,
-                                             int b, int k, int j, int i) {
-  return widen(edge_avg<Real, C>(m, e, b, k, j, i));
-}
 // The same, reading an edge off the block's faces at in-block offset off from the block's
 // base eb (no neighbour logic, no 64-bit index arithmetic); ML = false: the stored value
 // everywhere (a same-level mesh's block-face edges hold their averages already)
 template <typename Real, int C, bool ML>
-__device__ __forceinline__ double edge_value_at(const DevMesh& m, const Real* __restrict__ e,
-                                                const Real* __restrict__ eb, int off, int b,
-                                                int k, int j, int i) {
-  if (!ML) return widen(__ldg(eb + off));
+__device__ __forceinline__ Real edge_at(const DevMesh& m, const Real* __restrict__ e,
+                                        const Real* __restrict__ eb, int off, int b, int k,
+                                        int j, int i) {
+  if (!ML) return __ldg(eb + off);
   const bool on_face = (C != 0 && (i == m.is || i == m.ie + 1)) ||
                        (C != 1 && (j == m.js || j == m.je + 1)) ||
                        (C != 2 && (k == m.ks || k == m.ke + 1));
-  if (!on_face) return widen(__ldg(eb + off));
-  return edge_value<Real, C>(m, e, b, k, j, i);
+  if (!on_face) return __ldg(eb + off);
+  return edge_avg<Real, C>(m, e, b, k, j, i);
 }
 
 // The average of the block-face edges over the blocks sharing them (edge_avg above) on a
@@ -1134,12 +1127,13 @@ edge_put_kernel(DevMesh m, const int4* __restrict__ plan, int n0, int n1, int n2
 // j<=je.  The three faces share the edges e1, e2, e3 at (k,j,i), so a thread reads nine
 // edge values for up to three faces.  Edge EMFs are read with the correction above.
 // FP64 path (Real = double): (wght/area)*(len*e(+) - len*e(-)) exactly as the reference.
-// FP32 path: the corner EMFs are FP32, widened exactly, and the update is
-// ((wght/area)*len)*(e(+) - e(-)) in FP64 (the difference of two floats is exact in FP64).
-// bin/bout may alias.
-// ML: a multi-level mesh, whose block-face edges take the corrected values
-// (edge_value_at).  On a same-level mesh the block-face edges already hold their averages
-// (edge_fix_kernel, edge_put_kernel), so the kernel reads plain edges.
+// FP32 path: the corner EMFs are FP32 and the update is ((wght/area)*len)*(e(+) - e(-)) in
+// FP64, the difference of the two floats formed on the integer pipe (fsub_f64: the FP64
+// subtraction's bits), which leaves two FP64 operations per face on GB300's narrow FP64
+// pipe instead of four.  bin/bout may alias.
+// ML: a multi-level mesh, whose block-face edges take the corrected values (edge_at).  On
+// a same-level mesh the block-face edges already hold their averages (edge_fix_kernel,
+// edge_put_kernel), so the kernel reads plain edges.
 template <typename Real, bool ML>
 __global__ void __launch_bounds__(256)
 ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
@@ -1179,8 +1173,8 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const bool f3 = i <= m.ie && j <= m.je;
   const double l1 = dx1f[m.is], l2 = dx2f[m.js], l3 = dx3f[m.ks];
   const bool exact = sizeof(Real) == 8;
-  auto term = [&](double qd, double len, double qlen, double ep, double em) -> double {
-    return exact ? qd * (len * ep - len * em) : qlen * (ep - em);
+  auto term = [&](double qd, double len, double qlen, Real ep, Real em) -> double {
+    return exact ? qd * (len * (double)ep - len * (double)em) : qlen * fsub_f64(ep, em);
   };
   // in-block offsets of the edges at (k,j,i) and the block bases of the edge arrays
   const int c1 = m.nc1, c2 = m.nc2;
@@ -1191,36 +1185,36 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const Real* E2 = e2 + (i64)b * m.ne2;
   const Real* E3 = e3 + (i64)b * m.ne3;
   // the shared edges, each read once (and only where a face of this thread uses it)
-  const double e1c = (f2 || f3) ? edge_value_at<Real, 0, ML>(m, e1, E1, oe1, b, k, j, i) : 0.0;
-  const double e2c = (f1 || f3) ? edge_value_at<Real, 1, ML>(m, e2, E2, oe2, b, k, j, i) : 0.0;
-  const double e3c = (f1 || f2) ? edge_value_at<Real, 2, ML>(m, e3, E3, oe3, b, k, j, i) : 0.0;
+  const Real e1c = (f2 || f3) ? edge_at<Real, 0, ML>(m, e1, E1, oe1, b, k, j, i) : Real(0);
+  const Real e2c = (f1 || f3) ? edge_at<Real, 1, ML>(m, e2, E2, oe2, b, k, j, i) : Real(0);
+  const Real e3c = (f1 || f2) ? edge_at<Real, 2, ML>(m, e3, E3, oe3, b, k, j, i) : Real(0);
   if (f1) {
     const i64 o = (i64)b * m.nf1 + (k * c2 + j) * (c1 + 1) + i;
     double v = b1in[o];
     if (b1avg) v = g1 * b1avg[o] + g2 * v;
     v -= term(q[0], l3, ql[0],
-              edge_value_at<Real, 2, ML>(m, e3, E3, oe3 + (c1 + 1), b, k, j + 1, i), e3c);
+              edge_at<Real, 2, ML>(m, e3, E3, oe3 + (c1 + 1), b, k, j + 1, i), e3c);
     v += term(q[0], l2, ql[1],
-              edge_value_at<Real, 1, ML>(m, e2, E2, oe2 + c2 * (c1 + 1), b, k + 1, j, i), e2c);
+              edge_at<Real, 1, ML>(m, e2, E2, oe2 + c2 * (c1 + 1), b, k + 1, j, i), e2c);
     b1out[o] = v;
   }
   if (f2) {
     const i64 o = (i64)b * m.nf2 + (k * (c2 + 1) + j) * c1 + i;
     double v = b2in[o];
     if (b2avg) v = g1 * b2avg[o] + g2 * v;
-    v += term(q[1], l3, ql[2], edge_value_at<Real, 2, ML>(m, e3, E3, oe3 + 1, b, k, j, i + 1),
+    v += term(q[1], l3, ql[2], edge_at<Real, 2, ML>(m, e3, E3, oe3 + 1, b, k, j, i + 1),
               e3c);
     v -= term(q[1], l1, ql[3],
-              edge_value_at<Real, 0, ML>(m, e1, E1, oe1 + (c2 + 1) * c1, b, k + 1, j, i), e1c);
+              edge_at<Real, 0, ML>(m, e1, E1, oe1 + (c2 + 1) * c1, b, k + 1, j, i), e1c);
     b2out[o] = v;
   }
   if (f3) {
     const i64 o = (i64)b * m.nf3 + (k * c2 + j) * c1 + i;
     double v = b3in[o];
     if (b3avg) v = g1 * b3avg[o] + g2 * v;
-    v -= term(q[2], l2, ql[4], edge_value_at<Real, 1, ML>(m, e2, E2, oe2 + 1, b, k, j, i + 1),
+    v -= term(q[2], l2, ql[4], edge_at<Real, 1, ML>(m, e2, E2, oe2 + 1, b, k, j, i + 1),
               e2c);
-    v += term(q[2], l1, ql[5], edge_value_at<Real, 0, ML>(m, e1, E1, oe1 + c1, b, k, j + 1, i),
+    v += term(q[2], l1, ql[5], edge_at<Real, 0, ML>(m, e1, E1, oe1 + c1, b, k, j + 1, i),
               e1c);
     b3out[o] = v;
   }

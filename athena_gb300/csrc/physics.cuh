@@ -59,6 +59,40 @@ __device__ __forceinline__ double f2d_exact(float f) {
   if ((b << 1) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // +-0
   return (double)f;
 }
+// The FP64 difference of two floats, (double)a - (double)b, on the integer pipe: when both
+// are normal and their exponents differ by at most 28, the exact difference has at most 53
+// significant bits (2^52 + 2^24 < 2^53), so it is an FP64 number; it is formed from the
+// two significands aligned in one 64-bit integer, normalised with a leading-zero count.
+// Other operands take the FP64 subtraction.  Same bits as the hardware in every case.
+__device__ __forceinline__ double fsub_f64(float a, float b) {
+  unsigned ua = __float_as_uint(a), ub = __float_as_uint(b) ^ 0x80000000u;  // a + (-b)
+  unsigned ea = (ua >> 23) & 0xffu, eb = (ub >> 23) & 0xffu;
+  if (ea < eb) {  // (ua, ea): the operand of the larger exponent
+    const unsigned tu = ua, te = ea;
+    ua = ub; ea = eb; ub = tu; eb = te;
+  }
+  const unsigned d = ea - eb;
+  if (eb - 1u < 254u && ea < 255u && d <= 28u) {
+    long long x = (long long)((ua & 0x7fffffu) | 0x800000u) << d;
+    const long long y = (long long)((ub & 0x7fffffu) | 0x800000u);
+    x = ((ua ^ ub) >> 31) ? x - y : x + y;
+    unsigned long long sign = ua >> 31;
+    if (x < 0) {
+      x = -x;
+      sign ^= 1ull;
+    }
+    if (x == 0) return 0.0;  // exact cancellation: +0 under round to nearest
+    const int nb = 64 - __clzll(x);  // significant bits, 1..53
+    // value = x * 2^(eb - 150): the aligned significand's leading bit lands in the exponent
+    // field as +1, hence nb + eb + 872 - 1
+    const unsigned long long bits = ((unsigned long long)x << (53 - nb)) +
+                                    ((unsigned long long)(nb + (int)eb + 871) << 52) +
+                                    (sign << 63);
+    return __longlong_as_double((long long)bits);
+  }
+  return f2d_exact(a) - f2d_exact(b);
+}
+__device__ __forceinline__ double fsub_f64(double a, double b) { return a - b; }
 // a face-field (always FP64) value in the bulk precision (hardware conversion: where the
 // kernel is not bound by the FP64 pipe, F2F costs fewer issue slots than d2f_rn)
 __device__ __forceinline__ double to_real(double x, double) { return x; }

@@ -24,8 +24,17 @@ __global__ void conversion_check_kernel(long long n, const double* __restrict__ 
   const float y = f[q];
   const bool bad64 = __double_as_longlong(athgpu::f2d_exact(y)) !=
                      __double_as_longlong((double)y);
+  // the difference of the pair (f[q], f[q ^ 1]) (a NaN result compares as NaN)
+  const long long p = q ^ 1;
+  bool badsub = false;
+  if (p < n) {
+    const float z = f[p];
+    const double hw = (double)y - (double)z, sw = athgpu::fsub_f64(y, z);
+    badsub = (hw != hw) ? (sw == sw) : __double_as_longlong(hw) != __double_as_longlong(sw);
+  }
   if (bad32) atomicAdd(mismatches, 1ull);
   if (bad64) atomicAdd(mismatches + 1, 1ull);
+  if (badsub) atomicAdd(mismatches + 2, 1ull);
 }
 
 // One Riemann solve per face in the solvers' local order (d, v_n, v_t1, v_t2, p, B_t1,
@@ -111,7 +120,7 @@ extern "C" athgpu_status athgpu_selftest_conversions(long long n, const double* 
     return ATHGPU_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(mismatches, 0, 2 * sizeof(unsigned long long), s);
+  cudaError_t e = cudaMemsetAsync(mismatches, 0, 3 * sizeof(unsigned long long), s);
   if (e == cudaSuccess && n > 0) {
     conversion_check_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, d, f, mismatches);
     e = cudaGetLastError();

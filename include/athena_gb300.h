@@ -533,11 +533,12 @@ athgpu_status athgpu_mlp_train(const float *features, const float *targets, long
                                float *params, int steps, int batch, float lr,
                                unsigned long long seed, float *loss_history, void *stream);
 
-/* Self-check of the FP64 <-> FP32 conversions the FP32 kernels do on the integer pipe
+/* Self-check of the FP64 <-> FP32 arithmetic the FP32 kernels do on the integer pipe
  * (GB300's FP64 pipe, which also runs the conversion instructions, is narrow): for device
  * arrays d[n], f[n], mismatches[0] (device) receives the number of d[q] whose integer-pipe
  * rounding to float differs bitwise from the hardware's, mismatches[1] the same for the
- * widening of f[q].  No counterpart in the reference. */
+ * widening of f[q], mismatches[2] the same for the FP64 difference of the pair
+ * (f[q], f[q ^ 1]) that the FP32 CT update forms.  No counterpart in the reference. */
 athgpu_status athgpu_selftest_conversions(long long n, const double *d, const float *f,
                                           unsigned long long *mismatches, void *stream);
 

@@ -1,5 +1,6 @@
-"""The integer-pipe FP64 <-> FP32 conversions of the FP32 kernels against the hardware
-conversions, bit for bit, on random values and the rounding edge cases."""
+"""The integer-pipe FP64 <-> FP32 conversions and the FP64 difference of two floats that
+the FP32 kernels form against the hardware's, bit for bit, on random values and the
+rounding edge cases."""
 import ctypes
 
 import numpy as np
@@ -47,6 +48,35 @@ def _floats(rng, n):
     return np.concatenate([bits.view(np.float32), special])
 
 
+def _float_pairs(rng, n):
+    """Consecutive pairs (f[2q], f[2q+1]) for the FP64 difference: random bits, close
+    values, every exponent gap up to beyond the integer path's 28, equal and opposite
+    values, zeros, subnormals, infinities and NaNs."""
+    n -= n % 2
+    a = rng.standard_normal(n // 2).astype(np.float32) * np.float32(2.0) ** rng.integers(
+        -100, 100, n // 2).astype(np.float32)
+    kind = np.arange(n // 2) % 6
+    gap = rng.integers(0, 36, n // 2)
+    b = np.where(kind == 0, rng.integers(0, 1 << 32, n // 2, dtype=np.uint64)
+                 .astype(np.uint32).view(np.float32),
+                 np.where(kind == 1, a * (1 + rng.standard_normal(n // 2).astype(np.float32)
+                                          * np.float32(1e-3)),
+                 np.where(kind == 2, rng.standard_normal(n // 2).astype(np.float32) * a
+                          * np.float32(2.0) ** -gap.astype(np.float32),
+                 np.where(kind == 3, a, np.where(kind == 4, -a,
+                          rng.standard_normal(n // 2).astype(np.float32) * a
+                          * np.float32(2.0) ** gap.astype(np.float32))))))
+    out = np.empty(n, np.float32)
+    out[0::2] = a
+    out[1::2] = b.astype(np.float32)
+    special = np.array([0.0, 1.0, -0.0, 1.0, 1.0, 0.0, 1e-40, 1.0, 1.0, -1e-45, np.inf, 1.0,
+                        1.0, np.nan, np.finfo(np.float32).max, -np.finfo(np.float32).max,
+                        np.finfo(np.float32).tiny, np.finfo(np.float32).tiny * 2,
+                        1.0, 1.0 + 2.0 ** -23, 2.0 ** 28, 1.0, 2.0 ** 29, 1.0],
+                       dtype=np.float32)
+    return np.concatenate([special, out])
+
+
 def test_integer_pipe_conversions_match_hardware():
     import torch
     L = load_library()
@@ -56,13 +86,14 @@ def test_integer_pipe_conversions_match_hardware():
     f.restype = ctypes.c_int
     rng = np.random.default_rng(12)
     d = _doubles(rng, 1 << 20)
-    fl = _floats(rng, d.size)[:d.size]
+    head = _floats(rng, d.size // 2)
+    fl = np.concatenate([head[:head.size - head.size % 2], _float_pairs(rng, d.size)])
     fl = np.resize(fl, d.size)
     dev = torch.device("cuda", 0)
     td = torch.from_numpy(d).to(dev)
     tf = torch.from_numpy(fl).to(dev)
-    mm = torch.zeros(2, dtype=torch.int64, device=dev)
+    mm = torch.zeros(3, dtype=torch.int64, device=dev)
     _check(f(d.size, td.data_ptr(), tf.data_ptr(), mm.data_ptr(),
              torch.cuda.current_stream().cuda_stream), "athgpu_selftest_conversions")
     torch.cuda.synchronize()
-    assert mm.cpu().tolist() == [0, 0]
+    assert mm.cpu().tolist() == [0, 0, 0]
