@@ -231,6 +231,52 @@ __device__ __forceinline__ void mbar_wait_bounded(unsigned long long* mbar, unsi
   }
 }
 
+// PPM of the seven wave components of one cell from its stencil window q[0..4][n] (cells
+// c-2 .. c+2 along the sweep).  lo[n]: the cell's limited lower interface, formed here
+// unless CARRY (then the caller's: the previous cell's upper one); up[n] receives the
+// limited upper interface (lo and up may alias).  FP32: the components (0,1), (2,3), (4,5)
+// as packed pairs (ppm_face2, ppm_finish2).
+template <typename Real, bool CARRY>
+__device__ __forceinline__ void ppm_waves(const Real (*q)[NWAVE], Real* lo, Real* up,
+                                          Real* qlp, Real* qrm, bool fast) {
+  if constexpr (sizeof(Real) == 4) {
+    if (!fast) {
+#pragma unroll
+      for (int n = 0; n + 1 < NWAVE; n += 2) {
+        float2 v[5];
+#pragma unroll
+        for (int t = 0; t < 5; ++t) v[t] = make_float2(q[t][n], q[t][n + 1]);
+        const float2 l = CARRY ? make_float2(lo[n], lo[n + 1])
+                               : ppm_face2(v[0], v[1], v[2], v[3]);
+        const float2 u = ppm_face2(v[1], v[2], v[3], v[4]);
+        float2 a, c;
+        ppm_finish2(v[0], v[1], v[2], v[3], v[4], l, u, a, c);
+        qlp[n] = a.x;
+        qlp[n + 1] = a.y;
+        qrm[n] = c.x;
+        qrm[n + 1] = c.y;
+        up[n] = u.x;
+        up[n + 1] = u.y;
+      }
+      if constexpr (NWAVE % 2 == 1) {
+        constexpr int n = NWAVE - 1;
+        const Real l = CARRY ? lo[n] : ppm_face<Real>(q[0][n], q[1][n], q[2][n], q[3][n]);
+        up[n] = ppm_face<Real>(q[1][n], q[2][n], q[3][n], q[4][n]);
+        ppm_finish<Real>(q[0][n], q[1][n], q[2][n], q[3][n], q[4][n], l, up[n], qlp[n],
+                         qrm[n], false);
+      }
+      return;
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < NWAVE; ++n) {
+    const Real l = CARRY ? lo[n] : ppm_face<Real>(q[0][n], q[1][n], q[2][n], q[3][n]);
+    up[n] = ppm_face<Real>(q[1][n], q[2][n], q[3][n], q[4][n]);
+    ppm_finish<Real>(q[0][n], q[1][n], q[2][n], q[3][n], q[4][n], l, up[n], qlp[n], qrm[n],
+                     fast);
+  }
+}
+
 // ---------------------------------------------------------------------------------------
 // Reconstruction of one cell along DIR: wave vector (natural order d, v1, v2, v3, p, then
 // the two transverse cell-centred field components, plm.cpp:45-57 / :196-208) of the
@@ -243,6 +289,7 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
   const i64 base_w = cidx(m, b, 0, NHYDRO, k, j, i);
   const i64 base_b = cidx(m, b, 0, 3, k, j, i);
   const i64 vs = m.ncell;  // variable stride within a block
+  Real q5[ORDER >= 3 ? 5 : 1][NWAVE];  // PPM: the stencil of every component
 #pragma unroll
   for (int n = 0; n < NWAVE; ++n) {
     const Real* src;
@@ -264,9 +311,13 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
       plm_one<Real>(__ldg(src + o - sw), __ldg(src + o), __ldg(src + o + sw), __ldg(pc + c),
                     __ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
     } else {
-      ppm_one<Real>(__ldg(src + o - 2 * sw), __ldg(src + o - sw), __ldg(src + o),
-                    __ldg(src + o + sw), __ldg(src + o + 2 * sw), qlp[n], qrm[n], ORDER == 4);
+#pragma unroll
+      for (int t = 0; t < 5; ++t) q5[t][n] = __ldg(src + o + (t - 2) * sw);
     }
+  }
+  if (ORDER >= 3) {
+    Real up[NWAVE];
+    ppm_waves<Real, false>(q5, nullptr, up, qlp, qrm, ORDER == 4);
   }
   if (ORDER == 3) {  // ApplyPrimitiveFloors, adiabatic_mhd.cpp:162-172 (ppm.cpp:326-331)
     const Real dfl = rdfloor(m, Real()), pfl = rpfloor(m, Real());
@@ -304,16 +355,18 @@ __device__ __forceinline__ void ppm_floors(const DevMesh& m, Real* qlp, Real* qr
 template <typename Real, int ORDER>
 __device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)[NWAVE],
                                              Real cp, Real cm, Real* qlp, Real* qrm) {
+  if constexpr (ORDER >= 3) {
+    Real up[NWAVE];
+    ppm_waves<Real, false>(win, nullptr, up, qlp, qrm, ORDER == 4);
+  } else {
 #pragma unroll
-  for (int n = 0; n < NWAVE; ++n) {
-    if (ORDER == 1) {
-      qlp[n] = win[0][n];
-      qrm[n] = win[0][n];
-    } else if (ORDER == 2) {
-      plm_one<Real>(win[0][n], win[1][n], win[2][n], cp, cm, qlp[n], qrm[n]);
-    } else {
-      ppm_one<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], qlp[n], qrm[n],
-                    ORDER == 4);
+    for (int n = 0; n < NWAVE; ++n) {
+      if (ORDER == 1) {
+        qlp[n] = win[0][n];
+        qrm[n] = win[0][n];
+      } else {
+        plm_one<Real>(win[0][n], win[1][n], win[2][n], cp, cm, qlp[n], qrm[n]);
+      }
     }
   }
   if (ORDER == 3) ppm_floors(m, qlp, qrm);
@@ -657,13 +710,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     Real win[WN][NWAVE];
     window(0, win);
     if constexpr (ORDER >= 3) {
-#pragma unroll
-      for (int n = 0; n < NWAVE; ++n) {
-        const Real lo = ppm_face<Real>(win[0][n], win[1][n], win[2][n], win[3][n]);
-        dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
-        ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo, dphc[n],
-                         wl[n], qrm[n], ORDER == 4);
-      }
+      ppm_waves<Real, false>(win, nullptr, dphc, wl, qrm, ORDER == 4);
       if (ORDER == 3) ppm_floors(m, wl, qrm);  // time/floor_ppm_fast is false
     } else {
       recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + c0 - 1) : Real(0),
@@ -725,13 +772,7 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
       Real win[WN][NWAVE];
       window(rel0, win);
       if constexpr (ORDER >= 3) {  // the lower interface is the previous cell's upper one
-#pragma unroll
-        for (int n = 0; n < NWAVE; ++n) {
-          const Real lo = dphc[n];
-          dphc[n] = ppm_face<Real>(win[1][n], win[2][n], win[3][n], win[4][n]);
-          ppm_finish<Real>(win[0][n], win[1][n], win[2][n], win[3][n], win[4][n], lo,
-                           dphc[n], qlp[n], qrm[n], ORDER == 4);
-        }
+        ppm_waves<Real, true>(win, dphc, dphc, qlp, qrm, ORDER == 4);
         if (ORDER == 3) ppm_floors(m, qlp, qrm);
       } else {
         recon_window<Real, ORDER>(m, win, ORDER == 2 ? __ldg(pc + s) : Real(0),

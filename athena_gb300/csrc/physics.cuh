@@ -805,6 +805,112 @@ __device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_
                    ppm_face<Real>(q_im1, qc, q_ip1, q_ip2), qlp, qrm, fast);
 }
 
+// FP32 PPM on two wave components at once.  The additions, multiplications and FMAs of
+// ppm_face / ppm_finish run as packed FP32x2 instructions (one instruction, two
+// independent IEEE operations rounded to nearest); the limiters' comparisons and
+// selections run per component.  The operations are those of the scalar functions with
+// the FMA contractions written out, so each component matches the scalar FP32 result up
+// to where the compiler's own contraction of the scalar code differs.
+__device__ __forceinline__ float2 pk(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // a + (-1)*b: one rounding
+  return __ffma2_rn(pk(-1.0f), b, a);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+
+// the Step 2a curvature limiter of one interface (ppm.cpp:150-158)
+__device__ __forceinline__ float ppm_face_d(float a, float b, float c) {
+  float d = 0.0f;
+  if (sgn(a) == sgn(b) && sgn(a) == sgn(c))
+    d = sgn(a) * smin(1.25f * dabs(b), smin(1.25f * dabs(c), dabs(a)));
+  return d;
+}
+
+__device__ __forceinline__ float2 ppm_face2(float2 q_im2, float2 q_im1, float2 qc,
+                                            float2 q_ip1) {
+  const float2 half = pk(0.5f), m2 = pk(-2.0f);
+  const float2 qa = sub2(qc, q_im1);
+  const float2 qb = sub2(q_ip1, qc);
+  const float2 dd_im1 = fma2(half, qa, mul2(half, sub2(q_im1, q_im2)));
+  const float2 dd = fma2(half, qb, mul2(half, qa));
+  const float2 s = add2(q_im1, qc);
+  float2 dph = add2(fma2(half, q_im1, mul2(half, qc)),
+                    fma2(pk(1.0f / 6.0f), dd_im1, mul2(pk(-1.0f / 6.0f), dd)));
+  const float2 d2qc_im1 = fma2(m2, q_im1, add2(q_im2, qc));
+  const float2 d2qc = fma2(m2, qc, add2(q_im1, q_ip1));
+  const float2 qq = mul2(sub2(dph, q_im1), sub2(qc, dph));
+  const float2 a = mul2(pk(3.0f), fma2(m2, dph, s));
+  const float2 d = make_float2(ppm_face_d(a.x, d2qc_im1.x, d2qc.x),
+                               ppm_face_d(a.y, d2qc_im1.y, d2qc.y));
+  const float2 dph_tmp = fma2(pk(-1.0f / 6.0f), d, mul2(half, s));
+  if (qq.x < 0.0f) dph.x = dph_tmp.x;
+  if (qq.y < 0.0f) dph.y = dph_tmp.y;
+  return dph;
+}
+
+// the Step 3 limiter of one component (ppm.cpp:236-315) from the packed parts below
+__device__ __forceinline__ float ppm_rho(float q_im2, float q_im1, float qc, float q_ip1,
+                                         float q_ip2, float d2qc_im1, float d2qc,
+                                         float d2qc_ip1, float d2qf) {
+  float e = 0.0f;
+  if (sgn(d2qc_im1) == sgn(d2qc) && sgn(d2qc_im1) == sgn(d2qc_ip1) &&
+      sgn(d2qc_im1) == sgn(d2qf))
+    e = sgn(d2qf) * smin(smin(1.25f * dabs(d2qc_im1), 1.25f * dabs(d2qc)),
+                         smin(1.25f * dabs(d2qc_ip1), dabs(d2qf)));
+  const float a = smax(dabs(q_im1), dabs(q_im2));
+  const float b = smax(smax(dabs(qc), dabs(q_ip1)), dabs(q_ip2));
+  float rho = 0.0f;
+  if (dabs(d2qf) > 1.0e-12f * smax(a, b)) rho = e / d2qf;
+  return rho;
+}
+__device__ __forceinline__ void ppm_pick(float qa_tmp, float qb_tmp, float rho,
+                                         float dqf_minus, float dqf_plus, float tmp_m,
+                                         float tmp_p, float tmp2_m, float tmp2_p,
+                                         float& qminus, float& qplus) {
+  if (qa_tmp <= 0.0f || qb_tmp <= 0.0f) {
+    if (rho <= (1.0f - 1.0e-12f)) {
+      qminus = tmp_m;
+      qplus = tmp_p;
+    }
+  } else {
+    if (dabs(dqf_minus) >= 2.0f * dabs(dqf_plus)) qminus = tmp2_m;
+    if (dabs(dqf_plus) >= 2.0f * dabs(dqf_minus)) qplus = tmp2_p;
+  }
+}
+
+__device__ __forceinline__ void ppm_finish2(float2 q_im2, float2 q_im1, float2 qc,
+                                            float2 q_ip1, float2 q_ip2, float2 dph,
+                                            float2 dph_ip1, float2& qlp, float2& qrm) {
+  const float2 m2 = pk(-2.0f), two = pk(2.0f);
+  const float2 d2qc_im1 = fma2(m2, q_im1, add2(q_im2, qc));
+  const float2 d2qc = fma2(m2, qc, add2(q_im1, q_ip1));
+  const float2 d2qc_ip1 = fma2(m2, q_ip1, add2(qc, q_ip2));
+  const float2 d2qf = mul2(pk(6.0f), fma2(m2, qc, add2(dph, dph_ip1)));
+  const float2 dqf_minus = sub2(qc, dph);
+  const float2 dqf_plus = sub2(dph_ip1, qc);
+  const float2 qa_tmp = mul2(dqf_minus, dqf_plus);
+  const float2 qb_tmp = mul2(sub2(q_ip1, qc), sub2(qc, q_im1));
+  const float2 rho =
+      make_float2(ppm_rho(q_im2.x, q_im1.x, qc.x, q_ip1.x, q_ip2.x, d2qc_im1.x, d2qc.x,
+                          d2qc_ip1.x, d2qf.x),
+                  ppm_rho(q_im2.y, q_im1.y, qc.y, q_ip1.y, q_ip2.y, d2qc_im1.y, d2qc.y,
+                          d2qc_ip1.y, d2qf.y));
+  const float2 tmp_m = fma2(make_float2(-rho.x, -rho.y), dqf_minus, qc);
+  const float2 tmp_p = fma2(rho, dqf_plus, qc);
+  const float2 tmp2_m = fma2(m2, dqf_plus, qc);
+  const float2 tmp2_p = fma2(two, dqf_minus, qc);
+  float2 qminus = dph, qplus = dph_ip1;
+  ppm_pick(qa_tmp.x, qb_tmp.x, rho.x, dqf_minus.x, dqf_plus.x, tmp_m.x, tmp_p.x, tmp2_m.x,
+           tmp2_p.x, qminus.x, qplus.x);
+  ppm_pick(qa_tmp.y, qb_tmp.y, rho.y, dqf_minus.y, dqf_plus.y, tmp_m.y, tmp_p.y, tmp2_m.y,
+           tmp2_p.y, qminus.y, qplus.y);
+  qlp = qplus;
+  qrm = qminus;
+}
+
 
 // ---------------------------------------------------------------------------------------
 // Special-relativistic MHD.  Primitive velocities are the spatial 4-velocity u^i.
