@@ -399,7 +399,9 @@ __device__ __forceinline__ void vel_cell(const DevMesh& m, const Real* __restric
 // (calculate_fluxes.cpp:102/:221/:340; hlld.cpp:372-376) and returns the five hydro
 // fluxes in natural slots (IDN, IM1, IM2, IM3, IEN).
 // RS 7 (LHLLD) also takes the face's velocity differences dvn, dvt (vel_cell below).
-template <typename Real, int DIR, int RS>
+// PK: FP32 HLLD on packed left/right pairs (hlld_pk); off where the caller's register
+// budget would spill with it (the donor-cell x3 sweep).
+template <typename Real, int DIR, int RS, bool PK = true>
 __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, const Real* wr,
                                            Real bx, Real dx, Real dt, i64 fo, Real* fn,
                                            Real* __restrict__ ey, Real* __restrict__ ez,
@@ -411,7 +413,8 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   Real wri[NWAVE] = {wr[IDN], wr[ivx], wr[ivy], wr[ivz], wr[IPR], wr[IBY], wr[IBZ]};
   Real f[NWAVE];
   const Real gam = rgamma(m, Real());
-  if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
+  if constexpr (RS == 0 && PK && sizeof(Real) == 4) hlld_pk(gam, wli, wri, bx, f);
+  else if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
   else if (RS == 1) hlle<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
   else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);
@@ -792,7 +795,8 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
         t1_p = t1;
         t2_p = t2;
       }
-      solve_face<Real, DIR, RS>(m, wl, qrm, to_real(fbuf[(s & 1) * bd], Real()),
+      solve_face<Real, DIR, RS, !(DIR == 2 && ORDER == 1)>(m, wl, qrm,
+                                                         to_real(fbuf[(s & 1) * bd], Real()),
                                 __ldg(dxs + s), dt, fo, fn, ey, ez, wct, dvn, dvt);
     } else {
 #pragma unroll

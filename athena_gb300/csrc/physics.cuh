@@ -119,11 +119,172 @@ __device__ __forceinline__ Real weight_for_ct(Real dflx, Real rhol, Real rhor, R
   return RC(0.5) + smax(RC(-0.5), tmp_min);
 }
 
+// Packed FP32x2 arithmetic (Blackwell FADD2 / FMUL2 / FFMA2): one instruction for two
+// independent float operations, each rounded to nearest as the scalar one.
+__device__ __forceinline__ float2 pk(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // a + (-1)*b: one rounding
+  return __ffma2_rn(pk(-1.0f), b, a);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+
 // Riemann solvers.  wl/wr: local order (d, v_normal, v_t1, v_t2, p, By, Bz)
 // (hlld.cpp:59-75).  f[0..4]: mass, normal, two transverse momentum and energy fluxes;
 // f[5] = F(By), f[6] = F(Bz).
 template <typename Real>
 struct Cons1D { Real d, mx, my, mz, e, by, bz; };
+
+// HLLD in FP32 with the left and right states as the two halves of packed FP32x2
+// operands (x = left, y = right): the conserved states, fast speeds, fluxes and
+// single-star states of both sides are formed by one instruction each; what mixes the
+// sides (wave speeds, the double-star state, the flux selection), the divisions and the
+// square roots run per side.  Same operations as hlld<float> below (hlld.cpp:36-376),
+// with the FMA contractions written out.
+__device__ __forceinline__ float2 lr(const float* wli, const float* wri, int n) {
+  return make_float2(wli[n], wri[n]);
+}
+__device__ __forceinline__ void hlld_pk(float gamma, const float* wli, const float* wri,
+                                        float bxi, float* f) {
+  const float SMALL_NUMBER = 1.0e-4f;
+  const float igm1 = 1.0f / (gamma - 1.0f);
+  const float2 d = lr(wli, wri, IDN), vx = lr(wli, wri, IVX), vy = lr(wli, wri, IVY),
+               vz = lr(wli, wri, IVZ), p = lr(wli, wri, IPR), by = lr(wli, wri, IBY),
+               bz = lr(wli, wri, IBZ);
+  const float bxsq = bxi * bxi;
+  const float2 ct2 = fma2(by, by, mul2(bz, bz));  // by^2 + bz^2
+  const float2 pb = mul2(pk(0.5f), add2(pk(bxsq), ct2));
+  const float2 ke = mul2(mul2(pk(0.5f), d), fma2(vx, vx, fma2(vy, vy, mul2(vz, vz))));
+  const float2 mx = mul2(vx, d), my = mul2(vy, d), mz = mul2(vz, d);
+  const float2 e = add2(fma2(p, pk(igm1), ke), pb);
+
+  // FastMagnetosonicSpeed of both sides (eos/adiabatic_mhd.cpp:149-156)
+  const float2 asq = mul2(pk(gamma), p);
+  const float2 vc = add2(pk(bxsq), ct2);
+  const float2 qsq = add2(vc, asq), tq = sub2(vc, asq);
+  const float2 rad = fma2(tq, tq, mul2(mul2(pk(4.0f), asq), ct2));
+  const float2 hq = mul2(pk(0.5f), add2(qsq, make_float2(sqrtf(rad.x), sqrtf(rad.y))));
+  const float2 cf = make_float2(sqrtf(hq.x / d.x), sqrtf(hq.y / d.y));
+  const float2 vm = sub2(vx, cf), vp = add2(vx, cf);
+  const float spd0 = smin(vm.x, vm.y), spd4 = smax(vp.x, vp.y);
+
+  const float2 pt = add2(p, pb);
+  const float2 nbx = pk(-bxi);
+  const float2 vb = fma2(vy, by, mul2(vz, bz));
+  const float2 fmx = sub2(fma2(mx, vx, pt), pk(bxsq));
+  const float2 fmy = fma2(nbx, by, mul2(my, vx));
+  const float2 fmz = fma2(nbx, bz, mul2(mz, vx));
+  const float2 fe = fma2(nbx, vb, mul2(vx, sub2(add2(e, pt), pk(bxsq))));
+  const float2 fby = fma2(nbx, vy, mul2(by, vx));
+  const float2 fbz = fma2(nbx, vz, mul2(bz, vx));
+
+  const float2 sd = sub2(make_float2(spd0, spd4), vx);  // sdl, sdr
+  const float2 sdd = mul2(sd, d);                        // ul.d*sdl, ur.d*sdr
+  const float2 sm = mul2(sd, mx);
+  const float spd2 = ((sm.y - sm.x) + (pt.x - pt.y)) / (sdd.y - sdd.x);
+  const float2 sdm = sub2(make_float2(spd0, spd4), pk(spd2));  // sdml, sdmr
+  const float2 sdm_inv = make_float2(1.0f / sdm.x, 1.0f / sdm.y);
+  const float2 sd_ = mul2(sdd, sdm_inv);  // ulst.d, urst.d
+  const float2 sd_inv = make_float2(1.0f / sd_.x, 1.0f / sd_.y);
+  const float sqrtdl = sqrtf(sd_.x), sqrtdr = sqrtf(sd_.y);
+  const float spd1 = spd2 - dabs(bxi) / sqrtdl;
+  const float spd3 = spd2 + dabs(bxi) / sqrtdr;
+  const float2 ptsts = fma2(sdd, sub2(pk(spd2), vx), pt);  // ptstl, ptstr
+  const float ptst = 0.5f * (ptsts.y + ptsts.x);
+
+  // single-star states of both sides (hlld.cpp:196-250)
+  const float2 smx = mul2(sd_, pk(spd2));
+  const float2 den = fma2(sdd, sdm, pk(-bxsq));  // ul.d*sdl*sdml - bxsq
+  const float2 xa = mul2(pk(bxi), sub2(sd, sdm));
+  const float2 xb = fma2(d, mul2(sd, sd), pk(-bxsq));
+  const float2 nta = make_float2(-(xa.x / den.x), -(xa.y / den.y));
+  const float2 tb = make_float2(xb.x / den.x, xb.y / den.y);
+  float2 smy = mul2(sd_, fma2(by, nta, vy));
+  float2 smz = mul2(sd_, fma2(bz, nta, vz));
+  float2 sby = mul2(by, tb), sbz = mul2(bz, tb);
+  const float2 smy0 = mul2(sd_, vy), smz0 = mul2(sd_, vz);
+  if (dabs(den.x) < SMALL_NUMBER * ptst) {
+    smy.x = smy0.x;
+    smz.x = smz0.x;
+    sby.x = by.x;
+    sbz.x = bz.x;
+  }
+  if (dabs(den.y) < SMALL_NUMBER * ptst) {
+    smy.y = smy0.y;
+    smz.y = smz0.y;
+    sby.y = by.y;
+    sbz.y = bz.y;
+  }
+  const float2 vbst =
+      mul2(fma2(smx, pk(bxi), fma2(smy, sby, mul2(smz, sbz))), sd_inv);
+  const float2 t1 = add2(sub2(mul2(sd, e), mul2(pt, vx)), pk(ptst * spd2));
+  const float2 t2 = sub2(fma2(vx, pk(bxi), vb), vbst);
+  const float2 se = mul2(fma2(pk(bxi), t2, t1), sdm_inv);
+
+  // double-star states (hlld.cpp:254-300)
+  const float invsumd = 1.0f / (sqrtdl + sqrtdr);
+  const float bxsig = (bxi > 0.0f ? 1.0f : -1.0f);
+  const float2 vyst = mul2(smy, sd_inv), vzst = mul2(smz, sd_inv);
+  float tmp = invsumd * (sqrtdl * vyst.x + sqrtdr * vyst.y + bxsig * (sby.y - sby.x));
+  const float2 ddmy = mul2(sd_, pk(tmp));
+  tmp = invsumd * (sqrtdl * vzst.x + sqrtdr * vzst.y + bxsig * (sbz.y - sbz.x));
+  const float2 ddmz = mul2(sd_, pk(tmp));
+  const float ddby = invsumd * (sqrtdl * sby.y + sqrtdr * sby.x +
+                                bxsig * sqrtdl * sqrtdr * (vyst.y - vyst.x));
+  const float ddbz = invsumd * (sqrtdl * sbz.y + sqrtdr * sbz.x +
+                                bxsig * sqrtdl * sqrtdr * (vzst.y - vzst.x));
+  tmp = spd2 * bxi + (ddmy.x * ddby + ddmz.x * ddbz) / sd_.x;
+  const float ddel = se.x - sqrtdl * bxsig * (vbst.x - tmp);
+  const float dder = se.y + sqrtdr * bxsig * (vbst.y - tmp);
+
+  // the upwind flux (hlld.cpp:302-370), components paired as (d, mx), (my, mz), (e, by), bz
+  const bool left = spd2 >= 0.0f;  // the side of the contact (used past the outer waves)
+  auto pick = [&](float2 v) { return left ? v.x : v.y; };
+  float u[7] = {pick(d), pick(mx), pick(my), pick(mz), pick(e), pick(by), pick(bz)};
+  float fs[7] = {pick(mx), pick(fmx), pick(fmy), pick(fmz), pick(fe), pick(fby), pick(fbz)};
+  if (spd0 >= 0.0f || spd4 <= 0.0f) {
+    const bool l = spd0 >= 0.0f;
+    f[0] = l ? mx.x : mx.y;
+    f[1] = l ? fmx.x : fmx.y;
+    f[2] = l ? fmy.x : fmy.y;
+    f[3] = l ? fmz.x : fmz.y;
+    f[4] = l ? fe.x : fe.y;
+    f[5] = l ? fby.x : fby.y;
+    f[6] = l ? fbz.x : fbz.y;
+    return;
+  }
+  const float so = left ? spd0 : spd4;  // the outer wave
+  const float st[7] = {pick(sd_), pick(smx), pick(smy), pick(smz), pick(se), pick(sby),
+                       pick(sbz)};
+  const float2 s2 = pk(so);
+  float2 a = fma2(s2, sub2(make_float2(st[0], st[1]), make_float2(u[0], u[1])),
+                  make_float2(fs[0], fs[1]));
+  float2 b = fma2(s2, sub2(make_float2(st[2], st[3]), make_float2(u[2], u[3])),
+                  make_float2(fs[2], fs[3]));
+  float2 c = fma2(s2, sub2(make_float2(st[4], st[5]), make_float2(u[4], u[5])),
+                  make_float2(fs[4], fs[5]));
+  float g = fs[6] + so * (st[6] - u[6]);
+  const bool inner = left ? !(spd1 >= 0.0f) : !(spd3 <= 0.0f);  // past the Alfven wave
+  if (inner) {
+    const float si = left ? spd1 : spd3;
+    const float dd[7] = {st[0], st[1], left ? ddmy.x : ddmy.y, left ? ddmz.x : ddmz.y,
+                         left ? ddel : dder, ddby, ddbz};
+    const float2 s1 = pk(si);
+    a = fma2(s1, sub2(make_float2(dd[0], dd[1]), make_float2(st[0], st[1])), a);
+    b = fma2(s1, sub2(make_float2(dd[2], dd[3]), make_float2(st[2], st[3])), b);
+    c = fma2(s1, sub2(make_float2(dd[4], dd[5]), make_float2(st[4], st[5])), c);
+    g = g + si * (dd[6] - st[6]);
+  }
+  f[0] = a.x;
+  f[1] = a.y;
+  f[2] = b.x;
+  f[3] = b.y;
+  f[4] = c.x;
+  f[5] = c.y;
+  f[6] = g;
+}
 
 // HLLD (Miyoshi & Kusano 2005), hydro/rsolvers/mhd/hlld.cpp:36-376.  LD: the
 // low-dissipation HLLD of Minoshima et al. 2021, hydro/rsolvers/mhd/lhlld.cpp:33-380,
@@ -811,16 +972,6 @@ __device__ __forceinline__ void ppm_one(Real q_im2, Real q_im1, Real qc, Real q_
 // selections run per component.  The operations are those of the scalar functions with
 // the FMA contractions written out, so each component matches the scalar FP32 result up
 // to where the compiler's own contraction of the scalar code differs.
-__device__ __forceinline__ float2 pk(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // a + (-1)*b: one rounding
-  return __ffma2_rn(pk(-1.0f), b, a);
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-  return __ffma2_rn(a, b, c);
-}
-
 // the Step 2a curvature limiter of one interface (ppm.cpp:150-158)
 __device__ __forceinline__ float ppm_face_d(float a, float b, float c) {
   float d = 0.0f;

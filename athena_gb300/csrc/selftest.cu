@@ -38,33 +38,77 @@ __global__ void conversion_check_kernel(long long n, const double* __restrict__ 
 }
 
 // One Riemann solve per face in the solvers' local order (d, v_n, v_t1, v_t2, p, B_t1,
-// B_t2), FP64: wl/wr [n][7], bx [n], flux [n][7].
-template <int RS>
-__global__ void riemann_check_kernel(long long n, double gamma, const double* __restrict__ wl,
-                                     const double* __restrict__ wr,
-                                     const double* __restrict__ bx,
-                                     const double* __restrict__ dv,
-                                     double* __restrict__ flux) {
+// B_t2): wl/wr [n][7], bx [n], flux [n][7], in Real.  FP32 HLLD is the packed solver the
+// FP32 sweeps run (hlld_pk).
+template <typename Real, int RS>
+__global__ void riemann_check_kernel(long long n, Real gamma, const Real* __restrict__ wl,
+                                     const Real* __restrict__ wr,
+                                     const Real* __restrict__ bx,
+                                     const Real* __restrict__ dv,
+                                     Real* __restrict__ flux) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  double a[athgpu::NWAVE], b[athgpu::NWAVE], f[athgpu::NWAVE];
+  Real a[athgpu::NWAVE], b[athgpu::NWAVE], f[athgpu::NWAVE];
 #pragma unroll
   for (int v = 0; v < athgpu::NWAVE; ++v) {
     a[v] = wl[q * athgpu::NWAVE + v];
     b[v] = wr[q * athgpu::NWAVE + v];
   }
-  if (RS == 0) athgpu::hlld<double>(gamma, a, b, bx[q], f);
-  else if (RS == 1) athgpu::hlle<double>(gamma, a, b, bx[q], f);
-  else if (RS == 2) athgpu::hlle_sr<double>(gamma, a, b, bx[q], f);
-  else if (RS == 3) athgpu::llf<double>(gamma, a, b, bx[q], f);
-  else if (RS == 4) athgpu::roe<double>(gamma, a, b, bx[q], f);
-  else if (RS == 5) athgpu::llf_sr<double>(gamma, a, b, bx[q], f);
+  if constexpr (RS == 0 && sizeof(Real) == 4) athgpu::hlld_pk(gamma, a, b, bx[q], f);
+  else if (RS == 0) athgpu::hlld<Real>(gamma, a, b, bx[q], f);
+  else if (RS == 1) athgpu::hlle<Real>(gamma, a, b, bx[q], f);
+  else if (RS == 2) athgpu::hlle_sr<Real>(gamma, a, b, bx[q], f);
+  else if (RS == 3) athgpu::llf<Real>(gamma, a, b, bx[q], f);
+  else if (RS == 4) athgpu::roe<Real>(gamma, a, b, bx[q], f);
+  else if (RS == 5) athgpu::llf_sr<Real>(gamma, a, b, bx[q], f);
   else if (RS == 7)
-    athgpu::hlld<double, true>(gamma, a, b, bx[q], f, dv ? dv[2 * q] : 0.0,
-                               dv ? dv[2 * q + 1] : 0.0);
-  else athgpu::hlld_sr<double>(gamma, a, b, bx[q], f);
+    athgpu::hlld<Real, true>(gamma, a, b, bx[q], f, dv ? dv[2 * q] : Real(0),
+                             dv ? dv[2 * q + 1] : Real(0));
+  else athgpu::hlld_sr<Real>(gamma, a, b, bx[q], f);
 #pragma unroll
   for (int v = 0; v < athgpu::NWAVE; ++v) flux[q * athgpu::NWAVE + v] = f[v];
+}
+
+template <typename Real>
+athgpu_status selftest_riemann(const char* name, int rsolver, int relativistic, double gamma,
+                               long long n, const Real* wl, const Real* wr, const Real* bx,
+                               const Real* dv, Real* flux, void* stream) {
+  if (n < 0 || (n > 0 && (!wl || !wr || !bx || !flux)) ||
+      rsolver < ATHGPU_HLLD || rsolver > ATHGPU_LHLLD ||
+      (relativistic && (rsolver == ATHGPU_ROE || rsolver == ATHGPU_LHLLD)) ||
+      !(gamma > 1.0)) {
+    athgpu::set_last_error(std::string(name) + ": bad arguments");
+    return ATHGPU_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  const Real g = (Real)gamma;
+  if (n > 0) {
+    if (relativistic) {
+      if (rsolver == ATHGPU_HLLD)
+        riemann_check_kernel<Real, 6><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+      else if (rsolver == ATHGPU_LLF)
+        riemann_check_kernel<Real, 5><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+      else
+        riemann_check_kernel<Real, 2><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+    } else if (rsolver == ATHGPU_HLLD) {
+      riemann_check_kernel<Real, 0><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+    } else if (rsolver == ATHGPU_HLLE) {
+      riemann_check_kernel<Real, 1><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+    } else if (rsolver == ATHGPU_LLF) {
+      riemann_check_kernel<Real, 3><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+    } else if (rsolver == ATHGPU_LHLLD) {
+      riemann_check_kernel<Real, 7><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+    } else {
+      riemann_check_kernel<Real, 4><<<grid, 128, 0, s>>>(n, g, wl, wr, bx, dv, flux);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    athgpu::set_last_error(std::string(name) + ": " + cudaGetErrorString(e));
+    return ATHGPU_ERR_CUDA;
+  }
+  return ATHGPU_OK;
 }
 
 }  // namespace
@@ -74,41 +118,17 @@ extern "C" athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, 
                                                  const double* wr, const double* bx,
                                                  const double* dv, double* flux,
                                                  void* stream) {
-  if (n < 0 || (n > 0 && (!wl || !wr || !bx || !flux)) ||
-      rsolver < ATHGPU_HLLD || rsolver > ATHGPU_LHLLD ||
-      (relativistic && (rsolver == ATHGPU_ROE || rsolver == ATHGPU_LHLLD)) ||
-      !(gamma > 1.0)) {
-    athgpu::set_last_error("selftest_riemann: bad arguments");
-    return ATHGPU_ERR_ARG;
-  }
-  cudaStream_t s = (cudaStream_t)stream;
-  const unsigned grid = (unsigned)((n + 127) / 128);
-  if (n > 0) {
-    if (relativistic) {
-      if (rsolver == ATHGPU_HLLD)
-        riemann_check_kernel<6><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-      else if (rsolver == ATHGPU_LLF)
-        riemann_check_kernel<5><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-      else
-        riemann_check_kernel<2><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-    } else if (rsolver == ATHGPU_HLLD) {
-      riemann_check_kernel<0><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-    } else if (rsolver == ATHGPU_HLLE) {
-      riemann_check_kernel<1><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-    } else if (rsolver == ATHGPU_LLF) {
-      riemann_check_kernel<3><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-    } else if (rsolver == ATHGPU_LHLLD) {
-      riemann_check_kernel<7><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-    } else {
-      riemann_check_kernel<4><<<grid, 128, 0, s>>>(n, gamma, wl, wr, bx, dv, flux);
-    }
-  }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    athgpu::set_last_error(std::string("selftest_riemann: ") + cudaGetErrorString(e));
-    return ATHGPU_ERR_CUDA;
-  }
-  return ATHGPU_OK;
+  return selftest_riemann<double>("selftest_riemann", rsolver, relativistic, gamma, n, wl, wr,
+                                  bx, dv, flux, stream);
+}
+
+extern "C" athgpu_status athgpu_selftest_riemann_fp32(int rsolver, int relativistic,
+                                                      double gamma, long long n,
+                                                      const float* wl, const float* wr,
+                                                      const float* bx, const float* dv,
+                                                      float* flux, void* stream) {
+  return selftest_riemann<float>("selftest_riemann_fp32", rsolver, relativistic, gamma, n, wl,
+                                 wr, bx, dv, flux, stream);
 }
 
 extern "C" athgpu_status athgpu_selftest_conversions(long long n, const double* d,

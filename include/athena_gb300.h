@@ -558,6 +558,13 @@ athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, double gamm
                                       const double *bx, const double *dv, double *flux,
                                       void *stream);
 
+/* The same in FP32 (float arrays, same layout), with the solvers the FP32 sweeps run
+ * (HLLD: the packed left/right form).  Replaces no reference interface. */
+athgpu_status athgpu_selftest_riemann_fp32(int rsolver, int relativistic, double gamma,
+                                           long long n, const float *wl, const float *wr,
+                                           const float *bx, const float *dv, float *flux,
+                                           void *stream);
+
 /* Conserved->primitive over whole MeshBlocks plus the first CFL time step, for callers
  * that cannot let a library allocate device memory: hosts whose device memory belongs
  * to their own pool allocator, real-time loops that forbid allocation latency, plugins
