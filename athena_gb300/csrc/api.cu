@@ -351,6 +351,96 @@ athgpu_status download_bulk(athgpu_ctx* c, double* h, const void* dev, const voi
   }
   return ATHGPU_OK;
 }
+
+// ATHGPU_COPY_INTERIOR: the (j, k) range of a block's own cells (or faces) with whole x1
+// rows, i.e. per volume (one variable of one MeshBlock) a run of nr rows from row r0 in
+// each of np planes from plane p0; as 3-D copies of about COPY_CHUNK bytes each (x =
+// the rows' bytes within a plane, y = planes, z = volumes), round-robin over the copy
+// streams.  row_bytes: one x1 row; rpp: rows per plane; ppv: planes per volume.
+struct Slabs {
+  int row_bytes, rpp, r0, nr, ppv, p0, np;
+  long long nvol;
+  long long vol_elems() const { return (long long)row_bytes / 8 * rpp * ppv; }
+  long long chunk_vols() const {
+    const long long per = (long long)row_bytes * nr * np;
+    const long long v = COPY_CHUNK / (per > 0 ? per : 1);
+    return v > 0 ? v : 1;
+  }
+};
+cudaError_t copy_slab_chunk(const Slabs& sl, void* dst, const void* src, long long z0,
+                            long long nz, cudaMemcpyKind kind, cudaStream_t cs) {
+  cudaMemcpy3DParms p = {};
+  const size_t pitch = (size_t)sl.row_bytes * sl.rpp;
+  p.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), pitch, pitch, sl.ppv);
+  p.dstPtr = make_cudaPitchedPtr(dst, pitch, pitch, sl.ppv);
+  p.srcPos = make_cudaPos((size_t)sl.r0 * sl.row_bytes, sl.p0, (size_t)z0);
+  p.dstPos = p.srcPos;
+  p.extent = make_cudaExtent((size_t)sl.nr * sl.row_bytes, sl.np, (size_t)nz);
+  p.kind = kind;
+  return cudaMemcpy3DAsync(&p, cs);
+}
+// a plain FP64 array's slabs, host <-> device (after fork_copies)
+athgpu_status copy_slabs(athgpu_ctx* c, const Slabs& sl, void* dst, const void* src,
+                         cudaMemcpyKind kind, int* rr) {
+  const long long cv = sl.chunk_vols();
+  for (long long z0 = 0; z0 < sl.nvol; z0 += cv) {
+    const long long nz = sl.nvol - z0 < cv ? sl.nvol - z0 : cv;
+    CK(copy_slab_chunk(sl, dst, src, z0, nz, kind,
+                       c->copy_stream[(*rr)++ % athgpu_ctx::NCOPY]));
+  }
+  return ATHGPU_OK;
+}
+// the slabs of U into a bulk-precision register: FP32 contexts take each chunk through
+// the FP64 staging buffer (whole volumes, the same layout) and convert its volumes
+athgpu_status upload_slabs(athgpu_ctx* c, const Slabs& sl, const double* h, void* dev,
+                           void* lo, int* rr) {
+  if (c->real_bytes == 8) return copy_slabs(c, sl, dev, h, cudaMemcpyHostToDevice, rr);
+  const long long cv = sl.chunk_vols(), ve = sl.vol_elems();
+  for (long long z0 = 0; z0 < sl.nvol; z0 += cv) {
+    const long long nz = sl.nvol - z0 < cv ? sl.nvol - z0 : cv;
+    cudaStream_t cs = c->copy_stream[(*rr)++ % athgpu_ctx::NCOPY];
+    CK(copy_slab_chunk(sl, c->staging, h, z0, nz, cudaMemcpyHostToDevice, cs));
+    cudaEvent_t ev = next_copy_event(c);
+    CK(cudaEventRecord(ev, cs));
+    CK(cudaStreamWaitEvent(c->stream, ev, 0));
+    const long long off = z0 * ve, cn = nz * ve;
+    split_kernel<<<(unsigned)ceil_div(cn, 256), 256, 0, c->stream>>>(
+        c->staging + off, (float*)dev + off, lo ? (float*)lo + off : nullptr, cn);
+    CK(cudaGetLastError());
+  }
+  return ATHGPU_OK;
+}
+athgpu_status download_slabs(athgpu_ctx* c, const Slabs& sl, double* h, const void* dev,
+                             const void* lo, int* rr) {
+  if (c->real_bytes == 8) return copy_slabs(c, sl, h, dev, cudaMemcpyDeviceToHost, rr);
+  const long long cv = sl.chunk_vols(), ve = sl.vol_elems();
+  for (long long z0 = 0; z0 < sl.nvol; z0 += cv) {
+    const long long nz = sl.nvol - z0 < cv ? sl.nvol - z0 : cv;
+    const long long off = z0 * ve, cn = nz * ve;
+    join_kernel<<<(unsigned)ceil_div(cn, 256), 256, 0, c->stream>>>(
+        (const float*)dev + off, lo ? (const float*)lo + off : nullptr, c->staging + off, cn);
+    CK(cudaGetLastError());
+    cudaEvent_t ev = next_copy_event(c);
+    CK(cudaEventRecord(ev, c->stream));
+    cudaStream_t cs = c->copy_stream[(*rr)++ % athgpu_ctx::NCOPY];
+    CK(cudaStreamWaitEvent(cs, ev, 0));
+    CK(copy_slab_chunk(sl, h, c->staging, z0, nz, cudaMemcpyDeviceToHost, cs));
+  }
+  return ATHGPU_OK;
+}
+// the slab geometry of U (what = 0) and of the face arrays b1..b3 (what = 1..3)
+Slabs state_slabs(const DevMesh& m, int what) {
+  Slabs s;
+  s.row_bytes = (m.nc1 + (what == 1 ? 1 : 0)) * 8;
+  s.rpp = m.nc2 + (what == 2 ? 1 : 0);
+  s.r0 = m.js;
+  s.nr = m.nx2 + (what == 2 ? 1 : 0);
+  s.ppv = m.nc3 + (what == 3 ? 1 : 0);
+  s.p0 = m.ks;
+  s.np = m.nx3 + (what == 3 ? 1 : 0);
+  s.nvol = (long long)m.nb * (what == 0 ? 5 : 1);
+  return s;
+}
 }  // namespace
 
 namespace athgpu {
@@ -840,6 +930,18 @@ athgpu_status athgpu_upload_state(athgpu_ctx* c, const double* u, const double* 
   athgpu_status s;
   int rr = 0;
   CK(fork_copies(c));
+  if (c->copy_extent == ATHGPU_COPY_INTERIOR) {
+    double* fb[3] = {c->r.b1, c->r.b2, c->r.b3};
+    const double* hb[3] = {b1, b2, b3};
+    for (int d = 0; d < 3; ++d)
+      if (hb[d] && (s = copy_slabs(c, state_slabs(m, d + 1), fb[d], hb[d],
+                                   cudaMemcpyHostToDevice, &rr)))
+        return s;
+    if (u && (s = upload_slabs(c, state_slabs(m, 0), u, c->r.u, c->r.ulo, &rr))) return s;
+    CK(join_copies(c));
+    CK(cudaStreamSynchronize(c->stream));
+    return ATHGPU_OK;
+  }
   // the face fields first: plain copies that need no conversion
   if (b1 && (s = copy_chunked(c, c->r.b1, b1, m.nb * m.nf1 * 8, cudaMemcpyHostToDevice, &rr)))
     return s;
@@ -879,6 +981,18 @@ athgpu_status athgpu_download_state(athgpu_ctx* c, double* u, double* b1, double
   // exchange also rewrites the face fields' ghosts), then every copy follows it
   if (u) CK(c->desc.precision == ATHGPU_FP64 ? exchange_u_fp64(c) : exchange_u_fp32(c));
   CK(fork_copies(c));
+  if (c->copy_extent == ATHGPU_COPY_INTERIOR) {
+    const double* fb[3] = {c->r.b1, c->r.b2, c->r.b3};
+    double* hb[3] = {b1, b2, b3};
+    for (int d = 0; d < 3; ++d)
+      if (hb[d] && (s = copy_slabs(c, state_slabs(m, d + 1), hb[d], fb[d],
+                                   cudaMemcpyDeviceToHost, &rr)))
+        return s;
+    if (u && (s = download_slabs(c, state_slabs(m, 0), u, c->r.u, c->r.ulo, &rr))) return s;
+    CK(join_copies(c));
+    CK(cudaStreamSynchronize(c->stream));
+    return ATHGPU_OK;
+  }
   if (b1 && (s = copy_chunked(c, b1, c->r.b1, m.nb * m.nf1 * 8, cudaMemcpyDeviceToHost, &rr)))
     return s;
   if (b2 && (s = copy_chunked(c, b2, c->r.b2, m.nb * m.nf2 * 8, cudaMemcpyDeviceToHost, &rr)))
@@ -915,6 +1029,14 @@ athgpu_status athgpu_set_host_copy(athgpu_ctx* c, int mode) {
   if (!c) return fail(ATHGPU_ERR_ARG, "null context");
   if (mode != 0 && mode != 1) return fail(ATHGPU_ERR_ARG, "host copy mode must be 0 or 1");
   c->host_copy_mode = mode;
+  return ATHGPU_OK;
+}
+
+athgpu_status athgpu_set_copy_extent(athgpu_ctx* c, int extent) {
+  if (!c) return fail(ATHGPU_ERR_ARG, "null context");
+  if (extent != ATHGPU_COPY_WHOLE && extent != ATHGPU_COPY_INTERIOR)
+    return fail(ATHGPU_ERR_ARG, "copy extent must be ATHGPU_COPY_WHOLE or ATHGPU_COPY_INTERIOR");
+  c->copy_extent = extent;
   return ATHGPU_OK;
 }
 

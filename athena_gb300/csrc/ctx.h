@@ -85,6 +85,7 @@ struct athgpu_ctx {
   cudaEvent_t copy_ev[NCOPY_EV] = {};
   int copy_ev_next = 0;
   int host_copy_mode = 0;  // athgpu_set_host_copy
+  int copy_extent = 0;     // athgpu_set_copy_extent (ATHGPU_COPY_WHOLE / _INTERIOR)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t cycle_exec = nullptr;
   cudaGraph_t cycle_graph = nullptr;

@@ -24,6 +24,7 @@ _RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF, "roe": ROE, "lhlld": LHLLD}
 FP64, FP32 = 0, 1
 VL2, RK2 = 0, 1
 _INTEGRATORS = {"vl2": VL2, "rk2": RK2}
+COPY_WHOLE, COPY_INTERIOR = 0, 1
 
 
 class AthGPUError(RuntimeError):
@@ -432,6 +433,14 @@ class StageUpdate:
         """0: chunked DMA over several copy streams (default); 1: conversion kernels on
         page-locked host memory."""
         _check(load_library().athgpu_set_host_copy(self.h, int(mode)), "athgpu_set_host_copy")
+
+    def set_copy_extent(self, extent):
+        """COPY_WHOLE (default): set_state/state move whole arrays; COPY_INTERIOR: only
+        each MeshBlock's x2/x3 range of own cells and faces, with whole x1 rows (the
+        host's x2/x3 ghost zones neither read nor written; initialize() recomputes every
+        ghost zone after an upload)."""
+        _check(load_library().athgpu_set_copy_extent(self.h, int(extent)),
+               "athgpu_set_copy_extent")
 
     def set_x3_staging(self, bulk):
         """x3 sweep staging: 0 per-thread cp.async, 1 TMA bulk copies."""

@@ -222,7 +222,7 @@ def run_gpu(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
     from athena_gb300 import build
-    from athena_gb300.runtime import StageUpdate
+    from athena_gb300.runtime import COPY_INTERIOR, COPY_WHOLE, StageUpdate
     build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -294,17 +294,25 @@ def run_gpu(args, rank, world, local_rank):
             # the faster host-copy mode of the library on this machine (chunked DMA over
             # several streams, or conversion kernels on the pinned arrays), by one timed
             # upload + download of each
+            # upload + download of each; and the copies of each block's x2/x3 interior with
+            # whole x1 rows (COPY_INTERIOR: initialize() recomputes the ghost zones)
             mode_ms = {}
-            for mode in (0, 1):
+            for name, extent, mode in (("whole/dma", COPY_WHOLE, 0),
+                                       ("whole/link", COPY_WHOLE, 1),
+                                       ("interior/dma", COPY_INTERIOR, 0)):
+                g.set_copy_extent(extent)
                 g.set_host_copy(mode)
                 g.set_state(*pinned)
                 g.state(out=pinned_out)
                 t0 = time.perf_counter()
                 g.set_state(*pinned)
                 g.state(out=pinned_out)
-                mode_ms[mode] = (time.perf_counter() - t0) * 1e3
+                mode_ms[name] = (time.perf_counter() - t0) * 1e3
             host_mode = min(mode_ms, key=mode_ms.get)
-            g.set_host_copy(host_mode)
+            extent = COPY_INTERIOR if host_mode.startswith("interior") else COPY_WHOLE
+            g.set_copy_extent(extent)
+            g.set_host_copy(1 if host_mode == "whole/link" else 0)
+            cbytes = state_copy_bytes(mesh, extent)
             for _ in range(2):
                 g.set_state(*pinned)
                 g.initialize()
@@ -329,11 +337,12 @@ def run_gpu(args, rank, world, local_rank):
                 dist.all_reduce(t, op=dist.ReduceOp.MAX)
                 te = float(t.item())
             res["e2e"] = {"value": world * zones * e_steps / te, "unit": "zone-cycles/s",
-                          "h2d_bytes_per_step": ebytes, "d2h_bytes_per_step": ebytes,
+                          "h2d_bytes_per_step": cbytes, "d2h_bytes_per_step": cbytes,
                           "steps": e_steps, "ms_per_step": te / e_steps * 1e3,
-                          "host_copy_mode": host_mode,
+                          "host_copy_mode": host_mode, "whole_state_bytes": ebytes,
                           "step_ms": {"min": min(step_ms), "median": float(np.median(step_ms)),
-                                      "max": max(step_ms)},
+                                      "max": max(step_ms),
+                                      "all": [round(x, 2) for x in step_ms]},
                           "upload_download_ms_by_mode": mode_ms,
                           "link_ceiling": link_ceiling(dev, ebytes)}
         g.close()
@@ -736,6 +745,19 @@ def amr_cpu_baseline(ic, threads=None):
     return {"value": zones / t, "unit": "zone-cycles/s", "cores": threads, "kind": "port",
             "sample": "1 cycle (with its refinement step) of the %d-block mesh after the "
                       "adaptive initial loop" % (zones // 16 ** 3)}
+
+
+def state_copy_bytes(mesh, extent):
+    """Bytes one upload (or download) of U and the three face arrays moves: whole
+    arrays, or (COPY_INTERIOR) per block the own x2/x3 range with whole x1 rows."""
+    from athena_gb300.runtime import COPY_WHOLE
+    c1, c2, c3 = mesh.nc
+    if extent == COPY_WHOLE:
+        n = 5 * c3 * c2 * c1 + c3 * c2 * (c1 + 1) + c3 * (c2 + 1) * c1 + (c3 + 1) * c2 * c1
+    else:
+        n1, n2, n3 = mesh.bx
+        n = 5 * n3 * n2 * c1 + n3 * n2 * (c1 + 1) + n3 * (n2 + 1) * c1 + (n3 + 1) * n2 * c1
+    return 8 * n * mesh.nblocks
 
 
 def l1_rel(a, b):
