@@ -63,7 +63,12 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // are normal and their exponents differ by at most 28, the exact difference has at most 53
 // significant bits (2^52 + 2^24 < 2^53), so it is an FP64 number; it is formed from the
 // two significands aligned in one 64-bit integer, normalised with a leading-zero count.
-// Other operands take the FP64 subtraction.  Same bits as the hardware in every case.
+// Other operands take the FP64 subtraction, in a function of its own: a real branch, so
+// that its FP64-pipe instructions are not issued (predicated off) on the common path.
+// Same bits as the hardware in every case.
+static __device__ __noinline__ double fsub_f64_slow(float a, float b) {
+  return (double)a - (double)b;
+}
 __device__ __forceinline__ double fsub_f64(float a, float b) {
   unsigned ua = __float_as_uint(a), ub = __float_as_uint(b) ^ 0x80000000u;  // a + (-b)
   unsigned ea = (ua >> 23) & 0xffu, eb = (ub >> 23) & 0xffu;
@@ -90,7 +95,7 @@ __device__ __forceinline__ double fsub_f64(float a, float b) {
                                     (sign << 63);
     return __longlong_as_double((long long)bits);
   }
-  return f2d_exact(a) - f2d_exact(b);
+  return fsub_f64_slow(a, b);
 }
 __device__ __forceinline__ double fsub_f64(double a, double b) { return a - b; }
 // a face-field (always FP64) value in the bulk precision (hardware conversion: where the
