@@ -1218,8 +1218,16 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const bool f3 = i <= m.ie && j <= m.je;
   const double l1 = dx1f[m.is], l2 = dx2f[m.js], l3 = dx3f[m.ks];
   const bool exact = sizeof(Real) == 8;
-  auto term = [&](double qd, double len, double qlen, Real ep, Real em) -> double {
-    return exact ? qd * (len * (double)ep - len * (double)em) : qlen * fsub_f64(ep, em);
+  // v -/+ the term of edges ep, em: FP64 path (wght/area)*(len*ep - len*em), then the
+  // sum, as the reference; FP32 path one FMA of ((wght/area)*len) and the exact edge
+  // difference (written out: the compiler does not contract it through the difference)
+  auto upd = [&](double v, bool minus, double qd, double len, double qlen, Real ep,
+                 Real em) -> double {
+    if (exact) {
+      const double t = qd * (len * (double)ep - len * (double)em);
+      return minus ? v - t : v + t;
+    }
+    return __fma_rn(minus ? -qlen : qlen, fsub_f64(ep, em), v);
   };
   // in-block offsets of the edges at (k,j,i) and the block bases of the edge arrays
   const int c1 = m.nc1, c2 = m.nc2;
@@ -1237,9 +1245,9 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
     const i64 o = (i64)b * m.nf1 + (k * c2 + j) * (c1 + 1) + i;
     double v = b1in[o];
     if (b1avg) v = g1 * b1avg[o] + g2 * v;
-    v -= term(q[0], l3, ql[0],
+    v = upd(v, true, q[0], l3, ql[0],
               edge_at<Real, 2, ML>(m, e3, E3, oe3 + (c1 + 1), b, k, j + 1, i), e3c);
-    v += term(q[0], l2, ql[1],
+    v = upd(v, false, q[0], l2, ql[1],
               edge_at<Real, 1, ML>(m, e2, E2, oe2 + c2 * (c1 + 1), b, k + 1, j, i), e2c);
     b1out[o] = v;
   }
@@ -1247,9 +1255,9 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
     const i64 o = (i64)b * m.nf2 + (k * (c2 + 1) + j) * c1 + i;
     double v = b2in[o];
     if (b2avg) v = g1 * b2avg[o] + g2 * v;
-    v += term(q[1], l3, ql[2], edge_at<Real, 2, ML>(m, e3, E3, oe3 + 1, b, k, j, i + 1),
+    v = upd(v, false, q[1], l3, ql[2], edge_at<Real, 2, ML>(m, e3, E3, oe3 + 1, b, k, j, i + 1),
               e3c);
-    v -= term(q[1], l1, ql[3],
+    v = upd(v, true, q[1], l1, ql[3],
               edge_at<Real, 0, ML>(m, e1, E1, oe1 + (c2 + 1) * c1, b, k + 1, j, i), e1c);
     b2out[o] = v;
   }
@@ -1257,9 +1265,9 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
     const i64 o = (i64)b * m.nf3 + (k * c2 + j) * c1 + i;
     double v = b3in[o];
     if (b3avg) v = g1 * b3avg[o] + g2 * v;
-    v -= term(q[2], l2, ql[4], edge_at<Real, 1, ML>(m, e2, E2, oe2 + 1, b, k, j, i + 1),
+    v = upd(v, true, q[2], l2, ql[4], edge_at<Real, 1, ML>(m, e2, E2, oe2 + 1, b, k, j, i + 1),
               e2c);
-    v += term(q[2], l1, ql[5], edge_at<Real, 0, ML>(m, e1, E1, oe1 + c1, b, k, j + 1, i),
+    v = upd(v, false, q[2], l1, ql[5], edge_at<Real, 0, ML>(m, e1, E1, oe1 + c1, b, k, j + 1, i),
               e1c);
     b3out[o] = v;
   }

@@ -63,10 +63,17 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // are normal and their exponents differ by at most 28, the exact difference has at most 53
 // significant bits (2^52 + 2^24 < 2^53), so it is an FP64 number; it is formed from the
 // two significands aligned in one 64-bit integer, normalised with a leading-zero count.
-// Other operands take the FP64 subtraction, in a function of its own: a real branch, so
-// that its FP64-pipe instructions are not issued (predicated off) on the common path.
-// Same bits as the hardware in every case.
+// Other operands take a function of its own (a real branch, so that nothing of it is
+// issued predicated-off on the common path): a zero operand gives the other one widened
+// on the integer pipe (f2d_exact; two zeros: -0 only for (-0) - (+0), as IEEE addition of
+// a + (-b)), anything else the FP64 subtraction.  Same bits as the hardware in every case.
 static __device__ __noinline__ double fsub_f64_slow(float a, float b) {
+  const unsigned ua = __float_as_uint(a), ub = __float_as_uint(b) ^ 0x80000000u;
+  if ((ub << 1) == 0u) {
+    if ((ua << 1) != 0u) return f2d_exact(a);
+    return __longlong_as_double((long long)(ua & ub & 0x80000000u) << 32);
+  }
+  if ((ua << 1) == 0u) return f2d_exact(__uint_as_float(ub));
   return (double)a - (double)b;
 }
 __device__ __forceinline__ double fsub_f64(float a, float b) {

@@ -72,7 +72,9 @@ def _float_pairs(rng, n):
     special = np.array([0.0, 1.0, -0.0, 1.0, 1.0, 0.0, 1e-40, 1.0, 1.0, -1e-45, np.inf, 1.0,
                         1.0, np.nan, np.finfo(np.float32).max, -np.finfo(np.float32).max,
                         np.finfo(np.float32).tiny, np.finfo(np.float32).tiny * 2,
-                        1.0, 1.0 + 2.0 ** -23, 2.0 ** 28, 1.0, 2.0 ** 29, 1.0],
+                        1.0, 1.0 + 2.0 ** -23, 2.0 ** 28, 1.0, 2.0 ** 29, 1.0,
+                        0.0, -0.0, -0.0, 0.0, -0.0, -0.0, 0.0, 0.0, -0.0, 2.5, 3.0, -0.0,
+                        0.0, 1e-40, -1e-45, 0.0, 0.0, np.inf, -np.inf, -0.0, np.nan, 0.0],
                        dtype=np.float32)
     return np.concatenate([special, out])
 
