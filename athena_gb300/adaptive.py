@@ -170,6 +170,7 @@ class NativeAmr:
                                    (ctypes.c_int * 6)(*self.bcs), int(numlevel),
                                    int(derefine_count)), "athgpu_amr_create")
         self.h = h
+        self.generation = 0   # counts the mesh changes (NativeMesh's lazy tables check it)
 
     def close(self):
         if getattr(self, "h", None):
@@ -191,16 +192,22 @@ class NativeAmr:
     def add_block(self, loc):
         _check(load_library().athgpu_amr_add_block(self.h, loc.level, loc.lx1, loc.lx2,
                                                    loc.lx3), "athgpu_amr_add_block")
+        self.generation += 1
 
-    def tables(self, coords=True):
+    def tables(self, coords=True, nbrs=True):
         """(loc[nb][4], nbr_table[nb][56][10], nbr_count[nb], nblevel[nb][27], fine
-        coordinates (x1f, dx1f, ...), coarse coordinates) of the current mesh."""
+        coordinates (x1f, dx1f, ...), coarse coordinates) of the current mesh; without
+        nbrs the three neighbour tables are None, without coords the coordinate lists
+        are empty."""
         nb = self.nblocks
         bx = [self.nx[d] // self.nrbx[d] for d in range(3)]
         loc = np.zeros((nb, 4), dtype=np.int64)
-        t = np.zeros((nb, 56, 10), dtype=np.int32)
-        cnt = np.zeros(nb, dtype=np.int32)
-        lv = np.zeros((nb, 27), dtype=np.int32)
+        t = cnt = lv = None
+        if nbrs:
+            t = np.zeros((nb, 56, 10), dtype=np.int32)
+            cnt = np.zeros(nb, dtype=np.int32)
+            lv = np.zeros((nb, 27), dtype=np.int32)
+        inull = ctypes.POINTER(ctypes.c_int)()
         fine, coarse = [], []
         if coords:
             for d in range(3):
@@ -210,8 +217,9 @@ class NativeAmr:
         null = ctypes.POINTER(ctypes.c_double)()
         ptrs = [_dp(a) for a in fine + coarse] if coords else [null] * 12
         _check(load_library().athgpu_amr_tables(
-            self.h, loc.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), _ip(t), _ip(cnt),
-            _ip(lv), *ptrs), "athgpu_amr_tables")
+            self.h, loc.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+            *[(_ip(a) if a is not None else inull) for a in (t, cnt, lv)], *ptrs),
+            "athgpu_amr_tables")
         return loc, t, cnt, lv, fine, coarse
 
     def flags(self, ret):
@@ -243,6 +251,7 @@ class NativeAmr:
 
     def accept(self):
         _check(load_library().athgpu_amr_accept(self.h), "athgpu_amr_accept")
+        self.generation += 1
 
     def deref_counts(self):
         out = np.zeros(self.nblocks, dtype=np.int32)
@@ -255,6 +264,8 @@ class NativeAmr:
         r = ctypes.c_int()
         _check(load_library().athgpu_amr_step(su.h, self.h, float(thr), int(after_cycle),
                                               ctypes.byref(r)), "athgpu_amr_step")
+        if r.value:
+            self.generation += 1
         return bool(r.value)
 
 
@@ -268,7 +279,10 @@ class _RootInfo:
 
 class NativeMesh(MultiLevelMesh):
     """The current mesh of a NativeAmr with the interface of MultiLevelMesh (block list,
-    shapes, coordinates, neighbour tables); the tables come from the library."""
+    shapes, coordinates, neighbour tables); the tables come from the library.  Only the
+    block locations are fetched when the object is made (a regrid makes one); the
+    neighbour tables, coordinates and Loc list on first use, which must come before the
+    tree changes again."""
 
     def __init__(self, amr: NativeAmr):
         self.nx, self.nrbx, self.ng = amr.nx, amr.nrbx, amr.ng
@@ -278,22 +292,36 @@ class NativeMesh(MultiLevelMesh):
         self.cng = (self.ng + 1) // 2 + 1
         self.ncc = tuple(self.bx[d] // 2 + 2 * self.ng for d in range(3))
         self.tree = _RootInfo(self.nrbx)
-        loc, t, cnt, lv, fine, coarse = amr.tables()
-        self._tab = (t, cnt, lv, loc)
-        self._fine, self._coarse = fine, coarse
-        self.locs = [Loc(int(r[0]), int(r[1]), int(r[2]), int(r[3])) for r in loc]
-        self.nblocks = len(self.locs)
+        self._amr, self._gen = amr, amr.generation
+        loc = amr.tables(coords=False, nbrs=False)[0]
+        self._loc = loc
+        self.nblocks = loc.shape[0]
         self.levels = loc[:, 0].astype(np.int32)
-        self._nblev = lv
+        self._tables = None
+        self._locs = None
+
+    def _fetch(self):
+        if self._tables is None:
+            if self._amr.generation != self._gen:
+                raise RuntimeError("the adaptive mesh changed since this block list was made")
+            _, t, cnt, lv, fine, coarse = self._amr.tables()
+            self._tables = ((t, cnt, lv, self._loc), lv, fine, coarse)
+        return self._tables
+
+    @property
+    def locs(self):
+        if self._locs is None:
+            self._locs = [Loc(int(r[0]), int(r[1]), int(r[2]), int(r[3])) for r in self._loc]
+        return self._locs
 
     def neighbor_table(self):
-        return self._tab
+        return self._fetch()[0]
 
     def nblevel_array(self):
-        return self._nblev
+        return self._fetch()[1]
 
     def coordinate_arrays(self):
-        return list(self._fine)
+        return list(self._fetch()[2])
 
     def coarse_coordinate_arrays(self):
-        return list(self._coarse)
+        return list(self._fetch()[3])

@@ -458,7 +458,13 @@ extern "C" {
 const char* athgpu_last_error(void) { return g_err.c_str(); }
 const char* athgpu_version(void) { return "athena_gb300 0.1 (sm_103a)"; }
 
-athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
+}  // extern "C"
+
+namespace athgpu {
+// athgpu_create; sync_end = false leaves the context's set-up (register clearing, small
+// uploads) running on its stream when it returns (the regrid's new context, whose stream
+// the regrid synchronizes after building the multi-level plan on the host meanwhile)
+athgpu_status create_context(athgpu_ctx** out, const athgpu_mesh_desc* d, bool sync_end) {
   if (!out || !d) return fail(ATHGPU_ERR_ARG, "null argument");
   *out = nullptr;
   if (d->nbx1 < 1 || d->nbx2 < 1 || d->nbx3 < 1 || d->nx1 < 1 || d->nx2 < 1 || d->nx3 < 1)
@@ -614,8 +620,6 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     a.bytes += 4096;
     e = pool_alloc(a.p, a.bytes, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync"));
-    e = cudaMemsetAsync(*a.p, 0, a.bytes, c->stream);
-    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemset"));
   }
 
   // coordinates: dx?f [nb][nc?] and the PLM interface coefficients
@@ -643,10 +647,12 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
         hc[plmoff + ((b * 3 + dd) * 2 + 0) * m.ncmax + cc] = (f[cc + 1] - xv) / df[cc];
         hc[plmoff + ((b * 3 + dd) * 2 + 1) * m.ncmax + cc] = (xv - f[cc]) / df[cc];
       }
+  // (the small uploads below are stream-ordered after their allocations and before the
+  // registers' clearing, so none of them waits for it)
   e = pool_alloc((void**)&c->coords, sizeof(double) * ncoord, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync coords"));
-  e = cudaMemcpy(c->coords, hc.data(), sizeof(double) * ncoord, cudaMemcpyHostToDevice);
+  e = cudaMemcpyAsync(c->coords, hc.data(), sizeof(double) * ncoord, cudaMemcpyHostToDevice,
+                      c->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy coords"));
   m.dx1f = c->coords + dxoff[0];
   m.dx2f = c->coords + dxoff[1];
@@ -656,9 +662,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     std::vector<float> hf(ncoord);
     for (i64 q = 0; q < ncoord; ++q) hf[q] = (float)hc[q];
     e = pool_alloc((void**)&c->coords32, sizeof(float) * ncoord, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync coords32"));
-    e = cudaMemcpy(c->coords32, hf.data(), sizeof(float) * ncoord, cudaMemcpyHostToDevice);
+    e = cudaMemcpyAsync(c->coords32, hf.data(), sizeof(float) * ncoord,
+                        cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy coords32"));
     m.dx1f32 = c->coords32 + dxoff[0];
     m.dx2f32 = c->coords32 + dxoff[1];
@@ -676,9 +682,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
           hv[o++] = 0.5 * (f[cc + 1] + f[cc]);
         }
     e = pool_alloc((void**)&c->fxv, sizeof(double) * hv.size(), c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync fxv"));
-    e = cudaMemcpy(c->fxv, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice);
+    e = cudaMemcpyAsync(c->fxv, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice,
+                        c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy fxv"));
   }
 
@@ -708,9 +714,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
         }
   }
   e = pool_alloc((void**)&c->nbr, sizeof(int) * hn.size(), c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMallocAsync nbr"));
-  e = cudaMemcpy(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice);
+  e = cudaMemcpyAsync(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice,
+                      c->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy nbr"));
   m.nbr = c->nbr;
 
@@ -722,13 +728,12 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     e = pool_alloc((void**)&c->xplan, sizeof(unsigned) * plan.size(), c->stream);
     if (e == cudaSuccess)
       e = pool_alloc((void**)&c->xdelta, sizeof(int) * delta.size(), c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess)
-      e = cudaMemcpy(c->xplan, plan.data(), sizeof(unsigned) * plan.size(),
-                     cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(c->xplan, plan.data(), sizeof(unsigned) * plan.size(),
+                          cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess)
-      e = cudaMemcpy(c->xdelta, delta.data(), sizeof(int) * delta.size(),
-                     cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(c->xdelta, delta.data(), sizeof(int) * delta.size(),
+                          cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "ghost plan"));
   }
   {  // the blocks' face edges for the same-level edge averaging (edge_fix_kernel)
@@ -737,10 +742,9 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
     e = pool_alloc((void**)&c->eplan, sizeof(int4) * plan.size(), c->stream);
     if (e == cudaSuccess)
       e = pool_alloc(&c->escratch, (size_t)c->real_bytes * plan.size() * nb, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess)
-      e = cudaMemcpy(c->eplan, plan.data(), sizeof(int4) * plan.size(),
-                     cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(c->eplan, plan.data(), sizeof(int4) * plan.size(),
+                          cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "edge plan"));
   }
 
@@ -754,12 +758,27 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   hclk.dtf = (float)hclk.dt;
   hclk.dt_prev = DBL_MAX;
   hclk.dtmin_prev_bits = hclk.dtmin_bits;
-  e = cudaMemcpy(c->clk, &hclk, sizeof(hclk), cudaMemcpyHostToDevice);
+  // the registers start cleared (the tables above are not among them), then the clock,
+  // which is (pageable copies are staged at once: none of this waits on the host)
+  for (auto& a : allocs) {
+    e = cudaMemsetAsync(*a.p, 0, a.bytes, c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemset"));
+  }
+  e = cudaMemcpyAsync(c->clk, &hclk, sizeof(hclk), cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy clock"));
-  e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return bail(cuda_fail(e, "create sync"));
+  if (sync_end) {
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "create sync"));
+  }
   *out = c;
   return ATHGPU_OK;
+}
+}  // namespace athgpu
+
+extern "C" {
+
+athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
+  return athgpu::create_context(out, d, true);
 }
 
 athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,

@@ -35,6 +35,7 @@
 namespace athgpu {
 athgpu_status api_fail(athgpu_status code, const std::string& msg);
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
+athgpu_status create_context(athgpu_ctx** out, const athgpu_mesh_desc* d, bool sync_end);
 }
 
 namespace {
@@ -296,7 +297,8 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     g_phase_ms[q] += t - tp;
     tp = t;
   };
-  athgpu_status st = athgpu_create(&nc, desc);
+  // (its registers are cleared on its stream while the host builds the plan below)
+  athgpu_status st = athgpu::create_context(&nc, desc, false);
   phase(0);
   if (st != ATHGPU_OK) return st;
   st = athgpu_set_multilevel(nc, nbr_table, nbr_count, nblevel, loc, cx1f, cdx1f, cx2f, cdx2f,
