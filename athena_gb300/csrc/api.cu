@@ -781,15 +781,36 @@ athgpu_status athgpu_create(athgpu_ctx** out, const athgpu_mesh_desc* d) {
   return athgpu::create_context(out, d, true);
 }
 
-athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
-                                    const int* nbr_count, const int* nblevel,
-                                    const long long* loc, const double* cx1f,
-                                    const double* cdx1f, const double* cx2f,
-                                    const double* cdx2f, const double* cx3f,
-                                    const double* cdx3f) {
+}  // extern "C"
+
+namespace athgpu {
+// a device copy of host data (or a cleared array for h = NULL), stream-ordered on the
+// context's stream and released with the context
+static cudaError_t ml_dev(athgpu_ctx* c, const void* h, size_t bytes, void** out) {
+  *out = nullptr;
+  if (bytes == 0) return cudaSuccess;
+  cudaError_t e = pool_alloc(out, bytes, c->stream);
+  if (e != cudaSuccess) return e;
+  c->mld.allocs.push_back(*out);
+  if (h) return cudaMemcpyAsync(*out, h, bytes, cudaMemcpyHostToDevice, c->stream);
+  return cudaMemsetAsync(*out, 0, bytes, c->stream);
+}
+#define DEV(h, bytes, field)                                                           \
+  do {                                                                                 \
+    void* p_;                                                                          \
+    cudaError_t e_ = ml_dev(c, h, bytes, &p_);                                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, "multi-level allocation");             \
+    field = (decltype(field))p_;                                                       \
+  } while (0)
+
+// athgpu_set_multilevel, first part: the checks, the coarse buffers, correction arrays,
+// neighbour tables and coarse coordinates (what the regrid's copies and prolongation use),
+// stream-ordered on the context's stream without waiting
+athgpu_status ml_prepare(athgpu_ctx* c, const int* nbr_table, const int* nbr_count,
+                         const int* nblevel, const long long* loc, const double* cx1f,
+                         const double* cx2f, const double* cx3f) {
   if (!c || !nbr_table || !nbr_count || !nblevel || !loc || !cx1f || !cx2f || !cx3f)
     return fail(ATHGPU_ERR_ARG, "null argument");
-  (void)cdx1f; (void)cdx2f; (void)cdx3f;
   if (c->initialized || c->m.ml.on)
     return fail(ATHGPU_ERR_STATE, "athgpu_set_multilevel must come before athgpu_initialize");
   if (c->desc.relativistic)
@@ -803,25 +824,6 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
   if (m.nx1 % 2 || m.nx2 % 2 || m.nx3 % 2 || m.nx1 / 2 < 2 || m.nx2 / 2 < 2 || m.nx3 / 2 < 2)
     return fail(ATHGPU_ERR_ARG, "mesh refinement needs even MeshBlock sizes of at least 4");
   const int nb = m.nb;
-  MlDims dims;
-  dims.nx[0] = m.nx1; dims.nx[1] = m.nx2; dims.nx[2] = m.nx3;
-  dims.ng = m.ng;
-  for (int f = 0; f < 6; ++f) dims.bc[f] = m.bc[f];
-  MlPlan& plan = c->mlplan;
-  std::string err;
-  if (!build_ml_plan(dims, nb, nbr_table, nbr_count, nblevel, loc, &plan, &err))
-    return fail(ATHGPU_ERR_ARG, err.c_str());
-  auto& al = c->mld.allocs;
-  auto dev = [&](const void* h, size_t bytes, void** out) -> cudaError_t {
-    *out = nullptr;
-    if (bytes == 0) return cudaSuccess;
-    cudaError_t e = pool_alloc(out, bytes, c->stream);
-    if (e != cudaSuccess) return e;
-    al.push_back(*out);
-    // stream-ordered after the allocation; the host data live until the final sync
-    if (h) return cudaMemcpyAsync(*out, h, bytes, cudaMemcpyHostToDevice, c->stream);
-    return cudaMemsetAsync(*out, 0, bytes, c->stream);
-  };
   DevML& L = m.ml;
   const int rb = c->real_bytes;
   const int cng = (m.ng + 1) / 2 + 1;
@@ -847,18 +849,11 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
         cxv[d][(size_t)b * ncc[d] + q] = 0.5 * (cxf[d][(size_t)b * (ncc[d] + 1) + q + 1] +
                                                  cxf[d][(size_t)b * (ncc[d] + 1) + q]);
   }
-  void* p;
-#define DEV(h, bytes, field) \
-  do { cudaError_t e_ = dev(h, bytes, &p); if (e_ != cudaSuccess) return cuda_fail(e_, "multi-level allocation"); field = (decltype(field))p; } while (0)
   const void* nullh = nullptr;
   c->mld.hloc.assign(loc, loc + (size_t)nb * 4);
   DEV(nblevel, sizeof(int) * (size_t)nb * 27, L.nblev);
   DEV(nbr_table, sizeof(int) * (size_t)nb * ML_MAXNB * ML_NF, L.nbrt);
   DEV(nbr_count, sizeof(int) * (size_t)nb, L.nnbr);
-  DEV(plan.eflag.data(), sizeof(int) * plan.eflag.size(), L.eflag);
-  DEV(plan.nfine.data(), sizeof(int) * plan.nfine.size(), L.nfine);
-  DEV(plan.fmask.data(), sizeof(int) * plan.fmask.size(), L.fmask);
-  DEV(plan.level.data(), sizeof(int) * plan.level.size(), L.level);
   DEV(nullh, (size_t)nb * 5 * L.nccell * rb, L.ccons);
   DEV(nullh, (size_t)nb * 5 * L.nccell * rb, L.cprim);
   DEV(nullh, (size_t)nb * 3 * L.nccell * rb, L.cbcc);
@@ -879,6 +874,38 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
   DEV(nullh, (size_t)nb * m.ne1 * rb, L.ecorr1);
   DEV(nullh, (size_t)nb * m.ne2 * rb, L.ecorr2);
   DEV(nullh, (size_t)nb * m.ne3 * rb, L.ecorr3);
+  // the 27-entry table now only marks which neighbours exist (the boundary kernels'
+  // has-neighbour test): the block itself for an existing one, -1 for none
+  std::vector<int> hn((size_t)nb * 27);
+  for (int b = 0; b < nb; ++b)
+    for (int q = 0; q < 27; ++q) hn[(size_t)b * 27 + q] = nblevel[(size_t)b * 27 + q] < 0 ? -1 : b;
+  CK(cudaMemcpyAsync(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice,
+                     c->stream));
+  L.on = 1;
+  if (c->cycle_exec) { cudaGraphExecDestroy(c->cycle_exec); c->cycle_exec = nullptr; }
+  if (c->cycle_graph) { cudaGraphDestroy(c->cycle_graph); c->cycle_graph = nullptr; }
+  return ATHGPU_OK;
+}
+
+// second part: the multi-level plan (built on the host) and its device copies; waits
+// for the context's stream at the end
+athgpu_status ml_plan_upload(athgpu_ctx* c, const int* nbr_table, const int* nbr_count,
+                             const int* nblevel, const long long* loc) {
+  DevMesh& m = c->m;
+  DevML& L = m.ml;
+  const int nb = m.nb;
+  MlDims dims;
+  dims.nx[0] = m.nx1; dims.nx[1] = m.nx2; dims.nx[2] = m.nx3;
+  dims.ng = m.ng;
+  for (int f = 0; f < 6; ++f) dims.bc[f] = m.bc[f];
+  MlPlan& plan = c->mlplan;
+  std::string err;
+  if (!build_ml_plan(dims, nb, nbr_table, nbr_count, nblevel, loc, &plan, &err))
+    return fail(ATHGPU_ERR_ARG, err.c_str());
+  DEV(plan.eflag.data(), sizeof(int) * plan.eflag.size(), L.eflag);
+  DEV(plan.nfine.data(), sizeof(int) * plan.nfine.size(), L.nfine);
+  DEV(plan.fmask.data(), sizeof(int) * plan.fmask.size(), L.fmask);
+  DEV(plan.level.data(), sizeof(int) * plan.level.size(), L.level);
   MlOpList* lists[3] = {&plan.r, &plan.x, &plan.p};
   for (int ph = 0; ph < 3; ++ph) {
     c->mld.nblk[ph] = (int)lists[ph]->blk.size();
@@ -888,20 +915,24 @@ athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
   }
   c->mld.nflux = (int)plan.flux_tasks.size();
   DEV(plan.flux_tasks.data(), sizeof(MlFluxTask) * plan.flux_tasks.size(), c->mld.flux_tasks);
-#undef DEV
-  // the 27-entry table now only marks which neighbours exist (the boundary kernels'
-  // has-neighbour test): the block itself for an existing one, -1 for none
-  std::vector<int> hn((size_t)nb * 27);
-  for (int b = 0; b < nb; ++b)
-    for (int q = 0; q < 27; ++q) hn[(size_t)b * 27 + q] = nblevel[(size_t)b * 27 + q] < 0 ? -1 : b;
-  CK(cudaMemcpyAsync(c->nbr, hn.data(), sizeof(int) * hn.size(), cudaMemcpyHostToDevice,
-                     c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  L.on = 1;
-  if (c->cycle_exec) { cudaGraphExecDestroy(c->cycle_exec); c->cycle_exec = nullptr; }
-  if (c->cycle_graph) { cudaGraphDestroy(c->cycle_graph); c->cycle_graph = nullptr; }
   CK(cudaStreamSynchronize(c->stream));
   return ATHGPU_OK;
+}
+#undef DEV
+}  // namespace athgpu
+
+extern "C" {
+
+athgpu_status athgpu_set_multilevel(athgpu_ctx* c, const int* nbr_table,
+                                    const int* nbr_count, const int* nblevel,
+                                    const long long* loc, const double* cx1f,
+                                    const double* cdx1f, const double* cx2f,
+                                    const double* cdx2f, const double* cx3f,
+                                    const double* cdx3f) {
+  (void)cdx1f; (void)cdx2f; (void)cdx3f;
+  athgpu_status st = athgpu::ml_prepare(c, nbr_table, nbr_count, nblevel, loc, cx1f, cx2f, cx3f);
+  if (st != ATHGPU_OK) return st;
+  return athgpu::ml_plan_upload(c, nbr_table, nbr_count, nblevel, loc);
 }
 
 athgpu_status athgpu_ml_plan_check(const int* nx, int nghost, const int* bc, int nblocks,

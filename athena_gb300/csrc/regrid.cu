@@ -36,6 +36,11 @@ namespace athgpu {
 athgpu_status api_fail(athgpu_status code, const std::string& msg);
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
 athgpu_status create_context(athgpu_ctx** out, const athgpu_mesh_desc* d, bool sync_end);
+athgpu_status ml_prepare(athgpu_ctx* c, const int* nbr_table, const int* nbr_count,
+                         const int* nblevel, const long long* loc, const double* cx1f,
+                         const double* cx2f, const double* cx3f);
+athgpu_status ml_plan_upload(athgpu_ctx* c, const int* nbr_table, const int* nbr_count,
+                             const int* nblevel, const long long* loc);
 }
 
 namespace {
@@ -297,16 +302,15 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     g_phase_ms[q] += t - tp;
     tp = t;
   };
-  // (its registers are cleared on its stream while the host builds the plan below)
+  // The new context's set-up, its copies from the old mesh and the prolongation are
+  // queued on its stream first; the host builds the multi-level plan while they run.
+  (void)cdx1f; (void)cdx2f; (void)cdx3f;
   athgpu_status st = athgpu::create_context(&nc, desc, false);
-  phase(0);
   if (st != ATHGPU_OK) return st;
-  st = athgpu_set_multilevel(nc, nbr_table, nbr_count, nblevel, loc, cx1f, cdx1f, cx2f, cdx2f,
-                             cx3f, cdx3f);
+  st = athgpu::ml_prepare(nc, nbr_table, nbr_count, nblevel, loc, cx1f, cx2f, cx3f);
   if (st != ATHGPU_OK) { athgpu_destroy(nc); return st; }
-  cudaError_t e = cudaStreamSynchronize(nc->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  phase(1);
+  cudaError_t e = cudaSuccess;
+  phase(0);
   nc->lc = c->lc;
   const DevMesh& nm = nc->m;
   const int rb = c->real_bytes;
@@ -341,7 +345,7 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     if (e != cudaSuccess) return fail_cleanup(e, "regrid restriction");
   }
 
-  phase(2);
+  phase(1);
   // 2. box copies old -> new
   std::vector<RgCopy> tasks;
   bool boxes_ok = true;
@@ -477,7 +481,7 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
     if (e != cudaSuccess) return fail_cleanup(e, "regrid clock");
   }
 
-  phase(3);
+  phase(2);
   // 3. new mesh: ProlongateMeshBlock of every new child
   {
     MlOpList L;
@@ -500,9 +504,12 @@ athgpu_status athgpu_regrid(athgpu_ctx* c, const athgpu_mesh_desc* desc, const i
       L.add(n, ops);
     }
     e = rb == 8 ? run_ops<double>(nc, L) : run_ops<float>(nc, L);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(nc->stream);
     if (e != cudaSuccess) return fail_cleanup(e, "regrid prolongation");
   }
+  phase(3);
+  // the multi-level plan of the new mesh (host), then the new context's stream completes
+  st = athgpu::ml_plan_upload(nc, nbr_table, nbr_count, nblevel, loc);
+  if (st != ATHGPU_OK) { athgpu_destroy(nc); return st; }
 
   phase(4);
   // the new context takes the old one's place behind the caller's handle

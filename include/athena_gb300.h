@@ -162,9 +162,10 @@ athgpu_status athgpu_regrid(athgpu_ctx* ctx, const athgpu_mesh_desc* desc,
                             const double* cx2f, const double* cdx2f, const double* cx3f,
                             const double* cdx3f, const int* newtoold, const int* kind,
                             int nffc, const int* ffc, int after_cycle);
-/* Host wall milliseconds of the phases of the last athgpu_regrid: ms[8] = new registers,
- * multi-level plan, restriction on the old mesh, box copies, prolongation, release of the
- * old registers, Initialize(2), (unused). */
+/* Host wall milliseconds of the phases of the last athgpu_regrid: ms[8] = new registers
+ * (queued), restriction on the old mesh, box copies (queued), prolongation (queued),
+ * multi-level plan (built on the host while the queued work runs, then the wait for it),
+ * release of the old registers, Initialize(2), (unused). */
 athgpu_status athgpu_regrid_profile(double* ms);
 /* Mesh::NewTimeStep again from the block time steps of the last W(U) (the main loop's call
  * after a regrid, main.cpp:541, or the one after the initial refinement loop).
