@@ -472,21 +472,26 @@ bool for_blocks(int nb, F f);
 void mark_runs(MlOpList* L, const Ix& x) {
   const int nq = L->off.empty() ? 0 : (int)L->off.size() - 1;
   for_blocks(nq, [&](int q) {
-    std::vector<Reg> rd, wr;
-    std::vector<Reg> run_w[RA_SB3 + 1], run_r[RA_SB3 + 1];
+    // per-thread buffers, reused from block to block (no allocation per block)
+    thread_local std::vector<Reg> rd, wr;
+    thread_local std::vector<Reg> run_w[RA_SB3 + 1], run_r[RA_SB3 + 1];
+    for (int a = 0; a <= RA_SB3; ++a) { run_w[a].clear(); run_r[a].clear(); }
     unsigned used = 0;
     const int b = L->blk[q];
+    auto hits = [](const Reg& a, const std::vector<Reg>& v) {
+      for (const Reg& g : v)
+        if (overlap(a, g)) return true;
+      return false;
+    };
     for (int i = L->off[q]; i < L->off[q + 1]; ++i) {
       MlOp& op = L->ops[i];
       op_regions(op, b, x, &rd, &wr);
       bool conflict = false;
-      for (const Reg& w : wr) {
-        for (const Reg& g : run_w[w.arr]) conflict = conflict || overlap(w, g);
-        for (const Reg& g : run_r[w.arr]) conflict = conflict || overlap(w, g);
-      }
-      for (const Reg& r : rd)
-        if (r.blk == b)
-          for (const Reg& g : run_w[r.arr]) conflict = conflict || overlap(r, g);
+      for (const Reg& w : wr)
+        if (hits(w, run_w[w.arr]) || hits(w, run_r[w.arr])) { conflict = true; break; }
+      if (!conflict)
+        for (const Reg& r : rd)
+          if (r.blk == b && hits(r, run_w[r.arr])) { conflict = true; break; }
       if (conflict && i > L->off[q]) {
         L->ops[i - 1].nosync = 0;
         for (int a = 0; a <= RA_SB3; ++a)
