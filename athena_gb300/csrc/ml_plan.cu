@@ -472,10 +472,8 @@ bool for_blocks(int nb, F f);
 void mark_runs(MlOpList* L, const Ix& x) {
   const int nq = L->off.empty() ? 0 : (int)L->off.size() - 1;
   for_blocks(nq, [&](int q) {
-    // per-thread buffers, reused from block to block (no allocation per block)
-    thread_local std::vector<Reg> rd, wr;
-    thread_local std::vector<Reg> run_w[RA_SB3 + 1], run_r[RA_SB3 + 1];
-    for (int a = 0; a <= RA_SB3; ++a) { run_w[a].clear(); run_r[a].clear(); }
+    std::vector<Reg> rd, wr;
+    std::vector<Reg> run_w[RA_SB3 + 1], run_r[RA_SB3 + 1];
     unsigned used = 0;
     const int b = L->blk[q];
     auto hits = [](const Reg& a, const std::vector<Reg>& v) {
