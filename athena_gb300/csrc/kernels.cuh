@@ -811,8 +811,19 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
     if (upd) {
       // cell s-1: this direction's flux difference
       if (DIR == 1) {
+        int n0 = 0;
+        if constexpr (sizeof(Real) == 4) {  // FP32: components (0,1), (2,3) packed
 #pragma unroll
-        for (int n = 0; n < NHYDRO; ++n) {
+          for (; n0 + 1 < NHYDRO; n0 += 2) {
+            const float2 d = add2(make_float2(aux[n0 * bd], aux[(n0 + 1) * bd]),
+                                  fma2(pk(area), make_float2(fn[n0], fn[n0 + 1]),
+                                       mul2(pk(-area), make_float2(fprev[n0], fprev[n0 + 1]))));
+            dflx[cc0 + n0 * vs] = d.x;
+            dflx[cc0 + (n0 + 1) * vs] = d.y;
+          }
+        }
+#pragma unroll
+        for (int n = n0; n < NHYDRO; ++n) {
           Real d = aux[n * bd];
           d += (area * fn[n] - area * fprev[n]);
           dflx[cc0 + n * vs] = d;
@@ -824,8 +835,57 @@ flux_sweep_kernel(DevMesh m, int seg, const Real* __restrict__ w,
         // beta is 1/2 or 1, so beta * (FP32 dt) equals the FP32 rounding of beta * dt
         const Real wght = (sizeof(Real) == 8) ? (Real)(ua.beta * clk->dt)
                                               : (Real)ua.beta * dt;
+        int n0 = 0;
+        if constexpr (sizeof(Real) == 4 && KAHAN == 1) {
+          if (!uavg) {
+            // FP32, no register average: components (0,1), (2,3) on packed pairs, the
+            // update as du = (-wght/vol)*d, then the compensated sum of the scalar path
+            const float sc = -(wght / vol);
+            for (; n0 + 1 < NHYDRO; n0 += 2) {
+              const i64 cc = cc0 + n0 * vs;
+              const float2 d = add2(make_float2(aux[n0 * bd], aux[(n0 + 1) * bd]),
+                                    fma2(pk(area), make_float2(fn[n0], fn[n0 + 1]),
+                                         mul2(pk(-area),
+                                              make_float2(fprev[n0], fprev[n0 + 1]))));
+              const float2 du = mul2(pk(sc), d);
+              const float2 hi = make_float2(aux[(NHYDRO + n0) * bd],
+                                            aux[(NHYDRO + n0 + 1) * bd]);
+              const float2 lw = make_float2(aux[(2 * NHYDRO + n0) * bd],
+                                            aux[(2 * NHYDRO + n0 + 1) * bd]);
+              if (ua.stage == 1) {
+                const float2 o = add2(hi, add2(lw, du));
+                uout[cc] = o.x;
+                uout[cc + vs] = o.y;
+              } else {
+                const float2 y = add2(du, lw);
+                const float2 t2 = add2(hi, y);
+                const float2 r = sub2(y, sub2(t2, hi));
+                ulo[cc] = r.x;
+                ulo[cc + vs] = r.y;
+                uout[cc] = t2.x;
+                uout[cc + vs] = t2.y;
+              }
+            }
+            {  // the last component, the same operations
+              const int n = NHYDRO - 1;
+              const i64 cc = cc0 + n * vs;
+              const float d = aux[n * bd] + (area * fn[n] - area * fprev[n]);
+              const float du = sc * d;
+              const float hi = aux[(NHYDRO + n) * bd], lw = aux[(2 * NHYDRO + n) * bd];
+              if (ua.stage == 1) {
+                uout[cc] = hi + (lw + du);
+              } else {
+                const float y = du + lw;
+                const float t2 = hi + y;
+                ulo[cc] = y - (t2 - hi);
+                uout[cc] = t2;
+              }
+            }
+            n0 = NHYDRO;
+          }
+        }
 #pragma unroll
-        for (int n = 0; n < NHYDRO; ++n) {
+        for (int n = n0; n < NHYDRO; ++n) {
           const i64 cc = cc0 + n * vs;
           Real d = aux[n * bd];
           d += (area * fn[n] - area * fprev[n]);
