@@ -231,6 +231,29 @@ __device__ __forceinline__ void mbar_wait_bounded(unsigned long long* mbar, unsi
   }
 }
 
+// PLM of the seven wave components of one cell from its stencil window q[0..2][n] (cells
+// c-1 .. c+1) and the cell's PLM coefficients cp, cm; FP32: components (0,1), (2,3), (4,5)
+// as packed pairs (plm_two)
+template <typename Real>
+__device__ __forceinline__ void plm_waves(const Real (*q)[NWAVE], Real cp, Real cm, Real* qlp,
+                                          Real* qrm) {
+  int n = 0;
+  if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+    for (; n + 1 < NWAVE; n += 2) {
+      float2 a, c;
+      plm_two(make_float2(q[0][n], q[0][n + 1]), make_float2(q[1][n], q[1][n + 1]),
+              make_float2(q[2][n], q[2][n + 1]), cp, cm, a, c);
+      qlp[n] = a.x;
+      qlp[n + 1] = a.y;
+      qrm[n] = c.x;
+      qrm[n + 1] = c.y;
+    }
+  }
+#pragma unroll
+  for (; n < NWAVE; ++n) plm_one<Real>(q[0][n], q[1][n], q[2][n], cp, cm, qlp[n], qrm[n]);
+}
+
 // PPM of the seven wave components of one cell from its stencil window q[0..4][n] (cells
 // c-2 .. c+2 along the sweep).  lo[n]: the cell's limited lower interface, formed here
 // unless CARRY (then the caller's: the previous cell's upper one); up[n] receives the
@@ -289,7 +312,7 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
   const i64 base_w = cidx(m, b, 0, NHYDRO, k, j, i);
   const i64 base_b = cidx(m, b, 0, 3, k, j, i);
   const i64 vs = m.ncell;  // variable stride within a block
-  Real q5[ORDER >= 3 ? 5 : 1][NWAVE];  // PPM: the stencil of every component
+  Real q5[ORDER >= 3 ? 5 : ORDER == 2 ? 3 : 1][NWAVE];  // PLM / PPM: every component's stencil
 #pragma unroll
   for (int n = 0; n < NWAVE; ++n) {
     const Real* src;
@@ -306,14 +329,17 @@ __device__ __forceinline__ void recon_cell(const DevMesh& m, const Real* __restr
       qlp[n] = q;
       qrm[n] = q;
     } else if (ORDER == 2) {
-      int c = DIR == 0 ? i : DIR == 1 ? j : k;
-      const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
-      plm_one<Real>(__ldg(src + o - sw), __ldg(src + o), __ldg(src + o + sw), __ldg(pc + c),
-                    __ldg(pc + m.ncmax + c), qlp[n], qrm[n]);
+#pragma unroll
+      for (int t = 0; t < 3; ++t) q5[t][n] = __ldg(src + o + (t - 1) * sw);
     } else {
 #pragma unroll
       for (int t = 0; t < 5; ++t) q5[t][n] = __ldg(src + o + (t - 2) * sw);
     }
+  }
+  if (ORDER == 2) {
+    const int c = DIR == 0 ? i : DIR == 1 ? j : k;
+    const Real* pc = rplm(m, Real()) + ((i64)b * 3 + DIR) * 2 * m.ncmax;
+    plm_waves<Real>(q5, __ldg(pc + c), __ldg(pc + m.ncmax + c), qlp, qrm);
   }
   if (ORDER >= 3) {
     Real up[NWAVE];
@@ -359,13 +385,13 @@ __device__ __forceinline__ void recon_window(const DevMesh& m, const Real (*win)
     Real up[NWAVE];
     ppm_waves<Real, false>(win, nullptr, up, qlp, qrm, ORDER == 4);
   } else {
+    if (ORDER == 2) {
+      plm_waves<Real>(win, cp, cm, qlp, qrm);
+    } else {
 #pragma unroll
-    for (int n = 0; n < NWAVE; ++n) {
-      if (ORDER == 1) {
+      for (int n = 0; n < NWAVE; ++n) {
         qlp[n] = win[0][n];
         qrm[n] = win[0][n];
-      } else {
-        plm_one<Real>(win[0][n], win[1][n], win[2][n], cp, cm, qlp[n], qrm[n]);
       }
     }
   }
@@ -399,8 +425,8 @@ __device__ __forceinline__ void vel_cell(const DevMesh& m, const Real* __restric
 // (calculate_fluxes.cpp:102/:221/:340; hlld.cpp:372-376) and returns the five hydro
 // fluxes in natural slots (IDN, IM1, IM2, IM3, IEN).
 // RS 7 (LHLLD) also takes the face's velocity differences dvn, dvt (vel_cell below).
-// PK: FP32 HLLD on packed left/right pairs (hlld_pk); off where the caller's register
-// budget would spill with it (the donor-cell x3 sweep).
+// PK: FP32 HLLD / HLLE on packed left/right pairs (hlld_pk, hlle_pk); off where the
+// caller's register budget would spill with it (the donor-cell x3 sweep).
 template <typename Real, int DIR, int RS, bool PK = true>
 __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, const Real* wr,
                                            Real bx, Real dx, Real dt, i64 fo, Real* fn,
@@ -414,6 +440,7 @@ __device__ __forceinline__ void solve_face(const DevMesh& m, const Real* wl, con
   Real f[NWAVE];
   const Real gam = rgamma(m, Real());
   if constexpr (RS == 0 && PK && sizeof(Real) == 4) hlld_pk(gam, wli, wri, bx, f);
+  else if constexpr (RS == 1 && PK && sizeof(Real) == 4) hlle_pk(gam, wli, wri, bx, f);
   else if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
   else if (RS == 1) hlle<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);

@@ -592,10 +592,12 @@ __device__ __forceinline__ void face_flux(const DevMesh& m, const Real* __restri
   Real f[NWAVE];
   const Real gam = rgamma(m, Real());
   const Real bx = to_real(__ldg(bn + fo), Real());
-  // the solver the sweep of that direction runs (FP32 HLLD: packed, but for the donor-cell
-  // x3 sweep), so that both sides of a coarse/fine face use the same fluxes bit for bit
-  if constexpr (RS == 0 && sizeof(Real) == 4 && !(DIR == 2 && ORDER == 1))
-    hlld_pk(gam, wli, wri, bx, f);
+  // the solver the sweep of that direction runs (FP32 HLLD / HLLE: packed, but for the
+  // donor-cell x3 sweep), so that both sides of a coarse/fine face use the same fluxes bit
+  // for bit
+  constexpr bool PK = sizeof(Real) == 4 && !(DIR == 2 && ORDER == 1);
+  if constexpr (RS == 0 && PK) hlld_pk(gam, wli, wri, bx, f);
+  else if constexpr (RS == 1 && PK) hlle_pk(gam, wli, wri, bx, f);
   else if (RS == 0) hlld<Real>(gam, wli, wri, bx, f);
   else if (RS == 3) llf<Real>(gam, wli, wri, bx, f);
   else if (RS == 4) roe<Real>(gam, wli, wri, bx, f);

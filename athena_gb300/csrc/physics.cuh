@@ -868,6 +868,86 @@ __device__ __forceinline__ void hlle(Real gamma, const Real* wli, const Real* wr
     flxi[n] = RC(0.5) * (fl[n] + fr[n]) + (fl[n] - fr[n]) * tmp;
 }
 
+// HLLE in FP32 with the left and right states as the halves of packed FP32x2 operands
+// (x = left, y = right): the magnetic pressures, energies, fast speeds and the seven
+// fluxes of both sides by one instruction each; the Roe averages and the wave speeds,
+// which mix the sides, and the divisions and roots per side.  Same operations as
+// hlle<float> above (hlle_mhd.cpp:33-175), with the FMA contractions written out.
+__device__ __forceinline__ void hlle_pk(float gamma, const float* wli, const float* wri,
+                                        float bxi, float* flxi) {
+  const float gm1 = gamma - 1.0f;
+  const float2 d = lr(wli, wri, IDN), vx = lr(wli, wri, IVX), vy = lr(wli, wri, IVY),
+               vz = lr(wli, wri, IVZ), p = lr(wli, wri, IPR), by = lr(wli, wri, IBY),
+               bz = lr(wli, wri, IBZ);
+  const float sqrtdl = sqrtf(d.x), sqrtdr = sqrtf(d.y);
+  const float isdlpdr = 1.0f / (sqrtdl + sqrtdr);
+  const float wroe_d = sqrtdl * sqrtdr;
+  const float wroe_vx = (sqrtdl * vx.x + sqrtdr * vx.y) * isdlpdr;
+  const float wroe_vy = (sqrtdl * vy.x + sqrtdr * vy.y) * isdlpdr;
+  const float wroe_vz = (sqrtdl * vz.x + sqrtdr * vz.y) * isdlpdr;
+  const float wroe_by = (sqrtdr * by.x + sqrtdl * by.y) * isdlpdr;
+  const float wroe_bz = (sqrtdr * bz.x + sqrtdl * bz.y) * isdlpdr;
+  const float dby = by.x - by.y, dbz = bz.x - bz.y, sdd = sqrtdl + sqrtdr;
+  const float x = 0.5f * (dby * dby + dbz * dbz) / (sdd * sdd);
+  const float y = 0.5f * (d.x + d.y) / wroe_d;
+  const float bxsq = bxi * bxi;
+  const float2 ct2s = fma2(by, by, mul2(bz, bz));  // by^2 + bz^2 of each side
+  const float2 pb = mul2(pk(0.5f), add2(pk(bxsq), ct2s));
+  const float2 e = add2(fma2(p, pk(1.0f / gm1),
+                             mul2(mul2(pk(0.5f), d), fma2(vx, vx, fma2(vy, vy, mul2(vz, vz))))),
+                        pb);
+  const float2 h = add2(add2(e, p), pb);
+  const float hroe = (h.x / sqrtdl + h.y / sqrtdr) * isdlpdr;
+  // FastMagnetosonicSpeed of both sides (eos/adiabatic_mhd.cpp:149-156)
+  const float2 asq = mul2(pk(gamma), p);
+  const float2 vc = add2(pk(bxsq), ct2s);
+  const float2 qsq = add2(vc, asq), tq = sub2(vc, asq);
+  const float2 rad = fma2(tq, tq, mul2(mul2(pk(4.0f), asq), ct2s));
+  const float2 hq = mul2(pk(0.5f), add2(qsq, make_float2(sqrtf(rad.x), sqrtf(rad.y))));
+  const float cl = sqrtf(hq.x / d.x), cr = sqrtf(hq.y / d.y);
+  const float btsq = wroe_by * wroe_by + wroe_bz * wroe_bz;
+  const float vaxsq = bxsq / wroe_d;
+  const float bt_starsq = (gm1 - (gm1 - 1.0f) * y) * btsq;
+  const float hp = hroe - (vaxsq + btsq / wroe_d);
+  const float vsq = wroe_vx * wroe_vx + wroe_vy * wroe_vy + wroe_vz * wroe_vz;
+  const float twid_asq = smax((gm1 * (hp - 0.5f * vsq) - (gm1 - 1.0f) * x), 0.0f);
+  const float ct2 = bt_starsq / wroe_d;
+  const float tsum = vaxsq + ct2 + twid_asq;
+  const float tdif = vaxsq + ct2 - twid_asq;
+  const float cf2_cs2 = sqrtf(tdif * tdif + 4.0f * twid_asq * ct2);
+  const float cfsq = 0.5f * (tsum + cf2_cs2);
+  const float a = sqrtf(cfsq);
+  const float al = smin((wroe_vx - a), (vx.x - cl));
+  const float ar = smax((wroe_vx + a), (vx.y + cr));
+  const float bp = ar > 0.0f ? ar : 0.0f;
+  const float bm = al < 0.0f ? al : 0.0f;
+  const float2 vxs = sub2(vx, make_float2(bm, bp));  // vxl, vxr
+  const float2 nbx = pk(-bxi);
+  const float2 dvx = mul2(d, vxs);
+  const float2 f0 = dvx;
+  const float2 f1 = add2(sub2(fma2(mul2(d, vx), vxs, pb), pk(bxsq)), p);
+  const float2 f2 = fma2(mul2(d, vy), vxs, mul2(nbx, by));
+  const float2 f3 = fma2(mul2(d, vz), vxs, mul2(nbx, bz));
+  const float2 f4 = fma2(nbx, fma2(by, vy, mul2(bz, vz)),
+                         fma2(e, vxs, mul2(vx, sub2(add2(p, pb), pk(bxsq)))));
+  const float2 f5 = fma2(by, vxs, mul2(nbx, vy));
+  const float2 f6 = fma2(bz, vxs, mul2(nbx, vz));
+  float tmp = 0.0f;
+  if (bp != bm) tmp = 0.5f * (bp + bm) / (bp - bm);
+  // 0.5*(fl + fr) + (fl - fr)*tmp, components paired
+  const float2 fs[7] = {f0, f1, f2, f3, f4, f5, f6};
+#pragma unroll
+  for (int n = 0; n + 1 < NWAVE; n += 2) {
+    const float2 sm = make_float2(fs[n].x + fs[n].y, fs[n + 1].x + fs[n + 1].y);
+    const float2 df = make_float2(fs[n].x - fs[n].y, fs[n + 1].x - fs[n + 1].y);
+    const float2 o = fma2(df, pk(tmp), mul2(pk(0.5f), sm));
+    flxi[n] = o.x;
+    flxi[n + 1] = o.y;
+  }
+  flxi[NWAVE - 1] = 0.5f * (fs[NWAVE - 1].x + fs[NWAVE - 1].y) +
+                    (fs[NWAVE - 1].x - fs[NWAVE - 1].y) * tmp;
+}
+
 // PiecewiseLinearX1/2/3, uniform van Leer branch (reconstruct/plm.cpp:103-112) and the
 // interface values (:148-152).  One wave component.
 template <typename Real>
@@ -880,6 +960,21 @@ __device__ __forceinline__ void plm_one(Real qm, Real q0, Real qp, Real cp, Real
   if (dw2 <= RC(0.0)) dwm = RC(0.0);
   qlp = q0 + cp * dwm;
   qrm = q0 - cm * dwm;
+}
+
+// plm_one on two wave components at once (FP32): the differences, products and face
+// values as packed pairs, the van Leer quotient and the sign test per component
+__device__ __forceinline__ void plm_two(float2 qm, float2 q0, float2 qp, float cp, float cm,
+                                        float2& qlp, float2& qrm) {
+  const float2 dwl = sub2(q0, qm);
+  const float2 dwr = sub2(qp, q0);
+  const float2 dw2 = mul2(dwl, dwr);
+  const float2 num = mul2(pk(2.0f), dw2), den = add2(dwl, dwr);
+  float2 dwm = make_float2(num.x / den.x, num.y / den.y);
+  if (dw2.x <= 0.0f) dwm.x = 0.0f;
+  if (dw2.y <= 0.0f) dwm.y = 0.0f;
+  qlp = fma2(pk(cp), dwm, q0);
+  qrm = fma2(pk(-cm), dwm, q0);
 }
 
 // PiecewiseParabolicX1/2/3, uniform-Cartesian Colella-Sekora branch

@@ -38,8 +38,8 @@ __global__ void conversion_check_kernel(long long n, const double* __restrict__ 
 }
 
 // One Riemann solve per face in the solvers' local order (d, v_n, v_t1, v_t2, p, B_t1,
-// B_t2): wl/wr [n][7], bx [n], flux [n][7], in Real.  FP32 HLLD is the packed solver the
-// FP32 sweeps run (hlld_pk).
+// B_t2): wl/wr [n][7], bx [n], flux [n][7], in Real.  FP32 HLLD and HLLE are the packed
+// solvers the FP32 sweeps run (hlld_pk, hlle_pk).
 template <typename Real, int RS>
 __global__ void riemann_check_kernel(long long n, Real gamma, const Real* __restrict__ wl,
                                      const Real* __restrict__ wr,
@@ -55,6 +55,7 @@ __global__ void riemann_check_kernel(long long n, Real gamma, const Real* __rest
     b[v] = wr[q * athgpu::NWAVE + v];
   }
   if constexpr (RS == 0 && sizeof(Real) == 4) athgpu::hlld_pk(gamma, a, b, bx[q], f);
+  else if constexpr (RS == 1 && sizeof(Real) == 4) athgpu::hlle_pk(gamma, a, b, bx[q], f);
   else if (RS == 0) athgpu::hlld<Real>(gamma, a, b, bx[q], f);
   else if (RS == 1) athgpu::hlle<Real>(gamma, a, b, bx[q], f);
   else if (RS == 2) athgpu::hlle_sr<Real>(gamma, a, b, bx[q], f);

@@ -572,7 +572,7 @@ athgpu_status athgpu_selftest_riemann(int rsolver, int relativistic, double gamm
                                       void *stream);
 
 /* The same in FP32 (float arrays, same layout), with the solvers the FP32 sweeps run
- * (HLLD: the packed left/right form).  Replaces no reference interface. */
+ * (HLLD and HLLE: the packed left/right forms).  Replaces no reference interface. */
 athgpu_status athgpu_selftest_riemann_fp32(int rsolver, int relativistic, double gamma,
                                            long long n, const float *wl, const float *wr,
                                            const float *bx, const float *dv, float *flux,
