@@ -1172,6 +1172,8 @@ __device__ __forceinline__ Real edge_at(const DevMesh& m, const Real* __restrict
 // blockIdx.x covers the plan, blockIdx.y the MeshBlocks: EB per thread, their loads
 // issued together.
 constexpr int EB = 4;
+// MeshBlocks per thread of the face-field ghost exchange (exchange_plan_kernel)
+constexpr int EXCHANGE_XB = 8;
 template <typename Real>
 __global__ void __launch_bounds__(128)
 edge_fix_kernel(DevMesh m, const int4* __restrict__ plan, int n0, int n1, int n2,
@@ -1486,7 +1488,7 @@ exchange_plan_kernel(DevMesh m, const unsigned* __restrict__ plan, int p0, int n
   // never a ghost, so no store here changes a value loaded here)
   double* f = what == 1 ? b1 : what == 2 ? b2 : b3;
   const i64 nf = what == 1 ? m.nf1 : what == 2 ? m.nf2 : m.nf3;
-  constexpr int XB = 4;
+  constexpr int XB = EXCHANGE_XB;
   for (int b0 = blockIdx.y; b0 < m.nb; b0 += XB * gridDim.y) {
     int sb[XB];
     double v[XB];

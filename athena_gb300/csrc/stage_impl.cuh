@@ -108,8 +108,8 @@ static void launch_exchange(athgpu_ctx* c, Real* u, double* b1, double* b2, doub
     const int* xn = c->xplan_n;
     const int p0 = with_u ? 0 : xn[0];
     const long long cnt = (long long)xn[0] + xn[1] + xn[2] + xn[3] - p0;
-    // four MeshBlocks per thread (exchange_plan_kernel's XB)
-    const long long gy = (m.nb + 3) / 4;
+    // EXCHANGE_XB MeshBlocks per thread
+    const long long gy = (m.nb + EXCHANGE_XB - 1) / EXCHANGE_XB;
     exchange_plan_kernel<Real><<<dim3(nblk(cnt, 256), gy < 65535 ? gy : 65535), 256, 0,
                                  st>>>(m, c->xplan, p0, xn[0], xn[1], xn[2], xn[3],
                                        c->xdelta, u, b1, b2, b3);

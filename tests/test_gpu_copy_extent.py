@@ -74,3 +74,38 @@ def test_copy_extent_rejects_unknown_values():
     with pytest.raises(Exception):
         g.set_copy_extent(2)
     g.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_interior_copies_on_a_multilevel_mesh(precision):
+    """The same on a statically refined mesh, whose initialize rebuilds the ghost zones
+    through the multi-level exchange and prolongation."""
+    from golden_cases import load_ml_case, ml_case_names
+    c, mesh, ic, _ = load_ml_case(ml_case_names()[0])
+
+    def run(extent):
+        g = StageUpdate(mesh, c["gamma"], xorder=c["xorder"], rsolver=c["rsolver"],
+                        precision=precision, cfl=c["cfl"], tlim=c["tlim"],
+                        integrator=c.get("integrator", "vl2"))
+        g.set_copy_extent(extent)
+        host = [a.copy() for a in ic]
+        if extent == COPY_INTERIOR:
+            for w, a in enumerate(host):
+                keep = a[_copied(mesh, w)].copy()
+                a[...] = np.nan
+                a[_copied(mesh, w)] = keep
+        g.set_state(*host)
+        g.initialize()
+        g.cycle(3)
+        out = [np.full(a.shape, SENTINEL) for a in ic]
+        g.state(out=out)
+        g.close()
+        return out
+
+    whole, part = run(COPY_WHOLE), run(COPY_INTERIOR)
+    for w, (a, b) in enumerate(zip(whole, part)):
+        sel = _copied(mesh, w)
+        assert np.array_equal(a[sel], b[sel]), (precision, w)
+        rest = np.ones(b.shape, bool)
+        rest[sel] = False
+        assert (b[rest] == SENTINEL).all(), (precision, w)
