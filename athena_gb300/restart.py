@@ -195,7 +195,16 @@ def state(r, mesh):
 def save(path, stage_update, ncycle, params, costs=None):
     """Write a restart file of a StageUpdate (or AdaptiveStageUpdate): the state with
     ghost zones, the clock and the block list."""
-    st = stage_update.state()
+    from .runtime import COPY_WHOLE
+    su = getattr(stage_update, "su", stage_update)   # AdaptiveStageUpdate wraps one
+    extent = getattr(su, "copy_extent", COPY_WHOLE)
+    if extent != COPY_WHOLE:   # the file holds whole arrays
+        su.set_copy_extent(COPY_WHOLE)
+    try:
+        st = stage_update.state()
+    finally:
+        if extent != COPY_WHOLE:
+            su.set_copy_extent(extent)
     time, dt = stage_update.clock()
     write(path, make(stage_update.mesh, st, time, dt, ncycle, params, costs))
 

@@ -441,6 +441,7 @@ class StageUpdate:
         ghost zone after an upload)."""
         _check(load_library().athgpu_set_copy_extent(self.h, int(extent)),
                "athgpu_set_copy_extent")
+        self.copy_extent = int(extent)
 
     def set_x3_staging(self, bulk):
         """x3 sweep staging: 0 per-thread cp.async, 1 TMA bulk copies."""
