@@ -499,8 +499,10 @@ struct UpdateArgs {
 // lanes 1..30 form their cell's x1 flux difference with the face flux of lane L+1 (shuffle
 // down).  Warps advance by 30 cells, so every cell is reconstructed at most twice, every
 // face solved at most twice (identical duplicate stores) and every difference formed once.
+// (FP32: eight CTAs per SM for donor cell, measured faster despite a few spilled
+// registers; seven, i.e. at most 73 registers, otherwise)
 template <typename Real, int ORDER, int RS>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(Real) == 4 ? (ORDER == 1 ? 8 : 7) : 1)
 flux_x1_kernel(DevMesh m, const Real* __restrict__ w, const Real* __restrict__ bcc,
                const double* __restrict__ b1, const DevClock* __restrict__ clk,
                Real* __restrict__ dflx, Real* __restrict__ e3, Real* __restrict__ e2,
