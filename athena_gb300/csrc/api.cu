@@ -187,8 +187,9 @@ bool build_exchange_plan(const DevMesh& m, std::vector<unsigned>& plan, int n[4]
 
 // The own edges of one MeshBlock that lie on block faces, as edge_fix_kernel visits them:
 // x1-directed, then x2- and x3-directed, each k-major.  Per edge its in-block offset and
-// the neighbours edge_avg adds, in its order: the face neighbours across x1, x2, x3 (those
-// whose face the edge lies on), then for an edge on two faces the edge neighbour; each as
+// the neighbours whose values the average adds, in the reference's order: the face
+// neighbours across x1, x2, x3 (those whose face the edge lies on), then for an edge on
+// two faces the edge neighbour; each as
 // (offset index << 27) | the edge's offset in that neighbour, ~0 when absent.  An edge of
 // direction C has own range [s, e] along C and [s, e + 1] across.
 void build_edge_plan(const DevMesh& m, std::vector<int4>& plan, int n[3]) {

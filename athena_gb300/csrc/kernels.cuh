@@ -1089,88 +1089,19 @@ corner_e_kernel(DevMesh m, const Real* __restrict__ cc, const Real* __restrict__
 // edge on a block face is the sum of the pre-averaging values of the blocks sharing it,
 // own value first and the others in neighbour-list order (faces x1, x2, x3, then the
 // edge neighbour; bvals_base.cpp:326-720), times 1/2 (two blocks) or 1/4 (four blocks).
-// C = 0, 1, 2 for e1, e2, e3.
+// The neighbour block across offset (o1, o2, o3), or -1 across a physical mesh face.
 __device__ __forceinline__ int nbr_of(const DevMesh& m, int b, int o1, int o2, int o3) {
   return __ldg(m.nbr + (i64)b * 27 + ((o3 + 1) * 3 + (o2 + 1)) * 3 + (o1 + 1));
 }
 
-// The corner EMF of edge (b,k,j,i) as CT uses it: the value itself, or on a block face /
-// edge the average over the blocks that share it (flux_correction_fc.cpp), formed in the
-// bulk precision.
-template <typename Real, int C>
-__device__ __forceinline__ Real edge_avg(const DevMesh& m, const Real* __restrict__ e,
-                                         int b, int k, int j, int i) {
-  auto at = [&](int bb, int kk, int jj, int ii) -> Real {
-    return __ldg(e + (C == 0 ? e1idx(m, bb, kk, jj, ii)
-                     : C == 1 ? e2idx(m, bb, kk, jj, ii) : e3idx(m, bb, kk, jj, ii)));
-  };
-  int o1 = 0, o2 = 0, o3 = 0;
-  if (C != 0) o1 = (i == m.is) ? -1 : (i == m.ie + 1) ? 1 : 0;
-  if (C != 1) o2 = (j == m.js) ? -1 : (j == m.je + 1) ? 1 : 0;
-  if (C != 2) o3 = (k == m.ks) ? -1 : (k == m.ke + 1) ? 1 : 0;
-  Real own = at(b, k, j, i);
-  const int on = (o1 != 0) + (o2 != 0) + (o3 != 0);
-  if (on == 0) return own;
-  if (m.ml.on) {  // multi-level mesh: corrected by ml_emf_kernel
-    const Real* ec = (const Real*)(C == 0 ? m.ml.ecorr1 : C == 1 ? m.ml.ecorr2 : m.ml.ecorr3);
-    return ec[C == 0 ? e1idx(m, b, k, j, i) : C == 1 ? e2idx(m, b, k, j, i)
-                                                     : e3idx(m, b, k, j, i)];
-  }
-  Real sum = own;
-  int count = 1;  // blocks sharing the edge: a physical mesh face contributes none
-  // face neighbours in list order: x1 before x2 before x3
-  if (o1 != 0) {
-    const int nb = nbr_of(m, b, o1, 0, 0);
-    if (nb >= 0) { sum += at(nb, k, j, i - o1 * m.nx1); ++count; }
-  }
-  if (o2 != 0) {
-    const int nb = nbr_of(m, b, 0, o2, 0);
-    if (nb >= 0) { sum += at(nb, k, j - o2 * m.nx2, i); ++count; }
-  }
-  if (o3 != 0) {
-    const int nb = nbr_of(m, b, 0, 0, o3);
-    if (nb >= 0) { sum += at(nb, k - o3 * m.nx3, j, i); ++count; }
-  }
-  if (on == 2) {
-    // an edge shared by four blocks is scaled by 1/4; along a physical mesh face by 1/count
-    // (flux_correction_fc.cpp:1477-1481)
-    const int nb = nbr_of(m, b, o1, o2, o3);
-    if (nb >= 0) {
-      sum += at(nb, k - o3 * m.nx3, j - o2 * m.nx2, i - o1 * m.nx1);
-      ++count;
-    }
-    if (count == 4) return sum * Real(0.25);
-    if (count == 1) return own;
-    return sum * (Real(1.0) / Real(count));
-  }
-  // inside a block face: halved when the face has a neighbour (flux_correction_fc.cpp:
-  // 1362-1380)
-  return count == 2 ? sum * Real(0.5) : own;
-}
-
-// The same, reading an edge off the block's faces at in-block offset off from the block's
-// base eb (no neighbour logic, no 64-bit index arithmetic); ML = false: the stored value
-// everywhere (a same-level mesh's block-face edges hold their averages already)
-template <typename Real, int C, bool ML>
-__device__ __forceinline__ Real edge_at(const DevMesh& m, const Real* __restrict__ e,
-                                        const Real* __restrict__ eb, int off, int b, int k,
-                                        int j, int i) {
-  if (!ML) return __ldg(eb + off);
-  const bool on_face = (C != 0 && (i == m.is || i == m.ie + 1)) ||
-                       (C != 1 && (j == m.js || j == m.je + 1)) ||
-                       (C != 2 && (k == m.ks || k == m.ke + 1));
-  if (!on_face) return __ldg(eb + off);
-  return edge_avg<Real, C>(m, e, b, k, j, i);
-}
-
-// The average of the block-face edges over the blocks sharing them (edge_avg above) on a
-// same-level mesh, done before CT in two launches so that every value averaged is a
-// pre-average one: edge_fix_kernel writes the averages of the plan's edges into scratch,
-// edge_put_kernel stores them into the edge arrays.  The plan (edge_plan, built when the
-// mesh is set up) lists per block its own edges on block faces, x1-directed (n0), then
-// x2- (n1) and x3-directed (n2): the in-block offset, then the candidates to add in
-// edge_avg's order (x1-, x2-, x3-face neighbour, then the edge neighbour for an edge on
-// two faces), each as (offset index << 27) | offset in the neighbour, ~0u past the last.
+// The average of the block-face edges over the blocks sharing them on a same-level mesh,
+// done before CT in two launches so that every value averaged is a pre-average one:
+// edge_fix_kernel writes the averages of the plan's edges into scratch, edge_put_kernel
+// stores them into the edge arrays.  The plan (edge_plan, built when the mesh is set up)
+// lists per block its own edges on block faces, x1-directed (n0), then x2- (n1) and
+// x3-directed (n2): the in-block offset, then the candidates to add in the order above
+// (x1-, x2-, x3-face neighbour, then the edge neighbour for an edge on two faces), each as
+// (offset index << 27) | offset in the neighbour, ~0u past the last.
 // blockIdx.x covers the plan, blockIdx.y the MeshBlocks: EB per thread, their loads
 // issued together.
 constexpr int EB = 4;
@@ -1261,16 +1192,15 @@ edge_put_kernel(DevMesh m, const int4* __restrict__ plan, int n0, int n1, int n2
 // point (k,j,i) of [ks,ke+1]x[js,je+1]x[is,ie+1] and updates the faces whose lower corner
 // it is: x1 face (k,j,i) for j<=je, k<=ke; x2 face for i<=ie, k<=ke; x3 face for i<=ie,
 // j<=je.  The three faces share the edges e1, e2, e3 at (k,j,i), so a thread reads nine
-// edge values for up to three faces.  Edge EMFs are read with the correction above.
+// edge values for up to three faces.  The block-face edges already hold their corrected
+// values: on a same-level mesh the averages (edge_fix_kernel, edge_put_kernel), on a
+// multi-level mesh the cross-level corrections (ml_emf_kernel, ml_emf_put_kernel).
 // FP64 path (Real = double): (wght/area)*(len*e(+) - len*e(-)) exactly as the reference.
 // FP32 path: the corner EMFs are FP32 and the update is ((wght/area)*len)*(e(+) - e(-)) in
 // FP64, the difference of the two floats formed on the integer pipe (fsub_f64: the FP64
 // subtraction's bits), which leaves two FP64 operations per face on GB300's narrow FP64
 // pipe instead of four.  bin/bout may alias.
-// ML: a multi-level mesh, whose block-face edges take the corrected values (edge_at).  On
-// a same-level mesh the block-face edges already hold their averages (edge_fix_kernel,
-// edge_put_kernel), so the kernel reads plain edges.
-template <typename Real, bool ML>
+template <typename Real>
 __global__ void __launch_bounds__(256)
 ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
           const Real* __restrict__ e1, const Real* __restrict__ e2,
@@ -1329,36 +1259,36 @@ ct_kernel(DevMesh m, double beta, const DevClock* __restrict__ clk,
   const Real* E2 = e2 + (i64)b * m.ne2;
   const Real* E3 = e3 + (i64)b * m.ne3;
   // the shared edges, each read once (and only where a face of this thread uses it)
-  const Real e1c = (f2 || f3) ? edge_at<Real, 0, ML>(m, e1, E1, oe1, b, k, j, i) : Real(0);
-  const Real e2c = (f1 || f3) ? edge_at<Real, 1, ML>(m, e2, E2, oe2, b, k, j, i) : Real(0);
-  const Real e3c = (f1 || f2) ? edge_at<Real, 2, ML>(m, e3, E3, oe3, b, k, j, i) : Real(0);
+  const Real e1c = (f2 || f3) ? __ldg(E1 + oe1) : Real(0);
+  const Real e2c = (f1 || f3) ? __ldg(E2 + oe2) : Real(0);
+  const Real e3c = (f1 || f2) ? __ldg(E3 + oe3) : Real(0);
   if (f1) {
     const i64 o = (i64)b * m.nf1 + (k * c2 + j) * (c1 + 1) + i;
     double v = b1in[o];
     if (b1avg) v = g1 * b1avg[o] + g2 * v;
     v = upd(v, true, q[0], l3, ql[0],
-              edge_at<Real, 2, ML>(m, e3, E3, oe3 + (c1 + 1), b, k, j + 1, i), e3c);
+              __ldg(E3 + oe3 + (c1 + 1)), e3c);
     v = upd(v, false, q[0], l2, ql[1],
-              edge_at<Real, 1, ML>(m, e2, E2, oe2 + c2 * (c1 + 1), b, k + 1, j, i), e2c);
+              __ldg(E2 + oe2 + c2 * (c1 + 1)), e2c);
     b1out[o] = v;
   }
   if (f2) {
     const i64 o = (i64)b * m.nf2 + (k * (c2 + 1) + j) * c1 + i;
     double v = b2in[o];
     if (b2avg) v = g1 * b2avg[o] + g2 * v;
-    v = upd(v, false, q[1], l3, ql[2], edge_at<Real, 2, ML>(m, e3, E3, oe3 + 1, b, k, j, i + 1),
+    v = upd(v, false, q[1], l3, ql[2], __ldg(E3 + oe3 + 1),
               e3c);
     v = upd(v, true, q[1], l1, ql[3],
-              edge_at<Real, 0, ML>(m, e1, E1, oe1 + (c2 + 1) * c1, b, k + 1, j, i), e1c);
+              __ldg(E1 + oe1 + (c2 + 1) * c1), e1c);
     b2out[o] = v;
   }
   if (f3) {
     const i64 o = (i64)b * m.nf3 + (k * c2 + j) * c1 + i;
     double v = b3in[o];
     if (b3avg) v = g1 * b3avg[o] + g2 * v;
-    v = upd(v, true, q[2], l2, ql[4], edge_at<Real, 1, ML>(m, e2, E2, oe2 + 1, b, k, j, i + 1),
+    v = upd(v, true, q[2], l2, ql[4], __ldg(E2 + oe2 + 1),
               e2c);
-    v = upd(v, false, q[2], l1, ql[5], edge_at<Real, 0, ML>(m, e1, E1, oe1 + c1, b, k, j + 1, i),
+    v = upd(v, false, q[2], l1, ql[5], __ldg(E1 + oe1 + c1),
               e1c);
     b3out[o] = v;
   }

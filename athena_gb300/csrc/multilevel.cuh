@@ -848,6 +848,50 @@ __host__ __device__ __forceinline__ i64 ml_emf_positions(const DevMesh& m) {
          (i64)m.nx3 * 2 * (m.nx1 + m.nx2);
 }
 
+// The corrected EMFs into the edge arrays themselves, at the same positions, once every
+// correction is formed (ml_emf_kernel reads the neighbours' uncorrected values): CT then
+// reads plain edges on a multi-level mesh as on a uniform one.
+template <typename Real>
+__global__ void __launch_bounds__(128)
+ml_emf_put_kernel(DevMesh m, Real* __restrict__ e1, Real* __restrict__ e2,
+                  Real* __restrict__ e3) {
+  const int nx1 = m.nx1, nx2 = m.nx2, nx3 = m.nx3;
+  const int b = blockIdx.x;
+  const DevML& L = m.ml;
+  const i64 npos = ml_emf_positions(m);
+  for (i64 r0 = (i64)blockIdx.y * blockDim.x + threadIdx.x; r0 < npos;
+       r0 += (i64)gridDim.y * blockDim.x) {
+    // the position's component c and (k, j, i), as in ml_emf_kernel
+    const int nxs[3] = {nx1, nx2, nx3};
+    int c = 0;
+    i64 r = r0;
+    for (; c < 2; ++c) {
+      const int ta_ = c == 0 ? 1 : 0, tb_ = c == 2 ? 1 : 2;
+      const i64 nc = (i64)nxs[c] * 2 * (nxs[ta_] + nxs[tb_]);
+      if (r < nc) break;
+      r -= nc;
+    }
+    const int ta0 = c == 0 ? 1 : 0, tb0 = c == 2 ? 1 : 2;
+    const int na = nxs[ta0], nbt = nxs[tb0];
+    const int per = 2 * (na + nbt);
+    const int pc = (int)(r / per);
+    int pr = (int)(r % per), pa, pb;
+    if (pr < na + 1) { pa = pr; pb = 0; }
+    else if ((pr -= na + 1) < na + 1) { pa = pr; pb = nbt; }
+    else { pr -= na + 1; pa = (pr & 1) ? na : 0; pb = 1 + (pr >> 1); }
+    int q3[3];
+    q3[c] = pc;
+    q3[ta0] = pa;
+    q3[tb0] = pb;
+    const int i = m.is + q3[0], j = m.js + q3[1], k = m.ks + q3[2];
+    const i64 idx = c == 0 ? e1idx(m, b, k, j, i) : c == 1 ? e2idx(m, b, k, j, i)
+                                                           : e3idx(m, b, k, j, i);
+    const Real* ec = (const Real*)(c == 0 ? L.ecorr1 : c == 1 ? L.ecorr2 : L.ecorr3);
+    Real* e = c == 0 ? e1 : c == 1 ? e2 : e3;
+    e[idx] = ec[idx];
+  }
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(128)
 ml_emf_kernel(DevMesh m, const Real* __restrict__ e1, const Real* __restrict__ e2,

@@ -327,7 +327,8 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
     dim3 grid(m.nb, (unsigned)(chunks < 65535 ? chunks : 65535));
     ml_emf_kernel<Real><<<grid, 128, 0, s>>>(m, (const Real*)r.e1, (const Real*)r.e2,
                                              (const Real*)r.e3);
-    c->launches += 1;
+    ml_emf_put_kernel<Real><<<grid, 128, 0, s>>>(m, (Real*)r.e1, (Real*)r.e2, (Real*)r.e3);
+    c->launches += 2;
   }
   double* o1 = (stage == 1) ? r.bs1 : r.b1;
   double* o2 = (stage == 1) ? r.bs2 : r.b2;
@@ -336,7 +337,8 @@ static cudaError_t run_stage(athgpu_ctx* c, int stage) {
     const long long per = (long long)(m.nx3 + 1) * (m.nx2 + 1) * (m.nx1 + 1);
     dim3 grid(nblk(per, 256), m.nb);
     ProfScope ps(c, "ct");
-    (m.ml.on ? ct_kernel<Real, true> : ct_kernel<Real, false>)<<<grid, 256, 0, s>>>(
+    // (multi-level meshes too: the corrected block-face EMFs are in the edge arrays)
+    ct_kernel<Real><<<grid, 256, 0, s>>>(
         m, beta, c->clk, (const Real*)r.e1, (const Real*)r.e2, (const Real*)r.e3, r.b1, r.b2,
         r.b3, o1, o2, o3, avg ? r.bs1 : nullptr, avg ? r.bs2 : nullptr,
         avg ? r.bs3 : nullptr, g1, g2);
