@@ -77,3 +77,28 @@ def test_native_static_blocks_match_python_regions():
     with pytest.raises(Exception):
         nat.add_block(Loc(9, 0, 0, 0))       # beyond numlevel
     nat.close()
+
+
+def test_native_mesh_tables_are_fetched_lazily_and_guarded():
+    """A NativeMesh fetches only the block list when made; its neighbour tables and
+    coordinates, fetched on first use, equal an eager fetch, and a block list made before
+    the tree changed refuses to fetch them afterwards."""
+    from athena_gb300.meshtree import Loc
+    nat = NativeAmr((16, 16, 16), (2, 2, 2), 2, (-.5,) * 3, (.5,) * 3, (0,) * 6, 3, 2)
+    m = NativeMesh(nat)
+    assert m.nblocks == 8 and m._tables is None
+    loc, t, cnt, lv, fine, coarse = nat.tables()
+    t1, c1, l1, loc1 = m.neighbor_table()
+    np.testing.assert_array_equal(t1, t)
+    np.testing.assert_array_equal(c1, cnt)
+    np.testing.assert_array_equal(l1, lv)
+    np.testing.assert_array_equal(loc1, loc)
+    for a, b in zip(m.coordinate_arrays(), fine):
+        np.testing.assert_array_equal(a, b)
+    stale = NativeMesh(nat)
+    nat.add_block(Loc(2, 0, 0, 0))   # refine the first root block: the tree changes
+    assert NativeMesh(nat).nblocks == 15
+    with pytest.raises(RuntimeError):
+        stale.neighbor_table()
+    # the block list itself stays the one it was made with
+    assert stale.nblocks == 8 and len(stale.locs) == 8
