@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/athena_gb300_diag.h"
 #include "ctx.h"
 #include "ml_plan.h"
 

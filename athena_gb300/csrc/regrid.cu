@@ -28,6 +28,7 @@
 #include <utility>
 #include <vector>
 
+#include "../../include/athena_gb300_diag.h"
 #include "ctx.h"
 #include "ml_plan.h"
 #include "multilevel.cuh"

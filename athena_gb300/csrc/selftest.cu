@@ -3,7 +3,7 @@
 
 #include <string>
 
-#include "../../include/athena_gb300.h"
+#include "../../include/athena_gb300_diag.h"
 #include "physics.cuh"
 
 namespace athgpu {

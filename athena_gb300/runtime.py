@@ -18,6 +18,7 @@ from .mesh import MeshSpec
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libathgpu.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300.h")
+DIAG_HEADER = os.path.join(os.path.dirname(HERE), "include", "athena_gb300_diag.h")
 
 HLLD, HLLE, LLF, ROE, LHLLD = 0, 1, 2, 3, 4
 _RSOLVERS = {"hlld": HLLD, "hlle": HLLE, "llf": LLF, "roe": ROE, "lhlld": LHLLD}
@@ -164,10 +165,11 @@ def load_library(path=LIB_PATH):
     return L
 
 
-def header_functions(path=HEADER):
-    """Names of the functions declared in include/athena_gb300.h."""
+def header_functions(paths=(HEADER, DIAG_HEADER)):
+    """Names of the functions declared in include/athena_gb300.h and the diagnostics
+    header include/athena_gb300_diag.h."""
     import re
-    text = open(path).read()
+    text = "".join(open(p).read() for p in paths)
     return sorted(set(re.findall(r"\b(athgpu_[a-z_0-9]+)\s*\(", text)))
 
 
